@@ -1,0 +1,174 @@
+/*
+ * mossco_sed.h -- C ABI of the GB300 sediment-column solver.
+ *
+ * A drop-in for MOSSCO's sediment-column hot path: the fabm_sediment
+ * driver's right-hand side integrated by the solver_library ODE stepper
+ * over every column of the grid.  Plain pointers and sizes only; every call
+ * returns SED_OK (0) or a negative SED_E_* code.  A handle owns one CUDA
+ * stream and its device buffers; calls on one handle are not thread safe.
+ *
+ * Array layout is the reference's Fortran order read backwards (C order):
+ *   per cell      [ntr][kmax][ncol]  == conc(i,j,k,n), i fastest, col=i+inum*j
+ *   per layer     [kmax][ncol]       == dz(i,j,k), porosity(i,j,k), ...
+ *   dzc           [kmax-1][ncol]     == grid%dzc(i,j,k)
+ *   bdys          [ntr+1][ncol]      == bdys(i,j,1:nvar+1), temperature first
+ *   fluxes        [ntr][ncol]        == fluxes(i,j,1:nvar)
+ * (src/components/fabm_sediment_component.F90:521,538-541).
+ *
+ * Reference interfaces replaced (paths inside platipodium/mossco-code):
+ *   ode_solver(rhs_driver, dt, method)  src/utilities/solver_library.F90:80-90
+ *   type_sed%get_rhs(rhs)               src/drivers/fabm_sediment_driver.F90:575-582
+ *   Run-loop epilogue (NaN, clamp)      src/components/fabm_sediment_component.F90:1715-1732
+ */
+#ifndef MOSSCO_SED_H
+#define MOSSCO_SED_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SED_NTR 11        /* OMEXDIA+P tracers, order in sed_tracer_name() */
+#define SED_KMAX_LIMIT 64 /* layers per column the kernels hold on chip */
+
+/* return codes */
+#define SED_OK 0
+#define SED_E_ARG (-1)          /* bad size, pointer or option */
+#define SED_E_NAN (-2)          /* NaN in the state after a step */
+#define SED_E_SUBSTEP_CAP (-3)  /* adaptive loop hit max_attempts */
+#define SED_E_CUDA (-4)         /* CUDA runtime error */
+#define SED_E_STATE (-5)        /* call order: grid / forcing / state missing */
+#define SED_E_NOMEM (-6)        /* device or pinned allocation failed */
+#define SED_E_NODEVICE (-7)     /* no CUDA device */
+#define SED_E_TIMEOUT (-8)      /* a bounded device wait gave up */
+
+/* ode_solver methods (solver_library.F90:32-35) */
+#define SED_EULER 0
+#define SED_RUNGE_KUTTA_4 1
+#define SED_ADAPTIVE_EULER 2
+#define SED_RUNGE_KUTTA_4_38 3
+
+/* step-cut scope of the adaptive method */
+#define SED_CUT_PER_COLUMN 0 /* each column cuts its own substep */
+#define SED_CUT_GLOBAL 1     /* one cut for the whole grid, as on one PET */
+
+/* state precision on the device */
+#define SED_FP32 0
+#define SED_FP64 1
+
+typedef struct sed_params {
+  /* type_sed scalars (fabm_sediment_driver.F90:72-80, sed_nml :211-231) */
+  double diffusivity;         /* cm2/d, molecular part for mol_diff_mode 0 */
+  double bioturbation;        /* cm2/d */
+  int bcup_dissolved;         /* 1 flux, 2 concentration, 3 zero flux */
+  int bcup_particulate;       /* 1 flux, 4 capped flux cascade */
+  int mol_diff_mode;          /* 0 (diffusivity+0.035 T) phi_i,
+                                 1 mol_diff_d0 phi_i / (1 - 2 ln phi_i) */
+  double mol_diff_d0;         /* m2/s */
+  /* type_rhs_driver scalars (solver_library.F90:40-41) */
+  double dt_min;              /* s */
+  double relative_change_min; /* e.g. -0.9 */
+  int max_attempts;           /* adaptive attempts per column-step, > 0 */
+  int cut_scope;              /* SED_CUT_PER_COLUMN or SED_CUT_GLOBAL */
+  /* OMEXDIA+P, per-day units (examples/standalone/omexdia_p/fabm_sed.nml) */
+  double rLabile, rSemilabile, NCrLdet, NCrSdet, PAds, PAdsODU, NH3Ads,
+      CprodMax, rnit, ksO2nitri, rODUox, ksO2oduox, ksO2oxic, ksNO3denit,
+      kinO2denit, kinNO3anox, kinO2anox;
+  /* component epilogue (fabm_sediment_component.F90:1718-1732) */
+  int epilogue;               /* 1: NaN check + clamp after each step */
+  double minimum[SED_NTR];    /* clamp value per tracer */
+  /* device options */
+  int precision;              /* SED_FP32 (default) or SED_FP64 */
+  int budgets;                /* 1: FP64 P and N budgets per column-step */
+  int device;                 /* CUDA ordinal */
+} sed_params;
+
+typedef struct sed_stats {
+  long long attempts;     /* adaptive attempts, summed over columns */
+  long long accepted;     /* accepted substeps */
+  long long column_steps; /* active columns x coupling steps */
+  int max_col_attempts;   /* max attempts of one column in one step */
+  int capped_columns;     /* column-steps that hit max_attempts */
+  int nan_cells;          /* NaN cells found by the epilogue */
+  int gpu_launches;       /* kernels this library launched for the call */
+  double min_dt;          /* smallest accepted substep (s) */
+  double device_ms;       /* device time of the call's steps (CUDA events
+                             on the handle's stream) */
+} sed_stats;
+
+typedef struct sed_handle sed_handle;
+
+/* Reference defaults: sed_nml defaults, BcUp 2/1, dt_min 1e-9, -0.9,
+ * hzg_omexdia_p parameters of fabm_sed.nml:51-77, clamp at 0, FP32. */
+int sed_default_params(sed_params *p);
+
+/* Create a solver for an inum x jnum grid of kmax layers (kmax <= 64) and
+ * ntr tracers (must be SED_NTR).  Replaces the allocations of
+ * fabm_sediment_component.F90:521-541 and type_sed%initialize. */
+int sed_create(const sed_params *p, int inum, int jnum, int kmax, int ntr,
+               sed_handle **out);
+
+/* Grid and porosity (fabm_sediment_driver.F90:127-177, :278-304, :430-435).
+ * flux_cap may be NULL unless bcup_particulate == 4.  kact[ncol] gives the
+ * active layers per column (0 = land); when NULL, mask[kmax][ncol] (the
+ * reference's mask, > 0 masked, whole columns or a masked tail only) is
+ * used; when both are NULL every column is active with kmax layers. */
+int sed_set_grid(sed_handle *h, const double *dz, const double *dzc,
+                 const double *phi, const double *phi_i, const double *biofac,
+                 const double *flux_cap, const int *kact, const int *mask);
+
+/* Boundary conditions of get_boundary_conditions
+ * (fabm_sediment_component.F90:1865-2030): bdys[0] is temperature. */
+int sed_set_forcing(sed_handle *h, const double *bdys, const double *fluxes);
+
+int sed_set_state(sed_handle *h, const double *conc);
+int sed_get_state(sed_handle *h, double *conc);
+
+/* nsteps coupling steps of length dt on the device-resident state (each a
+ * captured CUDA graph); forcing stays as last set. */
+int sed_step(sed_handle *h, double dt, int method, int nsteps,
+             sed_stats *stats);
+
+/* Drop-in for `call ode_solver(sed, dt, method)` followed by the component
+ * epilogue: conc is the caller's host array, updated in place; fluxes is
+ * read (flux boundaries) and its dissolved rows are overwritten with the
+ * surface flux of the last right-hand side, as get_rhs does (:692). */
+int sed_ode_solver(sed_handle *h, double *conc, const double *bdys,
+                   double *fluxes, double dt, int method, sed_stats *stats);
+
+/* Drop-in for type_sed%get_rhs (fabm_sediment_driver.F90:575-717): rhs of
+ * conc with the current forcing; fluxes as in sed_ode_solver. */
+int sed_get_rhs(sed_handle *h, const double *conc, double *rhs,
+                double *fluxes);
+
+/* Surface fluxes [ntr][ncol] after the last step (dissolved rows). */
+int sed_get_fluxes(sed_handle *h, double *fluxes);
+
+/* Per column of the last step: attempts [ncol] (0 on land). */
+int sed_get_attempts(sed_handle *h, int *attempts);
+
+/* FP64 budgets of the last step, [4][ncol]: P inventory, P residual,
+ * N inventory, N residual (mmol/m2).  Requires params.budgets. */
+int sed_get_budgets(sed_handle *h, double *budgets);
+
+/* Run the handle's work on a caller's CUDA stream (a cudaStream_t passed
+ * as void*; NULL restores the handle's own stream).  The stream must not be
+ * the legacy default stream, because a step is captured as a CUDA graph. */
+int sed_set_stream(sed_handle *h, void *stream);
+
+/* Pin (or unpin) a caller's host array so copies run at full speed. */
+int sed_host_register(void *ptr, size_t bytes);
+int sed_host_unregister(void *ptr);
+
+const char *sed_error_string(int code);
+const char *sed_last_error(const sed_handle *h);
+const char *sed_tracer_name(int n);
+int sed_tracer_is_particulate(int n);
+
+void sed_destroy(sed_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

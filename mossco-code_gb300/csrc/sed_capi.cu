@@ -1,0 +1,880 @@
+// sed_capi.cu -- host side of the C ABI declared in include/mossco_sed.h.
+//
+// A handle owns one CUDA stream, the device-resident column state and the
+// per-layer coefficients.  Active columns are compacted into "slots" sorted
+// by active-layer count (land columns are never touched on the device),
+// grouped into tiles of tc slots; columns of up to 32 layers run in the
+// one-layer-per-lane kernel, deeper ones (to 64) in the two-layer one.  A
+// coupling step is a captured CUDA graph (queue reset + one persistent
+// kernel per depth class), replayed for every step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/mossco_sed.h"
+#include "sed_launch.h"
+
+using namespace sed;
+
+namespace {
+
+const char* kTracerNames[SED_NTR] = {
+    "detritus_labile_carbon",       "detritus_semilabile_carbon",
+    "detritus_labile_nitrogen",     "detritus_semilabile_nitrogen",
+    "detritus_labile_phosphorus",   "adsorbed_phosphorus",
+    "dissolved_oxygen",             "dissolved_nitrate",
+    "dissolved_ammonium",           "dissolved_reduced_substances",
+    "dissolved_phosphate"};
+
+struct Bin {
+  int lpl = 1;
+  int tile0 = 0, ntiles = 0;
+  int blocks = 0;
+};
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t alloc(size_t b) {
+    if (p && bytes >= b) return cudaSuccess;
+    if (p) { cudaFree(p); p = nullptr; bytes = 0; }
+    cudaError_t e = cudaMalloc(&p, b ? b : 16);
+    if (e == cudaSuccess) bytes = b;
+    return e;
+  }
+  template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace
+
+struct sed_handle {
+  sed_params prm{};
+  int inum = 0, jnum = 0, ncol = 0, kmax = 0;
+  int device = 0, sms = 0;
+  cudaStream_t stream = nullptr;      // stream in use
+  cudaStream_t own_stream = nullptr;  // stream created by the handle
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  bool have_grid = false, have_forcing = false, have_state = false;
+  // slots
+  int tc = 32, threads = 256, nslot = 0, ntiles = 0, nactive = 0;
+  std::vector<int> slot_col, slot_k;
+  Bin bins[2];
+  int nbins = 0;
+  // device buffers
+  DevBuf d_slot_col, d_kact, d_tile_k, d_conc, d_coef, d_cap, d_force, d_sflux,
+      d_budget, d_nsub, d_queue, d_stats, d_flag, d_stage, d_bdys, d_fluxes,
+      d_rhs, d_rhs_stage, d_grid;
+  DevStats* h_stats = nullptr;  // pinned
+  int* h_flag = nullptr;        // pinned
+  // graph of one coupling step
+  cudaGraphExec_t graph = nullptr;
+  double graph_dt = -1.0;
+  int graph_method = -1;
+  int graph_launches = 0;
+  long long launches = 0;
+
+  int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* what) {
+    return fail(SED_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  }
+  bool fp64() const { return prm.precision == SED_FP64; }
+  size_t rsize() const { return fp64() ? sizeof(double) : sizeof(float); }
+  ~sed_handle();
+};
+
+#define CK(expr, what)                                      \
+  do {                                                      \
+    cudaError_t e_ = (expr);                                \
+    if (e_ != cudaSuccess) return h->cuda_fail(e_, what);   \
+  } while (0)
+
+namespace {
+
+template <typename real>
+Params<real> make_params(const sed_params& s) {
+  Params<real> p{};
+  const double spd = 86400.0;
+  p.rF = (real)(s.rLabile / spd);
+  p.rS = (real)(s.rSemilabile / spd);
+  p.cmax = (real)(s.CprodMax / spd);
+  p.rnit = (real)(s.rnit / spd);
+  p.rodu = (real)(s.rODUox / spd);
+  p.pads = (real)(s.PAds / spd);
+  p.ksO2oxic = (real)s.ksO2oxic;
+  p.kinO2denit = (real)s.kinO2denit;
+  p.ksNO3denit = (real)s.ksNO3denit;
+  p.kinO2anox = (real)s.kinO2anox;
+  p.kinNO3anox = (real)s.kinNO3anox;
+  p.ksO2nitri = (real)s.ksO2nitri;
+  p.ksO2oduox = (real)s.ksO2oduox;
+  p.PAdsODU = (real)s.PAdsODU;
+  p.nh3fac = (real)(1.0 / (1.0 + s.NH3Ads));
+  p.keep = (real)(1.0 + s.relative_change_min);
+  for (int n = 0; n < NTR; n++) p.minimum[n] = (real)s.minimum[n];
+  p.dt_min = s.dt_min;
+  p.bcup_d = s.bcup_dissolved;
+  p.max_attempts = s.max_attempts;
+  p.epilogue = s.epilogue;
+  p.budgets = s.budgets;
+  return p;
+}
+
+int check_params(sed_handle* h, const sed_params& p) {
+  if (p.bcup_dissolved < 1 || p.bcup_dissolved > 3)
+    return h->fail(SED_E_ARG, "bcup_dissolved must be 1, 2 or 3 (got %d)", p.bcup_dissolved);
+  if (p.bcup_particulate != 1 && p.bcup_particulate != 4)
+    return h->fail(SED_E_ARG, "bcup_particulate must be 1 or 4 (got %d)", p.bcup_particulate);
+  if (p.mol_diff_mode != 0 && p.mol_diff_mode != 1)
+    return h->fail(SED_E_ARG, "mol_diff_mode must be 0 or 1");
+  if (p.max_attempts <= 0) return h->fail(SED_E_ARG, "max_attempts must be > 0");
+  if (p.precision != SED_FP32 && p.precision != SED_FP64)
+    return h->fail(SED_E_ARG, "precision must be SED_FP32 or SED_FP64");
+  if (p.cut_scope != SED_CUT_PER_COLUMN && p.cut_scope != SED_CUT_GLOBAL)
+    return h->fail(SED_E_ARG, "cut_scope must be per-column or global");
+  return SED_OK;
+}
+
+void reset_graph(sed_handle* h) {
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  h->graph = nullptr;
+  h->graph_dt = -1.0;
+  h->graph_method = -1;
+}
+
+template <typename real>
+ColumnArgs<real> column_args(sed_handle* h, const Bin& b, int bin_index,
+                             double dt, int method) {
+  ColumnArgs<real> a{};
+  a.conc = h->d_conc.as<real>();
+  a.out = h->d_rhs.as<real>();
+  a.coef = h->d_coef.as<real>();
+  a.cap = h->prm.bcup_particulate == 4 ? h->d_cap.as<real>() : nullptr;
+  a.force = h->d_force.as<real>();
+  a.kact = h->d_kact.as<int>();
+  a.tile_k = h->d_tile_k.as<int>();
+  a.sflux = h->d_sflux.as<real>();
+  a.budget = h->prm.budgets ? h->d_budget.as<double>() : nullptr;
+  a.nsub = h->d_nsub.as<int>();
+  a.queue = h->d_queue.as<unsigned>() + bin_index;
+  a.stats = h->d_stats.as<DevStats>();
+  a.nslot = h->nslot;
+  a.kmax = h->kmax;
+  a.tc = h->tc;
+  a.tile0 = b.tile0;
+  a.ntiles = b.ntiles;
+  a.dt = dt;
+  a.method = method;
+  return a;
+}
+
+// Enqueue the tile kernels of every depth class (one coupling step, or one
+// right-hand side for KIND_RHS).
+template <typename real>
+int enqueue_columns(sed_handle* h, double dt, int method, int kind) {
+  const Params<real> p = make_params<real>(h->prm);
+  CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
+  for (int b = 0; b < h->nbins; b++) {
+    const Bin& bin = h->bins[b];
+    if (bin.ntiles == 0) continue;
+    ColumnArgs<real> a = column_args<real>(h, bin, b, dt, method);
+    CK(launch_column<real>(a, p, bin.lpl, h->prm.bcup_particulate == 4, kind,
+                           bin.blocks, h->threads, h->stream),
+       "column kernel launch");
+    h->launches++;
+  }
+  return SED_OK;
+}
+
+int stats_reset(sed_handle* h) {
+  DevStats z{};
+  z.min_dt_bits = 0x7FF0000000000000ull;  // +inf
+  *h->h_stats = z;
+  CK(cudaMemcpyAsync(h->d_stats.p, h->h_stats, sizeof(DevStats),
+                     cudaMemcpyHostToDevice, h->stream), "stats reset");
+  return SED_OK;
+}
+
+int stats_fetch(sed_handle* h, sed_stats* out, long long launches0,
+                bool timed = false) {
+  CK(cudaMemcpyAsync(h->h_stats, h->d_stats.p, sizeof(DevStats),
+                     cudaMemcpyDeviceToHost, h->stream), "stats fetch");
+  CK(cudaStreamSynchronize(h->stream), "step");
+  const DevStats& s = *h->h_stats;
+  float ms = 0.0f;
+  if (timed) CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1), "event time");
+  if (out) {
+    out->device_ms = ms;
+    out->attempts = (long long)s.attempts;
+    out->accepted = (long long)s.accepted;
+    out->column_steps = (long long)s.column_steps;
+    out->max_col_attempts = s.max_col_attempts;
+    out->capped_columns = s.capped;
+    out->nan_cells = s.nan_cells;
+    out->gpu_launches = (int)(h->launches - launches0);
+    double md;
+    unsigned long long bits = s.min_dt_bits;
+    memcpy(&md, &bits, sizeof md);
+    out->min_dt = md;
+  }
+  if (s.status & ST_NAN)
+    return h->fail(SED_E_NAN, "NaN in %d cells after the step", s.nan_cells);
+  if (s.status & ST_CAP)
+    return h->fail(SED_E_SUBSTEP_CAP, "%d column-steps hit max_attempts=%d", s.capped,
+                   h->prm.max_attempts);
+  return SED_OK;
+}
+
+// One coupling step of every column, per-column cut (graph replay).
+template <typename real>
+int step_percol(sed_handle* h, double dt, int method) {
+  const int kind = method == SED_ADAPTIVE_EULER ? KIND_ADAPT : KIND_FIXED;
+  if (!h->graph || h->graph_dt != dt || h->graph_method != method) {
+    reset_graph(h);
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    const long long l0 = h->launches;
+    int rc = enqueue_columns<real>(h, dt, method, kind);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (rc != SED_OK) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return h->cuda_fail(e, "end capture");
+    h->graph_launches = (int)(h->launches - l0);
+    h->launches = l0;
+    e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { h->graph = nullptr; return h->cuda_fail(e, "graph instantiate"); }
+    h->graph_dt = dt;
+    h->graph_method = method;
+  }
+  CK(cudaGraphLaunch(h->graph, h->stream), "graph launch");
+  h->launches += h->graph_launches;
+  return SED_OK;
+}
+
+// One coupling step with the reference's grid-wide cut: any() over every
+// active cell of the grid decides the substep (solver_library.F90:121).
+template <typename real>
+int step_global(sed_handle* h, double dt) {
+  const Params<real> p = make_params<real>(h->prm);
+  const size_t n = (size_t)NTR * h->kmax * h->nslot;
+  CK(h->d_rhs.alloc(n * sizeof(real)), "rhs buffer");
+  double dt_int = 0.0, dt_red = dt;
+  bool need_rhs = true;
+  long long att = 0, acc = 0;
+  double min_dt = 1e300;
+  bool capped = false;
+  while (dt_int < dt) {
+    if (att >= h->prm.max_attempts) {
+      capped = true;
+      break;
+    }
+    att++;
+    if (need_rhs) {
+      int rc = enqueue_columns<real>(h, dt, 0, KIND_RHS);
+      if (rc) return rc;
+      need_rhs = false;
+    }
+    CK(cudaMemsetAsync(h->d_flag.p, 0, sizeof(int), h->stream), "flag reset");
+    CK(launch_trial<real>(h->d_conc.as<real>(), h->d_rhs.as<real>(), h->d_kact.as<int>(),
+                          h->nslot, h->kmax, (real)dt_red, p.keep, h->d_flag.as<int>(),
+                          h->sms, h->stream), "trial launch");
+    h->launches++;
+    CK(cudaMemcpyAsync(h->h_flag, h->d_flag.p, sizeof(int), cudaMemcpyDeviceToHost,
+                       h->stream), "flag fetch");
+    CK(cudaStreamSynchronize(h->stream), "trial");
+    if (*h->h_flag && dt_red > h->prm.dt_min) {
+      dt_red = dt_red * 0.25;
+    } else {
+      CK(launch_accept<real>(h->d_conc.as<real>(), h->d_rhs.as<real>(), h->d_kact.as<int>(),
+                             h->nslot, h->kmax, (real)dt_red, h->sms, h->stream),
+         "accept launch");
+      h->launches++;
+      dt_int = dt_int + dt_red;
+      acc++;
+      if (dt_red < min_dt) min_dt = dt_red;
+      need_rhs = true;
+    }
+  }
+  if (h->prm.epilogue) {
+    CK(launch_epilogue<real>(h->d_conc.as<real>(), h->d_kact.as<int>(), h->nslot,
+                             h->kmax, p, h->d_stats.as<DevStats>(), h->sms, h->stream),
+       "epilogue launch");
+    h->launches++;
+  }
+  // host-side counters merged into the device stats record
+  DevStats tmp;
+  CK(cudaMemcpyAsync(&tmp, h->d_stats.p, sizeof tmp, cudaMemcpyDeviceToHost, h->stream),
+     "stats");
+  CK(cudaStreamSynchronize(h->stream), "global step");
+  tmp.attempts += (unsigned long long)(att * h->nactive);
+  tmp.accepted += (unsigned long long)(acc * h->nactive);
+  tmp.column_steps += (unsigned long long)h->nactive;
+  tmp.max_col_attempts = std::max(tmp.max_col_attempts, (int)att);
+  if (capped) { tmp.status |= ST_CAP; tmp.capped += h->nactive; }
+  unsigned long long bits;
+  memcpy(&bits, &min_dt, sizeof bits);
+  if (acc > 0 && bits < tmp.min_dt_bits) tmp.min_dt_bits = bits;
+  CK(cudaMemcpyAsync(h->d_stats.p, &tmp, sizeof tmp, cudaMemcpyHostToDevice, h->stream),
+     "stats");
+  CK(cudaStreamSynchronize(h->stream), "global step");
+  return SED_OK;
+}
+
+template <typename real>
+int step_any(sed_handle* h, double dt, int method) {
+  if (method == SED_ADAPTIVE_EULER && h->prm.cut_scope == SED_CUT_GLOBAL)
+    return step_global<real>(h, dt);
+  return step_percol<real>(h, dt, method);
+}
+
+int dispatch_step(sed_handle* h, double dt, int method) {
+  return h->fp64() ? step_any<double>(h, dt, method) : step_any<float>(h, dt, method);
+}
+
+template <typename real>
+int gather_state(sed_handle* h) {
+  CK(launch_gather<real>(h->d_stage.as<double>(), h->d_conc.as<real>(),
+                         h->d_slot_col.as<int>(), NTR, h->kmax, h->ncol, h->nslot,
+                         h->sms, h->stream), "gather launch");
+  h->launches++;
+  return SED_OK;
+}
+
+template <typename real>
+int scatter_state(sed_handle* h, const real* src, double* dst) {
+  CK(launch_scatter<real>(src, dst, h->d_slot_col.as<int>(),
+                          h->d_kact.as<int>(), NTR, h->kmax, h->ncol, h->nslot,
+                          h->sms, h->stream), "scatter launch");
+  h->launches++;
+  return SED_OK;
+}
+
+template <typename real>
+int scatter_fluxes(sed_handle* h) {
+  CK(launch_scatter_flux<real>(h->d_sflux.as<real>(), h->d_fluxes.as<double>(),
+                               h->d_slot_col.as<int>(), h->d_kact.as<int>(), h->ncol,
+                               h->nslot, h->sms, h->stream), "flux scatter launch");
+  h->launches++;
+  return SED_OK;
+}
+
+template <typename real>
+int prep_force(sed_handle* h) {
+  CK(launch_prep_force<real>(h->d_bdys.as<double>(), h->d_fluxes.as<double>(),
+                             h->d_slot_col.as<int>(), h->d_force.as<real>(), h->ncol,
+                             h->nslot, h->prm.bioturbation, h->prm.diffusivity,
+                             h->prm.mol_diff_mode, h->prm.bcup_dissolved, h->sms,
+                             h->stream), "forcing launch");
+  h->launches++;
+  return SED_OK;
+}
+
+int upload_forcing(sed_handle* h, const double* bdys, const double* fluxes) {
+  const size_t nb = (size_t)(NTR + 1) * h->ncol * sizeof(double);
+  const size_t nf = (size_t)NTR * h->ncol * sizeof(double);
+  CK(cudaMemcpyAsync(h->d_bdys.p, bdys, nb, cudaMemcpyHostToDevice, h->stream), "bdys copy");
+  CK(cudaMemcpyAsync(h->d_fluxes.p, fluxes, nf, cudaMemcpyHostToDevice, h->stream), "fluxes copy");
+  int rc = h->fp64() ? prep_force<double>(h) : prep_force<float>(h);
+  if (rc) return rc;
+  h->have_forcing = true;
+  return SED_OK;
+}
+
+int upload_state(sed_handle* h, const double* conc) {
+  const size_t bytes = (size_t)NTR * h->kmax * h->ncol * sizeof(double);
+  CK(cudaMemcpyAsync(h->d_stage.p, conc, bytes, cudaMemcpyHostToDevice, h->stream), "conc copy");
+  int rc = h->fp64() ? gather_state<double>(h) : gather_state<float>(h);
+  if (rc) return rc;
+  h->have_state = true;
+  return SED_OK;
+}
+
+int download_state(sed_handle* h, double* conc) {
+  const size_t bytes = (size_t)NTR * h->kmax * h->ncol * sizeof(double);
+  int rc = h->fp64() ? scatter_state<double>(h, h->d_conc.as<double>(), h->d_stage.as<double>())
+                     : scatter_state<float>(h, h->d_conc.as<float>(), h->d_stage.as<double>());
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(conc, h->d_stage.p, bytes, cudaMemcpyDeviceToHost, h->stream), "conc copy back");
+  return SED_OK;
+}
+
+int ready(sed_handle* h) {
+  if (!h) return SED_E_ARG;
+  if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
+  if (!h->have_forcing) return h->fail(SED_E_STATE, "sed_set_forcing has not been called");
+  return SED_OK;
+}
+
+}  // namespace
+
+sed_handle::~sed_handle() {
+  cudaSetDevice(device);
+  if (stream) cudaStreamSynchronize(stream);
+  reset_graph(this);
+  if (h_stats) cudaFreeHost(h_stats);
+  if (h_flag) cudaFreeHost(h_flag);
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
+  if (own_stream) cudaStreamDestroy(own_stream);
+}
+
+// ===========================================================================
+extern "C" {
+
+int sed_default_params(sed_params* p) {
+  if (!p) return SED_E_ARG;
+  memset(p, 0, sizeof *p);
+  p->diffusivity = 0.9;
+  p->bioturbation = 0.9;
+  p->bcup_dissolved = 2;
+  p->bcup_particulate = 1;
+  p->mol_diff_mode = 0;
+  p->mol_diff_d0 = 1.0e-9;
+  p->dt_min = 1.0e-9;
+  p->relative_change_min = -0.9;
+  p->max_attempts = 8192;
+  p->cut_scope = SED_CUT_PER_COLUMN;
+  p->rLabile = 0.043;
+  p->rSemilabile = 0.001;
+  p->NCrLdet = 0.22;
+  p->NCrSdet = 0.005;
+  p->PAds = 0.01;
+  p->PAdsODU = 70.0;
+  p->NH3Ads = 0.0;
+  p->CprodMax = 9600.0;
+  p->rnit = 200.0;
+  p->ksO2nitri = 20.0;
+  p->rODUox = 20.0;
+  p->ksO2oduox = 1.0;
+  p->ksO2oxic = 3.0;
+  p->ksNO3denit = 1.0;
+  p->kinO2denit = 70.0;
+  p->kinNO3anox = 1.0;
+  p->kinO2anox = 1.0;
+  p->epilogue = 1;
+  p->precision = SED_FP32;
+  p->budgets = 0;
+  p->device = 0;
+  return SED_OK;
+}
+
+int sed_create(const sed_params* p, int inum, int jnum, int kmax, int ntr,
+               sed_handle** out) {
+  if (!p || !out) return SED_E_ARG;
+  *out = nullptr;
+  if (ntr != SED_NTR || inum <= 0 || jnum <= 0 || kmax < 1 || kmax > SED_KMAX_LIMIT)
+    return SED_E_ARG;
+  if ((long long)inum * jnum > (1LL << 30)) return SED_E_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return SED_E_NODEVICE;
+  }
+  if (p->device < 0 || p->device >= ndev) return SED_E_ARG;
+  std::unique_ptr<sed_handle> h(new sed_handle());
+  h->prm = *p;
+  int rc = check_params(h.get(), *p);
+  if (rc) return rc;
+  h->inum = inum;
+  h->jnum = jnum;
+  h->ncol = inum * jnum;
+  h->kmax = kmax;
+  h->device = p->device;
+  sed_handle* hh = h.get();
+  {
+    sed_handle* h = hh;
+    CK(cudaSetDevice(h->device), "set device");
+    CK(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device), "SM count");
+    CK(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking), "stream");
+    h->stream = h->own_stream;
+    CK(cudaEventCreate(&h->ev0), "event");
+    CK(cudaEventCreate(&h->ev1), "event");
+    CK(cudaHostAlloc((void**)&h->h_stats, sizeof(DevStats), cudaHostAllocDefault), "pinned stats");
+    CK(cudaHostAlloc((void**)&h->h_flag, sizeof(int), cudaHostAllocDefault), "pinned flag");
+    CK(h->d_queue.alloc(4 * sizeof(unsigned)), "queue");
+    CK(h->d_stats.alloc(sizeof(DevStats)), "stats");
+    CK(h->d_flag.alloc(sizeof(int)), "flag");
+    const size_t ncol = (size_t)h->ncol;
+    CK(h->d_stage.alloc((size_t)NTR * kmax * ncol * sizeof(double)), "state staging");
+    CK(h->d_bdys.alloc((size_t)(NTR + 1) * ncol * sizeof(double)), "bdys");
+    CK(h->d_fluxes.alloc((size_t)NTR * ncol * sizeof(double)), "fluxes");
+  }
+  *out = h.release();
+  return SED_OK;
+}
+
+int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
+                 const double* phi, const double* phi_i, const double* biofac,
+                 const double* flux_cap, const int* kact, const int* mask) {
+  if (!h) return SED_E_ARG;
+  if (!dz || !phi || !phi_i || !biofac || (h->kmax > 1 && !dzc))
+    return h->fail(SED_E_ARG, "sed_set_grid: dz, dzc, phi, phi_i and biofac are required");
+  if (h->prm.bcup_particulate == 4 && !flux_cap)
+    return h->fail(SED_E_ARG, "sed_set_grid: flux_cap is required for bcup_particulate 4");
+  CK(cudaSetDevice(h->device), "set device");
+  const int ncol = h->ncol, kmax = h->kmax;
+  // active layers per column
+  std::vector<int> ka(ncol, kmax);
+  if (kact) {
+    for (int c = 0; c < ncol; c++) {
+      if (kact[c] < 0 || kact[c] > kmax)
+        return h->fail(SED_E_ARG, "kact[%d]=%d outside 0..%d", c, kact[c], kmax);
+      ka[c] = kact[c];
+    }
+  } else if (mask) {
+    for (int c = 0; c < ncol; c++) {
+      int K = 0;
+      while (K < kmax && mask[(size_t)K * ncol + c] <= 0) K++;
+      for (int k = K; k < kmax; k++)
+        if (mask[(size_t)k * ncol + c] <= 0)
+          return h->fail(SED_E_ARG, "mask of column %d has an unmasked cell below a masked one", c);
+      ka[c] = K;
+    }
+  }
+  // check_domain (fabm_sediment_driver.F90:503-530) on active cells
+  for (int c = 0; c < ncol; c++)
+    for (int k = 0; k < ka[c]; k++) {
+      const size_t i = (size_t)k * ncol + c;
+      if (!(phi[i] > 0.0) || phi[i] > 1.0 || !(phi_i[i] > 0.0) || phi_i[i] > 1.0)
+        return h->fail(SED_E_ARG, "porosity outside (0,1] at column %d layer %d", c, k);
+      if (!(dz[i] > 0.0)) return h->fail(SED_E_ARG, "dz <= 0 at column %d layer %d", c, k);
+      if (k > 0 && !(dzc[(size_t)(k - 1) * ncol + c] > 0.0))
+        return h->fail(SED_E_ARG, "dzc <= 0 at column %d layer %d", c, k);
+    }
+  // slots: active columns sorted by depth class then layers (stable)
+  std::vector<int> order;
+  order.reserve(ncol);
+  for (int c = 0; c < ncol; c++)
+    if (ka[c] > 0) order.push_back(c);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    const int ba = ka[a] > 32, bb = ka[b] > 32;
+    if (ba != bb) return ba < bb;
+    return ka[a] < ka[b];
+  });
+  h->nactive = (int)order.size();
+  int n1 = 0;
+  for (int c : order) n1 += ka[c] <= 32;
+  const int n2 = h->nactive - n1;
+  // tile width: 32 columns for the one-layer class, 16 when deep columns exist
+  h->tc = (kmax > 32) ? 16 : 32;
+  const int tc = h->tc;
+  const int nt1 = (n1 + tc - 1) / tc, nt2 = (n2 + tc - 1) / tc;
+  h->ntiles = nt1 + nt2;
+  h->nslot = std::max(1, h->ntiles) * tc;
+  h->slot_col.assign(h->nslot, -1);
+  h->slot_k.assign(h->nslot, 0);
+  for (int i = 0; i < n1; i++) { h->slot_col[i] = order[i]; h->slot_k[i] = ka[order[i]]; }
+  for (int i = 0; i < n2; i++) {
+    h->slot_col[nt1 * tc + i] = order[n1 + i];
+    h->slot_k[nt1 * tc + i] = ka[order[n1 + i]];
+  }
+  std::vector<int> tile_k(std::max(1, h->ntiles), 1);
+  for (int t = 0; t < h->ntiles; t++) {
+    int m = 1;
+    for (int j = 0; j < tc; j++) m = std::max(m, h->slot_k[t * tc + j]);
+    tile_k[t] = m;
+  }
+  h->nbins = 0;
+  const bool bc4 = h->prm.bcup_particulate == 4;
+  const int kind = KIND_ADAPT;
+  for (int b = 0; b < 2; b++) {
+    Bin& bin = h->bins[h->nbins];
+    bin.lpl = b == 0 ? 1 : 2;
+    bin.tile0 = b == 0 ? 0 : nt1;
+    bin.ntiles = b == 0 ? nt1 : nt2;
+    if (bin.ntiles == 0) continue;
+    int occ = 1 << 30;
+    for (int kd = 0; kd < 3; kd++) {
+      // also sets every variant's shared-memory limit before any capture
+      const int o = h->fp64() ? column_blocks_per_sm<double>(tc, bin.lpl, bc4, kd, h->threads)
+                              : column_blocks_per_sm<float>(tc, bin.lpl, bc4, kd, h->threads);
+      if (kd == kind) occ = o;
+      if (o <= 0) return h->fail(SED_E_CUDA, "column kernel does not fit on the device");
+    }
+    bin.blocks = std::min(bin.ntiles, occ * h->sms);
+    h->nbins++;
+  }
+  // device buffers
+  const size_t ns = (size_t)h->nslot, rs = h->rsize();
+  CK(h->d_slot_col.alloc(ns * sizeof(int)), "slot map");
+  CK(h->d_kact.alloc(ns * sizeof(int)), "kact");
+  CK(h->d_tile_k.alloc(tile_k.size() * sizeof(int)), "tile_k");
+  CK(h->d_conc.alloc((size_t)NTR * kmax * ns * rs), "state");
+  CK(h->d_coef.alloc((size_t)NCOEF * kmax * ns * rs), "coefficients");
+  CK(h->d_force.alloc((size_t)NFORCE * ns * rs), "forcing");
+  CK(h->d_sflux.alloc((size_t)NDISS * ns * rs), "surface flux");
+  CK(h->d_nsub.alloc(ns * sizeof(int)), "attempts");
+  if (h->prm.budgets) CK(h->d_budget.alloc(4 * ns * sizeof(double)), "budgets");
+  if (bc4) CK(h->d_cap.alloc((size_t)kmax * ns * rs), "flux cap");
+  CK(cudaMemsetAsync(h->d_conc.p, 0, (size_t)NTR * kmax * ns * rs, h->stream), "state clear");
+  CK(cudaMemsetAsync(h->d_sflux.p, 0, (size_t)NDISS * ns * rs, h->stream), "flux clear");
+  CK(cudaMemsetAsync(h->d_nsub.p, 0, ns * sizeof(int), h->stream), "attempts clear");
+  if (h->prm.budgets)
+    CK(cudaMemsetAsync(h->d_budget.p, 0, 4 * ns * sizeof(double), h->stream), "budget clear");
+  CK(cudaMemcpyAsync(h->d_slot_col.p, h->slot_col.data(), ns * sizeof(int),
+                     cudaMemcpyHostToDevice, h->stream), "slot map copy");
+  CK(cudaMemcpyAsync(h->d_kact.p, h->slot_k.data(), ns * sizeof(int),
+                     cudaMemcpyHostToDevice, h->stream), "kact copy");
+  CK(cudaMemcpyAsync(h->d_tile_k.p, tile_k.data(), tile_k.size() * sizeof(int),
+                     cudaMemcpyHostToDevice, h->stream), "tile_k copy");
+  // grid arrays through a temporary FP64 staging area
+  const size_t lay = (size_t)kmax * ncol;
+  CK(h->d_grid.alloc(6 * lay * sizeof(double)), "grid staging");
+  double* g = h->d_grid.as<double>();
+  CK(cudaMemcpyAsync(g + 0 * lay, dz, lay * sizeof(double), cudaMemcpyHostToDevice, h->stream), "dz");
+  if (kmax > 1)
+    CK(cudaMemcpyAsync(g + 1 * lay, dzc, (size_t)(kmax - 1) * ncol * sizeof(double),
+                       cudaMemcpyHostToDevice, h->stream), "dzc");
+  CK(cudaMemcpyAsync(g + 2 * lay, phi, lay * sizeof(double), cudaMemcpyHostToDevice, h->stream), "phi");
+  CK(cudaMemcpyAsync(g + 3 * lay, phi_i, lay * sizeof(double), cudaMemcpyHostToDevice, h->stream), "phi_i");
+  CK(cudaMemcpyAsync(g + 4 * lay, biofac, lay * sizeof(double), cudaMemcpyHostToDevice, h->stream), "biofac");
+  if (bc4)
+    CK(cudaMemcpyAsync(g + 5 * lay, flux_cap, lay * sizeof(double), cudaMemcpyHostToDevice,
+                       h->stream), "flux_cap");
+  cudaError_t e;
+  if (h->fp64())
+    e = launch_prep_grid<double>(g, g + lay, g + 2 * lay, g + 3 * lay, g + 4 * lay,
+                                 bc4 ? g + 5 * lay : nullptr, h->d_slot_col.as<int>(),
+                                 h->d_coef.as<double>(), bc4 ? h->d_cap.as<double>() : nullptr,
+                                 kmax, ncol, h->nslot, h->prm.mol_diff_mode,
+                                 h->prm.mol_diff_d0, h->sms, h->stream);
+  else
+    e = launch_prep_grid<float>(g, g + lay, g + 2 * lay, g + 3 * lay, g + 4 * lay,
+                                bc4 ? g + 5 * lay : nullptr, h->d_slot_col.as<int>(),
+                                h->d_coef.as<float>(), bc4 ? h->d_cap.as<float>() : nullptr,
+                                kmax, ncol, h->nslot, h->prm.mol_diff_mode,
+                                h->prm.mol_diff_d0, h->sms, h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "grid launch");
+  h->launches++;
+  CK(cudaStreamSynchronize(h->stream), "set_grid");
+  h->d_grid.release();
+  reset_graph(h);
+  h->have_grid = true;
+  h->have_state = false;
+  h->have_forcing = false;
+  return SED_OK;
+}
+
+int sed_set_forcing(sed_handle* h, const double* bdys, const double* fluxes) {
+  if (!h) return SED_E_ARG;
+  if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
+  if (!bdys || !fluxes) return h->fail(SED_E_ARG, "bdys and fluxes are required");
+  CK(cudaSetDevice(h->device), "set device");
+  int rc = upload_forcing(h, bdys, fluxes);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(h->stream), "set_forcing");
+  return SED_OK;
+}
+
+int sed_set_state(sed_handle* h, const double* conc) {
+  if (!h) return SED_E_ARG;
+  if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
+  if (!conc) return h->fail(SED_E_ARG, "conc is required");
+  CK(cudaSetDevice(h->device), "set device");
+  int rc = upload_state(h, conc);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(h->stream), "set_state");
+  return SED_OK;
+}
+
+int sed_get_state(sed_handle* h, double* conc) {
+  if (!h) return SED_E_ARG;
+  if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");
+  if (!conc) return h->fail(SED_E_ARG, "conc is required");
+  CK(cudaSetDevice(h->device), "set device");
+  int rc = download_state(h, conc);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(h->stream), "get_state");
+  return SED_OK;
+}
+
+int sed_step(sed_handle* h, double dt, int method, int nsteps, sed_stats* stats) {
+  int rc = ready(h);
+  if (rc) return rc;
+  if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");
+  if (method < 0 || method > 3 || !(dt > 0.0) || nsteps < 0)
+    return h->fail(SED_E_ARG, "bad dt, method or nsteps");
+  CK(cudaSetDevice(h->device), "set device");
+  const long long l0 = h->launches;
+  rc = stats_reset(h);
+  if (rc) return rc;
+  CK(cudaEventRecord(h->ev0, h->stream), "event");
+  for (int s = 0; s < nsteps; s++) {
+    rc = h->fp64() ? step_any<double>(h, dt, method) : step_any<float>(h, dt, method);
+    if (rc) return rc;
+  }
+  CK(cudaEventRecord(h->ev1, h->stream), "event");
+  return stats_fetch(h, stats, l0, true);
+}
+
+int sed_ode_solver(sed_handle* h, double* conc, const double* bdys, double* fluxes,
+                   double dt, int method, sed_stats* stats) {
+  int rc;
+  if (!h) return SED_E_ARG;
+  if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
+  if (!conc || !bdys || !fluxes) return h->fail(SED_E_ARG, "conc, bdys and fluxes are required");
+  if (method < 0 || method > 3 || !(dt > 0.0)) return h->fail(SED_E_ARG, "bad dt or method");
+  CK(cudaSetDevice(h->device), "set device");
+  const long long l0 = h->launches;
+  if ((rc = stats_reset(h))) return rc;
+  CK(cudaEventRecord(h->ev0, h->stream), "event");
+  if ((rc = upload_state(h, conc))) return rc;
+  if ((rc = upload_forcing(h, bdys, fluxes))) return rc;
+  if ((rc = dispatch_step(h, dt, method))) return rc;
+  if ((rc = download_state(h, conc))) return rc;
+  rc = h->fp64() ? scatter_fluxes<double>(h) : scatter_fluxes<float>(h);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(fluxes, h->d_fluxes.p, (size_t)NTR * h->ncol * sizeof(double),
+                     cudaMemcpyDeviceToHost, h->stream), "fluxes copy back");
+  CK(cudaEventRecord(h->ev1, h->stream), "event");
+  return stats_fetch(h, stats, l0, true);
+}
+
+int sed_get_rhs(sed_handle* h, const double* conc, double* rhs, double* fluxes) {
+  int rc;
+  if (!h) return SED_E_ARG;
+  if ((rc = ready(h))) return rc;
+  if (!conc || !rhs) return h->fail(SED_E_ARG, "conc and rhs are required");
+  CK(cudaSetDevice(h->device), "set device");
+  const size_t n = (size_t)NTR * h->kmax * h->nslot * h->rsize();
+  CK(h->d_rhs.alloc(n), "rhs buffer");
+  if ((rc = upload_state(h, conc))) return rc;
+  if ((rc = h->fp64() ? enqueue_columns<double>(h, 0.0, 0, KIND_RHS)
+                      : enqueue_columns<float>(h, 0.0, 0, KIND_RHS)))
+    return rc;
+  // rhs of inactive cells is zero (get_rhs :703-708)
+  const size_t bytes = (size_t)NTR * h->kmax * h->ncol * sizeof(double);
+  CK(h->d_rhs_stage.alloc(bytes), "rhs staging");
+  CK(cudaMemsetAsync(h->d_rhs_stage.p, 0, bytes, h->stream), "rhs clear");
+  rc = h->fp64() ? scatter_state<double>(h, h->d_rhs.as<double>(), h->d_rhs_stage.as<double>())
+                 : scatter_state<float>(h, h->d_rhs.as<float>(), h->d_rhs_stage.as<double>());
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(rhs, h->d_rhs_stage.p, bytes, cudaMemcpyDeviceToHost, h->stream),
+     "rhs copy back");
+  if (fluxes) {
+    rc = h->fp64() ? scatter_fluxes<double>(h) : scatter_fluxes<float>(h);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(fluxes, h->d_fluxes.p, (size_t)NTR * h->ncol * sizeof(double),
+                       cudaMemcpyDeviceToHost, h->stream), "fluxes copy back");
+  }
+  CK(cudaStreamSynchronize(h->stream), "get_rhs");
+  return SED_OK;
+}
+
+int sed_get_fluxes(sed_handle* h, double* fluxes) {
+  if (!h) return SED_E_ARG;
+  if (!h->have_forcing) return h->fail(SED_E_STATE, "sed_set_forcing has not been called");
+  if (!fluxes) return h->fail(SED_E_ARG, "fluxes is required");
+  CK(cudaSetDevice(h->device), "set device");
+  int rc = h->fp64() ? scatter_fluxes<double>(h) : scatter_fluxes<float>(h);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(fluxes, h->d_fluxes.p, (size_t)NTR * h->ncol * sizeof(double),
+                     cudaMemcpyDeviceToHost, h->stream), "fluxes copy back");
+  CK(cudaStreamSynchronize(h->stream), "get_fluxes");
+  return SED_OK;
+}
+
+int sed_get_attempts(sed_handle* h, int* attempts) {
+  if (!h || !attempts) return SED_E_ARG;
+  if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
+  CK(cudaSetDevice(h->device), "set device");
+  std::vector<int> tmp(h->nslot);
+  CK(cudaMemcpyAsync(tmp.data(), h->d_nsub.p, tmp.size() * sizeof(int), cudaMemcpyDeviceToHost,
+                     h->stream), "attempts copy");
+  CK(cudaStreamSynchronize(h->stream), "attempts");
+  for (int c = 0; c < h->ncol; c++) attempts[c] = 0;
+  for (int s = 0; s < h->nslot; s++)
+    if (h->slot_col[s] >= 0) attempts[h->slot_col[s]] = tmp[s];
+  return SED_OK;
+}
+
+int sed_get_budgets(sed_handle* h, double* budgets) {
+  if (!h || !budgets) return SED_E_ARG;
+  if (!h->prm.budgets) return h->fail(SED_E_STATE, "budgets were not enabled in sed_params");
+  if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
+  CK(cudaSetDevice(h->device), "set device");
+  std::vector<double> tmp((size_t)4 * h->nslot);
+  CK(cudaMemcpyAsync(tmp.data(), h->d_budget.p, tmp.size() * sizeof(double),
+                     cudaMemcpyDeviceToHost, h->stream), "budget copy");
+  CK(cudaStreamSynchronize(h->stream), "budgets");
+  for (size_t i = 0; i < (size_t)4 * h->ncol; i++) budgets[i] = 0.0;
+  for (int b = 0; b < 4; b++)
+    for (int s = 0; s < h->nslot; s++)
+      if (h->slot_col[s] >= 0)
+        budgets[(size_t)b * h->ncol + h->slot_col[s]] = tmp[(size_t)b * h->nslot + s];
+  return SED_OK;
+}
+
+int sed_set_stream(sed_handle* h, void* stream) {
+  if (!h) return SED_E_ARG;
+  CK(cudaSetDevice(h->device), "set device");
+  CK(cudaStreamSynchronize(h->stream), "stream switch");
+  h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
+  reset_graph(h);
+  return SED_OK;
+}
+
+int sed_host_register(void* ptr, size_t bytes) {
+  if (!ptr || !bytes) return SED_E_ARG;
+  cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+  if (e != cudaSuccess) { cudaGetLastError(); return SED_E_CUDA; }
+  return SED_OK;
+}
+
+int sed_host_unregister(void* ptr) {
+  if (!ptr) return SED_E_ARG;
+  cudaError_t e = cudaHostUnregister(ptr);
+  if (e != cudaSuccess) { cudaGetLastError(); return SED_E_CUDA; }
+  return SED_OK;
+}
+
+const char* sed_error_string(int code) {
+  switch (code) {
+    case SED_OK: return "ok";
+    case SED_E_ARG: return "invalid argument";
+    case SED_E_NAN: return "NaN in state";
+    case SED_E_SUBSTEP_CAP: return "adaptive substep cap reached";
+    case SED_E_CUDA: return "CUDA error";
+    case SED_E_STATE: return "call order: grid, forcing or state missing";
+    case SED_E_NOMEM: return "out of memory";
+    case SED_E_NODEVICE: return "no CUDA device";
+    case SED_E_TIMEOUT: return "bounded device wait gave up";
+    default: return "unknown error";
+  }
+}
+
+const char* sed_last_error(const sed_handle* h) { return h ? h->err.c_str() : ""; }
+
+const char* sed_tracer_name(int n) {
+  return (n >= 0 && n < SED_NTR) ? kTracerNames[n] : "";
+}
+
+int sed_tracer_is_particulate(int n) { return (n >= 0 && n < NPART) ? 1 : 0; }
+
+void sed_destroy(sed_handle* h) { delete h; }
+
+}  // extern "C"

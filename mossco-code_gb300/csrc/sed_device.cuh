@@ -1,0 +1,270 @@
+// sed_device.cuh -- device-side building blocks of the sediment-column solver.
+//
+// One warp owns one sediment column: lane l holds layers l and (for LPL=2)
+// l+32 of all 11 tracers in registers, so a right-hand side evaluation is
+// local arithmetic plus two warp shuffles per tracer for the interface
+// fluxes, and the adaptive step decision is one warp vote.
+//
+// Reference semantics followed here (paths inside platipodium/mossco-code):
+//   get_rhs   src/drivers/fabm_sediment_driver.F90:575-717
+//   diff3d    src/drivers/fabm_sediment_driver.F90:739-825
+//   ode_solver src/utilities/solver_library.F90:80-189
+//   epilogue  src/components/fabm_sediment_component.F90:1715-1732
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sed {
+
+constexpr int NTR = 11;    // tracers
+constexpr int NPART = 6;   // tracers 0..5 are particulate
+constexpr int NDISS = 5;   // tracers 6..10 are dissolved
+constexpr int NCOEF = 4;   // per-layer coefficient rows: phi, vol, gb, gm
+constexpr int NFORCE = 13; // per-column forcing rows: bioT, dmul, bnd[11]
+constexpr unsigned FULL = 0xffffffffu;
+
+enum : int { ST_NAN = 1, ST_CAP = 2, ST_ARG = 4 };
+
+// Tracer indices
+enum : int {
+  T_FDETC = 0, T_SDETC, T_FDETN, T_SDETN, T_FDETP, T_ADSP,
+  T_O2, T_NO3, T_NH4, T_ODU, T_PO4
+};
+
+// Reaction and solver constants in kernel units (rates per second).
+template <typename real>
+struct Params {
+  real rF, rS, cmax, rnit, rodu, pads;
+  real ksO2oxic, kinO2denit, ksNO3denit, kinO2anox, kinNO3anox, ksO2nitri,
+      ksO2oduox, PAdsODU, nh3fac;
+  real keep;          // 1 + relative_change_min
+  real minimum[NTR];  // clamp of the component epilogue
+  double dt_min;
+  int bcup_d;         // 1 flux, 2 concentration, 3 zero
+  int max_attempts;
+  int epilogue;
+  int budgets;
+};
+
+struct DevStats {
+  unsigned long long attempts;
+  unsigned long long accepted;
+  unsigned long long column_steps;
+  unsigned long long min_dt_bits;  // bit pattern of a positive double
+  int max_col_attempts;
+  int capped;
+  int nan_cells;
+  int status;
+};
+
+// ---------------------------------------------------------------------------
+// division helpers: fast reciprocal in FP32, IEEE division in FP64
+__device__ __forceinline__ float sdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double sdiv(double a, double b) { return a / b; }
+
+// ---------------------------------------------------------------------------
+// OMEXDIA+P local rates of one cell (per second).  Published OMEXDIA
+// (Soetaert, Herman, Middelburg 1996): two detritus classes with first-order
+// decay; carbon mineralisation split into oxic / denitrification / anoxic
+// pathways by Monod limitation and inhibition terms rescaled to sum to one;
+// nitrification and ODU oxidation with O2 Monod terms; 0.8 mol NO3 per mol C
+// denitrified; NH4 adsorption factor 1/(1+NH3Ads).  P extension: detrital P
+// mineralises at the labile rate and PO4 exchanges with an adsorbed-P pool at
+// rate PAds, the sorbing share being PAdsODU/(PAdsODU+ODU).
+template <typename real>
+__device__ __forceinline__ void omexdia_p(const Params<real>& p,
+                                          const real (&c)[NTR],
+                                          real (&r)[NTR], real& denit) {
+  const real fdetC = c[T_FDETC], sdetC = c[T_SDETC], fdetN = c[T_FDETN];
+  const real sdetN = c[T_SDETN], fdetP = c[T_FDETP], adsP = c[T_ADSP];
+  const real O2 = c[T_O2], NO3 = c[T_NO3], NH4 = c[T_NH4], ODU = c[T_ODU];
+  const real PO4 = c[T_PO4];
+  const real CprodF = p.rF * fdetC;
+  const real CprodS = p.rS * sdetC;
+  const real Cprod = CprodF + CprodS;
+  real lim = real(1);
+  if (Cprod > p.cmax) lim = sdiv(p.cmax, Cprod);
+  const real oxlim = sdiv(O2, O2 + p.ksO2oxic);
+  const real dnlim = sdiv(p.kinO2denit, O2 + p.kinO2denit) * sdiv(NO3, NO3 + p.ksNO3denit);
+  const real anlim = sdiv(p.kinO2anox, O2 + p.kinO2anox) * sdiv(p.kinNO3anox, NO3 + p.kinNO3anox);
+  const real Cmin = sdiv(lim * Cprod, oxlim + dnlim + anlim);
+  const real OxicMin = Cmin * oxlim;
+  const real Denit = Cmin * dnlim;
+  const real AnoxicMin = Cmin * anlim;
+  const real Nitri = p.rnit * NH4 * sdiv(O2, O2 + p.ksO2nitri);
+  const real OduOx = p.rodu * ODU * sdiv(O2, O2 + p.ksO2oduox);
+  const real Rads = sdiv(p.pads * (p.PAdsODU * PO4 - ODU * adsP), p.PAdsODU + ODU);
+  const real NprodF = p.rF * fdetN;
+  const real NprodS = p.rS * sdetN;
+  const real Pprod = p.rF * fdetP;
+  r[T_FDETC] = -(lim * CprodF);
+  r[T_SDETC] = -(lim * CprodS);
+  r[T_FDETN] = -(lim * NprodF);
+  r[T_SDETN] = -(lim * NprodS);
+  r[T_FDETP] = -(lim * Pprod);
+  r[T_ADSP] = Rads;
+  r[T_O2] = -OxicMin - real(2) * Nitri - OduOx;
+  r[T_NO3] = Nitri - real(0.8) * Denit;
+  r[T_NH4] = (lim * (NprodF + NprodS) - Nitri) * p.nh3fac;
+  r[T_ODU] = AnoxicMin - OduOx;
+  r[T_PO4] = lim * Pprod - Rads;
+  denit = Denit;
+}
+
+// ---------------------------------------------------------------------------
+// Neighbour exchange along the column.  Layer L = s*32 + lane.
+template <typename real, int LPL>
+__device__ __forceinline__ void from_above(const real (&v)[LPL], real (&out)[LPL],
+                                           int lane) {
+#pragma unroll
+  for (int s = 0; s < LPL; s++) out[s] = __shfl_up_sync(FULL, v[s], 1);
+  if (LPL > 1) {
+#pragma unroll
+    for (int s = 1; s < LPL; s++) {
+      real t = __shfl_sync(FULL, v[s - 1], 31);
+      if (lane == 0) out[s] = t;
+    }
+  }
+}
+
+template <typename real, int LPL>
+__device__ __forceinline__ void from_below(const real (&v)[LPL], real (&out)[LPL],
+                                           int lane) {
+#pragma unroll
+  for (int s = 0; s < LPL; s++) out[s] = __shfl_down_sync(FULL, v[s], 1);
+  if (LPL > 1) {
+#pragma unroll
+    for (int s = 0; s + 1 < LPL; s++) {
+      real t = __shfl_sync(FULL, v[s + 1], 0);
+      if (lane == 31) out[s] = t;
+    }
+  }
+}
+
+// Per-lane coefficients of one column for one coupling step.
+template <typename real, int LPL, bool BC4>
+struct Lane {
+  real phi[LPL];   // porosity at the layer centre
+  real ivol[LPL];  // 1 / (phi dz)
+  real ad[LPL];    // dissolved interface conductance D/len (upper interface)
+  real ap[LPL];    // particulate interface conductance
+  real vol[LPL];   // phi dz (budgets)
+  real bnd[NTR];   // per tracer: bottom-water value or downward surface flux
+  real src[BC4 ? LPL : 1][BC4 ? NPART : 1];  // capped-flux cascade sources
+};
+
+// Right-hand side of one column: OMEXDIA+P rates plus diff3d transport.
+// ftop receives the flux through the sediment surface (lane 0 only).
+template <typename real, int LPL, bool BC4>
+__device__ __forceinline__ void column_rhs(const Params<real>& p,
+                                           const Lane<real, LPL, BC4>& lc,
+                                           int lane, int K,
+                                           const real (&C)[LPL][NTR],
+                                           real (&R)[LPL][NTR],
+                                           real (&ftop)[NTR],
+                                           real (&dn)[LPL]) {
+#pragma unroll
+  for (int s = 0; s < LPL; s++) omexdia_p<real>(p, C[s], R[s], dn[s]);
+#pragma unroll
+  for (int n = 0; n < NTR; n++) {
+    const bool part = n < NPART;
+    real v[LPL], vm[LPL], F[LPL], Fb[LPL];
+#pragma unroll
+    for (int s = 0; s < LPL; s++) v[s] = part ? lc.phi[s] * C[s][n] : C[s][n];
+    from_above<real, LPL>(v, vm, lane);
+#pragma unroll
+    for (int s = 0; s < LPL; s++) F[s] = (part ? lc.ap[s] : lc.ad[s]) * (vm[s] - v[s]);
+    if (lane == 0) {
+      real f0;
+      if (part) f0 = lc.bnd[n];
+      else if (p.bcup_d == 2) f0 = lc.ad[0] * (lc.bnd[n] - v[0]);
+      else if (p.bcup_d == 1) f0 = lc.bnd[n];
+      else f0 = real(0);
+      F[0] = f0;
+      ftop[n] = f0;
+    }
+    from_below<real, LPL>(F, Fb, lane);
+#pragma unroll
+    for (int s = 0; s < LPL; s++) {
+      const int L = s * 32 + lane;
+      const real below = (L >= K - 1) ? real(0) : Fb[s];
+      real t = (F[s] - below) * lc.ivol[s];
+      if (BC4 && part) t += lc.src[s][n];
+      R[s][n] = (L < K) ? R[s][n] + t : real(0);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 warp sum (budgets)
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
+
+template <typename real>
+__device__ __forceinline__ real warp_incl_scan(real v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    real t = __shfl_up_sync(FULL, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+
+// Sources of the BcUp=4 capped-flux cascade (diff3d :791-802): the surface
+// flux beyond each layer's cap is passed down, and what reaches the bottom
+// is added to the last interior interface.  The cascade is constant during
+// a coupling step, so it enters as a fixed source per layer.
+template <typename real, int LPL, bool BC4>
+__device__ __forceinline__ void cascade_sources(Lane<real, LPL, BC4>& lc,
+                                                const real (&cap)[LPL],
+                                                int lane, int K) {
+  if (!BC4) return;
+  // inclusive prefix of caps over layers
+  real pre[LPL];
+  real carry = real(0);
+#pragma unroll
+  for (int s = 0; s < LPL; s++) {
+    pre[s] = warp_incl_scan<real>(cap[s], lane) + carry;
+    carry = __shfl_sync(FULL, pre[s], 31);
+  }
+#pragma unroll
+  for (int n = 0; n < NPART; n++) {
+    const real fup = lc.bnd[n];
+    real rest[LPL];  // rest after layer L: fup - sum_{j<=L} cap_j
+#pragma unroll
+    for (int s = 0; s < LPL; s++) rest[s] = fup - pre[s];
+    real ra[LPL];    // rest after the layer above (rest_{L-1})
+    from_above<real, LPL>(rest, ra, lane);
+    real extra[LPL];
+#pragma unroll
+    for (int s = 0; s < LPL; s++) {
+      const int L = s * 32 + lane;
+      real e = real(0);
+      if (L >= 1 && L <= K - 1 && ra[s] > real(0)) e = ra[s];
+      extra[s] = e;
+    }
+    // what is left after the last layer goes to interface K-1
+#pragma unroll
+    for (int s = 0; s < LPL; s++) {
+      const int L = s * 32 + lane;
+      if (L == K - 1) {
+        if (K == 1) extra[s] += rest[s];
+        else if (ra[s] > real(0)) extra[s] += rest[s];
+      }
+    }
+    real eb[LPL];
+    from_below<real, LPL>(extra, eb, lane);
+#pragma unroll
+    for (int s = 0; s < LPL; s++) {
+      const int L = s * 32 + lane;
+      const real below = (L >= K - 1) ? real(0) : eb[s];
+      lc.src[s][n] = (L < K) ? (extra[s] - below) * lc.ivol[s] : real(0);
+    }
+  }
+}
+
+}  // namespace sed

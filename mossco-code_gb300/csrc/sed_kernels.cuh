@@ -1,0 +1,862 @@
+// sed_kernels.cuh -- sm_103a kernels of the sediment-column solver
+// (templates; sed_kernels_f32.cu and sed_kernels_f64.cu instantiate them).
+//
+// k_column_step: persistent kernel, one coupling step for every column.
+//   Blocks pull tiles of TC consecutive column slots from a device work
+//   counter (atomicAdd, no waits), stage the tile's state, coefficients and
+//   forcing into shared memory with coalesced 16-byte loads, then each warp
+//   pulls columns of the tile (shared-memory counter) and integrates one
+//   column entirely in registers: per-column adaptive Euler (or Euler / RK4
+//   / RK4 3/8), FP64 step bookkeeping, fused NaN check + clamp, FP64
+//   budgets.  The tile is written back with coalesced stores.
+// k_column_rhs:   the same staging, one right-hand side (get_rhs mirror and
+//                 the grid-wide adaptive mode).
+// k_trial / k_accept / k_epilogue: elementwise steps of the grid-wide cut.
+// k_gather_* / k_scatter_* / k_prep_*: layout and precision conversion
+//   between the reference's FP64 host arrays and the device layout.
+#pragma once
+#include "sed_device.cuh"
+#include "sed_launch.h"
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace sed {
+
+// ---------------------------------------------------------------------------
+// shared-memory tile layout
+template <typename real>
+struct TileLayout {
+  int tcp, kt;
+  size_t conc, coef, cap, force, sflux, bud, nsub, total;
+  __host__ __device__ TileLayout(int tc, int kt_, bool bc4) : kt(kt_) {
+    tcp = tc + 16 / (int)sizeof(real);  // row pad keeps 16-byte alignment
+    size_t r = sizeof(real);
+    conc = 0;
+    coef = conc + (size_t)NTR * kt * tcp * r;
+    cap = coef + (size_t)NCOEF * kt * tcp * r;
+    force = cap + (bc4 ? (size_t)kt * tcp * r : 0);
+    sflux = force + (size_t)NFORCE * tcp * r;
+    bud = sflux + (size_t)NDISS * tcp * r;
+    bud = (bud + 15) & ~(size_t)15;
+    nsub = bud + (size_t)4 * tc * sizeof(double);
+    total = nsub + (size_t)tc * sizeof(int);
+    total = (total + 15) & ~(size_t)15;
+  }
+};
+
+template <typename real>
+size_t tile_smem_bytes(int tc, int lpl, bool bc4) {
+  return TileLayout<real>(tc, 32 * lpl, bc4).total;
+}
+
+// Copy `rows` rows of tc reals between global (row stride gstride, first
+// element at gbase + row_index*gstride) and shared memory (row stride tcp).
+template <typename real, bool TO_SHARED>
+__device__ __forceinline__ void copy_rows(real* sm, real* gbase, size_t gstride,
+                                          int rows, int tc, int tcp,
+                                          int row_step_global, int tid,
+                                          int nthreads) {
+  constexpr int EPV = 16 / sizeof(real);  // elements per 16-byte vector
+  const int vpr = tc / EPV;
+  const int total = rows * vpr;
+  for (int i = tid; i < total; i += nthreads) {
+    const int row = i / vpr;
+    const int v = i - row * vpr;
+    real* g = gbase + (size_t)row * row_step_global * gstride + v * EPV;
+    real* s = sm + (size_t)row * tcp + v * EPV;
+    if (TO_SHARED)
+      *reinterpret_cast<uint4*>(s) = *reinterpret_cast<const uint4*>(g);
+    else
+      *reinterpret_cast<uint4*>(g) = *reinterpret_cast<const uint4*>(s);
+  }
+}
+
+// rows of a [nrow_groups][kmax][nslot] array restricted to k < kt:
+// copies group g, layer k for all g < ngroups, k < kt.
+template <typename real, bool TO_SHARED>
+__device__ __forceinline__ void copy_grouped(real* sm, real* g0, int ngroups,
+                                             int kt, int KT, int kmax,
+                                             size_t nslot, int tc, int tcp,
+                                             int tid, int nthreads) {
+  constexpr int EPV = 16 / sizeof(real);
+  const int vpr = tc / EPV;
+  const int total = ngroups * kt * vpr;
+  for (int i = tid; i < total; i += nthreads) {
+    const int row = i / vpr;
+    const int v = i - row * vpr;
+    const int g = row / kt;
+    const int k = row - g * kt;
+    real* gp = g0 + ((size_t)g * kmax + k) * nslot + v * EPV;
+    real* sp = sm + ((size_t)g * KT + k) * tcp + v * EPV;
+    if (TO_SHARED)
+      *reinterpret_cast<uint4*>(sp) = *reinterpret_cast<const uint4*>(gp);
+    else
+      *reinterpret_cast<uint4*>(gp) = *reinterpret_cast<const uint4*>(sp);
+  }
+}
+
+// ---------------------------------------------------------------------------
+template <typename real, int LPL, bool BC4>
+__device__ __forceinline__ void load_lane(Lane<real, LPL, BC4>& lc,
+                                          real (&C)[LPL][NTR],
+                                          const real* s_conc,
+                                          const real* s_coef,
+                                          const real* s_cap,
+                                          const real* s_force, int j, int KT,
+                                          int tcp, int lane, int K) {
+  const real bioT = s_force[0 * tcp + j];
+  const real dmul = s_force[1 * tcp + j];
+#pragma unroll
+  for (int n = 0; n < NTR; n++) lc.bnd[n] = s_force[(2 + n) * tcp + j];
+  real cap[LPL];
+#pragma unroll
+  for (int s = 0; s < LPL; s++) {
+    const int L = s * 32 + lane;
+    const bool act = L < K;
+    const int Lc = act ? L : 0;
+    const real phi = s_coef[(0 * KT + Lc) * tcp + j];
+    const real vol = s_coef[(1 * KT + Lc) * tcp + j];
+    const real gb = s_coef[(2 * KT + Lc) * tcp + j];
+    const real gm = s_coef[(3 * KT + Lc) * tcp + j];
+    lc.phi[s] = act ? phi : real(0);
+    lc.vol[s] = act ? vol : real(0);
+    lc.ivol[s] = act ? real(1) / vol : real(0);
+    lc.ap[s] = act ? bioT * gb : real(0);
+    lc.ad[s] = act ? bioT * gb + dmul * gm : real(0);
+    cap[s] = (BC4 && act) ? s_cap[Lc * tcp + j] : real(0);
+#pragma unroll
+    for (int n = 0; n < NTR; n++)
+      C[s][n] = act ? s_conc[(n * KT + Lc) * tcp + j] : real(0);
+  }
+  cascade_sources<real, LPL, BC4>(lc, cap, lane, K);
+}
+
+// FP64 column inventories of the P and N pools (warp-reduced).
+template <typename real, int LPL, bool BC4>
+__device__ __forceinline__ void inventories(const Lane<real, LPL, BC4>& lc,
+                                            const real (&C)[LPL][NTR],
+                                            double& invP, double& invN) {
+  double p = 0.0, nn = 0.0;
+#pragma unroll
+  for (int s = 0; s < LPL; s++) {
+    const double v = (double)lc.vol[s];
+    p += v * ((double)C[s][T_FDETP] + (double)C[s][T_ADSP] + (double)C[s][T_PO4]);
+    nn += v * ((double)C[s][T_FDETN] + (double)C[s][T_SDETN] +
+               (double)C[s][T_NO3] + (double)C[s][T_NH4]);
+  }
+  invP = warp_sum(p);
+  invN = warp_sum(nn);
+}
+
+struct ColResult {
+  int attempts;
+  int accepted;
+  int capped;
+  int nan;
+  double min_dt;
+};
+
+// Budget bookkeeping of one column over one coupling step.
+template <typename real, int LPL, bool BC4>
+struct Budget {
+  double inP, inN, inv0P, inv0N;
+  real n2[LPL];
+  __device__ __forceinline__ void start(const Params<real>& p,
+                                        const Lane<real, LPL, BC4>& lc,
+                                        const real (&C)[LPL][NTR]) {
+    inP = 0.0; inN = 0.0; inv0P = 0.0; inv0N = 0.0;
+#pragma unroll
+    for (int s = 0; s < LPL; s++) n2[s] = real(0);
+    if (p.budgets) inventories<real, LPL, BC4>(lc, C, inv0P, inv0N);
+  }
+  // one right-hand side entering the update with weight w (seconds)
+  __device__ __forceinline__ void account(const Params<real>& p, double w,
+                                          const real (&ftop)[NTR],
+                                          const real (&dn)[LPL]) {
+    if (!p.budgets) return;
+    inP += w * ((double)ftop[T_FDETP] + (double)ftop[T_ADSP] + (double)ftop[T_PO4]);
+    inN += w * ((double)ftop[T_FDETN] + (double)ftop[T_SDETN] +
+                (double)ftop[T_NO3] + (double)ftop[T_NH4]);
+    const real wr = (real)w;
+#pragma unroll
+    for (int s = 0; s < LPL; s++) n2[s] += wr * real(0.8) * dn[s];
+  }
+  __device__ __forceinline__ void finish(const Params<real>& p,
+                                         const Lane<real, LPL, BC4>& lc,
+                                         const real (&C)[LPL][NTR],
+                                         double (&bud)[4]) {
+    if (!p.budgets) return;
+    double inv1P, inv1N;
+    inventories<real, LPL, BC4>(lc, C, inv1P, inv1N);
+    double loss = 0.0;
+#pragma unroll
+    for (int s = 0; s < LPL; s++) loss += (double)lc.vol[s] * (double)n2[s];
+    loss = warp_sum(loss);
+    const double fP = __shfl_sync(FULL, inP, 0);
+    const double fN = __shfl_sync(FULL, inN, 0);
+    bud[0] = inv1P;
+    bud[1] = inv1P - inv0P - fP;
+    bud[2] = inv1N;
+    bud[3] = inv1N - inv0N - fN + loss;
+  }
+};
+
+// Component epilogue: NaN check (:1718-1723) and clamp (:1726-1732).
+template <typename real, int LPL>
+__device__ __forceinline__ int epilogue(const Params<real>& p, int lane, int K,
+                                        real (&C)[LPL][NTR]) {
+  if (!p.epilogue) return 0;
+  int nan = 0;
+#pragma unroll
+  for (int s = 0; s < LPL; s++) {
+    const bool act = s * 32 + lane < K;
+#pragma unroll
+    for (int n = 0; n < NTR; n++) {
+      const real v = C[s][n];
+      if (act && v != v) nan++;
+      else if (act && v < p.minimum[n]) C[s][n] = p.minimum[n];
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nan += __shfl_xor_sync(FULL, nan, o);
+  return nan;
+}
+
+// ADAPTIVE_EULER (solver_library.F90:104-140) on one column, cut decided by
+// the column's own cells.  A rejected attempt re-evaluates get_rhs at the
+// same state in the reference, which yields the same rhs, so it is reused.
+template <typename real, int LPL, bool BC4>
+__device__ __forceinline__ ColResult solve_adaptive(
+    const Params<real>& p, const Lane<real, LPL, BC4>& lc, int lane, int K,
+    real (&C)[LPL][NTR], real (&ftop)[NTR], double dt, double (&bud)[4]) {
+  real R[LPL][NTR];
+  real dn[LPL];
+  ColResult res{0, 0, 0, 0, 1e300};
+  Budget<real, LPL, BC4> B;
+  B.start(p, lc, C);
+  double dt_int = 0.0, dt_red = dt;
+  column_rhs<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+  while (dt_int < dt) {
+    if (res.attempts >= p.max_attempts) { res.capped = 1; break; }
+    res.attempts++;
+    const real dtr = (real)dt_red;
+    bool bad = false;
+#pragma unroll
+    for (int s = 0; s < LPL; s++) {
+      const bool act = s * 32 + lane < K;
+#pragma unroll
+      for (int n = 0; n < NTR; n++) {
+        const real c1 = fma(dtr, R[s][n], C[s][n]);
+        // sign of c1 - (1+rcm) c, exact for the operands (one rounding)
+        bad |= act && (fma(-p.keep, C[s][n], c1) < real(0));
+      }
+    }
+    const bool reject = __any_sync(FULL, bad);
+    if (reject && dt_red > p.dt_min) {
+      dt_red = dt_red * 0.25;
+    } else {
+      B.account(p, dt_red, ftop, dn);
+#pragma unroll
+      for (int s = 0; s < LPL; s++)
+#pragma unroll
+        for (int n = 0; n < NTR; n++) C[s][n] = fma(dtr, R[s][n], C[s][n]);
+      dt_int = dt_int + dt_red;
+      res.accepted++;
+      if (dt_red < res.min_dt) res.min_dt = dt_red;
+      if (dt_int < dt) column_rhs<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+    }
+  }
+  B.finish(p, lc, C, bud);
+  res.nan = epilogue<real, LPL>(p, lane, K, C);
+  return res;
+}
+
+// EULER (:99-102), RUNGE_KUTTA_4 (:142-163), RUNGE_KUTTA_4_38 (:164-185).
+template <typename real, int LPL, bool BC4>
+__device__ __forceinline__ ColResult solve_fixed(
+    const Params<real>& p, const Lane<real, LPL, BC4>& lc, int lane, int K,
+    real (&C)[LPL][NTR], real (&ftop)[NTR], double dt, int method,
+    double (&bud)[4]) {
+  real R[LPL][NTR];
+  real dn[LPL];
+  ColResult res{1, 1, 0, 0, dt};
+  Budget<real, LPL, BC4> B;
+  B.start(p, lc, C);
+  const real dtr = (real)dt;
+  if (method == 0) {
+    column_rhs<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+    B.account(p, dt, ftop, dn);
+#pragma unroll
+    for (int s = 0; s < LPL; s++)
+#pragma unroll
+      for (int n = 0; n < NTR; n++) C[s][n] = fma(dtr, R[s][n], C[s][n]);
+  } else {
+    const bool rk38 = method == 3;
+    const real third = real(1) / real(3);
+    real Cs[LPL][NTR], acc[LPL][NTR], R0[LPL][NTR];
+    // stage 1: rhs0 at conc
+    column_rhs<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+    B.account(p, rk38 ? dt / 8.0 : dt / 6.0, ftop, dn);
+#pragma unroll
+    for (int s = 0; s < LPL; s++)
+#pragma unroll
+      for (int n = 0; n < NTR; n++) {
+        R0[s][n] = R[s][n];
+        acc[s][n] = rk38 ? R[s][n] : real(0.5) * R[s][n];
+        Cs[s][n] = rk38 ? C[s][n] + third * dtr * R[s][n]
+                        : C[s][n] + real(0.5) * dtr * R[s][n];
+      }
+    // stage 2: rhs1 at c1
+    column_rhs<real, LPL, BC4>(p, lc, lane, K, Cs, R, ftop, dn);
+    B.account(p, rk38 ? 3.0 * dt / 8.0 : dt / 3.0, ftop, dn);
+#pragma unroll
+    for (int s = 0; s < LPL; s++)
+#pragma unroll
+      for (int n = 0; n < NTR; n++) {
+        acc[s][n] += rk38 ? real(3) * R[s][n] : R[s][n];
+        Cs[s][n] = rk38 ? C[s][n] + dtr * (R[s][n] - third * R0[s][n])
+                        : C[s][n] + real(0.5) * dtr * R[s][n];
+        R0[s][n] = R0[s][n] - R[s][n];  // rhs0 - rhs1 (3/8 rule, stage 3)
+      }
+    // stage 3: rhs2
+    column_rhs<real, LPL, BC4>(p, lc, lane, K, Cs, R, ftop, dn);
+    B.account(p, rk38 ? 3.0 * dt / 8.0 : dt / 3.0, ftop, dn);
+#pragma unroll
+    for (int s = 0; s < LPL; s++)
+#pragma unroll
+      for (int n = 0; n < NTR; n++) {
+        acc[s][n] += rk38 ? real(3) * R[s][n] : R[s][n];
+        Cs[s][n] = rk38 ? C[s][n] + dtr * (R0[s][n] + R[s][n])
+                        : C[s][n] + dtr * R[s][n];
+      }
+    // stage 4: rhs3 and the combination
+    column_rhs<real, LPL, BC4>(p, lc, lane, K, Cs, R, ftop, dn);
+    B.account(p, rk38 ? dt / 8.0 : dt / 6.0, ftop, dn);
+#pragma unroll
+    for (int s = 0; s < LPL; s++)
+#pragma unroll
+      for (int n = 0; n < NTR; n++) {
+        if (rk38)
+          C[s][n] = C[s][n] + dtr * real(1) / real(8) * (acc[s][n] + R[s][n]);
+        else
+          C[s][n] = C[s][n] + dtr * third * (acc[s][n] + real(0.5) * R[s][n]);
+      }
+  }
+  B.finish(p, lc, C, bud);
+  res.nan = epilogue<real, LPL>(p, lane, K, C);
+  return res;
+}
+
+// ---------------------------------------------------------------------------
+// KIND_ADAPT / KIND_FIXED: one coupling step; KIND_RHS: one right-hand side
+// written to a.out.
+template <typename real, int LPL, bool BC4, int KIND>
+__global__ void __launch_bounds__(256)
+k_column(ColumnArgs<real> a, Params<real> p) {
+  constexpr int mode = KIND == KIND_RHS ? 1 : 0;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tc = a.tc;
+  constexpr int KT = 32 * LPL;
+  TileLayout<real> L(tc, KT, BC4);
+  const int tcp = L.tcp;
+  real* s_conc = reinterpret_cast<real*>(smem + L.conc);
+  real* s_coef = reinterpret_cast<real*>(smem + L.coef);
+  real* s_cap = reinterpret_cast<real*>(smem + L.cap);
+  real* s_force = reinterpret_cast<real*>(smem + L.force);
+  real* s_sflux = reinterpret_cast<real*>(smem + L.sflux);
+  double* s_bud = reinterpret_cast<double*>(smem + L.bud);
+  int* s_nsub = reinterpret_cast<int*>(smem + L.nsub);
+  __shared__ int s_tile, s_next;
+  __shared__ unsigned long long b_att, b_acc, b_cols, b_mindt;
+  __shared__ int b_maxatt, b_cap, b_nan;
+
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int lane = tid & 31;
+  if (tid == 0) {
+    b_att = 0; b_acc = 0; b_cols = 0; b_mindt = 0x7FF0000000000000ull;
+    b_maxatt = 0; b_cap = 0; b_nan = 0;
+  }
+  const size_t ns = (size_t)a.nslot;
+
+  for (;;) {
+    if (tid == 0) { s_tile = (int)atomicAdd(a.queue, 1u); s_next = 0; }
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= a.ntiles) break;
+    const int t = a.tile0 + tile;
+    const int slot0 = t * tc;
+    const int kt = a.tile_k[t];
+    // stage in
+    copy_grouped<real, true>(s_conc, a.conc + slot0, NTR, kt, KT, a.kmax, ns,
+                             tc, tcp, tid, nthr);
+    copy_grouped<real, true>(s_coef, const_cast<real*>(a.coef) + slot0, NCOEF,
+                             kt, KT, a.kmax, ns, tc, tcp, tid, nthr);
+    if (BC4)
+      copy_grouped<real, true>(s_cap, const_cast<real*>(a.cap) + slot0, 1, kt,
+                               KT, a.kmax, ns, tc, tcp, tid, nthr);
+    copy_rows<real, true>(s_force, const_cast<real*>(a.force) + slot0, ns,
+                          NFORCE, tc, tcp, 1, tid, nthr);
+    __syncthreads();
+
+    for (;;) {
+      int j = 0;
+      if (lane == 0) j = atomicAdd(&s_next, 1);
+      j = __shfl_sync(FULL, j, 0);
+      if (j >= tc) break;
+      const int K = a.kact[slot0 + j];
+      if (K <= 0) {
+        if (lane == 0) {
+          s_nsub[j] = 0;
+#pragma unroll
+          for (int d = 0; d < NDISS; d++) s_sflux[d * tcp + j] = real(0);
+          for (int b = 0; b < 4; b++) s_bud[b * tc + j] = 0.0;
+        }
+        continue;
+      }
+      Lane<real, LPL, BC4> lc;
+      real C[LPL][NTR];
+      load_lane<real, LPL, BC4>(lc, C, s_conc, s_coef, s_cap, s_force, j, KT,
+                                tcp, lane, K);
+      real ftop[NTR];
+#pragma unroll
+      for (int n = 0; n < NTR; n++) ftop[n] = real(0);
+      if (KIND == KIND_RHS) {
+        real R[LPL][NTR];
+        real dn[LPL];
+        column_rhs<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+#pragma unroll
+        for (int s = 0; s < LPL; s++) {
+          const int Ll = s * 32 + lane;
+          if (Ll < K)
+#pragma unroll
+            for (int n = 0; n < NTR; n++) s_conc[(n * KT + Ll) * tcp + j] = R[s][n];
+        }
+        if (lane == 0) {
+#pragma unroll
+          for (int d = 0; d < NDISS; d++) s_sflux[d * tcp + j] = ftop[NPART + d];
+          s_nsub[j] = 1;
+        }
+        continue;
+      }
+      double bud[4] = {0.0, 0.0, 0.0, 0.0};
+      ColResult r;
+      if (KIND == KIND_ADAPT)
+        r = solve_adaptive<real, LPL, BC4>(p, lc, lane, K, C, ftop, a.dt, bud);
+      else
+        r = solve_fixed<real, LPL, BC4>(p, lc, lane, K, C, ftop, a.dt, a.method,
+                                        bud);
+#pragma unroll
+      for (int s = 0; s < LPL; s++) {
+        const int Ll = s * 32 + lane;
+        if (Ll < K)
+#pragma unroll
+          for (int n = 0; n < NTR; n++) s_conc[(n * KT + Ll) * tcp + j] = C[s][n];
+      }
+      if (lane == 0) {
+#pragma unroll
+        for (int d = 0; d < NDISS; d++) s_sflux[d * tcp + j] = ftop[NPART + d];
+        for (int b = 0; b < 4; b++) s_bud[b * tc + j] = bud[b];
+        s_nsub[j] = r.attempts;
+        atomicAdd(&b_att, (unsigned long long)r.attempts);
+        atomicAdd(&b_acc, (unsigned long long)r.accepted);
+        atomicAdd(&b_cols, 1ull);
+        atomicMax(&b_maxatt, r.attempts);
+        if (r.capped) atomicAdd(&b_cap, 1);
+        if (r.nan) atomicAdd(&b_nan, r.nan);
+        if (r.accepted > 0)
+          atomicMin(&b_mindt, (unsigned long long)__double_as_longlong(r.min_dt));
+      }
+    }
+    __syncthreads();
+    // stage out
+    real* dst = (mode == 1) ? a.out : a.conc;
+    copy_grouped<real, false>(s_conc, dst + slot0, NTR, kt, KT, a.kmax, ns, tc,
+                              tcp, tid, nthr);
+    copy_rows<real, false>(s_sflux, a.sflux + slot0, ns, NDISS, tc, tcp, 1,
+                           tid, nthr);
+    for (int i = tid; i < tc; i += nthr) {
+      a.nsub[slot0 + i] = s_nsub[i];
+      if (a.budget)
+        for (int b = 0; b < 4; b++) a.budget[(size_t)b * ns + slot0 + i] = s_bud[b * tc + i];
+    }
+  }
+  __syncthreads();
+  if (tid == 0 && mode == 0) {
+    atomicAdd(&a.stats->attempts, b_att);
+    atomicAdd(&a.stats->accepted, b_acc);
+    atomicAdd(&a.stats->column_steps, b_cols);
+    atomicMin(&a.stats->min_dt_bits, b_mindt);
+    atomicMax(&a.stats->max_col_attempts, b_maxatt);
+    if (b_cap) { atomicAdd(&a.stats->capped, b_cap); atomicOr(&a.stats->status, ST_CAP); }
+    if (b_nan) { atomicAdd(&a.stats->nan_cells, b_nan); atomicOr(&a.stats->status, ST_NAN); }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Grid-wide adaptive cut (the reference's any() over the whole local grid).
+template <typename real>
+__global__ void k_trial(const real* __restrict__ conc, const real* __restrict__ rhs,
+                        const int* __restrict__ kact, int nslot, int kmax,
+                        real dtr, real keep, int* flag) {
+  const size_t total = (size_t)NTR * kmax * nslot;
+  bool bad = false;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int slot = (int)(i % nslot);
+    const int k = (int)((i / nslot) % kmax);
+    if (k >= kact[slot]) continue;
+    const real c = conc[i];
+    const real c1 = fma(dtr, rhs[i], c);
+    bad |= fma(-keep, c, c1) < real(0);
+  }
+  if (__any_sync(FULL, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+template <typename real>
+__global__ void k_accept(real* __restrict__ conc, const real* __restrict__ rhs,
+                         const int* __restrict__ kact, int nslot, int kmax,
+                         real dtr) {
+  const size_t total = (size_t)NTR * kmax * nslot;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int slot = (int)(i % nslot);
+    const int k = (int)((i / nslot) % kmax);
+    if (k >= kact[slot]) continue;
+    conc[i] = fma(dtr, rhs[i], conc[i]);
+  }
+}
+
+template <typename real>
+__global__ void k_epilogue(real* __restrict__ conc, const int* __restrict__ kact,
+                           int nslot, int kmax, Params<real> p, DevStats* st) {
+  const size_t total = (size_t)NTR * kmax * nslot;
+  int nan = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int slot = (int)(i % nslot);
+    const int k = (int)((i / nslot) % kmax);
+    const int n = (int)(i / ((size_t)nslot * kmax));
+    if (k >= kact[slot]) continue;
+    const real v = conc[i];
+    if (v != v) nan++;
+    else if (v < p.minimum[n]) conc[i] = p.minimum[n];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nan += __shfl_xor_sync(FULL, nan, o);
+  if ((threadIdx.x & 31) == 0 && nan) {
+    atomicAdd(&st->nan_cells, nan);
+    atomicOr(&st->status, ST_NAN);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Layout / precision conversion.  host layout [g][kmax][ncol] (FP64),
+// device layout [g][kmax][nslot] (real), slot_col maps slot -> column (-1 pad)
+template <typename real>
+__global__ void k_gather(const double* __restrict__ src, real* __restrict__ dst,
+                         const int* __restrict__ slot_col, int ngroups, int kmax,
+                         int ncol, int nslot) {
+  const size_t total = (size_t)ngroups * kmax * nslot;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int slot = (int)(i % nslot);
+    const size_t gk = i / nslot;
+    const int col = slot_col[slot];
+    dst[i] = col >= 0 ? (real)src[gk * ncol + col] : real(0);
+  }
+}
+
+template <typename real>
+__global__ void k_scatter(const real* __restrict__ src, double* __restrict__ dst,
+                          const int* __restrict__ slot_col,
+                          const int* __restrict__ kact, int ngroups, int kmax,
+                          int ncol, int nslot) {
+  const size_t total = (size_t)ngroups * kmax * nslot;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int slot = (int)(i % nslot);
+    const size_t gk = i / nslot;
+    const int k = (int)(gk % kmax);
+    const int col = slot_col[slot];
+    if (col >= 0 && k < kact[slot]) dst[gk * ncol + col] = (double)src[i];
+  }
+}
+
+// dissolved surface fluxes [NDISS][nslot] -> rows NPART.. of fluxes[NTR][ncol]
+template <typename real>
+__global__ void k_scatter_flux(const real* __restrict__ sflux,
+                               double* __restrict__ fluxes,
+                               const int* __restrict__ slot_col,
+                               const int* __restrict__ kact, int ncol,
+                               int nslot) {
+  const size_t total = (size_t)NDISS * nslot;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int slot = (int)(i % nslot);
+    const int d = (int)(i / nslot);
+    const int col = slot_col[slot];
+    if (col >= 0 && kact[slot] > 0)
+      fluxes[(size_t)(NPART + d) * ncol + col] = (double)sflux[i];
+  }
+}
+
+// Per-layer coefficients of the transport, from the reference's arrays:
+//   phi, vol = phi dz, gb = (1-phi_i) biofac / len / 8.64e8,
+//   gm = phi_i / len / 8.64e8 (mode 0) or d0 phi_i / (1 - 2 ln phi_i) / len,
+// len = dz for the surface interface, dzc below (diff3d :777,786) and
+// 8.64e8 = 86400 s * 1e4 cm2/m2 (get_rhs :652,683).
+template <typename real>
+__global__ void k_prep_grid(const double* __restrict__ dz,
+                            const double* __restrict__ dzc,
+                            const double* __restrict__ phi,
+                            const double* __restrict__ phi_i,
+                            const double* __restrict__ biofac,
+                            const double* __restrict__ cap,
+                            const int* __restrict__ slot_col,
+                            real* __restrict__ coef, real* __restrict__ capd,
+                            int kmax, int ncol, int nslot, int mode, double d0) {
+  const size_t total = (size_t)kmax * nslot;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int slot = (int)(i % nslot);
+    const int k = (int)(i / nslot);
+    const int col = slot_col[slot];
+    double v_phi = 1.0, v_vol = 1.0, v_gb = 0.0, v_gm = 0.0, v_cap = 0.0;
+    if (col >= 0) {
+      const size_t c = (size_t)k * ncol + col;
+      const double ph = phi[c], pi = phi_i[c];
+      const double len = (k == 0) ? dz[c] : dzc[(size_t)(k - 1) * ncol + col];
+      v_phi = ph;
+      v_vol = ph * dz[c];
+      v_gb = (1.0 - pi) * biofac[c] / len / 8.64e8;
+      if (mode == 1)
+        v_gm = d0 * pi / (1.0 - 2.0 * log(pi)) / len;
+      else
+        v_gm = pi / len / 8.64e8;
+      if (cap) v_cap = cap[c];
+    }
+    coef[(0 * (size_t)kmax + k) * nslot + slot] = (real)v_phi;
+    coef[(1 * (size_t)kmax + k) * nslot + slot] = (real)v_vol;
+    coef[(2 * (size_t)kmax + k) * nslot + slot] = (real)v_gb;
+    coef[(3 * (size_t)kmax + k) * nslot + slot] = (real)v_gm;
+    if (capd) capd[i] = (real)v_cap;
+  }
+}
+
+// Per-column forcing of one coupling step: bioturbation x f_T (get_rhs :648,
+// :652), the molecular multiplier, and the surface value of every tracer
+// (bottom-water concentration or downward flux, diff3d's Cup / fluxup).
+template <typename real>
+__global__ void k_prep_force(const double* __restrict__ bdys,
+                             const double* __restrict__ fluxes,
+                             const int* __restrict__ slot_col,
+                             real* __restrict__ force, int ncol, int nslot,
+                             double bio, double diffusivity, int mode,
+                             int bcup_d) {
+  for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < nslot;
+       slot += gridDim.x * blockDim.x) {
+    const int col = slot_col[slot];
+    double f[NFORCE];
+    for (int i = 0; i < NFORCE; i++) f[i] = 0.0;
+    if (col >= 0) {
+      const double T = bdys[col];
+      const double fT = 1.0 * exp(-4500.0 * (1.0 / (T + 273.0) - (1.0 / 288.0)));
+      f[0] = bio * fT;
+      f[1] = (mode == 1) ? 1.0 : (diffusivity + T * 0.035);
+      for (int n = 0; n < NTR; n++) {
+        const bool part = n < NPART;
+        const double fl = fluxes[(size_t)n * ncol + col];
+        const double cb = bdys[(size_t)(n + 1) * ncol + col];
+        f[2 + n] = part ? fl : (bcup_d == 1 ? fl : cb);
+      }
+    }
+    for (int i = 0; i < NFORCE; i++) force[(size_t)i * nslot + slot] = (real)f[i];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+static int grid_for(size_t total, int block, int sms) {
+  size_t g = (total + block - 1) / block;
+  size_t cap = (size_t)sms * 8;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+template <typename real, int LPL, bool BC4, int KIND>
+static cudaError_t launch_column_t(const ColumnArgs<real>& a, const Params<real>& p,
+                                   int blocks, int threads, cudaStream_t st) {
+  // the shared-memory limit was raised by column_blocks_per_sm at set-up, so
+  // this launch makes no attribute call and can be stream-captured
+  const size_t smem = tile_smem_bytes<real>(a.tc, LPL, BC4);
+  k_column<real, LPL, BC4, KIND><<<blocks, threads, smem, st>>>(a, p);
+  return cudaGetLastError();
+}
+
+template <typename real, int LPL, bool BC4>
+static cudaError_t launch_column_k(const ColumnArgs<real>& a, const Params<real>& p,
+                                   int kind, int blocks, int threads,
+                                   cudaStream_t st) {
+  if (kind == KIND_ADAPT)
+    return launch_column_t<real, LPL, BC4, KIND_ADAPT>(a, p, blocks, threads, st);
+  if (kind == KIND_FIXED)
+    return launch_column_t<real, LPL, BC4, KIND_FIXED>(a, p, blocks, threads, st);
+  return launch_column_t<real, LPL, BC4, KIND_RHS>(a, p, blocks, threads, st);
+}
+
+template <typename real>
+cudaError_t launch_column(const ColumnArgs<real>& a, const Params<real>& p,
+                          int lpl, bool bc4, int kind, int blocks, int threads,
+                          cudaStream_t st) {
+  if (lpl == 1)
+    return bc4 ? launch_column_k<real, 1, true>(a, p, kind, blocks, threads, st)
+               : launch_column_k<real, 1, false>(a, p, kind, blocks, threads, st);
+  return bc4 ? launch_column_k<real, 2, true>(a, p, kind, blocks, threads, st)
+             : launch_column_k<real, 2, false>(a, p, kind, blocks, threads, st);
+}
+
+template <typename real, int LPL, bool BC4, int KIND>
+static int occupancy_t(int tc, int threads) {
+  const size_t smem = tile_smem_bytes<real>(tc, LPL, BC4);
+  auto fn = k_column<real, LPL, BC4, KIND>;
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem) != cudaSuccess)
+    return 0;
+  return nb;
+}
+
+template <typename real, int LPL, bool BC4>
+static int occupancy_k(int tc, int kind, int threads) {
+  if (kind == KIND_ADAPT) return occupancy_t<real, LPL, BC4, KIND_ADAPT>(tc, threads);
+  if (kind == KIND_FIXED) return occupancy_t<real, LPL, BC4, KIND_FIXED>(tc, threads);
+  return occupancy_t<real, LPL, BC4, KIND_RHS>(tc, threads);
+}
+
+template <typename real>
+int column_blocks_per_sm(int tc, int lpl, bool bc4, int kind, int threads) {
+  if (lpl == 1)
+    return bc4 ? occupancy_k<real, 1, true>(tc, kind, threads)
+               : occupancy_k<real, 1, false>(tc, kind, threads);
+  return bc4 ? occupancy_k<real, 2, true>(tc, kind, threads)
+             : occupancy_k<real, 2, false>(tc, kind, threads);
+}
+
+template <typename real>
+cudaError_t launch_trial(const real* conc, const real* rhs, const int* kact,
+                         int nslot, int kmax, real dtr, real keep, int* flag,
+                         int sms, cudaStream_t st) {
+  const size_t total = (size_t)NTR * kmax * nslot;
+  k_trial<real><<<grid_for(total, 256, sms), 256, 0, st>>>(conc, rhs, kact, nslot,
+                                                          kmax, dtr, keep, flag);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_accept(real* conc, const real* rhs, const int* kact, int nslot,
+                          int kmax, real dtr, int sms, cudaStream_t st) {
+  const size_t total = (size_t)NTR * kmax * nslot;
+  k_accept<real><<<grid_for(total, 256, sms), 256, 0, st>>>(conc, rhs, kact, nslot,
+                                                           kmax, dtr);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_epilogue(real* conc, const int* kact, int nslot, int kmax,
+                            const Params<real>& p, DevStats* stats, int sms,
+                            cudaStream_t st) {
+  const size_t total = (size_t)NTR * kmax * nslot;
+  k_epilogue<real><<<grid_for(total, 256, sms), 256, 0, st>>>(conc, kact, nslot,
+                                                             kmax, p, stats);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_gather(const double* src, real* dst, const int* slot_col,
+                          int ngroups, int kmax, int ncol, int nslot, int sms,
+                          cudaStream_t st) {
+  const size_t total = (size_t)ngroups * kmax * nslot;
+  k_gather<real><<<grid_for(total, 256, sms), 256, 0, st>>>(src, dst, slot_col,
+                                                           ngroups, kmax, ncol, nslot);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_scatter(const real* src, double* dst, const int* slot_col,
+                           const int* kact, int ngroups, int kmax, int ncol,
+                           int nslot, int sms, cudaStream_t st) {
+  const size_t total = (size_t)ngroups * kmax * nslot;
+  k_scatter<real><<<grid_for(total, 256, sms), 256, 0, st>>>(
+      src, dst, slot_col, kact, ngroups, kmax, ncol, nslot);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_scatter_flux(const real* sflux, double* fluxes,
+                                const int* slot_col, const int* kact, int ncol,
+                                int nslot, int sms, cudaStream_t st) {
+  const size_t total = (size_t)NDISS * nslot;
+  k_scatter_flux<real><<<grid_for(total, 256, sms), 256, 0, st>>>(
+      sflux, fluxes, slot_col, kact, ncol, nslot);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_prep_grid(const double* dz, const double* dzc,
+                             const double* phi, const double* phi_i,
+                             const double* biofac, const double* cap,
+                             const int* slot_col, real* coef, real* capd,
+                             int kmax, int ncol, int nslot, int mode, double d0,
+                             int sms, cudaStream_t st) {
+  const size_t total = (size_t)kmax * nslot;
+  k_prep_grid<real><<<grid_for(total, 256, sms), 256, 0, st>>>(
+      dz, dzc, phi, phi_i, biofac, cap, slot_col, coef, capd, kmax, ncol,
+      nslot, mode, d0);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
+                              const int* slot_col, real* force, int ncol,
+                              int nslot, double bio, double diffusivity,
+                              int mode, int bcup_d, int sms, cudaStream_t st) {
+  k_prep_force<real><<<grid_for(nslot, 128, sms), 128, 0, st>>>(
+      bdys, fluxes, slot_col, force, ncol, nslot, bio, diffusivity, mode, bcup_d);
+  return cudaGetLastError();
+}
+
+#define SED_INSTANTIATE(real)                                                   \
+  template size_t tile_smem_bytes<real>(int, int, bool);                        \
+  template cudaError_t launch_column<real>(const ColumnArgs<real>&,             \
+                                           const Params<real>&, int, bool, int, \
+                                           int, int, cudaStream_t);             \
+  template int column_blocks_per_sm<real>(int, int, bool, int, int);            \
+  template cudaError_t launch_trial<real>(const real*, const real*, const int*, \
+                                          int, int, real, real, int*, int,      \
+                                          cudaStream_t);                        \
+  template cudaError_t launch_accept<real>(real*, const real*, const int*, int, \
+                                           int, real, int, cudaStream_t);       \
+  template cudaError_t launch_epilogue<real>(real*, const int*, int, int,       \
+                                             const Params<real>&, DevStats*,    \
+                                             int, cudaStream_t);                \
+  template cudaError_t launch_gather<real>(const double*, real*, const int*,    \
+                                           int, int, int, int, int,             \
+                                           cudaStream_t);                       \
+  template cudaError_t launch_scatter<real>(const real*, double*, const int*,   \
+                                            const int*, int, int, int, int,     \
+                                            int, cudaStream_t);                 \
+  template cudaError_t launch_scatter_flux<real>(const real*, double*,          \
+                                                 const int*, const int*, int,   \
+                                                 int, int, cudaStream_t);       \
+  template cudaError_t launch_prep_grid<real>(                                  \
+      const double*, const double*, const double*, const double*,               \
+      const double*, const double*, const int*, real*, real*, int, int, int,    \
+      int, double, int, cudaStream_t);                                          \
+  template cudaError_t launch_prep_force<real>(const double*, const double*,    \
+                                               const int*, real*, int, int,     \
+                                               double, double, int, int, int,   \
+                                               cudaStream_t);
+
+}  // namespace sed

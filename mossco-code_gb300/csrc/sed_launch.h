@@ -1,0 +1,91 @@
+// sed_launch.h -- host-visible kernel arguments and launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "sed_device.cuh"
+
+namespace sed {
+
+enum : int { KIND_ADAPT = 0, KIND_FIXED = 1, KIND_RHS = 2 };
+
+// Arguments of the tile kernel.  Device layouts (slot = compacted column):
+//   conc  [NTR][kmax][nslot]     coef  [NCOEF][kmax][nslot]
+//   cap   [kmax][nslot] (BcUp 4) force [NFORCE][nslot]
+//   sflux [NDISS][nslot]         budget[4][nslot] (FP64)
+template <typename real>
+struct ColumnArgs {
+  real* conc;
+  real* out;          // KIND_RHS destination
+  const real* coef;
+  const real* cap;
+  const real* force;
+  const int* kact;    // [nslot]
+  const int* tile_k;  // [ntiles_total] layers to stage per tile
+  real* sflux;
+  double* budget;     // may be null
+  int* nsub;          // [nslot] attempts of the last step
+  unsigned* queue;    // tile counter, zero before the launch
+  DevStats* stats;
+  int nslot, kmax, tc, tile0, ntiles;
+  double dt;
+  int method;
+};
+
+template <typename real>
+size_t tile_smem_bytes(int tc, int lpl, bool bc4);
+
+template <typename real>
+cudaError_t launch_column(const ColumnArgs<real>& a, const Params<real>& p,
+                          int lpl, bool bc4, int kind, int blocks, int threads,
+                          cudaStream_t st);
+
+template <typename real>
+int column_blocks_per_sm(int tc, int lpl, bool bc4, int kind, int threads);
+
+template <typename real>
+cudaError_t launch_trial(const real* conc, const real* rhs, const int* kact,
+                         int nslot, int kmax, real dtr, real keep, int* flag,
+                         int sms, cudaStream_t st);
+
+template <typename real>
+cudaError_t launch_accept(real* conc, const real* rhs, const int* kact,
+                          int nslot, int kmax, real dtr, int sms,
+                          cudaStream_t st);
+
+template <typename real>
+cudaError_t launch_epilogue(real* conc, const int* kact, int nslot, int kmax,
+                            const Params<real>& p, DevStats* stats, int sms,
+                            cudaStream_t st);
+
+template <typename real>
+cudaError_t launch_gather(const double* src, real* dst, const int* slot_col,
+                          int ngroups, int kmax, int ncol, int nslot, int sms,
+                          cudaStream_t st);
+
+template <typename real>
+cudaError_t launch_scatter(const real* src, double* dst, const int* slot_col,
+                           const int* kact, int ngroups, int kmax, int ncol,
+                           int nslot, int sms, cudaStream_t st);
+
+template <typename real>
+cudaError_t launch_scatter_flux(const real* sflux, double* fluxes,
+                                const int* slot_col, const int* kact, int ncol,
+                                int nslot, int sms, cudaStream_t st);
+
+template <typename real>
+cudaError_t launch_prep_grid(const double* dz, const double* dzc,
+                             const double* phi, const double* phi_i,
+                             const double* biofac, const double* cap,
+                             const int* slot_col, real* coef, real* capd,
+                             int kmax, int ncol, int nslot, int mode,
+                             double d0, int sms, cudaStream_t st);
+
+template <typename real>
+cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
+                              const int* slot_col, real* force, int ncol,
+                              int nslot, double bio, double diffusivity,
+                              int mode, int bcup_d, int sms, cudaStream_t st);
+
+}  // namespace sed

@@ -1,0 +1,307 @@
+"""ctypes binding of the C ABI in include/mossco_sed.h.
+
+This is the same binding a Python caller of the library would write; the
+Fortran host binds the same symbols through ISO_C_BINDING.  The library is
+the only compute path: if it cannot be loaded, or no GPU is present,
+:class:`Solver` raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+from typing import Optional
+
+import numpy as np
+
+from . import build as _build
+from .model import BGC_NAMES, NTR, ColumnSet
+
+SED_OK, SED_E_ARG, SED_E_NAN, SED_E_SUBSTEP_CAP = 0, -1, -2, -3
+SED_E_CUDA, SED_E_STATE, SED_E_NOMEM, SED_E_NODEVICE = -4, -5, -6, -7
+SED_E_TIMEOUT = -8
+SED_FP32, SED_FP64 = 0, 1
+SED_CUT_PER_COLUMN, SED_CUT_GLOBAL = 0, 1
+SED_KMAX_LIMIT = 64
+
+
+class SedError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{msg} (code {code})")
+        self.code = code
+
+
+class SedParams(ctypes.Structure):
+    _fields_ = ([("diffusivity", ctypes.c_double),
+                 ("bioturbation", ctypes.c_double),
+                 ("bcup_dissolved", ctypes.c_int),
+                 ("bcup_particulate", ctypes.c_int),
+                 ("mol_diff_mode", ctypes.c_int),
+                 ("mol_diff_d0", ctypes.c_double),
+                 ("dt_min", ctypes.c_double),
+                 ("relative_change_min", ctypes.c_double),
+                 ("max_attempts", ctypes.c_int),
+                 ("cut_scope", ctypes.c_int)]
+                + [(n, ctypes.c_double) for n in BGC_NAMES]
+                + [("epilogue", ctypes.c_int),
+                   ("minimum", ctypes.c_double * NTR),
+                   ("precision", ctypes.c_int),
+                   ("budgets", ctypes.c_int),
+                   ("device", ctypes.c_int)])
+
+
+class SedStats(ctypes.Structure):
+    _fields_ = [("attempts", ctypes.c_longlong),
+                ("accepted", ctypes.c_longlong),
+                ("column_steps", ctypes.c_longlong),
+                ("max_col_attempts", ctypes.c_int),
+                ("capped_columns", ctypes.c_int),
+                ("nan_cells", ctypes.c_int),
+                ("gpu_launches", ctypes.c_int),
+                ("min_dt", ctypes.c_double),
+                ("device_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_vp = ctypes.c_void_p
+_H = ctypes.c_void_p
+
+# name -> (restype, argtypes); must list every function of mossco_sed.h
+SIGNATURES = {
+    "sed_default_params": (ctypes.c_int, [ctypes.POINTER(SedParams)]),
+    "sed_create": (ctypes.c_int, [ctypes.POINTER(SedParams), ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.POINTER(_H)]),
+    "sed_set_grid": (ctypes.c_int, [_H, _dp, _dp, _dp, _dp, _dp, _dp, _ip,
+                                    _ip]),
+    "sed_set_forcing": (ctypes.c_int, [_H, _dp, _dp]),
+    "sed_set_state": (ctypes.c_int, [_H, _dp]),
+    "sed_get_state": (ctypes.c_int, [_H, _dp]),
+    "sed_step": (ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int,
+                                ctypes.c_int, ctypes.POINTER(SedStats)]),
+    "sed_ode_solver": (ctypes.c_int, [_H, _dp, _dp, _dp, ctypes.c_double,
+                                      ctypes.c_int,
+                                      ctypes.POINTER(SedStats)]),
+    "sed_get_rhs": (ctypes.c_int, [_H, _dp, _dp, _dp]),
+    "sed_get_fluxes": (ctypes.c_int, [_H, _dp]),
+    "sed_get_attempts": (ctypes.c_int, [_H, _ip]),
+    "sed_get_budgets": (ctypes.c_int, [_H, _dp]),
+    "sed_set_stream": (ctypes.c_int, [_H, _vp]),
+    "sed_host_register": (ctypes.c_int, [_vp, ctypes.c_size_t]),
+    "sed_host_unregister": (ctypes.c_int, [_vp]),
+    "sed_error_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "sed_last_error": (ctypes.c_char_p, [_H]),
+    "sed_tracer_name": (ctypes.c_char_p, [ctypes.c_int]),
+    "sed_tracer_is_particulate": (ctypes.c_int, [ctypes.c_int]),
+    "sed_destroy": (None, [_H]),
+}
+
+_lib = None
+
+
+def header_functions() -> list:
+    """Function names declared in include/mossco_sed.h."""
+    path = os.path.join(_build.INCLUDE, "mossco_sed.h")
+    text = open(path).read()
+    return sorted(set(re.findall(r"\b(sed_[a-z_0-9]+)\s*\(", text)))
+
+
+def load(build: bool = True):
+    """Load libsedgpu.so (building it first when sources changed)."""
+    global _lib
+    if _lib is None:
+        path = _build.build() if build else _build.LIB_PATH
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a: Optional[np.ndarray], ptype=_dp):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ptype)
+
+
+def default_params() -> SedParams:
+    p = SedParams()
+    rc = load().sed_default_params(ctypes.byref(p))
+    if rc != SED_OK:
+        raise SedError(rc, "sed_default_params")
+    return p
+
+
+def params_from(cs: ColumnSet, precision: int = SED_FP32, budgets: bool = False,
+                cut_scope: int = SED_CUT_PER_COLUMN, epilogue: bool = True,
+                device: int = 0) -> SedParams:
+    """sed_params for a ColumnSet (driver + OMEXDIA+P parameters)."""
+    p = default_params()
+    d = cs.driver
+    p.diffusivity = d.diffusivity
+    p.bioturbation = d.bioturbation
+    p.bcup_dissolved = d.bcup_dissolved
+    p.bcup_particulate = d.bcup_particulate
+    p.mol_diff_mode = d.mol_diff_mode
+    p.mol_diff_d0 = d.mol_diff_d0
+    p.dt_min = d.dt_min
+    p.relative_change_min = d.relative_change_min
+    p.max_attempts = int(d.max_attempts)
+    p.cut_scope = cut_scope
+    for n in BGC_NAMES:
+        setattr(p, n, float(cs.bgc[n]))
+    p.epilogue = int(epilogue)
+    mins = d.minimum_array()
+    for i in range(NTR):
+        p.minimum[i] = float(mins[i])
+    p.precision = precision
+    p.budgets = int(budgets)
+    p.device = device
+    return p
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Solver:
+    """One library handle over a ColumnSet's grid."""
+
+    def __init__(self, cs: ColumnSet, precision: int = SED_FP32,
+                 budgets: bool = False, cut_scope: int = SED_CUT_PER_COLUMN,
+                 epilogue: bool = True, params: Optional[SedParams] = None):
+        self.lib = load()
+        self.cs = cs
+        self.params = params or params_from(cs, precision, budgets, cut_scope,
+                                            epilogue)
+        h = _H()
+        rc = self.lib.sed_create(ctypes.byref(self.params), cs.inum, cs.jnum,
+                                 cs.kmax, NTR, ctypes.byref(h))
+        if rc != SED_OK:
+            raise SedError(rc, "sed_create: " +
+                           self.lib.sed_error_string(rc).decode())
+        self.h = h
+        self._keep = {}
+        self._check(self.lib.sed_set_grid(
+            h, _p(_f64(cs.dz)), _p(_f64(cs.dzc)), _p(_f64(cs.phi)),
+            _p(_f64(cs.phi_i)), _p(_f64(cs.biofac)),
+            _p(_f64(cs.flux_cap)),
+            _p(np.ascontiguousarray(cs.kact, dtype=np.int32), _ip), None),
+            "sed_set_grid")
+
+    def _check(self, rc: int, what: str):
+        if rc != SED_OK:
+            msg = self.lib.sed_last_error(self.h).decode()
+            raise SedError(rc, f"{what}: {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sed_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- state / forcing -------------------------------------------------
+    def set_forcing(self, bdys=None, fluxes=None):
+        cs = self.cs
+        b = _f64(cs.bdys if bdys is None else bdys)
+        f = _f64(cs.fluxes if fluxes is None else fluxes)
+        self._check(self.lib.sed_set_forcing(self.h, _p(b), _p(f)),
+                    "sed_set_forcing")
+
+    def set_state(self, conc):
+        c = _f64(conc)
+        self._check(self.lib.sed_set_state(self.h, _p(c)), "sed_set_state")
+
+    def get_state(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        cs = self.cs
+        if out is None:
+            out = np.array(cs.conc, dtype=np.float64, copy=True)
+        self._check(self.lib.sed_get_state(self.h, _p(out)), "sed_get_state")
+        return out
+
+    # -- stepping ------------------------------------------------------------
+    def step(self, nsteps: int = 1, dt: Optional[float] = None,
+             method: int = 2, raise_on_error: bool = True):
+        st = SedStats()
+        dt = self.cs.dt if dt is None else dt
+        rc = self.lib.sed_step(self.h, float(dt), int(method), int(nsteps),
+                               ctypes.byref(st))
+        if raise_on_error:
+            self._check(rc, "sed_step")
+            return st.as_dict()
+        return rc, st.as_dict()
+
+    def ode_solver(self, conc: np.ndarray, bdys: np.ndarray,
+                   fluxes: np.ndarray, dt: float, method: int = 2,
+                   raise_on_error: bool = True):
+        """Drop-in for `call ode_solver(sed, dt, method)` + epilogue on host
+        arrays (conc and fluxes updated in place)."""
+        assert conc.dtype == np.float64 and conc.flags.c_contiguous
+        assert fluxes.dtype == np.float64 and fluxes.flags.c_contiguous
+        b = _f64(bdys)
+        st = SedStats()
+        rc = self.lib.sed_ode_solver(self.h, _p(conc), _p(b), _p(fluxes),
+                                     float(dt), int(method), ctypes.byref(st))
+        if raise_on_error:
+            self._check(rc, "sed_ode_solver")
+            return st.as_dict()
+        return rc, st.as_dict()
+
+    def get_rhs(self, conc: np.ndarray, fluxes: Optional[np.ndarray] = None):
+        cs = self.cs
+        c = _f64(conc)
+        rhs = np.zeros_like(c)
+        fl = np.array(cs.fluxes if fluxes is None else fluxes,
+                      dtype=np.float64, copy=True)
+        self._check(self.lib.sed_get_rhs(self.h, _p(c), _p(rhs), _p(fl)),
+                    "sed_get_rhs")
+        return rhs, fl
+
+    def set_stream(self, stream_handle: int) -> None:
+        """Use a caller's CUDA stream (e.g. torch.cuda.Stream().cuda_stream)."""
+        self._check(self.lib.sed_set_stream(self.h, ctypes.c_void_p(stream_handle)),
+                    "sed_set_stream")
+
+    def fluxes(self) -> np.ndarray:
+        out = np.array(self.cs.fluxes, dtype=np.float64, copy=True)
+        self._check(self.lib.sed_get_fluxes(self.h, _p(out)), "sed_get_fluxes")
+        return out
+
+    def attempts(self) -> np.ndarray:
+        out = np.zeros(self.cs.ncol, dtype=np.int32)
+        self._check(self.lib.sed_get_attempts(self.h, _p(out, _ip)),
+                    "sed_get_attempts")
+        return out
+
+    def budgets(self) -> np.ndarray:
+        out = np.zeros((4, self.cs.ncol))
+        self._check(self.lib.sed_get_budgets(self.h, _p(out)),
+                    "sed_get_budgets")
+        return out
+
+
+def host_register(a: np.ndarray) -> None:
+    rc = load().sed_host_register(a.ctypes.data, a.nbytes)
+    if rc != SED_OK:
+        raise SedError(rc, "sed_host_register")
+
+
+def host_unregister(a: np.ndarray) -> None:
+    load().sed_host_unregister(a.ctypes.data)

@@ -1,0 +1,246 @@
+"""GPU parity of the CUDA library (through the C ABI) against the FP64 oracle.
+
+FP64 device state reproduces the oracle to rounding (same algorithm); FP32
+device state stays within the 1e-3 per-tracer relative error of the
+workload's accuracy target (relative to |ref| plus a floor of 1e-4 x the
+tracer's largest value, since deep O2 / NO3 fall to ~0).
+"""
+import numpy as np
+import pytest
+
+from cases import constant_rhs_case, decay_case, no_reactions, small
+from conftest import relerr
+from sedgpu import capi, synth
+from sedgpu.model import (ADAPTIVE_EULER, EULER, NTR, RUNGE_KUTTA_4,
+                          RUNGE_KUTTA_4_38)
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-9
+FP32_TOL = 1e-3
+
+
+def run_gpu(cs, nsteps, method=ADAPTIVE_EULER, dt=None, precision=capi.SED_FP32,
+            cut=capi.SED_CUT_PER_COLUMN, budgets=False):
+    s = capi.Solver(cs, precision=precision, cut_scope=cut, budgets=budgets)
+    s.set_forcing()
+    s.set_state(cs.conc)
+    st = s.step(nsteps, dt=dt, method=method)
+    out = s.get_state()
+    fl = s.fluxes()
+    att = s.attempts()
+    bud = s.budgets() if budgets else None
+    s.close()
+    return out, fl, st, att, bud
+
+
+def run_oracle(oracle_mod, cs, nsteps, method=ADAPTIVE_EULER, dt=None, percol=True):
+    om = oracle_mod.OracleModel(cs)
+    c = cs.conc.copy()
+    rc, st, fl = om.run(c, nsteps=nsteps, dt=dt, method=method, percol=percol)
+    assert rc == 0
+    return c, fl, st
+
+
+def active(cs, c):
+    """Active cells only, as [ntr][cells]."""
+    K = np.arange(cs.kmax)[:, None] < cs.kact[None, :]
+    return c[:, K]
+
+
+def test_rhs_fp64_matches_oracle(oracle_mod):
+    cs = synth.make_workload("plain_cpu_10x10")
+    s = capi.Solver(cs, precision=capi.SED_FP64)
+    s.set_forcing()
+    rhs, fl = s.get_rhs(cs.conc)
+    s.close()
+    ref, fref, _ = oracle_mod.OracleModel(cs).get_rhs(cs.conc)
+    scale = np.abs(ref).max(axis=(1, 2), keepdims=True)
+    assert np.max(np.abs(rhs - ref) / scale) < 1e-12
+    np.testing.assert_allclose(fl[6:], fref[6:], rtol=1e-12)
+
+
+def test_rhs_fp32_matches_oracle(oracle_mod):
+    cs = synth.make_workload("plain_cpu_10x10")
+    s = capi.Solver(cs, precision=capi.SED_FP32)
+    s.set_forcing()
+    rhs, fl = s.get_rhs(cs.conc)
+    s.close()
+    ref, _, _ = oracle_mod.OracleModel(cs).get_rhs(cs.conc)
+    scale = np.abs(ref).max(axis=(1, 2), keepdims=True)
+    assert np.max(np.abs(rhs - ref) / scale) < 2e-5
+
+
+@pytest.mark.parametrize("precision,tol", [(capi.SED_FP64, FP64_TOL),
+                                           (capi.SED_FP32, FP32_TOL)])
+def test_adaptive_percol_10x10(oracle_mod, precision, tol):
+    cs = synth.make_workload("plain_cpu_10x10")
+    n = 48
+    out, fl, st, att, _ = run_gpu(cs, n, precision=precision)
+    ref, fref, sref = run_oracle(oracle_mod, cs, n)
+    err = relerr(active(cs, out), active(cs, ref))
+    assert err.max() < tol, err
+    if precision == capi.SED_FP64:
+        assert st["attempts"] == sref["attempts"]
+        assert st["accepted"] == sref["accepted"]
+
+
+def test_adaptive_global_cut_10x10(oracle_mod):
+    # the reference's own semantics: one cut for the whole grid
+    cs = synth.make_workload("plain_cpu_10x10")
+    n = 12
+    out, fl, st, _, _ = run_gpu(cs, n, precision=capi.SED_FP64,
+                                cut=capi.SED_CUT_GLOBAL)
+    ref, fref, sref = run_oracle(oracle_mod, cs, n, percol=False)
+    err = relerr(active(cs, out), active(cs, ref))
+    assert err.max() < FP64_TOL, err
+    assert st["accepted"] == sref["accepted"] * cs.n_active
+
+
+@pytest.mark.parametrize("method", [EULER, RUNGE_KUTTA_4, RUNGE_KUTTA_4_38])
+def test_fixed_methods(oracle_mod, method):
+    cs = small(32, 20, seed=9)
+    out, fl, st, _, _ = run_gpu(cs, 30, method=method, dt=60.0,
+                                precision=capi.SED_FP64)
+    ref, fref, _ = run_oracle(oracle_mod, cs, 30, method=method, dt=60.0)
+    err = relerr(active(cs, out), active(cs, ref))
+    assert err.max() < FP64_TOL, err
+    np.testing.assert_allclose(fl[6:], fref[6:], rtol=1e-9)
+
+
+def test_uneven_columns_and_land(oracle_mod):
+    cols = np.arange(0, 1024 * 1024, 1024 * 1024 // 300)[:300]
+    cs = synth.make_workload("uneven_1024x1024", cols=cols)
+    assert (cs.kact == 0).any() and (cs.kact > 32).any() and (cs.kact <= 32).any()
+    n = 12
+    out, fl, st, att, _ = run_gpu(cs, n, precision=capi.SED_FP64)
+    ref, fref, sref = run_oracle(oracle_mod, cs, n)
+    err = relerr(active(cs, out), active(cs, ref))
+    assert err.max() < FP64_TOL, err
+    # land columns and inactive layers are returned untouched
+    land = cs.kact == 0
+    np.testing.assert_array_equal(out[:, :, land], cs.conc[:, :, land])
+    assert np.all(att[land] == 0) and np.all(att[~land] > 0)
+    out32, _, _, _, _ = run_gpu(cs, n, precision=capi.SED_FP32)
+    err32 = relerr(active(cs, out32), active(cs, ref))
+    assert err32.max() < FP32_TOL, err32
+
+
+def test_bcup_variants(oracle_mod):
+    cs = small(24, 16, seed=21)
+    cs.driver.bcup_dissolved = 1
+    cs.fluxes[6:] = -2e-6
+    cs.driver.bcup_particulate = 4
+    cs.flux_cap[:] = 2e-5 * cs.dz / cs.dz[0]
+    cs.driver.mol_diff_mode = 0
+    for n in range(6):
+        cs.fluxes[n] *= 50.0
+    out, fl, st, _, _ = run_gpu(cs, 8, precision=capi.SED_FP64)
+    ref, fref, _ = run_oracle(oracle_mod, cs, 8)
+    err = relerr(active(cs, out), active(cs, ref))
+    assert err.max() < FP64_TOL, err
+
+
+def test_constant_rhs_exact_on_gpu():
+    cs = constant_rhs_case()
+    for method in (EULER, RUNGE_KUTTA_4, ADAPTIVE_EULER, RUNGE_KUTTA_4_38):
+        out, _, _, _, _ = run_gpu(cs, 5, method=method, dt=600.0,
+                                  precision=capi.SED_FP64)
+        rhs_top = cs.fluxes[:6] / (cs.phi[0] * cs.dz[0])
+        expect = cs.conc.copy()
+        expect[:6, 0, :] += 5 * 600.0 * rhs_top
+        np.testing.assert_allclose(out, expect, rtol=1e-13)
+
+
+def test_cut_sequence_on_gpu():
+    cs = decay_case()
+    for prec in (capi.SED_FP64, capi.SED_FP32):
+        out, _, st, att, _ = run_gpu(cs, 1, precision=prec)
+        assert st["attempts"] == 18 * cs.ncol
+        assert st["accepted"] == 16 * cs.ncol
+        assert st["min_dt"] == cs.dt / 16
+        assert np.all(att == 18)
+
+
+def test_drop_in_ode_solver_host_arrays(oracle_mod):
+    # sed_ode_solver: host FP64 arrays in and out, as ode_solver + epilogue
+    cs = synth.make_workload("plain_cpu_10x10")
+    s = capi.Solver(cs, precision=capi.SED_FP64)
+    conc = cs.conc.copy()
+    fl = cs.fluxes.copy()
+    for _ in range(6):
+        s.ode_solver(conc, cs.bdys, fl, cs.dt, ADAPTIVE_EULER)
+    s.close()
+    ref, fref, _ = run_oracle(oracle_mod, cs, 6)
+    err = relerr(active(cs, conc), active(cs, ref))
+    assert err.max() < FP64_TOL
+    np.testing.assert_allclose(fl, fref, rtol=1e-9, atol=1e-300)
+
+
+def test_budgets_fp64(oracle_mod):
+    cs = small(64, 30, seed=13, total=0.2)
+    out, fl, st, att, bud = run_gpu(cs, 4, precision=capi.SED_FP32, budgets=True)
+    invP, resP, invN, resN = bud
+    assert np.all(invP > 0) and np.all(invN > 0)
+    # FP32 state: the residual of the last step is at rounding level
+    assert np.max(np.abs(resP) / invP) < 1e-5
+    assert np.max(np.abs(resN) / invN) < 1e-5
+
+
+def test_status_codes():
+    cs = decay_case()
+    cs.driver.max_attempts = 3
+    s = capi.Solver(cs)
+    s.set_forcing()
+    s.set_state(cs.conc)
+    rc, st = s.step(1, raise_on_error=False)
+    assert rc == capi.SED_E_SUBSTEP_CAP and st["capped_columns"] == cs.ncol
+    s.close()
+    # NaN in the input state surfaces as SED_E_NAN, the context stays usable
+    cs = small(8, 10, seed=1)
+    bad = cs.conc.copy()
+    bad[6, 3, 2] = np.nan
+    s = capi.Solver(cs)
+    s.set_forcing()
+    s.set_state(bad)
+    rc, st = s.step(1, raise_on_error=False)
+    assert rc == capi.SED_E_NAN and st["nan_cells"] >= 1
+    s.set_state(cs.conc)
+    rc, st = s.step(1, raise_on_error=False)
+    assert rc == capi.SED_OK
+    s.close()
+    # call order and argument checks
+    lib = capi.load()
+    p = capi.params_from(cs)
+    h = capi._H()
+    import ctypes
+    assert lib.sed_create(ctypes.byref(p), 4, 4, 65, 11, ctypes.byref(h)) == capi.SED_E_ARG
+    assert lib.sed_create(ctypes.byref(p), 4, 4, 10, 12, ctypes.byref(h)) == capi.SED_E_ARG
+    p.bcup_dissolved = 7
+    assert lib.sed_create(ctypes.byref(p), 4, 4, 10, 11, ctypes.byref(h)) == capi.SED_E_ARG
+    s = capi.Solver(cs)
+    rc = lib.sed_step(s.h, 3600.0, 2, 1, None)
+    assert rc == capi.SED_E_STATE
+    s.close()
+
+
+def test_full_size_workload_properties(oracle_mod):
+    """256 x 256 x 30 for 48 coupling steps on the GPU; a column subsample is
+    rerun by the oracle (per-column cuts make any subset exact)."""
+    cs = synth.make_workload("plain_gpu_256x256")
+    n = 48
+    s = capi.Solver(cs, precision=capi.SED_FP32, budgets=True)
+    s.set_forcing()
+    s.set_state(cs.conc)
+    st = s.step(n)
+    out = s.get_state()
+    bud = s.budgets()
+    s.close()
+    assert np.isfinite(out).all() and (out >= 0).all()
+    assert st["column_steps"] == cs.ncol * n
+    assert np.max(np.abs(bud[1]) / bud[0]) < 1e-4
+    cols = np.random.default_rng(3).choice(cs.ncol, 64, replace=False)
+    sub = cs.subset(cols)
+    ref, _, _ = run_oracle(oracle_mod, sub, n)
+    err = relerr(active(sub, out[:, :, cols]), active(sub, ref))
+    assert err.max() < FP32_TOL, err

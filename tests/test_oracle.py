@@ -1,0 +1,190 @@
+"""CPU tests of the FP64 oracle: known-answer tests of the stepper built from
+the reference's own solver test and source, conservation and steady-state
+properties of the transport, and the golden regression vectors."""
+import os
+
+import numpy as np
+import pytest
+
+from cases import constant_rhs_case, decay_case, no_reactions, no_transport, small
+from sedgpu import synth
+from sedgpu.model import (ADAPTIVE_EULER, EULER, NTR, RUNGE_KUTTA_4,
+                          RUNGE_KUTTA_4_38)
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.mark.parametrize("method", [EULER, RUNGE_KUTTA_4, ADAPTIVE_EULER,
+                                    RUNGE_KUTTA_4_38])
+@pytest.mark.parametrize("percol", [True, False])
+def test_constant_rhs_exact(oracle_mod, method, percol):
+    # src/test/test_Solver.F90:36-43: a constant rhs is integrated exactly
+    cs = constant_rhs_case()
+    om = oracle_mod.OracleModel(cs)
+    c0 = cs.conc.copy()
+    rhs, _, _ = om.get_rhs(c0)
+    assert np.all(rhs[:, 1:, :] == 0.0)
+    assert np.all(rhs[6:] == 0.0)
+    c = c0.copy()
+    nsteps, dt = 5, 600.0
+    rc, st, _ = om.run(c, nsteps=nsteps, dt=dt, method=method, percol=percol)
+    assert rc == 0
+    expect = c0.copy()
+    for _ in range(nsteps):
+        expect = expect + dt * rhs
+    np.testing.assert_allclose(c, expect, rtol=1e-13, atol=0)
+
+
+def test_constant_rhs_is_flux_over_volume(oracle_mod):
+    cs = constant_rhs_case()
+    om = oracle_mod.OracleModel(cs)
+    rhs, _, _ = om.get_rhs(cs.conc)
+    top = cs.fluxes[:6] / (cs.phi[0] * cs.dz[0])
+    np.testing.assert_allclose(rhs[:6, 0, :], top, rtol=1e-14)
+
+
+@pytest.mark.parametrize("percol", [True, False])
+def test_adaptive_cut_sequence(oracle_mod, percol):
+    # solver_library.F90:121-127: c1 = c(1 - 8) and c(1 - 2) are rejected,
+    # c(1 - 0.5) is accepted -> 2 cuts, 16 accepted substeps of dt/16.
+    cs = decay_case()
+    om = oracle_mod.OracleModel(cs)
+    c = cs.conc.copy()
+    rc, st, _ = om.run(c, nsteps=1, method=ADAPTIVE_EULER, percol=percol)
+    assert rc == 0
+    assert st["min_dt"] == cs.dt / 16
+    if percol:
+        assert st["accepted"] == 16 * cs.ncol
+        assert st["attempts"] == 18 * cs.ncol
+        assert st["max_col_attempts"] == 18
+    else:
+        assert st["accepted"] == 16 and st["attempts"] == 18
+    np.testing.assert_allclose(c[0], cs.conc[0] * 0.5 ** 16, rtol=1e-12)
+
+
+def test_dt_min_accepts_bad_step(oracle_mod):
+    # the dt_min guard (:126): once dt_red <= dt_min the step is accepted
+    cs = decay_case(lam_dt=8.0)
+    cs.driver.dt_min = cs.dt / 4   # 900 s is the smallest cut
+    om = oracle_mod.OracleModel(cs)
+    c = cs.conc.copy()
+    rc, st, _ = om.run(c, nsteps=1, method=ADAPTIVE_EULER, percol=True)
+    assert rc == 0
+    assert st["min_dt"] == cs.dt / 4
+    assert st["accepted"] == 4 * cs.ncol
+    # each accepted substep multiplies by 1 - 2 = -1: four of them give +c0
+    np.testing.assert_allclose(c[0], cs.conc[0], rtol=1e-12)
+
+
+def test_substep_cap_reported(oracle_mod):
+    cs = decay_case()
+    cs.driver.max_attempts = 3
+    om = oracle_mod.OracleModel(cs)
+    c = cs.conc.copy()
+    rc, st, _ = om.run(c, nsteps=1, method=ADAPTIVE_EULER, percol=True)
+    assert rc == -3 and st["capped"] == cs.ncol
+
+
+@pytest.mark.parametrize("bcup", [1, 2])
+def test_transport_conserves_mass(oracle_mod, bcup):
+    # diff3d :818-820 + no-flux bottom: inventory changes by the surface flux
+    cs = no_reactions(small(8, 15, seed=11))
+    cs.driver.bcup_dissolved = bcup
+    if bcup == 1:
+        cs.fluxes[6:] = 1e-5
+    om = oracle_mod.OracleModel(cs)
+    c = cs.conc.copy()
+    inv0 = om.inventory(c)
+    _, fl, _ = om.get_rhs(c)
+    rc, st, _ = om.run(c, nsteps=1, dt=60.0, method=EULER, percol=True)
+    inv1 = om.inventory(c)
+    expect = inv0 + 60.0 * fl
+    np.testing.assert_allclose(inv1, expect, rtol=1e-11)
+
+
+def test_dirichlet_steady_state_uniform(oracle_mod):
+    # Dirichlet top, no-flux bottom, no reactions: the dissolved profiles
+    # relax to the bottom-water value.  The coupling step is short enough for
+    # explicit Euler to be stable (at 3600 s the positivity limiter of
+    # solver_library.F90:121 accepts 900 s steps that are oscillatory for the
+    # 1 mm top layers, and the profile settles into a bounded limit cycle).
+    cs = no_reactions(small(3, 6, seed=2, total=0.0061))
+    om = oracle_mod.OracleModel(cs)
+    c = cs.conc.copy()
+    rc, st, _ = om.run(c, nsteps=4000, dt=120.0, method=ADAPTIVE_EULER,
+                       percol=True)
+    assert rc == 0
+    for n in range(6, NTR):
+        np.testing.assert_allclose(c[n], np.broadcast_to(cs.bdys[n + 1], c[n].shape),
+                                   rtol=2e-3, atol=1e-6)
+
+
+def test_reaction_budgets_close(oracle_mod):
+    # P moves between pools without loss; N is lost only by denitrification
+    import oracle as O
+    rng = np.random.default_rng(0)
+    for _ in range(50):
+        c = rng.uniform(0.0, 300.0, NTR)
+        r, dn = O.omexdia_rates(synth.BGC_DEFAULTS, c)
+        assert abs(r[4] + r[5] + r[10]) <= 1e-15 * np.abs(r[[4, 5, 10]]).max() + 1e-300
+        n_sum = r[2] + r[3] + r[7] + r[8]
+        assert abs(n_sum + 0.8 * dn) <= 1e-12 * (np.abs(r).max() + 1e-30)
+
+
+def test_percol_equals_single_column_runs(oracle_mod):
+    # per-column mode: each column's result does not depend on the others
+    cs = small(6, 10, seed=4, days=1)
+    om = oracle_mod.OracleModel(cs)
+    c = cs.conc.copy()
+    om.run(c, nsteps=6, method=ADAPTIVE_EULER, percol=True)
+    for col in (0, 3, 5):
+        sub = cs.subset(np.array([col]))
+        cc = sub.conc.copy()
+        oracle_mod.OracleModel(sub).run(cc, nsteps=6, method=ADAPTIVE_EULER,
+                                        percol=False)
+        np.testing.assert_array_equal(cc[:, :, 0], c[:, :, col])
+
+
+def test_linear_grid_matches_reference_formula(oracle_mod):
+    from sedgpu import driver
+    dz, zc, zi, dzc = oracle_mod.init_grid_linear(24, 0.003)
+    g = driver.SedGrid(1, 1, 24, 0.003)
+    driver.init_grid(g)
+    np.testing.assert_allclose(g.dz[:, 0], dz, rtol=1e-15)
+    np.testing.assert_allclose(g.dzc[:, 0], dzc, rtol=1e-13)
+    fac = 0.18 / ((24 + 1) / 2.0 * 0.003) - 1.0
+    assert dz[-1] == pytest.approx(fac * 0.003, rel=1e-14)
+
+
+def test_bcup4_cascade(oracle_mod):
+    # diff3d :791-802 with a flux larger than the first caps
+    K = 5
+    cap = np.array([1.0, 2.0, 0.5, 0.5, 0.5])
+    C = np.zeros(K)
+    ones = np.ones(K)
+    flux, dC = oracle_mod.diff3d(C, 0.0, 3.2, 4, 0 * ones, ones, ones,
+                                 np.ones(K - 1), flux_cap=cap)
+    # rest: 3.2-1=2.2 -> F2 += 2.2; 2.2-2=0.2 -> F3 += 0.2; 0.2-0.5<0 stop
+    np.testing.assert_allclose(flux[:K + 1], [3.2, 2.2, 0.2, 0.0, 0.0, 0.0])
+    flux, dC = oracle_mod.diff3d(C, 0.0, 10.0, 4, 0 * ones, ones, ones,
+                                 np.ones(K - 1), flux_cap=cap)
+    # all caps exceeded: rests 9, 7, 6.5, 6, 5.5; the last added to F(K)
+    np.testing.assert_allclose(flux[:K + 1], [10.0, 9.0, 7.0, 6.5, 6.0 + 5.5, 0.0])
+
+
+def _golden_files():
+    if not os.path.isdir(GOLDEN):
+        return []
+    return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+
+
+@pytest.mark.parametrize("fname", _golden_files())
+def test_golden_regression(oracle_mod, fname):
+    """The oracle reproduces the committed fixtures (tests/golden/make_golden.py)."""
+    import make_golden_cases
+    g = np.load(os.path.join(GOLDEN, fname))
+    cs = make_golden_cases.case(str(g["case"]))
+    out = make_golden_cases.run_oracle(oracle_mod, cs, str(g["case"]))
+    for key in out:
+        np.testing.assert_allclose(out[key], g[key], rtol=1e-11, atol=1e-300,
+                                   err_msg=key)
