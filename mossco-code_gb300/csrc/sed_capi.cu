@@ -80,7 +80,8 @@ struct sed_handle {
   // device buffers
   DevBuf d_slot_col, d_kact, d_tile_k, d_conc, d_coef, d_cap, d_force, d_sflux,
       d_budget, d_nsub, d_queue, d_stats, d_flag, d_stage, d_bdys, d_fluxes,
-      d_rhs, d_rhs_stage, d_grid;
+      d_rhs, d_rhs_stage, d_grid, d_force64;
+  std::vector<double> force64;  // host forcing rows (FP64 state)
   DevStats* h_stats = nullptr;  // pinned
   int* h_flag = nullptr;        // pinned
   // graph of one coupling step
@@ -134,6 +135,8 @@ Params<real> make_params(const sed_params& s) {
   p.ksO2oduox = (real)s.ksO2oduox;
   p.PAdsODU = (real)s.PAdsODU;
   p.nh3fac = (real)(1.0 / (1.0 + s.NH3Ads));
+  p.nh3den = (real)(1.0 + s.NH3Ads);
+  p.mol_mode = s.mol_diff_mode;
   p.keep = (real)(1.0 + s.relative_change_min);
   for (int n = 0; n < NTR; n++) p.minimum[n] = (real)s.minimum[n];
   p.dt_min = s.dt_min;
@@ -393,12 +396,42 @@ int prep_force(sed_handle* h) {
   return SED_OK;
 }
 
+// FP64 state: the per-column forcing rows are formed on the host with the
+// host's exp, exactly as get_rhs forms them (:648, :652, :682), then
+// gathered into slot order, so FP64 device results match the CPU
+// restatement bit for bit.
+int prep_force_host64(sed_handle* h, const double* bdys, const double* fluxes) {
+  const int ncol = h->ncol;
+  h->force64.assign((size_t)NFORCE * ncol, 0.0);
+  double* f = h->force64.data();
+  for (int c = 0; c < ncol; c++) {
+    const double T = bdys[c];
+    const double f_T = 1.0 * std::exp(-4500.0 * (1.0 / (T + 273.0) - (1.0 / 288.0)));
+    f[c] = h->prm.bioturbation * f_T;
+    f[(size_t)ncol + c] = h->prm.mol_diff_mode == 1 ? 1.0 : (h->prm.diffusivity + T * 0.035);
+    for (int n = 0; n < NTR; n++) {
+      const double fl = fluxes[(size_t)n * ncol + c];
+      const double cb = bdys[(size_t)(n + 1) * ncol + c];
+      f[(size_t)(2 + n) * ncol + c] =
+          n < NPART ? fl : (h->prm.bcup_dissolved == 1 ? fl : cb);
+    }
+  }
+  CK(h->d_force64.alloc(h->force64.size() * sizeof(double)), "forcing staging");
+  CK(cudaMemcpyAsync(h->d_force64.p, f, h->force64.size() * sizeof(double),
+                     cudaMemcpyHostToDevice, h->stream), "forcing copy");
+  CK(launch_gather<double>(h->d_force64.as<double>(), h->d_force.as<double>(),
+                           h->d_slot_col.as<int>(), NFORCE, 1, ncol, h->nslot, h->sms,
+                           h->stream), "forcing gather");
+  h->launches++;
+  return SED_OK;
+}
+
 int upload_forcing(sed_handle* h, const double* bdys, const double* fluxes) {
   const size_t nb = (size_t)(NTR + 1) * h->ncol * sizeof(double);
   const size_t nf = (size_t)NTR * h->ncol * sizeof(double);
   CK(cudaMemcpyAsync(h->d_bdys.p, bdys, nb, cudaMemcpyHostToDevice, h->stream), "bdys copy");
   CK(cudaMemcpyAsync(h->d_fluxes.p, fluxes, nf, cudaMemcpyHostToDevice, h->stream), "fluxes copy");
-  int rc = h->fp64() ? prep_force<double>(h) : prep_force<float>(h);
+  int rc = h->fp64() ? prep_force_host64(h, bdys, fluxes) : prep_force<float>(h);
   if (rc) return rc;
   h->have_forcing = true;
   return SED_OK;
@@ -624,7 +657,8 @@ int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
   CK(h->d_kact.alloc(ns * sizeof(int)), "kact");
   CK(h->d_tile_k.alloc(tile_k.size() * sizeof(int)), "tile_k");
   CK(h->d_conc.alloc((size_t)NTR * kmax * ns * rs), "state");
-  CK(h->d_coef.alloc((size_t)NCOEF * kmax * ns * rs), "coefficients");
+  const int ncoef = h->fp64() ? NCOEF64 : NCOEF;
+  CK(h->d_coef.alloc((size_t)ncoef * kmax * ns * rs), "coefficients");
   CK(h->d_force.alloc((size_t)NFORCE * ns * rs), "forcing");
   CK(h->d_sflux.alloc((size_t)NDISS * ns * rs), "surface flux");
   CK(h->d_nsub.alloc(ns * sizeof(int)), "attempts");
@@ -643,7 +677,18 @@ int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
                      cudaMemcpyHostToDevice, h->stream), "tile_k copy");
   // grid arrays through a temporary FP64 staging area
   const size_t lay = (size_t)kmax * ncol;
-  CK(h->d_grid.alloc(6 * lay * sizeof(double)), "grid staging");
+  CK(h->d_grid.alloc(7 * lay * sizeof(double)), "grid staging");
+  // tortuosity-corrected molecular diffusivity (mode 1) with the host's
+  // logarithm: d0 phi_i / (1 - 2 ln phi_i)
+  std::vector<double> mol;
+  if (h->prm.mol_diff_mode == 1) {
+    mol.assign(lay, 0.0);
+    for (int c = 0; c < ncol; c++)
+      for (int k = 0; k < ka[c]; k++) {
+        const size_t i = (size_t)k * ncol + c;
+        mol[i] = h->prm.mol_diff_d0 * phi_i[i] / (1.0 - 2.0 * std::log(phi_i[i]));
+      }
+  }
   double* g = h->d_grid.as<double>();
   CK(cudaMemcpyAsync(g + 0 * lay, dz, lay * sizeof(double), cudaMemcpyHostToDevice, h->stream), "dz");
   if (kmax > 1)
@@ -655,16 +700,22 @@ int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
   if (bc4)
     CK(cudaMemcpyAsync(g + 5 * lay, flux_cap, lay * sizeof(double), cudaMemcpyHostToDevice,
                        h->stream), "flux_cap");
+  const double* gmol = nullptr;
+  if (!mol.empty()) {
+    CK(cudaMemcpyAsync(g + 6 * lay, mol.data(), lay * sizeof(double), cudaMemcpyHostToDevice,
+                       h->stream), "mol");
+    gmol = g + 6 * lay;
+  }
   cudaError_t e;
   if (h->fp64())
     e = launch_prep_grid<double>(g, g + lay, g + 2 * lay, g + 3 * lay, g + 4 * lay,
-                                 bc4 ? g + 5 * lay : nullptr, h->d_slot_col.as<int>(),
+                                 bc4 ? g + 5 * lay : nullptr, gmol, h->d_slot_col.as<int>(),
                                  h->d_coef.as<double>(), bc4 ? h->d_cap.as<double>() : nullptr,
                                  kmax, ncol, h->nslot, h->prm.mol_diff_mode,
                                  h->prm.mol_diff_d0, h->sms, h->stream);
   else
     e = launch_prep_grid<float>(g, g + lay, g + 2 * lay, g + 3 * lay, g + 4 * lay,
-                                bc4 ? g + 5 * lay : nullptr, h->d_slot_col.as<int>(),
+                                bc4 ? g + 5 * lay : nullptr, gmol, h->d_slot_col.as<int>(),
                                 h->d_coef.as<float>(), bc4 ? h->d_cap.as<float>() : nullptr,
                                 kmax, ncol, h->nslot, h->prm.mol_diff_mode,
                                 h->prm.mol_diff_d0, h->sms, h->stream);

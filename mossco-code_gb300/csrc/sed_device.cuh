@@ -15,12 +15,15 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace sed {
 
 constexpr int NTR = 11;    // tracers
 constexpr int NPART = 6;   // tracers 0..5 are particulate
 constexpr int NDISS = 5;   // tracers 6..10 are dissolved
-constexpr int NCOEF = 4;   // per-layer coefficient rows: phi, vol, gb, gm
+constexpr int NCOEF = 4;   // FP32 per-layer coefficient rows: phi, vol, gb, gm
+constexpr int NCOEF64 = 6; // FP64 rows: phi, phi_i, biofac, dz, len, mol
 constexpr int NFORCE = 13; // per-column forcing rows: bioT, dmul, bnd[11]
 constexpr unsigned FULL = 0xffffffffu;
 
@@ -32,16 +35,23 @@ enum : int {
   T_O2, T_NO3, T_NH4, T_ODU, T_PO4
 };
 
+// Coefficient rows staged per layer: the FP32 kernels use folded
+// conductances, the FP64 kernels the reference's own per-cell arrays so
+// that they evaluate get_rhs in its exact operation order.
+template <typename real> struct CoefRows { static constexpr int value = NCOEF; };
+template <> struct CoefRows<double> { static constexpr int value = NCOEF64; };
+
 // Reaction and solver constants in kernel units (rates per second).
 template <typename real>
 struct Params {
   real rF, rS, cmax, rnit, rodu, pads;
   real ksO2oxic, kinO2denit, ksNO3denit, kinO2anox, kinNO3anox, ksO2nitri,
-      ksO2oduox, PAdsODU, nh3fac;
+      ksO2oduox, PAdsODU, nh3fac, nh3den;
   real keep;          // 1 + relative_change_min
   real minimum[NTR];  // clamp of the component epilogue
   double dt_min;
   int bcup_d;         // 1 flux, 2 concentration, 3 zero
+  int mol_mode;       // 0 (diffusivity + 0.035 T) phi_i, 1 tortuosity
   int max_attempts;
   int epilogue;
   int budgets;
@@ -152,6 +162,10 @@ struct Lane {
   real vol[LPL];   // phi dz (budgets)
   real bnd[NTR];   // per tracer: bottom-water value or downward surface flux
   real src[BC4 ? LPL : 1][BC4 ? NPART : 1];  // capped-flux cascade sources
+  // FP64 reference-order path (diff3d's own operands)
+  real dz[LPL], len[LPL], Dp[LPL], Dd[LPL];
+  real ext_a[BC4 ? LPL : 1][BC4 ? NPART : 1];  // cascade additions in the loop
+  real ext_b[BC4 ? LPL : 1][BC4 ? NPART : 1];  // and the final one (:800-802)
 };
 
 // Right-hand side of one column: OMEXDIA+P rates plus diff3d transport.
@@ -263,6 +277,152 @@ __device__ __forceinline__ void cascade_sources(Lane<real, LPL, BC4>& lc,
       const int L = s * 32 + lane;
       const real below = (L >= K - 1) ? real(0) : eb[s];
       lc.src[s][n] = (L < K) ? (extra[s] - below) * lc.ivol[s] : real(0);
+    }
+  }
+}
+
+
+// ---------------------------------------------------------------------------
+// FP64 reference-order path.  The same OMEXDIA+P rates and diff3d transport
+// written operation for operation as the FP64 CPU restatement evaluates them
+// (compiled without FMA contraction), so that FP64 device results equal the
+// restatement bit for bit and the decisions of the adaptive loop coincide.
+__device__ __forceinline__ void omexdia_p_ref(const Params<double>& p,
+                                              const double (&c)[NTR],
+                                              double (&r)[NTR], double& denit) {
+  const double fdetC = c[T_FDETC], sdetC = c[T_SDETC], fdetN = c[T_FDETN];
+  const double sdetN = c[T_SDETN], fdetP = c[T_FDETP], adsP = c[T_ADSP];
+  const double O2 = c[T_O2], NO3 = c[T_NO3], NH4 = c[T_NH4], ODU = c[T_ODU];
+  const double PO4 = c[T_PO4];
+  const double CprodF = p.rF * fdetC;
+  const double CprodS = p.rS * sdetC;
+  const double NprodF = p.rF * fdetN;
+  const double NprodS = p.rS * sdetN;
+  const double Pprod = p.rF * fdetP;
+  const double Cprod = CprodF + CprodS;
+  double lim = 1.0;
+  if (Cprod > p.cmax) lim = p.cmax / Cprod;
+  const double oxlim = O2 / (O2 + p.ksO2oxic);
+  const double dnlim = (1.0 - O2 / (O2 + p.kinO2denit)) * (NO3 / (NO3 + p.ksNO3denit));
+  const double anlim = (1.0 - O2 / (O2 + p.kinO2anox)) * (1.0 - NO3 / (NO3 + p.kinNO3anox));
+  const double rescale = 1.0 / (oxlim + dnlim + anlim);
+  const double Cmin = lim * Cprod;
+  const double OxicMin = Cmin * oxlim * rescale;
+  const double Denit = Cmin * dnlim * rescale;
+  const double AnoxicMin = Cmin * anlim * rescale;
+  const double Nitri = p.rnit * NH4 * (O2 / (O2 + p.ksO2nitri));
+  const double OduOx = p.rodu * ODU * (O2 / (O2 + p.ksO2oduox));
+  const double fox = p.PAdsODU / (p.PAdsODU + ODU);
+  const double Rads = p.pads * (fox * PO4 - (1.0 - fox) * adsP);
+  r[T_FDETC] = -(lim * CprodF);
+  r[T_SDETC] = -(lim * CprodS);
+  r[T_FDETN] = -(lim * NprodF);
+  r[T_SDETN] = -(lim * NprodS);
+  r[T_FDETP] = -(lim * Pprod);
+  r[T_ADSP] = Rads;
+  r[T_O2] = -OxicMin - 2.0 * Nitri - OduOx;
+  r[T_NO3] = -0.8 * Denit + Nitri;
+  r[T_NH4] = (lim * (NprodF + NprodS) - Nitri) / p.nh3den;
+  r[T_ODU] = AnoxicMin - OduOx;
+  r[T_PO4] = lim * Pprod - Rads;
+  denit = Denit;
+}
+
+template <int LPL, bool BC4>
+__device__ __forceinline__ void column_rhs_ref(const Params<double>& p,
+                                               const Lane<double, LPL, BC4>& lc,
+                                               int lane, int K,
+                                               const double (&C)[LPL][NTR],
+                                               double (&R)[LPL][NTR],
+                                               double (&ftop)[NTR],
+                                               double (&dn)[LPL]) {
+#pragma unroll
+  for (int s = 0; s < LPL; s++) omexdia_p_ref(p, C[s], R[s], dn[s]);
+#pragma unroll
+  for (int n = 0; n < NTR; n++) {
+    const bool part = n < NPART;
+    double v[LPL], vm[LPL], F[LPL], Fb[LPL];
+#pragma unroll
+    for (int s = 0; s < LPL; s++) v[s] = part ? C[s][n] * lc.phi[s] : C[s][n];
+    from_above<double, LPL>(v, vm, lane);
+    // diff3d :776-778, interior interfaces
+#pragma unroll
+    for (int s = 0; s < LPL; s++) {
+      const double D = part ? lc.Dp[s] : lc.Dd[s];
+      F[s] = -D * (v[s] - vm[s]) / lc.len[s];
+    }
+    // :782-803 upper boundary
+    if (lane == 0) {
+      double f0;
+      if (part) f0 = lc.bnd[n];
+      else if (p.bcup_d == 2) f0 = -lc.Dd[0] * (v[0] - lc.bnd[n]) / lc.dz[0];
+      else if (p.bcup_d == 1) f0 = lc.bnd[n];
+      else f0 = 0.0;
+      F[0] = f0;
+    }
+    if (BC4 && part) {
+#pragma unroll
+      for (int s = 0; s < LPL; s++) {
+        F[s] = F[s] + lc.ext_a[BC4 ? s : 0][BC4 ? n : 0];
+        F[s] = F[s] + lc.ext_b[BC4 ? s : 0][BC4 ? n : 0];
+      }
+    }
+    if (lane == 0) ftop[n] = F[0];
+    from_below<double, LPL>(F, Fb, lane);
+    // :818-820 divergence; particulates scaled back to pore water (:677-678)
+#pragma unroll
+    for (int s = 0; s < LPL; s++) {
+      const int L = s * 32 + lane;
+      const double below = (L >= K - 1) ? 0.0 : Fb[s];
+      double t;
+      if (part) {
+        const double dC = (F[s] - below) / ((1.0 - lc.phi[s]) * lc.dz[s]);
+        t = dC * (1.0 - lc.phi[s]) / lc.phi[s];
+      } else {
+        t = (F[s] - below) / (lc.phi[s] * lc.dz[s]);
+      }
+      R[s][n] = (L < K) ? R[s][n] + t : 0.0;
+    }
+  }
+}
+
+// BcUp=4 cascade in the reference's serial order (diff3d :791-802): the
+// running rest is broadcast layer by layer so every addition rounds as in
+// the CPU loop.
+template <int LPL, bool BC4>
+__device__ __forceinline__ void cascade_ref(Lane<double, LPL, BC4>& lc,
+                                            const double (&cap)[LPL],
+                                            int lane, int K) {
+  if (!BC4) return;
+#pragma unroll
+  for (int n = 0; n < NPART; n++) {
+#pragma unroll
+    for (int s = 0; s < LPL; s++) {
+      lc.ext_a[BC4 ? s : 0][BC4 ? n : 0] = 0.0;
+      lc.ext_b[BC4 ? s : 0][BC4 ? n : 0] = 0.0;
+    }
+    const double fup = lc.bnd[n];
+    double rest = fup - __shfl_sync(FULL, cap[0], 0);
+    int k = 1;
+    while (rest > 0.0 && k <= K - 1) {
+      const int ks = k >> 5, kl = k & 31;
+#pragma unroll
+      for (int s = 0; s < LPL; s++)
+        if (s == ks && lane == kl) lc.ext_a[BC4 ? s : 0][BC4 ? n : 0] = rest;
+      double ck = 0.0;
+#pragma unroll
+      for (int s = 0; s < LPL; s++) {
+        const double t = __shfl_sync(FULL, cap[s], kl);
+        if (s == ks) ck = t;
+      }
+      rest = rest - ck;
+      k++;
+    }
+    if (k > K - 1) {
+      const int L = K - 1, ks = L >> 5, kl = L & 31;
+#pragma unroll
+      for (int s = 0; s < LPL; s++)
+        if (s == ks && lane == kl) lc.ext_b[BC4 ? s : 0][BC4 ? n : 0] = rest;
     }
   }
 }

@@ -34,7 +34,7 @@ struct TileLayout {
     size_t r = sizeof(real);
     conc = 0;
     coef = conc + (size_t)NTR * kt * tcp * r;
-    cap = coef + (size_t)NCOEF * kt * tcp * r;
+    cap = coef + (size_t)CoefRows<real>::value * kt * tcp * r;
     force = cap + (bc4 ? (size_t)kt * tcp * r : 0);
     sflux = force + (size_t)NFORCE * tcp * r;
     bud = sflux + (size_t)NDISS * tcp * r;
@@ -104,7 +104,8 @@ __device__ __forceinline__ void load_lane(Lane<real, LPL, BC4>& lc,
                                           const real* s_coef,
                                           const real* s_cap,
                                           const real* s_force, int j, int KT,
-                                          int tcp, int lane, int K) {
+                                          int tcp, int lane, int K,
+                                          int mol_mode) {
   const real bioT = s_force[0 * tcp + j];
   const real dmul = s_force[1 * tcp + j];
 #pragma unroll
@@ -115,21 +116,64 @@ __device__ __forceinline__ void load_lane(Lane<real, LPL, BC4>& lc,
     const int L = s * 32 + lane;
     const bool act = L < K;
     const int Lc = act ? L : 0;
-    const real phi = s_coef[(0 * KT + Lc) * tcp + j];
-    const real vol = s_coef[(1 * KT + Lc) * tcp + j];
-    const real gb = s_coef[(2 * KT + Lc) * tcp + j];
-    const real gm = s_coef[(3 * KT + Lc) * tcp + j];
-    lc.phi[s] = act ? phi : real(0);
-    lc.vol[s] = act ? vol : real(0);
-    lc.ivol[s] = act ? real(1) / vol : real(0);
-    lc.ap[s] = act ? bioT * gb : real(0);
-    lc.ad[s] = act ? bioT * gb + dmul * gm : real(0);
+    auto row = [&](int r) { return s_coef[(r * KT + Lc) * tcp + j]; };
+    if constexpr (std::is_same<real, double>::value) {
+      // the reference's operands: get_rhs :652-653 and :682-683
+      const double phi = row(0), phi_i = row(1), bf = row(2), dz = row(3);
+      const double len = row(4), mol1 = row(5);
+      const double diff = bioT / 86400.0 / 10000.0 * (1.0 - phi_i) * bf;
+      const double mol = mol_mode == 1 ? mol1 : dmul * phi_i / 86400.0 / 10000.0;
+      lc.phi[s] = act ? phi : 1.0;
+      lc.dz[s] = act ? dz : 1.0;
+      lc.len[s] = act ? len : 1.0;
+      lc.Dp[s] = act ? diff : 0.0;
+      lc.Dd[s] = act ? diff + mol : 0.0;
+      lc.vol[s] = act ? phi * dz : 0.0;
+      lc.ivol[s] = 0.0;
+      lc.ad[s] = 0.0;
+      lc.ap[s] = 0.0;
+    } else {
+      const real phi = row(0), vol = row(1), gb = row(2), gm = row(3);
+      lc.phi[s] = act ? phi : real(0);
+      lc.vol[s] = act ? vol : real(0);
+      lc.ivol[s] = act ? real(1) / vol : real(0);
+      lc.ap[s] = act ? bioT * gb : real(0);
+      lc.ad[s] = act ? bioT * gb + dmul * gm : real(0);
+    }
     cap[s] = (BC4 && act) ? s_cap[Lc * tcp + j] : real(0);
 #pragma unroll
     for (int n = 0; n < NTR; n++)
       C[s][n] = act ? s_conc[(n * KT + Lc) * tcp + j] : real(0);
   }
-  cascade_sources<real, LPL, BC4>(lc, cap, lane, K);
+  if constexpr (std::is_same<real, double>::value)
+    cascade_ref<LPL, BC4>(lc, cap, lane, K);
+  else
+    cascade_sources<real, LPL, BC4>(lc, cap, lane, K);
+}
+
+// The right-hand side used by the steppers: folded FP32 form, or the
+// reference-order FP64 form.
+template <typename real, int LPL, bool BC4>
+__device__ __forceinline__ void rhs_any(const Params<real>& p,
+                                        const Lane<real, LPL, BC4>& lc, int lane,
+                                        int K, const real (&C)[LPL][NTR],
+                                        real (&R)[LPL][NTR], real (&ftop)[NTR],
+                                        real (&dn)[LPL]) {
+  if constexpr (std::is_same<real, double>::value)
+    column_rhs_ref<LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+  else
+    column_rhs<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+}
+
+// c + dt r (one rounding in FP32 via FMA; the reference's multiply then add
+// in FP64) and the sign of c1 - keep c (:121).
+__device__ __forceinline__ float upd(float c, float dt, float r) { return fmaf(dt, r, c); }
+__device__ __forceinline__ double upd(double c, double dt, double r) { return c + dt * r; }
+__device__ __forceinline__ bool below_keep(float c1, float keep, float c) {
+  return fmaf(-keep, c, c1) < 0.0f;
+}
+__device__ __forceinline__ bool below_keep(double c1, double keep, double c) {
+  return c1 - keep * c < 0.0;
 }
 
 // FP64 column inventories of the P and N pools (warp-reduced).
@@ -236,7 +280,7 @@ __device__ __forceinline__ ColResult solve_adaptive(
   Budget<real, LPL, BC4> B;
   B.start(p, lc, C);
   double dt_int = 0.0, dt_red = dt;
-  column_rhs<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+  rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
   while (dt_int < dt) {
     if (res.attempts >= p.max_attempts) { res.capped = 1; break; }
     res.attempts++;
@@ -247,9 +291,9 @@ __device__ __forceinline__ ColResult solve_adaptive(
       const bool act = s * 32 + lane < K;
 #pragma unroll
       for (int n = 0; n < NTR; n++) {
-        const real c1 = fma(dtr, R[s][n], C[s][n]);
-        // sign of c1 - (1+rcm) c, exact for the operands (one rounding)
-        bad |= act && (fma(-p.keep, C[s][n], c1) < real(0));
+        const real c1 = upd(C[s][n], dtr, R[s][n]);
+        // sign of c1 - (1+rcm) c; in FP32 exact for the operands (one FMA)
+        bad |= act && below_keep(c1, p.keep, C[s][n]);
       }
     }
     const bool reject = __any_sync(FULL, bad);
@@ -260,11 +304,11 @@ __device__ __forceinline__ ColResult solve_adaptive(
 #pragma unroll
       for (int s = 0; s < LPL; s++)
 #pragma unroll
-        for (int n = 0; n < NTR; n++) C[s][n] = fma(dtr, R[s][n], C[s][n]);
+        for (int n = 0; n < NTR; n++) C[s][n] = upd(C[s][n], dtr, R[s][n]);
       dt_int = dt_int + dt_red;
       res.accepted++;
       if (dt_red < res.min_dt) res.min_dt = dt_red;
-      if (dt_int < dt) column_rhs<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+      if (dt_int < dt) rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
     }
   }
   B.finish(p, lc, C, bud);
@@ -272,7 +316,8 @@ __device__ __forceinline__ ColResult solve_adaptive(
   return res;
 }
 
-// EULER (:99-102), RUNGE_KUTTA_4 (:142-163), RUNGE_KUTTA_4_38 (:164-185).
+// EULER (:99-102), RUNGE_KUTTA_4 (:142-163), RUNGE_KUTTA_4_38 (:164-185),
+// each stage combined in the reference's operation order.
 template <typename real, int LPL, bool BC4>
 __device__ __forceinline__ ColResult solve_fixed(
     const Params<real>& p, const Lane<real, LPL, BC4>& lc, int lane, int K,
@@ -285,62 +330,58 @@ __device__ __forceinline__ ColResult solve_fixed(
   B.start(p, lc, C);
   const real dtr = (real)dt;
   if (method == 0) {
-    column_rhs<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+    rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
     B.account(p, dt, ftop, dn);
 #pragma unroll
     for (int s = 0; s < LPL; s++)
 #pragma unroll
-      for (int n = 0; n < NTR; n++) C[s][n] = fma(dtr, R[s][n], C[s][n]);
+      for (int n = 0; n < NTR; n++) C[s][n] = upd(C[s][n], dtr, R[s][n]);
   } else {
     const bool rk38 = method == 3;
-    const real third = real(1) / real(3);
-    real Cs[LPL][NTR], acc[LPL][NTR], R0[LPL][NTR];
+    const real third = real(1.0 / 3.0);
+    real Cs[LPL][NTR], R0[LPL][NTR], R1[LPL][NTR], R2[LPL][NTR];
     // stage 1: rhs0 at conc
-    column_rhs<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+    rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R0, ftop, dn);
     B.account(p, rk38 ? dt / 8.0 : dt / 6.0, ftop, dn);
 #pragma unroll
     for (int s = 0; s < LPL; s++)
 #pragma unroll
-      for (int n = 0; n < NTR; n++) {
-        R0[s][n] = R[s][n];
-        acc[s][n] = rk38 ? R[s][n] : real(0.5) * R[s][n];
-        Cs[s][n] = rk38 ? C[s][n] + third * dtr * R[s][n]
-                        : C[s][n] + real(0.5) * dtr * R[s][n];
-      }
+      for (int n = 0; n < NTR; n++)
+        Cs[s][n] = rk38 ? C[s][n] + third * dtr * R0[s][n]
+                        : C[s][n] + real(0.5) * dtr * R0[s][n];
     // stage 2: rhs1 at c1
-    column_rhs<real, LPL, BC4>(p, lc, lane, K, Cs, R, ftop, dn);
+    rhs_any<real, LPL, BC4>(p, lc, lane, K, Cs, R1, ftop, dn);
     B.account(p, rk38 ? 3.0 * dt / 8.0 : dt / 3.0, ftop, dn);
 #pragma unroll
     for (int s = 0; s < LPL; s++)
 #pragma unroll
-      for (int n = 0; n < NTR; n++) {
-        acc[s][n] += rk38 ? real(3) * R[s][n] : R[s][n];
-        Cs[s][n] = rk38 ? C[s][n] + dtr * (R[s][n] - third * R0[s][n])
-                        : C[s][n] + real(0.5) * dtr * R[s][n];
-        R0[s][n] = R0[s][n] - R[s][n];  // rhs0 - rhs1 (3/8 rule, stage 3)
-      }
+      for (int n = 0; n < NTR; n++)
+        Cs[s][n] = rk38 ? C[s][n] + dtr * (R1[s][n] - third * R0[s][n])
+                        : C[s][n] + real(0.5) * dtr * R1[s][n];
     // stage 3: rhs2
-    column_rhs<real, LPL, BC4>(p, lc, lane, K, Cs, R, ftop, dn);
+    rhs_any<real, LPL, BC4>(p, lc, lane, K, Cs, R2, ftop, dn);
     B.account(p, rk38 ? 3.0 * dt / 8.0 : dt / 3.0, ftop, dn);
 #pragma unroll
     for (int s = 0; s < LPL; s++)
 #pragma unroll
-      for (int n = 0; n < NTR; n++) {
-        acc[s][n] += rk38 ? real(3) * R[s][n] : R[s][n];
-        Cs[s][n] = rk38 ? C[s][n] + dtr * (R0[s][n] + R[s][n])
-                        : C[s][n] + dtr * R[s][n];
-      }
+      for (int n = 0; n < NTR; n++)
+        Cs[s][n] = rk38 ? C[s][n] + dtr * (R0[s][n] - R1[s][n] + R2[s][n])
+                        : C[s][n] + dtr * R2[s][n];
     // stage 4: rhs3 and the combination
-    column_rhs<real, LPL, BC4>(p, lc, lane, K, Cs, R, ftop, dn);
+    rhs_any<real, LPL, BC4>(p, lc, lane, K, Cs, R, ftop, dn);
     B.account(p, rk38 ? dt / 8.0 : dt / 6.0, ftop, dn);
 #pragma unroll
     for (int s = 0; s < LPL; s++)
 #pragma unroll
       for (int n = 0; n < NTR; n++) {
         if (rk38)
-          C[s][n] = C[s][n] + dtr * real(1) / real(8) * (acc[s][n] + R[s][n]);
+          C[s][n] = C[s][n] + dtr * real(1) / real(8) *
+                                  (R0[s][n] + real(3) * R1[s][n] +
+                                   real(3) * R2[s][n] + R[s][n]);
         else
-          C[s][n] = C[s][n] + dtr * third * (acc[s][n] + real(0.5) * R[s][n]);
+          C[s][n] = C[s][n] + dtr * third *
+                                  (real(0.5) * R0[s][n] + R1[s][n] + R2[s][n] +
+                                   real(0.5) * R[s][n]);
       }
   }
   B.finish(p, lc, C, bud);
@@ -390,8 +431,9 @@ k_column(ColumnArgs<real> a, Params<real> p) {
     // stage in
     copy_grouped<real, true>(s_conc, a.conc + slot0, NTR, kt, KT, a.kmax, ns,
                              tc, tcp, tid, nthr);
-    copy_grouped<real, true>(s_coef, const_cast<real*>(a.coef) + slot0, NCOEF,
-                             kt, KT, a.kmax, ns, tc, tcp, tid, nthr);
+    copy_grouped<real, true>(s_coef, const_cast<real*>(a.coef) + slot0,
+                             CoefRows<real>::value, kt, KT, a.kmax, ns, tc, tcp,
+                             tid, nthr);
     if (BC4)
       copy_grouped<real, true>(s_cap, const_cast<real*>(a.cap) + slot0, 1, kt,
                                KT, a.kmax, ns, tc, tcp, tid, nthr);
@@ -417,14 +459,14 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       Lane<real, LPL, BC4> lc;
       real C[LPL][NTR];
       load_lane<real, LPL, BC4>(lc, C, s_conc, s_coef, s_cap, s_force, j, KT,
-                                tcp, lane, K);
+                                tcp, lane, K, p.mol_mode);
       real ftop[NTR];
 #pragma unroll
       for (int n = 0; n < NTR; n++) ftop[n] = real(0);
       if (KIND == KIND_RHS) {
         real R[LPL][NTR];
         real dn[LPL];
-        column_rhs<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+        rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
 #pragma unroll
         for (int s = 0; s < LPL; s++) {
           const int Ll = s * 32 + lane;
@@ -507,8 +549,8 @@ __global__ void k_trial(const real* __restrict__ conc, const real* __restrict__ 
     const int k = (int)((i / nslot) % kmax);
     if (k >= kact[slot]) continue;
     const real c = conc[i];
-    const real c1 = fma(dtr, rhs[i], c);
-    bad |= fma(-keep, c, c1) < real(0);
+    const real c1 = upd(c, dtr, rhs[i]);
+    bad |= below_keep(c1, keep, c);
   }
   if (__any_sync(FULL, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
 }
@@ -523,7 +565,7 @@ __global__ void k_accept(real* __restrict__ conc, const real* __restrict__ rhs,
     const int slot = (int)(i % nslot);
     const int k = (int)((i / nslot) % kmax);
     if (k >= kact[slot]) continue;
-    conc[i] = fma(dtr, rhs[i], conc[i]);
+    conc[i] = upd(conc[i], dtr, rhs[i]);
   }
 }
 
@@ -606,6 +648,9 @@ __global__ void k_scatter_flux(const real* __restrict__ sflux,
 //   gm = phi_i / len / 8.64e8 (mode 0) or d0 phi_i / (1 - 2 ln phi_i) / len,
 // len = dz for the surface interface, dzc below (diff3d :777,786) and
 // 8.64e8 = 86400 s * 1e4 cm2/m2 (get_rhs :652,683).
+// The FP64 variant stores the reference's per-cell operands instead:
+//   phi, phi_i, biofac, dz, len, mol (mol = d0 phi_i/(1-2 ln phi_i) computed
+//   on the host for mode 1, so both sides use the same logarithm).
 template <typename real>
 __global__ void k_prep_grid(const double* __restrict__ dz,
                             const double* __restrict__ dzc,
@@ -613,9 +658,34 @@ __global__ void k_prep_grid(const double* __restrict__ dz,
                             const double* __restrict__ phi_i,
                             const double* __restrict__ biofac,
                             const double* __restrict__ cap,
+                            const double* __restrict__ mol,
                             const int* __restrict__ slot_col,
                             real* __restrict__ coef, real* __restrict__ capd,
                             int kmax, int ncol, int nslot, int mode, double d0) {
+  if constexpr (std::is_same<real, double>::value) {
+    const size_t total = (size_t)kmax * nslot;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+         i += (size_t)gridDim.x * blockDim.x) {
+      const int slot = (int)(i % nslot);
+      const int k = (int)(i / nslot);
+      const int col = slot_col[slot];
+      double v[NCOEF64] = {1.0, 1.0, 0.0, 1.0, 1.0, 0.0};
+      double v_cap = 0.0;
+      if (col >= 0) {
+        const size_t c = (size_t)k * ncol + col;
+        v[0] = phi[c];
+        v[1] = phi_i[c];
+        v[2] = biofac[c];
+        v[3] = dz[c];
+        v[4] = (k == 0) ? dz[c] : dzc[(size_t)(k - 1) * ncol + col];
+        v[5] = mol ? mol[c] : 0.0;
+        if (cap) v_cap = cap[c];
+      }
+      for (int r = 0; r < NCOEF64; r++) coef[((size_t)r * kmax + k) * nslot + slot] = v[r];
+      if (capd) capd[i] = v_cap;
+    }
+    return;
+  }
   const size_t total = (size_t)kmax * nslot;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
@@ -631,7 +701,7 @@ __global__ void k_prep_grid(const double* __restrict__ dz,
       v_vol = ph * dz[c];
       v_gb = (1.0 - pi) * biofac[c] / len / 8.64e8;
       if (mode == 1)
-        v_gm = d0 * pi / (1.0 - 2.0 * log(pi)) / len;
+        v_gm = (mol ? mol[c] : d0 * pi / (1.0 - 2.0 * log(pi))) / len;
       else
         v_gm = pi / len / 8.64e8;
       if (cap) v_cap = cap[c];
@@ -807,12 +877,12 @@ template <typename real>
 cudaError_t launch_prep_grid(const double* dz, const double* dzc,
                              const double* phi, const double* phi_i,
                              const double* biofac, const double* cap,
-                             const int* slot_col, real* coef, real* capd,
-                             int kmax, int ncol, int nslot, int mode, double d0,
-                             int sms, cudaStream_t st) {
+                             const double* mol, const int* slot_col, real* coef,
+                             real* capd, int kmax, int ncol, int nslot, int mode,
+                             double d0, int sms, cudaStream_t st) {
   const size_t total = (size_t)kmax * nslot;
   k_prep_grid<real><<<grid_for(total, 256, sms), 256, 0, st>>>(
-      dz, dzc, phi, phi_i, biofac, cap, slot_col, coef, capd, kmax, ncol,
+      dz, dzc, phi, phi_i, biofac, cap, mol, slot_col, coef, capd, kmax, ncol,
       nslot, mode, d0);
   return cudaGetLastError();
 }
@@ -852,8 +922,8 @@ cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
                                                  int, int, cudaStream_t);       \
   template cudaError_t launch_prep_grid<real>(                                  \
       const double*, const double*, const double*, const double*,               \
-      const double*, const double*, const int*, real*, real*, int, int, int,    \
-      int, double, int, cudaStream_t);                                          \
+      const double*, const double*, const double*, const int*, real*, real*,    \
+      int, int, int, int, double, int, cudaStream_t);                           \
   template cudaError_t launch_prep_force<real>(const double*, const double*,    \
                                                const int*, real*, int, int,     \
                                                double, double, int, int, int,   \

@@ -11,7 +11,7 @@ namespace sed {
 enum : int { KIND_ADAPT = 0, KIND_FIXED = 1, KIND_RHS = 2 };
 
 // Arguments of the tile kernel.  Device layouts (slot = compacted column):
-//   conc  [NTR][kmax][nslot]     coef  [NCOEF][kmax][nslot]
+//   conc  [NTR][kmax][nslot]     coef  [CoefRows][kmax][nslot]
 //   cap   [kmax][nslot] (BcUp 4) force [NFORCE][nslot]
 //   sflux [NDISS][nslot]         budget[4][nslot] (FP64)
 template <typename real>
@@ -78,8 +78,8 @@ template <typename real>
 cudaError_t launch_prep_grid(const double* dz, const double* dzc,
                              const double* phi, const double* phi_i,
                              const double* biofac, const double* cap,
-                             const int* slot_col, real* coef, real* capd,
-                             int kmax, int ncol, int nslot, int mode,
+                             const double* mol, const int* slot_col, real* coef,
+                             real* capd, int kmax, int ncol, int nslot, int mode,
                              double d0, int sms, cudaStream_t st);
 
 template <typename real>

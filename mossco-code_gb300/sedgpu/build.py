@@ -22,10 +22,16 @@ LIB_NAME = "libsedgpu.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 
 SOURCES = ["sed_kernels_f32.cu", "sed_kernels_f64.cu", "sed_capi.cu"]
+# The FP64 kernels evaluate the reference's arithmetic operation by
+# operation: no multiply-add contraction.
+EXTRA_FLAGS = {"sed_kernels_f64.cu": ["-fmad=false"]}
 HEADERS = ["sed_device.cuh", "sed_kernels.cuh", "sed_launch.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no multiply-add contraction either (aarch64 g++ contracts by
+# default), so host-side FP64 forcing rows match the CPU restatement's
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-fno-strict-aliasing"]
+              "-Xcompiler", "-fno-strict-aliasing",
+              "-Xcompiler", "-ffp-contract=off"]
 
 
 def nvcc() -> str:
@@ -60,7 +66,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src):
         obj = os.path.join(BUILD_DIR, src.replace(".cu", f".{tag}.o"))
-        cmd = [cc, *ARCH, *NVCC_FLAGS, "-I", INCLUDE, "-c",
+        cmd = [cc, *ARCH, *NVCC_FLAGS, *EXTRA_FLAGS.get(src, []), "-I", INCLUDE, "-c",
                os.path.join(CSRC, src), "-o", obj]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")

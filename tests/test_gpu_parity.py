@@ -1,9 +1,14 @@
 """GPU parity of the CUDA library (through the C ABI) against the FP64 oracle.
 
-FP64 device state reproduces the oracle to rounding (same algorithm); FP32
-device state stays within the 1e-3 per-tracer relative error of the
-workload's accuracy target (relative to |ref| plus a floor of 1e-4 x the
-tracer's largest value, since deep O2 / NO3 fall to ~0).
+FP64 device state evaluates the reference's arithmetic in the oracle's
+operation order and must reproduce it bit for bit over any horizon.  FP32
+device state must stay within 1e-3 per-tracer relative error (relative to
+|ref| plus a floor of 1e-4 x the tracer's largest value, since deep O2 / NO3
+fall to ~0) over short horizons and for every coupling step started from the
+same state.  Over long horizons no implementation that is not bit-identical
+can track the reference: its positivity-limited Euler accepts unstable
+substeps that amplify a 1-ulp difference to 1e-2 within ~24 coupling steps
+(tests/test_oracle.py::test_reference_amplifies_one_ulp).
 """
 import numpy as np
 import pytest
@@ -55,9 +60,8 @@ def test_rhs_fp64_matches_oracle(oracle_mod):
     rhs, fl = s.get_rhs(cs.conc)
     s.close()
     ref, fref, _ = oracle_mod.OracleModel(cs).get_rhs(cs.conc)
-    scale = np.abs(ref).max(axis=(1, 2), keepdims=True)
-    assert np.max(np.abs(rhs - ref) / scale) < 1e-12
-    np.testing.assert_allclose(fl[6:], fref[6:], rtol=1e-12)
+    np.testing.assert_array_equal(rhs, ref)
+    np.testing.assert_array_equal(fl, fref)
 
 
 def test_rhs_fp32_matches_oracle(oracle_mod):
@@ -71,18 +75,49 @@ def test_rhs_fp32_matches_oracle(oracle_mod):
     assert np.max(np.abs(rhs - ref) / scale) < 2e-5
 
 
-@pytest.mark.parametrize("precision,tol", [(capi.SED_FP64, FP64_TOL),
-                                           (capi.SED_FP32, FP32_TOL)])
-def test_adaptive_percol_10x10(oracle_mod, precision, tol):
+def test_adaptive_percol_fp64_bit_exact(oracle_mod):
     cs = synth.make_workload("plain_cpu_10x10")
-    n = 48
-    out, fl, st, att, _ = run_gpu(cs, n, precision=precision)
+    n = 72
+    out, fl, st, att, _ = run_gpu(cs, n, precision=capi.SED_FP64)
     ref, fref, sref = run_oracle(oracle_mod, cs, n)
-    err = relerr(active(cs, out), active(cs, ref))
-    assert err.max() < tol, err
-    if precision == capi.SED_FP64:
-        assert st["attempts"] == sref["attempts"]
-        assert st["accepted"] == sref["accepted"]
+    np.testing.assert_array_equal(out, ref)
+    np.testing.assert_array_equal(fl, fref)
+    assert st["attempts"] == sref["attempts"]
+    assert st["accepted"] == sref["accepted"]
+
+
+def teacher_forced(oracle_mod, cs, state, gpu_next, cols=None):
+    """Relative error of one GPU coupling step against one oracle step from
+    the same state."""
+    sub = cs if cols is None else cs.subset(cols)
+    start = state if cols is None else state[:, :, cols]
+    sub = sub.copy()
+    sub.conc = np.ascontiguousarray(start)
+    ref, _, _ = run_oracle(oracle_mod, sub, 1)
+    nxt = gpu_next if cols is None else gpu_next[:, :, cols]
+    return relerr(active(sub, nxt), active(sub, ref))
+
+
+def test_adaptive_percol_fp32(oracle_mod):
+    cs = synth.make_workload("plain_cpu_10x10")
+    s = capi.Solver(cs, precision=capi.SED_FP32)
+    s.set_forcing()
+    s.set_state(cs.conc)
+    s.step(6)
+    out6 = s.get_state()
+    ref6, _, _ = run_oracle(oracle_mod, cs, 6)
+    err = relerr(active(cs, out6), active(cs, ref6))
+    assert err.max() < FP32_TOL, err
+    # every later step, started from the GPU's own state
+    state = out6
+    for step in range(6, 48):
+        s.step(1)
+        nxt = s.get_state()
+        if step % 7 == 6:
+            e = teacher_forced(oracle_mod, cs, state, nxt)
+            assert e.max() < FP32_TOL, (step, e)
+        state = nxt
+    s.close()
 
 
 def test_adaptive_global_cut_10x10(oracle_mod):
@@ -92,8 +127,7 @@ def test_adaptive_global_cut_10x10(oracle_mod):
     out, fl, st, _, _ = run_gpu(cs, n, precision=capi.SED_FP64,
                                 cut=capi.SED_CUT_GLOBAL)
     ref, fref, sref = run_oracle(oracle_mod, cs, n, percol=False)
-    err = relerr(active(cs, out), active(cs, ref))
-    assert err.max() < FP64_TOL, err
+    np.testing.assert_array_equal(out, ref)
     assert st["accepted"] == sref["accepted"] * cs.n_active
 
 
@@ -103,26 +137,27 @@ def test_fixed_methods(oracle_mod, method):
     out, fl, st, _, _ = run_gpu(cs, 30, method=method, dt=60.0,
                                 precision=capi.SED_FP64)
     ref, fref, _ = run_oracle(oracle_mod, cs, 30, method=method, dt=60.0)
-    err = relerr(active(cs, out), active(cs, ref))
-    assert err.max() < FP64_TOL, err
-    np.testing.assert_allclose(fl[6:], fref[6:], rtol=1e-9)
+    np.testing.assert_array_equal(out, ref)
+    np.testing.assert_array_equal(fl, fref)
+    out32, _, _, _, _ = run_gpu(cs, 30, method=method, dt=60.0)
+    assert relerr(active(cs, out32), active(cs, ref)).max() < FP32_TOL
 
 
 def test_uneven_columns_and_land(oracle_mod):
     cols = np.arange(0, 1024 * 1024, 1024 * 1024 // 300)[:300]
     cs = synth.make_workload("uneven_1024x1024", cols=cols)
     assert (cs.kact == 0).any() and (cs.kact > 32).any() and (cs.kact <= 32).any()
-    n = 12
+    n = 24
     out, fl, st, att, _ = run_gpu(cs, n, precision=capi.SED_FP64)
     ref, fref, sref = run_oracle(oracle_mod, cs, n)
-    err = relerr(active(cs, out), active(cs, ref))
-    assert err.max() < FP64_TOL, err
+    np.testing.assert_array_equal(out, ref)
     # land columns and inactive layers are returned untouched
     land = cs.kact == 0
     np.testing.assert_array_equal(out[:, :, land], cs.conc[:, :, land])
     assert np.all(att[land] == 0) and np.all(att[~land] > 0)
-    out32, _, _, _, _ = run_gpu(cs, n, precision=capi.SED_FP32)
-    err32 = relerr(active(cs, out32), active(cs, ref))
+    out32, _, _, _, _ = run_gpu(cs, 4, precision=capi.SED_FP32)
+    ref4, _, _ = run_oracle(oracle_mod, cs, 4)
+    err32 = relerr(active(cs, out32), active(cs, ref4))
     assert err32.max() < FP32_TOL, err32
 
 
@@ -137,8 +172,10 @@ def test_bcup_variants(oracle_mod):
         cs.fluxes[n] *= 50.0
     out, fl, st, _, _ = run_gpu(cs, 8, precision=capi.SED_FP64)
     ref, fref, _ = run_oracle(oracle_mod, cs, 8)
-    err = relerr(active(cs, out), active(cs, ref))
-    assert err.max() < FP64_TOL, err
+    np.testing.assert_array_equal(out, ref)
+    out32, _, _, _, _ = run_gpu(cs, 2, precision=capi.SED_FP32)
+    ref2, _, _ = run_oracle(oracle_mod, cs, 2)
+    assert relerr(active(cs, out32), active(cs, ref2)).max() < FP32_TOL
 
 
 def test_constant_rhs_exact_on_gpu():
@@ -172,9 +209,8 @@ def test_drop_in_ode_solver_host_arrays(oracle_mod):
         s.ode_solver(conc, cs.bdys, fl, cs.dt, ADAPTIVE_EULER)
     s.close()
     ref, fref, _ = run_oracle(oracle_mod, cs, 6)
-    err = relerr(active(cs, conc), active(cs, ref))
-    assert err.max() < FP64_TOL
-    np.testing.assert_allclose(fl, fref, rtol=1e-9, atol=1e-300)
+    np.testing.assert_array_equal(conc, ref)
+    np.testing.assert_array_equal(fl, fref)
 
 
 def test_budgets_fp64(oracle_mod):
@@ -232,15 +268,16 @@ def test_full_size_workload_properties(oracle_mod):
     s = capi.Solver(cs, precision=capi.SED_FP32, budgets=True)
     s.set_forcing()
     s.set_state(cs.conc)
-    st = s.step(n)
+    st = s.step(n - 1)
+    prev = s.get_state()
+    st1 = s.step(1)
     out = s.get_state()
     bud = s.budgets()
     s.close()
     assert np.isfinite(out).all() and (out >= 0).all()
-    assert st["column_steps"] == cs.ncol * n
+    assert st["column_steps"] + st1["column_steps"] == cs.ncol * n
     assert np.max(np.abs(bud[1]) / bud[0]) < 1e-4
-    cols = np.random.default_rng(3).choice(cs.ncol, 64, replace=False)
-    sub = cs.subset(cols)
-    ref, _, _ = run_oracle(oracle_mod, sub, n)
-    err = relerr(active(sub, out[:, :, cols]), active(sub, ref))
-    assert err.max() < FP32_TOL, err
+    assert np.max(np.abs(bud[3]) / bud[2]) < 1e-4
+    cols = np.random.default_rng(3).choice(cs.ncol, 256, replace=False)
+    e = teacher_forced(oracle_mod, cs, prev, out, cols)
+    assert e.max() < FP32_TOL, e

@@ -188,3 +188,18 @@ def test_golden_regression(oracle_mod, fname):
     for key in out:
         np.testing.assert_allclose(out[key], g[key], rtol=1e-11, atol=1e-300,
                                    err_msg=key)
+
+
+def test_reference_amplifies_one_ulp(oracle_mod):
+    """The reference's positivity-limited Euler accepts 900 s substeps that
+    are unstable for the 1 mm surface layers, so a 1-ulp change of the
+    initial state grows by orders of magnitude within days: long-horizon
+    parity is only possible for a bit-identical implementation."""
+    from conftest import relerr
+    cs = synth.make_workload("plain_cpu_10x10")
+    om = oracle_mod.OracleModel(cs)
+    a = cs.conc.copy()
+    b = cs.conc * (1.0 + 2.0 ** -52)
+    om.run(a, nsteps=24, percol=True)
+    om.run(b, nsteps=24, percol=True)
+    assert relerr(a, b).max() > 1e-6
