@@ -69,6 +69,10 @@ typedef struct sed_params {
   /* type_rhs_driver scalars (solver_library.F90:40-41) */
   double dt_min;              /* s */
   double relative_change_min; /* e.g. -0.9 */
+  double atol;                /* absolute tolerance of the positivity test:
+                                 a substep is rejected if c1 - (1+rcm) c <
+                                 -atol in any cell (0: the reference's test,
+                                 solver_library.F90:121) */
   int max_attempts;           /* adaptive attempts per column-step, > 0 */
   int cut_scope;              /* SED_CUT_PER_COLUMN or SED_CUT_GLOBAL */
   /* OMEXDIA+P, per-day units (examples/standalone/omexdia_p/fabm_sed.nml) */

@@ -138,6 +138,7 @@ Params<real> make_params(const sed_params& s) {
   p.nh3den = (real)(1.0 + s.NH3Ads);
   p.mol_mode = s.mol_diff_mode;
   p.keep = (real)(1.0 + s.relative_change_min);
+  p.natol = (real)(-s.atol);
   for (int n = 0; n < NTR; n++) p.minimum[n] = (real)s.minimum[n];
   p.dt_min = s.dt_min;
   p.bcup_d = s.bcup_dissolved;
@@ -155,6 +156,7 @@ int check_params(sed_handle* h, const sed_params& p) {
   if (p.mol_diff_mode != 0 && p.mol_diff_mode != 1)
     return h->fail(SED_E_ARG, "mol_diff_mode must be 0 or 1");
   if (p.max_attempts <= 0) return h->fail(SED_E_ARG, "max_attempts must be > 0");
+  if (!(p.atol >= 0.0)) return h->fail(SED_E_ARG, "atol must be >= 0");
   if (p.precision != SED_FP32 && p.precision != SED_FP64)
     return h->fail(SED_E_ARG, "precision must be SED_FP32 or SED_FP64");
   if (p.cut_scope != SED_CUT_PER_COLUMN && p.cut_scope != SED_CUT_GLOBAL)
@@ -195,11 +197,32 @@ ColumnArgs<real> column_args(sed_handle* h, const Bin& b, int bin_index,
   return a;
 }
 
+// Cut levels of the adaptive loop for a coupling step dt: mstop is the
+// first m with dt/4^m <= dt_min (cuts stop there, solver_library.F90:126).
+// The partial sums dt_int = sum dt/4^m are then multiples of dt/4^mstop; if
+// dt's significand has b bits and b + 2 mstop <= 53 every one of them is
+// exact in FP64, so integer ticks take the reference's decisions exactly.
+template <typename real>
+void set_clock(Params<real>& p, double dt, double dt_min) {
+  int mstop = 0;
+  double d = dt;
+  while (!(d <= dt_min) && mstop < 64) { d *= 0.25; mstop++; }
+  int e = 0;
+  const double mant = std::frexp(dt, &e);
+  unsigned long long sig = (unsigned long long)std::ldexp(mant, 53);
+  int tz = 0;
+  while (sig && !(sig & 1ull)) { sig >>= 1; tz++; }
+  const int bits = 53 - tz;
+  p.mstop = mstop;
+  p.ticks = (mstop <= 31 && bits + 2 * mstop <= 53) ? 1 : 0;
+}
+
 // Enqueue the tile kernels of every depth class (one coupling step, or one
 // right-hand side for KIND_RHS).
 template <typename real>
 int enqueue_columns(sed_handle* h, double dt, int method, int kind) {
-  const Params<real> p = make_params<real>(h->prm);
+  Params<real> p = make_params<real>(h->prm);
+  set_clock(p, dt, h->prm.dt_min);
   CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
   for (int b = 0; b < h->nbins; b++) {
     const Bin& bin = h->bins[b];
@@ -303,8 +326,8 @@ int step_global(sed_handle* h, double dt) {
     }
     CK(cudaMemsetAsync(h->d_flag.p, 0, sizeof(int), h->stream), "flag reset");
     CK(launch_trial<real>(h->d_conc.as<real>(), h->d_rhs.as<real>(), h->d_kact.as<int>(),
-                          h->nslot, h->kmax, (real)dt_red, p.keep, h->d_flag.as<int>(),
-                          h->sms, h->stream), "trial launch");
+                          h->nslot, h->kmax, (real)dt_red, p.keep, p.natol,
+                          h->d_flag.as<int>(), h->sms, h->stream), "trial launch");
     h->launches++;
     CK(cudaMemcpyAsync(h->h_flag, h->d_flag.p, sizeof(int), cudaMemcpyDeviceToHost,
                        h->stream), "flag fetch");

@@ -48,8 +48,11 @@ struct Params {
   real ksO2oxic, kinO2denit, ksNO3denit, kinO2anox, kinNO3anox, ksO2nitri,
       ksO2oduox, PAdsODU, nh3fac, nh3den;
   real keep;          // 1 + relative_change_min
+  real natol;         // -atol: reject if c1 - keep c < natol
   real minimum[NTR];  // clamp of the component epilogue
   double dt_min;
+  int mstop;          // first cut level m with dt/4^m <= dt_min
+  int ticks;          // 1: integer time ticks reproduce the FP64 sums
   int bcup_d;         // 1 flux, 2 concentration, 3 zero
   int mol_mode;       // 0 (diffusivity + 0.035 T) phi_i, 1 tortuosity
   int max_attempts;
@@ -160,7 +163,11 @@ struct Lane {
   real ad[LPL];    // dissolved interface conductance D/len (upper interface)
   real ap[LPL];    // particulate interface conductance
   real vol[LPL];   // phi dz (budgets)
-  real bnd[NTR];   // per tracer: bottom-water value or downward surface flux
+  // per tracer: bottom-water value or downward surface flux, read from the
+  // shared-memory forcing rows (only lane 0 uses them)
+  const real* bnd_s;
+  int bnd_stride;
+  __device__ __forceinline__ real bnd(int n) const { return bnd_s[n * bnd_stride]; }
   real src[BC4 ? LPL : 1][BC4 ? NPART : 1];  // capped-flux cascade sources
   // FP64 reference-order path (diff3d's own operands)
   real dz[LPL], len[LPL], Dp[LPL], Dd[LPL];
@@ -191,9 +198,9 @@ __device__ __forceinline__ void column_rhs(const Params<real>& p,
     for (int s = 0; s < LPL; s++) F[s] = (part ? lc.ap[s] : lc.ad[s]) * (vm[s] - v[s]);
     if (lane == 0) {
       real f0;
-      if (part) f0 = lc.bnd[n];
-      else if (p.bcup_d == 2) f0 = lc.ad[0] * (lc.bnd[n] - v[0]);
-      else if (p.bcup_d == 1) f0 = lc.bnd[n];
+      if (part) f0 = lc.bnd(n);
+      else if (p.bcup_d == 2) f0 = lc.ad[0] * (lc.bnd(n) - v[0]);
+      else if (p.bcup_d == 1) f0 = lc.bnd(n);
       else f0 = real(0);
       F[0] = f0;
       ftop[n] = f0;
@@ -247,7 +254,7 @@ __device__ __forceinline__ void cascade_sources(Lane<real, LPL, BC4>& lc,
   }
 #pragma unroll
   for (int n = 0; n < NPART; n++) {
-    const real fup = lc.bnd[n];
+    const real fup = lc.bnd(n);
     real rest[LPL];  // rest after layer L: fup - sum_{j<=L} cap_j
 #pragma unroll
     for (int s = 0; s < LPL; s++) rest[s] = fup - pre[s];
@@ -354,9 +361,9 @@ __device__ __forceinline__ void column_rhs_ref(const Params<double>& p,
     // :782-803 upper boundary
     if (lane == 0) {
       double f0;
-      if (part) f0 = lc.bnd[n];
-      else if (p.bcup_d == 2) f0 = -lc.Dd[0] * (v[0] - lc.bnd[n]) / lc.dz[0];
-      else if (p.bcup_d == 1) f0 = lc.bnd[n];
+      if (part) f0 = lc.bnd(n);
+      else if (p.bcup_d == 2) f0 = -lc.Dd[0] * (v[0] - lc.bnd(n)) / lc.dz[0];
+      else if (p.bcup_d == 1) f0 = lc.bnd(n);
       else f0 = 0.0;
       F[0] = f0;
     }
@@ -401,7 +408,7 @@ __device__ __forceinline__ void cascade_ref(Lane<double, LPL, BC4>& lc,
       lc.ext_a[BC4 ? s : 0][BC4 ? n : 0] = 0.0;
       lc.ext_b[BC4 ? s : 0][BC4 ? n : 0] = 0.0;
     }
-    const double fup = lc.bnd[n];
+    const double fup = lc.bnd(n);
     double rest = fup - __shfl_sync(FULL, cap[0], 0);
     int k = 1;
     while (rest > 0.0 && k <= K - 1) {

@@ -109,7 +109,10 @@ __device__ __forceinline__ void load_lane(Lane<real, LPL, BC4>& lc,
   const real bioT = s_force[0 * tcp + j];
   const real dmul = s_force[1 * tcp + j];
 #pragma unroll
-  for (int n = 0; n < NTR; n++) lc.bnd[n] = s_force[(2 + n) * tcp + j];
+  for (int n = 0; n < 1; n++) {
+    lc.bnd_s = s_force + 2 * tcp + j;
+    lc.bnd_stride = tcp;
+  }
   real cap[LPL];
 #pragma unroll
   for (int s = 0; s < LPL; s++) {
@@ -169,11 +172,11 @@ __device__ __forceinline__ void rhs_any(const Params<real>& p,
 // in FP64) and the sign of c1 - keep c (:121).
 __device__ __forceinline__ float upd(float c, float dt, float r) { return fmaf(dt, r, c); }
 __device__ __forceinline__ double upd(double c, double dt, double r) { return c + dt * r; }
-__device__ __forceinline__ bool below_keep(float c1, float keep, float c) {
-  return fmaf(-keep, c, c1) < 0.0f;
+__device__ __forceinline__ bool below_keep(float c1, float keep, float c, float natol) {
+  return fmaf(-keep, c, c1) < natol;
 }
-__device__ __forceinline__ bool below_keep(double c1, double keep, double c) {
-  return c1 - keep * c < 0.0;
+__device__ __forceinline__ bool below_keep(double c1, double keep, double c, double natol) {
+  return c1 - keep * c < natol;
 }
 
 // FP64 column inventories of the P and N pools (warp-reduced).
@@ -201,30 +204,48 @@ struct ColResult {
   double min_dt;
 };
 
-// Budget bookkeeping of one column over one coupling step.
+// Compensated running sum (Knuth's TwoSum): FP32 operations carrying the
+// rounding error along, so the per-substep surface-flux integral needs no
+// FP64 arithmetic inside the substep loop.
+template <typename real>
+struct CompSum {
+  real s, c;
+  __device__ __forceinline__ void zero() { s = real(0); c = real(0); }
+  __device__ __forceinline__ void add(real x) {
+    const real t = s + x;
+    const real bp = t - s;
+    c += (s - (t - bp)) + (x - bp);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+// Budget bookkeeping of one column over one coupling step: FP64 column
+// inventories of the P and N pools at the start and end of the step (warp
+// reductions), the surface inflow of both pools and the N lost to
+// denitrification (0.8 mol N per mol C) accumulated per substep.
 template <typename real, int LPL, bool BC4>
 struct Budget {
-  double inP, inN, inv0P, inv0N;
+  double inv0P, inv0N;
+  CompSum<real> inP, inN;
   real n2[LPL];
   __device__ __forceinline__ void start(const Params<real>& p,
                                         const Lane<real, LPL, BC4>& lc,
                                         const real (&C)[LPL][NTR]) {
-    inP = 0.0; inN = 0.0; inv0P = 0.0; inv0N = 0.0;
+    inP.zero(); inN.zero(); inv0P = 0.0; inv0N = 0.0;
 #pragma unroll
     for (int s = 0; s < LPL; s++) n2[s] = real(0);
     if (p.budgets) inventories<real, LPL, BC4>(lc, C, inv0P, inv0N);
   }
   // one right-hand side entering the update with weight w (seconds)
-  __device__ __forceinline__ void account(const Params<real>& p, double w,
+  __device__ __forceinline__ void account(const Params<real>& p, real w,
                                           const real (&ftop)[NTR],
                                           const real (&dn)[LPL]) {
     if (!p.budgets) return;
-    inP += w * ((double)ftop[T_FDETP] + (double)ftop[T_ADSP] + (double)ftop[T_PO4]);
-    inN += w * ((double)ftop[T_FDETN] + (double)ftop[T_SDETN] +
-                (double)ftop[T_NO3] + (double)ftop[T_NH4]);
-    const real wr = (real)w;
+    inP.add(w * (ftop[T_FDETP] + ftop[T_ADSP] + ftop[T_PO4]));
+    inN.add(w * (ftop[T_FDETN] + ftop[T_SDETN] + ftop[T_NO3] + ftop[T_NH4]));
 #pragma unroll
-    for (int s = 0; s < LPL; s++) n2[s] += wr * real(0.8) * dn[s];
+    for (int s = 0; s < LPL; s++) n2[s] += w * real(0.8) * dn[s];
   }
   __device__ __forceinline__ void finish(const Params<real>& p,
                                          const Lane<real, LPL, BC4>& lc,
@@ -237,8 +258,8 @@ struct Budget {
 #pragma unroll
     for (int s = 0; s < LPL; s++) loss += (double)lc.vol[s] * (double)n2[s];
     loss = warp_sum(loss);
-    const double fP = __shfl_sync(FULL, inP, 0);
-    const double fN = __shfl_sync(FULL, inN, 0);
+    const double fP = __shfl_sync(FULL, inP.value(), 0);
+    const double fN = __shfl_sync(FULL, inN.value(), 0);
     bud[0] = inv1P;
     bud[1] = inv1P - inv0P - fP;
     bud[2] = inv1N;
@@ -270,7 +291,13 @@ __device__ __forceinline__ int epilogue(const Params<real>& p, int lane, int K,
 // ADAPTIVE_EULER (solver_library.F90:104-140) on one column, cut decided by
 // the column's own cells.  A rejected attempt re-evaluates get_rhs at the
 // same state in the reference, which yields the same rhs, so it is reused.
-template <typename real, int LPL, bool BC4>
+//
+// Time bookkeeping: the reference sums dt_int += dt_red in FP64 with
+// dt_red = dt/4^m.  When the host has shown that every such partial sum is
+// exact in FP64 (p.ticks), the same decisions are taken with integer ticks
+// of dt/4^mstop (mstop = first level with dt/4^m <= dt_min), which keeps the
+// loop off the FP64 pipe; otherwise the FP64 sums are kept.
+template <typename real, int LPL, bool BC4, bool TICKS>
 __device__ __forceinline__ ColResult solve_adaptive(
     const Params<real>& p, const Lane<real, LPL, BC4>& lc, int lane, int K,
     real (&C)[LPL][NTR], real (&ftop)[NTR], double dt, double (&bud)[4]) {
@@ -279,12 +306,15 @@ __device__ __forceinline__ ColResult solve_adaptive(
   ColResult res{0, 0, 0, 0, 1e300};
   Budget<real, LPL, BC4> B;
   B.start(p, lc, C);
+  unsigned long long t = 0, T = 0, inc = 0;
   double dt_int = 0.0, dt_red = dt;
+  if (TICKS) { T = 1ull << (2 * p.mstop); inc = T; }
+  int m = 0, mmax = -1;
+  real dtr = (real)dt;
   rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
-  while (dt_int < dt) {
+  while (TICKS ? (t < T) : (dt_int < dt)) {
     if (res.attempts >= p.max_attempts) { res.capped = 1; break; }
     res.attempts++;
-    const real dtr = (real)dt_red;
     bool bad = false;
 #pragma unroll
     for (int s = 0; s < LPL; s++) {
@@ -293,24 +323,31 @@ __device__ __forceinline__ ColResult solve_adaptive(
       for (int n = 0; n < NTR; n++) {
         const real c1 = upd(C[s][n], dtr, R[s][n]);
         // sign of c1 - (1+rcm) c; in FP32 exact for the operands (one FMA)
-        bad |= act && below_keep(c1, p.keep, C[s][n]);
+        bad |= act && below_keep(c1, p.keep, C[s][n], p.natol);
       }
     }
     const bool reject = __any_sync(FULL, bad);
-    if (reject && dt_red > p.dt_min) {
-      dt_red = dt_red * 0.25;
+    const bool can_cut = TICKS ? (m < p.mstop) : (dt_red > p.dt_min);
+    if (reject && can_cut) {
+      m++;
+      dtr = dtr * real(0.25);
+      if (TICKS) inc >>= 2;
+      else dt_red = dt_red * 0.25;
     } else {
-      B.account(p, dt_red, ftop, dn);
+      B.account(p, dtr, ftop, dn);
 #pragma unroll
       for (int s = 0; s < LPL; s++)
 #pragma unroll
         for (int n = 0; n < NTR; n++) C[s][n] = upd(C[s][n], dtr, R[s][n]);
-      dt_int = dt_int + dt_red;
+      if (TICKS) t += inc;
+      else dt_int = dt_int + dt_red;
       res.accepted++;
-      if (dt_red < res.min_dt) res.min_dt = dt_red;
-      if (dt_int < dt) rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+      mmax = m > mmax ? m : mmax;
+      if (TICKS ? (t < T) : (dt_int < dt))
+        rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
     }
   }
+  if (mmax >= 0) res.min_dt = ldexp(dt, -2 * mmax);
   B.finish(p, lc, C, bud);
   res.nan = epilogue<real, LPL>(p, lane, K, C);
   return res;
@@ -331,7 +368,7 @@ __device__ __forceinline__ ColResult solve_fixed(
   const real dtr = (real)dt;
   if (method == 0) {
     rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
-    B.account(p, dt, ftop, dn);
+    B.account(p, dtr, ftop, dn);
 #pragma unroll
     for (int s = 0; s < LPL; s++)
 #pragma unroll
@@ -342,7 +379,7 @@ __device__ __forceinline__ ColResult solve_fixed(
     real Cs[LPL][NTR], R0[LPL][NTR], R1[LPL][NTR], R2[LPL][NTR];
     // stage 1: rhs0 at conc
     rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R0, ftop, dn);
-    B.account(p, rk38 ? dt / 8.0 : dt / 6.0, ftop, dn);
+    B.account(p, (real)(rk38 ? dt / 8.0 : dt / 6.0), ftop, dn);
 #pragma unroll
     for (int s = 0; s < LPL; s++)
 #pragma unroll
@@ -351,7 +388,7 @@ __device__ __forceinline__ ColResult solve_fixed(
                         : C[s][n] + real(0.5) * dtr * R0[s][n];
     // stage 2: rhs1 at c1
     rhs_any<real, LPL, BC4>(p, lc, lane, K, Cs, R1, ftop, dn);
-    B.account(p, rk38 ? 3.0 * dt / 8.0 : dt / 3.0, ftop, dn);
+    B.account(p, (real)(rk38 ? 3.0 * dt / 8.0 : dt / 3.0), ftop, dn);
 #pragma unroll
     for (int s = 0; s < LPL; s++)
 #pragma unroll
@@ -360,7 +397,7 @@ __device__ __forceinline__ ColResult solve_fixed(
                         : C[s][n] + real(0.5) * dtr * R1[s][n];
     // stage 3: rhs2
     rhs_any<real, LPL, BC4>(p, lc, lane, K, Cs, R2, ftop, dn);
-    B.account(p, rk38 ? 3.0 * dt / 8.0 : dt / 3.0, ftop, dn);
+    B.account(p, (real)(rk38 ? 3.0 * dt / 8.0 : dt / 3.0), ftop, dn);
 #pragma unroll
     for (int s = 0; s < LPL; s++)
 #pragma unroll
@@ -369,7 +406,7 @@ __device__ __forceinline__ ColResult solve_fixed(
                         : C[s][n] + dtr * R2[s][n];
     // stage 4: rhs3 and the combination
     rhs_any<real, LPL, BC4>(p, lc, lane, K, Cs, R, ftop, dn);
-    B.account(p, rk38 ? dt / 8.0 : dt / 6.0, ftop, dn);
+    B.account(p, (real)(rk38 ? dt / 8.0 : dt / 6.0), ftop, dn);
 #pragma unroll
     for (int s = 0; s < LPL; s++)
 #pragma unroll
@@ -392,8 +429,16 @@ __device__ __forceinline__ ColResult solve_fixed(
 // ---------------------------------------------------------------------------
 // KIND_ADAPT / KIND_FIXED: one coupling step; KIND_RHS: one right-hand side
 // written to a.out.
+// Resident blocks per SM the register allocation is sized for: three
+// 256-thread blocks for FP32 one-layer-per-lane columns (80 registers), two
+// for two layers per lane, one for the FP64 path.
+template <typename real, int LPL>
+struct MinBlocks {
+  static constexpr int value = sizeof(real) == 4 ? (LPL == 1 ? 3 : 2) : 1;
+};
+
 template <typename real, int LPL, bool BC4, int KIND>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, (MinBlocks<real, LPL>::value))
 k_column(ColumnArgs<real> a, Params<real> p) {
   constexpr int mode = KIND == KIND_RHS ? 1 : 0;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -484,7 +529,8 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       double bud[4] = {0.0, 0.0, 0.0, 0.0};
       ColResult r;
       if (KIND == KIND_ADAPT)
-        r = solve_adaptive<real, LPL, BC4>(p, lc, lane, K, C, ftop, a.dt, bud);
+        r = p.ticks ? solve_adaptive<real, LPL, BC4, true>(p, lc, lane, K, C, ftop, a.dt, bud)
+                    : solve_adaptive<real, LPL, BC4, false>(p, lc, lane, K, C, ftop, a.dt, bud);
       else
         r = solve_fixed<real, LPL, BC4>(p, lc, lane, K, C, ftop, a.dt, a.method,
                                         bud);
@@ -540,7 +586,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
 template <typename real>
 __global__ void k_trial(const real* __restrict__ conc, const real* __restrict__ rhs,
                         const int* __restrict__ kact, int nslot, int kmax,
-                        real dtr, real keep, int* flag) {
+                        real dtr, real keep, real natol, int* flag) {
   const size_t total = (size_t)NTR * kmax * nslot;
   bool bad = false;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
@@ -550,7 +596,7 @@ __global__ void k_trial(const real* __restrict__ conc, const real* __restrict__ 
     if (k >= kact[slot]) continue;
     const real c = conc[i];
     const real c1 = upd(c, dtr, rhs[i]);
-    bad |= below_keep(c1, keep, c);
+    bad |= below_keep(c1, keep, c, natol);
   }
   if (__any_sync(FULL, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
 }
@@ -792,6 +838,8 @@ static int occupancy_t(int tc, int threads) {
   const size_t smem = tile_smem_bytes<real>(tc, LPL, BC4);
   auto fn = k_column<real, LPL, BC4, KIND>;
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                       cudaSharedmemCarveoutMaxShared);
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem) != cudaSuccess)
     return 0;
@@ -816,11 +864,11 @@ int column_blocks_per_sm(int tc, int lpl, bool bc4, int kind, int threads) {
 
 template <typename real>
 cudaError_t launch_trial(const real* conc, const real* rhs, const int* kact,
-                         int nslot, int kmax, real dtr, real keep, int* flag,
-                         int sms, cudaStream_t st) {
+                         int nslot, int kmax, real dtr, real keep, real natol,
+                         int* flag, int sms, cudaStream_t st) {
   const size_t total = (size_t)NTR * kmax * nslot;
   k_trial<real><<<grid_for(total, 256, sms), 256, 0, st>>>(conc, rhs, kact, nslot,
-                                                          kmax, dtr, keep, flag);
+                                                          kmax, dtr, keep, natol, flag);
   return cudaGetLastError();
 }
 
@@ -904,8 +952,8 @@ cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
                                            int, int, cudaStream_t);             \
   template int column_blocks_per_sm<real>(int, int, bool, int, int);            \
   template cudaError_t launch_trial<real>(const real*, const real*, const int*, \
-                                          int, int, real, real, int*, int,      \
-                                          cudaStream_t);                        \
+                                          int, int, real, real, real, int*,     \
+                                          int, cudaStream_t);                   \
   template cudaError_t launch_accept<real>(real*, const real*, const int*, int, \
                                            int, real, int, cudaStream_t);       \
   template cudaError_t launch_epilogue<real>(real*, const int*, int, int,       \

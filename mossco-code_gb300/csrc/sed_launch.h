@@ -46,8 +46,8 @@ int column_blocks_per_sm(int tc, int lpl, bool bc4, int kind, int threads);
 
 template <typename real>
 cudaError_t launch_trial(const real* conc, const real* rhs, const int* kact,
-                         int nslot, int kmax, real dtr, real keep, int* flag,
-                         int sms, cudaStream_t st);
+                         int nslot, int kmax, real dtr, real keep, real natol,
+                         int* flag, int sms, cudaStream_t st);
 
 template <typename real>
 cudaError_t launch_accept(real* conc, const real* rhs, const int* kact,

@@ -40,6 +40,7 @@ class SedParams(ctypes.Structure):
                  ("mol_diff_d0", ctypes.c_double),
                  ("dt_min", ctypes.c_double),
                  ("relative_change_min", ctypes.c_double),
+                 ("atol", ctypes.c_double),
                  ("max_attempts", ctypes.c_int),
                  ("cut_scope", ctypes.c_int)]
                 + [(n, ctypes.c_double) for n in BGC_NAMES]
@@ -152,6 +153,7 @@ def params_from(cs: ColumnSet, precision: int = SED_FP32, budgets: bool = False,
     p.mol_diff_d0 = d.mol_diff_d0
     p.dt_min = d.dt_min
     p.relative_change_min = d.relative_change_min
+    p.atol = d.atol
     p.max_attempts = int(d.max_attempts)
     p.cut_scope = cut_scope
     for n in BGC_NAMES:

@@ -74,6 +74,7 @@ class DriverParams:
     mol_diff_d0: float = 1.0e-9         # m2/s (mode 1)
     dt_min: float = 1.0e-9              # s
     relative_change_min: float = -0.9
+    atol: float = 0.0                   # absolute floor of the positivity test
     max_attempts: int = 8192            # adaptive loop guard per step
     minimum: Optional[np.ndarray] = None  # clamp per tracer (default 0)
 

@@ -23,9 +23,10 @@ bioturbation 1e-11 m2/s exp(-z/0.05 m), i.e. the reference's exponential
 bioturbation profile (src/drivers/fabm_sediment_driver.F90:299-301) with a
 5 cm depth scale and bioturbation = 1e-11 m2/s in cm2/d; bottom water O2
 U[150,300], NO3 U[5,30], NH4 U[1,10], PO4 U[0.2,2] mmol/m3, ODU 0,
-temperature U[5,15] degC; surface POC flux split evenly between the labile
-and semilabile classes, N and P by Redfield 106:16:1 (all detrital P to the
-labile P pool, no adsorbed-P deposition).  Initial profiles: bottom-water
+temperature U[5,15] degC; positivity-test floor atol = 1e-12 mmol/m3 (the
+reference's test is recovered with atol = 0); surface POC flux split evenly
+between the labile and semilabile classes, N and P by Redfield 106:16:1 (all
+detrital P to the labile P pool, no adsorbed-P deposition).  Initial profiles: bottom-water
 values times exp(-z/z_e) (z_e = 5 mm for O2, 2 cm otherwise) times
 (1 + 0.01 N(0,1)); particulate pools start from the fabm_sed.nml initial
 values (per total volume, divided by porosity as init_concentrations does,
@@ -111,6 +112,12 @@ def interface_porosity(phi: np.ndarray) -> np.ndarray:
 _PART_INIT = (4.0e3, 4.0e3, 0.92e3, 0.04e3, 4.0e1, 10.0)
 _BW_RANGE = {6: (150.0, 300.0), 7: (5.0, 30.0), 8: (1.0, 10.0), 10: (0.2, 2.0)}
 FAST_FRACTION = 0.5
+# Absolute tolerance of the positivity test in the workloads (mmol/m3).
+# The reference's test is purely relative, so concentrations decaying
+# towards zero keep forcing substep cuts at any magnitude; FP32 state cannot
+# represent them below ~1e-38, so an FP32 solver can only follow an FP64 one
+# with a floor well above that range.  0 restores the reference's test.
+ATOL = 1.0e-12
 REDFIELD_NC = 16.0 / 106.0
 REDFIELD_PC = 1.0 / 106.0
 
@@ -225,7 +232,8 @@ def make_columns(inum: int, jnum: int, kmin: int, kmax: int, total: float,
                              conc, np.where(kact[None, None, :] == 0, 1.0e20, 0.0))
 
     drv = DriverParams(bioturbation=1.0e-11 * 1.0e4 * 86400.0,
-                       mol_diff_mode=1, mol_diff_d0=1.0e-9, dt_min=1.0)
+                       mol_diff_mode=1, mol_diff_d0=1.0e-9, dt_min=1.0,
+                       atol=ATOL)
     cs = ColumnSet(inum=oi, jnum=oj, kmax=kmax, kact=kact,
                    dz=np.ascontiguousarray(dz), dzc=np.ascontiguousarray(dzc),
                    zc=np.ascontiguousarray(zc), zi=np.ascontiguousarray(zi),

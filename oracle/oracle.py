@@ -68,6 +68,7 @@ class Model(ctypes.Structure):
         ("bcup_dissolved", ctypes.c_int), ("bcup_particulate", ctypes.c_int),
         ("mol_diff_mode", ctypes.c_int), ("mol_diff_d0", ctypes.c_double),
         ("dt_min", ctypes.c_double), ("relative_change_min", ctypes.c_double),
+        ("atol", ctypes.c_double),
         ("max_attempts", ctypes.c_long),
         ("bgc", Bgc),
     ]
@@ -158,6 +159,7 @@ class OracleModel:
         m.mol_diff_d0 = d.mol_diff_d0
         m.dt_min = d.dt_min
         m.relative_change_min = d.relative_change_min
+        m.atol = d.atol
         m.max_attempts = d.max_attempts
         for n in BGC_NAMES:
             setattr(m.bgc, n, float(cs.bgc[n]))

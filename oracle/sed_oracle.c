@@ -352,7 +352,7 @@ static int ode_solver_ws(const orc_model *m, double *conc, const double *bdys,
       int reject = 0;
       FOR_ACTIVE(m, {
         c1[i_] = conc[i_] + dt_red * w->rhs0[i_];
-        if (c1[i_] - keep * conc[i_] < 0.0) reject = 1;
+        if (c1[i_] - keep * conc[i_] < -m->atol) reject = 1;
       });
       if (reject && dt_red > m->dt_min) {
         dt_red = dt_red * 0.25;

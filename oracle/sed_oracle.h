@@ -58,6 +58,8 @@ typedef struct {
   double mol_diff_d0;     /* m2/s, mode 1 free-solution diffusivity */
   double dt_min;
   double relative_change_min;
+  double atol;            /* absolute tolerance of the positivity test:
+                             reject if c1 - (1+rcm) c < -atol (0 = reference) */
   long max_attempts;      /* guard on the adaptive loop (reference has none) */
   orc_bgc bgc;
 } orc_model;

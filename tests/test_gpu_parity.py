@@ -75,8 +75,11 @@ def test_rhs_fp32_matches_oracle(oracle_mod):
     assert np.max(np.abs(rhs - ref) / scale) < 2e-5
 
 
-def test_adaptive_percol_fp64_bit_exact(oracle_mod):
+@pytest.mark.parametrize("atol", [0.0, 1e-12])
+def test_adaptive_percol_fp64_bit_exact(oracle_mod, atol):
+    # atol = 0 is the reference's positivity test (solver_library.F90:121)
     cs = synth.make_workload("plain_cpu_10x10")
+    cs.driver.atol = atol
     n = 72
     out, fl, st, att, _ = run_gpu(cs, n, precision=capi.SED_FP64)
     ref, fref, sref = run_oracle(oracle_mod, cs, n)
@@ -121,8 +124,9 @@ def test_adaptive_percol_fp32(oracle_mod):
 
 
 def test_adaptive_global_cut_10x10(oracle_mod):
-    # the reference's own semantics: one cut for the whole grid
+    # the reference's own semantics: one cut for the whole grid, its test
     cs = synth.make_workload("plain_cpu_10x10")
+    cs.driver.atol = 0.0
     n = 12
     out, fl, st, _, _ = run_gpu(cs, n, precision=capi.SED_FP64,
                                 cut=capi.SED_CUT_GLOBAL)

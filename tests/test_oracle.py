@@ -131,6 +131,20 @@ def test_reaction_budgets_close(oracle_mod):
         assert abs(n_sum + 0.8 * dn) <= 1e-12 * (np.abs(r).max() + 1e-30)
 
 
+def test_atol_floor(oracle_mod):
+    """The positivity test ignores cells whose value is within atol of zero:
+    a cell at 1e-20 decaying at lam*dt = 8 forces the cut sequence with
+    atol = 0 (the reference's test) and none with atol = 1e-12."""
+    cs = decay_case()
+    cs.conc[0] = 1e-20
+    cs.conc[1:6] = 0.0
+    for atol, accepted in ((0.0, 16), (1e-12, 1)):
+        cs.driver.atol = atol
+        c = cs.conc.copy()
+        rc, st, _ = oracle_mod.OracleModel(cs).run(c, nsteps=1, percol=True)
+        assert st["accepted"] == accepted * cs.ncol, (atol, st)
+
+
 def test_percol_equals_single_column_runs(oracle_mod):
     # per-column mode: each column's result does not depend on the others
     cs = small(6, 10, seed=4, days=1)
@@ -197,6 +211,7 @@ def test_reference_amplifies_one_ulp(oracle_mod):
     parity is only possible for a bit-identical implementation."""
     from conftest import relerr
     cs = synth.make_workload("plain_cpu_10x10")
+    cs.driver.atol = 0.0
     om = oracle_mod.OracleModel(cs)
     a = cs.conc.copy()
     b = cs.conc * (1.0 + 2.0 ** -52)
