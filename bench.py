@@ -238,7 +238,37 @@ def run_gpu(args) -> None:
     ms_per_step = dev_ms / args.steps
     value = world * cs.n_active * args.steps / (dev_ms / 1e3)
 
-    # budgets of the last step
+    # accuracy: one FP32 coupling step against the FP64 device path (which
+    # reproduces the FP64 CPU restatement bit for bit) from the same state,
+    # on an evenly spaced column sample
+    acc_cols = np.unique(np.linspace(0, cs.ncol - 1, min(args.acc_columns, cs.ncol)
+                                     ).astype(np.int64))
+    S = s.get_state()
+    sub = cs.subset(acc_cols)
+    sub.conc = np.ascontiguousarray(S[:, :, acc_cols])
+    errs = []
+    outs = []
+    for prec in (capi.SED_FP32, capi.SED_FP64):
+        pp = capi.params_from(sub, prec, budgets=False, device=local)
+        ss = capi.Solver(sub, params=pp)
+        ss.set_forcing()
+        ss.set_state(sub.conc)
+        ss.step(1)
+        outs.append(ss.get_state())
+        ss.close()
+    act_mask = np.arange(sub.kmax)[:, None] < sub.kact[None, :]
+    for n in range(NTR):
+        r = outs[1][n][act_mask]
+        x = outs[0][n][act_mask]
+        floor = 1e-4 * max(np.abs(r).max(), 1e-300)
+        errs.append(float(np.max(np.abs(x - r) / (np.abs(r) + floor))))
+    accuracy = {"max_rel_err_per_tracer": errs, "max_rel_err": max(errs),
+                "columns": int(len(acc_cols)),
+                "reference": "FP64 device path (bit-identical to the FP64 CPU "
+                             "restatement), one coupling step from the same state",
+                "floor": "1e-4 x tracer max"}
+
+    # budgets of the last timed step
     bud = s.budgets()
     act = cs.kact > 0
     drift_P = float(np.max(np.abs(bud[1][act]) / bud[0][act]))
@@ -317,6 +347,7 @@ def run_gpu(args) -> None:
                      "accepted_per_column_step": acc / max(col_steps, 1),
                      "max_attempts": max_att},
         "budget_drift": {"P": drift_P, "N": drift_N},
+        "accuracy": accuracy,
         "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches,
         "clocks": clk, "wall_s": wall,
     }
@@ -334,6 +365,7 @@ def main():
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--cpu-columns", type=int, default=8192)
     ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--acc-columns", type=int, default=4096)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

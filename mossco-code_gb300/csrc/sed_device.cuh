@@ -96,8 +96,7 @@ __device__ __forceinline__ void omexdia_p(const Params<real>& p,
   const real CprodF = p.rF * fdetC;
   const real CprodS = p.rS * sdetC;
   const real Cprod = CprodF + CprodS;
-  real lim = real(1);
-  if (Cprod > p.cmax) lim = sdiv(p.cmax, Cprod);
+  const real lim = Cprod > p.cmax ? sdiv(p.cmax, Cprod) : real(1);
   const real oxlim = sdiv(O2, O2 + p.ksO2oxic);
   const real dnlim = sdiv(p.kinO2denit, O2 + p.kinO2denit) * sdiv(NO3, NO3 + p.ksNO3denit);
   const real anlim = sdiv(p.kinO2anox, O2 + p.kinO2anox) * sdiv(p.kinNO3anox, NO3 + p.kinNO3anox);
@@ -177,6 +176,10 @@ struct Lane {
 
 // Right-hand side of one column: OMEXDIA+P rates plus diff3d transport.
 // ftop receives the flux through the sediment surface (lane 0 only).
+// Branch-free: lanes beyond the column's K layers hold zero state and zero
+// conductances, so their rates and fluxes vanish by construction; the
+// surface boundary enters by selects on lane 0, the no-flux bottom by
+// dropping the flux from below at layer K-1.
 template <typename real, int LPL, bool BC4>
 __device__ __forceinline__ void column_rhs(const Params<real>& p,
                                            const Lane<real, LPL, BC4>& lc,
@@ -187,6 +190,12 @@ __device__ __forceinline__ void column_rhs(const Params<real>& p,
                                            real (&dn)[LPL]) {
 #pragma unroll
   for (int s = 0; s < LPL; s++) omexdia_p<real>(p, C[s], R[s], dn[s]);
+  const bool top = lane == 0;
+  const bool dirichlet = p.bcup_d == 2;
+  const bool fluxbc = p.bcup_d == 1;
+  bool bottom[LPL];
+#pragma unroll
+  for (int s = 0; s < LPL; s++) bottom[s] = s * 32 + lane >= K - 1;
 #pragma unroll
   for (int n = 0; n < NTR; n++) {
     const bool part = n < NPART;
@@ -194,25 +203,25 @@ __device__ __forceinline__ void column_rhs(const Params<real>& p,
 #pragma unroll
     for (int s = 0; s < LPL; s++) v[s] = part ? lc.phi[s] * C[s][n] : C[s][n];
     from_above<real, LPL>(v, vm, lane);
+    const real b = lc.bnd(n);
+    if (part) {
 #pragma unroll
-    for (int s = 0; s < LPL; s++) F[s] = (part ? lc.ap[s] : lc.ad[s]) * (vm[s] - v[s]);
-    if (lane == 0) {
-      real f0;
-      if (part) f0 = lc.bnd(n);
-      else if (p.bcup_d == 2) f0 = lc.ad[0] * (lc.bnd(n) - v[0]);
-      else if (p.bcup_d == 1) f0 = lc.bnd(n);
-      else f0 = real(0);
-      F[0] = f0;
-      ftop[n] = f0;
+      for (int s = 0; s < LPL; s++) F[s] = lc.ap[s] * (vm[s] - v[s]);
+      F[0] = top ? b : F[0];  // downward flux through the surface (BcUp 1)
+    } else {
+      // Dirichlet (BcUp 2): the surface interface sees the bottom water
+      vm[0] = (top && dirichlet) ? b : vm[0];
+#pragma unroll
+      for (int s = 0; s < LPL; s++) F[s] = lc.ad[s] * (vm[s] - v[s]);
+      F[0] = (top && !dirichlet) ? (fluxbc ? b : real(0)) : F[0];
     }
+    ftop[n] = F[0];
     from_below<real, LPL>(F, Fb, lane);
 #pragma unroll
     for (int s = 0; s < LPL; s++) {
-      const int L = s * 32 + lane;
-      const real below = (L >= K - 1) ? real(0) : Fb[s];
-      real t = (F[s] - below) * lc.ivol[s];
+      real t = (F[s] - (bottom[s] ? real(0) : Fb[s])) * lc.ivol[s];
       if (BC4 && part) t += lc.src[s][n];
-      R[s][n] = (L < K) ? R[s][n] + t : real(0);
+      R[s][n] += t;
     }
   }
 }

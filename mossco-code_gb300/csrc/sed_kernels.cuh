@@ -180,20 +180,66 @@ __device__ __forceinline__ bool below_keep(double c1, double keep, double c, dou
 }
 
 // FP64 column inventories of the P and N pools (warp-reduced).
-template <typename real, int LPL, bool BC4>
-__device__ __forceinline__ void inventories(const Lane<real, LPL, BC4>& lc,
-                                            const real (&C)[LPL][NTR],
+template <int LPL, bool BC4>
+__device__ __forceinline__ void inventories(const Lane<double, LPL, BC4>& lc,
+                                            const double (&C)[LPL][NTR],
                                             double& invP, double& invN) {
   double p = 0.0, nn = 0.0;
 #pragma unroll
   for (int s = 0; s < LPL; s++) {
-    const double v = (double)lc.vol[s];
-    p += v * ((double)C[s][T_FDETP] + (double)C[s][T_ADSP] + (double)C[s][T_PO4]);
-    nn += v * ((double)C[s][T_FDETN] + (double)C[s][T_SDETN] +
-               (double)C[s][T_NO3] + (double)C[s][T_NH4]);
+    const double v = lc.vol[s];
+    p += v * (C[s][T_FDETP] + C[s][T_ADSP] + C[s][T_PO4]);
+    nn += v * (C[s][T_FDETN] + C[s][T_SDETN] + C[s][T_NO3] + C[s][T_NH4]);
   }
   invP = warp_sum(p);
   invN = warp_sum(nn);
+}
+
+// Double-word (hi + lo) FP32 arithmetic: error-free TwoSum / TwoProduct
+// (Knuth, Dekker) keep ~48 significant bits, so the FP32 kernels carry their
+// budget reductions at about FP64 accuracy without the FP64 pipe (GB300
+// issues FP64 at a small fraction of its FP32 rate).
+struct DW {
+  float hi, lo;
+};
+__device__ __forceinline__ DW dw_add(DW x, DW y) {
+  const float s = x.hi + y.hi;
+  const float bp = s - x.hi;
+  const float e = (x.hi - (s - bp)) + (y.hi - bp) + (x.lo + y.lo);
+  const float hi = s + e;
+  return DW{hi, e - (hi - s)};
+}
+__device__ __forceinline__ DW dw_prod(float a, float b) {
+  const float p = a * b;
+  return DW{p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ DW dw_from(float a) { return DW{a, 0.0f}; }
+__device__ __forceinline__ DW dw_warp_sum(DW x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    DW y{__shfl_xor_sync(FULL, x.hi, o), __shfl_xor_sync(FULL, x.lo, o)};
+    x = dw_add(x, y);
+  }
+  return x;
+}
+__device__ __forceinline__ double dw_value(DW x) { return (double)x.hi + (double)x.lo; }
+
+// sum_k vol_k * (sum of the pool's tracers), double-word, warp-reduced
+template <int LPL, bool BC4, int NP>
+__device__ __forceinline__ DW dw_inventory(const Lane<float, LPL, BC4>& lc,
+                                           const float (&C)[LPL][NTR],
+                                           const int (&idx)[NP]) {
+  DW acc = dw_from(0.0f);
+#pragma unroll
+  for (int s = 0; s < LPL; s++) {
+    DW pool = dw_from(C[s][idx[0]]);
+#pragma unroll
+    for (int q = 1; q < NP; q++) pool = dw_add(pool, dw_from(C[s][idx[q]]));
+    DW prod = dw_prod(lc.vol[s], pool.hi);
+    prod.lo = fmaf(lc.vol[s], pool.lo, prod.lo);
+    acc = dw_add(acc, prod);
+  }
+  return dw_warp_sum(acc);
 }
 
 struct ColResult {
@@ -220,50 +266,103 @@ struct CompSum {
   __device__ __forceinline__ double value() const { return (double)s + (double)c; }
 };
 
-// Budget bookkeeping of one column over one coupling step: FP64 column
+// Budget bookkeeping of one column over one coupling step: column
 // inventories of the P and N pools at the start and end of the step (warp
 // reductions), the surface inflow of both pools and the N lost to
-// denitrification (0.8 mol N per mol C) accumulated per substep.
+// denitrification (0.8 mol N per mol C) accumulated per substep.  FP64
+// state: FP64 throughout.  FP32 state: double-word FP32 sums, converted to
+// FP64 once per column-step.
 template <typename real, int LPL, bool BC4>
-struct Budget {
-  double inv0P, inv0N;
-  CompSum<real> inP, inN;
-  real n2[LPL];
-  __device__ __forceinline__ void start(const Params<real>& p,
-                                        const Lane<real, LPL, BC4>& lc,
-                                        const real (&C)[LPL][NTR]) {
-    inP.zero(); inN.zero(); inv0P = 0.0; inv0N = 0.0;
+struct Budget;
+
+template <int LPL, bool BC4>
+struct Budget<double, LPL, BC4> {
+  double inv0P, inv0N, inP, inN;
+  double n2[LPL];
+  __device__ __forceinline__ void start(const Params<double>& p,
+                                        const Lane<double, LPL, BC4>& lc,
+                                        const double (&C)[LPL][NTR]) {
+    inP = 0.0; inN = 0.0; inv0P = 0.0; inv0N = 0.0;
 #pragma unroll
-    for (int s = 0; s < LPL; s++) n2[s] = real(0);
-    if (p.budgets) inventories<real, LPL, BC4>(lc, C, inv0P, inv0N);
+    for (int s = 0; s < LPL; s++) n2[s] = 0.0;
+    if (p.budgets) inventories<LPL, BC4>(lc, C, inv0P, inv0N);
   }
-  // one right-hand side entering the update with weight w (seconds)
-  __device__ __forceinline__ void account(const Params<real>& p, real w,
-                                          const real (&ftop)[NTR],
-                                          const real (&dn)[LPL]) {
+  __device__ __forceinline__ void account(const Params<double>& p, double w,
+                                          const double (&ftop)[NTR],
+                                          const double (&dn)[LPL]) {
     if (!p.budgets) return;
-    inP.add(w * (ftop[T_FDETP] + ftop[T_ADSP] + ftop[T_PO4]));
-    inN.add(w * (ftop[T_FDETN] + ftop[T_SDETN] + ftop[T_NO3] + ftop[T_NH4]));
+    inP += w * (ftop[T_FDETP] + ftop[T_ADSP] + ftop[T_PO4]);
+    inN += w * (ftop[T_FDETN] + ftop[T_SDETN] + ftop[T_NO3] + ftop[T_NH4]);
 #pragma unroll
-    for (int s = 0; s < LPL; s++) n2[s] += w * real(0.8) * dn[s];
+    for (int s = 0; s < LPL; s++) n2[s] += w * 0.8 * dn[s];
   }
-  __device__ __forceinline__ void finish(const Params<real>& p,
-                                         const Lane<real, LPL, BC4>& lc,
-                                         const real (&C)[LPL][NTR],
-                                         double (&bud)[4]) {
+  __device__ __forceinline__ void finish(const Params<double>& p,
+                                         const Lane<double, LPL, BC4>& lc,
+                                         const double (&C)[LPL][NTR],
+                                         double (&bud)[4], int lane) {
     if (!p.budgets) return;
     double inv1P, inv1N;
-    inventories<real, LPL, BC4>(lc, C, inv1P, inv1N);
+    inventories<LPL, BC4>(lc, C, inv1P, inv1N);
     double loss = 0.0;
 #pragma unroll
-    for (int s = 0; s < LPL; s++) loss += (double)lc.vol[s] * (double)n2[s];
+    for (int s = 0; s < LPL; s++) loss += lc.vol[s] * n2[s];
     loss = warp_sum(loss);
-    const double fP = __shfl_sync(FULL, inP.value(), 0);
-    const double fN = __shfl_sync(FULL, inN.value(), 0);
+    const double fP = __shfl_sync(FULL, inP, 0);
+    const double fN = __shfl_sync(FULL, inN, 0);
     bud[0] = inv1P;
     bud[1] = inv1P - inv0P - fP;
     bud[2] = inv1N;
     bud[3] = inv1N - inv0N - fN + loss;
+  }
+};
+
+template <int LPL, bool BC4>
+struct Budget<float, LPL, BC4> {
+  DW inv0P, inv0N;
+  CompSum<float> inP, inN;
+  float n2[LPL];
+  __device__ __forceinline__ void start(const Params<float>& p,
+                                        const Lane<float, LPL, BC4>& lc,
+                                        const float (&C)[LPL][NTR]) {
+    inP.zero(); inN.zero();
+#pragma unroll
+    for (int s = 0; s < LPL; s++) n2[s] = 0.0f;
+    if (p.budgets) {
+      constexpr int iP[3] = {T_FDETP, T_ADSP, T_PO4};
+      constexpr int iN[4] = {T_FDETN, T_SDETN, T_NO3, T_NH4};
+      inv0P = dw_inventory<LPL, BC4, 3>(lc, C, iP);
+      inv0N = dw_inventory<LPL, BC4, 4>(lc, C, iN);
+    }
+  }
+  __device__ __forceinline__ void account(const Params<float>& p, float w,
+                                          const float (&ftop)[NTR],
+                                          const float (&dn)[LPL]) {
+    if (!p.budgets) return;
+    inP.add(w * (ftop[T_FDETP] + ftop[T_ADSP] + ftop[T_PO4]));
+    inN.add(w * (ftop[T_FDETN] + ftop[T_SDETN] + ftop[T_NO3] + ftop[T_NH4]));
+#pragma unroll
+    for (int s = 0; s < LPL; s++) n2[s] = fmaf(w * 0.8f, dn[s], n2[s]);
+  }
+  __device__ __forceinline__ void finish(const Params<float>& p,
+                                         const Lane<float, LPL, BC4>& lc,
+                                         const float (&C)[LPL][NTR],
+                                         double (&bud)[4], int lane) {
+    if (!p.budgets) return;
+    constexpr int iP[3] = {T_FDETP, T_ADSP, T_PO4};
+    constexpr int iN[4] = {T_FDETN, T_SDETN, T_NO3, T_NH4};
+    const DW inv1P = dw_inventory<LPL, BC4, 3>(lc, C, iP);
+    const DW inv1N = dw_inventory<LPL, BC4, 4>(lc, C, iN);
+    DW loss = dw_from(0.0f);
+#pragma unroll
+    for (int s = 0; s < LPL; s++) loss = dw_add(loss, dw_prod(lc.vol[s], n2[s]));
+    loss = dw_warp_sum(loss);
+    if (lane == 0) {  // lane 0 holds the surface inflow sums
+      const double v1P = dw_value(inv1P), v1N = dw_value(inv1N);
+      bud[0] = v1P;
+      bud[1] = v1P - dw_value(inv0P) - inP.value();
+      bud[2] = v1N;
+      bud[3] = v1N - dw_value(inv0N) - inN.value() + dw_value(loss);
+    }
   }
 };
 
@@ -318,12 +417,12 @@ __device__ __forceinline__ ColResult solve_adaptive(
     bool bad = false;
 #pragma unroll
     for (int s = 0; s < LPL; s++) {
-      const bool act = s * 32 + lane < K;
+      // lanes past the column hold zeros: c1 = 0 never falls below -atol
 #pragma unroll
       for (int n = 0; n < NTR; n++) {
         const real c1 = upd(C[s][n], dtr, R[s][n]);
         // sign of c1 - (1+rcm) c; in FP32 exact for the operands (one FMA)
-        bad |= act && below_keep(c1, p.keep, C[s][n], p.natol);
+        bad |= below_keep(c1, p.keep, C[s][n], p.natol);
       }
     }
     const bool reject = __any_sync(FULL, bad);
@@ -348,7 +447,7 @@ __device__ __forceinline__ ColResult solve_adaptive(
     }
   }
   if (mmax >= 0) res.min_dt = ldexp(dt, -2 * mmax);
-  B.finish(p, lc, C, bud);
+  B.finish(p, lc, C, bud, lane);
   res.nan = epilogue<real, LPL>(p, lane, K, C);
   return res;
 }
@@ -421,7 +520,7 @@ __device__ __forceinline__ ColResult solve_fixed(
                                    real(0.5) * R[s][n]);
       }
   }
-  B.finish(p, lc, C, bud);
+  B.finish(p, lc, C, bud, lane);
   res.nan = epilogue<real, LPL>(p, lane, K, C);
   return res;
 }
