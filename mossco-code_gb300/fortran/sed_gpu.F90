@@ -1,0 +1,158 @@
+!> @file sed_gpu.F90
+!! @brief ISO_C_BINDING interface to the GB300 sediment-column solver.
+!!
+!! Binds the C ABI of include/mossco_sed.h for MOSSCO's Fortran host.  The
+!! module mirrors the reference's call `call ode_solver(sed, dt, method)`
+!! (src/utilities/solver_library.F90:80) with `call sed_gpu_ode_solver(gpu,
+!! sed, dt, method, rc)`, which advances sed%conc in place and applies the
+!! component's NaN check and clamp (src/components/fabm_sediment_component.F90
+!! :1715-1732) on the device.  Arrays are passed in their Fortran layout:
+!! conc(i,j,k,n), bdys(i,j,n+1), fluxes(i,j,n) are exactly the C ABI's
+!! [ntr][kmax][ncol], [ntr+1][ncol], [ntr][ncol] with col = i + inum*(j-1).
+module sed_gpu
+
+  use iso_c_binding
+  implicit none
+  private
+
+  integer, parameter, public :: SED_NTR = 11
+  integer, parameter, public :: SED_OK = 0, SED_E_ARG = -1, SED_E_NAN = -2
+  integer, parameter, public :: SED_E_SUBSTEP_CAP = -3, SED_E_CUDA = -4
+  integer, parameter, public :: SED_E_STATE = -5, SED_E_NOMEM = -6
+  integer, parameter, public :: SED_E_NODEVICE = -7
+  integer, parameter, public :: SED_FP32 = 0, SED_FP64 = 1
+  integer, parameter, public :: SED_CUT_PER_COLUMN = 0, SED_CUT_GLOBAL = 1
+
+  !> sed_params of mossco_sed.h (same member order and kinds)
+  type, bind(C), public :: sed_params_t
+    real(c_double)  :: diffusivity, bioturbation
+    integer(c_int)  :: bcup_dissolved, bcup_particulate, mol_diff_mode
+    real(c_double)  :: mol_diff_d0
+    real(c_double)  :: dt_min, relative_change_min, atol
+    integer(c_int)  :: max_attempts, cut_scope
+    real(c_double)  :: rLabile, rSemilabile, NCrLdet, NCrSdet, PAds, PAdsODU, &
+                       NH3Ads, CprodMax, rnit, ksO2nitri, rODUox, ksO2oduox, &
+                       ksO2oxic, ksNO3denit, kinO2denit, kinNO3anox, kinO2anox
+    integer(c_int)  :: epilogue
+    real(c_double)  :: minimum(SED_NTR)
+    integer(c_int)  :: precision, budgets, device
+  end type
+
+  type, bind(C), public :: sed_stats_t
+    integer(c_long_long) :: attempts, accepted, column_steps
+    integer(c_int)       :: max_col_attempts, capped_columns, nan_cells, &
+                            gpu_launches
+    real(c_double)       :: min_dt, device_ms
+  end type
+
+  !> a solver handle
+  type, public :: sed_gpu_t
+    type(c_ptr) :: h = c_null_ptr
+  end type
+
+  interface
+    integer(c_int) function sed_default_params(p) bind(C, name='sed_default_params')
+      import :: c_int, sed_params_t
+      type(sed_params_t), intent(out) :: p
+    end function
+    integer(c_int) function sed_create(p, inum, jnum, kmax, ntr, h) bind(C, name='sed_create')
+      import :: c_int, c_ptr, sed_params_t
+      type(sed_params_t), intent(in) :: p
+      integer(c_int), value :: inum, jnum, kmax, ntr
+      type(c_ptr), intent(out) :: h
+    end function
+    integer(c_int) function sed_set_grid(h, dz, dzc, phi, phi_i, biofac, flux_cap, kact, mask) &
+        bind(C, name='sed_set_grid')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, dz, dzc, phi, phi_i, biofac, flux_cap, kact, mask
+    end function
+    integer(c_int) function sed_ode_solver(h, conc, bdys, fluxes, dt, method, st) &
+        bind(C, name='sed_ode_solver')
+      import :: c_int, c_ptr, c_double, sed_stats_t
+      type(c_ptr), value :: h, conc, bdys, fluxes
+      real(c_double), value :: dt
+      integer(c_int), value :: method
+      type(sed_stats_t), intent(out) :: st
+    end function
+    integer(c_int) function sed_get_rhs(h, conc, rhs, fluxes) bind(C, name='sed_get_rhs')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, conc, rhs, fluxes
+    end function
+    integer(c_int) function sed_set_forcing(h, bdys, fluxes) bind(C, name='sed_set_forcing')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, bdys, fluxes
+    end function
+    integer(c_int) function sed_host_register(ptr, bytes) bind(C, name='sed_host_register')
+      import :: c_int, c_ptr, c_size_t
+      type(c_ptr), value :: ptr
+      integer(c_size_t), value :: bytes
+    end function
+    subroutine sed_destroy(h) bind(C, name='sed_destroy')
+      import :: c_ptr
+      type(c_ptr), value :: h
+    end subroutine
+  end interface
+
+  public :: sed_default_params, sed_gpu_init, sed_gpu_ode_solver, &
+            sed_gpu_get_rhs, sed_gpu_finalize
+
+contains
+
+  !> Create a handle for the driver's grid (after type_sed%initialize):
+  !! grid%dz, grid%dzc, porosity, intf_porosity, bioturbation_factor,
+  !! flux_cap and mask (masked columns, or masked bottom layers only).
+  subroutine sed_gpu_init(gpu, p, inum, jnum, knum, dz, dzc, porosity, &
+                          intf_porosity, bioturbation_factor, flux_cap, mask, rc)
+    type(sed_gpu_t), intent(out) :: gpu
+    type(sed_params_t), intent(in) :: p
+    integer, intent(in) :: inum, jnum, knum
+    real(c_double), dimension(:,:,:), intent(in), target, contiguous :: &
+      dz, dzc, porosity, intf_porosity, bioturbation_factor, flux_cap
+    integer(c_int), dimension(:,:,:), intent(in), target, contiguous :: mask
+    integer, intent(out) :: rc
+    rc = sed_create(p, int(inum, c_int), int(jnum, c_int), int(knum, c_int), &
+                    int(SED_NTR, c_int), gpu%h)
+    if (rc /= SED_OK) return
+    rc = sed_set_grid(gpu%h, c_loc(dz), c_loc(dzc), c_loc(porosity), &
+                      c_loc(intf_porosity), c_loc(bioturbation_factor), &
+                      c_loc(flux_cap), c_null_ptr, c_loc(mask))
+  end subroutine
+
+  !> Drop-in for `call ode_solver(sed, dt, ode_method)` plus the component
+  !! epilogue: conc advanced in place, dissolved rows of fluxes set to the
+  !! surface fluxes of the last right-hand side (get_rhs :692).
+  subroutine sed_gpu_ode_solver(gpu, conc, bdys, fluxes, dt, method, rc, stats)
+    type(sed_gpu_t), intent(in) :: gpu
+    real(c_double), dimension(:,:,:,:), intent(inout), target, contiguous :: conc
+    real(c_double), dimension(:,:,:), intent(in), target, contiguous :: bdys
+    real(c_double), dimension(:,:,:), intent(inout), target, contiguous :: fluxes
+    real(c_double), intent(in) :: dt
+    integer, intent(in) :: method
+    integer, intent(out) :: rc
+    type(sed_stats_t), intent(out), optional :: stats
+    type(sed_stats_t) :: st
+    rc = sed_ode_solver(gpu%h, c_loc(conc), c_loc(bdys), c_loc(fluxes), dt, &
+                        int(method, c_int), st)
+    if (present(stats)) stats = st
+  end subroutine
+
+  !> Drop-in for type_sed%get_rhs (fabm_sediment_driver.F90:575-717).
+  subroutine sed_gpu_get_rhs(gpu, conc, bdys, fluxes, rhs, rc)
+    type(sed_gpu_t), intent(in) :: gpu
+    real(c_double), dimension(:,:,:,:), intent(in), target, contiguous :: conc
+    real(c_double), dimension(:,:,:), intent(in), target, contiguous :: bdys
+    real(c_double), dimension(:,:,:), intent(inout), target, contiguous :: fluxes
+    real(c_double), dimension(:,:,:,:), intent(out), target, contiguous :: rhs
+    integer, intent(out) :: rc
+    rc = sed_set_forcing(gpu%h, c_loc(bdys), c_loc(fluxes))
+    if (rc /= SED_OK) return
+    rc = sed_get_rhs(gpu%h, c_loc(conc), c_loc(rhs), c_loc(fluxes))
+  end subroutine
+
+  subroutine sed_gpu_finalize(gpu)
+    type(sed_gpu_t), intent(inout) :: gpu
+    call sed_destroy(gpu%h)
+    gpu%h = c_null_ptr
+  end subroutine
+
+end module sed_gpu
