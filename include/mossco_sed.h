@@ -42,6 +42,10 @@ extern "C" {
 #define SED_E_NOMEM (-6)        /* device or pinned allocation failed */
 #define SED_E_NODEVICE (-7)     /* no CUDA device */
 #define SED_E_TIMEOUT (-8)      /* a bounded device wait gave up */
+#define SED_E_TOO_LARGE (-9)    /* grid exceeds the no-allocation scratch */
+
+/* Size of the device array behind sed_ode_solver_noalloc (64 MiB). */
+#define SED_NOALLOC_SCRATCH_BYTES (64u << 20)
 
 /* ode_solver methods (solver_library.F90:32-35) */
 #define SED_EULER 0
@@ -164,6 +168,31 @@ int sed_set_stream(sed_handle *h, void *stream);
 /* Pin (or unpin) a caller's host array so copies run at full speed. */
 int sed_host_register(void *ptr, size_t bytes);
 int sed_host_unregister(void *ptr);
+
+/* One coupling step of the drop-in above for callers that cannot allocate
+ * device memory (no counterpart in the reference).  Some callers cannot
+ * call cudaMalloc: a component whose framework owns the GPU's memory pool
+ * and forbids other allocators, or a call site that cannot keep a solver
+ * handle (and the buffers sed_create allocates) alive between calls.  This
+ * call creates no handle and allocates nothing: every device buffer of the
+ * step lives in one static device array of SED_NOALLOC_SCRATCH_BYTES, which
+ * each GPU that loads the library holds until the process exits.  The
+ * arguments are the host arrays of sed_set_grid and sed_ode_solver (conc
+ * and fluxes updated in place); p must ask for SED_FP32 state and
+ * per-column cuts, and budgets are not computed.  A grid whose buffers do
+ * not fit the array (about 4.7 KB per column at 30 layers, so ~14 000
+ * columns) is rejected with SED_E_TOO_LARGE.  The first call on a device
+ * looks up the array's device address; make that first call before any
+ * stream capture.  All calls share the array, so calls that overlap on the
+ * GPU (from several host threads) race; the work runs on the legacy
+ * default stream and the call returns when it is done. */
+int sed_ode_solver_noalloc(const sed_params *p, int inum, int jnum, int kmax,
+                           const double *dz, const double *dzc,
+                           const double *phi, const double *phi_i,
+                           const double *biofac, const double *flux_cap,
+                           const int *kact, double *conc, const double *bdys,
+                           double *fluxes, double dt, int method,
+                           sed_stats *stats);
 
 const char *sed_error_string(int code);
 const char *sed_last_error(const sed_handle *h);

@@ -21,7 +21,8 @@ BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_NAME = "libsedgpu.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 
-SOURCES = ["sed_kernels_f32.cu", "sed_kernels_f64.cu", "sed_capi.cu"]
+SOURCES = ["sed_kernels_f32.cu", "sed_kernels_f64.cu", "sed_capi.cu",
+           "sed_noalloc.cu"]
 # The FP64 kernels evaluate the reference's arithmetic operation by
 # operation: no multiply-add contraction.
 EXTRA_FLAGS = {"sed_kernels_f64.cu": ["-fmad=false"]}

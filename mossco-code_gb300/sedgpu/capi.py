@@ -19,7 +19,7 @@ from .model import BGC_NAMES, NTR, ColumnSet
 
 SED_OK, SED_E_ARG, SED_E_NAN, SED_E_SUBSTEP_CAP = 0, -1, -2, -3
 SED_E_CUDA, SED_E_STATE, SED_E_NOMEM, SED_E_NODEVICE = -4, -5, -6, -7
-SED_E_TIMEOUT = -8
+SED_E_TIMEOUT, SED_E_TOO_LARGE = -8, -9
 SED_FP32, SED_FP64 = 0, 1
 SED_CUT_PER_COLUMN, SED_CUT_GLOBAL = 0, 1
 SED_KMAX_LIMIT = 64
@@ -94,6 +94,10 @@ SIGNATURES = {
     "sed_set_stream": (ctypes.c_int, [_H, _vp]),
     "sed_host_register": (ctypes.c_int, [_vp, ctypes.c_size_t]),
     "sed_host_unregister": (ctypes.c_int, [_vp]),
+    "sed_ode_solver_noalloc": (ctypes.c_int, [
+        ctypes.POINTER(SedParams), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+        _dp, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp, ctypes.c_double,
+        ctypes.c_int, ctypes.POINTER(SedStats)]),
     "sed_error_string": (ctypes.c_char_p, [ctypes.c_int]),
     "sed_last_error": (ctypes.c_char_p, [_H]),
     "sed_tracer_name": (ctypes.c_char_p, [ctypes.c_int]),
