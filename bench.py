@@ -143,10 +143,10 @@ def cpu_run(cs, warmup: int, steps: int, threads: int):
     return cs.n_active * steps / dt, dt, st
 
 
-def cpu_sample(ncol_full: int, n: int, seed: int):
+def cpu_sample(ncol_full: int, n: int, seed: int, workload: str = WORKLOAD):
     from sedgpu import synth
     cols = np.linspace(0, ncol_full - 1, min(n, ncol_full)).astype(np.int64)
-    return synth.make_workload(WORKLOAD, seed=seed, cols=np.unique(cols))
+    return synth.make_workload(workload, seed=seed, cols=np.unique(cols))
 
 
 def run_reference(args) -> None:
@@ -156,10 +156,10 @@ def run_reference(args) -> None:
     import oracle
     oracle.build()
     from sedgpu import synth
-    full = synth.WORKLOADS[WORKLOAD]
+    full = synth.WORKLOADS[args.workload]
     ncol = full["inum"] * full["jnum"]
     threads = os.cpu_count() or 1
-    cs = cpu_sample(ncol, args.cpu_columns, args.seed)
+    cs = cpu_sample(ncol, args.cpu_columns, args.seed, args.workload)
     val, secs, st = cpu_run(cs, args.warmup, args.steps, threads)
     line = {
         "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
@@ -167,7 +167,7 @@ def run_reference(args) -> None:
         "ms_per_step": secs * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
         "data": "synthetic (seeded)", "impl": "reference",
-        "config": {"workload": WORKLOAD, "columns_sampled": cs.n_active,
+        "config": {"workload": args.workload, "columns_sampled": cs.n_active,
                    "layers": cs.kmax, "tracers": NTR, "dt_s": cs.dt,
                    "method": "adaptive_euler", "cut": "per_column"},
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads,
@@ -195,8 +195,8 @@ def run_gpu(args) -> None:
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    # weak scaling: every rank integrates its own 256 x 256 block of columns
-    cs = synth.make_workload(WORKLOAD, seed=args.seed + 7919 * rank)
+    # weak scaling: every rank integrates its own block of columns
+    cs = synth.make_workload(args.workload, seed=args.seed + 7919 * rank)
     p = capi.params_from(cs, capi.SED_FP32, budgets=True, device=local)
     s = capi.Solver(cs, params=p)
     s.set_forcing()
@@ -317,7 +317,7 @@ def run_gpu(args) -> None:
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
-        sample = cpu_sample(cs.ncol, args.cpu_columns, args.seed)
+        sample = cpu_sample(cs.ncol, args.cpu_columns, args.seed, args.workload)
         val, secs, _ = cpu_run(sample, args.warmup, args.steps, threads)
         cpu = {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{sample.n_active} of {cs.ncol} columns, coupling "
@@ -329,8 +329,11 @@ def run_gpu(args) -> None:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "columns": cs.n_active,
-                   "layers": cs.kmax, "tracers": NTR, "dt_s": cs.dt,
+        "config": {"workload": args.workload, "columns": cs.n_active,
+                   "layers": cs.kmax if cs.kact.min() == cs.kmax else
+                   f"{int(cs.kact[cs.kact > 0].min())}..{int(cs.kact.max())}",
+                   "land_fraction": float(np.mean(cs.kact == 0)),
+                   "tracers": NTR, "dt_s": cs.dt,
                    "method": "adaptive_euler", "cut": "per_column",
                    "state": "fp32", "budgets": "fp64",
                    "l2": "flushed between timed steps",
@@ -339,7 +342,7 @@ def run_gpu(args) -> None:
                      "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_kind": peak_kind,
                      "bytes_per_launch": bytes_step,
-                     "kernel": "k_column<float,1,false,ADAPT>"},
+                     "kernel": "k_column<float,LPL,false,ADAPT>"},
         "compute": {"fp32_tflops_est": fp32_ach, "fp32_peak_tflops": fp32_peak,
                     "frac": fp32_ach / fp32_peak,
                     "note": "nominal 152 SM x 128 FMA/clk at the sampled clock"},
@@ -362,6 +365,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--cpu-columns", type=int, default=8192)
     ap.add_argument("--e2e-steps", type=int, default=10)
