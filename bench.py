@@ -42,6 +42,9 @@ UNIT = "column-steps/s"
 WORKLOAD = "plain_gpu_256x256"
 NTR, NCOEF, NFORCE, NDISS = 11, 4, 13, 5
 L2_BYTES = 129 * 1024 * 1024
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_column launch from
+# an ncu capture (profiles/k_column_plain_gpu_256x256.md)
+MEASURED_TRAFFIC = {"plain_gpu_256x256": 157.1e6}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -241,14 +244,16 @@ def run_gpu(args) -> None:
     # accuracy: one FP32 coupling step against the FP64 device path (which
     # reproduces the FP64 CPU restatement bit for bit) from the same state,
     # on an evenly spaced column sample
+    accuracy = None
     acc_cols = np.unique(np.linspace(0, cs.ncol - 1, min(args.acc_columns, cs.ncol)
-                                     ).astype(np.int64))
-    S = s.get_state()
-    sub = cs.subset(acc_cols)
-    sub.conc = np.ascontiguousarray(S[:, :, acc_cols])
+                                     ).astype(np.int64)) if args.acc_columns > 0 else []
+    S = s.get_state() if len(acc_cols) else None
     errs = []
     outs = []
-    for prec in (capi.SED_FP32, capi.SED_FP64):
+    sub = cs.subset(acc_cols) if len(acc_cols) else None
+    if sub is not None:
+        sub.conc = np.ascontiguousarray(S[:, :, acc_cols])
+    for prec in ((capi.SED_FP32, capi.SED_FP64) if sub is not None else ()):
         pp = capi.params_from(sub, prec, budgets=False, device=local)
         ss = capi.Solver(sub, params=pp)
         ss.set_forcing()
@@ -256,17 +261,18 @@ def run_gpu(args) -> None:
         ss.step(1)
         outs.append(ss.get_state())
         ss.close()
-    act_mask = np.arange(sub.kmax)[:, None] < sub.kact[None, :]
-    for n in range(NTR):
-        r = outs[1][n][act_mask]
-        x = outs[0][n][act_mask]
-        floor = 1e-4 * max(np.abs(r).max(), 1e-300)
-        errs.append(float(np.max(np.abs(x - r) / (np.abs(r) + floor))))
-    accuracy = {"max_rel_err_per_tracer": errs, "max_rel_err": max(errs),
-                "columns": int(len(acc_cols)),
-                "reference": "FP64 device path (bit-identical to the FP64 CPU "
-                             "restatement), one coupling step from the same state",
-                "floor": "1e-4 x tracer max"}
+    if sub is not None:
+        act_mask = np.arange(sub.kmax)[:, None] < sub.kact[None, :]
+        for n in range(NTR):
+            r = outs[1][n][act_mask]
+            x = outs[0][n][act_mask]
+            floor = 1e-4 * max(np.abs(r).max(), 1e-300)
+            errs.append(float(np.max(np.abs(x - r) / (np.abs(r) + floor))))
+        accuracy = {"max_rel_err_per_tracer": errs, "max_rel_err": max(errs),
+                    "columns": int(len(acc_cols)),
+                    "reference": "FP64 device path (bit-identical to the FP64 CPU "
+                                 "restatement), one coupling step from the same state",
+                    "floor": "1e-4 x tracer max"}
 
     # budgets of the last timed step
     bud = s.budgets()
@@ -340,7 +346,8 @@ def run_gpu(args) -> None:
                    "solver": "plain"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_kind": peak_kind,
+                     "traffic": MEASURED_TRAFFIC.get(args.workload),
+                     "peak_kind": peak_kind,
                      "bytes_per_launch": bytes_step,
                      "kernel": "k_column<float,LPL,false,ADAPT>"},
         "compute": {"fp32_tflops_est": fp32_ach, "fp32_peak_tflops": fp32_peak,

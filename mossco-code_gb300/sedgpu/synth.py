@@ -23,7 +23,7 @@ bioturbation 1e-11 m2/s exp(-z/0.05 m), i.e. the reference's exponential
 bioturbation profile (src/drivers/fabm_sediment_driver.F90:299-301) with a
 5 cm depth scale and bioturbation = 1e-11 m2/s in cm2/d; bottom water O2
 U[150,300], NO3 U[5,30], NH4 U[1,10], PO4 U[0.2,2] mmol/m3, ODU 0,
-temperature U[5,15] degC; positivity-test floor atol = 1e-12 mmol/m3 (the
+temperature U[5,15] degC; positivity-test floor atol = 1e-6 mmol/m3 (the
 reference's test is recovered with atol = 0); surface POC flux split evenly
 between the labile and semilabile classes, N and P by Redfield 106:16:1 (all
 detrital P to the labile P pool, no adsorbed-P deposition).  Initial profiles: bottom-water
@@ -115,9 +115,11 @@ FAST_FRACTION = 0.5
 # Absolute tolerance of the positivity test in the workloads (mmol/m3).
 # The reference's test is purely relative, so concentrations decaying
 # towards zero keep forcing substep cuts at any magnitude; FP32 state cannot
-# represent them below ~1e-38, so an FP32 solver can only follow an FP64 one
-# with a floor well above that range.  0 restores the reference's test.
-ATOL = 1.0e-12
+# represent them below ~1e-38 and cannot resolve them next to neighbours ~1e8
+# times larger, so an FP32 solver can only follow an FP64 one with a floor
+# well above that range.  1 nmol/m3 is negligible for every tracer.  0
+# restores the reference's test.
+ATOL = 1.0e-6
 REDFIELD_NC = 16.0 / 106.0
 REDFIELD_PC = 1.0 / 106.0
 
