@@ -194,6 +194,33 @@ int sed_ode_solver_noalloc(const sed_params *p, int inum, int jnum, int kmax,
                            double *fluxes, double dt, int method,
                            sed_stats *stats);
 
+/* ------------------------------------------------------------------------
+ * Column-increment surrogate (no counterpart in the reference): an MLP
+ * nin -> hidden (x nhidden, GELU) -> nout with BF16 tensor-core products,
+ * FP32 accumulation and FP32 master weights trained with Adam.  Parameters
+ * are exchanged unpadded, layer by layer: W[out][in] then b[out]. */
+typedef struct sed_surrogate sed_surrogate;
+int sed_sur_create(int nin, int nout, int hidden, int nhidden, int max_batch,
+                   unsigned long long seed, int device, sed_surrogate **out);
+int sed_sur_num_params(const sed_surrogate *s);
+int sed_sur_set_weights(sed_surrogate *s, const float *params);
+int sed_sur_get_weights(sed_surrogate *s, float *params);
+/* host rows x[m][nin] -> y[m][nout] */
+int sed_sur_forward(sed_surrogate *s, const float *x, float *y, int m);
+/* device rows: x BF16 [m][pad128(nin)] -> y FP32 [m][pad128(nout)],
+ * m a multiple of 128 */
+int sed_sur_forward_device(sed_surrogate *s, const void *x_dev, void *y_dev,
+                           int m);
+/* one Adam step on a device batch (x BF16 [m][pad128(nin)], y BF16
+ * [m][pad128(nout)], m a multiple of 128, <= max_batch); loss may be NULL */
+int sed_sur_train_step(sed_surrogate *s, const void *x_dev, const void *y_dev,
+                       int m, float lr, float *loss);
+/* MSE loss and its parameter gradients for host rows (no update) */
+int sed_sur_grads(sed_surrogate *s, const float *x, const float *y, int m,
+                  float *grads, float *loss);
+const char *sed_sur_last_error(const sed_surrogate *s);
+void sed_sur_destroy(sed_surrogate *s);
+
 const char *sed_error_string(int code);
 const char *sed_last_error(const sed_handle *h);
 const char *sed_tracer_name(int n);

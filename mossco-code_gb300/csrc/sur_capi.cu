@@ -1,0 +1,367 @@
+// sur_capi.cu -- host side of the surrogate MLP (C ABI in mossco_sed.h).
+//
+// An MLP nin -> hidden (x nhidden, GELU) -> nout with BF16 operands, FP32
+// accumulation and FP32 master weights trained by Adam.  Feature dimensions
+// are padded to multiples of 128 and batches to multiples of 128 so that
+// every product runs in the tiled tensor-core GEMM of sur_kernels.cu; the
+// padding holds zeros and receives zero gradients.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mossco_sed.h"
+#include "sur_kernels.h"
+
+using bf16 = __nv_bfloat16;
+
+namespace {
+constexpr int kMaxLayers = 8;
+int pad128(int x) { return (x + 127) / 128 * 128; }
+}  // namespace
+
+struct sed_surrogate {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int nin = 0, nout = 0, hidden = 0, nhidden = 0, L = 0, max_batch = 0;
+  int din[kMaxLayers], dout[kMaxLayers], pin[kMaxLayers], pout[kMaxLayers];
+  float *w[kMaxLayers] = {}, *b[kMaxLayers] = {}, *gw[kMaxLayers] = {}, *gb[kMaxLayers] = {};
+  float *mw[kMaxLayers] = {}, *vw[kMaxLayers] = {}, *mb[kMaxLayers] = {}, *vb[kMaxLayers] = {};
+  bf16 *wb[kMaxLayers] = {}, *wbt[kMaxLayers] = {};
+  float* z[kMaxLayers] = {};  // pre-activations [max_batch][pout]
+  bf16* a[kMaxLayers] = {};   // GELU activations of hidden layers
+  bf16 *x = nullptr, *y = nullptr, *dz = nullptr, *dz2 = nullptr, *dzt = nullptr, *at = nullptr;
+  float *mask = nullptr, *loss = nullptr;
+  int step = 0;
+  std::vector<void*> allocs;
+  std::string err;
+
+  int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+  }
+  template <typename T>
+  cudaError_t alloc(T** p, size_t n) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, n * sizeof(T) + 16);
+    if (e == cudaSuccess) {
+      allocs.push_back(q);
+      cudaMemset(q, 0, n * sizeof(T) + 16);
+    }
+    *p = static_cast<T*>(q);
+    return e;
+  }
+  ~sed_surrogate() {
+    cudaSetDevice(device);
+    if (stream) cudaStreamSynchronize(stream);
+    for (void* p : allocs) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+#define SCK(expr, what)                                                        \
+  do {                                                                         \
+    cudaError_t e_ = (expr);                                                   \
+    if (e_ != cudaSuccess)                                                     \
+      return s->fail(SED_E_CUDA, "%s: %s", what, cudaGetErrorString(e_));      \
+  } while (0)
+
+namespace {
+
+// forward pass over m rows already in s->x; output pre-activation in z[L-1]
+int forward(sed_surrogate* s, int m) {
+  const bf16* in = s->x;
+  for (int l = 0; l < s->L; l++) {
+    const bool last = l == s->L - 1;
+    SCK(sur::gemm_nt(last ? sur::EPI_BIAS : sur::EPI_BIAS_GELU, in, s->wb[l], m, s->pout[l],
+                     s->pin[l], s->b[l], s->z[l], last ? nullptr : s->a[l], nullptr,
+                     s->pout[l], s->stream),
+        "forward gemm");
+    in = s->a[l];
+  }
+  return SED_OK;
+}
+
+// loss + backward over m rows (targets in s->y); gradients in gw/gb
+int backward(sed_surrogate* s, int m, int m_valid) {
+  const int Lh = s->L - 1;
+  const int nout_p = s->pout[Lh];
+  SCK(cudaMemsetAsync(s->loss, 0, sizeof(float), s->stream), "loss reset");
+  const float inv = 1.0f / ((float)m_valid * (float)s->nout);
+  SCK(sur::mse(s->z[Lh], s->y, s->mask, m, nout_p, m_valid, inv, s->dz, s->loss, s->stream),
+      "mse");
+  bf16* dcur = s->dz;
+  bf16* dnext = s->dz2;
+  for (int l = Lh; l >= 0; l--) {
+    const int po = s->pout[l], pi = s->pin[l];
+    const bf16* ain = l == 0 ? s->x : s->a[l - 1];
+    // gW = dZ^T A_in : A = dZ^T [po x m], B = A_in^T [pi x m]
+    SCK(sur::transpose_bf16(dcur, s->dzt, m, po, s->stream), "transpose dZ");
+    SCK(sur::transpose_bf16(ain, s->at, m, pi, s->stream), "transpose A");
+    SCK(sur::gemm_nt(sur::EPI_F32, s->dzt, s->at, po, pi, m, nullptr, s->gw[l], nullptr,
+                     nullptr, pi, s->stream),
+        "weight gradient gemm");
+    SCK(cudaMemsetAsync(s->gb[l], 0, po * sizeof(float), s->stream), "gb reset");
+    SCK(sur::bias_grad(dcur, m, po, s->gb[l], s->stream), "bias gradient");
+    if (l > 0) {
+      // dZ_{l-1} = (dZ_l W_l) * GELU'(Z_{l-1}) : A = dZ [m x po], B = W^T [pi x po]
+      SCK(sur::gemm_nt(sur::EPI_GELU_BWD, dcur, s->wbt[l], m, pi, po, nullptr, nullptr, dnext,
+                       s->z[l - 1], pi, s->stream),
+          "input gradient gemm");
+      bf16* t = dcur;
+      dcur = dnext;
+      dnext = t;
+    }
+  }
+  return SED_OK;
+}
+
+void host_bf16(const float* src, int rows, int cols, int pcols, std::vector<bf16>& out) {
+  out.assign((size_t)rows * pcols, __float2bfloat16(0.0f));
+  for (int r = 0; r < rows; r++)
+    for (int c = 0; c < cols; c++) out[(size_t)r * pcols + c] = __float2bfloat16(src[(size_t)r * cols + c]);
+}
+
+int upload_rows(sed_surrogate* s, const float* x, int m, int cols, int pcols, bf16* dst) {
+  std::vector<bf16> tmp;
+  host_bf16(x, m, cols, pcols, tmp);
+  SCK(cudaMemsetAsync(dst, 0, (size_t)pad128(m) * pcols * sizeof(bf16), s->stream), "pad clear");
+  SCK(cudaMemcpyAsync(dst, tmp.data(), tmp.size() * sizeof(bf16), cudaMemcpyHostToDevice,
+                      s->stream),
+      "rows copy");
+  SCK(cudaStreamSynchronize(s->stream), "rows copy");
+  return SED_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sed_sur_create(int nin, int nout, int hidden, int nhidden, int max_batch,
+                   unsigned long long seed, int device, sed_surrogate** out) {
+  if (!out) return SED_E_ARG;
+  *out = nullptr;
+  if (nin <= 0 || nout <= 0 || hidden <= 0 || nhidden < 1 || nhidden + 1 > kMaxLayers ||
+      max_batch <= 0)
+    return SED_E_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return SED_E_NODEVICE;
+  }
+  if (device < 0 || device >= ndev) return SED_E_ARG;
+  sed_surrogate* s = new sed_surrogate();
+  s->device = device;
+  s->nin = nin;
+  s->nout = nout;
+  s->hidden = hidden;
+  s->nhidden = nhidden;
+  s->L = nhidden + 1;
+  s->max_batch = pad128(max_batch);
+  auto bail = [&](int rc) { delete s; return rc; };
+  if (cudaSetDevice(device) != cudaSuccess) return bail(SED_E_CUDA);
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(SED_E_CUDA);
+  int maxd = 0;
+  for (int l = 0; l < s->L; l++) {
+    s->din[l] = l == 0 ? nin : hidden;
+    s->dout[l] = l == s->L - 1 ? nout : hidden;
+    s->pin[l] = pad128(s->din[l]);
+    s->pout[l] = pad128(s->dout[l]);
+    maxd = std::max(maxd, std::max(s->pin[l], s->pout[l]));
+  }
+  const size_t B = s->max_batch;
+  bool ok = true;
+  for (int l = 0; l < s->L && ok; l++) {
+    const size_t nw = (size_t)s->pout[l] * s->pin[l], nb = s->pout[l];
+    ok = s->alloc(&s->w[l], nw) == cudaSuccess && s->alloc(&s->gw[l], nw) == cudaSuccess &&
+         s->alloc(&s->mw[l], nw) == cudaSuccess && s->alloc(&s->vw[l], nw) == cudaSuccess &&
+         s->alloc(&s->b[l], nb) == cudaSuccess && s->alloc(&s->gb[l], nb) == cudaSuccess &&
+         s->alloc(&s->mb[l], nb) == cudaSuccess && s->alloc(&s->vb[l], nb) == cudaSuccess &&
+         s->alloc(&s->wb[l], nw) == cudaSuccess && s->alloc(&s->wbt[l], nw) == cudaSuccess &&
+         s->alloc(&s->z[l], B * s->pout[l]) == cudaSuccess &&
+         (l == s->L - 1 || s->alloc(&s->a[l], B * s->pout[l]) == cudaSuccess);
+  }
+  ok = ok && s->alloc(&s->x, B * s->pin[0]) == cudaSuccess &&
+       s->alloc(&s->y, B * s->pout[s->L - 1]) == cudaSuccess &&
+       s->alloc(&s->dz, B * maxd) == cudaSuccess && s->alloc(&s->dz2, B * maxd) == cudaSuccess &&
+       s->alloc(&s->dzt, B * maxd) == cudaSuccess && s->alloc(&s->at, B * maxd) == cudaSuccess &&
+       s->alloc(&s->mask, (size_t)s->pout[s->L - 1]) == cudaSuccess &&
+       s->alloc(&s->loss, 4) == cudaSuccess;
+  if (!ok) return bail(SED_E_NOMEM);
+  // output mask; initial weights U(-1/sqrt(in), 1/sqrt(in)), zero biases
+  std::vector<float> mask(s->pout[s->L - 1], 0.0f);
+  for (int c = 0; c < nout; c++) mask[c] = 1.0f;
+  cudaMemcpy(s->mask, mask.data(), mask.size() * sizeof(float), cudaMemcpyHostToDevice);
+  unsigned long long st = seed ? seed : 0x9E3779B97F4A7C15ull;
+  auto rnd = [&]() {
+    st += 0x9E3779B97F4A7C15ull;
+    unsigned long long z = st;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+  };
+  for (int l = 0; l < s->L; l++) {
+    std::vector<float> w((size_t)s->pout[l] * s->pin[l], 0.0f);
+    const double a = 1.0 / std::sqrt((double)s->din[l]);
+    for (int r = 0; r < s->dout[l]; r++)
+      for (int c = 0; c < s->din[l]; c++) w[(size_t)r * s->pin[l] + c] = (float)((2.0 * rnd() - 1.0) * a);
+    if (cudaMemcpy(s->w[l], w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        sur::to_bf16(s->w[l], s->pout[l], s->pin[l], s->wb[l], s->wbt[l], s->stream) != cudaSuccess)
+      return bail(SED_E_CUDA);
+  }
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess) return bail(SED_E_CUDA);
+  *out = s;
+  return SED_OK;
+}
+
+int sed_sur_num_params(const sed_surrogate* s) {
+  if (!s) return SED_E_ARG;
+  int n = 0;
+  for (int l = 0; l < s->L; l++) n += s->dout[l] * s->din[l] + s->dout[l];
+  return n;
+}
+
+// Parameter layout (unpadded, FP32): for each layer W[out][in] then b[out].
+int sed_sur_set_weights(sed_surrogate* s, const float* params) {
+  if (!s || !params) return SED_E_ARG;
+  SCK(cudaSetDevice(s->device), "set device");
+  size_t o = 0;
+  for (int l = 0; l < s->L; l++) {
+    std::vector<float> w((size_t)s->pout[l] * s->pin[l], 0.0f), b(s->pout[l], 0.0f);
+    for (int r = 0; r < s->dout[l]; r++)
+      for (int c = 0; c < s->din[l]; c++) w[(size_t)r * s->pin[l] + c] = params[o++];
+    for (int r = 0; r < s->dout[l]; r++) b[r] = params[o++];
+    SCK(cudaMemcpy(s->w[l], w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice), "w");
+    SCK(cudaMemcpy(s->b[l], b.data(), b.size() * sizeof(float), cudaMemcpyHostToDevice), "b");
+    SCK(sur::to_bf16(s->w[l], s->pout[l], s->pin[l], s->wb[l], s->wbt[l], s->stream), "bf16");
+  }
+  SCK(cudaStreamSynchronize(s->stream), "set weights");
+  return SED_OK;
+}
+
+static int fetch_params(sed_surrogate* s, float* const* src_w, float* const* src_b, float* out) {
+  SCK(cudaStreamSynchronize(s->stream), "sync");
+  size_t o = 0;
+  for (int l = 0; l < s->L; l++) {
+    std::vector<float> w((size_t)s->pout[l] * s->pin[l]), b(s->pout[l]);
+    SCK(cudaMemcpy(w.data(), src_w[l], w.size() * sizeof(float), cudaMemcpyDeviceToHost), "w");
+    SCK(cudaMemcpy(b.data(), src_b[l], b.size() * sizeof(float), cudaMemcpyDeviceToHost), "b");
+    for (int r = 0; r < s->dout[l]; r++)
+      for (int c = 0; c < s->din[l]; c++) out[o++] = w[(size_t)r * s->pin[l] + c];
+    for (int r = 0; r < s->dout[l]; r++) out[o++] = b[r];
+  }
+  return SED_OK;
+}
+
+int sed_sur_get_weights(sed_surrogate* s, float* params) {
+  if (!s || !params) return SED_E_ARG;
+  SCK(cudaSetDevice(s->device), "set device");
+  return fetch_params(s, s->w, s->b, params);
+}
+
+// Forward pass on host rows x[m][nin] -> y[m][nout].
+int sed_sur_forward(sed_surrogate* s, const float* x, float* y, int m) {
+  if (!s || !x || !y || m <= 0) return SED_E_ARG;
+  SCK(cudaSetDevice(s->device), "set device");
+  const int nlast = s->pout[s->L - 1];
+  for (int r0 = 0; r0 < m; r0 += s->max_batch) {
+    const int mm = std::min(s->max_batch, m - r0);
+    const int mp = pad128(mm);
+    int rc = upload_rows(s, x + (size_t)r0 * s->nin, mm, s->nin, s->pin[0], s->x);
+    if (rc) return rc;
+    if ((rc = forward(s, mp))) return rc;
+    std::vector<float> out((size_t)mm * nlast);
+    SCK(cudaMemcpyAsync(out.data(), s->z[s->L - 1], out.size() * sizeof(float),
+                        cudaMemcpyDeviceToHost, s->stream), "y copy");
+    SCK(cudaStreamSynchronize(s->stream), "forward");
+    for (int r = 0; r < mm; r++)
+      for (int c = 0; c < s->nout; c++) y[(size_t)(r0 + r) * s->nout + c] = out[(size_t)r * nlast + c];
+  }
+  return SED_OK;
+}
+
+// Forward pass on device rows: x BF16 [m][pad128(nin)], y FP32
+// [m][pad128(nout)], m a multiple of 128 (at most max_batch per launch
+// group; larger m is processed in chunks).
+int sed_sur_forward_device(sed_surrogate* s, const void* x_dev, void* y_dev, int m) {
+  if (!s || !x_dev || !y_dev || m <= 0 || m % 128) return SED_E_ARG;
+  SCK(cudaSetDevice(s->device), "set device");
+  const int nlast = s->pout[s->L - 1];
+  for (int r0 = 0; r0 < m; r0 += s->max_batch) {
+    const int mm = std::min(s->max_batch, m - r0);
+    SCK(cudaMemcpyAsync(s->x, static_cast<const bf16*>(x_dev) + (size_t)r0 * s->pin[0],
+                        (size_t)mm * s->pin[0] * sizeof(bf16), cudaMemcpyDeviceToDevice,
+                        s->stream), "x copy");
+    int rc = forward(s, mm);
+    if (rc) return rc;
+    SCK(cudaMemcpyAsync(static_cast<float*>(y_dev) + (size_t)r0 * nlast, s->z[s->L - 1],
+                        (size_t)mm * nlast * sizeof(float), cudaMemcpyDeviceToDevice,
+                        s->stream), "y copy");
+  }
+  SCK(cudaStreamSynchronize(s->stream), "forward");
+  return SED_OK;
+}
+
+// One Adam step on a device batch: x BF16 [m][pad128(nin)], y BF16
+// [m][pad128(nout)], m a multiple of 128 and <= max_batch.  loss (host) may
+// be NULL (no synchronisation then).
+int sed_sur_train_step(sed_surrogate* s, const void* x_dev, const void* y_dev, int m,
+                       float lr, float* loss) {
+  if (!s || !x_dev || !y_dev || m <= 0 || m % 128 || m > s->max_batch) return SED_E_ARG;
+  SCK(cudaSetDevice(s->device), "set device");
+  SCK(cudaMemcpyAsync(s->x, x_dev, (size_t)m * s->pin[0] * sizeof(bf16),
+                      cudaMemcpyDeviceToDevice, s->stream), "x copy");
+  SCK(cudaMemcpyAsync(s->y, y_dev, (size_t)m * s->pout[s->L - 1] * sizeof(bf16),
+                      cudaMemcpyDeviceToDevice, s->stream), "y copy");
+  int rc = forward(s, m);
+  if (rc) return rc;
+  if ((rc = backward(s, m, m))) return rc;
+  s->step++;
+  for (int l = 0; l < s->L; l++) {
+    const int nw = s->pout[l] * s->pin[l];
+    SCK(sur::adam(s->w[l], s->mw[l], s->vw[l], s->gw[l], nw, lr, 0.9f, 0.999f, 1e-8f, s->step,
+                  s->wb[l], s->wbt[l], s->pout[l], s->pin[l], s->stream), "adam w");
+    SCK(sur::adam(s->b[l], s->mb[l], s->vb[l], s->gb[l], s->pout[l], lr, 0.9f, 0.999f, 1e-8f,
+                  s->step, nullptr, nullptr, 1, s->pout[l], s->stream), "adam b");
+  }
+  if (loss) {
+    SCK(cudaMemcpyAsync(loss, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->stream), "loss");
+    SCK(cudaStreamSynchronize(s->stream), "train step");
+  }
+  return SED_OK;
+}
+
+// Loss and parameter gradients (layout of sed_sur_get_weights) for host
+// rows x[m][nin], y[m][nout]; the weights are not updated.
+int sed_sur_grads(sed_surrogate* s, const float* x, const float* y, int m, float* grads,
+                  float* loss) {
+  if (!s || !x || !y || !grads || m <= 0 || m > s->max_batch) return SED_E_ARG;
+  SCK(cudaSetDevice(s->device), "set device");
+  const int mp = pad128(m);
+  int rc = upload_rows(s, x, m, s->nin, s->pin[0], s->x);
+  if (rc) return rc;
+  if ((rc = upload_rows(s, y, m, s->nout, s->pout[s->L - 1], s->y))) return rc;
+  if ((rc = forward(s, mp))) return rc;
+  if ((rc = backward(s, mp, m))) return rc;
+  if (loss) SCK(cudaMemcpyAsync(loss, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->stream), "loss");
+  return fetch_params(s, s->gw, s->gb, grads);
+}
+
+const char* sed_sur_last_error(const sed_surrogate* s) { return s ? s->err.c_str() : ""; }
+
+void sed_sur_destroy(sed_surrogate* s) { delete s; }
+
+}  // extern "C"

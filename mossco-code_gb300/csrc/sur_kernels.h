@@ -1,0 +1,27 @@
+// sur_kernels.h -- launchers of the surrogate's tensor-core kernels.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace sur {
+
+enum : int { EPI_BIAS_GELU = 0, EPI_BIAS = 1, EPI_F32 = 2, EPI_GELU_BWD = 3 };
+
+// C[M x N] = A[M x K] . B[N x K]^T; M % 128 == 0, N % 64 == 0, K % 32 == 0
+cudaError_t gemm_nt(int epi, const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N,
+                    int K, const float* bias, float* out_f32, __nv_bfloat16* out_bf16,
+                    const float* zprev, int ld_out, cudaStream_t st);
+cudaError_t transpose_bf16(const __nv_bfloat16* in, __nv_bfloat16* out, int rows, int cols,
+                           cudaStream_t st);
+cudaError_t mse(const float* yhat, const __nv_bfloat16* y, const float* mask, int M, int N,
+                int m_valid, float inv_count, __nv_bfloat16* dy, float* loss,
+                cudaStream_t st);
+cudaError_t bias_grad(const __nv_bfloat16* dz, int M, int N, float* db, cudaStream_t st);
+cudaError_t adam(float* w, float* m, float* v, const float* g, int n, float lr, float b1,
+                 float b2, float eps, int step, __nv_bfloat16* wb, __nv_bfloat16* wbt,
+                 int rows, int cols, cudaStream_t st);
+cudaError_t to_bf16(const float* w, int rows, int cols, __nv_bfloat16* wb,
+                    __nv_bfloat16* wbt, cudaStream_t st);
+
+}  // namespace sur

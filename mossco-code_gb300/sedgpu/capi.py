@@ -67,6 +67,7 @@ class SedStats(ctypes.Structure):
 
 
 _dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
 _ip = ctypes.POINTER(ctypes.c_int)
 _vp = ctypes.c_void_p
 _H = ctypes.c_void_p
@@ -98,6 +99,20 @@ SIGNATURES = {
         ctypes.POINTER(SedParams), ctypes.c_int, ctypes.c_int, ctypes.c_int,
         _dp, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp, ctypes.c_double,
         ctypes.c_int, ctypes.POINTER(SedStats)]),
+    "sed_sur_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_ulonglong, ctypes.c_int,
+                                      ctypes.POINTER(_H)]),
+    "sed_sur_num_params": (ctypes.c_int, [_H]),
+    "sed_sur_set_weights": (ctypes.c_int, [_H, _fp]),
+    "sed_sur_get_weights": (ctypes.c_int, [_H, _fp]),
+    "sed_sur_forward": (ctypes.c_int, [_H, _fp, _fp, ctypes.c_int]),
+    "sed_sur_forward_device": (ctypes.c_int, [_H, _vp, _vp, ctypes.c_int]),
+    "sed_sur_train_step": (ctypes.c_int, [_H, _vp, _vp, ctypes.c_int,
+                                          ctypes.c_float, _fp]),
+    "sed_sur_grads": (ctypes.c_int, [_H, _fp, _fp, ctypes.c_int, _fp, _fp]),
+    "sed_sur_last_error": (ctypes.c_char_p, [_H]),
+    "sed_sur_destroy": (None, [_H]),
     "sed_error_string": (ctypes.c_char_p, [ctypes.c_int]),
     "sed_last_error": (ctypes.c_char_p, [_H]),
     "sed_tracer_name": (ctypes.c_char_p, [ctypes.c_int]),

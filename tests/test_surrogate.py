@@ -1,0 +1,130 @@
+"""Surrogate MLP kernels: the FP64 reference is checked by finite
+differences on the CPU; the GPU forward pass and gradients (BF16 tensor-core
+products, FP32 accumulation) are checked against it; training reduces the
+loss."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import mlp_oracle as M
+
+SHAPE = dict(nin=343, nout=330, hidden=256, nhidden=4)
+
+
+def test_reference_mlp_finite_differences():
+    rng = np.random.default_rng(0)
+    shapes = M.layer_shapes(7, 5, 6, 2)
+    n = sum(r * c + r for r, c in shapes)
+    p = rng.normal(0, 0.5, n)
+    x = rng.normal(0, 1, (9, 7))
+    y = rng.normal(0, 1, (9, 5))
+    loss, g = M.loss_and_grads(p, shapes, x, y)
+    h = 1e-6
+    for i in rng.choice(n, 25, replace=False):
+        q = p.copy()
+        q[i] += h
+        lp, _ = M.loss_and_grads(q, shapes, x, y)
+        q[i] -= 2 * h
+        lm, _ = M.loss_and_grads(q, shapes, x, y)
+        assert abs((lp - lm) / (2 * h) - g[i]) < 1e-6 * max(1.0, abs(g[i]))
+
+
+def test_bf16_rounding_matches_definition():
+    v = np.array([1.0, 1.00390625, 1.01171875, 1.001953125, 3.14159],
+                 dtype=np.float32)
+    r = M.bf16_round(v)
+    # 1 + 2^-8 and 1 + 3 2^-8 are ties: to the even significand
+    assert r[0] == 1.0 and r[1] == 1.0 and r[2] == 1.015625 and r[3] == 1.0
+    assert r[4] == 3.140625
+
+
+def _sur(nin, nout, hidden, nhidden, batch, seed=3):
+    from sedgpu import capi
+    lib = capi.load()
+    h = capi._H()
+    rc = lib.sed_sur_create(nin, nout, hidden, nhidden, batch, seed, 0, ctypes.byref(h))
+    assert rc == 0, rc
+    return lib, h
+
+
+def _fp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+@pytest.mark.gpu
+def test_gpu_forward_and_gradients_match_fp64_reference():
+    lib, h = _sur(**SHAPE, batch=256)
+    try:
+        shapes = M.layer_shapes(**SHAPE)
+        n = lib.sed_sur_num_params(h)
+        assert n == sum(r * c + r for r, c in shapes)
+        rng = np.random.default_rng(1)
+        params = rng.normal(0, 1, n).astype(np.float32)
+        o = 0
+        for r, c in shapes:   # scale so activations stay O(1)
+            params[o:o + r * c] *= 1.0 / np.sqrt(c)
+            o += r * c + r
+        assert lib.sed_sur_set_weights(h, _fp(params)) == 0
+        m = 200  # not a multiple of 128: padded rows must not count
+        x = rng.normal(0, 1, (m, SHAPE["nin"])).astype(np.float32)
+        y = (0.3 * rng.normal(0, 1, (m, SHAPE["nout"]))).astype(np.float32)
+        # reference with the BF16 rounding of the GPU operands
+        pb = params.astype(np.float64).copy()
+        o = 0
+        for r, c in shapes:
+            pb[o:o + r * c] = M.bf16_round(params[o:o + r * c])
+            o += r * c + r
+        xb = M.bf16_round(x)
+        yb = M.bf16_round(y)
+        yref, _, _ = M.forward(pb, shapes, xb)
+        yg = np.zeros((m, SHAPE["nout"]), dtype=np.float32)
+        assert lib.sed_sur_forward(h, _fp(x), _fp(yg), m) == 0
+        rel = np.linalg.norm(yg - yref) / np.linalg.norm(yref)
+        assert rel < 1e-2, rel
+        lref, gref = M.loss_and_grads(pb, shapes, xb, yb)
+        g = np.zeros(n, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        assert lib.sed_sur_grads(h, _fp(x), _fp(y), m, _fp(g), _fp(loss)) == 0
+        assert abs(loss[0] - lref) < 2e-2 * lref
+        o = 0
+        for r, c in shapes:
+            for blk in (slice(o, o + r * c), slice(o + r * c, o + r * c + r)):
+                a, b = g[blk].astype(np.float64), gref[blk]
+                relg = np.linalg.norm(a - b) / np.linalg.norm(b)
+                cos = a @ b / (np.linalg.norm(a) * np.linalg.norm(b))
+                assert relg < 5e-2 and cos > 0.998, (relg, cos)
+            o += r * c + r
+    finally:
+        lib.sed_sur_destroy(h)
+
+
+@pytest.mark.gpu
+def test_gpu_training_reduces_loss():
+    import torch
+    lib, h = _sur(**SHAPE, batch=1024)
+    try:
+        rng = np.random.default_rng(2)
+        m = 1024
+        A = rng.normal(0, 1 / np.sqrt(SHAPE["nin"]), (SHAPE["nin"], SHAPE["nout"]))
+        x = rng.normal(0, 1, (m, SHAPE["nin"]))
+        y = np.tanh(x @ A)
+        xp = np.zeros((m, 384), dtype=np.float32)
+        yp = np.zeros((m, 384), dtype=np.float32)
+        xp[:, :SHAPE["nin"]] = x
+        yp[:, :SHAPE["nout"]] = y
+        xd = torch.tensor(xp, device="cuda").to(torch.bfloat16).contiguous()
+        yd = torch.tensor(yp, device="cuda").to(torch.bfloat16).contiguous()
+        torch.cuda.synchronize()
+        loss = np.zeros(1, dtype=np.float32)
+        losses = []
+        for it in range(300):
+            rc = lib.sed_sur_train_step(h, ctypes.c_void_p(xd.data_ptr()),
+                                        ctypes.c_void_p(yd.data_ptr()), m, 1e-3,
+                                        _fp(loss) if it % 50 == 0 or it == 299 else None)
+            assert rc == 0, lib.sed_sur_last_error(h)
+            if it % 50 == 0 or it == 299:
+                losses.append(float(loss[0]))
+        assert losses[-1] < 0.1 * losses[0], losses
+    finally:
+        lib.sed_sur_destroy(h)
