@@ -103,6 +103,7 @@ typedef struct sed_stats {
   double min_dt;          /* smallest accepted substep (s) */
   double device_ms;       /* device time of the call's steps (CUDA events
                              on the handle's stream) */
+  long long surrogate_columns; /* column-steps taken by the surrogate */
 } sed_stats;
 
 typedef struct sed_handle sed_handle;
@@ -219,6 +220,18 @@ int sed_sur_train_step(sed_surrogate *s, const void *x_dev, const void *y_dev,
 int sed_sur_grads(sed_surrogate *s, const float *x, const float *y, int m,
                   float *grads, float *loss);
 const char *sed_sur_last_error(const sed_surrogate *s);
+/* Normalisation of the column surrogate, n = 11 + 2 nin + 2 nout floats:
+ * c0[11] | mu_x[nin] | sd_x[nin] | mu_d[nout] | sd_d[nout], with nin =
+ * 11 K + 13 and nout = 11 K for a grid of K layers. */
+int sed_sur_set_norm(sed_surrogate *s, const float *norm, int n);
+/* nsteps coupling steps with the surrogate proposing every column's state;
+ * a column is accepted when its backward-Euler defect
+ * max |C' - C - dt f(C')| / (|C'| + |C| + dt |f(C')| + res_atol) <= tol,
+ * every other column is advanced by the plain adaptive solver.  FP32 state,
+ * all active columns at kmax layers.  stats.surrogate_columns counts the
+ * accepted column-steps. */
+int sed_step_surrogate(sed_handle *h, sed_surrogate *s, double dt, int nsteps,
+                       double tol, double res_atol, sed_stats *stats);
 void sed_sur_destroy(sed_surrogate *s);
 
 const char *sed_error_string(int code);

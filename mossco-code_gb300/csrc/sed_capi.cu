@@ -21,6 +21,8 @@
 #include "../../include/mossco_sed.h"
 #include "sed_launch.h"
 #include "sed_params.h"
+#include "sur_internal.h"
+#include "sur_loop.h"
 
 using namespace sed;
 
@@ -81,7 +83,7 @@ struct sed_handle {
   // device buffers
   DevBuf d_slot_col, d_kact, d_tile_k, d_conc, d_coef, d_cap, d_force, d_sflux,
       d_budget, d_nsub, d_queue, d_stats, d_flag, d_stage, d_bdys, d_fluxes,
-      d_rhs, d_rhs_stage, d_grid, d_force64;
+      d_rhs, d_rhs_stage, d_grid, d_force64, d_prop, d_skip, d_xfeat, d_yhat;
   std::vector<double> force64;  // host forcing rows (FP64 state)
   DevStats* h_stats = nullptr;  // pinned
   int* h_flag = nullptr;        // pinned
@@ -204,6 +206,7 @@ int stats_fetch(sed_handle* h, sed_stats* out, long long launches0,
   if (timed) CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1), "event time");
   if (out) {
     out->device_ms = ms;
+    out->surrogate_columns = (long long)s.surrogate;
     out->attempts = (long long)s.attempts;
     out->accepted = (long long)s.accepted;
     out->column_steps = (long long)s.column_steps;
@@ -773,6 +776,89 @@ int sed_ode_solver(sed_handle* h, double* conc, const double* bdys, double* flux
   if (rc) return rc;
   CK(cudaMemcpyAsync(fluxes, h->d_fluxes.p, (size_t)NTR * h->ncol * sizeof(double),
                      cudaMemcpyDeviceToHost, h->stream), "fluxes copy back");
+  CK(cudaEventRecord(h->ev1, h->stream), "event");
+  return stats_fetch(h, stats, l0, true);
+}
+
+int sed_sur_set_norm(sed_surrogate* s, const float* norm, int n) {
+  if (!s || !norm) return SED_E_ARG;
+  const int need = NTR + 2 * s->nin + 2 * s->nout;
+  if (n != need) return s->fail(SED_E_ARG, "norm has %d values, expected %d", n, need);
+  if (cudaSetDevice(s->device) != cudaSuccess) return SED_E_CUDA;
+  if (!s->norm) {
+    if (s->alloc(&s->norm, (size_t)need) != cudaSuccess) return SED_E_NOMEM;
+  }
+  if (cudaMemcpy(s->norm, norm, need * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+    return SED_E_CUDA;
+  s->norm_len = need;
+  return SED_OK;
+}
+
+int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, double tol,
+                       double res_atol, sed_stats* stats) {
+  int rc = ready(h);
+  if (rc) return rc;
+  if (!s) return h->fail(SED_E_ARG, "no surrogate");
+  if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");
+  if (h->fp64()) return h->fail(SED_E_ARG, "the surrogate step runs on FP32 state");
+  if (s->device != h->device) return h->fail(SED_E_ARG, "surrogate on another device");
+  const int K = h->kmax;
+  if (s->nin != NTR * K + NFORCE || s->nout != NTR * K)
+    return h->fail(SED_E_ARG, "surrogate sized for %d inputs / %d outputs, grid needs %d / %d",
+                   s->nin, s->nout, NTR * K + NFORCE, NTR * K);
+  if (!s->norm) return h->fail(SED_E_STATE, "sed_sur_set_norm has not been called");
+  for (int i = 0; i < h->nslot; i++)
+    if (h->slot_col[i] >= 0 && h->slot_k[i] != K)
+      return h->fail(SED_E_ARG, "the surrogate needs every active column at %d layers", K);
+  if (!(dt > 0.0) || nsteps < 0 || !(tol > 0.0) || !(res_atol >= 0.0))
+    return h->fail(SED_E_ARG, "bad dt, nsteps, tol or res_atol");
+  CK(cudaSetDevice(h->device), "set device");
+  const size_t ns = h->nslot;
+  const int rows = pad128(h->nslot);
+  CK(h->d_prop.alloc((size_t)NTR * K * ns * sizeof(float)), "proposal");
+  CK(h->d_skip.alloc(ns * sizeof(int)), "skip flags");
+  CK(h->d_xfeat.alloc((size_t)rows * s->pin[0] * sizeof(bf16)), "features");
+  CK(h->d_yhat.alloc((size_t)rows * s->pout[s->L - 1] * sizeof(float)), "predictions");
+  const long long l0 = h->launches;
+  if ((rc = stats_reset(h))) return rc;
+  Params<float> p = make_params<float>(h->prm);
+  set_clock(p, dt, h->prm.dt_min);
+  const bool bc4 = h->prm.bcup_particulate == 4;
+  CK(cudaEventRecord(h->ev0, h->stream), "event");
+  for (int step = 0; step < nsteps; step++) {
+    CK(sur::features(h->d_conc.as<float>(), h->d_force.as<float>(), s->norm, K, h->kmax,
+                     h->nslot, rows, s->nin, s->pin[0], h->d_xfeat.as<bf16>(), h->stream),
+       "features");
+    h->launches++;
+    CK(cudaStreamSynchronize(h->stream), "features");
+    rc = sed_sur_forward_device(s, h->d_xfeat.p, h->d_yhat.p, rows);
+    if (rc) return h->fail(rc, "surrogate forward: %s", s->err.c_str());
+    h->launches += 1 + 3 * s->L;
+    CK(sur::apply(h->d_yhat.as<float>(), h->d_conc.as<float>(), s->norm, K, h->kmax,
+                  h->nslot, s->nin, s->nout, s->pout[s->L - 1], h->d_prop.as<float>(),
+                  h->stream),
+       "apply");
+    h->launches++;
+    // residual test of every column, then the plain solver on the rejected
+    for (int kind : {KIND_RESID, KIND_ADAPT}) {
+      CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
+      for (int b = 0; b < h->nbins; b++) {
+        const Bin& bin = h->bins[b];
+        if (bin.ntiles == 0) continue;
+        ColumnArgs<float> a = column_args<float>(h, bin, b, dt, SED_ADAPTIVE_EULER);
+        a.out = h->d_prop.as<float>();
+        a.skip = h->d_skip.as<int>();
+        a.res_tol = tol;
+        a.res_atol = res_atol;
+        const int occ = column_blocks_per_sm<float>(h->tc, bin.lpl, bc4, kind, h->threads);
+        if (occ <= 0) return h->fail(SED_E_CUDA, "residual kernel does not fit");
+        CK(launch_column<float>(a, p, bin.lpl, bc4, kind,
+                                std::min(bin.ntiles, occ * h->sms), h->threads, h->stream),
+           "surrogate step launch");
+        h->launches++;
+      }
+    }
+  }
   CK(cudaEventRecord(h->ev1, h->stream), "event");
   return stats_fetch(h, stats, l0, true);
 }

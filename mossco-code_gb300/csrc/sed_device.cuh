@@ -61,6 +61,7 @@ struct Params {
 };
 
 struct DevStats {
+  unsigned long long surrogate;    // columns whose surrogate step was accepted
   unsigned long long attempts;
   unsigned long long accepted;
   unsigned long long column_steps;

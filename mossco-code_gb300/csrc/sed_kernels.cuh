@@ -28,12 +28,14 @@ namespace sed {
 template <typename real>
 struct TileLayout {
   int tcp, kt;
-  size_t conc, coef, cap, force, sflux, bud, nsub, total;
-  __host__ __device__ TileLayout(int tc, int kt_, bool bc4) : kt(kt_) {
+  size_t conc, conc2, coef, cap, force, sflux, bud, nsub, total;
+  __host__ __device__ TileLayout(int tc, int kt_, bool bc4, bool two_states = false)
+      : kt(kt_) {
     tcp = tc + 16 / (int)sizeof(real);  // row pad keeps 16-byte alignment
     size_t r = sizeof(real);
     conc = 0;
-    coef = conc + (size_t)NTR * kt * tcp * r;
+    conc2 = conc + (size_t)NTR * kt * tcp * r;
+    coef = conc2 + (two_states ? (size_t)NTR * kt * tcp * r : 0);
     cap = coef + (size_t)CoefRows<real>::value * kt * tcp * r;
     force = cap + (bc4 ? (size_t)kt * tcp * r : 0);
     sflux = force + (size_t)NFORCE * tcp * r;
@@ -46,8 +48,8 @@ struct TileLayout {
 };
 
 template <typename real>
-size_t tile_smem_bytes(int tc, int lpl, bool bc4) {
-  return TileLayout<real>(tc, 32 * lpl, bc4).total;
+size_t tile_smem_bytes(int tc, int lpl, bool bc4, int kind) {
+  return TileLayout<real>(tc, 32 * lpl, bc4, kind == KIND_RESID).total;
 }
 
 // Copy `rows` rows of tc reals between global (row stride gstride, first
@@ -543,9 +545,10 @@ k_column(ColumnArgs<real> a, Params<real> p) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int tc = a.tc;
   constexpr int KT = 32 * LPL;
-  TileLayout<real> L(tc, KT, BC4);
+  TileLayout<real> L(tc, KT, BC4, KIND == KIND_RESID);
   const int tcp = L.tcp;
   real* s_conc = reinterpret_cast<real*>(smem + L.conc);
+  real* s_conc2 = reinterpret_cast<real*>(smem + L.conc2);
   real* s_coef = reinterpret_cast<real*>(smem + L.coef);
   real* s_cap = reinterpret_cast<real*>(smem + L.cap);
   real* s_force = reinterpret_cast<real*>(smem + L.force);
@@ -553,13 +556,13 @@ k_column(ColumnArgs<real> a, Params<real> p) {
   double* s_bud = reinterpret_cast<double*>(smem + L.bud);
   int* s_nsub = reinterpret_cast<int*>(smem + L.nsub);
   __shared__ int s_tile, s_next;
-  __shared__ unsigned long long b_att, b_acc, b_cols, b_mindt;
+  __shared__ unsigned long long b_att, b_acc, b_cols, b_mindt, b_sur;
   __shared__ int b_maxatt, b_cap, b_nan;
 
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lane = tid & 31;
   if (tid == 0) {
-    b_att = 0; b_acc = 0; b_cols = 0; b_mindt = 0x7FF0000000000000ull;
+    b_att = 0; b_acc = 0; b_cols = 0; b_sur = 0; b_mindt = 0x7FF0000000000000ull;
     b_maxatt = 0; b_cap = 0; b_nan = 0;
   }
   const size_t ns = (size_t)a.nslot;
@@ -572,9 +575,12 @@ k_column(ColumnArgs<real> a, Params<real> p) {
     const int t = a.tile0 + tile;
     const int slot0 = t * tc;
     const int kt = a.tile_k[t];
-    // stage in
-    copy_grouped<real, true>(s_conc, a.conc + slot0, NTR, kt, KT, a.kmax, ns,
-                             tc, tcp, tid, nthr);
+    // stage in (KIND_RESID: the proposed state, and the start state)
+    copy_grouped<real, true>(s_conc, (KIND == KIND_RESID ? a.out : a.conc) + slot0, NTR,
+                             kt, KT, a.kmax, ns, tc, tcp, tid, nthr);
+    if (KIND == KIND_RESID)
+      copy_grouped<real, true>(s_conc2, a.conc + slot0, NTR, kt, KT, a.kmax, ns, tc,
+                               tcp, tid, nthr);
     copy_grouped<real, true>(s_coef, const_cast<real*>(a.coef) + slot0,
                              CoefRows<real>::value, kt, KT, a.kmax, ns, tc, tcp,
                              tid, nthr);
@@ -591,7 +597,18 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       j = __shfl_sync(FULL, j, 0);
       if (j >= tc) break;
       const int K = a.kact[slot0 + j];
+      if (KIND != KIND_RESID && K > 0 && a.skip && a.skip[slot0 + j]) {
+        // accepted surrogate step: state and surface flux already in place
+        if (lane == 0) {
+          s_nsub[j] = 0;
+#pragma unroll
+          for (int d = 0; d < NDISS; d++) s_sflux[d * tcp + j] = a.sflux[d * ns + slot0 + j];
+          for (int b = 0; b < 4; b++) s_bud[b * tc + j] = 0.0;
+        }
+        continue;
+      }
       if (K <= 0) {
+        if (KIND == KIND_RESID && lane == 0) a.skip[slot0 + j] = 0;
         if (lane == 0) {
           s_nsub[j] = 0;
 #pragma unroll
@@ -607,6 +624,53 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       real ftop[NTR];
 #pragma unroll
       for (int n = 0; n < NTR; n++) ftop[n] = real(0);
+      if (KIND == KIND_RESID) {
+        // backward-Euler defect of the proposed state C' over the step:
+        // |C' - C - dt f(C')| / (|C'| + |C| + dt |f(C')| + atol)
+        real R[LPL][NTR];
+        real dn[LPL];
+        rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+        const real dtr = (real)a.dt, at = (real)a.res_atol;
+        real rho = real(0);
+#pragma unroll
+        for (int s = 0; s < LPL; s++) {
+          const int Ll = s * 32 + lane;
+          if (Ll < K) {
+#pragma unroll
+            for (int n = 0; n < NTR; n++) {
+              const real c0 = s_conc2[(n * KT + Ll) * tcp + j];
+              const real num = fabs(C[s][n] - c0 - dtr * R[s][n]);
+              const real den = fabs(C[s][n]) + fabs(c0) + dtr * fabs(R[s][n]) + at;
+              rho = fmax(rho, num / den);
+            }
+          }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) rho = fmax(rho, __shfl_xor_sync(FULL, rho, o));
+        const bool pass = rho <= (real)a.res_tol;  // NaN fails
+        if (!pass) {  // hand the start state back for the fallback step
+#pragma unroll
+          for (int s = 0; s < LPL; s++) {
+            const int Ll = s * 32 + lane;
+            if (Ll < K)
+#pragma unroll
+              for (int n = 0; n < NTR; n++)
+                s_conc[(n * KT + Ll) * tcp + j] = s_conc2[(n * KT + Ll) * tcp + j];
+          }
+        }
+        if (lane == 0) {
+          a.skip[slot0 + j] = pass ? 1 : 0;
+#pragma unroll
+          for (int d = 0; d < NDISS; d++) s_sflux[d * tcp + j] = ftop[NPART + d];
+          s_nsub[j] = 0;
+          for (int b = 0; b < 4; b++) s_bud[b * tc + j] = 0.0;
+          if (pass) {
+            atomicAdd(&b_sur, 1ull);
+            atomicAdd(&b_cols, 1ull);
+          }
+        }
+        continue;
+      }
       if (KIND == KIND_RHS) {
         real R[LPL][NTR];
         real dn[LPL];
@@ -670,6 +734,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
   }
   __syncthreads();
   if (tid == 0 && mode == 0) {
+    atomicAdd(&a.stats->surrogate, b_sur);
     atomicAdd(&a.stats->attempts, b_att);
     atomicAdd(&a.stats->accepted, b_acc);
     atomicAdd(&a.stats->column_steps, b_cols);
@@ -905,7 +970,7 @@ static cudaError_t launch_column_t(const ColumnArgs<real>& a, const Params<real>
                                    int blocks, int threads, cudaStream_t st) {
   // the shared-memory limit was raised by column_blocks_per_sm at set-up, so
   // this launch makes no attribute call and can be stream-captured
-  const size_t smem = tile_smem_bytes<real>(a.tc, LPL, BC4);
+  const size_t smem = tile_smem_bytes<real>(a.tc, LPL, BC4, KIND);
   k_column<real, LPL, BC4, KIND><<<blocks, threads, smem, st>>>(a, p);
   return cudaGetLastError();
 }
@@ -918,6 +983,8 @@ static cudaError_t launch_column_k(const ColumnArgs<real>& a, const Params<real>
     return launch_column_t<real, LPL, BC4, KIND_ADAPT>(a, p, blocks, threads, st);
   if (kind == KIND_FIXED)
     return launch_column_t<real, LPL, BC4, KIND_FIXED>(a, p, blocks, threads, st);
+  if (kind == KIND_RESID)
+    return launch_column_t<real, LPL, BC4, KIND_RESID>(a, p, blocks, threads, st);
   return launch_column_t<real, LPL, BC4, KIND_RHS>(a, p, blocks, threads, st);
 }
 
@@ -934,7 +1001,7 @@ cudaError_t launch_column(const ColumnArgs<real>& a, const Params<real>& p,
 
 template <typename real, int LPL, bool BC4, int KIND>
 static int occupancy_t(int tc, int threads) {
-  const size_t smem = tile_smem_bytes<real>(tc, LPL, BC4);
+  const size_t smem = tile_smem_bytes<real>(tc, LPL, BC4, KIND);
   auto fn = k_column<real, LPL, BC4, KIND>;
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -949,6 +1016,7 @@ template <typename real, int LPL, bool BC4>
 static int occupancy_k(int tc, int kind, int threads) {
   if (kind == KIND_ADAPT) return occupancy_t<real, LPL, BC4, KIND_ADAPT>(tc, threads);
   if (kind == KIND_FIXED) return occupancy_t<real, LPL, BC4, KIND_FIXED>(tc, threads);
+  if (kind == KIND_RESID) return occupancy_t<real, LPL, BC4, KIND_RESID>(tc, threads);
   return occupancy_t<real, LPL, BC4, KIND_RHS>(tc, threads);
 }
 
@@ -1045,7 +1113,7 @@ cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
 }
 
 #define SED_INSTANTIATE(real)                                                   \
-  template size_t tile_smem_bytes<real>(int, int, bool);                        \
+  template size_t tile_smem_bytes<real>(int, int, bool, int);                   \
   template cudaError_t launch_column<real>(const ColumnArgs<real>&,             \
                                            const Params<real>&, int, bool, int, \
                                            int, int, cudaStream_t);             \

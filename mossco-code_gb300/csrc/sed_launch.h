@@ -8,7 +8,7 @@
 
 namespace sed {
 
-enum : int { KIND_ADAPT = 0, KIND_FIXED = 1, KIND_RHS = 2 };
+enum : int { KIND_ADAPT = 0, KIND_FIXED = 1, KIND_RHS = 2, KIND_RESID = 3 };
 
 // Arguments of the tile kernel.  Device layouts (slot = compacted column):
 //   conc  [NTR][kmax][nslot]     coef  [CoefRows][kmax][nslot]
@@ -31,10 +31,15 @@ struct ColumnArgs {
   int nslot, kmax, tc, tile0, ntiles;
   double dt;
   int method;
+  // surrogate coupling step: per-slot flags (1 = the surrogate's state was
+  // accepted, the step kernels skip the column) and the residual test of
+  // KIND_RESID (out = proposed state, conc = state at the start of the step)
+  int* skip;
+  double res_tol, res_atol;
 };
 
 template <typename real>
-size_t tile_smem_bytes(int tc, int lpl, bool bc4);
+size_t tile_smem_bytes(int tc, int lpl, bool bc4, int kind = KIND_ADAPT);
 
 template <typename real>
 cudaError_t launch_column(const ColumnArgs<real>& a, const Params<real>& p,

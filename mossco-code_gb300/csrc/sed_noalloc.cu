@@ -288,6 +288,7 @@ extern "C" int sed_ode_solver_noalloc(const sed_params* p, int inum, int jnum,
     memcpy(&md, &bits, sizeof md);
     stats->min_dt = md;
     stats->device_ms = 0.0;
+    stats->surrogate_columns = 0;
   }
   if (s.status & ST_NAN) return SED_E_NAN;
   if (s.status & ST_CAP) return SED_E_SUBSTEP_CAP;

@@ -17,58 +17,8 @@
 #include <vector>
 
 #include "../../include/mossco_sed.h"
+#include "sur_internal.h"
 #include "sur_kernels.h"
-
-using bf16 = __nv_bfloat16;
-
-namespace {
-constexpr int kMaxLayers = 8;
-int pad128(int x) { return (x + 127) / 128 * 128; }
-}  // namespace
-
-struct sed_surrogate {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  int nin = 0, nout = 0, hidden = 0, nhidden = 0, L = 0, max_batch = 0;
-  int din[kMaxLayers], dout[kMaxLayers], pin[kMaxLayers], pout[kMaxLayers];
-  float *w[kMaxLayers] = {}, *b[kMaxLayers] = {}, *gw[kMaxLayers] = {}, *gb[kMaxLayers] = {};
-  float *mw[kMaxLayers] = {}, *vw[kMaxLayers] = {}, *mb[kMaxLayers] = {}, *vb[kMaxLayers] = {};
-  bf16 *wb[kMaxLayers] = {}, *wbt[kMaxLayers] = {};
-  float* z[kMaxLayers] = {};  // pre-activations [max_batch][pout]
-  bf16* a[kMaxLayers] = {};   // GELU activations of hidden layers
-  bf16 *x = nullptr, *y = nullptr, *dz = nullptr, *dz2 = nullptr, *dzt = nullptr, *at = nullptr;
-  float *mask = nullptr, *loss = nullptr;
-  int step = 0;
-  std::vector<void*> allocs;
-  std::string err;
-
-  int fail(int code, const char* fmt, ...) {
-    char buf[512];
-    va_list ap;
-    va_start(ap, fmt);
-    vsnprintf(buf, sizeof buf, fmt, ap);
-    va_end(ap);
-    err = buf;
-    return code;
-  }
-  template <typename T>
-  cudaError_t alloc(T** p, size_t n) {
-    void* q = nullptr;
-    cudaError_t e = cudaMalloc(&q, n * sizeof(T) + 16);
-    if (e == cudaSuccess) {
-      allocs.push_back(q);
-      cudaMemset(q, 0, n * sizeof(T) + 16);
-    }
-    *p = static_cast<T*>(q);
-    return e;
-  }
-  ~sed_surrogate() {
-    cudaSetDevice(device);
-    if (stream) cudaStreamSynchronize(stream);
-    for (void* p : allocs) cudaFree(p);
-    if (stream) cudaStreamDestroy(stream);
-  }
-};
 
 #define SCK(expr, what)                                                        \
   do {                                                                         \
@@ -77,10 +27,8 @@ struct sed_surrogate {
       return s->fail(SED_E_CUDA, "%s: %s", what, cudaGetErrorString(e_));      \
   } while (0)
 
-namespace {
-
 // forward pass over m rows already in s->x; output pre-activation in z[L-1]
-int forward(sed_surrogate* s, int m) {
+int sur_forward_rows(sed_surrogate* s, int m) {
   const bf16* in = s->x;
   for (int l = 0; l < s->L; l++) {
     const bool last = l == s->L - 1;
@@ -92,6 +40,8 @@ int forward(sed_surrogate* s, int m) {
   }
   return SED_OK;
 }
+
+namespace {
 
 // loss + backward over m rows (targets in s->y); gradients in gw/gb
 int backward(sed_surrogate* s, int m, int m_valid) {
@@ -152,7 +102,7 @@ int sed_sur_create(int nin, int nout, int hidden, int nhidden, int max_batch,
                    unsigned long long seed, int device, sed_surrogate** out) {
   if (!out) return SED_E_ARG;
   *out = nullptr;
-  if (nin <= 0 || nout <= 0 || hidden <= 0 || nhidden < 1 || nhidden + 1 > kMaxLayers ||
+  if (nin <= 0 || nout <= 0 || hidden <= 0 || nhidden < 1 || nhidden + 1 > kSurMaxLayers ||
       max_batch <= 0)
     return SED_E_ARG;
   int ndev = 0;
@@ -282,7 +232,7 @@ int sed_sur_forward(sed_surrogate* s, const float* x, float* y, int m) {
     const int mp = pad128(mm);
     int rc = upload_rows(s, x + (size_t)r0 * s->nin, mm, s->nin, s->pin[0], s->x);
     if (rc) return rc;
-    if ((rc = forward(s, mp))) return rc;
+    if ((rc = sur_forward_rows(s, mp))) return rc;
     std::vector<float> out((size_t)mm * nlast);
     SCK(cudaMemcpyAsync(out.data(), s->z[s->L - 1], out.size() * sizeof(float),
                         cudaMemcpyDeviceToHost, s->stream), "y copy");
@@ -305,7 +255,7 @@ int sed_sur_forward_device(sed_surrogate* s, const void* x_dev, void* y_dev, int
     SCK(cudaMemcpyAsync(s->x, static_cast<const bf16*>(x_dev) + (size_t)r0 * s->pin[0],
                         (size_t)mm * s->pin[0] * sizeof(bf16), cudaMemcpyDeviceToDevice,
                         s->stream), "x copy");
-    int rc = forward(s, mm);
+    int rc = sur_forward_rows(s, mm);
     if (rc) return rc;
     SCK(cudaMemcpyAsync(static_cast<float*>(y_dev) + (size_t)r0 * nlast, s->z[s->L - 1],
                         (size_t)mm * nlast * sizeof(float), cudaMemcpyDeviceToDevice,
@@ -326,7 +276,7 @@ int sed_sur_train_step(sed_surrogate* s, const void* x_dev, const void* y_dev, i
                       cudaMemcpyDeviceToDevice, s->stream), "x copy");
   SCK(cudaMemcpyAsync(s->y, y_dev, (size_t)m * s->pout[s->L - 1] * sizeof(bf16),
                       cudaMemcpyDeviceToDevice, s->stream), "y copy");
-  int rc = forward(s, m);
+  int rc = sur_forward_rows(s, m);
   if (rc) return rc;
   if ((rc = backward(s, m, m))) return rc;
   s->step++;
@@ -354,7 +304,7 @@ int sed_sur_grads(sed_surrogate* s, const float* x, const float* y, int m, float
   int rc = upload_rows(s, x, m, s->nin, s->pin[0], s->x);
   if (rc) return rc;
   if ((rc = upload_rows(s, y, m, s->nout, s->pout[s->L - 1], s->y))) return rc;
-  if ((rc = forward(s, mp))) return rc;
+  if ((rc = sur_forward_rows(s, mp))) return rc;
   if ((rc = backward(s, mp, m))) return rc;
   if (loss) SCK(cudaMemcpyAsync(loss, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->stream), "loss");
   return fetch_params(s, s->gw, s->gb, grads);

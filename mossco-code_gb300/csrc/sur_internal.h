@@ -1,0 +1,69 @@
+// sur_internal.h -- the surrogate handle, shared by sur_capi.cu and the
+// surrogate coupling step in sed_capi.cu.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+using bf16 = __nv_bfloat16;
+
+constexpr int kSurMaxLayers = 8;
+inline int pad128(int x) { return (x + 127) / 128 * 128; }
+
+struct sed_surrogate {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int nin = 0, nout = 0, hidden = 0, nhidden = 0, L = 0, max_batch = 0;
+  int din[kSurMaxLayers], dout[kSurMaxLayers], pin[kSurMaxLayers], pout[kSurMaxLayers];
+  float *w[kSurMaxLayers] = {}, *b[kSurMaxLayers] = {}, *gw[kSurMaxLayers] = {}, *gb[kSurMaxLayers] = {};
+  float *mw[kSurMaxLayers] = {}, *vw[kSurMaxLayers] = {}, *mb[kSurMaxLayers] = {}, *vb[kSurMaxLayers] = {};
+  bf16 *wb[kSurMaxLayers] = {}, *wbt[kSurMaxLayers] = {};
+  float* z[kSurMaxLayers] = {};  // pre-activations [max_batch][pout]
+  bf16* a[kSurMaxLayers] = {};   // GELU activations of hidden layers
+  bf16 *x = nullptr, *y = nullptr, *dz = nullptr, *dz2 = nullptr, *dzt = nullptr, *at = nullptr;
+  float *mask = nullptr, *loss = nullptr;
+  int step = 0;
+  // feature and increment normalisation of the column surrogate:
+  // c0[11] | mu_x[nin] | sd_x[nin] | mu_d[nout] | sd_d[nout]
+  float* norm = nullptr;
+  int norm_len = 0;
+  std::vector<void*> allocs;
+  std::string err;
+
+  int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+  }
+  template <typename T>
+  cudaError_t alloc(T** p, size_t n) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, n * sizeof(T) + 16);
+    if (e == cudaSuccess) {
+      allocs.push_back(q);
+      cudaMemset(q, 0, n * sizeof(T) + 16);
+    }
+    *p = static_cast<T*>(q);
+    return e;
+  }
+  ~sed_surrogate() {
+    cudaSetDevice(device);
+    if (stream) cudaStreamSynchronize(stream);
+    for (void* p : allocs) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+
+// forward pass over m rows already in s->x; output pre-activation in z[L-1]
+int sur_forward_rows(sed_surrogate* s, int m);

@@ -22,12 +22,12 @@ LIB_NAME = "libsedgpu.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 
 SOURCES = ["sed_kernels_f32.cu", "sed_kernels_f64.cu", "sed_capi.cu",
-           "sed_noalloc.cu", "sur_kernels.cu", "sur_capi.cu"]
+           "sed_noalloc.cu", "sur_kernels.cu", "sur_capi.cu", "sur_loop.cu"]
 # The FP64 kernels evaluate the reference's arithmetic operation by
 # operation: no multiply-add contraction.
 EXTRA_FLAGS = {"sed_kernels_f64.cu": ["-fmad=false"]}
 HEADERS = ["sed_device.cuh", "sed_kernels.cuh", "sed_launch.h", "sed_params.h",
-           "sur_kernels.h"]
+           "sur_kernels.h", "sur_internal.h", "sur_loop.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no multiply-add contraction either (aarch64 g++ contracts by
 # default), so host-side FP64 forcing rows match the CPU restatement's

@@ -60,7 +60,8 @@ class SedStats(ctypes.Structure):
                 ("nan_cells", ctypes.c_int),
                 ("gpu_launches", ctypes.c_int),
                 ("min_dt", ctypes.c_double),
-                ("device_ms", ctypes.c_double)]
+                ("device_ms", ctypes.c_double),
+                ("surrogate_columns", ctypes.c_longlong)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -113,6 +114,10 @@ SIGNATURES = {
     "sed_sur_grads": (ctypes.c_int, [_H, _fp, _fp, ctypes.c_int, _fp, _fp]),
     "sed_sur_last_error": (ctypes.c_char_p, [_H]),
     "sed_sur_destroy": (None, [_H]),
+    "sed_sur_set_norm": (ctypes.c_int, [_H, _fp, ctypes.c_int]),
+    "sed_step_surrogate": (ctypes.c_int, [_H, _H, ctypes.c_double, ctypes.c_int,
+                                          ctypes.c_double, ctypes.c_double,
+                                          ctypes.POINTER(SedStats)]),
     "sed_error_string": (ctypes.c_char_p, [ctypes.c_int]),
     "sed_last_error": (ctypes.c_char_p, [_H]),
     "sed_tracer_name": (ctypes.c_char_p, [ctypes.c_int]),
