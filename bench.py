@@ -186,6 +186,75 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_surrogate(args) -> None:
+    """Surrogate + fallback coupling steps against the plain solver on the
+    same state (1-GPU).  A network is trained first on pairs generated by the
+    plain solver (a reduced version of the 200k-column training set, so that
+    the run stays within minutes)."""
+    import torch
+    from sedgpu import capi, synth
+    from sedgpu import surrogate as S
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    train_cs = synth.make_workload("surrogate_200k", cols=np.arange(args.sur_train_columns))
+    pairs = S.generate_pairs(train_cs, nsteps=train_cs.nsteps, samples=24, warm=24)
+    nz = S.fit_normalizer(pairs, train_cs.kmax)
+    X, Y = S.training_arrays(pairs, nz)
+    sur = S.Surrogate(train_cs.kmax, batch=8192)
+    sur.set_norm(nz)
+    log = sur.train(X, Y, steps=args.sur_train_steps, lr=1e-3,
+                    log_every=max(1, args.sur_train_steps // 5))
+    t_train = time.perf_counter() - t0
+    cs = synth.make_workload(args.workload)
+    base = capi.Solver(cs)
+    base.set_forcing()
+    base.set_state(cs.conc)
+    base.step(args.warmup)
+    S0 = base.get_state()
+    res = {}
+    for mode in ("plain", "surrogate"):
+        s = capi.Solver(cs)
+        s.set_forcing()
+        s.set_state(S0)
+        if mode == "plain":
+            st = s.step(args.steps)
+        else:
+            st = S.step_surrogate(s, sur, args.steps, tol=args.sur_tol)
+        res[mode] = (st, s.get_state())
+        s.close()
+    base.close()
+    plain_st, plain_state = res["plain"]
+    sur_st, sur_state = res["surrogate"]
+    v_plain = cs.n_active * args.steps / (plain_st["device_ms"] / 1e3)
+    v_sur = cs.n_active * args.steps / (sur_st["device_ms"] / 1e3)
+    act = np.arange(cs.kmax)[:, None] < cs.kact[None, :]
+    errs = []
+    for n in range(NTR):
+        r, x = plain_state[n][act], sur_state[n][act]
+        floor = 1e-4 * max(np.abs(r).max(), 1e-300)
+        errs.append(float(np.max(np.abs(x - r) / (np.abs(r) + floor))))
+    line = {
+        "metric": METRIC, "value": v_sur, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sur_st["device_ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32+bf16",
+        "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "columns": cs.n_active,
+                   "layers": cs.kmax, "solver": "surrogate+fallback",
+                   "residual_tol": args.sur_tol,
+                   "network": f"{S.NTR * cs.kmax + S.NFORCE}->{S.HIDDEN}x{S.NHIDDEN}->{S.NTR * cs.kmax}"},
+        "plain_value": v_plain, "speedup_vs_plain": v_sur / v_plain,
+        "surrogate_fraction": sur_st["surrogate_columns"] / max(sur_st["column_steps"], 1),
+        "max_rel_err_vs_plain": errs,
+        "training": {"columns": args.sur_train_columns, "pairs": int(X.shape[0]),
+                     "steps": args.sur_train_steps, "batch": 8192,
+                     "loss_log": [(int(i), round(l, 5)) for i, l, _ in log],
+                     "seconds": t_train},
+        "gpu_launches": sur_st["gpu_launches"],
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_gpu(args) -> None:
     import torch
     from sedgpu import capi, synth
@@ -377,6 +446,10 @@ def main():
     ap.add_argument("--cpu-columns", type=int, default=8192)
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--acc-columns", type=int, default=4096)
+    ap.add_argument("--solver", default="plain", choices=["plain", "surrogate"])
+    ap.add_argument("--sur-tol", type=float, default=1e-3)
+    ap.add_argument("--sur-train-columns", type=int, default=20000)
+    ap.add_argument("--sur-train-steps", type=int, default=5000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -384,6 +457,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.solver == "surrogate":
+        run_surrogate(args)
     else:
         run_gpu(args)
 
