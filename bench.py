@@ -275,6 +275,12 @@ def run_gpu(args) -> None:
     s.set_state(cs.conc)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
 
+    # launch tuning chosen by the library's autotuner on the warmed-up state
+    # (untimed; it restores the state it found), then the warm-up steps
+    tuning = None
+    if not args.no_autotune:
+        s.step(1)
+        tuning = s.autotune(flags=0 if args.no_e2e else capi.SED_TUNE_PIPELINE)
     for _ in range(args.warmup):
         s.step(1)
 
@@ -371,6 +377,12 @@ def run_gpu(args) -> None:
         e2e = {"value": world * cs.n_active * n_e2e / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "steps": n_e2e, "call": "sed_ode_solver"}
+    t_now = s.tuning().as_dict()
+    s_tuning = {k: t_now[k] for k in ("tile_columns", "threads", "pipeline_chunks",
+                                       "segments")}
+    s_tuning["chosen_by"] = "sed_autotune" if tuning else "defaults"
+    if tuning:
+        s_tuning["autotune_trials"] = tuning["trials"]
     s.close()
 
     if rank != 0:
@@ -412,7 +424,8 @@ def run_gpu(args) -> None:
                    "method": "adaptive_euler", "cut": "per_column",
                    "state": "fp32", "budgets": "fp64",
                    "l2": "flushed between timed steps",
-                   "solver": "plain"},
+                   "solver": "plain",
+                   "tuning": s_tuning},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak,
                      "traffic": MEASURED_TRAFFIC.get(args.workload),
@@ -451,6 +464,7 @@ def main():
     ap.add_argument("--sur-train-columns", type=int, default=20000)
     ap.add_argument("--sur-train-steps", type=int, default=5000)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":

@@ -170,6 +170,47 @@ int sed_set_stream(sed_handle *h, void *stream);
 int sed_host_register(void *ptr, size_t bytes);
 int sed_host_unregister(void *ptr);
 
+/* ------------------------------------------------------------------------
+ * Launch tuning (no counterpart in the reference, whose solver has no
+ * launch parameters).  Index [0] of the per-class fields is the class of
+ * columns with up to 32 active layers (one layer per lane), [1] the class
+ * with 33..64 (two layers per lane).  sed_set_grid lays the active columns
+ * out once (depth class, then `segments` contiguous column ranges balanced
+ * by active layers, each padded to 64 slots), so every tuning below is a
+ * pure launch choice: results are bit-identical under any of them. */
+typedef struct sed_tuning {
+  int tile_columns[2];  /* columns staged per tile: 8, 16, 32 or 64 */
+  int threads[2];       /* threads per block: 64, 128, 192 or 256 */
+  int blocks_per_sm[2]; /* resident blocks per SM of the persistent grid;
+                           0 = as many as fit */
+  int pipeline_chunks;  /* sed_ode_solver: column ranges whose host->device
+                           copy, step and device->host copy run in flight
+                           (1 = copy all, step, copy back); divides segments */
+  int segments;         /* column ranges of the layout (read-only) */
+  int max_attempts;     /* substep cap per column-step (= sed_params one) */
+  float step_ms;        /* sed_autotune: one coupling step, tuned */
+  float ode_solver_ms;  /* sed_autotune with SED_TUNE_PIPELINE: one
+                           sed_ode_solver call, tuned */
+  int trials;           /* sed_autotune: candidate launches timed */
+} sed_tuning;
+
+#define SED_TUNE_PIPELINE 1 /* also time sed_ode_solver's pipeline depth
+                               (pinned host scratch of one FP64 state) */
+#define SED_TUNE_CAP 2      /* also set max_attempts to 4x the largest
+                               per-column attempt count seen (>= 64) */
+
+int sed_get_tuning(const sed_handle *h, sed_tuning *t);
+/* Validates every field (SED_E_ARG) and that each class's tile fits the
+ * device (SED_E_CUDA); the output-only fields are ignored. */
+int sed_set_tuning(sed_handle *h, const sed_tuning *t);
+/* Times candidate tile widths and block sizes per depth class (and, with
+ * flags, the pipeline depth and the substep cap) on the handle's current
+ * state and forcing, keeps the fastest, and restores the state, surface
+ * fluxes and diagnostics it found.  Needs sed_set_state (or a previous
+ * sed_ode_solver) and sed_set_forcing.  out may be NULL. */
+int sed_autotune(sed_handle *h, double dt, int method, int flags,
+                 sed_tuning *out);
+
 /* One coupling step of the drop-in above for callers that cannot allocate
  * device memory (no counterpart in the reference).  Some callers cannot
  * call cudaMalloc: a component whose framework owns the GPU's memory pool

@@ -36,10 +36,26 @@ const char* kTracerNames[SED_NTR] = {
     "dissolved_ammonium",           "dissolved_reduced_substances",
     "dissolved_phosphate"};
 
+// Column ranges of the layout, and work counters: 2 for whole-class
+// launches, 2 per pipeline chunk and class.
+constexpr int kMaxSeg = 8;
+constexpr int kQueues = 2 + 2 * kMaxSeg;
+constexpr int kSlotPad = 64;  // every segment is a multiple of every tile width
+
+// One depth class: its slots, split into the segments of the column ranges,
+// and its launch tuning.
 struct Bin {
   int lpl = 1;
-  int tile0 = 0, ntiles = 0;
-  int blocks = 0;
+  int slot0 = 0, nslots = 0;       // slot range of the class
+  int segb[kMaxSeg + 1] = {};      // segment s = slots [segb[s], segb[s+1])
+  int tc = 32, threads = 256;      // tile width, threads per block
+  int bps = 0;                     // blocks per SM asked for (0 = all that fit)
+  int occ = 0;                     // blocks per SM that fit at (tc, threads)
+  int tk0 = 0;                     // first tile of the class in tile_k
+  int blocks(int sms, int ntiles) const {
+    const int per = (bps > 0 && bps < occ) ? bps : occ;
+    return std::max(1, std::min(ntiles, per * sms));
+  }
 };
 
 struct DevBuf {
@@ -75,15 +91,21 @@ struct sed_handle {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::string err;
   bool have_grid = false, have_forcing = false, have_state = false;
-  // slots
-  int tc = 32, threads = 256, nslot = 0, ntiles = 0, nactive = 0;
+  // slots: depth class, then column segment, then active layers
+  int nslot = 0, nactive = 0;
   std::vector<int> slot_col, slot_k;
   Bin bins[2];
-  int nbins = 0;
+  int nseg = 1;                 // column ranges of the layout
+  std::vector<int> seg_col;     // [nseg + 1] column bounds
+  int pipe = 1;                 // sed_ode_solver pipeline chunks
+  // pipelined sed_ode_solver: copy-in, two step, copy-out streams
+  cudaStream_t s_in = nullptr, s_out = nullptr, s_cmp[2] = {nullptr, nullptr};
+  cudaEvent_t pe_start = nullptr, pe_done = nullptr;
+  cudaEvent_t pe_in[kMaxSeg] = {}, pe_cmp[kMaxSeg] = {};
   // device buffers
   DevBuf d_slot_col, d_kact, d_tile_k, d_conc, d_coef, d_cap, d_force, d_sflux,
       d_budget, d_nsub, d_queue, d_stats, d_flag, d_stage, d_bdys, d_fluxes,
-      d_rhs, d_rhs_stage, d_grid, d_force64, d_prop, d_skip, d_xfeat, d_yhat;
+      d_rhs, d_rhs_stage, d_grid, d_force64, d_prop, d_skip, d_xfeat, d_yhat, d_backup;
   std::vector<double> force64;  // host forcing rows (FP64 state)
   DevStats* h_stats = nullptr;  // pinned
   int* h_flag = nullptr;        // pinned
@@ -160,12 +182,22 @@ ColumnArgs<real> column_args(sed_handle* h, const Bin& b, int bin_index,
   a.stats = h->d_stats.as<DevStats>();
   a.nslot = h->nslot;
   a.kmax = h->kmax;
-  a.tc = h->tc;
-  a.tile0 = b.tile0;
-  a.ntiles = b.ntiles;
+  a.tc = b.tc;
+  a.slot0 = b.slot0;
+  a.tile0 = b.tk0;
+  a.ntiles = b.nslots / b.tc;
   a.dt = dt;
   a.method = method;
   return a;
+}
+
+// restrict a class launch to its slots [s0, s1) (segment bounds)
+template <typename real>
+void restrict_args(ColumnArgs<real>& a, const Bin& b, int s0, int s1, unsigned* queue) {
+  a.slot0 = s0;
+  a.tile0 = b.tk0 + (s0 - b.slot0) / b.tc;
+  a.ntiles = (s1 - s0) / b.tc;
+  a.queue = queue;
 }
 
 // Enqueue the tile kernels of every depth class (one coupling step, or one
@@ -175,12 +207,12 @@ int enqueue_columns(sed_handle* h, double dt, int method, int kind) {
   Params<real> p = make_params<real>(h->prm);
   set_clock(p, dt, h->prm.dt_min);
   CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
-  for (int b = 0; b < h->nbins; b++) {
+  for (int b = 0; b < 2; b++) {
     const Bin& bin = h->bins[b];
-    if (bin.ntiles == 0) continue;
+    if (bin.nslots == 0) continue;
     ColumnArgs<real> a = column_args<real>(h, bin, b, dt, method);
     CK(launch_column<real>(a, p, bin.lpl, h->prm.bcup_particulate == 4, kind,
-                           bin.blocks, h->threads, h->stream),
+                           bin.blocks(h->sms, a.ntiles), bin.threads, h->stream),
        "column kernel launch");
     h->launches++;
   }
@@ -430,10 +462,324 @@ int download_state(sed_handle* h, double* conc) {
   return SED_OK;
 }
 
+// Blocks per SM of a class's tile at its (tc, threads) for every kernel
+// kind the handle launches; 0 when the tile does not fit.
+int class_occupancy(sed_handle* h, const Bin& b, int tc, int threads) {
+  const bool bc4 = h->prm.bcup_particulate == 4;
+  int occ = 1 << 30;
+  for (int kd : {KIND_ADAPT, KIND_FIXED, KIND_RHS}) {
+    const int o = h->fp64() ? column_blocks_per_sm<double>(tc, b.lpl, bc4, kd, threads)
+                            : column_blocks_per_sm<float>(tc, b.lpl, bc4, kd, threads);
+    occ = std::min(occ, o);
+  }
+  return occ;
+}
+
+// Occupancy and per-tile layer counts of the current tuning; raises the
+// kernels' shared-memory limit before any capture and drops the step graph.
+int apply_tuning(sed_handle* h) {
+  std::vector<int> tile_k;
+  for (int b = 0; b < 2; b++) {
+    Bin& bin = h->bins[b];
+    bin.tk0 = (int)tile_k.size();
+    bin.occ = 0;
+    if (bin.nslots == 0) continue;
+    bin.occ = class_occupancy(h, bin, bin.tc, bin.threads);
+    if (bin.occ <= 0)
+      return h->fail(SED_E_CUDA, "tile of %d columns x %d layers does not fit on the device",
+                     bin.tc, 32 * bin.lpl);
+    for (int t = 0; t < bin.nslots / bin.tc; t++) {
+      int m = 1;
+      for (int j = 0; j < bin.tc; j++) m = std::max(m, h->slot_k[bin.slot0 + t * bin.tc + j]);
+      tile_k.push_back(m);
+    }
+  }
+  if (tile_k.empty()) tile_k.push_back(1);
+  CK(h->d_tile_k.alloc(tile_k.size() * sizeof(int)), "tile_k");
+  CK(cudaMemcpyAsync(h->d_tile_k.p, tile_k.data(), tile_k.size() * sizeof(int),
+                     cudaMemcpyHostToDevice, h->stream), "tile_k copy");
+  CK(cudaStreamSynchronize(h->stream), "tile_k copy");
+  reset_graph(h);
+  return SED_OK;
+}
+
 int ready(sed_handle* h) {
   if (!h) return SED_E_ARG;
   if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
   if (!h->have_forcing) return h->fail(SED_E_STATE, "sed_set_forcing has not been called");
+  return SED_OK;
+}
+
+int ensure_pipeline(sed_handle* h) {
+  if (h->s_in) return SED_OK;
+  CK(cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking), "stream");
+  CK(cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking), "stream");
+  for (auto& st : h->s_cmp) CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
+  CK(cudaEventCreateWithFlags(&h->pe_start, cudaEventDisableTiming), "event");
+  CK(cudaEventCreateWithFlags(&h->pe_done, cudaEventDisableTiming), "event");
+  for (int c = 0; c < kMaxSeg; c++) {
+    CK(cudaEventCreateWithFlags(&h->pe_in[c], cudaEventDisableTiming), "event");
+    CK(cudaEventCreateWithFlags(&h->pe_cmp[c], cudaEventDisableTiming), "event");
+  }
+  return SED_OK;
+}
+
+// sed_ode_solver with the copies in flight: the columns are cut into
+// h->pipe chunks of whole segments.  Chunk c's host->device copy (one 2-D
+// copy of its column range in every [tracer][layer] row), its gather, step
+// and scatter (on one of two step streams, alternating), and its
+// device->host copy are ordered by events, so chunk c+1 arrives while c is
+// stepped and c-1 leaves.  Each chunk writes a disjoint column range of the
+// staging array and of conc, and its own slots.
+template <typename real>
+int ode_solver_pipelined(sed_handle* h, double* conc, double dt, int method) {
+  int rc = ensure_pipeline(h);
+  if (rc) return rc;
+  Params<real> p = make_params<real>(h->prm);
+  set_clock(p, dt, h->prm.dt_min);
+  const bool bc4 = h->prm.bcup_particulate == 4;
+  const int kind = method == SED_ADAPTIVE_EULER ? KIND_ADAPT : KIND_FIXED;
+  const size_t pitch = (size_t)h->ncol * sizeof(double);
+  const size_t rows = (size_t)NTR * h->kmax;
+  double* stage = h->d_stage.as<double>();
+  unsigned* q = h->d_queue.as<unsigned>();
+  CK(cudaMemsetAsync(q, 0, kQueues * sizeof(unsigned), h->stream), "queue reset");
+  CK(cudaEventRecord(h->pe_start, h->stream), "event");
+  CK(cudaStreamWaitEvent(h->s_in, h->pe_start, 0), "wait");
+  const int per = h->nseg / h->pipe;
+  for (int c = 0; c < h->pipe; c++) {
+    const int g0 = c * per, g1 = g0 + per;
+    const int col0 = h->seg_col[g0], col1 = h->seg_col[g1];
+    const size_t width = (size_t)(col1 - col0) * sizeof(double);
+    if (width)
+      CK(cudaMemcpy2DAsync(stage + col0, pitch, conc + col0, pitch, width, rows,
+                           cudaMemcpyHostToDevice, h->s_in), "conc chunk copy");
+    CK(cudaEventRecord(h->pe_in[c], h->s_in), "event");
+    cudaStream_t cs = h->s_cmp[c & 1];
+    CK(cudaStreamWaitEvent(cs, h->pe_in[c], 0), "wait");
+    for (int b = 0; b < 2; b++) {
+      const Bin& bin = h->bins[b];
+      const int sl0 = bin.segb[g0], sl1 = bin.segb[g1];
+      if (sl1 == sl0) continue;
+      CK(launch_gather_range<real>(stage, h->d_conc.as<real>(), h->d_slot_col.as<int>(), NTR,
+                                   h->kmax, h->ncol, h->nslot, sl0, sl1 - sl0, h->sms, cs),
+         "gather launch");
+      ColumnArgs<real> a = column_args<real>(h, bin, b, dt, method);
+      restrict_args(a, bin, sl0, sl1, q + 2 + 2 * c + b);
+      CK(launch_column<real>(a, p, bin.lpl, bc4, kind, bin.blocks(h->sms, a.ntiles),
+                             bin.threads, cs), "column kernel launch");
+      CK(launch_scatter_range<real>(h->d_conc.as<real>(), stage, h->d_slot_col.as<int>(),
+                                    h->d_kact.as<int>(), NTR, h->kmax, h->ncol, h->nslot,
+                                    sl0, sl1 - sl0, h->sms, cs), "scatter launch");
+      h->launches += 3;
+    }
+    CK(cudaEventRecord(h->pe_cmp[c], cs), "event");
+    CK(cudaStreamWaitEvent(h->s_out, h->pe_cmp[c], 0), "wait");
+    if (width)
+      CK(cudaMemcpy2DAsync(conc + col0, pitch, stage + col0, pitch, width, rows,
+                           cudaMemcpyDeviceToHost, h->s_out), "conc chunk copy back");
+  }
+  // s_out has waited for every chunk's step: the surface fluxes are final
+  CK(launch_scatter_flux<real>(h->d_sflux.as<real>(), h->d_fluxes.as<double>(),
+                               h->d_slot_col.as<int>(), h->d_kact.as<int>(), h->ncol,
+                               h->nslot, h->sms, h->s_out), "flux scatter launch");
+  h->launches++;
+  CK(cudaEventRecord(h->pe_done, h->s_out), "event");
+  CK(cudaStreamWaitEvent(h->stream, h->pe_done, 0), "wait");
+  return SED_OK;
+}
+
+// The drop-in step on host arrays (sed_ode_solver without the statistics).
+int ode_solver_impl(sed_handle* h, double* conc, const double* bdys, double* fluxes,
+                    double dt, int method) {
+  int rc;
+  if ((rc = upload_forcing(h, bdys, fluxes))) return rc;
+  const bool pipelined = h->pipe > 1 && !(method == SED_ADAPTIVE_EULER &&
+                                          h->prm.cut_scope == SED_CUT_GLOBAL);
+  if (pipelined) {
+    rc = h->fp64() ? ode_solver_pipelined<double>(h, conc, dt, method)
+                   : ode_solver_pipelined<float>(h, conc, dt, method);
+    if (rc) return rc;
+    h->have_state = true;
+  } else {
+    if ((rc = upload_state(h, conc))) return rc;
+    if ((rc = dispatch_step(h, dt, method))) return rc;
+    if ((rc = download_state(h, conc))) return rc;
+    rc = h->fp64() ? scatter_fluxes<double>(h) : scatter_fluxes<float>(h);
+    if (rc) return rc;
+  }
+  CK(cudaMemcpyAsync(fluxes, h->d_fluxes.p, (size_t)NTR * h->ncol * sizeof(double),
+                     cudaMemcpyDeviceToHost, h->stream), "fluxes copy back");
+  return SED_OK;
+}
+
+// ---------------------------------------------------------------------------
+// autotuner
+
+// device buffers a trial step changes, saved once and put back before every
+// trial and at the end
+struct Saved {
+  DevBuf* buf;
+  size_t bytes;
+};
+
+std::vector<Saved> trial_buffers(sed_handle* h) {
+  const size_t ns = h->nslot, rs = h->rsize();
+  std::vector<Saved> v = {{&h->d_conc, (size_t)NTR * h->kmax * ns * rs},
+                          {&h->d_sflux, (size_t)NDISS * ns * rs},
+                          {&h->d_nsub, ns * sizeof(int)},
+                          {&h->d_force, (size_t)NFORCE * ns * rs},
+                          {&h->d_fluxes, (size_t)NTR * h->ncol * sizeof(double)},
+                          {&h->d_bdys, (size_t)(NTR + 1) * h->ncol * sizeof(double)}};
+  if (h->prm.budgets) v.push_back({&h->d_budget, 4 * ns * sizeof(double)});
+  return v;
+}
+
+int save_state(sed_handle* h, bool restore) {
+  size_t off = 0, total = 0;
+  auto bufs = trial_buffers(h);
+  for (auto& b : bufs) total += (b.bytes + 255) & ~(size_t)255;
+  if (!restore) CK(h->d_backup.alloc(total), "autotune backup");
+  for (auto& b : bufs) {
+    char* bk = h->d_backup.as<char>() + off;
+    CK(cudaMemcpyAsync(restore ? b.buf->p : bk, restore ? bk : b.buf->p, b.bytes,
+                       cudaMemcpyDeviceToDevice, h->stream), "autotune backup copy");
+    off += (b.bytes + 255) & ~(size_t)255;
+  }
+  return SED_OK;
+}
+
+// time of one class's step kernel (b >= 0) or of a whole coupling step
+// (b < 0), from the saved state, best of `reps`
+template <typename real>
+int time_step(sed_handle* h, int b, double dt, int method, int reps, float* best) {
+  *best = 1e30f;
+  const int kind = method == SED_ADAPTIVE_EULER ? KIND_ADAPT : KIND_FIXED;
+  Params<real> p = make_params<real>(h->prm);
+  set_clock(p, dt, h->prm.dt_min);
+  for (int r = 0; r <= reps; r++) {  // r = 0 warms up
+    int rc = save_state(h, true);
+    if (rc) return rc;
+    CK(cudaEventRecord(h->ev0, h->stream), "event");
+    if (b >= 0) {
+      const Bin& bin = h->bins[b];
+      CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
+      ColumnArgs<real> a = column_args<real>(h, bin, b, dt, method);
+      CK(launch_column<real>(a, p, bin.lpl, h->prm.bcup_particulate == 4, kind,
+                             bin.blocks(h->sms, a.ntiles), bin.threads, h->stream),
+         "autotune launch");
+    } else {
+      rc = step_any<real>(h, dt, method);
+      if (rc) return rc;
+    }
+    CK(cudaEventRecord(h->ev1, h->stream), "event");
+    CK(cudaEventSynchronize(h->ev1), "autotune step");
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1), "event time");
+    if (r > 0) *best = std::min(*best, ms);
+  }
+  return SED_OK;
+}
+
+template <typename real>
+int autotune_t(sed_handle* h, double dt, int method, int flags, sed_tuning* out) {
+  int rc = save_state(h, false);
+  if (rc) return rc;
+  int trials = 0;
+  const int tcs[] = {8, 16, 32, 64};
+  const int thr[] = {64, 128, 256};
+  for (int b = 0; b < 2; b++) {
+    Bin& bin = h->bins[b];
+    if (bin.nslots == 0) continue;
+    int best_tc = bin.tc, best_thr = bin.threads;
+    float best_ms = 1e30f;
+    for (int tc : tcs)
+      for (int th : thr) {
+        const int occ = class_occupancy(h, bin, tc, th);
+        if (occ <= 0 || bin.nslots < tc) continue;
+        bin.tc = tc;
+        bin.threads = th;
+        bin.bps = 0;
+        if ((rc = apply_tuning(h))) return rc;
+        float ms;
+        if ((rc = time_step<real>(h, b, dt, method, 2, &ms))) return rc;
+        trials++;
+        if (ms < best_ms) { best_ms = ms; best_tc = tc; best_thr = th; }
+      }
+    bin.tc = best_tc;
+    bin.threads = best_thr;
+    if ((rc = apply_tuning(h))) return rc;
+  }
+  float step_ms;
+  if ((rc = time_step<real>(h, -1, dt, method, 2, &step_ms))) return rc;
+  if (flags & SED_TUNE_CAP) {
+    // attempts of the last timed step (the stats record of the trials)
+    DevStats z{};
+    z.min_dt_bits = 0x7FF0000000000000ull;
+    CK(cudaMemcpyAsync(h->d_stats.p, &z, sizeof z, cudaMemcpyHostToDevice, h->stream), "stats");
+    if ((rc = save_state(h, true))) return rc;
+    if ((rc = step_any<real>(h, dt, method))) return rc;
+    DevStats s;
+    CK(cudaMemcpyAsync(&s, h->d_stats.p, sizeof s, cudaMemcpyDeviceToHost, h->stream), "stats");
+    CK(cudaStreamSynchronize(h->stream), "autotune cap");
+    int cap = 64;
+    while (cap < 4 * s.max_col_attempts && cap < (1 << 30)) cap *= 2;
+    h->prm.max_attempts = cap;
+    reset_graph(h);
+  }
+  float ode_ms = 0.0f;
+  const size_t state_bytes = (size_t)NTR * h->kmax * h->ncol * sizeof(double);
+  if ((flags & SED_TUNE_PIPELINE) && state_bytes <= ((size_t)2 << 30)) {
+    // pinned host copies of the state and forcing the caller would pass
+    double *hc = nullptr, *hb = nullptr, *hf = nullptr;
+    const size_t nb = (size_t)(NTR + 1) * h->ncol * sizeof(double);
+    const size_t nf = (size_t)NTR * h->ncol * sizeof(double);
+    if (cudaHostAlloc((void**)&hc, state_bytes, cudaHostAllocDefault) != cudaSuccess ||
+        cudaHostAlloc((void**)&hb, nb, cudaHostAllocDefault) != cudaSuccess ||
+        cudaHostAlloc((void**)&hf, nf, cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      if (hc) cudaFreeHost(hc);
+      if (hb) cudaFreeHost(hb);
+      return h->fail(SED_E_NOMEM, "autotune: pinned host scratch of %zu bytes", state_bytes);
+    }
+    auto done = [&](int r) { cudaFreeHost(hc); cudaFreeHost(hb); cudaFreeHost(hf); return r; };
+    const int pipe0 = h->pipe;
+    int best_pipe = pipe0;
+    float best = 1e30f;
+    for (int pp = 1; pp <= h->nseg; pp *= 2) {
+      h->pipe = pp;
+      float t_best = 1e30f;
+      for (int r = 0; r <= 2; r++) {
+        if ((rc = save_state(h, true))) return done(rc);
+        if ((rc = download_state(h, hc))) return done(rc);
+        if (cudaMemcpyAsync(hb, h->d_bdys.p, nb, cudaMemcpyDeviceToHost, h->stream) ||
+            cudaMemcpyAsync(hf, h->d_fluxes.p, nf, cudaMemcpyDeviceToHost, h->stream) ||
+            cudaStreamSynchronize(h->stream))
+          return done(h->cuda_fail(cudaGetLastError(), "autotune scratch copy"));
+        if (cudaEventRecord(h->ev0, h->stream)) return done(h->cuda_fail(cudaGetLastError(), "event"));
+        if ((rc = ode_solver_impl(h, hc, hb, hf, dt, method))) return done(rc);
+        float ms = 0.0f;
+        if (cudaEventRecord(h->ev1, h->stream) || cudaEventSynchronize(h->ev1) ||
+            cudaEventElapsedTime(&ms, h->ev0, h->ev1))
+          return done(h->cuda_fail(cudaGetLastError(), "autotune pipeline"));
+        trials++;
+        if (r > 0) t_best = std::min(t_best, ms);
+      }
+      if (t_best < best) { best = t_best; best_pipe = pp; }
+    }
+    h->pipe = best_pipe;
+    ode_ms = best;
+    done(0);
+  }
+  if ((rc = save_state(h, true))) return rc;
+  CK(cudaStreamSynchronize(h->stream), "autotune restore");
+  reset_graph(h);
+  if (out) {
+    sed_get_tuning(h, out);
+    out->step_ms = step_ms;
+    out->ode_solver_ms = ode_ms;
+    out->trials = trials;
+  }
   return SED_OK;
 }
 
@@ -443,6 +789,13 @@ sed_handle::~sed_handle() {
   cudaSetDevice(device);
   if (stream) cudaStreamSynchronize(stream);
   reset_graph(this);
+  for (cudaStream_t st : {s_in, s_out, s_cmp[0], s_cmp[1]})
+    if (st) { cudaStreamSynchronize(st); cudaStreamDestroy(st); }
+  for (cudaEvent_t ev : {pe_start, pe_done}) if (ev) cudaEventDestroy(ev);
+  for (int c = 0; c < kMaxSeg; c++) {
+    if (pe_in[c]) cudaEventDestroy(pe_in[c]);
+    if (pe_cmp[c]) cudaEventDestroy(pe_cmp[c]);
+  }
   if (h_stats) cudaFreeHost(h_stats);
   if (h_flag) cudaFreeHost(h_flag);
   if (ev0) cudaEventDestroy(ev0);
@@ -523,7 +876,7 @@ int sed_create(const sed_params* p, int inum, int jnum, int kmax, int ntr,
     CK(cudaEventCreate(&h->ev1), "event");
     CK(cudaHostAlloc((void**)&h->h_stats, sizeof(DevStats), cudaHostAllocDefault), "pinned stats");
     CK(cudaHostAlloc((void**)&h->h_flag, sizeof(int), cudaHostAllocDefault), "pinned flag");
-    CK(h->d_queue.alloc(4 * sizeof(unsigned)), "queue");
+    CK(h->d_queue.alloc(kQueues * sizeof(unsigned)), "queue");
     CK(h->d_stats.alloc(sizeof(DevStats)), "stats");
     CK(h->d_flag.alloc(sizeof(int)), "flag");
     const size_t ncol = (size_t)h->ncol;
@@ -573,64 +926,61 @@ int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
       if (k > 0 && !(dzc[(size_t)(k - 1) * ncol + c] > 0.0))
         return h->fail(SED_E_ARG, "dzc <= 0 at column %d layer %d", c, k);
     }
-  // slots: active columns sorted by depth class then layers (stable)
-  std::vector<int> order;
-  order.reserve(ncol);
-  for (int c = 0; c < ncol; c++)
-    if (ka[c] > 0) order.push_back(c);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    const int ba = ka[a] > 32, bb = ka[b] > 32;
-    if (ba != bb) return ba < bb;
-    return ka[a] < ka[b];
-  });
-  h->nactive = (int)order.size();
-  int n1 = 0;
-  for (int c : order) n1 += ka[c] <= 32;
-  const int n2 = h->nactive - n1;
-  // tile width: 32 columns for the one-layer class, 16 when deep columns exist
-  h->tc = (kmax > 32) ? 16 : 32;
-  const int tc = h->tc;
-  const int nt1 = (n1 + tc - 1) / tc, nt2 = (n2 + tc - 1) / tc;
-  h->ntiles = nt1 + nt2;
-  h->nslot = std::max(1, h->ntiles) * tc;
-  h->slot_col.assign(h->nslot, -1);
-  h->slot_k.assign(h->nslot, 0);
-  for (int i = 0; i < n1; i++) { h->slot_col[i] = order[i]; h->slot_k[i] = ka[order[i]]; }
-  for (int i = 0; i < n2; i++) {
-    h->slot_col[nt1 * tc + i] = order[n1 + i];
-    h->slot_k[nt1 * tc + i] = ka[order[n1 + i]];
+  // column segments: power-of-two count, contiguous ranges with equal
+  // active-layer sums, bounds on multiples of 32 columns
+  h->nactive = 0;
+  long long work = 0;
+  for (int c = 0; c < ncol; c++) {
+    h->nactive += ka[c] > 0;
+    work += ka[c];
   }
-  std::vector<int> tile_k(std::max(1, h->ntiles), 1);
-  for (int t = 0; t < h->ntiles; t++) {
-    int m = 1;
-    for (int j = 0; j < tc; j++) m = std::max(m, h->slot_k[t * tc + j]);
-    tile_k[t] = m;
-  }
-  h->nbins = 0;
-  const bool bc4 = h->prm.bcup_particulate == 4;
-  const int kind = KIND_ADAPT;
-  for (int b = 0; b < 2; b++) {
-    Bin& bin = h->bins[h->nbins];
-    bin.lpl = b == 0 ? 1 : 2;
-    bin.tile0 = b == 0 ? 0 : nt1;
-    bin.ntiles = b == 0 ? nt1 : nt2;
-    if (bin.ntiles == 0) continue;
-    int occ = 1 << 30;
-    for (int kd = 0; kd < 3; kd++) {
-      // also sets every variant's shared-memory limit before any capture
-      const int o = h->fp64() ? column_blocks_per_sm<double>(tc, bin.lpl, bc4, kd, h->threads)
-                              : column_blocks_per_sm<float>(tc, bin.lpl, bc4, kd, h->threads);
-      if (kd == kind) occ = o;
-      if (o <= 0) return h->fail(SED_E_CUDA, "column kernel does not fit on the device");
+  h->nseg = 1;
+  while (h->nseg < kMaxSeg && h->nactive / (2 * h->nseg) >= 4096) h->nseg *= 2;
+  h->seg_col.assign(h->nseg + 1, ncol);
+  h->seg_col[0] = 0;
+  {
+    long long acc = 0;
+    int s = 1;
+    for (int c = 0; c < ncol && s < h->nseg; c++) {
+      acc += ka[c];
+      if (acc * h->nseg >= work * s && (c + 1) % 32 == 0) h->seg_col[s++] = c + 1;
     }
-    bin.blocks = std::min(bin.ntiles, occ * h->sms);
-    h->nbins++;
   }
+  // slots: depth class (<= 32 layers, 33..64), then segment, then active
+  // layers (stable); every (class, segment) run is padded to kSlotPad slots
+  h->slot_col.clear();
+  h->slot_k.clear();
+  for (int b = 0; b < 2; b++) {
+    Bin& bin = h->bins[b];
+    bin.lpl = b + 1;
+    bin.slot0 = (int)h->slot_col.size();
+    for (int sg = 0; sg < h->nseg; sg++) {
+      bin.segb[sg] = (int)h->slot_col.size();
+      std::vector<int> cols;
+      for (int c = h->seg_col[sg]; c < h->seg_col[sg + 1]; c++)
+        if (ka[c] > 0 && (ka[c] > 32) == (b == 1)) cols.push_back(c);
+      std::stable_sort(cols.begin(), cols.end(), [&](int x, int y) { return ka[x] < ka[y]; });
+      for (int c : cols) { h->slot_col.push_back(c); h->slot_k.push_back(ka[c]); }
+      while (h->slot_col.size() % kSlotPad) { h->slot_col.push_back(-1); h->slot_k.push_back(0); }
+    }
+    bin.segb[h->nseg] = (int)h->slot_col.size();
+    for (int sg = h->nseg + 1; sg <= kMaxSeg; sg++) bin.segb[sg] = bin.segb[h->nseg];
+    bin.nslots = (int)h->slot_col.size() - bin.slot0;
+    bin.tc = b == 0 ? 32 : 16;
+    bin.threads = 256;
+    bin.bps = 0;
+  }
+  if (h->slot_col.empty()) {
+    h->slot_col.assign(kSlotPad, -1);
+    h->slot_k.assign(kSlotPad, 0);
+  }
+  h->nslot = (int)h->slot_col.size();
+  h->pipe = std::min(4, h->nseg);
+  const bool bc4 = h->prm.bcup_particulate == 4;
   // device buffers
   const size_t ns = (size_t)h->nslot, rs = h->rsize();
   CK(h->d_slot_col.alloc(ns * sizeof(int)), "slot map");
   CK(h->d_kact.alloc(ns * sizeof(int)), "kact");
-  CK(h->d_tile_k.alloc(tile_k.size() * sizeof(int)), "tile_k");
   CK(h->d_conc.alloc((size_t)NTR * kmax * ns * rs), "state");
   const int ncoef = h->fp64() ? NCOEF64 : NCOEF;
   CK(h->d_coef.alloc((size_t)ncoef * kmax * ns * rs), "coefficients");
@@ -648,8 +998,11 @@ int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
                      cudaMemcpyHostToDevice, h->stream), "slot map copy");
   CK(cudaMemcpyAsync(h->d_kact.p, h->slot_k.data(), ns * sizeof(int),
                      cudaMemcpyHostToDevice, h->stream), "kact copy");
-  CK(cudaMemcpyAsync(h->d_tile_k.p, tile_k.data(), tile_k.size() * sizeof(int),
-                     cudaMemcpyHostToDevice, h->stream), "tile_k copy");
+  CK(h->d_tile_k.alloc((size_t)(h->nslot / 8 + 1) * sizeof(int)), "tile_k");
+  {
+    int rc = apply_tuning(h);
+    if (rc) return rc;
+  }
   // grid arrays through a temporary FP64 staging area
   const size_t lay = (size_t)kmax * ncol;
   CK(h->d_grid.alloc(7 * lay * sizeof(double)), "grid staging");
@@ -768,14 +1121,7 @@ int sed_ode_solver(sed_handle* h, double* conc, const double* bdys, double* flux
   const long long l0 = h->launches;
   if ((rc = stats_reset(h))) return rc;
   CK(cudaEventRecord(h->ev0, h->stream), "event");
-  if ((rc = upload_state(h, conc))) return rc;
-  if ((rc = upload_forcing(h, bdys, fluxes))) return rc;
-  if ((rc = dispatch_step(h, dt, method))) return rc;
-  if ((rc = download_state(h, conc))) return rc;
-  rc = h->fp64() ? scatter_fluxes<double>(h) : scatter_fluxes<float>(h);
-  if (rc) return rc;
-  CK(cudaMemcpyAsync(fluxes, h->d_fluxes.p, (size_t)NTR * h->ncol * sizeof(double),
-                     cudaMemcpyDeviceToHost, h->stream), "fluxes copy back");
+  if ((rc = ode_solver_impl(h, conc, bdys, fluxes, dt, method))) return rc;
   CK(cudaEventRecord(h->ev1, h->stream), "event");
   return stats_fetch(h, stats, l0, true);
 }
@@ -842,18 +1188,29 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
     // residual test of every column, then the plain solver on the rejected
     for (int kind : {KIND_RESID, KIND_ADAPT}) {
       CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
-      for (int b = 0; b < h->nbins; b++) {
+      for (int b = 0; b < 2; b++) {
         const Bin& bin = h->bins[b];
-        if (bin.ntiles == 0) continue;
+        if (bin.nslots == 0) continue;
         ColumnArgs<float> a = column_args<float>(h, bin, b, dt, SED_ADAPTIVE_EULER);
         a.out = h->d_prop.as<float>();
         a.skip = h->d_skip.as<int>();
         a.res_tol = tol;
         a.res_atol = res_atol;
-        const int occ = column_blocks_per_sm<float>(h->tc, bin.lpl, bc4, kind, h->threads);
-        if (occ <= 0) return h->fail(SED_E_CUDA, "residual kernel does not fit");
-        CK(launch_column<float>(a, p, bin.lpl, bc4, kind,
-                                std::min(bin.ntiles, occ * h->sms), h->threads, h->stream),
+        int blocks = bin.blocks(h->sms, a.ntiles);
+        if (kind == KIND_RESID) {
+          // two states per tile: the widest tile up to the class's that fits,
+          // staging every layer of the class
+          int tc = bin.tc, occ = 0;
+          for (; tc >= 8; tc /= 2)
+            if ((occ = column_blocks_per_sm<float>(tc, bin.lpl, bc4, kind, bin.threads)) > 0) break;
+          if (occ <= 0) return h->fail(SED_E_CUDA, "residual kernel does not fit");
+          a.tc = tc;
+          a.tile_k = nullptr;
+          a.tile0 = 0;
+          a.ntiles = bin.nslots / tc;
+          blocks = std::max(1, std::min(a.ntiles, occ * h->sms));
+        }
+        CK(launch_column<float>(a, p, bin.lpl, bc4, kind, blocks, bin.threads, h->stream),
            "surrogate step launch");
         h->launches++;
       }
@@ -945,6 +1302,68 @@ int sed_set_stream(sed_handle* h, void* stream) {
   h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
   reset_graph(h);
   return SED_OK;
+}
+
+int sed_get_tuning(const sed_handle* h, sed_tuning* t) {
+  if (!h || !t) return SED_E_ARG;
+  memset(t, 0, sizeof *t);
+  for (int b = 0; b < 2; b++) {
+    t->tile_columns[b] = h->bins[b].tc;
+    t->threads[b] = h->bins[b].threads;
+    t->blocks_per_sm[b] = h->bins[b].bps;
+  }
+  t->pipeline_chunks = h->pipe;
+  t->segments = h->nseg;
+  t->max_attempts = h->prm.max_attempts;
+  return SED_OK;
+}
+
+int sed_set_tuning(sed_handle* h, const sed_tuning* t) {
+  if (!h || !t) return SED_E_ARG;
+  if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
+  for (int b = 0; b < 2; b++) {
+    const int tc = t->tile_columns[b], th = t->threads[b];
+    if (tc != 8 && tc != 16 && tc != 32 && tc != 64)
+      return h->fail(SED_E_ARG, "tile_columns[%d]=%d: 8, 16, 32 or 64", b, tc);
+    if (th < 64 || th > 256 || th % 64 != 0)
+      return h->fail(SED_E_ARG, "threads[%d]=%d: 64, 128, 192 or 256", b, th);
+    if (t->blocks_per_sm[b] < 0) return h->fail(SED_E_ARG, "blocks_per_sm[%d] < 0", b);
+  }
+  const int pc = t->pipeline_chunks;
+  if (pc < 1 || pc > h->nseg || (h->nseg % pc) != 0 || (pc & (pc - 1)) != 0)
+    return h->fail(SED_E_ARG, "pipeline_chunks=%d must be a power of two dividing %d", pc,
+                   h->nseg);
+  if (t->max_attempts <= 0) return h->fail(SED_E_ARG, "max_attempts must be > 0");
+  CK(cudaSetDevice(h->device), "set device");
+  Bin keep[2] = {h->bins[0], h->bins[1]};
+  for (int b = 0; b < 2; b++) {
+    h->bins[b].tc = t->tile_columns[b];
+    h->bins[b].threads = t->threads[b];
+    h->bins[b].bps = t->blocks_per_sm[b];
+  }
+  int rc = apply_tuning(h);
+  if (rc) {
+    const std::string why = h->err;
+    h->bins[0] = keep[0];
+    h->bins[1] = keep[1];
+    apply_tuning(h);
+    h->err = why;
+    return rc;
+  }
+  h->pipe = pc;
+  h->prm.max_attempts = t->max_attempts;
+  return SED_OK;
+}
+
+int sed_autotune(sed_handle* h, double dt, int method, int flags, sed_tuning* out) {
+  int rc = ready(h);
+  if (rc) return rc;
+  if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");
+  if (method < 0 || method > 3 || !(dt > 0.0) || (flags & ~3))
+    return h->fail(SED_E_ARG, "bad dt, method or flags");
+  CK(cudaSetDevice(h->device), "set device");
+  return h->fp64() ? autotune_t<double>(h, dt, method, flags, out)
+                   : autotune_t<float>(h, dt, method, flags, out);
 }
 
 int sed_host_register(void* ptr, size_t bytes) {

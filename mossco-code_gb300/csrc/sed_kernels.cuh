@@ -572,9 +572,8 @@ k_column(ColumnArgs<real> a, Params<real> p) {
     __syncthreads();
     const int tile = s_tile;
     if (tile >= a.ntiles) break;
-    const int t = a.tile0 + tile;
-    const int slot0 = t * tc;
-    const int kt = a.tile_k[t];
+    const int slot0 = a.slot0 + tile * tc;
+    const int kt = a.tile_k ? a.tile_k[a.tile0 + tile] : (a.kmax < KT ? a.kmax : KT);
     // stage in (KIND_RESID: the proposed state, and the start state)
     copy_grouped<real, true>(s_conc, (KIND == KIND_RESID ? a.out : a.conc) + slot0, NTR,
                              kt, KT, a.kmax, ns, tc, tcp, tid, nthr);
@@ -808,14 +807,14 @@ __global__ void k_epilogue(real* __restrict__ conc, const int* __restrict__ kact
 template <typename real>
 __global__ void k_gather(const double* __restrict__ src, real* __restrict__ dst,
                          const int* __restrict__ slot_col, int ngroups, int kmax,
-                         int ncol, int nslot) {
-  const size_t total = (size_t)ngroups * kmax * nslot;
+                         int ncol, int nslot, int slot0, int nseg) {
+  const size_t total = (size_t)ngroups * kmax * nseg;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
-    const int slot = (int)(i % nslot);
-    const size_t gk = i / nslot;
+    const int slot = slot0 + (int)(i % nseg);
+    const size_t gk = i / nseg;
     const int col = slot_col[slot];
-    dst[i] = col >= 0 ? (real)src[gk * ncol + col] : real(0);
+    dst[gk * nslot + slot] = col >= 0 ? (real)src[gk * ncol + col] : real(0);
   }
 }
 
@@ -823,15 +822,15 @@ template <typename real>
 __global__ void k_scatter(const real* __restrict__ src, double* __restrict__ dst,
                           const int* __restrict__ slot_col,
                           const int* __restrict__ kact, int ngroups, int kmax,
-                          int ncol, int nslot) {
-  const size_t total = (size_t)ngroups * kmax * nslot;
+                          int ncol, int nslot, int slot0, int nseg) {
+  const size_t total = (size_t)ngroups * kmax * nseg;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
-    const int slot = (int)(i % nslot);
-    const size_t gk = i / nslot;
+    const int slot = slot0 + (int)(i % nseg);
+    const size_t gk = i / nseg;
     const int k = (int)(gk % kmax);
     const int col = slot_col[slot];
-    if (col >= 0 && k < kact[slot]) dst[gk * ncol + col] = (double)src[i];
+    if (col >= 0 && k < kact[slot]) dst[gk * ncol + col] = (double)src[gk * nslot + slot];
   }
 }
 
@@ -1003,7 +1002,19 @@ template <typename real, int LPL, bool BC4, int KIND>
 static int occupancy_t(int tc, int threads) {
   const size_t smem = tile_smem_bytes<real>(tc, LPL, BC4, KIND);
   auto fn = k_column<real, LPL, BC4, KIND>;
-  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // the limit is raised to the device maximum (never lowered), so handles
+  // with different tile widths can share the kernel
+  // (the opt-in maximum less the kernel's static shared variables)
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) return 0;
+  const int dyn_max = optin - (int)fa.sharedSizeBytes;
+  if (dyn_max < (int)smem) return 0;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_max) !=
+      cudaSuccess)
+    return 0;
   cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
                        cudaSharedmemCarveoutMaxShared);
   int nb = 0;
@@ -1059,12 +1070,33 @@ cudaError_t launch_epilogue(real* conc, const int* kact, int nslot, int kmax,
 }
 
 template <typename real>
+cudaError_t launch_gather_range(const double* src, real* dst, const int* slot_col,
+                                int ngroups, int kmax, int ncol, int nslot, int slot0,
+                                int nseg, int sms, cudaStream_t st) {
+  if (nseg <= 0) return cudaSuccess;
+  const size_t total = (size_t)ngroups * kmax * nseg;
+  k_gather<real><<<grid_for(total, 256, sms), 256, 0, st>>>(src, dst, slot_col, ngroups,
+                                                           kmax, ncol, nslot, slot0, nseg);
+  return cudaGetLastError();
+}
+
+template <typename real>
 cudaError_t launch_gather(const double* src, real* dst, const int* slot_col,
                           int ngroups, int kmax, int ncol, int nslot, int sms,
                           cudaStream_t st) {
-  const size_t total = (size_t)ngroups * kmax * nslot;
-  k_gather<real><<<grid_for(total, 256, sms), 256, 0, st>>>(src, dst, slot_col,
-                                                           ngroups, kmax, ncol, nslot);
+  return launch_gather_range<real>(src, dst, slot_col, ngroups, kmax, ncol, nslot, 0,
+                                   nslot, sms, st);
+}
+
+template <typename real>
+cudaError_t launch_scatter_range(const real* src, double* dst, const int* slot_col,
+                                 const int* kact, int ngroups, int kmax, int ncol,
+                                 int nslot, int slot0, int nseg, int sms,
+                                 cudaStream_t st) {
+  if (nseg <= 0) return cudaSuccess;
+  const size_t total = (size_t)ngroups * kmax * nseg;
+  k_scatter<real><<<grid_for(total, 256, sms), 256, 0, st>>>(
+      src, dst, slot_col, kact, ngroups, kmax, ncol, nslot, slot0, nseg);
   return cudaGetLastError();
 }
 
@@ -1072,10 +1104,8 @@ template <typename real>
 cudaError_t launch_scatter(const real* src, double* dst, const int* slot_col,
                            const int* kact, int ngroups, int kmax, int ncol,
                            int nslot, int sms, cudaStream_t st) {
-  const size_t total = (size_t)ngroups * kmax * nslot;
-  k_scatter<real><<<grid_for(total, 256, sms), 256, 0, st>>>(
-      src, dst, slot_col, kact, ngroups, kmax, ncol, nslot);
-  return cudaGetLastError();
+  return launch_scatter_range<real>(src, dst, slot_col, kact, ngroups, kmax, ncol, nslot,
+                                    0, nslot, sms, st);
 }
 
 template <typename real>
@@ -1132,6 +1162,13 @@ cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
   template cudaError_t launch_scatter<real>(const real*, double*, const int*,   \
                                             const int*, int, int, int, int,     \
                                             int, cudaStream_t);                 \
+  template cudaError_t launch_gather_range<real>(const double*, real*,          \
+                                                 const int*, int, int, int, int, \
+                                                 int, int, int, cudaStream_t);  \
+  template cudaError_t launch_scatter_range<real>(const real*, double*,         \
+                                                  const int*, const int*, int,  \
+                                                  int, int, int, int, int, int, \
+                                                  cudaStream_t);                \
   template cudaError_t launch_scatter_flux<real>(const real*, double*,          \
                                                  const int*, const int*, int,   \
                                                  int, int, cudaStream_t);       \

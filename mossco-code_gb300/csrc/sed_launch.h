@@ -22,13 +22,15 @@ struct ColumnArgs {
   const real* cap;
   const real* force;
   const int* kact;    // [nslot]
-  const int* tile_k;  // [ntiles_total] layers to stage per tile
+  const int* tile_k;  // layers to stage per tile, tile_k[tile0 + tile]; null:
+                      // stage min(kmax, 32 x layers per lane) layers
   real* sflux;
   double* budget;     // may be null
   int* nsub;          // [nslot] attempts of the last step
   unsigned* queue;    // tile counter, zero before the launch
   DevStats* stats;
-  int nslot, kmax, tc, tile0, ntiles;
+  // the launch covers slots [slot0, slot0 + ntiles * tc); tile0 indexes tile_k
+  int nslot, kmax, tc, slot0, tile0, ntiles;
   double dt;
   int method;
   // surrogate coupling step: per-slot flags (1 = the surrogate's state was
@@ -69,10 +71,22 @@ cudaError_t launch_gather(const double* src, real* dst, const int* slot_col,
                           int ngroups, int kmax, int ncol, int nslot, int sms,
                           cudaStream_t st);
 
+// the same restricted to slots [slot0, slot0 + nseg) of [ngroups][kmax][nslot]
+template <typename real>
+cudaError_t launch_gather_range(const double* src, real* dst, const int* slot_col,
+                                int ngroups, int kmax, int ncol, int nslot, int slot0,
+                                int nseg, int sms, cudaStream_t st);
+
 template <typename real>
 cudaError_t launch_scatter(const real* src, double* dst, const int* slot_col,
                            const int* kact, int ngroups, int kmax, int ncol,
                            int nslot, int sms, cudaStream_t st);
+
+template <typename real>
+cudaError_t launch_scatter_range(const real* src, double* dst, const int* slot_col,
+                                 const int* kact, int ngroups, int kmax, int ncol,
+                                 int nslot, int slot0, int nseg, int sms,
+                                 cudaStream_t st);
 
 template <typename real>
 cudaError_t launch_scatter_flux(const real* sflux, double* fluxes,

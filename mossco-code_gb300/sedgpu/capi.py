@@ -67,6 +67,28 @@ class SedStats(ctypes.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class SedTuning(ctypes.Structure):
+    _fields_ = [("tile_columns", ctypes.c_int * 2),
+                ("threads", ctypes.c_int * 2),
+                ("blocks_per_sm", ctypes.c_int * 2),
+                ("pipeline_chunks", ctypes.c_int),
+                ("segments", ctypes.c_int),
+                ("max_attempts", ctypes.c_int),
+                ("step_ms", ctypes.c_float),
+                ("ode_solver_ms", ctypes.c_float),
+                ("trials", ctypes.c_int)]
+
+    def as_dict(self):
+        d = {}
+        for n, _ in self._fields_:
+            v = getattr(self, n)
+            d[n] = list(v) if isinstance(v, ctypes.Array) else v
+        return d
+
+
+SED_TUNE_PIPELINE = 1
+SED_TUNE_CAP = 2
+
 _dp = ctypes.POINTER(ctypes.c_double)
 _fp = ctypes.POINTER(ctypes.c_float)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -96,6 +118,10 @@ SIGNATURES = {
     "sed_set_stream": (ctypes.c_int, [_H, _vp]),
     "sed_host_register": (ctypes.c_int, [_vp, ctypes.c_size_t]),
     "sed_host_unregister": (ctypes.c_int, [_vp]),
+    "sed_get_tuning": (ctypes.c_int, [_H, ctypes.POINTER(SedTuning)]),
+    "sed_set_tuning": (ctypes.c_int, [_H, ctypes.POINTER(SedTuning)]),
+    "sed_autotune": (ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                    ctypes.POINTER(SedTuning)]),
     "sed_ode_solver_noalloc": (ctypes.c_int, [
         ctypes.POINTER(SedParams), ctypes.c_int, ctypes.c_int, ctypes.c_int,
         _dp, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp, ctypes.c_double,
@@ -304,6 +330,31 @@ class Solver:
         """Use a caller's CUDA stream (e.g. torch.cuda.Stream().cuda_stream)."""
         self._check(self.lib.sed_set_stream(self.h, ctypes.c_void_p(stream_handle)),
                     "sed_set_stream")
+
+    # -- launch tuning ----------------------------------------------------
+    def tuning(self) -> SedTuning:
+        t = SedTuning()
+        self._check(self.lib.sed_get_tuning(self.h, ctypes.byref(t)), "sed_get_tuning")
+        return t
+
+    def set_tuning(self, t: SedTuning = None, **fields) -> None:
+        """Apply a tuning; keyword fields (tile_columns=(32, 16), ...) edit
+        the current one."""
+        t = t if t is not None else self.tuning()
+        for k, v in fields.items():
+            if isinstance(getattr(t, k), ctypes.Array):
+                getattr(t, k)[:] = list(v)
+            else:
+                setattr(t, k, v)
+        self._check(self.lib.sed_set_tuning(self.h, ctypes.byref(t)), "sed_set_tuning")
+
+    def autotune(self, dt: Optional[float] = None, method: int = 2,
+                 flags: int = 0) -> dict:
+        t = SedTuning()
+        dt = self.cs.dt if dt is None else dt
+        self._check(self.lib.sed_autotune(self.h, float(dt), int(method), int(flags),
+                                          ctypes.byref(t)), "sed_autotune")
+        return t.as_dict()
 
     def fluxes(self) -> np.ndarray:
         out = np.array(self.cs.fluxes, dtype=np.float64, copy=True)
