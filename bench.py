@@ -278,7 +278,10 @@ def run_gpu(args) -> None:
     # launch tuning chosen by the library's autotuner on the warmed-up state
     # (untimed; it restores the state it found), then the warm-up steps
     tuning = None
-    if not args.no_autotune:
+    if args.tuning:
+        tc0, tc1, th0, th1 = (int(v) for v in args.tuning.split(","))
+        s.set_tuning(tile_columns=(tc0, tc1), threads=(th0, th1))
+    elif not args.no_autotune:
         s.step(1)
         tuning = s.autotune(flags=0 if args.no_e2e else capi.SED_TUNE_PIPELINE)
     for _ in range(args.warmup):
@@ -380,7 +383,8 @@ def run_gpu(args) -> None:
     t_now = s.tuning().as_dict()
     s_tuning = {k: t_now[k] for k in ("tile_columns", "threads", "pipeline_chunks",
                                        "segments")}
-    s_tuning["chosen_by"] = "sed_autotune" if tuning else "defaults"
+    s_tuning["chosen_by"] = ("--tuning" if args.tuning else
+                             "sed_autotune" if tuning else "defaults")
     if tuning:
         s_tuning["autotune_trials"] = tuning["trials"]
     s.close()
@@ -465,6 +469,9 @@ def main():
     ap.add_argument("--sur-train-steps", type=int, default=5000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tuning", default="",
+                    help="tile columns and threads per depth class, 'tc0,tc1,th0,th1' "
+                         "(replaces the autotuner)")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":

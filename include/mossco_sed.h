@@ -90,6 +90,14 @@ typedef struct sed_params {
   int precision;              /* SED_FP32 (default) or SED_FP64 */
   int budgets;                /* 1: FP64 P and N budgets per column-step */
   int device;                 /* CUDA ordinal */
+  /* bioturbation_profile (fabm_sediment_driver.F90:73,204): 3 recomputes the
+   * bioturbation factor from the TOC profile at every right-hand side
+   * (Zhang & Wirtz 2017, get_rhs :618-645; biofac of sed_set_grid and the
+   * temperature factor are then unused); any other value uses biofac.  The
+   * constants are sed_nml's bioturb_* (:226-231). */
+  int bioturbation_profile;
+  double bioturb_k_l, bioturb_L1, bioturb_L2, bioturb_beta, bioturb_b,
+      bioturb_dry_density;
 } sed_params;
 
 typedef struct sed_stats {

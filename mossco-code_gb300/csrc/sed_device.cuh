@@ -38,8 +38,15 @@ enum : int {
 // Coefficient rows staged per layer: the FP32 kernels use folded
 // conductances, the FP64 kernels the reference's own per-cell arrays so
 // that they evaluate get_rhs in its exact operation order.
-template <typename real> struct CoefRows { static constexpr int value = NCOEF; };
-template <> struct CoefRows<double> { static constexpr int value = NCOEF64; };
+// Bioturbation profile 3 adds rows: FP32 the depth term and the averaging
+// weight (the bioturbation row then holds the conductance per unit factor);
+// FP64 exp(zc 100 k_l), exp(zc 200 k_l) and the column's cumdepth.
+constexpr int NCOEF_BIO3 = NCOEF + 2;
+constexpr int NCOEF64_BIO3 = NCOEF64 + 3;
+template <typename real>
+__host__ __device__ constexpr int coef_rows(bool bio3) {
+  return sizeof(real) == 8 ? (bio3 ? NCOEF64_BIO3 : NCOEF64) : (bio3 ? NCOEF_BIO3 : NCOEF);
+}
 
 // Reaction and solver constants in kernel units (rates per second).
 template <typename real>
@@ -58,6 +65,10 @@ struct Params {
   int max_attempts;
   int epilogue;
   int budgets;
+  // bioturbation profile 3 (get_rhs :618-645): POC-class factors to mg C per
+  // g dry mass (initialize :383,386), beta and the exponent b
+  int bio3;
+  real toc_f1, toc_f2, bio_beta, bio_b, bio_L1, bio_L2;
 };
 
 struct DevStats {
@@ -173,7 +184,45 @@ struct Lane {
   real dz[LPL], len[LPL], Dp[LPL], Dd[LPL];
   real ext_a[BC4 ? LPL : 1][BC4 ? NPART : 1];  // cascade additions in the loop
   real ext_b[BC4 ? LPL : 1][BC4 ? NPART : 1];  // and the final one (:800-802)
+  // bioturbation profile 3.  FP32: TOC weight phi/(1-phi), averaging weight
+  // dz/cumdepth, depth term exp(a z)/(L1 + L2 exp(2 a z)), the bioturbation
+  // conductance per unit factor and the molecular conductance.  FP64: the
+  // reference's exp(zc 100 k_l), exp(zc 200 k_l), cumdepth, the prefix
+  // bioturbation f_T / 86400 / 1e4 (1 - phi_i) and the molecular part.
+  real wc[LPL], hw[LPL], gz[LPL], gb3[LPL], dm[LPL];
+  real e1[LPL], e2[LPL], pre[LPL], mol[LPL];
+  real cum;
 };
+
+// Profile-3 conductances of one right-hand side, FP32 (get_rhs :624-644):
+// weighted TOC per layer, its dz-weighted column mean (a warp sum), infauna
+// biomass and the factor beta biomass^b / TOC, folded into the particulate
+// (ap) and dissolved (ad) interface conductances.  Lanes past the column
+// get zero conductances.
+template <typename real, int LPL, bool BC4>
+__device__ __forceinline__ void bio3_conductances(const Params<real>& p,
+                                                  const Lane<real, LPL, BC4>& lc,
+                                                  int lane, int K,
+                                                  const real (&C)[LPL][NTR],
+                                                  real (&ap)[LPL], real (&ad)[LPL]) {
+  real wt[LPL];
+  real part = real(0);
+#pragma unroll
+  for (int s = 0; s < LPL; s++) {
+    wt[s] = lc.wc[s] * (p.toc_f1 * C[s][T_FDETC] + p.toc_f2 * C[s][T_SDETC]);
+    part += lc.hw[s] * wt[s];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
+#pragma unroll
+  for (int s = 0; s < LPL; s++) {
+    const real biomass = wt[s] * lc.gz[s] * part;
+    const real fac = sdiv(p.bio_beta * __powf(biomass, p.bio_b), wt[s]);
+    const bool act = s * 32 + lane < K;
+    ap[s] = act ? lc.gb3[s] * fac : real(0);
+    ad[s] = act ? ap[s] + lc.dm[s] : real(0);
+  }
+}
 
 // Right-hand side of one column: OMEXDIA+P rates plus diff3d transport.
 // ftop receives the flux through the sediment surface (lane 0 only).
@@ -181,7 +230,7 @@ struct Lane {
 // conductances, so their rates and fluxes vanish by construction; the
 // surface boundary enters by selects on lane 0, the no-flux bottom by
 // dropping the flux from below at layer K-1.
-template <typename real, int LPL, bool BC4>
+template <typename real, int LPL, bool BC4, bool BIO3>
 __device__ __forceinline__ void column_rhs(const Params<real>& p,
                                            const Lane<real, LPL, BC4>& lc,
                                            int lane, int K,
@@ -189,6 +238,13 @@ __device__ __forceinline__ void column_rhs(const Params<real>& p,
                                            real (&R)[LPL][NTR],
                                            real (&ftop)[NTR],
                                            real (&dn)[LPL]) {
+  real apv[LPL], adv[LPL];
+  if constexpr (BIO3) {
+    bio3_conductances<real, LPL, BC4>(p, lc, lane, K, C, apv, adv);
+  } else {
+#pragma unroll
+    for (int s = 0; s < LPL; s++) { apv[s] = lc.ap[s]; adv[s] = lc.ad[s]; }
+  }
 #pragma unroll
   for (int s = 0; s < LPL; s++) omexdia_p<real>(p, C[s], R[s], dn[s]);
   const bool top = lane == 0;
@@ -207,13 +263,13 @@ __device__ __forceinline__ void column_rhs(const Params<real>& p,
     const real b = lc.bnd(n);
     if (part) {
 #pragma unroll
-      for (int s = 0; s < LPL; s++) F[s] = lc.ap[s] * (vm[s] - v[s]);
+      for (int s = 0; s < LPL; s++) F[s] = apv[s] * (vm[s] - v[s]);
       F[0] = top ? b : F[0];  // downward flux through the surface (BcUp 1)
     } else {
       // Dirichlet (BcUp 2): the surface interface sees the bottom water
       vm[0] = (top && dirichlet) ? b : vm[0];
 #pragma unroll
-      for (int s = 0; s < LPL; s++) F[s] = lc.ad[s] * (vm[s] - v[s]);
+      for (int s = 0; s < LPL; s++) F[s] = adv[s] * (vm[s] - v[s]);
       F[0] = (top && !dirichlet) ? (fluxbc ? b : real(0)) : F[0];
     }
     ftop[n] = F[0];
@@ -345,7 +401,49 @@ __device__ __forceinline__ void omexdia_p_ref(const Params<double>& p,
   denit = Denit;
 }
 
+// Profile-3 diffusivities of one right-hand side in the reference's
+// operation order (get_rhs :624-644, :652-653, :682-683): the column sum of
+// dz * TOC runs layer by layer as the Fortran sum does.  pow is CUDA's, so
+// the result can differ from the CPU restatement in the last bit.
 template <int LPL, bool BC4>
+__device__ __forceinline__ void bio3_diffusivities(const Params<double>& p,
+                                                   const Lane<double, LPL, BC4>& lc,
+                                                   int lane, int K,
+                                                   const double (&C)[LPL][NTR],
+                                                   double (&Dp)[LPL], double (&Dd)[LPL]) {
+  double wt[LPL], v[LPL];
+#pragma unroll
+  for (int s = 0; s < LPL; s++) {
+    const bool act = s * 32 + lane < K;
+    double w = 0.0;
+    w = w + p.toc_f1 * lc.phi[s] / (1.0 - lc.phi[s]) * C[s][T_FDETC];
+    w = w + p.toc_f2 * lc.phi[s] / (1.0 - lc.phi[s]) * C[s][T_SDETC];
+    wt[s] = act ? w : 1.0;
+    v[s] = act ? lc.dz[s] * w : 0.0;
+  }
+  double sum = 0.0;
+  for (int L = 0; L < K; L++) {
+    double t = 0.0;
+#pragma unroll
+    for (int s = 0; s < LPL; s++) {
+      const double u = __shfl_sync(FULL, v[s], L & 31);
+      if (s == (L >> 5)) t = u;
+    }
+    sum = sum + t;
+  }
+  const double avg = sum / lc.cum;
+#pragma unroll
+  for (int s = 0; s < LPL; s++) {
+    const bool act = s * 32 + lane < K;
+    const double biomass = wt[s] * lc.e1[s] * avg / (p.bio_L1 + p.bio_L2 * lc.e2[s]);
+    const double fac = p.bio_beta * pow(biomass, p.bio_b) / wt[s];
+    const double diff = lc.pre[s] * fac;
+    Dp[s] = act ? diff : 0.0;
+    Dd[s] = act ? diff + lc.mol[s] : 0.0;
+  }
+}
+
+template <int LPL, bool BC4, bool BIO3>
 __device__ __forceinline__ void column_rhs_ref(const Params<double>& p,
                                                const Lane<double, LPL, BC4>& lc,
                                                int lane, int K,
@@ -353,6 +451,13 @@ __device__ __forceinline__ void column_rhs_ref(const Params<double>& p,
                                                double (&R)[LPL][NTR],
                                                double (&ftop)[NTR],
                                                double (&dn)[LPL]) {
+  double Dpv[LPL], Ddv[LPL];
+  if constexpr (BIO3) {
+    bio3_diffusivities<LPL, BC4>(p, lc, lane, K, C, Dpv, Ddv);
+  } else {
+#pragma unroll
+    for (int s = 0; s < LPL; s++) { Dpv[s] = lc.Dp[s]; Ddv[s] = lc.Dd[s]; }
+  }
 #pragma unroll
   for (int s = 0; s < LPL; s++) omexdia_p_ref(p, C[s], R[s], dn[s]);
 #pragma unroll
@@ -365,14 +470,14 @@ __device__ __forceinline__ void column_rhs_ref(const Params<double>& p,
     // diff3d :776-778, interior interfaces
 #pragma unroll
     for (int s = 0; s < LPL; s++) {
-      const double D = part ? lc.Dp[s] : lc.Dd[s];
+      const double D = part ? Dpv[s] : Ddv[s];
       F[s] = -D * (v[s] - vm[s]) / lc.len[s];
     }
     // :782-803 upper boundary
     if (lane == 0) {
       double f0;
       if (part) f0 = lc.bnd(n);
-      else if (p.bcup_d == 2) f0 = -lc.Dd[0] * (v[0] - lc.bnd(n)) / lc.dz[0];
+      else if (p.bcup_d == 2) f0 = -Ddv[0] * (v[0] - lc.bnd(n)) / lc.dz[0];
       else if (p.bcup_d == 1) f0 = lc.bnd(n);
       else f0 = 0.0;
       F[0] = f0;

@@ -29,14 +29,14 @@ template <typename real>
 struct TileLayout {
   int tcp, kt;
   size_t conc, conc2, coef, cap, force, sflux, bud, nsub, total;
-  __host__ __device__ TileLayout(int tc, int kt_, bool bc4, bool two_states = false)
+  __host__ __device__ TileLayout(int tc, int kt_, bool bc4, bool two_states, int ncoef)
       : kt(kt_) {
     tcp = tc + 16 / (int)sizeof(real);  // row pad keeps 16-byte alignment
     size_t r = sizeof(real);
     conc = 0;
     conc2 = conc + (size_t)NTR * kt * tcp * r;
     coef = conc2 + (two_states ? (size_t)NTR * kt * tcp * r : 0);
-    cap = coef + (size_t)CoefRows<real>::value * kt * tcp * r;
+    cap = coef + (size_t)ncoef * kt * tcp * r;
     force = cap + (bc4 ? (size_t)kt * tcp * r : 0);
     sflux = force + (size_t)NFORCE * tcp * r;
     bud = sflux + (size_t)NDISS * tcp * r;
@@ -48,8 +48,8 @@ struct TileLayout {
 };
 
 template <typename real>
-size_t tile_smem_bytes(int tc, int lpl, bool bc4, int kind) {
-  return TileLayout<real>(tc, 32 * lpl, bc4, kind == KIND_RESID).total;
+size_t tile_smem_bytes(int tc, int lpl, bool bc4, int kind, bool bio3) {
+  return TileLayout<real>(tc, 32 * lpl, bc4, kind == KIND_RESID, coef_rows<real>(bio3)).total;
 }
 
 // Copy `rows` rows of tc reals between global (row stride gstride, first
@@ -99,7 +99,7 @@ __device__ __forceinline__ void copy_grouped(real* sm, real* g0, int ngroups,
 }
 
 // ---------------------------------------------------------------------------
-template <typename real, int LPL, bool BC4>
+template <typename real, int LPL, bool BC4, bool BIO3>
 __device__ __forceinline__ void load_lane(Lane<real, LPL, BC4>& lc,
                                           real (&C)[LPL][NTR],
                                           const real* s_conc,
@@ -126,8 +126,16 @@ __device__ __forceinline__ void load_lane(Lane<real, LPL, BC4>& lc,
       // the reference's operands: get_rhs :652-653 and :682-683
       const double phi = row(0), phi_i = row(1), bf = row(2), dz = row(3);
       const double len = row(4), mol1 = row(5);
-      const double diff = bioT / 86400.0 / 10000.0 * (1.0 - phi_i) * bf;
+      const double pre = bioT / 86400.0 / 10000.0 * (1.0 - phi_i);
+      const double diff = pre * bf;
       const double mol = mol_mode == 1 ? mol1 : dmul * phi_i / 86400.0 / 10000.0;
+      if constexpr (BIO3) {
+        lc.e1[s] = act ? row(NCOEF64) : 1.0;
+        lc.e2[s] = act ? row(NCOEF64 + 1) : 1.0;
+        lc.pre[s] = act ? pre : 0.0;
+        lc.mol[s] = act ? mol : 0.0;
+        if (s == 0) lc.cum = s_coef[((NCOEF64 + 2) * KT + 0) * tcp + j];
+      }
       lc.phi[s] = act ? phi : 1.0;
       lc.dz[s] = act ? dz : 1.0;
       lc.len[s] = act ? len : 1.0;
@@ -144,6 +152,13 @@ __device__ __forceinline__ void load_lane(Lane<real, LPL, BC4>& lc,
       lc.ivol[s] = act ? real(1) / vol : real(0);
       lc.ap[s] = act ? bioT * gb : real(0);
       lc.ad[s] = act ? bioT * gb + dmul * gm : real(0);
+      if constexpr (BIO3) {
+        lc.wc[s] = act ? phi / (real(1) - phi) : real(0);
+        lc.gz[s] = act ? row(NCOEF) : real(0);
+        lc.hw[s] = act ? row(NCOEF + 1) : real(0);
+        lc.gb3[s] = act ? gb : real(0);
+        lc.dm[s] = act ? dmul * gm : real(0);
+      }
     }
     cap[s] = (BC4 && act) ? s_cap[Lc * tcp + j] : real(0);
 #pragma unroll
@@ -158,16 +173,16 @@ __device__ __forceinline__ void load_lane(Lane<real, LPL, BC4>& lc,
 
 // The right-hand side used by the steppers: folded FP32 form, or the
 // reference-order FP64 form.
-template <typename real, int LPL, bool BC4>
+template <typename real, int LPL, bool BC4, bool BIO3>
 __device__ __forceinline__ void rhs_any(const Params<real>& p,
                                         const Lane<real, LPL, BC4>& lc, int lane,
                                         int K, const real (&C)[LPL][NTR],
                                         real (&R)[LPL][NTR], real (&ftop)[NTR],
                                         real (&dn)[LPL]) {
   if constexpr (std::is_same<real, double>::value)
-    column_rhs_ref<LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+    column_rhs_ref<LPL, BC4, BIO3>(p, lc, lane, K, C, R, ftop, dn);
   else
-    column_rhs<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+    column_rhs<real, LPL, BC4, BIO3>(p, lc, lane, K, C, R, ftop, dn);
 }
 
 // c + dt r (one rounding in FP32 via FMA; the reference's multiply then add
@@ -398,7 +413,7 @@ __device__ __forceinline__ int epilogue(const Params<real>& p, int lane, int K,
 // exact in FP64 (p.ticks), the same decisions are taken with integer ticks
 // of dt/4^mstop (mstop = first level with dt/4^m <= dt_min), which keeps the
 // loop off the FP64 pipe; otherwise the FP64 sums are kept.
-template <typename real, int LPL, bool BC4, bool TICKS>
+template <typename real, int LPL, bool BC4, bool BIO3, bool TICKS>
 __device__ __forceinline__ ColResult solve_adaptive(
     const Params<real>& p, const Lane<real, LPL, BC4>& lc, int lane, int K,
     real (&C)[LPL][NTR], real (&ftop)[NTR], double dt, double (&bud)[4]) {
@@ -412,7 +427,7 @@ __device__ __forceinline__ ColResult solve_adaptive(
   if (TICKS) { T = 1ull << (2 * p.mstop); inc = T; }
   int m = 0, mmax = -1;
   real dtr = (real)dt;
-  rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+  rhs_any<real, LPL, BC4, BIO3>(p, lc, lane, K, C, R, ftop, dn);
   while (TICKS ? (t < T) : (dt_int < dt)) {
     if (res.attempts >= p.max_attempts) { res.capped = 1; break; }
     res.attempts++;
@@ -445,7 +460,7 @@ __device__ __forceinline__ ColResult solve_adaptive(
       res.accepted++;
       mmax = m > mmax ? m : mmax;
       if (TICKS ? (t < T) : (dt_int < dt))
-        rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+        rhs_any<real, LPL, BC4, BIO3>(p, lc, lane, K, C, R, ftop, dn);
     }
   }
   if (mmax >= 0) res.min_dt = ldexp(dt, -2 * mmax);
@@ -456,7 +471,7 @@ __device__ __forceinline__ ColResult solve_adaptive(
 
 // EULER (:99-102), RUNGE_KUTTA_4 (:142-163), RUNGE_KUTTA_4_38 (:164-185),
 // each stage combined in the reference's operation order.
-template <typename real, int LPL, bool BC4>
+template <typename real, int LPL, bool BC4, bool BIO3>
 __device__ __forceinline__ ColResult solve_fixed(
     const Params<real>& p, const Lane<real, LPL, BC4>& lc, int lane, int K,
     real (&C)[LPL][NTR], real (&ftop)[NTR], double dt, int method,
@@ -468,7 +483,7 @@ __device__ __forceinline__ ColResult solve_fixed(
   B.start(p, lc, C);
   const real dtr = (real)dt;
   if (method == 0) {
-    rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+    rhs_any<real, LPL, BC4, BIO3>(p, lc, lane, K, C, R, ftop, dn);
     B.account(p, dtr, ftop, dn);
 #pragma unroll
     for (int s = 0; s < LPL; s++)
@@ -479,7 +494,7 @@ __device__ __forceinline__ ColResult solve_fixed(
     const real third = real(1.0 / 3.0);
     real Cs[LPL][NTR], R0[LPL][NTR], R1[LPL][NTR], R2[LPL][NTR];
     // stage 1: rhs0 at conc
-    rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R0, ftop, dn);
+    rhs_any<real, LPL, BC4, BIO3>(p, lc, lane, K, C, R0, ftop, dn);
     B.account(p, (real)(rk38 ? dt / 8.0 : dt / 6.0), ftop, dn);
 #pragma unroll
     for (int s = 0; s < LPL; s++)
@@ -488,7 +503,7 @@ __device__ __forceinline__ ColResult solve_fixed(
         Cs[s][n] = rk38 ? C[s][n] + third * dtr * R0[s][n]
                         : C[s][n] + real(0.5) * dtr * R0[s][n];
     // stage 2: rhs1 at c1
-    rhs_any<real, LPL, BC4>(p, lc, lane, K, Cs, R1, ftop, dn);
+    rhs_any<real, LPL, BC4, BIO3>(p, lc, lane, K, Cs, R1, ftop, dn);
     B.account(p, (real)(rk38 ? 3.0 * dt / 8.0 : dt / 3.0), ftop, dn);
 #pragma unroll
     for (int s = 0; s < LPL; s++)
@@ -497,7 +512,7 @@ __device__ __forceinline__ ColResult solve_fixed(
         Cs[s][n] = rk38 ? C[s][n] + dtr * (R1[s][n] - third * R0[s][n])
                         : C[s][n] + real(0.5) * dtr * R1[s][n];
     // stage 3: rhs2
-    rhs_any<real, LPL, BC4>(p, lc, lane, K, Cs, R2, ftop, dn);
+    rhs_any<real, LPL, BC4, BIO3>(p, lc, lane, K, Cs, R2, ftop, dn);
     B.account(p, (real)(rk38 ? 3.0 * dt / 8.0 : dt / 3.0), ftop, dn);
 #pragma unroll
     for (int s = 0; s < LPL; s++)
@@ -506,7 +521,7 @@ __device__ __forceinline__ ColResult solve_fixed(
         Cs[s][n] = rk38 ? C[s][n] + dtr * (R0[s][n] - R1[s][n] + R2[s][n])
                         : C[s][n] + dtr * R2[s][n];
     // stage 4: rhs3 and the combination
-    rhs_any<real, LPL, BC4>(p, lc, lane, K, Cs, R, ftop, dn);
+    rhs_any<real, LPL, BC4, BIO3>(p, lc, lane, K, Cs, R, ftop, dn);
     B.account(p, (real)(rk38 ? dt / 8.0 : dt / 6.0), ftop, dn);
 #pragma unroll
     for (int s = 0; s < LPL; s++)
@@ -538,14 +553,15 @@ struct MinBlocks {
   static constexpr int value = sizeof(real) == 4 ? (LPL == 1 ? 3 : 2) : 1;
 };
 
-template <typename real, int LPL, bool BC4, int KIND>
+template <typename real, int LPL, bool BC4, bool BIO3, int KIND>
 __global__ void __launch_bounds__(256, (MinBlocks<real, LPL>::value))
 k_column(ColumnArgs<real> a, Params<real> p) {
   constexpr int mode = KIND == KIND_RHS ? 1 : 0;
+  constexpr int NCO = coef_rows<real>(BIO3);
   extern __shared__ __align__(16) unsigned char smem[];
   const int tc = a.tc;
   constexpr int KT = 32 * LPL;
-  TileLayout<real> L(tc, KT, BC4, KIND == KIND_RESID);
+  TileLayout<real> L(tc, KT, BC4, KIND == KIND_RESID, NCO);
   const int tcp = L.tcp;
   real* s_conc = reinterpret_cast<real*>(smem + L.conc);
   real* s_conc2 = reinterpret_cast<real*>(smem + L.conc2);
@@ -580,9 +596,8 @@ k_column(ColumnArgs<real> a, Params<real> p) {
     if (KIND == KIND_RESID)
       copy_grouped<real, true>(s_conc2, a.conc + slot0, NTR, kt, KT, a.kmax, ns, tc,
                                tcp, tid, nthr);
-    copy_grouped<real, true>(s_coef, const_cast<real*>(a.coef) + slot0,
-                             CoefRows<real>::value, kt, KT, a.kmax, ns, tc, tcp,
-                             tid, nthr);
+    copy_grouped<real, true>(s_coef, const_cast<real*>(a.coef) + slot0, NCO, kt, KT,
+                             a.kmax, ns, tc, tcp, tid, nthr);
     if (BC4)
       copy_grouped<real, true>(s_cap, const_cast<real*>(a.cap) + slot0, 1, kt,
                                KT, a.kmax, ns, tc, tcp, tid, nthr);
@@ -618,8 +633,8 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       }
       Lane<real, LPL, BC4> lc;
       real C[LPL][NTR];
-      load_lane<real, LPL, BC4>(lc, C, s_conc, s_coef, s_cap, s_force, j, KT,
-                                tcp, lane, K, p.mol_mode);
+      load_lane<real, LPL, BC4, BIO3>(lc, C, s_conc, s_coef, s_cap, s_force, j, KT,
+                                      tcp, lane, K, p.mol_mode);
       real ftop[NTR];
 #pragma unroll
       for (int n = 0; n < NTR; n++) ftop[n] = real(0);
@@ -628,7 +643,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
         // |C' - C - dt f(C')| / (|C'| + |C| + dt |f(C')| + atol)
         real R[LPL][NTR];
         real dn[LPL];
-        rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+        rhs_any<real, LPL, BC4, BIO3>(p, lc, lane, K, C, R, ftop, dn);
         const real dtr = (real)a.dt, at = (real)a.res_atol;
         real rho = real(0);
 #pragma unroll
@@ -673,7 +688,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       if (KIND == KIND_RHS) {
         real R[LPL][NTR];
         real dn[LPL];
-        rhs_any<real, LPL, BC4>(p, lc, lane, K, C, R, ftop, dn);
+        rhs_any<real, LPL, BC4, BIO3>(p, lc, lane, K, C, R, ftop, dn);
 #pragma unroll
         for (int s = 0; s < LPL; s++) {
           const int Ll = s * 32 + lane;
@@ -691,11 +706,11 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       double bud[4] = {0.0, 0.0, 0.0, 0.0};
       ColResult r;
       if (KIND == KIND_ADAPT)
-        r = p.ticks ? solve_adaptive<real, LPL, BC4, true>(p, lc, lane, K, C, ftop, a.dt, bud)
-                    : solve_adaptive<real, LPL, BC4, false>(p, lc, lane, K, C, ftop, a.dt, bud);
+        r = p.ticks ? solve_adaptive<real, LPL, BC4, BIO3, true>(p, lc, lane, K, C, ftop, a.dt, bud)
+                    : solve_adaptive<real, LPL, BC4, BIO3, false>(p, lc, lane, K, C, ftop, a.dt, bud);
       else
-        r = solve_fixed<real, LPL, BC4>(p, lc, lane, K, C, ftop, a.dt, a.method,
-                                        bud);
+        r = solve_fixed<real, LPL, BC4, BIO3>(p, lc, lane, K, C, ftop, a.dt, a.method,
+                                              bud);
 #pragma unroll
       for (int s = 0; s < LPL; s++) {
         const int Ll = s * 32 + lane;
@@ -932,7 +947,7 @@ __global__ void k_prep_force(const double* __restrict__ bdys,
                              const int* __restrict__ slot_col,
                              real* __restrict__ force, int ncol, int nslot,
                              double bio, double diffusivity, int mode,
-                             int bcup_d) {
+                             int bcup_d, int bio3) {
   for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < nslot;
        slot += gridDim.x * blockDim.x) {
     const int col = slot_col[slot];
@@ -941,7 +956,7 @@ __global__ void k_prep_force(const double* __restrict__ bdys,
     if (col >= 0) {
       const double T = bdys[col];
       const double fT = 1.0 * exp(-4500.0 * (1.0 / (T + 273.0) - (1.0 / 288.0)));
-      f[0] = bio * fT;
+      f[0] = bio3 ? 1.0 : bio * fT;  // profile 3: bioturbation = f_T = 1 (:622-623)
       f[1] = (mode == 1) ? 1.0 : (diffusivity + T * 0.035);
       for (int n = 0; n < NTR; n++) {
         const bool part = n < NPART;
@@ -964,27 +979,91 @@ static int grid_for(size_t total, int block, int sms) {
   return (int)g;
 }
 
-template <typename real, int LPL, bool BC4, int KIND>
+// Coefficient rows of bioturbation profile 3 from the host's per-cell
+// exp(zc 100 k_l), exp(zc 200 k_l) and per-column cumdepth (the depth of
+// the last layer's upper interface).  FP32: row 2 becomes the bioturbation
+// conductance per unit factor (1 - phi_i) / len / 8.64e8, row NCOEF the
+// depth term e1 / (L1 + L2 e2) and row NCOEF+1 the averaging weight
+// dz / cumdepth.  FP64: rows NCOEF64.. hold e1, e2 and cumdepth.
+template <typename real>
+__global__ void k_prep_bio3(const double* __restrict__ dz, const double* __restrict__ dzc,
+                            const double* __restrict__ phi_i, const double* __restrict__ e1,
+                            const double* __restrict__ e2, const double* __restrict__ cum,
+                            const int* __restrict__ slot_col, real* __restrict__ coef,
+                            int kmax, int ncol, int nslot, double L1, double L2) {
+  const size_t total = (size_t)kmax * nslot;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int slot = (int)(i % nslot);
+    const int k = (int)(i / nslot);
+    const int col = slot_col[slot];
+    auto at = [&](int r) -> real& { return coef[((size_t)r * kmax + k) * nslot + slot]; };
+    if constexpr (std::is_same<real, double>::value) {
+      double v0 = 1.0, v1 = 1.0, v2 = 1.0;
+      if (col >= 0) {
+        const size_t c = (size_t)k * ncol + col;
+        v0 = e1[c];
+        v1 = e2[c];
+        v2 = cum[col];
+      }
+      at(NCOEF64) = v0;
+      at(NCOEF64 + 1) = v1;
+      at(NCOEF64 + 2) = v2;
+    } else {
+      double gb = 0.0, g = 0.0, hw = 0.0;
+      if (col >= 0) {
+        const size_t c = (size_t)k * ncol + col;
+        const double len = (k == 0) ? dz[c] : dzc[(size_t)(k - 1) * ncol + col];
+        gb = (1.0 - phi_i[c]) / len / 8.64e8;
+        g = e1[c] / (L1 + L2 * e2[c]);
+        hw = dz[c] / cum[col];
+      }
+      at(2) = (real)gb;
+      at(NCOEF) = (real)g;
+      at(NCOEF + 1) = (real)hw;
+    }
+  }
+}
+
+template <typename real>
+cudaError_t launch_prep_bio3(const double* dz, const double* dzc, const double* phi_i,
+                             const double* e1, const double* e2, const double* cum,
+                             const int* slot_col, real* coef, int kmax, int ncol, int nslot,
+                             double L1, double L2, int sms, cudaStream_t st) {
+  const size_t total = (size_t)kmax * nslot;
+  k_prep_bio3<real><<<grid_for(total, 256, sms), 256, 0, st>>>(
+      dz, dzc, phi_i, e1, e2, cum, slot_col, coef, kmax, ncol, nslot, L1, L2);
+  return cudaGetLastError();
+}
+
+template <typename real, int LPL, bool BC4, bool BIO3, int KIND>
 static cudaError_t launch_column_t(const ColumnArgs<real>& a, const Params<real>& p,
                                    int blocks, int threads, cudaStream_t st) {
   // the shared-memory limit was raised by column_blocks_per_sm at set-up, so
   // this launch makes no attribute call and can be stream-captured
-  const size_t smem = tile_smem_bytes<real>(a.tc, LPL, BC4, KIND);
-  k_column<real, LPL, BC4, KIND><<<blocks, threads, smem, st>>>(a, p);
+  const size_t smem = tile_smem_bytes<real>(a.tc, LPL, BC4, KIND, BIO3);
+  k_column<real, LPL, BC4, BIO3, KIND><<<blocks, threads, smem, st>>>(a, p);
   return cudaGetLastError();
 }
 
-template <typename real, int LPL, bool BC4>
-static cudaError_t launch_column_k(const ColumnArgs<real>& a, const Params<real>& p,
+template <typename real, int LPL, bool BC4, bool BIO3>
+cudaError_t launch_column_k(const ColumnArgs<real>& a, const Params<real>& p,
                                    int kind, int blocks, int threads,
                                    cudaStream_t st) {
   if (kind == KIND_ADAPT)
-    return launch_column_t<real, LPL, BC4, KIND_ADAPT>(a, p, blocks, threads, st);
+    return launch_column_t<real, LPL, BC4, BIO3, KIND_ADAPT>(a, p, blocks, threads, st);
   if (kind == KIND_FIXED)
-    return launch_column_t<real, LPL, BC4, KIND_FIXED>(a, p, blocks, threads, st);
+    return launch_column_t<real, LPL, BC4, BIO3, KIND_FIXED>(a, p, blocks, threads, st);
   if (kind == KIND_RESID)
-    return launch_column_t<real, LPL, BC4, KIND_RESID>(a, p, blocks, threads, st);
-  return launch_column_t<real, LPL, BC4, KIND_RHS>(a, p, blocks, threads, st);
+    return launch_column_t<real, LPL, BC4, BIO3, KIND_RESID>(a, p, blocks, threads, st);
+  return launch_column_t<real, LPL, BC4, BIO3, KIND_RHS>(a, p, blocks, threads, st);
+}
+
+template <typename real, int LPL, bool BC4>
+static cudaError_t launch_column_b(const ColumnArgs<real>& a, const Params<real>& p,
+                                   int kind, int blocks, int threads, cudaStream_t st) {
+  return p.bio3 ? launch_column_k<real, LPL, BC4, true>(a, p, kind, blocks, threads, st)
+                : launch_column_k<real, LPL, BC4, false>(a, p, kind, blocks, threads, st);
 }
 
 template <typename real>
@@ -992,16 +1071,16 @@ cudaError_t launch_column(const ColumnArgs<real>& a, const Params<real>& p,
                           int lpl, bool bc4, int kind, int blocks, int threads,
                           cudaStream_t st) {
   if (lpl == 1)
-    return bc4 ? launch_column_k<real, 1, true>(a, p, kind, blocks, threads, st)
-               : launch_column_k<real, 1, false>(a, p, kind, blocks, threads, st);
-  return bc4 ? launch_column_k<real, 2, true>(a, p, kind, blocks, threads, st)
-             : launch_column_k<real, 2, false>(a, p, kind, blocks, threads, st);
+    return bc4 ? launch_column_b<real, 1, true>(a, p, kind, blocks, threads, st)
+               : launch_column_b<real, 1, false>(a, p, kind, blocks, threads, st);
+  return bc4 ? launch_column_b<real, 2, true>(a, p, kind, blocks, threads, st)
+             : launch_column_b<real, 2, false>(a, p, kind, blocks, threads, st);
 }
 
-template <typename real, int LPL, bool BC4, int KIND>
+template <typename real, int LPL, bool BC4, bool BIO3, int KIND>
 static int occupancy_t(int tc, int threads) {
-  const size_t smem = tile_smem_bytes<real>(tc, LPL, BC4, KIND);
-  auto fn = k_column<real, LPL, BC4, KIND>;
+  const size_t smem = tile_smem_bytes<real>(tc, LPL, BC4, KIND, BIO3);
+  auto fn = k_column<real, LPL, BC4, BIO3, KIND>;
   // the limit is raised to the device maximum (never lowered), so handles
   // with different tile widths can share the kernel
   // (the opt-in maximum less the kernel's static shared variables)
@@ -1023,21 +1102,27 @@ static int occupancy_t(int tc, int threads) {
   return nb;
 }
 
+template <typename real, int LPL, bool BC4, bool BIO3>
+int occupancy_k(int tc, int kind, int threads) {
+  if (kind == KIND_ADAPT) return occupancy_t<real, LPL, BC4, BIO3, KIND_ADAPT>(tc, threads);
+  if (kind == KIND_FIXED) return occupancy_t<real, LPL, BC4, BIO3, KIND_FIXED>(tc, threads);
+  if (kind == KIND_RESID) return occupancy_t<real, LPL, BC4, BIO3, KIND_RESID>(tc, threads);
+  return occupancy_t<real, LPL, BC4, BIO3, KIND_RHS>(tc, threads);
+}
+
 template <typename real, int LPL, bool BC4>
-static int occupancy_k(int tc, int kind, int threads) {
-  if (kind == KIND_ADAPT) return occupancy_t<real, LPL, BC4, KIND_ADAPT>(tc, threads);
-  if (kind == KIND_FIXED) return occupancy_t<real, LPL, BC4, KIND_FIXED>(tc, threads);
-  if (kind == KIND_RESID) return occupancy_t<real, LPL, BC4, KIND_RESID>(tc, threads);
-  return occupancy_t<real, LPL, BC4, KIND_RHS>(tc, threads);
+static int occupancy_b(int tc, int kind, int threads, bool bio3) {
+  return bio3 ? occupancy_k<real, LPL, BC4, true>(tc, kind, threads)
+              : occupancy_k<real, LPL, BC4, false>(tc, kind, threads);
 }
 
 template <typename real>
-int column_blocks_per_sm(int tc, int lpl, bool bc4, int kind, int threads) {
+int column_blocks_per_sm(int tc, int lpl, bool bc4, int kind, int threads, bool bio3) {
   if (lpl == 1)
-    return bc4 ? occupancy_k<real, 1, true>(tc, kind, threads)
-               : occupancy_k<real, 1, false>(tc, kind, threads);
-  return bc4 ? occupancy_k<real, 2, true>(tc, kind, threads)
-             : occupancy_k<real, 2, false>(tc, kind, threads);
+    return bc4 ? occupancy_b<real, 1, true>(tc, kind, threads, bio3)
+               : occupancy_b<real, 1, false>(tc, kind, threads, bio3);
+  return bc4 ? occupancy_b<real, 2, true>(tc, kind, threads, bio3)
+             : occupancy_b<real, 2, false>(tc, kind, threads, bio3);
 }
 
 template <typename real>
@@ -1136,18 +1221,35 @@ template <typename real>
 cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
                               const int* slot_col, real* force, int ncol,
                               int nslot, double bio, double diffusivity,
-                              int mode, int bcup_d, int sms, cudaStream_t st) {
+                              int mode, int bcup_d, int bio3, int sms, cudaStream_t st) {
   k_prep_force<real><<<grid_for(nslot, 128, sms), 128, 0, st>>>(
-      bdys, fluxes, slot_col, force, ncol, nslot, bio, diffusivity, mode, bcup_d);
+      bdys, fluxes, slot_col, force, ncol, nslot, bio, diffusivity, mode, bcup_d, bio3);
   return cudaGetLastError();
 }
 
+// The kernels of one profile-3 setting for every layers-per-lane / BcUp-4
+// combination: the BIO3 = true set is compiled in its own translation unit
+// (declared extern where the dispatchers are instantiated).
+#define SED_VARIANT(prefix, real, BIO3)                                         \
+  prefix template cudaError_t launch_column_k<real, 1, false, BIO3>(            \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t); \
+  prefix template cudaError_t launch_column_k<real, 1, true, BIO3>(             \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t); \
+  prefix template cudaError_t launch_column_k<real, 2, false, BIO3>(            \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t); \
+  prefix template cudaError_t launch_column_k<real, 2, true, BIO3>(             \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t); \
+  prefix template int occupancy_k<real, 1, false, BIO3>(int, int, int);         \
+  prefix template int occupancy_k<real, 1, true, BIO3>(int, int, int);          \
+  prefix template int occupancy_k<real, 2, false, BIO3>(int, int, int);         \
+  prefix template int occupancy_k<real, 2, true, BIO3>(int, int, int);
+
 #define SED_INSTANTIATE(real)                                                   \
-  template size_t tile_smem_bytes<real>(int, int, bool, int);                   \
+  template size_t tile_smem_bytes<real>(int, int, bool, int, bool);             \
   template cudaError_t launch_column<real>(const ColumnArgs<real>&,             \
                                            const Params<real>&, int, bool, int, \
                                            int, int, cudaStream_t);             \
-  template int column_blocks_per_sm<real>(int, int, bool, int, int);            \
+  template int column_blocks_per_sm<real>(int, int, bool, int, int, bool);      \
   template cudaError_t launch_trial<real>(const real*, const real*, const int*, \
                                           int, int, real, real, real, int*,     \
                                           int, cudaStream_t);                   \
@@ -1179,6 +1281,10 @@ cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
   template cudaError_t launch_prep_force<real>(const double*, const double*,    \
                                                const int*, real*, int, int,     \
                                                double, double, int, int, int,   \
-                                               cudaStream_t);
+                                               int, cudaStream_t);              \
+  template cudaError_t launch_prep_bio3<real>(                                  \
+      const double*, const double*, const double*, const double*,               \
+      const double*, const double*, const int*, real*, int, int, int, double,   \
+      double, int, cudaStream_t);
 
 }  // namespace sed

@@ -11,7 +11,7 @@ namespace sed {
 enum : int { KIND_ADAPT = 0, KIND_FIXED = 1, KIND_RHS = 2, KIND_RESID = 3 };
 
 // Arguments of the tile kernel.  Device layouts (slot = compacted column):
-//   conc  [NTR][kmax][nslot]     coef  [CoefRows][kmax][nslot]
+//   conc  [NTR][kmax][nslot]     coef  [coef_rows][kmax][nslot]
 //   cap   [kmax][nslot] (BcUp 4) force [NFORCE][nslot]
 //   sflux [NDISS][nslot]         budget[4][nslot] (FP64)
 template <typename real>
@@ -41,7 +41,7 @@ struct ColumnArgs {
 };
 
 template <typename real>
-size_t tile_smem_bytes(int tc, int lpl, bool bc4, int kind = KIND_ADAPT);
+size_t tile_smem_bytes(int tc, int lpl, bool bc4, int kind, bool bio3);
 
 template <typename real>
 cudaError_t launch_column(const ColumnArgs<real>& a, const Params<real>& p,
@@ -49,7 +49,7 @@ cudaError_t launch_column(const ColumnArgs<real>& a, const Params<real>& p,
                           cudaStream_t st);
 
 template <typename real>
-int column_blocks_per_sm(int tc, int lpl, bool bc4, int kind, int threads);
+int column_blocks_per_sm(int tc, int lpl, bool bc4, int kind, int threads, bool bio3);
 
 template <typename real>
 cudaError_t launch_trial(const real* conc, const real* rhs, const int* kact,
@@ -105,6 +105,13 @@ template <typename real>
 cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
                               const int* slot_col, real* force, int ncol,
                               int nslot, double bio, double diffusivity,
-                              int mode, int bcup_d, int sms, cudaStream_t st);
+                              int mode, int bcup_d, int bio3, int sms, cudaStream_t st);
+
+// coefficient rows of bioturbation profile 3 (after launch_prep_grid)
+template <typename real>
+cudaError_t launch_prep_bio3(const double* dz, const double* dzc, const double* phi_i,
+                             const double* e1, const double* e2, const double* cum,
+                             const int* slot_col, real* coef, int kmax, int ncol, int nslot,
+                             double L1, double L2, int sms, cudaStream_t st);
 
 }  // namespace sed

@@ -115,6 +115,7 @@ extern "C" int sed_ode_solver_noalloc(const sed_params* p, int inum, int jnum,
   if (p->bcup_particulate == 4 && !flux_cap) return SED_E_ARG;
   if (p->mol_diff_mode != 0 && p->mol_diff_mode != 1) return SED_E_ARG;
   if (p->max_attempts <= 0 || !(p->atol >= 0.0)) return SED_E_ARG;
+  if (p->bioturbation_profile == 3) return SED_E_ARG;  // static biofac only
   if (method < 0 || method > 3 || !(dt > 0.0)) return SED_E_ARG;
   const int ncol = inum * jnum;
   // the same domain checks as sed_set_grid (fabm_sediment_driver.F90:503-530)
@@ -161,7 +162,7 @@ extern "C" int sed_ode_solver_noalloc(const sed_params* p, int inum, int jnum,
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess)
     return SED_E_CUDA;
   const int kind = method == SED_ADAPTIVE_EULER ? KIND_ADAPT : KIND_FIXED;
-  const int occ = column_blocks_per_sm<float>(tc, lpl, bc4, kind, 256);
+  const int occ = column_blocks_per_sm<float>(tc, lpl, bc4, kind, 256, false);
   if (occ <= 0) return SED_E_CUDA;
 
   cudaStream_t st = 0;
@@ -219,7 +220,7 @@ extern "C" int sed_ode_solver_noalloc(const sed_params* p, int inum, int jnum,
                                 reinterpret_cast<double*>(base + L.fluxes), slot_col,
                                 reinterpret_cast<float*>(base + L.force), ncol, nslot,
                                 p->bioturbation, p->diffusivity, p->mol_diff_mode,
-                                p->bcup_dissolved, sms, st));
+                                p->bcup_dissolved, 0, sms, st));
     launches += 2;
   }
   // work counter and statistics start from zero / +inf

@@ -39,6 +39,13 @@ inline Params<real> make_params(const sed_params& s) {
   p.max_attempts = s.max_attempts;
   p.epilogue = s.epilogue;
   p.budgets = s.budgets;
+  p.bio3 = s.bioturbation_profile == 3;
+  p.toc_f1 = (real)(1.0 / 1.2 * 12.01 / s.bioturb_dry_density / 1000.0);
+  p.toc_f2 = (real)(1.0 / 6.0 * 12.01 / s.bioturb_dry_density / 1000.0);
+  p.bio_beta = (real)s.bioturb_beta;
+  p.bio_b = (real)s.bioturb_b;
+  p.bio_L1 = (real)s.bioturb_L1;
+  p.bio_L2 = (real)s.bioturb_L2;
   return p;
 }
 

@@ -36,6 +36,10 @@ module sed_gpu
     integer(c_int)  :: epilogue
     real(c_double)  :: minimum(SED_NTR)
     integer(c_int)  :: precision, budgets, device
+    !> bioturbation_profile 3: Zhang & Wirtz factor from the TOC profile
+    integer(c_int)  :: bioturbation_profile
+    real(c_double)  :: bioturb_k_l, bioturb_L1, bioturb_L2, bioturb_beta, &
+                       bioturb_b, bioturb_dry_density
   end type
 
   type, bind(C), public :: sed_stats_t
@@ -43,7 +47,18 @@ module sed_gpu
     integer(c_int)       :: max_col_attempts, capped_columns, nan_cells, &
                             gpu_launches
     real(c_double)       :: min_dt, device_ms
+    integer(c_long_long) :: surrogate_columns
   end type
+
+  !> sed_tuning of mossco_sed.h: launch choices per depth class (1: up to
+  !! 32 layers, 2: 33..64), sed_ode_solver's pipeline depth, substep cap
+  type, bind(C), public :: sed_tuning_t
+    integer(c_int) :: tile_columns(2), threads(2), blocks_per_sm(2)
+    integer(c_int) :: pipeline_chunks, segments, max_attempts
+    real(c_float)  :: step_ms, ode_solver_ms
+    integer(c_int) :: trials
+  end type
+  integer, parameter, public :: SED_TUNE_PIPELINE = 1, SED_TUNE_CAP = 2
 
   !> a solver handle
   type, public :: sed_gpu_t
@@ -87,6 +102,23 @@ module sed_gpu
       type(c_ptr), value :: ptr
       integer(c_size_t), value :: bytes
     end function
+    integer(c_int) function sed_get_tuning(h, t) bind(C, name='sed_get_tuning')
+      import :: c_int, c_ptr, sed_tuning_t
+      type(c_ptr), value :: h
+      type(sed_tuning_t), intent(out) :: t
+    end function
+    integer(c_int) function sed_set_tuning(h, t) bind(C, name='sed_set_tuning')
+      import :: c_int, c_ptr, sed_tuning_t
+      type(c_ptr), value :: h
+      type(sed_tuning_t), intent(in) :: t
+    end function
+    integer(c_int) function sed_autotune(h, dt, method, flags, t) bind(C, name='sed_autotune')
+      import :: c_int, c_ptr, c_double, sed_tuning_t
+      type(c_ptr), value :: h
+      real(c_double), value :: dt
+      integer(c_int), value :: method, flags
+      type(sed_tuning_t), intent(out) :: t
+    end function
     subroutine sed_destroy(h) bind(C, name='sed_destroy')
       import :: c_ptr
       type(c_ptr), value :: h
@@ -94,7 +126,8 @@ module sed_gpu
   end interface
 
   public :: sed_default_params, sed_gpu_init, sed_gpu_ode_solver, &
-            sed_gpu_get_rhs, sed_gpu_finalize
+            sed_gpu_get_rhs, sed_gpu_finalize, sed_get_tuning, sed_set_tuning, &
+            sed_autotune
 
 contains
 

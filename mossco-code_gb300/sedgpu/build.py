@@ -21,11 +21,13 @@ BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_NAME = "libsedgpu.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 
-SOURCES = ["sed_kernels_f32.cu", "sed_kernels_f64.cu", "sed_capi.cu",
-           "sed_noalloc.cu", "sur_kernels.cu", "sur_capi.cu", "sur_loop.cu"]
+SOURCES = ["sed_kernels_f32.cu", "sed_kernels_f64.cu", "sed_kernels_f32_bio3.cu",
+           "sed_kernels_f64_bio3.cu", "sed_capi.cu", "sed_noalloc.cu", "sur_kernels.cu",
+           "sur_capi.cu", "sur_loop.cu"]
 # The FP64 kernels evaluate the reference's arithmetic operation by
 # operation: no multiply-add contraction.
-EXTRA_FLAGS = {"sed_kernels_f64.cu": ["-fmad=false"]}
+EXTRA_FLAGS = {"sed_kernels_f64.cu": ["-fmad=false"],
+               "sed_kernels_f64_bio3.cu": ["-fmad=false"]}
 HEADERS = ["sed_device.cuh", "sed_kernels.cuh", "sed_launch.h", "sed_params.h",
            "sur_kernels.h", "sur_internal.h", "sur_loop.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

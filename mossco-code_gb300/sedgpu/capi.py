@@ -48,7 +48,14 @@ class SedParams(ctypes.Structure):
                    ("minimum", ctypes.c_double * NTR),
                    ("precision", ctypes.c_int),
                    ("budgets", ctypes.c_int),
-                   ("device", ctypes.c_int)])
+                   ("device", ctypes.c_int),
+                   ("bioturbation_profile", ctypes.c_int),
+                   ("bioturb_k_l", ctypes.c_double),
+                   ("bioturb_L1", ctypes.c_double),
+                   ("bioturb_L2", ctypes.c_double),
+                   ("bioturb_beta", ctypes.c_double),
+                   ("bioturb_b", ctypes.c_double),
+                   ("bioturb_dry_density", ctypes.c_double)])
 
 
 class SedStats(ctypes.Structure):
@@ -215,6 +222,10 @@ def params_from(cs: ColumnSet, precision: int = SED_FP32, budgets: bool = False,
     p.precision = precision
     p.budgets = int(budgets)
     p.device = device
+    p.bioturbation_profile = int(d.bioturbation_profile)
+    for n in ("bioturb_k_l", "bioturb_L1", "bioturb_L2", "bioturb_beta", "bioturb_b",
+              "bioturb_dry_density"):
+        setattr(p, n, float(getattr(d, n)))
     return p
 
 

@@ -77,6 +77,16 @@ class DriverParams:
     atol: float = 0.0                   # absolute floor of the positivity test
     max_attempts: int = 8192            # adaptive loop guard per step
     minimum: Optional[np.ndarray] = None  # clamp per tracer (default 0)
+    # 3: bioturbation factor of Zhang & Wirtz (2017) recomputed from the TOC
+    # profile at every right-hand side (get_rhs :618-645); any other value:
+    # the static biofac profile.  Constants: sed_nml bioturb_* (:226-231).
+    bioturbation_profile: int = 1
+    bioturb_k_l: float = 0.11
+    bioturb_L1: float = 0.2
+    bioturb_L2: float = 0.6
+    bioturb_beta: float = 0.22
+    bioturb_b: float = 1.334
+    bioturb_dry_density: float = 1000.0
 
     def minimum_array(self) -> np.ndarray:
         if self.minimum is None:

@@ -71,6 +71,10 @@ class Model(ctypes.Structure):
         ("atol", ctypes.c_double),
         ("max_attempts", ctypes.c_long),
         ("bgc", Bgc),
+        ("bioturbation_profile", ctypes.c_int),
+        ("bioturb_k_l", ctypes.c_double), ("bioturb_L1", ctypes.c_double),
+        ("bioturb_L2", ctypes.c_double), ("bioturb_beta", ctypes.c_double),
+        ("bioturb_b", ctypes.c_double), ("bioturb_dry_density", ctypes.c_double),
     ]
 
 
@@ -163,6 +167,10 @@ class OracleModel:
         m.max_attempts = d.max_attempts
         for n in BGC_NAMES:
             setattr(m.bgc, n, float(cs.bgc[n]))
+        m.bioturbation_profile = int(d.bioturbation_profile)
+        for n in ("bioturb_k_l", "bioturb_L1", "bioturb_L2", "bioturb_beta",
+                  "bioturb_b", "bioturb_dry_density"):
+            setattr(m, n, float(getattr(d, n)))
         self.m = m
 
     def get_rhs(self, conc: np.ndarray, fluxes: Optional[np.ndarray] = None):

@@ -185,7 +185,7 @@ void orc_diff3d(int K, const double *C, double Cup, double Cdown,
 /* ------------------------------------------------------------------------ */
 typedef struct {
   double *dz, *dzc, *phi, *phi_i, *bf, *cap; /* column copies */
-  double *diff, *cin, *vf, *flux, *dC, *tr, *cell, *rate;
+  double *diff, *cin, *vf, *flux, *dC, *tr, *cell, *rate, *wt;
 } rhs_ws;
 
 static void rhs_ws_alloc(rhs_ws *w, int kmax, int ntr) {
@@ -204,12 +204,45 @@ static void rhs_ws_alloc(rhs_ws *w, int kmax, int ntr) {
   w->tr = calloc(K * ntr, sizeof(double));
   w->cell = calloc(ntr, sizeof(double));
   w->rate = calloc(ntr, sizeof(double));
+  w->wt = calloc(K, sizeof(double));
 }
 
 static void rhs_ws_free(rhs_ws *w) {
   free(w->dz); free(w->dzc); free(w->phi); free(w->phi_i); free(w->bf);
   free(w->cap); free(w->diff); free(w->cin); free(w->vf); free(w->flux);
-  free(w->dC); free(w->tr); free(w->cell); free(w->rate);
+  free(w->dC); free(w->tr); free(w->cell); free(w->rate); free(w->wt);
+}
+
+/* bioturbation_profile 3 (get_rhs :618-645) for one column of K layers:
+ * weighted TOC [mg C / g dry mass] from the two carbon detritus pools (POC
+ * class factors of initialize :380-386), its dz-weighted column sum divided
+ * by cumdepth -- the depth of the last layer's upper interface, the value the
+ * environment loop :593-605 leaves behind -- the infauna biomass and the
+ * factor beta biomass^b / TOC, in the reference's operation order.  zc is
+ * formed from dz as init_grid does (:150-152). */
+static void zhang_wirtz_factor(const orc_model *m, int K, const double *dz,
+                               const double *phi, const double *C0,
+                               const double *C1, double *wt, double *bf) {
+  const double f1 = 1.0 / 1.2 * 12.01 / m->bioturb_dry_density / 1000.0;
+  const double f2 = 1.0 / 6.0 * 12.01 / m->bioturb_dry_density / 1000.0;
+  for (int k = 0; k < K; k++) {
+    wt[k] = 0.0;
+    wt[k] = wt[k] + f1 * phi[k] / (1.0 - phi[k]) * C0[k];
+    wt[k] = wt[k] + f2 * phi[k] / (1.0 - phi[k]) * C1[k];
+  }
+  double cum = 0.0;
+  for (int k = 0; k < K - 1; k++) cum = cum + dz[k];
+  double sum = 0.0;
+  for (int k = 0; k < K; k++) sum = sum + dz[k] * wt[k];
+  const double avg = sum / cum;
+  double zi = 0.0;
+  for (int k = 0; k < K; k++) {
+    const double zc = zi + 0.5 * dz[k];
+    zi = zi + dz[k];
+    const double biomass = wt[k] * exp(zc * 100.0 * m->bioturb_k_l) * avg /
+                           (m->bioturb_L1 + m->bioturb_L2 * exp(zc * 200.0 * m->bioturb_k_l));
+    bf[k] = m->bioturb_beta * pow(biomass, m->bioturb_b) / wt[k];
+  }
 }
 
 /* get_rhs for one column `col` of model m (arrays of stride m->ncol). */
@@ -235,13 +268,24 @@ static void get_rhs_col(const orc_model *m, int col, const double *conc,
   }
   /* :593-605 temperature of the column = bottom-water temperature */
   const double T = bdys[col];
-  /* :648 f_T */
-  const double f_T = 1.0 * exp(-4500.0 * (1.0 / (T + 273.0) - (1.0 / 288.0)));
+  /* :648 f_T; with profile 3, f_T = 1 and bioturbation = 1 (:622-623) and
+   * the factor is recomputed from the state */
+  double f_T = 1.0 * exp(-4500.0 * (1.0 / (T + 273.0) - (1.0 / 288.0)));
+  double bioturbation = m->bioturbation;
+  if (m->bioturbation_profile == 3) {
+    for (int k = 0; k < K; k++) {
+      w->cin[k] = conc[IDX(0, k, col, KM, nc)];
+      w->vf[k] = conc[IDX(1, k, col, KM, nc)];
+    }
+    zhang_wirtz_factor(m, K, w->dz, w->phi, w->cin, w->vf, w->wt, w->bf);
+    f_T = 1.0;
+    bioturbation = 1.0;
+  }
 
   for (int n = 0; n < N; n++) {
     /* :652-653 */
     for (int k = 0; k < K; k++)
-      w->diff[k] = m->bioturbation * f_T / 86400.0 / 10000.0 *
+      w->diff[k] = bioturbation * f_T / 86400.0 / 10000.0 *
                    (1.0 - w->phi_i[k]) * w->bf[k];
     const double cup = bdys[(size_t)(n + 1) * nc + col];
     const double fup = fluxes[(size_t)n * nc + col];

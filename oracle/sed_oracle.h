@@ -62,6 +62,13 @@ typedef struct {
                              reject if c1 - (1+rcm) c < -atol (0 = reference) */
   long max_attempts;      /* guard on the adaptive loop (reference has none) */
   orc_bgc bgc;
+  /* bioturbation_profile 3 (Zhang & Wirtz 2017, get_rhs :618-645): the
+   * bioturbation factor follows an infauna biomass estimated from the TOC
+   * profile at every get_rhs, replacing biofac, with bioturbation * f_T = 1.
+   * Namelist constants bioturb_* (fabm_sediment_driver.F90:208,226-231). */
+  int bioturbation_profile;
+  double bioturb_k_l, bioturb_L1, bioturb_L2, bioturb_beta, bioturb_b,
+      bioturb_dry_density;
 } orc_model;
 
 typedef struct {

@@ -59,3 +59,27 @@ def decay_case(ncol=4, K=3, lam_dt=8.0, dt=3600.0):
     cs.conc[7] = 0.0   # NO3
     cs.dt = dt
     return cs
+
+
+def zhang_wirtz_factor(cs, conc):
+    """Bioturbation factor of profile 3 (fabm_sediment_driver.F90:624-644),
+    written from the reference's formula in numpy: weighted TOC from the two
+    carbon detritus pools, its dz-weighted column sum over cumdepth (depth of
+    the last layer's upper interface), biomass and beta biomass^b / TOC."""
+    d = cs.driver
+    f1 = 1.0 / 1.2 * 12.01 / d.bioturb_dry_density / 1000.0
+    f2 = 1.0 / 6.0 * 12.01 / d.bioturb_dry_density / 1000.0
+    fac = np.ones((cs.kmax, cs.ncol))
+    for col in range(cs.ncol):
+        K = int(cs.kact[col])
+        if K == 0:
+            continue
+        dz = cs.dz[:K, col]
+        phi = cs.phi[:K, col]
+        wt = f1 * phi / (1 - phi) * conc[0, :K, col] + f2 * phi / (1 - phi) * conc[1, :K, col]
+        avg = np.sum(dz * wt) / np.sum(dz[:K - 1])
+        zc = np.concatenate([[0.0], np.cumsum(dz)])[:K] + 0.5 * dz
+        biomass = (wt * np.exp(zc * 100 * d.bioturb_k_l) * avg /
+                   (d.bioturb_L1 + d.bioturb_L2 * np.exp(zc * 200 * d.bioturb_k_l)))
+        fac[:K, col] = d.bioturb_beta * biomass ** d.bioturb_b / wt
+    return fac

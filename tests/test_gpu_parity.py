@@ -286,3 +286,42 @@ def test_full_size_workload_properties(oracle_mod):
     cols = np.random.default_rng(3).choice(cs.ncol, 256, replace=False)
     e = teacher_forced(oracle_mod, cs, prev, out, cols)
     assert e.max() < FP32_TOL, e
+
+
+def with_profile3(cs):
+    cs = cs.copy()
+    cs.driver.bioturbation_profile = 3
+    return cs
+
+
+@pytest.mark.parametrize("workload", ["plain_cpu_10x10", "uneven"])
+def test_bioturbation_profile3(oracle_mod, workload):
+    """Zhang & Wirtz bioturbation recomputed at every right-hand side.  FP64
+    keeps the reference's operation order but takes CUDA's pow, which may
+    differ from the CPU's in the last bit, so FP64 is compared at 1e-13 per
+    right-hand side and 1e-9 after two steps instead of bit for bit."""
+    if workload == "uneven":   # both depth classes and land
+        cols = np.arange(0, 1024 * 1024, 1024 * 1024 // 200)[:200]
+        cs = with_profile3(synth.make_workload("uneven_1024x1024", cols=cols))
+    else:
+        cs = with_profile3(synth.make_workload(workload))
+    ref, fref, _ = oracle_mod.OracleModel(cs).get_rhs(cs.conc)
+    scale = np.abs(ref).max(axis=(1, 2), keepdims=True)
+    for prec, tol in ((capi.SED_FP64, 1e-13), (capi.SED_FP32, 1e-4)):
+        s = capi.Solver(cs, precision=prec)
+        s.set_forcing()
+        rhs, fl = s.get_rhs(cs.conc)
+        s.close()
+        assert np.max(np.abs(rhs - ref) / scale) < tol, prec
+    out64, _, _, _, _ = run_gpu(cs, 2, precision=capi.SED_FP64)
+    ref2, _, _ = run_oracle(oracle_mod, cs, 2)
+    assert relerr(active(cs, out64), active(cs, ref2)).max() < 1e-9
+    out32, _, _, _, _ = run_gpu(cs, 1, precision=capi.SED_FP32)
+    ref1, _, _ = run_oracle(oracle_mod, cs, 1)
+    err = relerr(active(cs, out32), active(cs, ref1))
+    assert err.max() < FP32_TOL, err
+    # the TOC-dependent factor changes the result against the static profile
+    plain = cs.copy()
+    plain.driver.bioturbation_profile = 1
+    static, _, _, _, _ = run_gpu(plain, 2, precision=capi.SED_FP64)
+    assert relerr(active(cs, static), active(cs, out64)).max() > 1e-6

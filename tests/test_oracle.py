@@ -218,3 +218,26 @@ def test_reference_amplifies_one_ulp(oracle_mod):
     om.run(a, nsteps=24, percol=True)
     om.run(b, nsteps=24, percol=True)
     assert relerr(a, b).max() > 1e-6
+
+
+def test_bioturbation_profile3_matches_formula(oracle_mod):
+    """Profile 3 equals the static profile whose factor is the Zhang & Wirtz
+    formula evaluated on the same state, with bioturbation = f_T = 1 (the
+    reference sets both to one, get_rhs :622-623; at T = 15 C the static
+    path's f_T is exactly one)."""
+    from cases import zhang_wirtz_factor
+    cs = synth.make_workload("plain_cpu_10x10")
+    cs.bdys[0] = 15.0
+    b3 = cs.copy()
+    b3.driver.bioturbation_profile = 3
+    r3, f3, _ = oracle_mod.OracleModel(b3).get_rhs(cs.conc)
+    st = cs.copy()
+    st.biofac = zhang_wirtz_factor(cs, cs.conc)
+    st.driver.bioturbation = 1.0
+    rs, fs, _ = oracle_mod.OracleModel(st).get_rhs(cs.conc)
+    scale = np.abs(rs).max(axis=(1, 2), keepdims=True)
+    assert np.max(np.abs(r3 - rs) / scale) < 1e-12
+    np.testing.assert_allclose(f3, fs, rtol=1e-12, atol=0)
+    # and the factor changes the transport: profile 3 is not the static one
+    r1, _, _ = oracle_mod.OracleModel(cs).get_rhs(cs.conc)
+    assert np.max(np.abs(r3 - r1) / scale) > 1e-6
