@@ -44,7 +44,7 @@ NTR, NCOEF, NFORCE, NDISS = 11, 4, 13, 5
 L2_BYTES = 129 * 1024 * 1024
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_column launch from
 # an ncu capture (profiles/k_column_plain_gpu_256x256.md)
-MEASURED_TRAFFIC = {"plain_gpu_256x256": 157.1e6}
+MEASURED_TRAFFIC = {"plain_gpu_256x256": 163.6e6}
 FALLBACK_HBM_GBS = 6800.0
 
 
