@@ -132,7 +132,7 @@ class ClockSampler:
 
 def cpu_run(cs, warmup: int, steps: int, threads: int):
     """FP64 oracle, per-column cuts, all given host threads: returns
-    (column-steps/s of the timed steps, seconds)."""
+    (column-steps/s of the timed steps, seconds, stats)."""
     import oracle
     om = oracle.OracleModel(cs)
     c = cs.conc.copy()
@@ -152,6 +152,31 @@ def cpu_sample(ncol_full: int, n: int, seed: int, workload: str = WORKLOAD):
     return synth.make_workload(workload, seed=seed, cols=np.unique(cols))
 
 
+def cpu_window(workload: str, seed: int, warmup: int, steps: int, threads: int,
+               max_columns: int, target_s: float = 15.0):
+    """The oracle over the same coupling steps as the GPU run, on an evenly
+    spaced column sample sized (from a 2-columns-per-thread pilot over the
+    same steps) to about target_s seconds of timed CPU work."""
+    from sedgpu import synth
+    full = synth.WORKLOADS[workload]
+    ncol = full["inum"] * full["jnum"]
+    n0 = min(max(2 * threads, 16), max_columns)
+    cs = cpu_sample(ncol, n0, seed, workload)
+    val, secs, st = cpu_run(cs, warmup, steps, threads)
+    n = int(min(max_columns, max(n0, n0 * target_s / max(secs, 1e-3))))
+    if n > 1.5 * n0:
+        cs = cpu_sample(ncol, n, seed, workload)
+        val, secs, st = cpu_run(cs, warmup, steps, threads)
+    sample = (f"{cs.n_active} active of {ncol} columns (evenly spaced), coupling steps "
+              f"{warmup + 1}..{warmup + steps}, {secs:.1f} s")
+    return {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": sample, "seconds": secs}
+
+
+def days(step0: int, step1: int, dt: float) -> str:
+    return f"{step0 * dt / 86400.0:.3f}..{step1 * dt / 86400.0:.3f}"
+
+
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -159,24 +184,21 @@ def run_reference(args) -> None:
     import oracle
     oracle.build()
     from sedgpu import synth
-    full = synth.WORKLOADS[args.workload]
-    ncol = full["inum"] * full["jnum"]
+    full = synth.make_workload(args.workload, cols=np.arange(1))
+    steps = args.steps or full.nsteps
     threads = os.cpu_count() or 1
-    cs = cpu_sample(ncol, args.cpu_columns, args.seed, args.workload)
-    val, secs, st = cpu_run(cs, args.warmup, args.steps, threads)
+    cpu = cpu_window(args.workload, args.seed, args.warmup, steps, threads, args.cpu_columns)
+    val = cpu["value"]
     line = {
         "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": secs * 1e3 / args.steps, "higher_is_better": True,
+        "steps": steps, "warmup": args.warmup,
+        "ms_per_step": cpu["seconds"] * 1e3 / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
         "data": "synthetic (seeded)", "impl": "reference",
-        "config": {"workload": args.workload, "columns_sampled": cs.n_active,
-                   "layers": cs.kmax, "tracers": NTR, "dt_s": cs.dt,
-                   "method": "adaptive_euler", "cut": "per_column"},
-        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads,
-                         "kind": "port",
-                         "sample": f"{cs.n_active} of {ncol} columns, steps "
-                                   f"{args.warmup + 1}..{args.warmup + args.steps}"},
+        "config": {"workload": args.workload, "tracers": NTR, "dt_s": full.dt,
+                   "method": "adaptive_euler", "cut": "per_column",
+                   "simulated_days_timed": days(args.warmup, args.warmup + steps, full.dt)},
+        "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "note": ("reference algorithm as the FP64 C restatement on the host "
@@ -206,10 +228,12 @@ def run_surrogate(args) -> None:
                     log_every=max(1, args.sur_train_steps // 5))
     t_train = time.perf_counter() - t0
     cs = synth.make_workload(args.workload)
+    steps = args.steps or 24
+    spin = max(args.warmup, 48)   # compare in the developed regime (day 2 on)
     base = capi.Solver(cs)
     base.set_forcing()
     base.set_state(cs.conc)
-    base.step(args.warmup)
+    base.step(spin)
     S0 = base.get_state()
     res = {}
     for mode in ("plain", "surrogate"):
@@ -217,16 +241,16 @@ def run_surrogate(args) -> None:
         s.set_forcing()
         s.set_state(S0)
         if mode == "plain":
-            st = s.step(args.steps)
+            st = s.step(steps)
         else:
-            st = S.step_surrogate(s, sur, args.steps, tol=args.sur_tol)
+            st = S.step_surrogate(s, sur, steps, tol=args.sur_tol)
         res[mode] = (st, s.get_state())
         s.close()
     base.close()
     plain_st, plain_state = res["plain"]
     sur_st, sur_state = res["surrogate"]
-    v_plain = cs.n_active * args.steps / (plain_st["device_ms"] / 1e3)
-    v_sur = cs.n_active * args.steps / (sur_st["device_ms"] / 1e3)
+    v_plain = cs.n_active * steps / (plain_st["device_ms"] / 1e3)
+    v_sur = cs.n_active * steps / (sur_st["device_ms"] / 1e3)
     act = np.arange(cs.kmax)[:, None] < cs.kact[None, :]
     errs = []
     for n in range(NTR):
@@ -235,8 +259,8 @@ def run_surrogate(args) -> None:
         errs.append(float(np.max(np.abs(x - r) / (np.abs(r) + floor))))
     line = {
         "metric": METRIC, "value": v_sur, "unit": UNIT, "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": sur_st["device_ms"] / args.steps, "higher_is_better": True,
+        "steps": steps, "warmup": spin,
+        "ms_per_step": sur_st["device_ms"] / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32+bf16",
         "data": "synthetic (seeded)",
         "config": {"workload": args.workload, "columns": cs.n_active,
@@ -253,6 +277,56 @@ def run_surrogate(args) -> None:
         "gpu_launches": sur_st["gpu_launches"],
     }
     print(json.dumps(line), flush=True)
+
+
+def coupled_e2e(s, cs, warmup, nsteps, world):
+    """Coupling steps with the state resident on the device: each step takes
+    the pelagic fields at the soil surface in (sed_set_boundary), steps, and
+    returns the surface fluxes (sed_get_fluxes), all on pinned host arrays.
+    The particulate fields reproduce the workload's deposition fluxes
+    (fluxes = -surface * velocity at a settling velocity of 1e-5 m/s)."""
+    import ctypes
+    from sedgpu import capi
+    T = np.array(cs.bdys[0], dtype=np.float64, copy=True)
+    surface = np.zeros((NTR, cs.ncol))
+    velocity = np.zeros((NTR, cs.ncol))
+    velocity[:6] = -1e-5
+    surface[:6] = cs.fluxes[:6] / 1e-5
+    surface[6:] = cs.bdys[7:]
+    fl = np.zeros((NTR, cs.ncol))
+    for a in (T, surface, velocity, fl):
+        capi.host_register(a)
+    s.set_state(cs.conc)
+    dp = ctypes.POINTER(ctypes.c_double)
+    args = [a.ctypes.data_as(dp) for a in (T, surface, velocity)]
+    st = capi.SedStats()
+    lib = s.lib
+    parts = {"sed_set_boundary": [], "sed_step": [], "sed_get_fluxes": []}
+    def one():
+        t = time.perf_counter()
+        s._check(lib.sed_set_boundary(s.h, *args, None), "sed_set_boundary")
+        t1 = time.perf_counter()
+        s._check(lib.sed_step(s.h, float(cs.dt), 2, 1, ctypes.byref(st)), "sed_step")
+        t2 = time.perf_counter()
+        s._check(lib.sed_get_fluxes(s.h, fl.ctypes.data_as(dp)), "sed_get_fluxes")
+        t3 = time.perf_counter()
+        for k, v in zip(parts, (t1 - t, t2 - t1, t3 - t2)):
+            parts[k].append(v)
+    for _ in range(warmup):
+        one()
+    for v in parts.values():
+        v.clear()
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        one()
+    sec = time.perf_counter() - t0
+    for a in (T, surface, velocity, fl):
+        capi.host_unregister(a)
+    return {"value": world * cs.n_active * nsteps / sec, "unit": UNIT,
+            "h2d_bytes_per_step": int(T.nbytes + surface.nbytes + velocity.nbytes),
+            "d2h_bytes_per_step": int(fl.nbytes), "steps": nsteps,
+            "calls": "sed_set_boundary + sed_step + sed_get_fluxes (state on the device)",
+            "ms_per_call": {k: round(1e3 * statistics.median(v), 3) for k, v in parts.items()}}
 
 
 def run_gpu(args) -> None:
@@ -275,15 +349,19 @@ def run_gpu(args) -> None:
     s.set_state(cs.conc)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
 
-    # launch tuning chosen by the library's autotuner on the warmed-up state
-    # (untimed; it restores the state it found), then the warm-up steps
+    steps = args.steps or cs.nsteps   # default: the configured run
+    # launch tuning chosen by the library's autotuner on a developed state
+    # (two simulated days in; the reference algorithm's substep count grows
+    # ~10x over the first days), untimed; the timed run then starts from the
+    # configured initial state
     tuning = None
     if args.tuning:
         tc0, tc1, th0, th1 = (int(v) for v in args.tuning.split(","))
         s.set_tuning(tile_columns=(tc0, tc1), threads=(th0, th1))
     elif not args.no_autotune:
-        s.step(1)
+        s.step(min(48, steps))
         tuning = s.autotune(flags=0 if args.no_e2e else capi.SED_TUNE_PIPELINE)
+    s.set_state(cs.conc)
     for _ in range(args.warmup):
         s.step(1)
 
@@ -298,7 +376,7 @@ def run_gpu(args) -> None:
     att = acc = 0
     max_att = 0
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         flush.zero_()            # L2 flush between timed steps
         torch.cuda.synchronize()
         st = s.step(1)
@@ -316,8 +394,8 @@ def run_gpu(args) -> None:
         dev_ms = float(t.item())
         dist.barrier()
     clk = clocks.stop()
-    ms_per_step = dev_ms / args.steps
-    value = world * cs.n_active * args.steps / (dev_ms / 1e3)
+    ms_per_step = dev_ms / steps
+    value = world * cs.n_active * steps / (dev_ms / 1e3)
 
     # accuracy: one FP32 coupling step against the FP64 device path (which
     # reproduces the FP64 CPU restatement bit for bit) from the same state,
@@ -358,16 +436,19 @@ def run_gpu(args) -> None:
     drift_P = float(np.max(np.abs(bud[1][act]) / bud[0][act]))
     drift_N = float(np.max(np.abs(bud[3][act]) / bud[2][act]))
 
-    # end-to-end through the drop-in call on pinned FP64 host arrays
+    # end-to-end through the drop-in call on pinned FP64 host arrays, over
+    # the same coupling steps as the device run (from the initial state)
     e2e = None
+    coupled = None
     if not args.no_e2e:
-        conc = s.get_state()
-        fluxes = s.fluxes()
-        bdys = np.ascontiguousarray(cs.bdys)
+        n_e2e = args.e2e_steps or steps
+        conc = np.array(cs.conc, dtype=np.float64, copy=True)
+        fluxes = np.array(cs.fluxes, dtype=np.float64, copy=True)
+        bdys = np.array(cs.bdys, dtype=np.float64, copy=True)
         for a in (conc, fluxes, bdys):
             capi.host_register(a)
-        n_e2e = max(1, min(args.steps, args.e2e_steps))
-        s.ode_solver(conc, bdys, fluxes, cs.dt)  # warm the graph
+        for _ in range(args.warmup):
+            s.ode_solver(conc, bdys, fluxes, cs.dt)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         for _ in range(n_e2e):
@@ -379,7 +460,10 @@ def run_gpu(args) -> None:
         d2h = conc.nbytes + fluxes.nbytes
         e2e = {"value": world * cs.n_active * n_e2e / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-               "steps": n_e2e, "call": "sed_ode_solver"}
+               "steps": n_e2e, "call": "sed_ode_solver",
+               "simulated_days_timed": days(args.warmup, args.warmup + n_e2e, cs.dt)}
+        coupled = coupled_e2e(s, cs, args.warmup, n_e2e, world)
+
     t_now = s.tuning().as_dict()
     s_tuning = {k: t_now[k] for k in ("tile_columns", "threads", "pipeline_chunks",
                                        "segments")}
@@ -407,17 +491,13 @@ def run_gpu(args) -> None:
 
     cpu = None
     if not args.no_cpu:
-        threads = os.cpu_count() or 1
-        sample = cpu_sample(cs.ncol, args.cpu_columns, args.seed, args.workload)
-        val, secs, _ = cpu_run(sample, args.warmup, args.steps, threads)
-        cpu = {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{sample.n_active} of {cs.ncol} columns, coupling "
-                         f"steps {args.warmup + 1}..{args.warmup + args.steps} "
-                         f"({secs:.1f} s)"}
+        cpu = cpu_window(args.workload, args.seed, args.warmup, steps, os.cpu_count() or 1,
+                         args.cpu_columns)
+        cpu.pop("seconds")
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32", "data": "synthetic (seeded)",
         "config": {"workload": args.workload, "columns": cs.n_active,
@@ -428,6 +508,9 @@ def run_gpu(args) -> None:
                    "method": "adaptive_euler", "cut": "per_column",
                    "state": "fp32", "budgets": "fp64",
                    "l2": "flushed between timed steps",
+                   "simulated_days_timed": days(args.warmup, args.warmup + steps, cs.dt),
+                   "window": ("the configured run" if steps == cs.nsteps else
+                              f"the first {steps} coupling steps"),
                    "solver": "plain",
                    "tuning": s_tuning},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
@@ -444,7 +527,7 @@ def run_gpu(args) -> None:
                      "max_attempts": max_att},
         "budget_drift": {"P": drift_P, "N": drift_N},
         "accuracy": accuracy,
-        "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches,
+        "e2e": e2e, "e2e_coupled": coupled, "cpu_baseline": cpu, "gpu_launches": launches,
         "clocks": clk, "wall_s": wall,
     }
     print(json.dumps(line), flush=True)
@@ -455,13 +538,15 @@ def run_gpu(args) -> None:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=0,
+                    help="coupling steps timed (default: the workload's configured run)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--cpu-columns", type=int, default=8192)
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=0,
+                    help="steps of the end-to-end legs (default: --steps)")
     ap.add_argument("--acc-columns", type=int, default=4096)
     ap.add_argument("--solver", default="plain", choices=["plain", "surrogate"])
     ap.add_argument("--sur-tol", type=float, default=1e-3)

@@ -139,6 +139,32 @@ int sed_set_grid(sed_handle *h, const double *dz, const double *dzc,
  * (fabm_sediment_component.F90:1865-2030): bdys[0] is temperature. */
 int sed_set_forcing(sed_handle *h, const double *bdys, const double *fluxes);
 
+/* Boundary conditions assembled on the device from the pelagic fields at the
+ * soil surface, as get_boundary_conditions does each coupling step
+ * (fabm_sediment_component.F90:1865-2030), so a device-resident state needs
+ * no host round trip:
+ *   temperature[ncol]    -> bdys[0]
+ *   surface[ntr][ncol]   pelagic concentration of each tracer at the soil
+ *                        surface (`<name>_at_soil_surface`)
+ *   velocity[ntr][ncol]  its vertical velocity, m/s, negative downward
+ *                        (`<name>_z_velocity_at_soil_surface`); read for
+ *                        particulate tracers only, may be NULL if none is
+ *                        present
+ *   present[ntr]         nonzero where the import state holds the tracer
+ *                        (NULL: all); absent tracers keep their values
+ * Particulate: fluxes[n] = -surface * velocity (:1978,1986).  Dissolved:
+ * bdys[n+1] = surface, fluxes[n] = the diffusive estimate of :2012-2014 from
+ * the state's first layer when bcup_dissolved is 1 (needs the state; 0 for
+ * land columns), else 0.  Then the step's forcing rows are formed, as
+ * sed_set_forcing does. */
+int sed_set_boundary(sed_handle *h, const double *temperature,
+                     const double *surface, const double *velocity,
+                     const int *present);
+/* The handle's current bdys [ntr+1][ncol] and fluxes [ntr][ncol] (either
+ * may be NULL).  After a step the dissolved rows of fluxes hold that step's
+ * surface fluxes, as get_rhs writes them (:692). */
+int sed_get_boundary(sed_handle *h, double *bdys, double *fluxes);
+
 int sed_set_state(sed_handle *h, const double *conc);
 int sed_get_state(sed_handle *h, double *conc);
 

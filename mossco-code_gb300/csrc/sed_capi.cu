@@ -48,9 +48,11 @@ struct Bin {
   int lpl = 1;
   int slot0 = 0, nslots = 0;       // slot range of the class
   int segb[kMaxSeg + 1] = {};      // segment s = slots [segb[s], segb[s+1])
-  int tc = 32, threads = 256;      // tile width, threads per block
+  int tc = 32, threads = 256;      // tile width (0: warp-direct), threads per block
   int bps = 0;                     // blocks per SM asked for (0 = all that fit)
   int occ = 0;                     // blocks per SM that fit at (tc, threads)
+  int occ_tile = 0;                // warp-direct classes: the 32-column tile
+                                   // kernel that serves the other kinds
   int tk0 = 0;                     // first tile of the class in tile_k
   int blocks(int sms, int ntiles) const {
     const int per = (bps > 0 && bps < occ) ? bps : occ;
@@ -105,7 +107,8 @@ struct sed_handle {
   // device buffers
   DevBuf d_slot_col, d_kact, d_tile_k, d_conc, d_coef, d_cap, d_force, d_sflux,
       d_budget, d_nsub, d_queue, d_stats, d_flag, d_stage, d_bdys, d_fluxes,
-      d_rhs, d_rhs_stage, d_grid, d_force64, d_prop, d_skip, d_xfeat, d_yhat, d_backup;
+      d_rhs, d_rhs_stage, d_grid, d_force64, d_prop, d_skip, d_xfeat, d_yhat, d_backup,
+      d_col_slot, d_top, d_bcin;
   std::vector<double> force64;  // host forcing rows (FP64 state)
   DevStats* h_stats = nullptr;  // pinned
   int* h_flag = nullptr;        // pinned
@@ -188,7 +191,7 @@ ColumnArgs<real> column_args(sed_handle* h, const Bin& b, int bin_index,
   a.tc = b.tc;
   a.slot0 = b.slot0;
   a.tile0 = b.tk0;
-  a.ntiles = b.nslots / b.tc;
+  a.ntiles = b.tc ? b.nslots / b.tc : b.nslots;
   a.dt = dt;
   a.method = method;
   return a;
@@ -198,9 +201,33 @@ ColumnArgs<real> column_args(sed_handle* h, const Bin& b, int bin_index,
 template <typename real>
 void restrict_args(ColumnArgs<real>& a, const Bin& b, int s0, int s1, unsigned* queue) {
   a.slot0 = s0;
-  a.tile0 = b.tk0 + (s0 - b.slot0) / b.tc;
-  a.ntiles = (s1 - s0) / b.tc;
+  a.tile0 = b.tc ? b.tk0 + (s0 - b.slot0) / b.tc : 0;
+  a.ntiles = b.tc ? (s1 - s0) / b.tc : s1 - s0;
   a.queue = queue;
+}
+
+// Launch one class's kernel over a's slot range.  Warp-direct classes
+// (tc 0, FP32) step with k_column_warp; their other kinds (rhs, residual) use
+// the tile kernel with 32-column tiles staging every layer of the class.
+template <typename real>
+cudaError_t launch_bin(sed_handle* h, ColumnArgs<real> a, const Params<real>& p,
+                       const Bin& bin, int kind, cudaStream_t st) {
+  const bool bc4 = h->prm.bcup_particulate == 4;
+  if (bin.tc == 0) {
+    if constexpr (std::is_same<real, float>::value) {
+      if (kind == KIND_ADAPT || kind == KIND_FIXED)
+        return launch_column_warp(a, p, bin.lpl, bc4, kind, bin.blocks(h->sms, a.ntiles),
+                                  bin.threads, st);
+    }
+    a.tc = 32;
+    a.tile_k = nullptr;
+    a.tile0 = 0;
+    a.ntiles /= 32;
+    const int blocks = std::max(1, std::min(a.ntiles, bin.occ_tile * h->sms));
+    return launch_column<real>(a, p, bin.lpl, bc4, kind, blocks, bin.threads, st);
+  }
+  return launch_column<real>(a, p, bin.lpl, bc4, kind, bin.blocks(h->sms, a.ntiles),
+                             bin.threads, st);
 }
 
 // Enqueue the tile kernels of every depth class (one coupling step, or one
@@ -214,9 +241,7 @@ int enqueue_columns(sed_handle* h, double dt, int method, int kind) {
     const Bin& bin = h->bins[b];
     if (bin.nslots == 0) continue;
     ColumnArgs<real> a = column_args<real>(h, bin, b, dt, method);
-    CK(launch_column<real>(a, p, bin.lpl, h->prm.bcup_particulate == 4, kind,
-                           bin.blocks(h->sms, a.ntiles), bin.threads, h->stream),
-       "column kernel launch");
+    CK(launch_bin<real>(h, a, p, bin, kind, h->stream), "column kernel launch");
     h->launches++;
   }
   return SED_OK;
@@ -490,6 +515,16 @@ int apply_tuning(sed_handle* h) {
     bin.tk0 = (int)tile_k.size();
     bin.occ = 0;
     if (bin.nslots == 0) continue;
+    if (bin.tc == 0) {
+      if (h->fp64()) return h->fail(SED_E_ARG, "the warp-direct kernel (tile width 0) is FP32");
+      const bool bc4 = h->prm.bcup_particulate == 4, bio3 = h->prm.bioturbation_profile == 3;
+      bin.occ = std::min(column_warp_blocks_per_sm(bin.lpl, bc4, KIND_ADAPT, bin.threads, bio3),
+                         column_warp_blocks_per_sm(bin.lpl, bc4, KIND_FIXED, bin.threads, bio3));
+      bin.occ_tile = class_occupancy(h, bin, 32, bin.threads);
+      if (bin.occ <= 0 || bin.occ_tile <= 0)
+        return h->fail(SED_E_CUDA, "warp-direct kernel of %d threads does not fit", bin.threads);
+      continue;
+    }
     bin.occ = class_occupancy(h, bin, bin.tc, bin.threads);
     if (bin.occ <= 0)
       return h->fail(SED_E_CUDA, "tile of %d columns x %d layers does not fit on the device",
@@ -572,8 +607,7 @@ int ode_solver_pipelined(sed_handle* h, double* conc, double dt, int method) {
          "gather launch");
       ColumnArgs<real> a = column_args<real>(h, bin, b, dt, method);
       restrict_args(a, bin, sl0, sl1, q + 2 + 2 * c + b);
-      CK(launch_column<real>(a, p, bin.lpl, bc4, kind, bin.blocks(h->sms, a.ntiles),
-                             bin.threads, cs), "column kernel launch");
+      CK(launch_bin<real>(h, a, p, bin, kind, cs), "column kernel launch");
       CK(launch_scatter_range<real>(h->d_conc.as<real>(), stage, h->d_slot_col.as<int>(),
                                     h->d_kact.as<int>(), NTR, h->kmax, h->ncol, h->nslot,
                                     sl0, sl1 - sl0, h->sms, cs), "scatter launch");
@@ -671,9 +705,7 @@ int time_step(sed_handle* h, int b, double dt, int method, int reps, float* best
       const Bin& bin = h->bins[b];
       CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
       ColumnArgs<real> a = column_args<real>(h, bin, b, dt, method);
-      CK(launch_column<real>(a, p, bin.lpl, h->prm.bcup_particulate == 4, kind,
-                             bin.blocks(h->sms, a.ntiles), bin.threads, h->stream),
-         "autotune launch");
+      CK(launch_bin<real>(h, a, p, bin, kind, h->stream), "autotune launch");
     } else {
       rc = step_any<real>(h, dt, method);
       if (rc) return rc;
@@ -692,7 +724,7 @@ int autotune_t(sed_handle* h, double dt, int method, int flags, sed_tuning* out)
   int rc = save_state(h, false);
   if (rc) return rc;
   int trials = 0;
-  const int tcs[] = {8, 16, 32, 64};
+  const int tcs[] = {0, 8, 16, 32, 64};
   const int thr[] = {64, 128, 256};
   for (int b = 0; b < 2; b++) {
     Bin& bin = h->bins[b];
@@ -701,8 +733,11 @@ int autotune_t(sed_handle* h, double dt, int method, int flags, sed_tuning* out)
     float best_ms = 1e30f;
     for (int tc : tcs)
       for (int th : thr) {
-        const int occ = class_occupancy(h, bin, tc, th);
-        if (occ <= 0 || bin.nslots < tc) continue;
+        if (tc == 0 && h->fp64()) continue;
+        if (tc > 0) {
+          const int occ = class_occupancy(h, bin, tc, th);
+          if (occ <= 0 || bin.nslots < tc) continue;
+        }
         bin.tc = tc;
         bin.threads = th;
         bin.bps = 0;
@@ -899,6 +934,9 @@ int sed_create(const sed_params* p, int inum, int jnum, int kmax, int ntr,
     CK(h->d_stage.alloc((size_t)NTR * kmax * ncol * sizeof(double)), "state staging");
     CK(h->d_bdys.alloc((size_t)(NTR + 1) * ncol * sizeof(double)), "bdys");
     CK(h->d_fluxes.alloc((size_t)NTR * ncol * sizeof(double)), "fluxes");
+    // tracers a boundary assembly does not set keep these values
+    CK(cudaMemset(h->d_bdys.p, 0, (size_t)(NTR + 1) * ncol * sizeof(double)), "bdys clear");
+    CK(cudaMemset(h->d_fluxes.p, 0, (size_t)NTR * ncol * sizeof(double)), "fluxes clear");
   }
   *out = h.release();
   return SED_OK;
@@ -1015,6 +1053,22 @@ int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
                      cudaMemcpyHostToDevice, h->stream), "slot map copy");
   CK(cudaMemcpyAsync(h->d_kact.p, h->slot_k.data(), ns * sizeof(int),
                      cudaMemcpyHostToDevice, h->stream), "kact copy");
+  // column -> slot map and FP64 dz(1), porosity(1) per column, for the
+  // boundary assembly's flux estimate
+  {
+    std::vector<int> col_slot(ncol, -1);
+    for (size_t i = 0; i < ns; i++)
+      if (h->slot_col[i] >= 0) col_slot[h->slot_col[i]] = (int)i;
+    std::vector<double> top(2 * (size_t)ncol);
+    for (int c = 0; c < ncol; c++) { top[c] = dz[c]; top[(size_t)ncol + c] = phi[c]; }
+    CK(h->d_col_slot.alloc((size_t)ncol * sizeof(int)), "column map");
+    CK(h->d_top.alloc(2 * (size_t)ncol * sizeof(double)), "surface layer");
+    CK(cudaMemcpyAsync(h->d_col_slot.p, col_slot.data(), (size_t)ncol * sizeof(int),
+                       cudaMemcpyHostToDevice, h->stream), "column map copy");
+    CK(cudaMemcpyAsync(h->d_top.p, top.data(), 2 * (size_t)ncol * sizeof(double),
+                       cudaMemcpyHostToDevice, h->stream), "surface layer copy");
+    CK(cudaStreamSynchronize(h->stream), "column map");
+  }
   CK(h->d_tile_k.alloc((size_t)(h->nslot / 8 + 1) * sizeof(int)), "tile_k");
   {
     int rc = apply_tuning(h);
@@ -1250,11 +1304,16 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
         a.skip = h->d_skip.as<int>();
         a.res_tol = tol;
         a.res_atol = res_atol;
-        int blocks = bin.blocks(h->sms, a.ntiles);
-        if (kind == KIND_RESID) {
+        if (kind == KIND_ADAPT) {
+          CK(launch_bin<float>(h, a, p, bin, kind, h->stream), "surrogate step launch");
+          h->launches++;
+          continue;
+        }
+        int blocks = 1;
+        {
           // two states per tile: the widest tile up to the class's that fits,
           // staging every layer of the class
-          int tc = bin.tc, occ = 0;
+          int tc = bin.tc ? bin.tc : 32, occ = 0;
           for (; tc >= 8; tc /= 2)
             if ((occ = column_blocks_per_sm<float>(tc, bin.lpl, bc4, kind, bin.threads,
                                                    p.bio3 != 0)) > 0)
@@ -1360,6 +1419,81 @@ int sed_set_stream(sed_handle* h, void* stream) {
   return SED_OK;
 }
 
+int sed_set_boundary(sed_handle* h, const double* temperature, const double* surface,
+                     const double* velocity, const int* present) {
+  if (!h) return SED_E_ARG;
+  if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
+  if (!temperature || !surface)
+    return h->fail(SED_E_ARG, "temperature and surface are required");
+  unsigned mask = 0;
+  for (int n = 0; n < NTR; n++)
+    if (!present || present[n]) mask |= 1u << n;
+  const unsigned part = (1u << NPART) - 1u;
+  if ((mask & part) && !velocity)
+    return h->fail(SED_E_ARG, "velocity is required for the particulate tracers present");
+  if (h->prm.bcup_dissolved == 1 && (mask & ~part) && !h->have_state)
+    return h->fail(SED_E_STATE, "the dissolved flux estimate needs the state: call "
+                                "sed_set_state first");
+  CK(cudaSetDevice(h->device), "set device");
+  const size_t nc = (size_t)h->ncol;
+  CK(h->d_bcin.alloc((1 + 2 * (size_t)NTR) * nc * sizeof(double)), "boundary staging");
+  double* bt = h->d_bcin.as<double>();
+  double* bs = bt + nc;
+  double* bv = bs + (size_t)NTR * nc;
+  CK(cudaMemcpyAsync(bt, temperature, nc * sizeof(double), cudaMemcpyHostToDevice, h->stream),
+     "temperature copy");
+  CK(cudaMemcpyAsync(bs, surface, (size_t)NTR * nc * sizeof(double), cudaMemcpyHostToDevice,
+                     h->stream), "surface copy");
+  if (velocity)
+    CK(cudaMemcpyAsync(bv, velocity, (size_t)NTR * nc * sizeof(double),
+                       cudaMemcpyHostToDevice, h->stream), "velocity copy");
+  cudaError_t e =
+      h->fp64()
+          ? launch_assemble_bc<double>(bt, bs, bv, mask, h->d_conc.as<double>(),
+                                       h->d_col_slot.as<int>(), h->d_top.as<double>(),
+                                       h->d_bdys.as<double>(), h->d_fluxes.as<double>(), h->ncol,
+                                       h->nslot, h->kmax, h->prm.bcup_dissolved,
+                                       h->prm.bioturbation, h->prm.diffusivity, h->sms, h->stream)
+          : launch_assemble_bc<float>(bt, bs, bv, mask, h->d_conc.as<float>(),
+                                      h->d_col_slot.as<int>(), h->d_top.as<double>(),
+                                      h->d_bdys.as<double>(), h->d_fluxes.as<double>(), h->ncol,
+                                      h->nslot, h->kmax, h->prm.bcup_dissolved,
+                                      h->prm.bioturbation, h->prm.diffusivity, h->sms, h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "boundary assembly launch");
+  h->launches++;
+  int rc;
+  if (h->fp64()) {
+    // the FP64 forcing rows use the host's exp (see prep_force_host64)
+    std::vector<double> hb((size_t)(NTR + 1) * nc), hf((size_t)NTR * nc);
+    CK(cudaMemcpyAsync(hb.data(), h->d_bdys.p, hb.size() * sizeof(double),
+                       cudaMemcpyDeviceToHost, h->stream), "bdys copy back");
+    CK(cudaMemcpyAsync(hf.data(), h->d_fluxes.p, hf.size() * sizeof(double),
+                       cudaMemcpyDeviceToHost, h->stream), "fluxes copy back");
+    CK(cudaStreamSynchronize(h->stream), "boundary assembly");
+    rc = prep_force_host64(h, hb.data(), hf.data());
+  } else {
+    rc = prep_force<float>(h);
+  }
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(h->stream), "boundary assembly");
+  h->have_forcing = true;
+  return SED_OK;
+}
+
+int sed_get_boundary(sed_handle* h, double* bdys, double* fluxes) {
+  if (!h) return SED_E_ARG;
+  if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
+  CK(cudaSetDevice(h->device), "set device");
+  if (bdys)
+    CK(cudaMemcpyAsync(bdys, h->d_bdys.p, (size_t)(NTR + 1) * h->ncol * sizeof(double),
+                       cudaMemcpyDeviceToHost, h->stream), "bdys copy back");
+  if (fluxes)
+    CK(cudaMemcpyAsync(fluxes, h->d_fluxes.p, (size_t)NTR * h->ncol * sizeof(double),
+                       cudaMemcpyDeviceToHost, h->stream), "fluxes copy back");
+  CK(cudaStreamSynchronize(h->stream), "get_boundary");
+  return SED_OK;
+}
+
 int sed_get_tuning(const sed_handle* h, sed_tuning* t) {
   if (!h || !t) return SED_E_ARG;
   memset(t, 0, sizeof *t);
@@ -1379,8 +1513,10 @@ int sed_set_tuning(sed_handle* h, const sed_tuning* t) {
   if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
   for (int b = 0; b < 2; b++) {
     const int tc = t->tile_columns[b], th = t->threads[b];
-    if (tc != 8 && tc != 16 && tc != 32 && tc != 64)
-      return h->fail(SED_E_ARG, "tile_columns[%d]=%d: 8, 16, 32 or 64", b, tc);
+    if (tc != 0 && tc != 8 && tc != 16 && tc != 32 && tc != 64)
+      return h->fail(SED_E_ARG, "tile_columns[%d]=%d: 0 (warp-direct), 8, 16, 32 or 64", b, tc);
+    if (tc == 0 && h->fp64())
+      return h->fail(SED_E_ARG, "tile_columns[%d]=0: the warp-direct kernel is FP32", b);
     if (th < 64 || th > 256 || th % 64 != 0)
       return h->fail(SED_E_ARG, "threads[%d]=%d: 64, 128, 192 or 256", b, th);
     if (t->blocks_per_sm[b] < 0) return h->fail(SED_E_ARG, "blocks_per_sm[%d] < 0", b);

@@ -87,6 +87,12 @@ struct DevStats {
 // division helpers: fast reciprocal in FP32, IEEE division in FP64
 __device__ __forceinline__ float sdiv(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ double sdiv(double a, double b) { return a / b; }
+// Explicit fused multiply-add.  The kernels are compiled without automatic
+// contraction, so every FP32 rounding is the one written here, and results
+// do not depend on which kernel (tile or warp-direct, any tuning) inlines
+// the code.
+__device__ __forceinline__ float fm(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fm(double a, double b, double c) { return fma(a, b, c); }
 
 // ---------------------------------------------------------------------------
 // OMEXDIA+P local rates of one cell (per second).  Published OMEXDIA
@@ -118,7 +124,7 @@ __device__ __forceinline__ void omexdia_p(const Params<real>& p,
   const real AnoxicMin = Cmin * anlim;
   const real Nitri = p.rnit * NH4 * sdiv(O2, O2 + p.ksO2nitri);
   const real OduOx = p.rodu * ODU * sdiv(O2, O2 + p.ksO2oduox);
-  const real Rads = sdiv(p.pads * (p.PAdsODU * PO4 - ODU * adsP), p.PAdsODU + ODU);
+  const real Rads = sdiv(p.pads * fm(p.PAdsODU, PO4, -(ODU * adsP)), p.PAdsODU + ODU);
   const real NprodF = p.rF * fdetN;
   const real NprodS = p.rS * sdetN;
   const real Pprod = p.rF * fdetP;
@@ -128,11 +134,11 @@ __device__ __forceinline__ void omexdia_p(const Params<real>& p,
   r[T_SDETN] = -(lim * NprodS);
   r[T_FDETP] = -(lim * Pprod);
   r[T_ADSP] = Rads;
-  r[T_O2] = -OxicMin - real(2) * Nitri - OduOx;
-  r[T_NO3] = Nitri - real(0.8) * Denit;
-  r[T_NH4] = (lim * (NprodF + NprodS) - Nitri) * p.nh3fac;
+  r[T_O2] = fm(real(-2), Nitri, -OxicMin) - OduOx;
+  r[T_NO3] = fm(real(-0.8), Denit, Nitri);
+  r[T_NH4] = fm(lim, NprodF + NprodS, -Nitri) * p.nh3fac;
   r[T_ODU] = AnoxicMin - OduOx;
-  r[T_PO4] = lim * Pprod - Rads;
+  r[T_PO4] = fm(lim, Pprod, -Rads);
   denit = Denit;
 }
 
@@ -209,8 +215,8 @@ __device__ __forceinline__ void bio3_conductances(const Params<real>& p,
   real part = real(0);
 #pragma unroll
   for (int s = 0; s < LPL; s++) {
-    wt[s] = lc.wc[s] * (p.toc_f1 * C[s][T_FDETC] + p.toc_f2 * C[s][T_SDETC]);
-    part += lc.hw[s] * wt[s];
+    wt[s] = lc.wc[s] * fm(p.toc_f1, C[s][T_FDETC], p.toc_f2 * C[s][T_SDETC]);
+    part = fm(lc.hw[s], wt[s], part);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
@@ -276,9 +282,11 @@ __device__ __forceinline__ void column_rhs(const Params<real>& p,
     from_below<real, LPL>(F, Fb, lane);
 #pragma unroll
     for (int s = 0; s < LPL; s++) {
-      real t = (F[s] - (bottom[s] ? real(0) : Fb[s])) * lc.ivol[s];
-      if (BC4 && part) t += lc.src[s][n];
-      R[s][n] += t;
+      const real div = F[s] - (bottom[s] ? real(0) : Fb[s]);
+      if (BC4 && part)
+        R[s][n] = R[s][n] + fm(div, lc.ivol[s], lc.src[s][n]);
+      else
+        R[s][n] = fm(div, lc.ivol[s], R[s][n]);
     }
   }
 }

@@ -151,7 +151,7 @@ __device__ __forceinline__ void load_lane(Lane<real, LPL, BC4>& lc,
       lc.vol[s] = act ? vol : real(0);
       lc.ivol[s] = act ? real(1) / vol : real(0);
       lc.ap[s] = act ? bioT * gb : real(0);
-      lc.ad[s] = act ? bioT * gb + dmul * gm : real(0);
+      lc.ad[s] = act ? fm(bioT, gb, dmul * gm) : real(0);
       if constexpr (BIO3) {
         lc.wc[s] = act ? phi / (real(1) - phi) : real(0);
         lc.gz[s] = act ? row(NCOEF) : real(0);
@@ -760,6 +760,107 @@ k_column(ColumnArgs<real> a, Params<real> p) {
 }
 
 // ---------------------------------------------------------------------------
+// Warp-direct form of the stepping kinds (KIND_ADAPT / KIND_FIXED).  The tile
+// kernel makes a block's warps wait at every tile boundary for the tile's
+// slowest column; once the column profiles develop, substep counts per
+// column spread over two orders of magnitude and those waits dominate.  Here
+// each warp pulls one column at a time from the work counter, loads it
+// straight from global memory (lane = layer; neighbouring warps share the L2
+// sectors of neighbouring slots), steps it and writes it back.  The only
+// shared memory is the warp's copy of its column's 11 surface values; the
+// only block barriers are at entry and exit.
+template <typename real, int LPL, bool BC4, bool BIO3, int KIND>
+__global__ void __launch_bounds__(256, (MinBlocks<real, LPL>::value))
+k_column_warp(ColumnArgs<real> a, Params<real> p) {
+  __shared__ real s_bnd[8][NFORCE];
+  __shared__ unsigned long long b_att, b_acc, b_cols, b_mindt;
+  __shared__ int b_maxatt, b_cap, b_nan;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    b_att = 0; b_acc = 0; b_cols = 0; b_mindt = 0x7FF0000000000000ull;
+    b_maxatt = 0; b_cap = 0; b_nan = 0;
+  }
+  __syncthreads();
+  const size_t ns = (size_t)a.nslot;
+  real* sb = s_bnd[warp];
+  for (;;) {
+    int j = 0;
+    if (lane == 0) j = (int)atomicAdd(a.queue, 1u);
+    j = __shfl_sync(FULL, j, 0);
+    if (j >= a.ntiles) break;
+    const int slot = a.slot0 + (a.order ? a.order[j] : j);
+    const int K = a.kact[slot];
+    const bool skipped = a.skip && K > 0 && a.skip[slot];
+    if (K <= 0 || skipped) {
+      // land or padding: zero outputs; accepted surrogate step: the state
+      // and surface flux are already in place
+      if (lane == 0) {
+        a.nsub[slot] = 0;
+        if (!skipped)
+          for (int d = 0; d < NDISS; d++) a.sflux[d * ns + slot] = real(0);
+        if (a.budget)
+          for (int b = 0; b < 4; b++) a.budget[b * ns + slot] = 0.0;
+      }
+      continue;
+    }
+    if (lane < NFORCE) sb[lane] = a.force[lane * ns + slot];
+    __syncwarp();
+    Lane<real, LPL, BC4> lc;
+    real C[LPL][NTR];
+    // global arrays in load_lane's (row, column) form: rows of kmax layers
+    // per tracer / coefficient, columns of stride nslot; then the surface
+    // values the substeps read come from the warp's shared copy
+    load_lane<real, LPL, BC4, BIO3>(lc, C, a.conc, a.coef, a.cap, a.force, slot, a.kmax,
+                                    (int)ns, lane, K, p.mol_mode);
+    lc.bnd_s = sb + 2;
+    lc.bnd_stride = 1;
+    real ftop[NTR];
+#pragma unroll
+    for (int n = 0; n < NTR; n++) ftop[n] = real(0);
+    double bud[4] = {0.0, 0.0, 0.0, 0.0};
+    ColResult r;
+    if (KIND == KIND_ADAPT)
+      r = p.ticks ? solve_adaptive<real, LPL, BC4, BIO3, true>(p, lc, lane, K, C, ftop, a.dt, bud)
+                  : solve_adaptive<real, LPL, BC4, BIO3, false>(p, lc, lane, K, C, ftop, a.dt, bud);
+    else
+      r = solve_fixed<real, LPL, BC4, BIO3>(p, lc, lane, K, C, ftop, a.dt, a.method, bud);
+#pragma unroll
+    for (int s = 0; s < LPL; s++) {
+      const int L = s * 32 + lane;
+      if (L < K)
+#pragma unroll
+        for (int n = 0; n < NTR; n++) a.conc[((size_t)n * a.kmax + L) * ns + slot] = C[s][n];
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int d = 0; d < NDISS; d++) a.sflux[d * ns + slot] = ftop[NPART + d];
+      a.nsub[slot] = r.attempts;
+      if (a.budget)
+        for (int b = 0; b < 4; b++) a.budget[b * ns + slot] = bud[b];
+      atomicAdd(&b_att, (unsigned long long)r.attempts);
+      atomicAdd(&b_acc, (unsigned long long)r.accepted);
+      atomicAdd(&b_cols, 1ull);
+      atomicMax(&b_maxatt, r.attempts);
+      if (r.capped) atomicAdd(&b_cap, 1);
+      if (r.nan) atomicAdd(&b_nan, r.nan);
+      if (r.accepted > 0)
+        atomicMin(&b_mindt, (unsigned long long)__double_as_longlong(r.min_dt));
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    atomicAdd(&a.stats->attempts, b_att);
+    atomicAdd(&a.stats->accepted, b_acc);
+    atomicAdd(&a.stats->column_steps, b_cols);
+    atomicMin(&a.stats->min_dt_bits, b_mindt);
+    atomicMax(&a.stats->max_col_attempts, b_maxatt);
+    if (b_cap) { atomicAdd(&a.stats->capped, b_cap); atomicOr(&a.stats->status, ST_CAP); }
+    if (b_nan) { atomicAdd(&a.stats->nan_cells, b_nan); atomicOr(&a.stats->status, ST_NAN); }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Grid-wide adaptive cut (the reference's any() over the whole local grid).
 template <typename real>
 __global__ void k_trial(const real* __restrict__ conc, const real* __restrict__ rhs,
@@ -938,6 +1039,45 @@ __global__ void k_prep_grid(const double* __restrict__ dz,
   }
 }
 
+// get_boundary_conditions (fabm_sediment_component.F90:1865-2030) on the
+// device, per column: temperature -> bdys[0]; for every tracer in
+// present_mask, particulate fluxes[n] = -surface * velocity (downward
+// positive, :1978,1986), dissolved bdys[n+1] = surface and fluxes[n] = the
+// diffusive estimate of :2012-2014 (bcup_dissolved 1, from the state's first
+// layer; 0 for land) or 0.  top = [dz(1)][porosity(1)] per column (FP64).
+template <typename real>
+__global__ void k_assemble_bc(const double* __restrict__ temperature,
+                              const double* __restrict__ surface,
+                              const double* __restrict__ velocity, unsigned present_mask,
+                              const real* __restrict__ conc, const int* __restrict__ col_slot,
+                              const double* __restrict__ top, double* __restrict__ bdys,
+                              double* __restrict__ fluxes, int ncol, int nslot, int kmax,
+                              int bcup_d, double bioturbation, double diffusivity) {
+  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < ncol;
+       col += gridDim.x * blockDim.x) {
+    const double T = temperature[col];
+    bdys[col] = T;
+    const int slot = col_slot[col];
+    for (int n = 0; n < NTR; n++) {
+      if (!((present_mask >> n) & 1u)) continue;
+      const size_t i = (size_t)n * ncol + col;
+      if (n < NPART) {
+        fluxes[i] = -surface[i] * velocity[i];
+        continue;
+      }
+      const double cb = surface[i];
+      bdys[(size_t)(n + 1) * ncol + col] = cb;
+      double f = 0.0;
+      if (bcup_d == 1 && slot >= 0) {
+        const double c0 = (double)conc[(size_t)n * kmax * nslot + slot];
+        f = -(c0 - cb) / top[col] * (bioturbation + diffusivity + T * 0.035) *
+            top[(size_t)ncol + col] / 86400.0 / 10000.0;
+      }
+      fluxes[i] = f;
+    }
+  }
+}
+
 // Per-column forcing of one coupling step: bioturbation x f_T (get_rhs :648,
 // :652), the molecular multiplier, and the surface value of every tracer
 // (bottom-water concentration or downward flux, diff3d's Cup / fluxup).
@@ -1023,6 +1163,19 @@ __global__ void k_prep_bio3(const double* __restrict__ dz, const double* __restr
       at(NCOEF + 1) = (real)hw;
     }
   }
+}
+
+template <typename real>
+cudaError_t launch_assemble_bc(const double* temperature, const double* surface,
+                               const double* velocity, unsigned present_mask, const real* conc,
+                               const int* col_slot, const double* top, double* bdys,
+                               double* fluxes, int ncol, int nslot, int kmax, int bcup_d,
+                               double bioturbation, double diffusivity, int sms,
+                               cudaStream_t st) {
+  k_assemble_bc<real><<<grid_for(ncol, 128, sms), 128, 0, st>>>(
+      temperature, surface, velocity, present_mask, conc, col_slot, top, bdys, fluxes, ncol,
+      nslot, kmax, bcup_d, bioturbation, diffusivity);
+  return cudaGetLastError();
 }
 
 template <typename real>
@@ -1123,6 +1276,36 @@ int column_blocks_per_sm(int tc, int lpl, bool bc4, int kind, int threads, bool 
                : occupancy_b<real, 1, false>(tc, kind, threads, bio3);
   return bc4 ? occupancy_b<real, 2, true>(tc, kind, threads, bio3)
              : occupancy_b<real, 2, false>(tc, kind, threads, bio3);
+}
+
+template <int LPL, bool BC4, bool BIO3, int KIND>
+static cudaError_t launch_warp_t(const ColumnArgs<float>& a, const Params<float>& p, int blocks,
+                                 int threads, cudaStream_t st) {
+  k_column_warp<float, LPL, BC4, BIO3, KIND><<<blocks, threads, 0, st>>>(a, p);
+  return cudaGetLastError();
+}
+
+template <int LPL, bool BC4, bool BIO3>
+cudaError_t launch_warp_k(const ColumnArgs<float>& a, const Params<float>& p, int kind,
+                                 int blocks, int threads, cudaStream_t st) {
+  return kind == KIND_FIXED
+             ? launch_warp_t<LPL, BC4, BIO3, KIND_FIXED>(a, p, blocks, threads, st)
+             : launch_warp_t<LPL, BC4, BIO3, KIND_ADAPT>(a, p, blocks, threads, st);
+}
+
+template <int LPL, bool BC4, bool BIO3, int KIND>
+static int warp_occupancy_t(int threads) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &nb, k_column_warp<float, LPL, BC4, BIO3, KIND>, threads, 0) != cudaSuccess)
+    return 0;
+  return nb;
+}
+
+template <int LPL, bool BC4, bool BIO3>
+int warp_occupancy_k(int kind, int threads) {
+  return kind == KIND_FIXED ? warp_occupancy_t<LPL, BC4, BIO3, KIND_FIXED>(threads)
+                            : warp_occupancy_t<LPL, BC4, BIO3, KIND_ADAPT>(threads);
 }
 
 template <typename real>
@@ -1244,6 +1427,21 @@ cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
   prefix template int occupancy_k<real, 2, false, BIO3>(int, int, int);         \
   prefix template int occupancy_k<real, 2, true, BIO3>(int, int, int);
 
+// The warp-direct kernels (FP32) of one profile-3 setting.
+#define SED_WARP_VARIANT(prefix, BIO3)                                          \
+  prefix template cudaError_t launch_warp_k<1, false, BIO3>(                    \
+      const ColumnArgs<float>&, const Params<float>&, int, int, int, cudaStream_t); \
+  prefix template cudaError_t launch_warp_k<1, true, BIO3>(                     \
+      const ColumnArgs<float>&, const Params<float>&, int, int, int, cudaStream_t); \
+  prefix template cudaError_t launch_warp_k<2, false, BIO3>(                    \
+      const ColumnArgs<float>&, const Params<float>&, int, int, int, cudaStream_t); \
+  prefix template cudaError_t launch_warp_k<2, true, BIO3>(                     \
+      const ColumnArgs<float>&, const Params<float>&, int, int, int, cudaStream_t); \
+  prefix template int warp_occupancy_k<1, false, BIO3>(int, int);               \
+  prefix template int warp_occupancy_k<1, true, BIO3>(int, int);                \
+  prefix template int warp_occupancy_k<2, false, BIO3>(int, int);               \
+  prefix template int warp_occupancy_k<2, true, BIO3>(int, int);
+
 #define SED_INSTANTIATE(real)                                                   \
   template size_t tile_smem_bytes<real>(int, int, bool, int, bool);             \
   template cudaError_t launch_column<real>(const ColumnArgs<real>&,             \
@@ -1282,6 +1480,10 @@ cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
                                                const int*, real*, int, int,     \
                                                double, double, int, int, int,   \
                                                int, cudaStream_t);              \
+  template cudaError_t launch_assemble_bc<real>(                                \
+      const double*, const double*, const double*, unsigned, const real*,       \
+      const int*, const double*, double*, double*, int, int, int, int, double,  \
+      double, int, cudaStream_t);                                               \
   template cudaError_t launch_prep_bio3<real>(                                  \
       const double*, const double*, const double*, const double*,               \
       const double*, const double*, const int*, real*, int, int, int, double,   \

@@ -4,4 +4,5 @@
 
 namespace sed {
 SED_VARIANT(, float, true)
+SED_WARP_VARIANT(, true)
 }  // namespace sed

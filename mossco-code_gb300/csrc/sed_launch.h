@@ -38,6 +38,10 @@ struct ColumnArgs {
   // KIND_RESID (out = proposed state, conc = state at the start of the step)
   int* skip;
   double res_tol, res_atol;
+  // warp-direct kernel: optional processing order of the range's slots
+  // (order[j] = offset from slot0 of the j-th column handed out; null: in
+  // slot order)
+  const int* order;
 };
 
 template <typename real>
@@ -50,6 +54,14 @@ cudaError_t launch_column(const ColumnArgs<real>& a, const Params<real>& p,
 
 template <typename real>
 int column_blocks_per_sm(int tc, int lpl, bool bc4, int kind, int threads, bool bio3);
+
+// Warp-direct column kernel (tile width 0 in the tuning; FP32 state, the
+// stepping kinds): every warp pulls single columns from the work counter and
+// reads and writes them in global memory, with no shared tiles and no block
+// barriers.  a.ntiles counts the range's slots.
+cudaError_t launch_column_warp(const ColumnArgs<float>& a, const Params<float>& p, int lpl,
+                               bool bc4, int kind, int blocks, int threads, cudaStream_t st);
+int column_warp_blocks_per_sm(int lpl, bool bc4, int kind, int threads, bool bio3);
 
 template <typename real>
 cudaError_t launch_trial(const real* conc, const real* rhs, const int* kact,
@@ -106,6 +118,15 @@ cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
                               const int* slot_col, real* force, int ncol,
                               int nslot, double bio, double diffusivity,
                               int mode, int bcup_d, int bio3, int sms, cudaStream_t st);
+
+// boundary conditions from the pelagic fields at the soil surface
+template <typename real>
+cudaError_t launch_assemble_bc(const double* temperature, const double* surface,
+                               const double* velocity, unsigned present_mask, const real* conc,
+                               const int* col_slot, const double* top, double* bdys,
+                               double* fluxes, int ncol, int nslot, int kmax, int bcup_d,
+                               double bioturbation, double diffusivity, int sms,
+                               cudaStream_t st);
 
 // coefficient rows of bioturbation profile 3 (after launch_prep_grid)
 template <typename real>

@@ -8,7 +8,8 @@
 // molecular multiplier and the 11 surface values), zero in padded columns.
 // The network predicts the standardised change of log(C + c0) over one
 // coupling step; the proposed state is exp(log(C + c0) + mu_d + sd_d y) - c0,
-// clamped at zero.  Both kernels are 32 x 32 tiled transposes.
+// clamped at zero.  Both kernels are 32 x 32 tiled transposes (slot tiles
+// on blockIdx.x, feature tiles on blockIdx.y).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -24,7 +25,7 @@ __global__ void k_features(const float* __restrict__ conc, const float* __restri
                            const float* __restrict__ norm, int K, int kmax, int nslot,
                            int rows, int nin, int pin, __nv_bfloat16* __restrict__ x) {
   __shared__ float tile[32][33];
-  const int f0 = blockIdx.x * 32, s0 = blockIdx.y * 32;
+  const int f0 = blockIdx.y * 32, s0 = blockIdx.x * 32;
   const float* c0 = norm;
   const float* mu = norm + NTR;
   const float* sd = mu + nin;
@@ -55,7 +56,7 @@ __global__ void k_apply(const float* __restrict__ yhat, const float* __restrict_
                         const float* __restrict__ norm, int K, int kmax, int nslot, int nin,
                         int nout, int pout, float* __restrict__ prop) {
   __shared__ float tile[32][33];
-  const int f0 = blockIdx.x * 32, s0 = blockIdx.y * 32;
+  const int f0 = blockIdx.y * 32, s0 = blockIdx.x * 32;
   const float* c0 = norm;
   const float* mud = norm + NTR + 2 * nin;
   const float* sdd = mud + nout;
@@ -79,14 +80,15 @@ __global__ void k_apply(const float* __restrict__ yhat, const float* __restrict_
 
 cudaError_t features(const float* conc, const float* force, const float* norm, int K, int kmax,
                      int nslot, int rows, int nin, int pin, __nv_bfloat16* x, cudaStream_t st) {
-  dim3 grid((pin + 31) / 32, (rows + 31) / 32);
+  // slots on x (up to 2^31 - 1 blocks), features on y (a few dozen)
+  dim3 grid((rows + 31) / 32, (pin + 31) / 32);
   k_features<<<grid, dim3(32, 8), 0, st>>>(conc, force, norm, K, kmax, nslot, rows, nin, pin, x);
   return cudaGetLastError();
 }
 
 cudaError_t apply(const float* yhat, const float* conc, const float* norm, int K, int kmax,
                   int nslot, int nin, int nout, int pout, float* prop, cudaStream_t st) {
-  dim3 grid((nout + 31) / 32, (nslot + 31) / 32);
+  dim3 grid((nslot + 31) / 32, (nout + 31) / 32);
   k_apply<<<grid, dim3(32, 8), 0, st>>>(yhat, conc, norm, K, kmax, nslot, nin, nout, pout, prop);
   return cudaGetLastError();
 }

@@ -97,6 +97,15 @@ module sed_gpu
       import :: c_int, c_ptr
       type(c_ptr), value :: h, bdys, fluxes
     end function
+    integer(c_int) function sed_set_boundary(h, temperature, surface, velocity, present) &
+        bind(C, name='sed_set_boundary')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, temperature, surface, velocity, present
+    end function
+    integer(c_int) function sed_get_boundary(h, bdys, fluxes) bind(C, name='sed_get_boundary')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, bdys, fluxes
+    end function
     integer(c_int) function sed_host_register(ptr, bytes) bind(C, name='sed_host_register')
       import :: c_int, c_ptr, c_size_t
       type(c_ptr), value :: ptr
@@ -127,7 +136,7 @@ module sed_gpu
 
   public :: sed_default_params, sed_gpu_init, sed_gpu_ode_solver, &
             sed_gpu_get_rhs, sed_gpu_finalize, sed_get_tuning, sed_set_tuning, &
-            sed_autotune
+            sed_autotune, sed_set_boundary, sed_get_boundary
 
 contains
 

@@ -26,8 +26,13 @@ SOURCES = ["sed_kernels_f32.cu", "sed_kernels_f64.cu", "sed_kernels_f32_bio3.cu"
            "sur_capi.cu", "sur_loop.cu"]
 # The FP64 kernels evaluate the reference's arithmetic operation by
 # operation: no multiply-add contraction.
+# The FP32 kernels write every fused multiply-add explicitly (fmaf): without
+# automatic contraction their rounding is the same in every kernel that
+# inlines the code, so results do not depend on the launch tuning.
 EXTRA_FLAGS = {"sed_kernels_f64.cu": ["-fmad=false"],
-               "sed_kernels_f64_bio3.cu": ["-fmad=false"]}
+               "sed_kernels_f64_bio3.cu": ["-fmad=false"],
+               "sed_kernels_f32.cu": ["-fmad=false"],
+               "sed_kernels_f32_bio3.cu": ["-fmad=false"]}
 HEADERS = ["sed_device.cuh", "sed_kernels.cuh", "sed_launch.h", "sed_params.h",
            "sur_kernels.h", "sur_internal.h", "sur_loop.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -111,6 +111,8 @@ SIGNATURES = {
     "sed_set_grid": (ctypes.c_int, [_H, _dp, _dp, _dp, _dp, _dp, _dp, _ip,
                                     _ip]),
     "sed_set_forcing": (ctypes.c_int, [_H, _dp, _dp]),
+    "sed_set_boundary": (ctypes.c_int, [_H, _dp, _dp, _dp, _ip]),
+    "sed_get_boundary": (ctypes.c_int, [_H, _dp, _dp]),
     "sed_set_state": (ctypes.c_int, [_H, _dp]),
     "sed_get_state": (ctypes.c_int, [_H, _dp]),
     "sed_step": (ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int,
@@ -287,6 +289,21 @@ class Solver:
         f = _f64(cs.fluxes if fluxes is None else fluxes)
         self._check(self.lib.sed_set_forcing(self.h, _p(b), _p(f)),
                     "sed_set_forcing")
+
+    def set_boundary(self, temperature, surface, velocity=None, present=None):
+        """get_boundary_conditions on the device from pelagic surface fields."""
+        pr = None if present is None else np.ascontiguousarray(present, dtype=np.int32)
+        self._check(self.lib.sed_set_boundary(
+            self.h, _p(_f64(temperature)), _p(_f64(surface)),
+            None if velocity is None else _p(_f64(velocity)),
+            None if pr is None else _p(pr, _ip)), "sed_set_boundary")
+
+    def boundary(self):
+        cs = self.cs
+        bd = np.zeros((NTR + 1, cs.ncol))
+        fl = np.zeros((NTR, cs.ncol))
+        self._check(self.lib.sed_get_boundary(self.h, _p(bd), _p(fl)), "sed_get_boundary")
+        return bd, fl
 
     def set_state(self, conc):
         c = _f64(conc)

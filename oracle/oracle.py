@@ -120,6 +120,8 @@ def lib():
             ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
             ctypes.c_double, _dp, _dp, _dp, _dp]
         L.orc_bc_flux_estimate.argtypes = [P(Model), _dp, _dp, _dp]
+        L.orc_assemble_bc.argtypes = [P(Model), _dp, _dp, _dp, _dp,
+                                      P(ctypes.c_int), _dp, _dp]
         L.orc_inventory.argtypes = [P(Model), _dp, _dp]
         _lib = L
     return _lib
@@ -201,6 +203,22 @@ class OracleModel:
                            _ptr(fl), float(dt), int(method), int(percol),
                            int(nsteps), int(nthreads), ctypes.byref(st))
         return rc, st.as_dict(), fl
+
+    def assemble_bc(self, conc, temperature, surface, velocity, present=None,
+                    bdys=None, fluxes=None):
+        """get_boundary_conditions on host arrays; returns (bdys, fluxes)."""
+        cs = self.cs
+        bd = np.array(cs.bdys if bdys is None else bdys, dtype=np.float64, copy=True)
+        fl = np.array(cs.fluxes if fluxes is None else fluxes, dtype=np.float64, copy=True)
+        pr = None if present is None else np.ascontiguousarray(present, dtype=np.int32)
+        lib().orc_assemble_bc(
+            ctypes.byref(self.m), _ptr(np.ascontiguousarray(conc, dtype=np.float64)),
+            _ptr(np.ascontiguousarray(temperature, dtype=np.float64)),
+            _ptr(np.ascontiguousarray(surface, dtype=np.float64)),
+            _ptr(np.ascontiguousarray(velocity, dtype=np.float64)),
+            None if pr is None else pr.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+            _ptr(bd), _ptr(fl))
+        return bd, fl
 
     def inventory(self, conc: np.ndarray) -> np.ndarray:
         cs = self.cs

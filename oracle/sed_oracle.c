@@ -665,6 +665,32 @@ void orc_bc_flux_estimate(const orc_model *m, const double *conc,
   }
 }
 
+void orc_assemble_bc(const orc_model *m, const double *conc, const double *temperature,
+                     const double *surface, const double *velocity,
+                     const int *present, double *bdys, double *fluxes) {
+  const size_t nc = (size_t)m->ncol;
+  for (size_t col = 0; col < nc; col++) bdys[col] = temperature[col];
+  for (int n = 0; n < m->ntr; n++) {
+    if (present && !present[n]) continue;
+    for (size_t col = 0; col < nc; col++) {
+      const size_t i = (size_t)n * nc + col;
+      if (m->particulate[n]) {
+        fluxes[i] = -surface[i] * velocity[i];
+        continue;
+      }
+      bdys[(size_t)(n + 1) * nc + col] = surface[i];
+      if (m->bcup_dissolved == 1 && m->kact[col] > 0) {
+        const double T = bdys[col];
+        fluxes[i] = -(conc[IDX(n, 0, col, m->kmax, nc)] - bdys[(size_t)(n + 1) * nc + col]) /
+                    m->dz[col] * (m->bioturbation + m->diffusivity + T * 0.035) *
+                    m->phi[col] / 86400.0 / 10000.0;
+      } else {
+        fluxes[i] = 0.0;
+      }
+    }
+  }
+}
+
 void orc_inventory(const orc_model *m, const double *conc, double *inv) {
   const size_t nc = (size_t)m->ncol;
   for (int n = 0; n < m->ntr; n++)

@@ -144,6 +144,17 @@ int orc_run(const orc_model *m, double *conc, const double *bdys,
 void orc_bc_flux_estimate(const orc_model *m, const double *conc,
                           const double *bdys, double *fluxes);
 
+/* a13: get_boundary_conditions (fabm_sediment_component.F90:1865-2030) for
+ * every column: temperature -> bdys[0]; for each tracer n with present[n]
+ * (the import state holds it): particulate fluxes[n] = -surface[n] *
+ * velocity[n] (downward positive, :1978,1986); dissolved bdys[n+1] =
+ * surface[n] and fluxes[n] = the diffusive estimate of :2012-2014 for
+ * bcup_dissolved 1 (from conc's first layer; 0 for land columns), else 0.
+ * Absent tracers keep their bdys/fluxes. */
+void orc_assemble_bc(const orc_model *m, const double *conc, const double *temperature,
+                     const double *surface, const double *velocity,
+                     const int *present, double *bdys, double *fluxes);
+
 /* FP64 column inventories sum_k phi dz C for every tracer: [ntr][ncol]. */
 void orc_inventory(const orc_model *m, const double *conc, double *inv);
 

@@ -83,3 +83,15 @@ def zhang_wirtz_factor(cs, conc):
                    (d.bioturb_L1 + d.bioturb_L2 * np.exp(zc * 200 * d.bioturb_k_l)))
         fac[:K, col] = d.bioturb_beta * biomass ** d.bioturb_b / wt
     return fac
+
+
+def pelagic_fields(cs, seed=5):
+    """Synthetic soil-surface fields of a coupled pelagic model: temperature,
+    concentration of every tracer, settling velocity of the particulates."""
+    rng = np.random.default_rng(seed)
+    T = cs.bdys[0] + rng.uniform(-1, 1, cs.ncol)
+    surface = np.empty((11, cs.ncol))
+    surface[6:] = cs.bdys[7:] * rng.uniform(0.8, 1.2, (5, cs.ncol))
+    surface[:6] = rng.uniform(10, 500, (6, cs.ncol))
+    velocity = -rng.uniform(1e-6, 1e-4, (11, cs.ncol))
+    return T, surface, velocity

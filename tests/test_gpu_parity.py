@@ -13,7 +13,7 @@ substeps that amplify a 1-ulp difference to 1e-2 within ~24 coupling steps
 import numpy as np
 import pytest
 
-from cases import constant_rhs_case, decay_case, no_reactions, small
+from cases import constant_rhs_case, decay_case, no_reactions, pelagic_fields, small
 from conftest import relerr
 from sedgpu import capi, synth
 from sedgpu.model import (ADAPTIVE_EULER, EULER, NTR, RUNGE_KUTTA_4,
@@ -325,3 +325,66 @@ def test_bioturbation_profile3(oracle_mod, workload):
     plain.driver.bioturbation_profile = 1
     static, _, _, _, _ = run_gpu(plain, 2, precision=capi.SED_FP64)
     assert relerr(active(cs, static), active(cs, out64)).max() > 1e-6
+
+
+@pytest.mark.parametrize("bcup", [1, 2])
+def test_boundary_assembly_on_device(oracle_mod, bcup):
+    """sed_set_boundary equals get_boundary_conditions (the oracle's
+    orc_assemble_bc) bit for bit on FP64 state, absent tracers keep their
+    values, and the step that follows equals the oracle's step."""
+    cs = synth.make_workload("uneven_1024x1024",
+                             cols=np.arange(0, 1024 * 1024, 1024 * 1024 // 150)[:150])
+    cs.driver.bcup_dissolved = bcup
+    T, surf, vel = pelagic_fields(cs)
+    present = np.ones(NTR, dtype=np.int32)
+    present[[2, 9]] = 0
+    om = oracle_mod.OracleModel(cs)
+    bref, fref = om.assemble_bc(cs.conc, T, surf, vel, present)
+    s = capi.Solver(cs, precision=capi.SED_FP64)
+    s.set_forcing()
+    s.set_state(cs.conc)
+    s.set_boundary(T, surf, vel, present)
+    bd, fl = s.boundary()
+    np.testing.assert_array_equal(bd, bref)
+    np.testing.assert_array_equal(fl, fref)
+    s.step(1)
+    out = s.get_state()
+    fl_out = s.fluxes()
+    s.close()
+    c = cs.conc.copy()
+    sub = cs.copy()
+    sub.bdys, sub.fluxes = bref, fref
+    rc, _, fl_ref = oracle_mod.OracleModel(sub).run(c, nsteps=1)
+    assert rc == 0
+    np.testing.assert_array_equal(out, c)
+    np.testing.assert_array_equal(fl_out, fl_ref)
+    # FP32 state: the estimate is formed in FP64 from the FP32 first layer,
+    # i.e. the oracle's on the state rounded to FP32 (c0 - cb cancels, so
+    # the rounding of c0 shows at ~1e-4 against the FP64-state estimate)
+    s = capi.Solver(cs)
+    s.set_forcing()
+    s.set_state(cs.conc)
+    s.set_boundary(T, surf, vel, present)
+    bd32, fl32 = s.boundary()
+    s.close()
+    c32 = cs.conc.astype(np.float32).astype(np.float64)
+    _, fref32 = om.assemble_bc(c32, T, surf, vel, present)
+    np.testing.assert_array_equal(bd32, bref)
+    np.testing.assert_allclose(fl32, fref32, rtol=1e-12, atol=0)
+
+
+def test_boundary_assembly_errors():
+    cs = synth.make_workload("plain_cpu_10x10")
+    cs.driver.bcup_dissolved = 1
+    T, surf, vel = pelagic_fields(cs)
+    s = capi.Solver(cs)
+    with pytest.raises(capi.SedError) as e:
+        s.set_boundary(T, surf, vel)   # the flux estimate needs the state
+    assert e.value.code == capi.SED_E_STATE
+    s.set_state(cs.conc)
+    with pytest.raises(capi.SedError) as e:
+        s.set_boundary(T, surf, None)  # particulates present, no velocity
+    assert e.value.code == capi.SED_E_ARG
+    only_dissolved = np.array([0] * 6 + [1] * 5, dtype=np.int32)
+    s.set_boundary(T, surf, None, only_dissolved)
+    s.close()

@@ -241,3 +241,31 @@ def test_bioturbation_profile3_matches_formula(oracle_mod):
     # and the factor changes the transport: profile 3 is not the static one
     r1, _, _ = oracle_mod.OracleModel(cs).get_rhs(cs.conc)
     assert np.max(np.abs(r3 - r1) / scale) > 1e-6
+
+
+def test_assemble_bc_matches_reference_formulas(oracle_mod):
+    """orc_assemble_bc against get_boundary_conditions' formulas
+    (fabm_sediment_component.F90:1978,1986,2012-2014) written in numpy."""
+    from cases import pelagic_fields
+    cs = synth.make_workload("plain_cpu_10x10")
+    cs.driver.bcup_dissolved = 1
+    T, surf, vel = pelagic_fields(cs)
+    present = np.ones(NTR, dtype=np.int32)
+    present[[1, 8]] = 0
+    bd, fl = oracle_mod.OracleModel(cs).assemble_bc(cs.conc, T, surf, vel, present)
+    d = cs.driver
+    np.testing.assert_array_equal(bd[0], T)
+    for n in range(NTR):
+        if not present[n]:
+            np.testing.assert_array_equal(fl[n], cs.fluxes[n])
+            np.testing.assert_array_equal(bd[n + 1], cs.bdys[n + 1])
+        elif n < 6:
+            np.testing.assert_array_equal(fl[n], -surf[n] * vel[n])
+        else:
+            np.testing.assert_array_equal(bd[n + 1], surf[n])
+            est = (-(cs.conc[n, 0] - surf[n]) / cs.dz[0] *
+                   (d.bioturbation + d.diffusivity + T * 0.035) * cs.phi[0] / 86400.0 / 10000.0)
+            np.testing.assert_allclose(fl[n], est, rtol=1e-14, atol=0)
+    cs.driver.bcup_dissolved = 2
+    _, fl2 = oracle_mod.OracleModel(cs).assemble_bc(cs.conc, T, surf, vel)
+    assert np.all(fl2[6:] == 0.0)

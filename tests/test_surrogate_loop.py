@@ -63,6 +63,20 @@ def test_everything_accepted_is_the_proposal(trained):
     assert relerr(out, prop).max() < 5e-2
 
 
+def test_warp_direct_fallback_is_the_plain_step(trained):
+    sur, grid, state = trained
+    plain, _ = _one_step(grid, state)
+    s = capi.Solver(grid)
+    s.set_tuning(tile_columns=(0, 0))
+    s.set_forcing()
+    s.set_state(state)
+    st = S.step_surrogate(s, sur, 1, tol=1e-30)
+    out = s.get_state()
+    s.close()
+    assert st["surrogate_columns"] == 0
+    np.testing.assert_array_equal(out, plain)
+
+
 def test_mixed_columns_are_one_or_the_other(trained):
     sur, grid, state = trained
     plain, _ = _one_step(grid, state)

@@ -53,6 +53,8 @@ def test_default_tuning_and_segments():
 
 
 @pytest.mark.parametrize("tuning", [
+    dict(tile_columns=(0, 0), threads=(128, 64)),
+    dict(tile_columns=(0, 16), threads=(256, 256)),
     dict(tile_columns=(8, 8), threads=(64, 128)),
     dict(tile_columns=(64, 32), threads=(256, 192)),
     dict(tile_columns=(16, 8), threads=(128, 64), blocks_per_sm=(1, 1)),
@@ -65,17 +67,47 @@ def test_any_tuning_is_bit_identical(tuning):
         np.testing.assert_array_equal(g, r)
 
 
-def test_tuning_is_bit_identical_fixed_method():
+@pytest.mark.parametrize("tiles", [(8, 16), (0, 0)])
+def test_tuning_is_bit_identical_fixed_method(tiles):
     cs = plain(12000)
     ref = stepped(cs, 1, method=RUNGE_KUTTA_4)
-    got = stepped(cs, 1, dict(tile_columns=(8, 16), threads=(64, 256)), method=RUNGE_KUTTA_4)
+    got = stepped(cs, 1, dict(tile_columns=tiles, threads=(64, 256)), method=RUNGE_KUTTA_4)
     for r, g in zip(ref, got):
         np.testing.assert_array_equal(g, r)
 
 
-def drop_in(cs, chunks, nsteps=2, precision=capi.SED_FP32):
+def test_warp_direct_with_profile3_and_cascade():
+    cs = uneven(12000)
+    cs.driver.bioturbation_profile = 3
+    cs.driver.bcup_particulate = 4
+    ref = stepped(cs, 2)
+    got = stepped(cs, 2, dict(tile_columns=(0, 0), threads=(128, 128)))
+    for r, g in zip(ref, got):
+        np.testing.assert_array_equal(g, r)
+
+
+def test_warp_direct_rhs_and_fp64_rejection():
+    cs = uneven(9000)
+    s = capi.Solver(cs)
+    s.set_forcing()
+    ref = s.get_rhs(cs.conc)
+    s.set_tuning(tile_columns=(0, 0))
+    got = s.get_rhs(cs.conc)   # rhs kind served by the 32-column tile kernel
+    s.close()
+    for r, g in zip(ref, got):
+        np.testing.assert_array_equal(g, r)
+    s = capi.Solver(cs, precision=capi.SED_FP64)
+    with pytest.raises(capi.SedError) as e:
+        s.set_tuning(tile_columns=(0, 16))
+    assert e.value.code == capi.SED_E_ARG
+    s.close()
+
+
+def drop_in(cs, chunks, nsteps=2, precision=capi.SED_FP32, tiles=None):
     s = capi.Solver(cs, precision=precision)
     s.set_tuning(pipeline_chunks=chunks)
+    if tiles:
+        s.set_tuning(tile_columns=tiles)
     conc = cs.conc.copy()
     fl = np.array(cs.fluxes, dtype=np.float64, copy=True)
     stats = []
@@ -93,7 +125,7 @@ def test_pipelined_ode_solver_matches_unpipelined(make):
     ref = drop_in(cs, 1)
     p = 2
     while p <= nseg:
-        got = drop_in(cs, p)
+        got = drop_in(cs, p, tiles=(0, 0) if p == 2 else None)
         for r, g in zip(ref[:3], got[:3]):
             np.testing.assert_array_equal(g, r)
         for a, b in zip(ref[3], got[3]):
@@ -129,7 +161,7 @@ def test_autotune_restores_state_and_keeps_results():
     np.testing.assert_array_equal(s.get_state(), before)
     np.testing.assert_array_equal(s.fluxes(), fl_before)
     assert t["trials"] > 0 and t["step_ms"] > 0 and t["ode_solver_ms"] > 0
-    assert all(c in (8, 16, 32, 64) for c in t["tile_columns"])
+    assert all(c in (0, 8, 16, 32, 64) for c in t["tile_columns"])
     assert all(th in (64, 128, 256) for th in t["threads"])
     assert t["segments"] % t["pipeline_chunks"] == 0
     assert t["max_attempts"] >= 64
