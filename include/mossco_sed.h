@@ -213,7 +213,9 @@ int sed_host_unregister(void *ptr);
  * by active layers, each padded to 64 slots), so every tuning below is a
  * pure launch choice: results are bit-identical under any of them. */
 typedef struct sed_tuning {
-  int tile_columns[2];  /* columns staged per tile: 8, 16, 32 or 64 */
+  int tile_columns[2];  /* columns staged per tile: 8, 16, 32 or 64; 0 = the
+                           warp-direct kernel (FP32): every warp steps one
+                           column at a time in global memory, no tiles */
   int threads[2];       /* threads per block: 64, 128, 192 or 256 */
   int blocks_per_sm[2]; /* resident blocks per SM of the persistent grid;
                            0 = as many as fit */
