@@ -230,6 +230,107 @@ __device__ __forceinline__ void bio3_conductances(const Params<real>& p,
   }
 }
 
+// diff3d transport of tracer n added to R (FP32 folded form): interface
+// fluxes F = a (C_above - C) with the surface boundary on lane 0, then
+// dC = (F - F_below) / (phi dz).  Branch-free: lanes past the column hold
+// zero state and conductances; the no-flux bottom drops F_below at K-1.
+template <typename real, int LPL, bool BC4>
+__device__ __forceinline__ void transport_one(const Lane<real, LPL, BC4>& lc, int n,
+                                              const real (&apv)[LPL], const real (&adv)[LPL],
+                                              const bool (&bottom)[LPL], bool top,
+                                              bool dirichlet, bool fluxbc, int lane,
+                                              const real (&C)[LPL][NTR], real (&R)[LPL][NTR],
+                                              real (&ftop)[NTR]) {
+  const bool part = n < NPART;
+  real v[LPL], vm[LPL], F[LPL], Fb[LPL];
+#pragma unroll
+  for (int s = 0; s < LPL; s++) v[s] = part ? lc.phi[s] * C[s][n] : C[s][n];
+  from_above<real, LPL>(v, vm, lane);
+  const real b = lc.bnd(n);
+  if (part) {
+#pragma unroll
+    for (int s = 0; s < LPL; s++) F[s] = apv[s] * (vm[s] - v[s]);
+    F[0] = top ? b : F[0];  // downward flux through the surface (BcUp 1)
+  } else {
+    // Dirichlet (BcUp 2): the surface interface sees the bottom water
+    vm[0] = (top && dirichlet) ? b : vm[0];
+#pragma unroll
+    for (int s = 0; s < LPL; s++) F[s] = adv[s] * (vm[s] - v[s]);
+    F[0] = (top && !dirichlet) ? (fluxbc ? b : real(0)) : F[0];
+  }
+  ftop[n] = F[0];
+  from_below<real, LPL>(F, Fb, lane);
+#pragma unroll
+  for (int s = 0; s < LPL; s++) {
+    const real div = F[s] - (bottom[s] ? real(0) : Fb[s]);
+    if (BC4 && part)
+      R[s][n] = R[s][n] + fm(div, lc.ivol[s], lc.src[BC4 ? s : 0][BC4 ? n : 0]);
+    else
+      R[s][n] = fm(div, lc.ivol[s], R[s][n]);
+  }
+}
+
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 splat(float a) { return make_float2(a, a); }
+
+// transport_one for tracers n and n+1 of one class at once: the same
+// operations in packed FP32x2 arithmetic (each component rounds as the
+// scalar operation does), halving the arithmetic instructions.
+template <int LPL, bool BC4, bool PART>
+__device__ __forceinline__ void transport_pair(const Lane<float, LPL, BC4>& lc, int n,
+                                               const float (&a)[LPL], const bool (&bottom)[LPL],
+                                               bool top, bool dirichlet, bool fluxbc, int lane,
+                                               const float (&C)[LPL][NTR], float (&R)[LPL][NTR],
+                                               float (&ftop)[NTR]) {
+  float vx[LPL], vy[LPL], mx[LPL], my[LPL];
+  float2 v[LPL], F[LPL];
+#pragma unroll
+  for (int s = 0; s < LPL; s++) {
+    const float2 c = make_float2(C[s][n], C[s][n + 1]);
+    v[s] = PART ? __fmul2_rn(splat(lc.phi[s]), c) : c;
+    vx[s] = v[s].x;
+    vy[s] = v[s].y;
+  }
+  from_above<float, LPL>(vx, mx, lane);
+  from_above<float, LPL>(vy, my, lane);
+  const float b0 = lc.bnd(n), b1 = lc.bnd(n + 1);
+  if (!PART) {
+    mx[0] = (top && dirichlet) ? b0 : mx[0];
+    my[0] = (top && dirichlet) ? b1 : my[0];
+  }
+#pragma unroll
+  for (int s = 0; s < LPL; s++)
+    F[s] = __fmul2_rn(splat(a[s]), __fadd2_rn(make_float2(mx[s], my[s]), neg2(v[s])));
+  if (PART) {
+    F[0].x = top ? b0 : F[0].x;
+    F[0].y = top ? b1 : F[0].y;
+  } else {
+    F[0].x = (top && !dirichlet) ? (fluxbc ? b0 : 0.0f) : F[0].x;
+    F[0].y = (top && !dirichlet) ? (fluxbc ? b1 : 0.0f) : F[0].y;
+  }
+  ftop[n] = F[0].x;
+  ftop[n + 1] = F[0].y;
+  float fx[LPL], fy[LPL], bx[LPL], by[LPL];
+#pragma unroll
+  for (int s = 0; s < LPL; s++) { fx[s] = F[s].x; fy[s] = F[s].y; }
+  from_below<float, LPL>(fx, bx, lane);
+  from_below<float, LPL>(fy, by, lane);
+#pragma unroll
+  for (int s = 0; s < LPL; s++) {
+    const float2 fb = bottom[s] ? make_float2(0.0f, 0.0f) : make_float2(bx[s], by[s]);
+    const float2 div = __fadd2_rn(F[s], neg2(fb));
+    float2 r = make_float2(R[s][n], R[s][n + 1]);
+    if (BC4 && PART)
+      r = __fadd2_rn(r, __ffma2_rn(div, splat(lc.ivol[s]),
+                                   make_float2(lc.src[BC4 ? s : 0][BC4 ? n : 0],
+                                               lc.src[BC4 ? s : 0][BC4 ? n + 1 : 0])));
+    else
+      r = __ffma2_rn(div, splat(lc.ivol[s]), r);
+    R[s][n] = r.x;
+    R[s][n + 1] = r.y;
+  }
+}
+
 // Right-hand side of one column: OMEXDIA+P rates plus diff3d transport.
 // ftop receives the flux through the sediment surface (lane 0 only).
 // Branch-free: lanes beyond the column's K layers hold zero state and zero
@@ -259,35 +360,20 @@ __device__ __forceinline__ void column_rhs(const Params<real>& p,
   bool bottom[LPL];
 #pragma unroll
   for (int s = 0; s < LPL; s++) bottom[s] = s * 32 + lane >= K - 1;
+  if constexpr (std::is_same<real, float>::value) {
+    // tracer pairs of one class in packed FP32x2 arithmetic, tracer 10 alone
+    transport_pair<LPL, BC4, true>(lc, 0, apv, bottom, top, dirichlet, fluxbc, lane, C, R, ftop);
+    transport_pair<LPL, BC4, true>(lc, 2, apv, bottom, top, dirichlet, fluxbc, lane, C, R, ftop);
+    transport_pair<LPL, BC4, true>(lc, 4, apv, bottom, top, dirichlet, fluxbc, lane, C, R, ftop);
+    transport_pair<LPL, BC4, false>(lc, 6, adv, bottom, top, dirichlet, fluxbc, lane, C, R, ftop);
+    transport_pair<LPL, BC4, false>(lc, 8, adv, bottom, top, dirichlet, fluxbc, lane, C, R, ftop);
+    transport_one<real, LPL, BC4>(lc, NTR - 1, apv, adv, bottom, top, dirichlet, fluxbc, lane, C,
+                                  R, ftop);
+  } else {
 #pragma unroll
-  for (int n = 0; n < NTR; n++) {
-    const bool part = n < NPART;
-    real v[LPL], vm[LPL], F[LPL], Fb[LPL];
-#pragma unroll
-    for (int s = 0; s < LPL; s++) v[s] = part ? lc.phi[s] * C[s][n] : C[s][n];
-    from_above<real, LPL>(v, vm, lane);
-    const real b = lc.bnd(n);
-    if (part) {
-#pragma unroll
-      for (int s = 0; s < LPL; s++) F[s] = apv[s] * (vm[s] - v[s]);
-      F[0] = top ? b : F[0];  // downward flux through the surface (BcUp 1)
-    } else {
-      // Dirichlet (BcUp 2): the surface interface sees the bottom water
-      vm[0] = (top && dirichlet) ? b : vm[0];
-#pragma unroll
-      for (int s = 0; s < LPL; s++) F[s] = adv[s] * (vm[s] - v[s]);
-      F[0] = (top && !dirichlet) ? (fluxbc ? b : real(0)) : F[0];
-    }
-    ftop[n] = F[0];
-    from_below<real, LPL>(F, Fb, lane);
-#pragma unroll
-    for (int s = 0; s < LPL; s++) {
-      const real div = F[s] - (bottom[s] ? real(0) : Fb[s]);
-      if (BC4 && part)
-        R[s][n] = R[s][n] + fm(div, lc.ivol[s], lc.src[s][n]);
-      else
-        R[s][n] = fm(div, lc.ivol[s], R[s][n]);
-    }
+    for (int n = 0; n < NTR; n++)
+      transport_one<real, LPL, BC4>(lc, n, apv, adv, bottom, top, dirichlet, fluxbc, lane, C,
+                                    R, ftop);
   }
 }
 

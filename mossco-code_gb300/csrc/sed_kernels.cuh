@@ -435,11 +435,26 @@ __device__ __forceinline__ ColResult solve_adaptive(
 #pragma unroll
     for (int s = 0; s < LPL; s++) {
       // lanes past the column hold zeros: c1 = 0 never falls below -atol
+      if constexpr (std::is_same<real, float>::value) {
+        // tracer pairs in packed FP32x2 FMAs (per component the scalar's
+        // rounding), tracer 10 alone
 #pragma unroll
-      for (int n = 0; n < NTR; n++) {
-        const real c1 = upd(C[s][n], dtr, R[s][n]);
-        // sign of c1 - (1+rcm) c; in FP32 exact for the operands (one FMA)
-        bad |= below_keep(c1, p.keep, C[s][n], p.natol);
+        for (int n = 0; n + 1 < NTR; n += 2) {
+          const float2 c = make_float2(C[s][n], C[s][n + 1]);
+          const float2 c1 = __ffma2_rn(make_float2(dtr, dtr),
+                                       make_float2(R[s][n], R[s][n + 1]), c);
+          const float2 t = __ffma2_rn(make_float2(-p.keep, -p.keep), c, c1);
+          bad |= (t.x < p.natol) | (t.y < p.natol);
+        }
+        bad |= below_keep(upd(C[s][NTR - 1], dtr, R[s][NTR - 1]), p.keep, C[s][NTR - 1],
+                          p.natol);
+      } else {
+#pragma unroll
+        for (int n = 0; n < NTR; n++) {
+          const real c1 = upd(C[s][n], dtr, R[s][n]);
+          // sign of c1 - (1+rcm) c; in FP32 exact for the operands (one FMA)
+          bad |= below_keep(c1, p.keep, C[s][n], p.natol);
+        }
       }
     }
     const bool reject = __any_sync(FULL, bad);
@@ -452,9 +467,21 @@ __device__ __forceinline__ ColResult solve_adaptive(
     } else {
       B.account(p, dtr, ftop, dn);
 #pragma unroll
-      for (int s = 0; s < LPL; s++)
+      for (int s = 0; s < LPL; s++) {
+        if constexpr (std::is_same<real, float>::value) {
 #pragma unroll
-        for (int n = 0; n < NTR; n++) C[s][n] = upd(C[s][n], dtr, R[s][n]);
+          for (int n = 0; n + 1 < NTR; n += 2) {
+            const float2 c1 = __ffma2_rn(make_float2(dtr, dtr), make_float2(R[s][n], R[s][n + 1]),
+                                         make_float2(C[s][n], C[s][n + 1]));
+            C[s][n] = c1.x;
+            C[s][n + 1] = c1.y;
+          }
+          C[s][NTR - 1] = upd(C[s][NTR - 1], dtr, R[s][NTR - 1]);
+        } else {
+#pragma unroll
+          for (int n = 0; n < NTR; n++) C[s][n] = upd(C[s][n], dtr, R[s][n]);
+        }
+      }
       if (TICKS) t += inc;
       else dt_int = dt_int + dt_red;
       res.accepted++;
