@@ -173,6 +173,28 @@ int sed_get_state(sed_handle *h, double *conc);
 int sed_step(sed_handle *h, double dt, int method, int nsteps,
              sed_stats *stats);
 
+/* Spin-up before the run (fabm_sediment_component.F90:557-632: presimulation
+ * years of hourly ode_solver calls on a 1-column model, whose profile is then
+ * copied into every unmasked column).  nsteps coupling steps of dt with
+ * constant forcing, each warp keeping its column in registers for up to 24
+ * steps per launch.  Needs the initial state (sed_set_state).
+ *   SED_SPINUP_COLUMN: the reference's scheme.  Column `column` of the grid
+ *     (-1: the first column with the most active layers) is integrated alone
+ *     with bdys1[ntr+1] / fluxes1[ntr] (the namelist's bottom water and
+ *     deposition fluxes), then its profile is copied into every other active
+ *     column (their first min(K, K_column) layers).  The handle's own forcing
+ *     is left as it was.
+ *   SED_SPINUP_ALL: every active column is integrated with its own forcing
+ *     (sed_set_forcing / sed_set_boundary); bdys1 and fluxes1 are unused.
+ *     On the GPU this costs about as much as one column.
+ * The caller sets bcup_dissolved and bioturbation_profile as the reference
+ * does for its sed1d (:598-600). */
+#define SED_SPINUP_COLUMN 0
+#define SED_SPINUP_ALL 1
+int sed_spinup(sed_handle *h, int mode, int column, const double *bdys1,
+               const double *fluxes1, double dt, int method, long long nsteps,
+               sed_stats *stats);
+
 /* Drop-in for `call ode_solver(sed, dt, method)` followed by the component
  * epilogue: conc is the caller's host array, updated in place; fluxes is
  * read (flux boundaries) and its dissolved rows are overwritten with the
@@ -214,8 +236,8 @@ int sed_host_unregister(void *ptr);
  * pure launch choice: results are bit-identical under any of them. */
 typedef struct sed_tuning {
   int tile_columns[2];  /* columns staged per tile: 8, 16, 32 or 64; 0 = the
-                           warp-direct kernel (FP32): every warp steps one
-                           column at a time in global memory, no tiles */
+                           warp-direct kernel: every warp steps one column
+                           at a time in global memory, no tiles */
   int threads[2];       /* threads per block: 64, 128, 192 or 256 */
   int blocks_per_sm[2]; /* resident blocks per SM of the persistent grid;
                            0 = as many as fit */

@@ -51,8 +51,9 @@ struct Bin {
   int tc = 32, threads = 256;      // tile width (0: warp-direct), threads per block
   int bps = 0;                     // blocks per SM asked for (0 = all that fit)
   int occ = 0;                     // blocks per SM that fit at (tc, threads)
-  int occ_tile = 0;                // warp-direct classes: the 32-column tile
-                                   // kernel that serves the other kinds
+  int tc_fb = 32, occ_tile = 0;    // warp-direct classes: the tile kernel
+                                   // (widest of 32/16/8 that fits) serving
+                                   // the other kinds
   int tk0 = 0;                     // first tile of the class in tile_k
   int blocks(int sms, int ntiles) const {
     const int per = (bps > 0 && bps < occ) ? bps : occ;
@@ -206,23 +207,21 @@ void restrict_args(ColumnArgs<real>& a, const Bin& b, int s0, int s1, unsigned* 
   a.queue = queue;
 }
 
-// Launch one class's kernel over a's slot range.  Warp-direct classes
-// (tc 0, FP32) step with k_column_warp; their other kinds (rhs, residual) use
-// the tile kernel with 32-column tiles staging every layer of the class.
+// Launch one class's kernel over a's slot range.  Warp-direct classes (tc 0)
+// step with k_column_warp; their other kinds (rhs, residual) use the tile
+// kernel (the widest of 32/16/8 columns that fits) staging every layer.
 template <typename real>
 cudaError_t launch_bin(sed_handle* h, ColumnArgs<real> a, const Params<real>& p,
                        const Bin& bin, int kind, cudaStream_t st) {
   const bool bc4 = h->prm.bcup_particulate == 4;
   if (bin.tc == 0) {
-    if constexpr (std::is_same<real, float>::value) {
-      if (kind == KIND_ADAPT || kind == KIND_FIXED)
-        return launch_column_warp(a, p, bin.lpl, bc4, kind, bin.blocks(h->sms, a.ntiles),
-                                  bin.threads, st);
-    }
-    a.tc = 32;
+    if (kind == KIND_ADAPT || kind == KIND_FIXED)
+      return launch_column_warp<real>(a, p, bin.lpl, bc4, kind, bin.blocks(h->sms, a.ntiles),
+                                      bin.threads, st);
+    a.tc = bin.tc_fb;
     a.tile_k = nullptr;
     a.tile0 = 0;
-    a.ntiles /= 32;
+    a.ntiles /= bin.tc_fb;
     const int blocks = std::max(1, std::min(a.ntiles, bin.occ_tile * h->sms));
     return launch_column<real>(a, p, bin.lpl, bc4, kind, blocks, bin.threads, st);
   }
@@ -516,11 +515,15 @@ int apply_tuning(sed_handle* h) {
     bin.occ = 0;
     if (bin.nslots == 0) continue;
     if (bin.tc == 0) {
-      if (h->fp64()) return h->fail(SED_E_ARG, "the warp-direct kernel (tile width 0) is FP32");
       const bool bc4 = h->prm.bcup_particulate == 4, bio3 = h->prm.bioturbation_profile == 3;
-      bin.occ = std::min(column_warp_blocks_per_sm(bin.lpl, bc4, KIND_ADAPT, bin.threads, bio3),
-                         column_warp_blocks_per_sm(bin.lpl, bc4, KIND_FIXED, bin.threads, bio3));
-      bin.occ_tile = class_occupancy(h, bin, 32, bin.threads);
+      auto occ = [&](int kind) {
+        return h->fp64() ? column_warp_blocks_per_sm<double>(bin.lpl, bc4, kind, bin.threads, bio3)
+                         : column_warp_blocks_per_sm<float>(bin.lpl, bc4, kind, bin.threads, bio3);
+      };
+      bin.occ = std::min(occ(KIND_ADAPT), occ(KIND_FIXED));
+      bin.occ_tile = 0;
+      for (bin.tc_fb = 32; bin.tc_fb >= 8; bin.tc_fb /= 2)
+        if ((bin.occ_tile = class_occupancy(h, bin, bin.tc_fb, bin.threads)) > 0) break;
       if (bin.occ <= 0 || bin.occ_tile <= 0)
         return h->fail(SED_E_CUDA, "warp-direct kernel of %d threads does not fit", bin.threads);
       continue;
@@ -733,7 +736,6 @@ int autotune_t(sed_handle* h, double dt, int method, int flags, sed_tuning* out)
     float best_ms = 1e30f;
     for (int tc : tcs)
       for (int th : thr) {
-        if (tc == 0 && h->fp64()) continue;
         if (tc > 0) {
           const int occ = class_occupancy(h, bin, tc, th);
           if (occ <= 0 || bin.nslots < tc) continue;
@@ -1419,6 +1421,135 @@ int sed_set_stream(sed_handle* h, void* stream) {
   return SED_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Forcing rows of one column on the host, as get_rhs forms them (the FP64
+// path's prep_force_host64 for a single column).
+void column_forcing(const sed_params& prm, const double* bdys1, const double* fluxes1,
+                    double (&f)[NFORCE]) {
+  const double T = bdys1[0];
+  const double f_T = 1.0 * std::exp(-4500.0 * (1.0 / (T + 273.0) - (1.0 / 288.0)));
+  f[0] = prm.bioturbation_profile == 3 ? 1.0 : prm.bioturbation * f_T;
+  f[1] = prm.mol_diff_mode == 1 ? 1.0 : (prm.diffusivity + T * 0.035);
+  for (int n = 0; n < NTR; n++)
+    f[2 + n] = (n < NPART || prm.bcup_dissolved == 1) ? fluxes1[n] : bdys1[n + 1];
+}
+
+// nsteps coupling steps of the warp-direct kernel over slots [s0, s1) of a
+// class, in launches of up to kRepeat steps.
+constexpr int kRepeat = 24;
+
+template <typename real>
+int spin_range(sed_handle* h, const Bin& bin, int b, int s0, int s1, double dt, int method,
+               long long nsteps, int blocks, int threads) {
+  Params<real> p = make_params<real>(h->prm);
+  set_clock(p, dt, h->prm.dt_min);
+  const int kind = method == SED_ADAPTIVE_EULER ? KIND_ADAPT : KIND_FIXED;
+  for (long long done = 0; done < nsteps; done += kRepeat) {
+    ColumnArgs<real> a = column_args<real>(h, bin, b, dt, method);
+    a.tc = 0;
+    a.tile_k = nullptr;
+    a.slot0 = s0;
+    a.tile0 = 0;
+    a.ntiles = s1 - s0;
+    a.nrepeat = (int)std::min<long long>(kRepeat, nsteps - done);
+    CK(cudaMemsetAsync(a.queue, 0, sizeof(unsigned), h->stream), "queue reset");
+    CK(launch_column_warp<real>(a, p, bin.lpl, h->prm.bcup_particulate == 4, kind, blocks,
+                                threads, h->stream), "spin-up launch");
+    h->launches++;
+  }
+  return SED_OK;
+}
+
+template <typename real>
+int spinup_t(sed_handle* h, int mode, int column, const double* bdys1, const double* fluxes1,
+             double dt, int method, long long nsteps) {
+  const bool bc4 = h->prm.bcup_particulate == 4, bio3 = h->prm.bioturbation_profile == 3;
+  const int kind = method == SED_ADAPTIVE_EULER ? KIND_ADAPT : KIND_FIXED;
+  if (mode == SED_SPINUP_ALL) {
+    for (int b = 0; b < 2; b++) {
+      const Bin& bin = h->bins[b];
+      if (bin.nslots == 0) continue;
+      const int occ = column_warp_blocks_per_sm<real>(bin.lpl, bc4, kind, 128, bio3);
+      if (occ <= 0) return h->fail(SED_E_CUDA, "spin-up kernel does not fit");
+      const int blocks = std::max(1, std::min((bin.nslots + 3) / 4, occ * h->sms));
+      int rc = spin_range<real>(h, bin, b, bin.slot0, bin.slot0 + bin.nslots, dt, method, nsteps,
+                                blocks, 128);
+      if (rc) return rc;
+    }
+    return SED_OK;
+  }
+  // the column and its slot
+  int slot = -1;
+  if (column < 0) {
+    int best = 0;
+    for (int s = 0; s < h->nslot; s++)
+      if (h->slot_col[s] >= 0 && h->slot_k[s] > best) { best = h->slot_k[s]; slot = s; }
+    // the first such column in grid order
+    for (int s = 0; s < h->nslot; s++)
+      if (h->slot_col[s] >= 0 && h->slot_k[s] == best && h->slot_col[s] < h->slot_col[slot])
+        slot = s;
+  } else {
+    for (int s = 0; s < h->nslot; s++)
+      if (h->slot_col[s] == column) slot = s;
+  }
+  if (slot < 0) return h->fail(SED_E_ARG, "spin-up column %d is not an active column", column);
+  const int b = slot >= h->bins[1].slot0 && h->bins[1].nslots > 0 ? 1 : 0;
+  // its forcing rows replaced by the spin-up forcing, and put back after
+  const size_t rs = h->rsize(), pitch = (size_t)h->nslot * rs;
+  std::vector<real> saved(NFORCE), spin(NFORCE);
+  double f[NFORCE];
+  column_forcing(h->prm, bdys1, fluxes1, f);
+  for (int r = 0; r < NFORCE; r++) spin[r] = (real)f[r];
+  real* fcol = h->d_force.as<real>() + slot;
+  CK(cudaMemcpy2DAsync(saved.data(), rs, fcol, pitch, rs, NFORCE, cudaMemcpyDeviceToHost,
+                       h->stream), "forcing save");
+  CK(cudaMemcpy2DAsync(fcol, pitch, spin.data(), rs, rs, NFORCE, cudaMemcpyHostToDevice,
+                       h->stream), "spin-up forcing");
+  int rc = spin_range<real>(h, h->bins[b], b, slot, slot + 1, dt, method, nsteps, 1, 32);
+  if (rc) return rc;
+  CK(cudaMemcpy2DAsync(fcol, pitch, saved.data(), rs, rs, NFORCE, cudaMemcpyHostToDevice,
+                       h->stream), "forcing restore");
+  CK(launch_broadcast<real>(h->d_conc.as<real>(), h->d_kact.as<int>(), slot, h->nslot, h->kmax,
+                            h->sms, h->stream), "broadcast launch");
+  h->launches++;
+  CK(cudaStreamSynchronize(h->stream), "spin-up");  // the host vectors above
+  return SED_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sed_spinup(sed_handle* h, int mode, int column, const double* bdys1, const double* fluxes1,
+               double dt, int method, long long nsteps, sed_stats* stats) {
+  int rc;
+  if (!h) return SED_E_ARG;
+  if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
+  if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");
+  if (mode != SED_SPINUP_COLUMN && mode != SED_SPINUP_ALL)
+    return h->fail(SED_E_ARG, "mode must be SED_SPINUP_COLUMN or SED_SPINUP_ALL");
+  if (mode == SED_SPINUP_ALL && !h->have_forcing)
+    return h->fail(SED_E_STATE, "sed_set_forcing has not been called");
+  if (mode == SED_SPINUP_COLUMN && (!bdys1 || !fluxes1))
+    return h->fail(SED_E_ARG, "bdys1 and fluxes1 are required for the column spin-up");
+  if (method < 0 || method > 3 || !(dt > 0.0) || nsteps < 0)
+    return h->fail(SED_E_ARG, "bad dt, method or nsteps");
+  if (method == SED_ADAPTIVE_EULER && h->prm.cut_scope == SED_CUT_GLOBAL)
+    return h->fail(SED_E_ARG, "the spin-up cuts per column (the 1-column model has no other)");
+  CK(cudaSetDevice(h->device), "set device");
+  const long long l0 = h->launches;
+  if ((rc = stats_reset(h))) return rc;
+  CK(cudaEventRecord(h->ev0, h->stream), "event");
+  rc = h->fp64() ? spinup_t<double>(h, mode, column, bdys1, fluxes1, dt, method, nsteps)
+                 : spinup_t<float>(h, mode, column, bdys1, fluxes1, dt, method, nsteps);
+  if (rc) return rc;
+  CK(cudaEventRecord(h->ev1, h->stream), "event");
+  return stats_fetch(h, stats, l0, true);
+}
+
 int sed_set_boundary(sed_handle* h, const double* temperature, const double* surface,
                      const double* velocity, const int* present) {
   if (!h) return SED_E_ARG;
@@ -1515,8 +1646,6 @@ int sed_set_tuning(sed_handle* h, const sed_tuning* t) {
     const int tc = t->tile_columns[b], th = t->threads[b];
     if (tc != 0 && tc != 8 && tc != 16 && tc != 32 && tc != 64)
       return h->fail(SED_E_ARG, "tile_columns[%d]=%d: 0 (warp-direct), 8, 16, 32 or 64", b, tc);
-    if (tc == 0 && h->fp64())
-      return h->fail(SED_E_ARG, "tile_columns[%d]=0: the warp-direct kernel is FP32", b);
     if (th < 64 || th > 256 || th % 64 != 0)
       return h->fail(SED_E_ARG, "threads[%d]=%d: 64, 128, 192 or 256", b, th);
     if (t->blocks_per_sm[b] < 0) return h->fail(SED_E_ARG, "blocks_per_sm[%d] < 0", b);

@@ -815,7 +815,7 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
     if (lane == 0) j = (int)atomicAdd(a.queue, 1u);
     j = __shfl_sync(FULL, j, 0);
     if (j >= a.ntiles) break;
-    const int slot = a.slot0 + (a.order ? a.order[j] : j);
+    const int slot = a.slot0 + j;
     const int K = a.kact[slot];
     const bool skipped = a.skip && K > 0 && a.skip[slot];
     if (K <= 0 || skipped) {
@@ -842,15 +842,30 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
     lc.bnd_s = sb + 2;
     lc.bnd_stride = 1;
     real ftop[NTR];
-#pragma unroll
-    for (int n = 0; n < NTR; n++) ftop[n] = real(0);
-    double bud[4] = {0.0, 0.0, 0.0, 0.0};
+    double bud[4];
     ColResult r;
-    if (KIND == KIND_ADAPT)
-      r = p.ticks ? solve_adaptive<real, LPL, BC4, BIO3, true>(p, lc, lane, K, C, ftop, a.dt, bud)
-                  : solve_adaptive<real, LPL, BC4, BIO3, false>(p, lc, lane, K, C, ftop, a.dt, bud);
-    else
-      r = solve_fixed<real, LPL, BC4, BIO3>(p, lc, lane, K, C, ftop, a.dt, a.method, bud);
+    const int nrep = a.nrepeat > 1 ? a.nrepeat : 1;
+    for (int rep = 0; rep < nrep; rep++) {
+#pragma unroll
+      for (int n = 0; n < NTR; n++) ftop[n] = real(0);
+      for (int b = 0; b < 4; b++) bud[b] = 0.0;
+      if (KIND == KIND_ADAPT)
+        r = p.ticks
+                ? solve_adaptive<real, LPL, BC4, BIO3, true>(p, lc, lane, K, C, ftop, a.dt, bud)
+                : solve_adaptive<real, LPL, BC4, BIO3, false>(p, lc, lane, K, C, ftop, a.dt, bud);
+      else
+        r = solve_fixed<real, LPL, BC4, BIO3>(p, lc, lane, K, C, ftop, a.dt, a.method, bud);
+      if (lane == 0) {
+        atomicAdd(&b_att, (unsigned long long)r.attempts);
+        atomicAdd(&b_acc, (unsigned long long)r.accepted);
+        atomicAdd(&b_cols, 1ull);
+        atomicMax(&b_maxatt, r.attempts);
+        if (r.capped) atomicAdd(&b_cap, 1);
+        if (r.nan) atomicAdd(&b_nan, r.nan);
+        if (r.accepted > 0)
+          atomicMin(&b_mindt, (unsigned long long)__double_as_longlong(r.min_dt));
+      }
+    }
 #pragma unroll
     for (int s = 0; s < LPL; s++) {
       const int L = s * 32 + lane;
@@ -864,14 +879,6 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
       a.nsub[slot] = r.attempts;
       if (a.budget)
         for (int b = 0; b < 4; b++) a.budget[b * ns + slot] = bud[b];
-      atomicAdd(&b_att, (unsigned long long)r.attempts);
-      atomicAdd(&b_acc, (unsigned long long)r.accepted);
-      atomicAdd(&b_cols, 1ull);
-      atomicMax(&b_maxatt, r.attempts);
-      if (r.capped) atomicAdd(&b_cap, 1);
-      if (r.nan) atomicAdd(&b_nan, r.nan);
-      if (r.accepted > 0)
-        atomicMin(&b_mindt, (unsigned long long)__double_as_longlong(r.min_dt));
     }
     __syncwarp();
   }
@@ -884,6 +891,23 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
     atomicMax(&a.stats->max_col_attempts, b_maxatt);
     if (b_cap) { atomicAdd(&a.stats->capped, b_cap); atomicOr(&a.stats->status, ST_CAP); }
     if (b_nan) { atomicAdd(&a.stats->nan_cells, b_nan); atomicOr(&a.stats->status, ST_NAN); }
+  }
+}
+
+// Spin-up broadcast (fabm_sediment_component.F90:616-624): the profile of slot
+// src into every other active slot, first min(K, K_src) layers.
+template <typename real>
+__global__ void k_broadcast(real* __restrict__ conc, const int* __restrict__ kact, int src,
+                            int nslot, int kmax) {
+  const int ks = kact[src];
+  const size_t total = (size_t)NTR * kmax * nslot;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int slot = (int)(i % nslot);
+    const size_t nk = i / nslot;
+    const int k = (int)(nk % kmax);
+    if (slot == src || k >= kact[slot] || k >= ks) continue;
+    conc[i] = conc[nk * nslot + src];
   }
 }
 
@@ -1305,34 +1329,72 @@ int column_blocks_per_sm(int tc, int lpl, bool bc4, int kind, int threads, bool 
              : occupancy_b<real, 2, false>(tc, kind, threads, bio3);
 }
 
-template <int LPL, bool BC4, bool BIO3, int KIND>
-static cudaError_t launch_warp_t(const ColumnArgs<float>& a, const Params<float>& p, int blocks,
+template <typename real, int LPL, bool BC4, bool BIO3, int KIND>
+static cudaError_t launch_warp_t(const ColumnArgs<real>& a, const Params<real>& p, int blocks,
                                  int threads, cudaStream_t st) {
-  k_column_warp<float, LPL, BC4, BIO3, KIND><<<blocks, threads, 0, st>>>(a, p);
+  k_column_warp<real, LPL, BC4, BIO3, KIND><<<blocks, threads, 0, st>>>(a, p);
   return cudaGetLastError();
 }
 
-template <int LPL, bool BC4, bool BIO3>
-cudaError_t launch_warp_k(const ColumnArgs<float>& a, const Params<float>& p, int kind,
-                                 int blocks, int threads, cudaStream_t st) {
+template <typename real, int LPL, bool BC4, bool BIO3>
+cudaError_t launch_warp_k(const ColumnArgs<real>& a, const Params<real>& p, int kind,
+                          int blocks, int threads, cudaStream_t st) {
   return kind == KIND_FIXED
-             ? launch_warp_t<LPL, BC4, BIO3, KIND_FIXED>(a, p, blocks, threads, st)
-             : launch_warp_t<LPL, BC4, BIO3, KIND_ADAPT>(a, p, blocks, threads, st);
+             ? launch_warp_t<real, LPL, BC4, BIO3, KIND_FIXED>(a, p, blocks, threads, st)
+             : launch_warp_t<real, LPL, BC4, BIO3, KIND_ADAPT>(a, p, blocks, threads, st);
 }
 
-template <int LPL, bool BC4, bool BIO3, int KIND>
+template <typename real, int LPL, bool BC4, bool BIO3, int KIND>
 static int warp_occupancy_t(int threads) {
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &nb, k_column_warp<float, LPL, BC4, BIO3, KIND>, threads, 0) != cudaSuccess)
+          &nb, k_column_warp<real, LPL, BC4, BIO3, KIND>, threads, 0) != cudaSuccess)
     return 0;
   return nb;
 }
 
-template <int LPL, bool BC4, bool BIO3>
+template <typename real, int LPL, bool BC4, bool BIO3>
 int warp_occupancy_k(int kind, int threads) {
-  return kind == KIND_FIXED ? warp_occupancy_t<LPL, BC4, BIO3, KIND_FIXED>(threads)
-                            : warp_occupancy_t<LPL, BC4, BIO3, KIND_ADAPT>(threads);
+  return kind == KIND_FIXED ? warp_occupancy_t<real, LPL, BC4, BIO3, KIND_FIXED>(threads)
+                            : warp_occupancy_t<real, LPL, BC4, BIO3, KIND_ADAPT>(threads);
+}
+
+template <typename real>
+cudaError_t launch_column_warp(const ColumnArgs<real>& a, const Params<real>& p, int lpl,
+                               bool bc4, int kind, int blocks, int threads, cudaStream_t st) {
+  const bool b3 = p.bio3 != 0;
+  if (lpl == 1) {
+    if (bc4) return b3 ? launch_warp_k<real, 1, true, true>(a, p, kind, blocks, threads, st)
+                       : launch_warp_k<real, 1, true, false>(a, p, kind, blocks, threads, st);
+    return b3 ? launch_warp_k<real, 1, false, true>(a, p, kind, blocks, threads, st)
+              : launch_warp_k<real, 1, false, false>(a, p, kind, blocks, threads, st);
+  }
+  if (bc4) return b3 ? launch_warp_k<real, 2, true, true>(a, p, kind, blocks, threads, st)
+                     : launch_warp_k<real, 2, true, false>(a, p, kind, blocks, threads, st);
+  return b3 ? launch_warp_k<real, 2, false, true>(a, p, kind, blocks, threads, st)
+            : launch_warp_k<real, 2, false, false>(a, p, kind, blocks, threads, st);
+}
+
+template <typename real>
+int column_warp_blocks_per_sm(int lpl, bool bc4, int kind, int threads, bool bio3) {
+  if (lpl == 1) {
+    if (bc4) return bio3 ? warp_occupancy_k<real, 1, true, true>(kind, threads)
+                         : warp_occupancy_k<real, 1, true, false>(kind, threads);
+    return bio3 ? warp_occupancy_k<real, 1, false, true>(kind, threads)
+                : warp_occupancy_k<real, 1, false, false>(kind, threads);
+  }
+  if (bc4) return bio3 ? warp_occupancy_k<real, 2, true, true>(kind, threads)
+                       : warp_occupancy_k<real, 2, true, false>(kind, threads);
+  return bio3 ? warp_occupancy_k<real, 2, false, true>(kind, threads)
+              : warp_occupancy_k<real, 2, false, false>(kind, threads);
+}
+
+template <typename real>
+cudaError_t launch_broadcast(real* conc, const int* kact, int src, int nslot, int kmax, int sms,
+                             cudaStream_t st) {
+  const size_t total = (size_t)NTR * kmax * nslot;
+  k_broadcast<real><<<grid_for(total, 256, sms), 256, 0, st>>>(conc, kact, src, nslot, kmax);
+  return cudaGetLastError();
 }
 
 template <typename real>
@@ -1454,20 +1516,20 @@ cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
   prefix template int occupancy_k<real, 2, false, BIO3>(int, int, int);         \
   prefix template int occupancy_k<real, 2, true, BIO3>(int, int, int);
 
-// The warp-direct kernels (FP32) of one profile-3 setting.
-#define SED_WARP_VARIANT(prefix, BIO3)                                          \
-  prefix template cudaError_t launch_warp_k<1, false, BIO3>(                    \
-      const ColumnArgs<float>&, const Params<float>&, int, int, int, cudaStream_t); \
-  prefix template cudaError_t launch_warp_k<1, true, BIO3>(                     \
-      const ColumnArgs<float>&, const Params<float>&, int, int, int, cudaStream_t); \
-  prefix template cudaError_t launch_warp_k<2, false, BIO3>(                    \
-      const ColumnArgs<float>&, const Params<float>&, int, int, int, cudaStream_t); \
-  prefix template cudaError_t launch_warp_k<2, true, BIO3>(                     \
-      const ColumnArgs<float>&, const Params<float>&, int, int, int, cudaStream_t); \
-  prefix template int warp_occupancy_k<1, false, BIO3>(int, int);               \
-  prefix template int warp_occupancy_k<1, true, BIO3>(int, int);                \
-  prefix template int warp_occupancy_k<2, false, BIO3>(int, int);               \
-  prefix template int warp_occupancy_k<2, true, BIO3>(int, int);
+// The warp-direct kernels of one profile-3 setting.
+#define SED_WARP_VARIANT(prefix, real, BIO3)                                    \
+  prefix template cudaError_t launch_warp_k<real, 1, false, BIO3>(              \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t); \
+  prefix template cudaError_t launch_warp_k<real, 1, true, BIO3>(               \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t); \
+  prefix template cudaError_t launch_warp_k<real, 2, false, BIO3>(              \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t); \
+  prefix template cudaError_t launch_warp_k<real, 2, true, BIO3>(               \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t); \
+  prefix template int warp_occupancy_k<real, 1, false, BIO3>(int, int);         \
+  prefix template int warp_occupancy_k<real, 1, true, BIO3>(int, int);          \
+  prefix template int warp_occupancy_k<real, 2, false, BIO3>(int, int);         \
+  prefix template int warp_occupancy_k<real, 2, true, BIO3>(int, int);
 
 #define SED_INSTANTIATE(real)                                                   \
   template size_t tile_smem_bytes<real>(int, int, bool, int, bool);             \
@@ -1511,6 +1573,12 @@ cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
       const double*, const double*, const double*, unsigned, const real*,       \
       const int*, const double*, double*, double*, int, int, int, int, double,  \
       double, int, cudaStream_t);                                               \
+  template cudaError_t launch_column_warp<real>(const ColumnArgs<real>&,       \
+                                                const Params<real>&, int, bool, \
+                                                int, int, int, cudaStream_t);   \
+  template int column_warp_blocks_per_sm<real>(int, bool, int, int, bool);      \
+  template cudaError_t launch_broadcast<real>(real*, const int*, int, int, int, \
+                                              int, cudaStream_t);               \
   template cudaError_t launch_prep_bio3<real>(                                  \
       const double*, const double*, const double*, const double*,               \
       const double*, const double*, const int*, real*, int, int, int, double,   \

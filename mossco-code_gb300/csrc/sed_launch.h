@@ -38,10 +38,9 @@ struct ColumnArgs {
   // KIND_RESID (out = proposed state, conc = state at the start of the step)
   int* skip;
   double res_tol, res_atol;
-  // warp-direct kernel: optional processing order of the range's slots
-  // (order[j] = offset from slot0 of the j-th column handed out; null: in
-  // slot order)
-  const int* order;
+  // warp-direct kernel: coupling steps per launch with constant forcing
+  // (0 or 1: one); each warp keeps its column in registers between them
+  int nrepeat;
 };
 
 template <typename real>
@@ -55,12 +54,14 @@ cudaError_t launch_column(const ColumnArgs<real>& a, const Params<real>& p,
 template <typename real>
 int column_blocks_per_sm(int tc, int lpl, bool bc4, int kind, int threads, bool bio3);
 
-// Warp-direct column kernel (tile width 0 in the tuning; FP32 state, the
-// stepping kinds): every warp pulls single columns from the work counter and
+// Warp-direct column kernel (tile width 0 in the tuning; the stepping
+// kinds): every warp pulls single columns from the work counter and
 // reads and writes them in global memory, with no shared tiles and no block
 // barriers.  a.ntiles counts the range's slots.
-cudaError_t launch_column_warp(const ColumnArgs<float>& a, const Params<float>& p, int lpl,
+template <typename real>
+cudaError_t launch_column_warp(const ColumnArgs<real>& a, const Params<real>& p, int lpl,
                                bool bc4, int kind, int blocks, int threads, cudaStream_t st);
+template <typename real>
 int column_warp_blocks_per_sm(int lpl, bool bc4, int kind, int threads, bool bio3);
 
 template <typename real>
@@ -118,6 +119,11 @@ cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
                               const int* slot_col, real* force, int ncol,
                               int nslot, double bio, double diffusivity,
                               int mode, int bcup_d, int bio3, int sms, cudaStream_t st);
+
+// spin-up: the profile of slot src into every other active slot
+template <typename real>
+cudaError_t launch_broadcast(real* conc, const int* kact, int src, int nslot, int kmax, int sms,
+                             cudaStream_t st);
 
 // boundary conditions from the pelagic fields at the soil surface
 template <typename real>

@@ -93,6 +93,7 @@ class SedTuning(ctypes.Structure):
         return d
 
 
+SED_SPINUP_COLUMN, SED_SPINUP_ALL = 0, 1
 SED_TUNE_PIPELINE = 1
 SED_TUNE_CAP = 2
 
@@ -113,6 +114,8 @@ SIGNATURES = {
     "sed_set_forcing": (ctypes.c_int, [_H, _dp, _dp]),
     "sed_set_boundary": (ctypes.c_int, [_H, _dp, _dp, _dp, _ip]),
     "sed_get_boundary": (ctypes.c_int, [_H, _dp, _dp]),
+    "sed_spinup": (ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_double,
+                                  ctypes.c_int, ctypes.c_longlong, ctypes.POINTER(SedStats)]),
     "sed_set_state": (ctypes.c_int, [_H, _dp]),
     "sed_get_state": (ctypes.c_int, [_H, _dp]),
     "sed_step": (ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int,
@@ -327,6 +330,21 @@ class Solver:
             self._check(rc, "sed_step")
             return st.as_dict()
         return rc, st.as_dict()
+
+    def spinup(self, nsteps: int, mode: int = SED_SPINUP_COLUMN, column: int = -1,
+               bdys1=None, fluxes1=None, dt: Optional[float] = None, method: int = 2) -> dict:
+        """sed_spinup: nsteps coupling steps of the 1-column model (then its
+        profile copied into every column) or of every column."""
+        st = SedStats()
+        dt = self.cs.dt if dt is None else dt
+        b1 = None if bdys1 is None else _f64(bdys1)
+        f1 = None if fluxes1 is None else _f64(fluxes1)
+        self._check(self.lib.sed_spinup(self.h, int(mode), int(column),
+                                        None if b1 is None else _p(b1),
+                                        None if f1 is None else _p(f1), float(dt),
+                                        int(method), int(nsteps), ctypes.byref(st)),
+                    "sed_spinup")
+        return st.as_dict()
 
     def ode_solver(self, conc: np.ndarray, bdys: np.ndarray,
                    fluxes: np.ndarray, dt: float, method: int = 2,

@@ -86,7 +86,7 @@ def test_warp_direct_with_profile3_and_cascade():
         np.testing.assert_array_equal(g, r)
 
 
-def test_warp_direct_rhs_and_fp64_rejection():
+def test_warp_direct_rhs():
     cs = uneven(9000)
     s = capi.Solver(cs)
     s.set_forcing()
@@ -96,11 +96,16 @@ def test_warp_direct_rhs_and_fp64_rejection():
     s.close()
     for r, g in zip(ref, got):
         np.testing.assert_array_equal(g, r)
-    s = capi.Solver(cs, precision=capi.SED_FP64)
-    with pytest.raises(capi.SedError) as e:
-        s.set_tuning(tile_columns=(0, 16))
-    assert e.value.code == capi.SED_E_ARG
-    s.close()
+
+
+def test_warp_direct_fp64_matches_oracle(oracle_mod):
+    cols = np.arange(0, 1024 * 1024, 1024 * 1024 // 300)[:300]
+    cs = synth.make_workload("uneven_1024x1024", cols=cols)
+    out, _, _ = stepped(cs, 6, dict(tile_columns=(0, 0)), precision=capi.SED_FP64)
+    c = cs.conc.copy()
+    rc, _, _ = oracle_mod.OracleModel(cs).run(c, nsteps=6, percol=True)
+    assert rc == 0
+    np.testing.assert_array_equal(out, c)
 
 
 def drop_in(cs, chunks, nsteps=2, precision=capi.SED_FP32, tiles=None):
