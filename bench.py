@@ -279,6 +279,48 @@ def run_surrogate(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_spinup(args) -> None:
+    """Spin-up of the reference's 1-column model (sed1d, hourly steps for
+    --spinup-years) through sed_spinup's column mode, against the oracle's
+    1-column run on one host core (the reference runs sed1d on one PET)."""
+    import torch
+    import oracle
+    from sedgpu import capi, synth
+    torch.cuda.set_device(0)
+    cs = synth.make_workload(args.workload, cols=np.arange(1))
+    nsteps = int(round(args.spinup_years * 8760))
+    b1 = np.array(cs.bdys[:, 0], dtype=np.float64)
+    f1 = np.array(cs.fluxes[:, 0], dtype=np.float64)
+    out = {}
+    for prec, name in ((capi.SED_FP32, "fp32"), (capi.SED_FP64, "fp64")):
+        s = capi.Solver(cs, precision=prec)
+        s.set_forcing()
+        s.set_state(cs.conc)
+        s.spinup(24, capi.SED_SPINUP_COLUMN, bdys1=b1, fluxes1=f1)   # warm
+        s.set_state(cs.conc)
+        t0 = time.perf_counter()
+        st = s.spinup(nsteps, capi.SED_SPINUP_COLUMN, bdys1=b1, fluxes1=f1)
+        out[name] = {"seconds": time.perf_counter() - t0,
+                     "attempts_per_step": st["attempts"] / max(nsteps, 1),
+                     "gpu_launches": st["gpu_launches"]}
+        s.close()
+    # the oracle on one core over a bounded sample of the same run
+    cpu_steps = min(nsteps, args.spinup_cpu_steps)
+    c = cs.conc.copy()
+    t0 = time.perf_counter()
+    rc, sref, _ = oracle.OracleModel(cs).run(c, nsteps=cpu_steps, percol=True, nthreads=1)
+    cpu_s = time.perf_counter() - t0
+    line = {"metric": "spin-up of the 1-column model", "unit": "simulated years/s",
+            "workload": f"{args.workload}, one column, {cs.kmax} layers, dt 3600 s, "
+                        f"{args.spinup_years} years ({nsteps} steps)",
+            "gpu_fp32": {**out["fp32"], "years_per_s": args.spinup_years / out["fp32"]["seconds"]},
+            "gpu_fp64": {**out["fp64"], "years_per_s": args.spinup_years / out["fp64"]["seconds"]},
+            "cpu_oracle_1core": {"seconds": cpu_s, "steps": cpu_steps,
+                                 "years_per_s": cpu_steps / 8760 / cpu_s,
+                                 "attempts_per_step": sref["attempts"] / max(cpu_steps, 1)}}
+    print(json.dumps(line), flush=True)
+
+
 def coupled_e2e(s, cs, warmup, nsteps, world):
     """Coupling steps with the state resident on the device: each step takes
     the pelagic fields at the soil surface in (sed_set_boundary), steps, and
@@ -558,11 +600,16 @@ def main():
                     help="tile columns and threads per depth class, 'tc0,tc1,th0,th1' "
                          "(replaces the autotuner)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--spinup-years", type=float, default=0.0,
+                    help="time sed_spinup's 1-column model for this many years instead")
+    ap.add_argument("--spinup-cpu-steps", type=int, default=2000)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.spinup_years > 0:
+        run_spinup(args)
     elif args.solver == "surrogate":
         run_surrogate(args)
     else:

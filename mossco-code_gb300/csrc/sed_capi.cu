@@ -1447,14 +1447,17 @@ int spin_range(sed_handle* h, const Bin& bin, int b, int s0, int s1, double dt, 
   Params<real> p = make_params<real>(h->prm);
   set_clock(p, dt, h->prm.dt_min);
   const int kind = method == SED_ADAPTIVE_EULER ? KIND_ADAPT : KIND_FIXED;
-  for (long long done = 0; done < nsteps; done += kRepeat) {
+  const long long per = method == SED_ADAPTIVE_EULER ? kRepeat : 1;
+  for (long long done = 0; done < nsteps; done += per) {
     ColumnArgs<real> a = column_args<real>(h, bin, b, dt, method);
     a.tc = 0;
     a.tile_k = nullptr;
     a.slot0 = s0;
     a.tile0 = 0;
     a.ntiles = s1 - s0;
-    a.nrepeat = (int)std::min<long long>(kRepeat, nsteps - done);
+    // several steps per launch for the adaptive method, one otherwise
+    a.nrepeat = method == SED_ADAPTIVE_EULER ? (int)std::min<long long>(kRepeat, nsteps - done)
+                                             : 1;
     CK(cudaMemsetAsync(a.queue, 0, sizeof(unsigned), h->stream), "queue reset");
     CK(launch_column_warp<real>(a, p, bin.lpl, h->prm.bcup_particulate == 4, kind, blocks,
                                 threads, h->stream), "spin-up launch");

@@ -796,7 +796,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
 // sectors of neighbouring slots), steps it and writes it back.  The only
 // shared memory is the warp's copy of its column's 11 surface values; the
 // only block barriers are at entry and exit.
-template <typename real, int LPL, bool BC4, bool BIO3, int KIND>
+template <typename real, int LPL, bool BC4, bool BIO3, int KIND, bool MULTI>
 __global__ void __launch_bounds__(256, (MinBlocks<real, LPL>::value))
 k_column_warp(ColumnArgs<real> a, Params<real> p) {
   __shared__ real s_bnd[8][NFORCE];
@@ -844,7 +844,9 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
     real ftop[NTR];
     double bud[4];
     ColResult r;
-    const int nrep = a.nrepeat > 1 ? a.nrepeat : 1;
+    // MULTI: a.nrepeat steps in a row (the loop costs registers, so the
+    // single-step kernel has none)
+    const int nrep = MULTI ? (a.nrepeat > 1 ? a.nrepeat : 1) : 1;
     for (int rep = 0; rep < nrep; rep++) {
 #pragma unroll
       for (int n = 0; n < NTR; n++) ftop[n] = real(0);
@@ -1329,34 +1331,40 @@ int column_blocks_per_sm(int tc, int lpl, bool bc4, int kind, int threads, bool 
              : occupancy_b<real, 2, false>(tc, kind, threads, bio3);
 }
 
-template <typename real, int LPL, bool BC4, bool BIO3, int KIND>
+template <typename real, int LPL, bool BC4, bool BIO3, int KIND, bool MULTI>
 static cudaError_t launch_warp_t(const ColumnArgs<real>& a, const Params<real>& p, int blocks,
                                  int threads, cudaStream_t st) {
-  k_column_warp<real, LPL, BC4, BIO3, KIND><<<blocks, threads, 0, st>>>(a, p);
+  k_column_warp<real, LPL, BC4, BIO3, KIND, MULTI><<<blocks, threads, 0, st>>>(a, p);
   return cudaGetLastError();
 }
 
+// several steps per launch (a.nrepeat > 1) exist for the adaptive method
 template <typename real, int LPL, bool BC4, bool BIO3>
 cudaError_t launch_warp_k(const ColumnArgs<real>& a, const Params<real>& p, int kind,
                           int blocks, int threads, cudaStream_t st) {
-  return kind == KIND_FIXED
-             ? launch_warp_t<real, LPL, BC4, BIO3, KIND_FIXED>(a, p, blocks, threads, st)
-             : launch_warp_t<real, LPL, BC4, BIO3, KIND_ADAPT>(a, p, blocks, threads, st);
+  if (kind == KIND_FIXED) {
+    if (a.nrepeat > 1) return cudaErrorInvalidValue;
+    return launch_warp_t<real, LPL, BC4, BIO3, KIND_FIXED, false>(a, p, blocks, threads, st);
+  }
+  return a.nrepeat > 1
+             ? launch_warp_t<real, LPL, BC4, BIO3, KIND_ADAPT, true>(a, p, blocks, threads, st)
+             : launch_warp_t<real, LPL, BC4, BIO3, KIND_ADAPT, false>(a, p, blocks, threads, st);
 }
 
-template <typename real, int LPL, bool BC4, bool BIO3, int KIND>
+template <typename real, int LPL, bool BC4, bool BIO3, int KIND, bool MULTI>
 static int warp_occupancy_t(int threads) {
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &nb, k_column_warp<real, LPL, BC4, BIO3, KIND>, threads, 0) != cudaSuccess)
+          &nb, k_column_warp<real, LPL, BC4, BIO3, KIND, MULTI>, threads, 0) != cudaSuccess)
     return 0;
   return nb;
 }
 
 template <typename real, int LPL, bool BC4, bool BIO3>
 int warp_occupancy_k(int kind, int threads) {
-  return kind == KIND_FIXED ? warp_occupancy_t<real, LPL, BC4, BIO3, KIND_FIXED>(threads)
-                            : warp_occupancy_t<real, LPL, BC4, BIO3, KIND_ADAPT>(threads);
+  if (kind == KIND_FIXED) return warp_occupancy_t<real, LPL, BC4, BIO3, KIND_FIXED, false>(threads);
+  return std::min(warp_occupancy_t<real, LPL, BC4, BIO3, KIND_ADAPT, false>(threads),
+                  warp_occupancy_t<real, LPL, BC4, BIO3, KIND_ADAPT, true>(threads));
 }
 
 template <typename real>

@@ -59,6 +59,7 @@ module sed_gpu
     integer(c_int) :: trials
   end type
   integer, parameter, public :: SED_TUNE_PIPELINE = 1, SED_TUNE_CAP = 2
+  integer, parameter, public :: SED_SPINUP_COLUMN = 0, SED_SPINUP_ALL = 1
 
   !> a solver handle
   type, public :: sed_gpu_t
@@ -96,6 +97,15 @@ module sed_gpu
     integer(c_int) function sed_set_forcing(h, bdys, fluxes) bind(C, name='sed_set_forcing')
       import :: c_int, c_ptr
       type(c_ptr), value :: h, bdys, fluxes
+    end function
+    integer(c_int) function sed_spinup(h, mode, column, bdys1, fluxes1, dt, method, nsteps, st) &
+        bind(C, name='sed_spinup')
+      import :: c_int, c_ptr, c_double, c_long_long, sed_stats_t
+      type(c_ptr), value :: h, bdys1, fluxes1
+      integer(c_int), value :: mode, column, method
+      real(c_double), value :: dt
+      integer(c_long_long), value :: nsteps
+      type(sed_stats_t), intent(out) :: st
     end function
     integer(c_int) function sed_set_boundary(h, temperature, surface, velocity, present) &
         bind(C, name='sed_set_boundary')
@@ -136,7 +146,7 @@ module sed_gpu
 
   public :: sed_default_params, sed_gpu_init, sed_gpu_ode_solver, &
             sed_gpu_get_rhs, sed_gpu_finalize, sed_get_tuning, sed_set_tuning, &
-            sed_autotune, sed_set_boundary, sed_get_boundary
+            sed_autotune, sed_set_boundary, sed_get_boundary, sed_spinup
 
 contains
 
