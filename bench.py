@@ -42,9 +42,10 @@ UNIT = "column-steps/s"
 WORKLOAD = "plain_gpu_256x256"
 NTR, NCOEF, NFORCE, NDISS = 11, 4, 13, 5
 L2_BYTES = 129 * 1024 * 1024
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_column launch from
-# an ncu capture (profiles/k_column_plain_gpu_256x256.md)
-MEASURED_TRAFFIC = {"plain_gpu_256x256": 163.6e6}
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the hot
+# kernel from an ncu capture at day 10 of the run
+# (profiles/k_column_warp_plain_gpu_256x256.md)
+MEASURED_TRAFFIC = {"plain_gpu_256x256": 169.0e6}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -560,7 +561,8 @@ def run_gpu(args) -> None:
                      "traffic": MEASURED_TRAFFIC.get(args.workload),
                      "peak_kind": peak_kind,
                      "bytes_per_launch": bytes_step,
-                     "kernel": "k_column<float,LPL,false,ADAPT>"},
+                     "kernel": ("k_column_warp<float,1,...,ADAPT>" if s_tuning["tile_columns"][0] == 0
+                                else "k_column<float,1,...,ADAPT>")},
         "compute": {"fp32_tflops_est": fp32_ach, "fp32_peak_tflops": fp32_peak,
                     "frac": fp32_ach / fp32_peak,
                     "note": "nominal 152 SM x 128 FMA/clk at the sampled clock"},
