@@ -30,7 +30,8 @@ extern "C" {
 #endif
 
 #define SED_NTR 11        /* OMEXDIA+P tracers, order in sed_tracer_name() */
-#define SED_KMAX_LIMIT 64 /* layers per column the kernels hold on chip */
+#define SED_KMAX_LIMIT 63 /* layers per column the kernels hold on chip (one
+                             or two per lane of a warp, the last lane free) */
 
 /* return codes */
 #define SED_OK 0

@@ -1002,7 +1002,8 @@ int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
       if (acc * h->nseg >= work * s && (c + 1) % 32 == 0) h->seg_col[s++] = c + 1;
     }
   }
-  // slots: depth class (<= 32 layers, 33..64), then segment, then active
+  // slots: depth class (<= 31 layers, 32..63: the warp's last lane stays
+  // free, so the no-flux bottom needs no select), then segment, then active
   // layers (stable); every (class, segment) run is padded to kSlotPad slots
   h->slot_col.clear();
   h->slot_k.clear();
@@ -1014,7 +1015,7 @@ int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
       bin.segb[sg] = (int)h->slot_col.size();
       std::vector<int> cols;
       for (int c = h->seg_col[sg]; c < h->seg_col[sg + 1]; c++)
-        if (ka[c] > 0 && (ka[c] > 32) == (b == 1)) cols.push_back(c);
+        if (ka[c] > 0 && (ka[c] > 31) == (b == 1)) cols.push_back(c);
       std::stable_sort(cols.begin(), cols.end(), [&](int x, int y) { return ka[x] < ka[y]; });
       for (int c : cols) { h->slot_col.push_back(c); h->slot_k.push_back(ka[c]); }
       while (h->slot_col.size() % kSlotPad) { h->slot_col.push_back(-1); h->slot_k.push_back(0); }

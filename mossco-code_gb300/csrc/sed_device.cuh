@@ -111,27 +111,38 @@ __device__ __forceinline__ void omexdia_p(const Params<real>& p,
   const real sdetN = c[T_SDETN], fdetP = c[T_FDETP], adsP = c[T_ADSP];
   const real O2 = c[T_O2], NO3 = c[T_NO3], NH4 = c[T_NH4], ODU = c[T_ODU];
   const real PO4 = c[T_PO4];
-  const real CprodF = p.rF * fdetC;
-  const real CprodS = p.rS * sdetC;
+  // independent products and Monod denominators in FP32x2 pairs (each
+  // component rounds as the scalar operation would)
+  const float2 CprodFS = __fmul2_rn(make_float2(p.rF, p.rS), make_float2(fdetC, sdetC));
+  const float2 NprodFS = __fmul2_rn(make_float2(p.rF, p.rS), make_float2(fdetN, sdetN));
+  const float2 d01 = __fadd2_rn(make_float2(O2, O2), make_float2(p.ksO2oxic, p.kinO2denit));
+  const float2 d23 = __fadd2_rn(make_float2(O2, O2), make_float2(p.kinO2anox, p.ksO2nitri));
+  const float2 d45 = __fadd2_rn(make_float2(O2, NO3), make_float2(p.ksO2oduox, p.ksNO3denit));
+  const float2 d67 = __fadd2_rn(make_float2(NO3, p.PAdsODU), make_float2(p.kinNO3anox, ODU));
+  const real CprodF = CprodFS.x, CprodS = CprodFS.y;
   const real Cprod = CprodF + CprodS;
   const real lim = Cprod > p.cmax ? sdiv(p.cmax, Cprod) : real(1);
-  const real oxlim = sdiv(O2, O2 + p.ksO2oxic);
-  const real dnlim = sdiv(p.kinO2denit, O2 + p.kinO2denit) * sdiv(NO3, NO3 + p.ksNO3denit);
-  const real anlim = sdiv(p.kinO2anox, O2 + p.kinO2anox) * sdiv(p.kinNO3anox, NO3 + p.kinNO3anox);
+  const real oxlim = sdiv(O2, d01.x);
+  const real dnlim = sdiv(p.kinO2denit, d01.y) * sdiv(NO3, d45.y);
+  const real anlim = sdiv(p.kinO2anox, d23.x) * sdiv(p.kinNO3anox, d67.x);
   const real Cmin = sdiv(lim * Cprod, oxlim + dnlim + anlim);
-  const real OxicMin = Cmin * oxlim;
-  const real Denit = Cmin * dnlim;
+  const float2 OxDn = __fmul2_rn(make_float2(Cmin, Cmin), make_float2(oxlim, dnlim));
+  const real OxicMin = OxDn.x;
+  const real Denit = OxDn.y;
   const real AnoxicMin = Cmin * anlim;
-  const real Nitri = p.rnit * NH4 * sdiv(O2, O2 + p.ksO2nitri);
-  const real OduOx = p.rodu * ODU * sdiv(O2, O2 + p.ksO2oduox);
-  const real Rads = sdiv(p.pads * fm(p.PAdsODU, PO4, -(ODU * adsP)), p.PAdsODU + ODU);
-  const real NprodF = p.rF * fdetN;
-  const real NprodS = p.rS * sdetN;
+  const float2 NO = __fmul2_rn(__fmul2_rn(make_float2(p.rnit, p.rodu), make_float2(NH4, ODU)),
+                               make_float2(sdiv(O2, d23.y), sdiv(O2, d45.x)));
+  const real Nitri = NO.x;
+  const real OduOx = NO.y;
+  const real Rads = sdiv(p.pads * fm(p.PAdsODU, PO4, -(ODU * adsP)), d67.y);
+  const real NprodF = NprodFS.x, NprodS = NprodFS.y;
   const real Pprod = p.rF * fdetP;
-  r[T_FDETC] = -(lim * CprodF);
-  r[T_SDETC] = -(lim * CprodS);
-  r[T_FDETN] = -(lim * NprodF);
-  r[T_SDETN] = -(lim * NprodS);
+  const float2 rC = __fmul2_rn(make_float2(lim, lim), CprodFS);
+  const float2 rN = __fmul2_rn(make_float2(lim, lim), NprodFS);
+  r[T_FDETC] = -rC.x;
+  r[T_SDETC] = -rC.y;
+  r[T_FDETN] = -rN.x;
+  r[T_SDETN] = -rN.y;
   r[T_FDETP] = -(lim * Pprod);
   r[T_ADSP] = Rads;
   r[T_O2] = fm(real(-2), Nitri, -OxicMin) - OduOx;
@@ -262,7 +273,9 @@ __device__ __forceinline__ void transport_one(const Lane<real, LPL, BC4>& lc, in
   from_below<real, LPL>(F, Fb, lane);
 #pragma unroll
   for (int s = 0; s < LPL; s++) {
-    const real div = F[s] - (bottom[s] ? real(0) : Fb[s]);
+    // the flux below the last layer is zero by construction: the lane
+    // below holds zero conductance (columns leave the warp's last lane free)
+    const real div = F[s] - Fb[s];
     if (BC4 && part)
       R[s][n] = R[s][n] + fm(div, lc.ivol[s], lc.src[BC4 ? s : 0][BC4 ? n : 0]);
     else
@@ -317,8 +330,7 @@ __device__ __forceinline__ void transport_pair(const Lane<float, LPL, BC4>& lc, 
   from_below<float, LPL>(fy, by, lane);
 #pragma unroll
   for (int s = 0; s < LPL; s++) {
-    const float2 fb = bottom[s] ? make_float2(0.0f, 0.0f) : make_float2(bx[s], by[s]);
-    const float2 div = __fadd2_rn(F[s], neg2(fb));
+    const float2 div = __fadd2_rn(F[s], neg2(make_float2(bx[s], by[s])));
     float2 r = make_float2(R[s][n], R[s][n + 1]);
     if (BC4 && PART)
       r = __fadd2_rn(r, __ffma2_rn(div, splat(lc.ivol[s]),
@@ -357,9 +369,9 @@ __device__ __forceinline__ void column_rhs(const Params<real>& p,
   const bool top = lane == 0;
   const bool dirichlet = p.bcup_d == 2;
   const bool fluxbc = p.bcup_d == 1;
-  bool bottom[LPL];
+  bool bottom[LPL];  // unused by the FP32 form (see transport_one)
 #pragma unroll
-  for (int s = 0; s < LPL; s++) bottom[s] = s * 32 + lane >= K - 1;
+  for (int s = 0; s < LPL; s++) bottom[s] = false;
   if constexpr (std::is_same<real, float>::value) {
     // tracer pairs of one class in packed FP32x2 arithmetic, tracer 10 alone
     transport_pair<LPL, BC4, true>(lc, 0, apv, bottom, top, dirichlet, fluxbc, lane, C, R, ftop);
