@@ -45,7 +45,7 @@ L2_BYTES = 129 * 1024 * 1024
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the hot
 # kernel from an ncu capture at day 10 of the run
 # (profiles/k_column_warp_plain_gpu_256x256.md)
-MEASURED_TRAFFIC = {"plain_gpu_256x256": 169.0e6}
+MEASURED_TRAFFIC = {"plain_gpu_256x256": 166.7e6}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -394,15 +394,16 @@ def run_gpu(args) -> None:
 
     steps = args.steps or cs.nsteps   # default: the configured run
     # launch tuning chosen by the library's autotuner on a developed state
-    # (two simulated days in; the reference algorithm's substep count grows
-    # ~10x over the first days), untimed; the timed run then starts from the
-    # configured initial state
+    # (ten simulated days in, or the middle of a shorter window: the
+    # reference algorithm's substep count grows ~10x over the first days and
+    # the developed regime dominates the run), untimed; the timed run then
+    # starts from the configured initial state
     tuning = None
     if args.tuning:
         tc0, tc1, th0, th1 = (int(v) for v in args.tuning.split(","))
         s.set_tuning(tile_columns=(tc0, tc1), threads=(th0, th1))
     elif not args.no_autotune:
-        s.step(min(48, steps))
+        s.step(max(1, min(240, steps // 2)))
         tuning = s.autotune(flags=0 if args.no_e2e else capi.SED_TUNE_PIPELINE)
     s.set_state(cs.conc)
     for _ in range(args.warmup):

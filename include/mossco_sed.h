@@ -230,8 +230,8 @@ int sed_host_unregister(void *ptr);
 /* ------------------------------------------------------------------------
  * Launch tuning (no counterpart in the reference, whose solver has no
  * launch parameters).  Index [0] of the per-class fields is the class of
- * columns with up to 32 active layers (one layer per lane), [1] the class
- * with 33..64 (two layers per lane).  sed_set_grid lays the active columns
+ * columns with up to 31 active layers (one layer per lane), [1] the class
+ * with 32..63 (two layers per lane).  sed_set_grid lays the active columns
  * out once (depth class, then `segments` contiguous column ranges balanced
  * by active layers, each padded to 64 slots), so every tuning below is a
  * pure launch choice: results are bit-identical under any of them. */
