@@ -1,10 +1,11 @@
 // sed_capi.cu -- host side of the C ABI declared in include/mossco_sed.h.
 //
 // A handle owns one CUDA stream, the device-resident column state and the
-// per-layer coefficients.  Active columns are compacted into "slots" sorted
-// by active-layer count (land columns are never touched on the device),
-// grouped into tiles of tc slots; columns of up to 32 layers run in the
-// one-layer-per-lane kernel, deeper ones (to 64) in the two-layer one.  A
+// per-layer coefficients.  Active columns are compacted into "slots" (land
+// columns are never touched on the device): depth class, then column
+// segment, then active-layer count.  Columns of up to 31 layers run one
+// layer per lane, deeper ones (to 63) two.  Each class is stepped by the
+// tile kernel (tiles of tc slots) or the warp-direct kernel, as tuned.  A
 // coupling step is a captured CUDA graph (queue reset + one persistent
 // kernel per depth class), replayed for every step.
 #include <cuda_runtime.h>
