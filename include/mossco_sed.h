@@ -234,7 +234,9 @@ int sed_host_unregister(void *ptr);
  * with 32..63 (two layers per lane).  sed_set_grid lays the active columns
  * out once (depth class, then `segments` contiguous column ranges balanced
  * by active layers, each padded to 64 slots), so every tuning below is a
- * pure launch choice: results are bit-identical under any of them. */
+ * pure launch choice: results are bit-identical under any of them.  The
+ * defaults are the warp-direct kernel with 128 threads for FP32 state and
+ * tiles of 32 / 16 columns with 256 threads for FP64. */
 typedef struct sed_tuning {
   int tile_columns[2];  /* columns staged per tile: 8, 16, 32 or 64; 0 = the
                            warp-direct kernel: every warp steps one column

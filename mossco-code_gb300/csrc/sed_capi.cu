@@ -1024,8 +1024,10 @@ int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
     bin.segb[h->nseg] = (int)h->slot_col.size();
     for (int sg = h->nseg + 1; sg <= kMaxSeg; sg++) bin.segb[sg] = bin.segb[h->nseg];
     bin.nslots = (int)h->slot_col.size() - bin.slot0;
-    bin.tc = b == 0 ? 32 : 16;
-    bin.threads = 256;
+    // FP32: the warp-direct kernel (the faster one over every regime of the
+    // reference workloads); FP64: tiles
+    bin.tc = !h->fp64() ? 0 : (b == 0 ? 32 : 16);
+    bin.threads = !h->fp64() ? 128 : 256;
     bin.bps = 0;
   }
   if (h->slot_col.empty()) {

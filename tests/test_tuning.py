@@ -42,7 +42,11 @@ def test_default_tuning_and_segments():
     s = capi.Solver(uneven())
     t = s.tuning().as_dict()
     s.close()
-    assert t["tile_columns"] == [32, 16] and t["threads"] == [256, 256]
+    assert t["tile_columns"] == [0, 0] and t["threads"] == [128, 128]
+    s64 = capi.Solver(uneven(), precision=capi.SED_FP64)
+    t64 = s64.tuning().as_dict()
+    s64.close()
+    assert t64["tile_columns"] == [32, 16] and t64["threads"] == [256, 256]
     assert t["segments"] == 2 and t["pipeline_chunks"] == 2
     s = capi.Solver(plain())
     assert s.tuning().segments == 8 and s.tuning().pipeline_chunks == 4
@@ -53,6 +57,7 @@ def test_default_tuning_and_segments():
 
 
 @pytest.mark.parametrize("tuning", [
+    dict(tile_columns=(32, 16), threads=(256, 256)),
     dict(tile_columns=(0, 0), threads=(128, 64)),
     dict(tile_columns=(0, 16), threads=(256, 256)),
     dict(tile_columns=(8, 8), threads=(64, 128)),
