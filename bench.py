@@ -436,6 +436,12 @@ def run_gpu(args) -> None:
         t = torch.tensor([dev_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         dev_ms = float(t.item())
+        # whole-job substep statistics (scalars only; no state crosses ranks)
+        from sedgpu import shard
+        red = shard.reduce_stats({"attempts": att, "accepted": acc, "column_steps": col_steps,
+                                  "max_col_attempts": max_att})
+        att, acc, col_steps, max_att = (red["attempts"], red["accepted"],
+                                        red["column_steps"], red["max_col_attempts"])
         dist.barrier()
     clk = clocks.stop()
     ms_per_step = dev_ms / steps

@@ -1,0 +1,69 @@
+"""Column sharding across ranks (one process per GPU).
+
+Sediment columns are independent: the transport is vertical-only and the
+rates are local, so the reference decomposes the grid into ESMF PETs with no
+halo exchange (src/components/fabm_sediment_component.F90:382-387).  Here a
+rank owns a contiguous range of grid columns, balanced by active layers, and
+steps it with its own handle.  No data crosses ranks during a run; only the
+scalar step statistics are reduced, once, at the end.
+"""
+from __future__ import annotations
+
+from typing import Dict, List, Tuple
+
+import numpy as np
+
+from .model import ColumnSet
+
+
+def partition(kact: np.ndarray, world: int) -> List[Tuple[int, int]]:
+    """Contiguous column ranges [c0, c1), one per rank, with about equal
+    active-layer sums (land columns count as nothing)."""
+    kact = np.asarray(kact, dtype=np.int64)
+    ncol = kact.size
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    work = np.cumsum(kact)
+    total = int(work[-1]) if ncol else 0
+    bounds = [0]
+    for r in range(1, world):
+        target = total * r / world
+        c = int(np.searchsorted(work, target, side="left")) + 1
+        bounds.append(min(max(c, bounds[-1]), ncol))
+    bounds.append(ncol)
+    return [(bounds[r], bounds[r + 1]) for r in range(world)]
+
+
+def shard(cs: ColumnSet, rank: int, world: int) -> Tuple[ColumnSet, Tuple[int, int]]:
+    """The rank's columns as their own 1 x n grid, and its column range."""
+    c0, c1 = partition(cs.kact, world)[rank]
+    return cs.subset(np.arange(c0, c1)), (c0, c1)
+
+
+_SUM = ("attempts", "accepted", "column_steps", "capped_columns", "nan_cells",
+        "gpu_launches", "surrogate_columns")
+
+
+def reduce_stats(stats: Dict[str, float], group=None) -> Dict[str, float]:
+    """Whole-grid statistics from every rank's sed_stats dict: sums of the
+    counters, max of the per-column maxima and of the device time, min of the
+    smallest substep (torch.distributed, any backend)."""
+    import torch
+    import torch.distributed as dist
+    # nccl reduces device tensors, gloo host ones
+    dev = "cuda" if dist.get_backend(group) == "nccl" else "cpu"
+    keys = [k for k in _SUM if k in stats]
+    s = torch.tensor([float(stats[k]) for k in keys], dtype=torch.float64, device=dev)
+    mx = torch.tensor([float(stats.get("max_col_attempts", 0)),
+                       float(stats.get("device_ms", 0.0))], dtype=torch.float64, device=dev)
+    mn = torch.tensor([float(stats.get("min_dt", np.inf))], dtype=torch.float64, device=dev)
+    dist.all_reduce(s, op=dist.ReduceOp.SUM, group=group)
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX, group=group)
+    dist.all_reduce(mn, op=dist.ReduceOp.MIN, group=group)
+    out = dict(stats)
+    for k, v in zip(keys, s.tolist()):
+        out[k] = int(v)
+    out["max_col_attempts"] = int(mx[0].item())
+    out["device_ms"] = float(mx[1].item())
+    out["min_dt"] = float(mn[0].item())
+    return out

@@ -1,0 +1,89 @@
+"""Multi-rank path on the CPU: two gloo ranks each step their own contiguous
+column range (no data crosses ranks during the run) and reduce only the
+scalar statistics at the end.  The oracle stands in for each rank's device
+solver; the gathered states must equal a single-process run, column for
+column, and the reduced statistics the single-process ones."""
+import os
+import socket
+import sys
+
+import numpy as np
+import pytest
+
+from sedgpu import shard, synth
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+NSTEPS = 6
+
+
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, outdir):
+    for p in (os.path.join(ROOT, "mossco-code_gb300"), os.path.join(ROOT, "oracle")):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    import torch.distributed as dist
+    import oracle
+    from sedgpu import shard as sh
+    from sedgpu import synth as sy
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        cs = sy.make_workload("uneven_1024x1024",
+                              cols=np.arange(0, 1024 * 1024, 1024 * 1024 // 160)[:160])
+        mine, (c0, c1) = sh.shard(cs, rank, world)
+        c = mine.conc.copy()
+        rc, st, fl = oracle.OracleModel(mine).run(c, nsteps=NSTEPS, percol=True, nthreads=1)
+        assert rc == 0
+        st["column_steps"] = int(np.count_nonzero(mine.kact)) * NSTEPS
+        red = sh.reduce_stats(st)
+        np.savez(os.path.join(outdir, f"rank{rank}.npz"), conc=c, fluxes=fl,
+                 c0=c0, c1=c1, attempts=red["attempts"], accepted=red["accepted"],
+                 column_steps=red["column_steps"], max_col=red["max_col_attempts"],
+                 min_dt=red["min_dt"])
+    finally:
+        dist.destroy_process_group()
+
+
+def test_partition_balances_work_and_covers_the_grid():
+    kact = np.array([0, 30, 30, 0, 10, 60, 60, 5, 0, 30], dtype=np.int32)
+    for world in (1, 2, 3, 4):
+        parts = shard.partition(kact, world)
+        assert parts[0][0] == 0 and parts[-1][1] == kact.size
+        assert all(a[1] == b[0] for a, b in zip(parts, parts[1:]))
+        work = [int(kact[a:b].sum()) for a, b in parts]
+        assert max(work) <= kact.sum() / world + kact.max()
+
+
+def test_two_gloo_ranks_equal_one_process(oracle_mod, tmp_path):
+    import torch.multiprocessing as mp
+    port = _free_port()
+    mp.spawn(_rank_main, args=(2, port, str(tmp_path)), nprocs=2, join=True)
+    cs = synth.make_workload("uneven_1024x1024",
+                             cols=np.arange(0, 1024 * 1024, 1024 * 1024 // 160)[:160])
+    ref = cs.conc.copy()
+    rc, sref, fref = oracle_mod.OracleModel(cs).run(ref, nsteps=NSTEPS, percol=True,
+                                                   nthreads=1)
+    assert rc == 0
+    got = np.empty_like(ref)
+    fl = np.empty_like(fref)
+    reds = []
+    for r in range(2):
+        d = np.load(tmp_path / f"rank{r}.npz")
+        c0, c1 = int(d["c0"]), int(d["c1"])
+        got[:, :, c0:c1] = d["conc"]
+        fl[:, c0:c1] = d["fluxes"]
+        reds.append(d)
+    np.testing.assert_array_equal(got, ref)
+    np.testing.assert_array_equal(fl, fref)
+    for d in reds:   # every rank holds the same whole-grid statistics
+        assert int(d["attempts"]) == sref["attempts"]
+        assert int(d["accepted"]) == sref["accepted"]
+        assert int(d["column_steps"]) == int(np.count_nonzero(cs.kact)) * NSTEPS
+        assert int(d["max_col"]) == sref["max_col_attempts"]
+        assert float(d["min_dt"]) == sref["min_dt"]
