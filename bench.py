@@ -366,7 +366,7 @@ def coupled_e2e(s, cs, warmup, nsteps, world):
     for a in (T, surface, velocity, fl):
         capi.host_unregister(a)
     return {"value": world * cs.n_active * nsteps / sec, "unit": UNIT,
-            "h2d_bytes_per_step": int(T.nbytes + surface.nbytes + velocity.nbytes),
+            "h2d_bytes_per_step": int(T.nbytes + surface.nbytes + velocity[:6].nbytes),
             "d2h_bytes_per_step": int(fl.nbytes), "steps": nsteps,
             "calls": "sed_set_boundary + sed_step + sed_get_fluxes (state on the device)",
             "ms_per_call": {k: round(1e3 * statistics.median(v), 3) for k, v in parts.items()}}

@@ -1582,8 +1582,8 @@ int sed_set_boundary(sed_handle* h, const double* temperature, const double* sur
      "temperature copy");
   CK(cudaMemcpyAsync(bs, surface, (size_t)NTR * nc * sizeof(double), cudaMemcpyHostToDevice,
                      h->stream), "surface copy");
-  if (velocity)
-    CK(cudaMemcpyAsync(bv, velocity, (size_t)NTR * nc * sizeof(double),
+  if (velocity)  // only the particulate rows are read
+    CK(cudaMemcpyAsync(bv, velocity, (size_t)NPART * nc * sizeof(double),
                        cudaMemcpyHostToDevice, h->stream), "velocity copy");
   cudaError_t e =
       h->fp64()
