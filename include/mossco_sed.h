@@ -214,6 +214,12 @@ int sed_get_fluxes(sed_handle *h, double *fluxes);
 /* Per column of the last step: attempts [ncol] (0 on land). */
 int sed_get_attempts(sed_handle *h, int *attempts);
 
+/* Smallest accepted substep of every column in the last step, [ncol] (s;
+ * 0 for land columns and columns without one): the per-column form of
+ * type_rhs_driver's last_min_dt (solver_library.F90:130-136); the grid's
+ * minimum and its column are the minimum and argmin of this array. */
+int sed_get_min_dt(sed_handle *h, double *min_dt);
+
 /* FP64 budgets of the last step, [4][ncol]: P inventory, P residual,
  * N inventory, N residual (mmol/m2).  Requires params.budgets. */
 int sed_get_budgets(sed_handle *h, double *budgets);

@@ -110,7 +110,7 @@ struct sed_handle {
   DevBuf d_slot_col, d_kact, d_tile_k, d_conc, d_coef, d_cap, d_force, d_sflux,
       d_budget, d_nsub, d_queue, d_stats, d_flag, d_stage, d_bdys, d_fluxes,
       d_rhs, d_rhs_stage, d_grid, d_force64, d_prop, d_skip, d_xfeat, d_yhat, d_backup,
-      d_col_slot, d_top, d_bcin;
+      d_col_slot, d_top, d_bcin, d_mindt;
   std::vector<double> force64;  // host forcing rows (FP64 state)
   DevStats* h_stats = nullptr;  // pinned
   int* h_flag = nullptr;        // pinned
@@ -186,6 +186,7 @@ ColumnArgs<real> column_args(sed_handle* h, const Bin& b, int bin_index,
   a.sflux = h->d_sflux.as<real>();
   a.budget = h->prm.budgets ? h->d_budget.as<double>() : nullptr;
   a.nsub = h->d_nsub.as<int>();
+  a.mindt = h->d_mindt.as<double>();
   a.queue = h->d_queue.as<unsigned>() + bin_index;
   a.stats = h->d_stats.as<DevStats>();
   a.nslot = h->nslot;
@@ -373,6 +374,15 @@ int step_global(sed_handle* h, double dt) {
   tmp.column_steps += (unsigned long long)h->nactive;
   tmp.max_col_attempts = std::max(tmp.max_col_attempts, (int)att);
   if (capped) { tmp.status |= ST_CAP; tmp.capped += h->nactive; }
+  {
+    // one dt sequence for the whole grid: every active column's smallest
+    std::vector<double> md(h->nslot, 0.0);
+    for (int i = 0; i < h->nslot; i++)
+      if (h->slot_col[i] >= 0 && acc > 0) md[i] = min_dt;
+    CK(cudaMemcpyAsync(h->d_mindt.p, md.data(), md.size() * sizeof(double),
+                       cudaMemcpyHostToDevice, h->stream), "smallest substeps");
+    CK(cudaStreamSynchronize(h->stream), "global step");
+  }
   unsigned long long bits;
   memcpy(&bits, &min_dt, sizeof bits);
   if (acc > 0 && bits < tmp.min_dt_bits) tmp.min_dt_bits = bits;
@@ -1048,11 +1058,13 @@ int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
   CK(h->d_force.alloc((size_t)NFORCE * ns * rs), "forcing");
   CK(h->d_sflux.alloc((size_t)NDISS * ns * rs), "surface flux");
   CK(h->d_nsub.alloc(ns * sizeof(int)), "attempts");
+  CK(h->d_mindt.alloc(ns * sizeof(double)), "smallest substeps");
   if (h->prm.budgets) CK(h->d_budget.alloc(4 * ns * sizeof(double)), "budgets");
   if (bc4) CK(h->d_cap.alloc((size_t)kmax * ns * rs), "flux cap");
   CK(cudaMemsetAsync(h->d_conc.p, 0, (size_t)NTR * kmax * ns * rs, h->stream), "state clear");
   CK(cudaMemsetAsync(h->d_sflux.p, 0, (size_t)NDISS * ns * rs, h->stream), "flux clear");
   CK(cudaMemsetAsync(h->d_nsub.p, 0, ns * sizeof(int), h->stream), "attempts clear");
+  CK(cudaMemsetAsync(h->d_mindt.p, 0, ns * sizeof(double), h->stream), "substeps clear");
   if (h->prm.budgets)
     CK(cudaMemsetAsync(h->d_budget.p, 0, 4 * ns * sizeof(double), h->stream), "budget clear");
   CK(cudaMemcpyAsync(h->d_slot_col.p, h->slot_col.data(), ns * sizeof(int),
@@ -1396,6 +1408,20 @@ int sed_get_attempts(sed_handle* h, int* attempts) {
   for (int c = 0; c < h->ncol; c++) attempts[c] = 0;
   for (int s = 0; s < h->nslot; s++)
     if (h->slot_col[s] >= 0) attempts[h->slot_col[s]] = tmp[s];
+  return SED_OK;
+}
+
+int sed_get_min_dt(sed_handle* h, double* min_dt) {
+  if (!h || !min_dt) return SED_E_ARG;
+  if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
+  CK(cudaSetDevice(h->device), "set device");
+  std::vector<double> tmp(h->nslot);
+  CK(cudaMemcpyAsync(tmp.data(), h->d_mindt.p, tmp.size() * sizeof(double),
+                     cudaMemcpyDeviceToHost, h->stream), "substeps copy");
+  CK(cudaStreamSynchronize(h->stream), "min_dt");
+  for (int c = 0; c < h->ncol; c++) min_dt[c] = 0.0;
+  for (int s = 0; s < h->nslot; s++)
+    if (h->slot_col[s] >= 0) min_dt[h->slot_col[s]] = tmp[s];
   return SED_OK;
 }
 

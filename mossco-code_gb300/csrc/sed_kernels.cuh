@@ -642,6 +642,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
         // accepted surrogate step: state and surface flux already in place
         if (lane == 0) {
           s_nsub[j] = 0;
+          if (a.mindt) a.mindt[slot0 + j] = 0.0;
 #pragma unroll
           for (int d = 0; d < NDISS; d++) s_sflux[d * tcp + j] = a.sflux[d * ns + slot0 + j];
           for (int b = 0; b < 4; b++) s_bud[b * tc + j] = 0.0;
@@ -652,6 +653,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
         if (KIND == KIND_RESID && lane == 0) a.skip[slot0 + j] = 0;
         if (lane == 0) {
           s_nsub[j] = 0;
+          if (mode == 0 && KIND != KIND_RESID && a.mindt) a.mindt[slot0 + j] = 0.0;
 #pragma unroll
           for (int d = 0; d < NDISS; d++) s_sflux[d * tcp + j] = real(0);
           for (int b = 0; b < 4; b++) s_bud[b * tc + j] = 0.0;
@@ -750,6 +752,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
         for (int d = 0; d < NDISS; d++) s_sflux[d * tcp + j] = ftop[NPART + d];
         for (int b = 0; b < 4; b++) s_bud[b * tc + j] = bud[b];
         s_nsub[j] = r.attempts;
+        if (a.mindt) a.mindt[slot0 + j] = r.accepted > 0 ? r.min_dt : 0.0;
         atomicAdd(&b_att, (unsigned long long)r.attempts);
         atomicAdd(&b_acc, (unsigned long long)r.accepted);
         atomicAdd(&b_cols, 1ull);
@@ -823,6 +826,7 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
       // and surface flux are already in place
       if (lane == 0) {
         a.nsub[slot] = 0;
+        if (a.mindt) a.mindt[slot] = 0.0;
         if (!skipped)
           for (int d = 0; d < NDISS; d++) a.sflux[d * ns + slot] = real(0);
         if (a.budget)
@@ -879,6 +883,7 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
 #pragma unroll
       for (int d = 0; d < NDISS; d++) a.sflux[d * ns + slot] = ftop[NPART + d];
       a.nsub[slot] = r.attempts;
+      if (a.mindt) a.mindt[slot] = r.accepted > 0 ? r.min_dt : 0.0;
       if (a.budget)
         for (int b = 0; b < 4; b++) a.budget[b * ns + slot] = bud[b];
     }

@@ -27,6 +27,8 @@ struct ColumnArgs {
   real* sflux;
   double* budget;     // may be null
   int* nsub;          // [nslot] attempts of the last step
+  double* mindt;      // [nslot] smallest accepted substep of the last step
+                      // (0: no substep); may be null
   unsigned* queue;    // tile counter, zero before the launch
   DevStats* stats;
   // the launch covers slots [slot0, slot0 + ntiles * tc); tile0 indexes tile_k

@@ -112,6 +112,10 @@ module sed_gpu
       import :: c_int, c_ptr
       type(c_ptr), value :: h, temperature, surface, velocity, present
     end function
+    integer(c_int) function sed_get_min_dt(h, min_dt) bind(C, name='sed_get_min_dt')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, min_dt
+    end function
     integer(c_int) function sed_get_boundary(h, bdys, fluxes) bind(C, name='sed_get_boundary')
       import :: c_int, c_ptr
       type(c_ptr), value :: h, bdys, fluxes
@@ -146,7 +150,8 @@ module sed_gpu
 
   public :: sed_default_params, sed_gpu_init, sed_gpu_ode_solver, &
             sed_gpu_get_rhs, sed_gpu_finalize, sed_get_tuning, sed_set_tuning, &
-            sed_autotune, sed_set_boundary, sed_get_boundary, sed_spinup
+            sed_autotune, sed_set_boundary, sed_get_boundary, sed_spinup, &
+            sed_get_min_dt
 
 contains
 

@@ -127,6 +127,7 @@ SIGNATURES = {
     "sed_get_fluxes": (ctypes.c_int, [_H, _dp]),
     "sed_get_attempts": (ctypes.c_int, [_H, _ip]),
     "sed_get_budgets": (ctypes.c_int, [_H, _dp]),
+    "sed_get_min_dt": (ctypes.c_int, [_H, _dp]),
     "sed_set_stream": (ctypes.c_int, [_H, _vp]),
     "sed_host_register": (ctypes.c_int, [_vp, ctypes.c_size_t]),
     "sed_host_unregister": (ctypes.c_int, [_vp]),
@@ -411,6 +412,12 @@ class Solver:
         out = np.zeros(self.cs.ncol, dtype=np.int32)
         self._check(self.lib.sed_get_attempts(self.h, _p(out, _ip)),
                     "sed_get_attempts")
+        return out
+
+    def min_dt(self) -> np.ndarray:
+        """Smallest accepted substep of every column in the last step (s)."""
+        out = np.zeros(self.cs.ncol)
+        self._check(self.lib.sed_get_min_dt(self.h, _p(out)), "sed_get_min_dt")
         return out
 
     def budgets(self) -> np.ndarray:

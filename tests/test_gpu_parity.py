@@ -388,3 +388,34 @@ def test_boundary_assembly_errors():
     only_dissolved = np.array([0] * 6 + [1] * 5, dtype=np.int32)
     s.set_boundary(T, surf, None, only_dissolved)
     s.close()
+
+
+@pytest.mark.parametrize("cut", [capi.SED_CUT_PER_COLUMN, capi.SED_CUT_GLOBAL])
+def test_min_dt_per_column(oracle_mod, cut):
+    """The smallest accepted substep of every column in the last step (the
+    per-column form of last_min_dt, solver_library.F90:130-136) equals the
+    oracle's, column by column (per-column cut) or grid-wide (global cut)."""
+    cs = synth.make_workload("plain_cpu_10x10")
+    n = 30
+    s = capi.Solver(cs, precision=capi.SED_FP64, cut_scope=cut)
+    s.set_forcing()
+    s.set_state(cs.conc)
+    s.step(n - 1)
+    before = s.get_state()
+    st = s.step(1)
+    md = s.min_dt()
+    s.close()
+    assert md.min() == st["min_dt"]
+    if cut == capi.SED_CUT_GLOBAL:
+        sub = cs.copy()
+        sub.conc = before
+        c = before.copy()
+        rc, sref, _ = oracle_mod.OracleModel(sub).run(c, nsteps=1, percol=False)
+        assert np.all(md == sref["min_dt"])
+        return
+    for col in (0, 17, 42, 99):
+        sub = cs.subset([col])
+        c = np.ascontiguousarray(before[:, :, [col]])
+        rc, sref, _ = oracle_mod.OracleModel(sub).run(c, nsteps=1, percol=True)
+        assert rc == 0
+        assert md[col] == sref["min_dt"], col
