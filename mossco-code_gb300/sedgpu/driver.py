@@ -54,9 +54,22 @@ class TypeSed:
         self.nvar = NTR
         self.dt_min = 1.0e-9
         self.relative_change_min = -0.9
+        # absolute floor of the adaptive positivity test; 0 is the
+        # reference's purely relative test (solver_library.F90:121)
+        self.atol = 0.0
         self.bioturbation = 0.9
         self.diffusivity = 0.9
         self.bioturbation_profile = 1
+        # sed_nml bioturb_* (:226-231): Zhang & Wirtz profile 3 constants
+        self.bioturb_k_l = 0.11
+        self.bioturb_L1 = 0.2
+        self.bioturb_L2 = 0.6
+        self.bioturb_beta = 0.22
+        self.bioturb_b = 1.334
+        self.bioturb_dry_density = 1000.0
+        self.porosity_fac = 0.9
+        self.pom_flux_max = 2.0e4
+        self.missing_value = 1.0e20
         self.bcup_dissolved_variables = 2
         self.bcup_particulate_variables = 1
         self.mol_diff_mode = 0
@@ -96,7 +109,14 @@ class TypeSed:
                            mol_diff_mode=self.mol_diff_mode,
                            mol_diff_d0=self.mol_diff_d0, dt_min=self.dt_min,
                            relative_change_min=self.relative_change_min,
-                           minimum=self.minimum)
+                           atol=self.atol, minimum=self.minimum,
+                           bioturbation_profile=self.bioturbation_profile,
+                           bioturb_k_l=self.bioturb_k_l,
+                           bioturb_L1=self.bioturb_L1,
+                           bioturb_L2=self.bioturb_L2,
+                           bioturb_beta=self.bioturb_beta,
+                           bioturb_b=self.bioturb_b,
+                           bioturb_dry_density=self.bioturb_dry_density)
         return ColumnSet(inum=self.inum, jnum=self.jnum, kmax=self.knum,
                          kact=self.kact(), dz=g.dz, dzc=g.dzc, zc=g.zc,
                          zi=g.zi, phi=self.porosity,
@@ -108,9 +128,12 @@ class TypeSed:
 
     def solver(self) -> Solver:
         key = (self.cut_scope, self.precision, self.dt_min,
-               self.relative_change_min, self.bcup_dissolved_variables,
+               self.relative_change_min, self.atol, self.bcup_dissolved_variables,
                self.bcup_particulate_variables, tuple(sorted(self.bgc.items())),
                self.diffusivity, self.bioturbation, self.mol_diff_mode,
+               self.bioturbation_profile, self.bioturb_k_l, self.bioturb_L1,
+               self.bioturb_L2, self.bioturb_beta, self.bioturb_b,
+               self.bioturb_dry_density,
                id(self.porosity), id(self.grid.dz), id(self.mask))
         if self._solver is None or self._solver_key != key:
             if self._solver is not None:
@@ -137,23 +160,56 @@ def init_grid(grid: SedGrid, dzmin: Optional[float] = None) -> None:
     grid.dzc = np.ascontiguousarray(grid.zc[1:] - grid.zc[:-1])
 
 
-def update_porosity(sed: TypeSed) -> None:
-    """Masked cells to porosity 1 and the interface porosity
-    (fabm_sediment_driver.F90:430-435)."""
-    sed.porosity = np.where(sed.mask > 0, 1.0, sed.porosity)
-    phi_i = np.empty_like(sed.porosity)
-    phi_i[0] = sed.porosity[0]
-    phi_i[1:] = 0.5 * (sed.porosity[:-1] + sed.porosity[1:])
+def update_porosity(sed: TypeSed, from_surface: bool = False,
+                    reinitialize_concentrations: bool = False) -> None:
+    """type_sed%update_porosity (fabm_sediment_driver.F90:393-442).
+
+    from_surface: porosity below the top layer from the top layer's value,
+    phi(k) = phi(1) * (1 - porosity_fac * (zc(k) - zc(1))), and the POM flux
+    cap recomputed with its downward-monotone limit (:408-428).  Then, always:
+    masked cells get porosity 1 (:431) and the interface porosity is
+    phi_i(1) = phi(1), phi_i(k) = (phi(k-1) + phi(k)) / 2 (:434-435).
+    reinitialize_concentrations: init_concentrations again from the initial
+    values last given to it, if concentrations exist (:438-440)."""
+    g = sed.grid
+    phi = np.array(sed.porosity, dtype=np.float64)
+    if from_surface:
+        for k in range(1, g.knum):
+            phi[k] = phi[0] * (1.0 - sed.porosity_fac * (g.zc[k] - g.zc[0]))
+        sed.flux_cap = _flux_cap(sed.pom_flux_max, phi, g.dz)
+    phi = np.where(sed.mask > 0, 1.0, phi)
+    phi_i = np.empty_like(phi)
+    phi_i[0] = phi[0]
+    phi_i[1:] = 0.5 * (phi[:-1] + phi[1:])
+    sed.porosity = phi
     sed.intf_porosity = phi_i
+    if reinitialize_concentrations and sed.conc is not None:
+        init_concentrations(sed, getattr(sed, "initial_values", None))
+
+
+def _flux_cap(pom_flux_max: float, phi: np.ndarray, dz: np.ndarray) -> np.ndarray:
+    """POM flux cap per layer, each layer from the third down capped by the
+    one above (fabm_sediment_driver.F90:284-291, :419-426)."""
+    cap = pom_flux_max / 86400.0 * (1.0 - phi) * dz
+    for k in range(2, cap.shape[0]):
+        cap[k] = np.minimum(cap[k], cap[k - 1])
+    return cap
 
 
 def initialize(sed: TypeSed, sed_nml: Optional[dict] = None) -> None:
     """Porosity, flux cap and bioturbation profile from the sed_nml values
-    (fabm_sediment_driver.F90:211-304; defaults :217-231)."""
+    (fabm_sediment_driver.F90:211-304; defaults :217-231).  Profile 1 is a
+    linear decrease to bioturbation_min at bioturbation_depth, 2 an
+    exponential decrease, any other value a factor of 1 (:294-303)."""
     nml = dict(diffusivity=0.9, bioturbation=0.9, bioturbation_profile=1,
                bioturbation_depth=5.0, bioturbation_min=0.2, porosity_max=0.7,
                porosity_fac=0.9, k_par=2.0e-3, pom_flux_max=2.0e4,
-               distributed_pom_flux=False)
+               distributed_pom_flux=False, bioturb_k_l=0.11, bioturb_L1=0.2,
+               bioturb_L2=0.6, bioturb_beta=0.22, bioturb_b=1.334,
+               bioturb_dry_density=1000.0)
+    unknown = set(sed_nml or {}) - set(nml)
+    if unknown:
+        raise ValueError(f"unknown sed_nml entries: {sorted(unknown)}")
     nml.update(sed_nml or {})
     if sed.grid.dz is None:
         init_grid(sed.grid)
@@ -162,11 +218,13 @@ def initialize(sed: TypeSed, sed_nml: Optional[dict] = None) -> None:
     sed.bioturbation = nml["bioturbation"]
     sed.bioturbation_profile = nml["bioturbation_profile"]
     sed.k_par = nml["k_par"]
+    sed.porosity_fac = nml["porosity_fac"]
+    sed.pom_flux_max = nml["pom_flux_max"]
+    for name in ("bioturb_k_l", "bioturb_L1", "bioturb_L2", "bioturb_beta",
+                 "bioturb_b", "bioturb_dry_density"):
+        setattr(sed, name, nml[name])
     sed.bcup_particulate_variables = 4 if nml["distributed_pom_flux"] else 1
     phi = nml["porosity_max"] * (1.0 - nml["porosity_fac"] * g.zc)
-    cap = nml["pom_flux_max"] / 86400.0 * (1.0 - phi) * g.dz
-    for k in range(2, g.knum):
-        cap[k] = np.minimum(cap[k], cap[k - 1])
     prof = nml["bioturbation_profile"]
     if prof == 1:
         lin = np.maximum(nml["bioturbation_depth"] - 100.0 * g.zi[:g.knum], 0.0)
@@ -177,17 +235,26 @@ def initialize(sed: TypeSed, sed_nml: Optional[dict] = None) -> None:
     else:
         bf = np.ones_like(phi)
     sed.porosity = phi
-    sed.flux_cap = cap
+    sed.flux_cap = _flux_cap(nml["pom_flux_max"], phi, g.dz)
     sed.bioturbation_factor = bf
-    update_porosity(sed)
+    update_porosity(sed, from_surface=False)
 
 
-def init_concentrations(sed: TypeSed, initial_values) -> None:
-    """conc = initial_value / porosity, masked cells at the missing value
-    1e20 (fabm_sediment_driver.F90:449-468)."""
+def init_concentrations(sed: TypeSed, initial_values=None) -> None:
+    """type_sed%init_concentrations (fabm_sediment_driver.F90:449-467):
+    conc = initial_value / porosity, the namelist values being per total
+    cell volume; masked cells at sed.missing_value (1e20, :85).  initial_values has one
+    entry per tracer; None reuses the last values given."""
+    if initial_values is None:
+        initial_values = getattr(sed, "initial_values", None)
+        if initial_values is None:
+            raise ValueError("init_concentrations: no initial values")
     iv = np.asarray(initial_values, dtype=np.float64)
+    if iv.shape != (sed.nvar,):
+        raise ValueError(f"initial_values must have {sed.nvar} entries, got {iv.shape}")
+    sed.initial_values = iv.copy()
     conc = iv[:, None, None] / sed.porosity[None, :, :]
-    conc = np.where((sed.mask > 0)[None], 1.0e20, conc)
+    conc = np.where((sed.mask > 0)[None], sed.missing_value, conc)
     sed.conc = np.ascontiguousarray(conc)
 
 
