@@ -220,7 +220,16 @@ def _coupled_sed(profile, precision):
 @pytest.mark.parametrize("profile", [1, 2, 3])
 @pytest.mark.parametrize("method", [ADAPTIVE_EULER, RUNGE_KUTTA_4])
 def test_driver_ode_solver_fp64_matches_oracle(oracle_mod, profile, method):
+    """Bit for bit for the static profiles.  Profile 3 takes CUDA's pow,
+    which may differ from the CPU's in the last bit: 1e-9 relative there."""
     sed = _coupled_sed(profile, capi.SED_FP64)
+
+    def same(got, want):
+        if profile != 3:
+            np.testing.assert_array_equal(got, want)
+        else:
+            np.testing.assert_allclose(got, want, rtol=1e-9, atol=0.0)
+
     cs = sed.to_columns()
     ref = np.ascontiguousarray(sed.conc.copy())
     om = oracle_mod.OracleModel(cs)
@@ -231,12 +240,16 @@ def test_driver_ode_solver_fp64_matches_oracle(oracle_mod, profile, method):
         rc, _, fl_ref = om.run(ref, nsteps=1, dt=dt, method=method, fluxes=fl_ref)
         assert rc == 0
         act = np.arange(sed.knum)[:, None] < sed.kact()[None, :]
-        np.testing.assert_array_equal(sed.conc[:, act], ref[:, act])
+        same(sed.conc[:, act], ref[:, act])
     # masked cells keep the missing value
     assert np.all(sed.conc[:, sed.mask > 0] == 1.0e20)
     rhs = driver.get_rhs(sed)
     rref, _, _ = om.get_rhs(sed.conc)
-    np.testing.assert_array_equal(rhs[:, act], rref[:, act])
+    scale = np.abs(rref[:, act]).max(axis=1, keepdims=True)
+    if profile != 3:
+        np.testing.assert_array_equal(rhs[:, act], rref[:, act])
+    else:
+        assert np.max(np.abs(rhs[:, act] - rref[:, act]) / scale) < 1e-13
     sed.solver().close()
 
 
