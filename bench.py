@@ -46,6 +46,8 @@ L2_BYTES = 129 * 1024 * 1024
 # kernel from an ncu capture at day 10 of the run
 # (profiles/k_column_warp_plain_gpu_256x256.md)
 MEASURED_TRAFFIC = {"plain_gpu_256x256": 166.7e6}
+# the same for one Run of the pelagic kernel (set from an ncu capture)
+PEL_TRAFFIC = {}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -586,6 +588,207 @@ def run_gpu(args) -> None:
         dist.destroy_process_group()
 
 
+PEL_METRIC = "pelagic water-column Runs/s on 1 GB300 (fabm_pelagic driver, gotm_npzd)"
+PEL_WORKLOAD = "pelagic_1024x1024"
+
+
+def pel_bytes(pcs, rsize: int = 4) -> int:
+    """Bytes one Run must move: state read + write (2 r 4 per water cell),
+    layer height (r) and mask (1) per cell, I_0 and albedo (2 r) and the
+    bottom and surface flux rows (2 r 4) per column."""
+    cells = pcs.knum * pcs.ncol
+    water = int(pcs.water().sum())
+    return int(2 * rsize * 4 * water + (rsize + 1) * cells + 2 * rsize * pcs.ncol
+               + 2 * rsize * 4 * pcs.ncol)
+
+
+def pel_cpu(pcs, nruns: int, threads: int, max_columns: int, target_s: float = 15.0):
+    """The pelagic oracle (all host threads) on an evenly spaced column
+    sample sized, from a pilot, to about target_s seconds: the whole grid
+    and more Runs when one Run of it is shorter than that."""
+    import pel_oracle
+
+    def timed(n, runs):
+        cols = np.unique(np.linspace(0, pcs.ncol - 1, n).astype(np.int64))
+        sub = pcs.subset(cols)
+        c = sub.conc.copy()
+        t0 = time.perf_counter()
+        rc, _, _ = pel_oracle.PelOracle(sub).run(c, nthreads=threads, nruns=runs)
+        return sub, time.perf_counter() - t0, rc
+    n0 = min(max(64 * threads, 256), max_columns, pcs.ncol)
+    sub, secs, rc = timed(n0, 1)
+    per_col = secs / n0
+    n = int(min(max_columns, pcs.ncol, max(n0, target_s / max(per_col, 1e-9))))
+    nruns = max(nruns, int(target_s / max(per_col * n, 1e-9)))
+    if n > 1.5 * n0 or nruns > 1:
+        sub, secs, rc = timed(n, nruns)
+    val = sub.water_columns() * nruns / secs
+    return {"value": val, "unit": "column-runs/s", "cores": threads, "kind": "port",
+            "sample": (f"{sub.water_columns()} water columns of {pcs.ncol} (evenly spaced), "
+                       f"{nruns} Runs, {secs:.1f} s"), "seconds": secs, "status": rc,
+            "runs": nruns}
+
+
+def run_pelagic(args) -> None:
+    """The pelagic driver path: Runs of the component (light, 10 internal
+    RUNGE_KUTTA_4 steps of 360 s with their epilogues) on every water column
+    of a 1024 x 1024 grid, FP32 state resident in HBM."""
+    import torch
+    from sedgpu import capi, pelagic
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    pcs = pelagic.make_pelagic_workload(args.workload if args.workload != WORKLOAD
+                                        else PEL_WORKLOAD, seed=args.seed + 7919 * rank)
+    p = pcs.params(capi.SED_FP32)
+    p.device = local
+    s = pelagic.PelagicSolver(pcs, params=p)
+    s.set_state(pcs.conc)
+    runs = args.steps or pcs.nruns
+    for _ in range(args.warmup):
+        s.step(1)
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    dev_ms = 0.0
+    launches = 0
+    t0 = time.perf_counter()
+    for _ in range(runs):
+        st = s.step(1)
+        dev_ms += st["device_ms"]
+        launches += st["gpu_launches"]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([dev_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms = float(t.item())
+        dist.barrier()
+    clk = clocks.stop()
+    wcols = pcs.water_columns()
+    value = world * wcols * runs / (dev_ms / 1e3)
+
+    # accuracy: one FP32 Run against the FP64 device path (bit-identical to
+    # the FP64 CPU restatement) from the same state on a column sample
+    S = s.get_state()
+    cols = np.unique(np.linspace(0, pcs.ncol - 1, min(4096, pcs.ncol)).astype(np.int64))
+    sub = pcs.subset(cols)
+    sub.conc = np.ascontiguousarray(S[:, :, cols])
+    outs = []
+    for prec in (capi.SED_FP32, capi.SED_FP64):
+        ss = pelagic.PelagicSolver(sub, precision=prec)
+        ss.set_state(sub.conc)
+        ss.step(1)
+        outs.append(ss.get_state())
+        ss.close()
+    w = sub.water()
+    errs = [float(np.max(np.abs(outs[0][n][w] - outs[1][n][w]) /
+                         max(np.abs(outs[1][n][w]).max(), 1e-300))) for n in range(4)]
+
+    e2e = None
+    if not args.no_e2e:
+        conc = np.array(pcs.conc, dtype=np.float64, copy=True)
+        capi.host_register(conc)
+        for _ in range(args.warmup):
+            s.run(conc)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for _ in range(runs):
+            s.run(conc)
+        e2e_s = time.perf_counter() - t1
+        capi.host_unregister(conc)
+        e2e = {"value": world * wcols * runs / e2e_s, "unit": "column-runs/s",
+               "h2d_bytes_per_step": int(conc.nbytes), "d2h_bytes_per_step": int(conc.nbytes),
+               "steps": runs, "call": "pel_run"}
+    s.close()
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    ms = dev_ms / runs
+    bytes_run = pel_bytes(pcs)
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_run / (ms / 1e3) / 1e9
+    cells = int(pcs.water().sum())
+    nsub = int(np.ceil(pcs.t_couple / pcs.dt))
+    # FP32 work per cell and internal step of RUNGE_KUTTA_4: 4 rate
+    # evaluations of ~35 flops (plus one exp and one division each) and
+    # ~52 flops of stage updates
+    flops = cells * nsub * (4 * 35 + 52)
+    sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    cpu = None
+    if not args.no_cpu:
+        cpu = pel_cpu(pcs, 1, os.cpu_count() or 1, pcs.ncol)
+        for k in ("seconds", "status", "runs"):
+            cpu.pop(k)
+    line = {
+        "metric": PEL_METRIC, "value": value, "unit": "column-runs/s", "n_gpus": world,
+        "steps": runs, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32", "data": "synthetic (seeded)",
+        "config": {"workload": PEL_WORKLOAD, "columns": pcs.ncol, "water_columns": wcols,
+                   "layers": pcs.knum, "tracers": 4, "model": "gotm_npzd",
+                   "t_couple_s": pcs.t_couple, "dt_s": pcs.dt, "method": "runge_kutta_4",
+                   "state": "fp32",
+                   "l2": "inputs larger than L2 (state 0.5 GB)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": PEL_TRAFFIC.get(PEL_WORKLOAD),
+                     "peak_kind": peak_kind, "bytes_per_launch": bytes_run,
+                     "kernel": "k_pel_run<float,float,RK4,light,epilogue>"},
+        "compute": {"fp32_tflops_est": flops / (ms / 1e3) / 1e12,
+                    "fp32_peak_tflops": fp32_peak,
+                    "frac": flops / (ms / 1e3) / 1e12 / fp32_peak,
+                    "note": "nominal 152 SM x 128 FMA/clk at the sampled clock"},
+        "accuracy": {"max_rel_err_per_tracer": errs, "max_rel_err": max(errs),
+                     "columns": int(len(cols)),
+                     "reference": "FP64 device path (bit-identical to the FP64 CPU "
+                                  "restatement), one Run from the same state",
+                     "scale": "tracer max"},
+        "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches,
+        "clocks": clk, "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_reference_pelagic(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import pel_oracle
+    pel_oracle.build()
+    from sedgpu import pelagic
+    pcs = pelagic.make_pelagic_workload(PEL_WORKLOAD, seed=args.seed)
+    runs = args.steps or 1
+    cpu = pel_cpu(pcs, runs, os.cpu_count() or 1, pcs.ncol)
+    line = {
+        "metric": PEL_METRIC, "value": cpu["value"], "unit": "column-runs/s",
+        "n_gpus": args.gpus, "steps": cpu["runs"], "warmup": args.warmup,
+        "ms_per_step": cpu["seconds"] * 1e3 / cpu["runs"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+        "data": "synthetic (seeded)", "impl": "reference",
+        "config": {"workload": PEL_WORKLOAD, "layers": pcs.knum, "tracers": 4,
+                   "model": "gotm_npzd", "t_couple_s": pcs.t_couple, "dt_s": pcs.dt,
+                   "method": "runge_kutta_4"},
+        "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": cpu["value"], "unit": "column-runs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": ("reference algorithm as the FP64 C restatement on the host cores; the "
+                 "Fortran reference and FABM cannot be built on this machine"),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -612,10 +815,17 @@ def main():
     ap.add_argument("--spinup-years", type=float, default=0.0,
                     help="time sed_spinup's 1-column model for this many years instead")
     ap.add_argument("--spinup-cpu-steps", type=int, default=2000)
+    ap.add_argument("--path", default="sediment", choices=["sediment", "pelagic"],
+                    help="pelagic: the fabm_pelagic driver path instead")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
-    if args.impl == "reference":
+    if args.path == "pelagic":
+        if args.impl == "reference":
+            run_reference_pelagic(args)
+        else:
+            run_pelagic(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.spinup_years > 0:
         run_spinup(args)
