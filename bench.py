@@ -46,8 +46,9 @@ L2_BYTES = 129 * 1024 * 1024
 # kernel from an ncu capture at day 10 of the run
 # (profiles/k_column_warp_plain_gpu_256x256.md)
 MEASURED_TRAFFIC = {"plain_gpu_256x256": 166.7e6}
-# the same for one Run of the pelagic kernel (set from an ncu capture)
-PEL_TRAFFIC = {}
+# the same for one Run of the pelagic kernel
+# (profiles/k_pel_run_pelagic_1024x1024.md)
+PEL_TRAFFIC = {"pelagic_1024x1024": 1379.4e6}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -593,13 +594,14 @@ PEL_WORKLOAD = "pelagic_1024x1024"
 
 
 def pel_bytes(pcs, rsize: int = 4) -> int:
-    """Bytes one Run must move: state read + write (2 r 4 per water cell),
-    layer height (r) and mask (1) per cell, I_0 and albedo (2 r) and the
-    bottom and surface flux rows (2 r 4) per column."""
-    cells = pcs.knum * pcs.ncol
+    """Bytes one Run must move: state read + write (2 r 4) and the PAR the
+    handle keeps for later driver calls (r) per water cell, layer height (r)
+    and mask (1) per cell of a water column, I_0 and albedo (2 r) and the
+    bottom and surface flux rows (2 r 4) per water column."""
     water = int(pcs.water().sum())
-    return int(2 * rsize * 4 * water + (rsize + 1) * cells + 2 * rsize * pcs.ncol
-               + 2 * rsize * 4 * pcs.ncol)
+    wcols = pcs.water_columns()
+    return int(2 * rsize * 4 * water + rsize * water + (rsize + 1) * pcs.knum * wcols
+               + 2 * rsize * wcols + 2 * rsize * 4 * wcols)
 
 
 def pel_cpu(pcs, nruns: int, threads: int, max_columns: int, target_s: float = 15.0):
