@@ -325,6 +325,65 @@ def run_spinup(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def ensemble_sets(cs, seed: int) -> np.ndarray:
+    """[SED_NBGC][ncol]: the workload's parameter set with the labile and
+    semilabile decay rates, the oxic half saturation and the nitrification
+    rate of each column scaled by exp(U[-0.7, 0.7]) (a factor of 2 either
+    way), counter-based per column."""
+    from sedgpu import synth
+    from sedgpu.model import BGC_NAMES
+    tab = cs.bgc_columns().copy()
+    idx = np.arange(cs.ncol, dtype=np.int64)
+    for f, name in enumerate(("rLabile", "rSemilabile", "ksO2oxic", "rnit")):
+        u = synth.uniform(seed, 200 + f, idx)
+        tab[BGC_NAMES.index(name)] *= np.exp(-0.7 + 1.4 * u)
+    return tab
+
+
+def run_ensemble_spinup(args) -> None:
+    """An ensemble spin-up: --ensemble parameter sets as the columns of one
+    grid (sed_set_column_bgc), all spun up together for --spinup-years of
+    hourly steps by sed_spinup's all-columns mode, against the oracle with
+    every host thread on a bounded sample of the same sets and steps."""
+    import torch
+    import oracle
+    from sedgpu import capi, synth
+    torch.cuda.set_device(0)
+    n = args.ensemble
+    cs = synth.make_workload(args.workload, cols=np.zeros(n, dtype=np.int64))
+    tab = ensemble_sets(cs, args.seed)
+    cs.bgc_col = tab
+    nsteps = int(round(args.spinup_years * 8760))
+    s = capi.Solver(cs)
+    s.set_forcing()
+    s.set_state(cs.conc)
+    s.spinup(24, capi.SED_SPINUP_ALL)   # warm
+    s.set_state(cs.conc)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st = s.spinup(nsteps, capi.SED_SPINUP_ALL)
+    gpu_s = time.perf_counter() - t0
+    s.close()
+    threads = os.cpu_count() or 1
+    m = min(n, max(4 * threads, 64))
+    sub = cs.subset(np.arange(m))
+    cpu_steps = min(nsteps, args.spinup_cpu_steps)
+    c = sub.conc.copy()
+    t0 = time.perf_counter()
+    rc, _, _ = oracle.OracleModel(sub).run(c, nsteps=cpu_steps, percol=True, nthreads=threads)
+    cpu_s = time.perf_counter() - t0
+    line = {"metric": "ensemble spin-up", "unit": "parameter-set years/s",
+            "workload": f"{n} parameter sets on column 0 of {args.workload} "
+                        f"({cs.kmax} layers), {args.spinup_years} years of 3600 s steps",
+            "gpu_fp32": {"seconds": gpu_s, "value": n * args.spinup_years / gpu_s,
+                         "attempts_per_column_step": st["attempts"] / max(st["column_steps"], 1),
+                         "gpu_launches": st["gpu_launches"]},
+            "cpu_oracle": {"value": m * cpu_steps / 8760 / cpu_s, "cores": threads,
+                           "sample": f"{m} sets x {cpu_steps} steps, {cpu_s:.1f} s",
+                           "status": rc}}
+    print(json.dumps(line), flush=True)
+
+
 def coupled_e2e(s, cs, warmup, nsteps, world):
     """Coupling steps with the state resident on the device: each step takes
     the pelagic fields at the soil surface in (sed_set_boundary), steps, and
@@ -817,6 +876,8 @@ def main():
     ap.add_argument("--spinup-years", type=float, default=0.0,
                     help="time sed_spinup's 1-column model for this many years instead")
     ap.add_argument("--spinup-cpu-steps", type=int, default=2000)
+    ap.add_argument("--ensemble", type=int, default=0,
+                    help="with --spinup-years: spin up this many parameter sets at once")
     ap.add_argument("--path", default="sediment", choices=["sediment", "pelagic"],
                     help="pelagic: the fabm_pelagic driver path instead")
     args = ap.parse_args()
@@ -829,6 +890,8 @@ def main():
             run_pelagic(args)
     elif args.impl == "reference":
         run_reference(args)
+    elif args.spinup_years > 0 and args.ensemble > 0:
+        run_ensemble_spinup(args)
     elif args.spinup_years > 0:
         run_spinup(args)
     elif args.solver == "surrogate":

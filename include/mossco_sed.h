@@ -220,6 +220,19 @@ int sed_get_attempts(sed_handle *h, int *attempts);
  * minimum and its column are the minimum and argmin of this array. */
 int sed_get_min_dt(sed_handle *h, double *min_dt);
 
+/* Ensembles (no counterpart in the reference, whose rates take the one
+ * parameter set of fabm_sed.nml): an OMEXDIA+P parameter set per column,
+ * params[SED_NBGC][ncol] in sed_params' order and units (rLabile ...
+ * kinO2anox, per day), so that many parameter sets -- a calibration, a
+ * sensitivity study, an ensemble spin-up with SED_SPINUP_ALL -- run as the
+ * columns of one grid in one launch.  NULL returns every column to the
+ * handle's set.  With per-column sets the handle steps with the
+ * warp-direct kernels (tile width 0; sed_set_tuning refuses others) and
+ * per-column cuts; sed_get_rhs and the surrogate step answer SED_E_STATE.
+ * A column whose set equals the handle's gives the same bits as without. */
+#define SED_NBGC 17
+int sed_set_column_bgc(sed_handle *h, const double *params);
+
 /* FP64 budgets of the last step, [4][ncol]: P inventory, P residual,
  * N inventory, N residual (mmol/m2).  Requires params.budgets. */
 int sed_get_budgets(sed_handle *h, double *budgets);

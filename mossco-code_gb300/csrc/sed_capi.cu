@@ -95,6 +95,9 @@ struct sed_handle {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::string err;
   bool have_grid = false, have_forcing = false, have_state = false;
+  // per-column OMEXDIA+P parameter sets (sed_set_column_bgc), [SED_NBGC][ncol]
+  bool has_bgc = false;
+  std::vector<double> bgc_cols;
   // slots: depth class, then column segment, then active layers
   int nslot = 0, nactive = 0;
   std::vector<int> slot_col, slot_k;
@@ -107,6 +110,7 @@ struct sed_handle {
   cudaEvent_t pe_start = nullptr, pe_done = nullptr;
   cudaEvent_t pe_in[kMaxSeg] = {}, pe_cmp[kMaxSeg] = {};
   // device buffers
+  DevBuf d_bgc;  // [NBGC_DEV][nslot] derived per-slot rate parameters
   DevBuf d_slot_col, d_kact, d_tile_k, d_conc, d_coef, d_cap, d_force, d_sflux,
       d_budget, d_nsub, d_queue, d_stats, d_flag, d_stage, d_bdys, d_fluxes,
       d_rhs, d_rhs_stage, d_grid, d_force64, d_prop, d_skip, d_xfeat, d_yhat, d_backup,
@@ -197,6 +201,7 @@ ColumnArgs<real> column_args(sed_handle* h, const Bin& b, int bin_index,
   a.ntiles = b.tc ? b.nslots / b.tc : b.nslots;
   a.dt = dt;
   a.method = method;
+  a.bgc = h->has_bgc ? h->d_bgc.as<real>() : nullptr;
   return a;
 }
 
@@ -394,8 +399,11 @@ int step_global(sed_handle* h, double dt) {
 
 template <typename real>
 int step_any(sed_handle* h, double dt, int method) {
-  if (method == SED_ADAPTIVE_EULER && h->prm.cut_scope == SED_CUT_GLOBAL)
+  if (method == SED_ADAPTIVE_EULER && h->prm.cut_scope == SED_CUT_GLOBAL) {
+    if (h->has_bgc)
+      return h->fail(SED_E_STATE, "per-column parameter sets need per-column cuts");
     return step_global<real>(h, dt);
+  }
   return step_percol<real>(h, dt, method);
 }
 
@@ -518,6 +526,36 @@ int class_occupancy(sed_handle* h, const Bin& b, int tc, int threads) {
 
 // Occupancy and per-tile layer counts of the current tuning; raises the
 // kernels' shared-memory limit before any capture and drops the step graph.
+// The per-slot table of derived rate parameters of the ensemble: each
+// column's sed_params set through make_params, so a column with the
+// handle's own set gets the bits of the uniform path.
+template <typename real>
+int upload_bgc(sed_handle* h) {
+  const int ns = h->nslot, nc = h->ncol;
+  std::vector<real> tab((size_t)NBGC_DEV * ns);
+  Params<real> base = make_params<real>(h->prm);
+  for (int s = 0; s < ns; s++) {
+    const int c = h->slot_col[s];
+    Params<real> q = base;
+    if (c >= 0) {
+      sed_params sp = h->prm;
+      double* f[SED_NBGC] = {&sp.rLabile, &sp.rSemilabile, &sp.NCrLdet, &sp.NCrSdet,
+                             &sp.PAds, &sp.PAdsODU, &sp.NH3Ads, &sp.CprodMax, &sp.rnit,
+                             &sp.ksO2nitri, &sp.rODUox, &sp.ksO2oduox, &sp.ksO2oxic,
+                             &sp.ksNO3denit, &sp.kinO2denit, &sp.kinNO3anox, &sp.kinO2anox};
+      for (int i = 0; i < SED_NBGC; i++) *f[i] = h->bgc_cols[(size_t)i * nc + c];
+      q = make_params<real>(sp);
+    }
+    for (int i = 0; i < NBGC_DEV; i++) tab[(size_t)i * ns + s] = *bgc_field(q, i);
+  }
+  CK(h->d_bgc.alloc(tab.size() * sizeof(real)), "parameter sets");
+  CK(cudaMemcpyAsync(h->d_bgc.p, tab.data(), tab.size() * sizeof(real), cudaMemcpyHostToDevice,
+                     h->stream),
+     "parameter sets copy");
+  CK(cudaStreamSynchronize(h->stream), "parameter sets copy");
+  return SED_OK;
+}
+
 int apply_tuning(sed_handle* h) {
   std::vector<int> tile_k;
   for (int b = 0; b < 2; b++) {
@@ -747,6 +785,7 @@ int autotune_t(sed_handle* h, double dt, int method, int flags, sed_tuning* out)
     float best_ms = 1e30f;
     for (int tc : tcs)
       for (int th : thr) {
+        if (tc > 0 && h->has_bgc) continue;  // ensembles step warp-direct only
         if (tc > 0) {
           const int occ = class_occupancy(h, bin, tc, th);
           if (occ <= 0 || bin.nslots < tc) continue;
@@ -1088,6 +1127,11 @@ int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
     CK(cudaStreamSynchronize(h->stream), "column map");
   }
   CK(h->d_tile_k.alloc((size_t)(h->nslot / 8 + 1) * sizeof(int)), "tile_k");
+  if (h->has_bgc) {  // the ensemble's table follows the new layout
+    h->bins[0].tc = h->bins[1].tc = 0;
+    int rc = h->fp64() ? upload_bgc<double>(h) : upload_bgc<float>(h);
+    if (rc) return rc;
+  }
   {
     int rc = apply_tuning(h);
     if (rc) return rc;
@@ -1271,6 +1315,7 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
   int rc = ready(h);
   if (rc) return rc;
   if (!s) return h->fail(SED_E_ARG, "no surrogate");
+  if (h->has_bgc) return h->fail(SED_E_STATE, "the surrogate has no per-column parameter sets");
   if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");
   if (h->fp64()) return h->fail(SED_E_ARG, "the surrogate step runs on FP32 state");
   if (s->device != h->device) return h->fail(SED_E_ARG, "surrogate on another device");
@@ -1358,6 +1403,7 @@ int sed_get_rhs(sed_handle* h, const double* conc, double* rhs, double* fluxes) 
   if (!h) return SED_E_ARG;
   if ((rc = ready(h))) return rc;
   if (!conc || !rhs) return h->fail(SED_E_ARG, "conc and rhs are required");
+  if (h->has_bgc) return h->fail(SED_E_STATE, "sed_get_rhs has no per-column parameter sets");
   CK(cudaSetDevice(h->device), "set device");
   const size_t n = (size_t)NTR * h->kmax * h->nslot * h->rsize();
   CK(h->d_rhs.alloc(n), "rhs buffer");
@@ -1422,6 +1468,46 @@ int sed_get_min_dt(sed_handle* h, double* min_dt) {
   for (int c = 0; c < h->ncol; c++) min_dt[c] = 0.0;
   for (int s = 0; s < h->nslot; s++)
     if (h->slot_col[s] >= 0) min_dt[h->slot_col[s]] = tmp[s];
+  return SED_OK;
+}
+
+int sed_set_column_bgc(sed_handle* h, const double* params) {
+  if (!h) return SED_E_ARG;
+  if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
+  CK(cudaSetDevice(h->device), "set device");
+  if (!params) {
+    h->has_bgc = false;
+    h->bgc_cols.clear();
+    h->d_bgc.release();
+    reset_graph(h);
+    return SED_OK;
+  }
+  const size_t nc = (size_t)h->ncol;
+  for (int i = 0; i < SED_NBGC; i++)
+    for (size_t c = 0; c < nc; c++) {
+      const double v = params[i * nc + c];
+      if (!(v >= 0.0) || !std::isfinite(v))
+        return h->fail(SED_E_ARG, "parameter %d of column %zu is negative or not finite", i, c);
+    }
+  if (h->prm.cut_scope == SED_CUT_GLOBAL)
+    return h->fail(SED_E_ARG, "per-column parameter sets need per-column cuts");
+  h->bgc_cols.assign(params, params + SED_NBGC * nc);
+  h->has_bgc = true;
+  // ensembles step with the warp-direct kernels
+  Bin keep[2] = {h->bins[0], h->bins[1]};
+  h->bins[0].tc = h->bins[1].tc = 0;
+  int rc = h->fp64() ? upload_bgc<double>(h) : upload_bgc<float>(h);
+  if (!rc) rc = apply_tuning(h);
+  if (rc) {
+    const std::string why = h->err;
+    h->has_bgc = false;
+    h->bins[0] = keep[0];
+    h->bins[1] = keep[1];
+    apply_tuning(h);
+    h->err = why;
+    return rc;
+  }
+  reset_graph(h);
   return SED_OK;
 }
 
@@ -1681,6 +1767,8 @@ int sed_set_tuning(sed_handle* h, const sed_tuning* t) {
       return h->fail(SED_E_ARG, "tile_columns[%d]=%d: 0 (warp-direct), 8, 16, 32 or 64", b, tc);
     if (th < 64 || th > 256 || th % 64 != 0)
       return h->fail(SED_E_ARG, "threads[%d]=%d: 64, 128, 192 or 256", b, th);
+    if (tc != 0 && h->has_bgc)
+      return h->fail(SED_E_ARG, "per-column parameter sets step warp-direct only (tile 0)");
     if (t->blocks_per_sm[b] < 0) return h->fail(SED_E_ARG, "blocks_per_sm[%d] < 0", b);
   }
   const int pc = t->pipeline_chunks;

@@ -71,6 +71,40 @@ struct Params {
   real toc_f1, toc_f2, bio_beta, bio_b, bio_L1, bio_L2;
 };
 
+// The rate parameters of Params that a per-column parameter set replaces,
+// in the order of the per-slot table.
+constexpr int NBGC_DEV = 16;
+
+template <typename real>
+__host__ __device__ __forceinline__ real* bgc_field(Params<real>& p, int i) {
+  real* f[NBGC_DEV] = {&p.rF, &p.rS, &p.cmax, &p.rnit, &p.rodu, &p.pads, &p.ksO2oxic,
+                       &p.kinO2denit, &p.ksNO3denit, &p.kinO2anox, &p.kinNO3anox,
+                       &p.ksO2nitri, &p.ksO2oduox, &p.PAdsODU, &p.nh3fac, &p.nh3den};
+  return f[i];
+}
+
+// The column's parameter set from the per-slot table (warp-uniform loads).
+template <typename real>
+__device__ __forceinline__ void load_bgc(Params<real>& p, const real* __restrict__ tab,
+                                         size_t ns, int slot) {
+  p.rF = tab[0 * ns + slot];
+  p.rS = tab[1 * ns + slot];
+  p.cmax = tab[2 * ns + slot];
+  p.rnit = tab[3 * ns + slot];
+  p.rodu = tab[4 * ns + slot];
+  p.pads = tab[5 * ns + slot];
+  p.ksO2oxic = tab[6 * ns + slot];
+  p.kinO2denit = tab[7 * ns + slot];
+  p.ksNO3denit = tab[8 * ns + slot];
+  p.kinO2anox = tab[9 * ns + slot];
+  p.kinNO3anox = tab[10 * ns + slot];
+  p.ksO2nitri = tab[11 * ns + slot];
+  p.ksO2oduox = tab[12 * ns + slot];
+  p.PAdsODU = tab[13 * ns + slot];
+  p.nh3fac = tab[14 * ns + slot];
+  p.nh3den = tab[15 * ns + slot];
+}
+
 struct DevStats {
   unsigned long long surrogate;    // columns whose surrogate step was accepted
   unsigned long long attempts;

@@ -799,7 +799,8 @@ k_column(ColumnArgs<real> a, Params<real> p) {
 // sectors of neighbouring slots), steps it and writes it back.  The only
 // shared memory is the warp's copy of its column's 11 surface values; the
 // only block barriers are at entry and exit.
-template <typename real, int LPL, bool BC4, bool BIO3, int KIND, bool MULTI>
+// ENS: every column takes its own OMEXDIA+P parameter set from a.bgc.
+template <typename real, int LPL, bool BC4, bool BIO3, int KIND, bool MULTI, bool ENS>
 __global__ void __launch_bounds__(256, (MinBlocks<real, LPL>::value))
 k_column_warp(ColumnArgs<real> a, Params<real> p) {
   __shared__ real s_bnd[8][NFORCE];
@@ -845,6 +846,8 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
                                     (int)ns, lane, K, p.mol_mode);
     lc.bnd_s = sb + 2;
     lc.bnd_stride = 1;
+    Params<real> pc = p;
+    if (ENS) load_bgc(pc, a.bgc, ns, slot);
     real ftop[NTR];
     double bud[4];
     ColResult r;
@@ -856,11 +859,11 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
       for (int n = 0; n < NTR; n++) ftop[n] = real(0);
       for (int b = 0; b < 4; b++) bud[b] = 0.0;
       if (KIND == KIND_ADAPT)
-        r = p.ticks
-                ? solve_adaptive<real, LPL, BC4, BIO3, true>(p, lc, lane, K, C, ftop, a.dt, bud)
-                : solve_adaptive<real, LPL, BC4, BIO3, false>(p, lc, lane, K, C, ftop, a.dt, bud);
+        r = pc.ticks
+                ? solve_adaptive<real, LPL, BC4, BIO3, true>(pc, lc, lane, K, C, ftop, a.dt, bud)
+                : solve_adaptive<real, LPL, BC4, BIO3, false>(pc, lc, lane, K, C, ftop, a.dt, bud);
       else
-        r = solve_fixed<real, LPL, BC4, BIO3>(p, lc, lane, K, C, ftop, a.dt, a.method, bud);
+        r = solve_fixed<real, LPL, BC4, BIO3>(pc, lc, lane, K, C, ftop, a.dt, a.method, bud);
       if (lane == 0) {
         atomicAdd(&b_att, (unsigned long long)r.attempts);
         atomicAdd(&b_acc, (unsigned long long)r.accepted);
@@ -1336,31 +1339,44 @@ int column_blocks_per_sm(int tc, int lpl, bool bc4, int kind, int threads, bool 
              : occupancy_b<real, 2, false>(tc, kind, threads, bio3);
 }
 
-template <typename real, int LPL, bool BC4, bool BIO3, int KIND, bool MULTI>
+template <typename real, int LPL, bool BC4, bool BIO3, int KIND, bool MULTI, bool ENS>
 static cudaError_t launch_warp_t(const ColumnArgs<real>& a, const Params<real>& p, int blocks,
                                  int threads, cudaStream_t st) {
-  k_column_warp<real, LPL, BC4, BIO3, KIND, MULTI><<<blocks, threads, 0, st>>>(a, p);
+  k_column_warp<real, LPL, BC4, BIO3, KIND, MULTI, ENS><<<blocks, threads, 0, st>>>(a, p);
   return cudaGetLastError();
 }
 
-// several steps per launch (a.nrepeat > 1) exist for the adaptive method
-template <typename real, int LPL, bool BC4, bool BIO3>
-cudaError_t launch_warp_k(const ColumnArgs<real>& a, const Params<real>& p, int kind,
+// several steps per launch (a.nrepeat > 1) exist for the adaptive method;
+// ENS: the per-column parameter-set variants (compiled in their own units)
+template <typename real, int LPL, bool BC4, bool BIO3, bool ENS>
+cudaError_t launch_warp_e(const ColumnArgs<real>& a, const Params<real>& p, int kind,
                           int blocks, int threads, cudaStream_t st) {
   if (kind == KIND_FIXED) {
     if (a.nrepeat > 1) return cudaErrorInvalidValue;
-    return launch_warp_t<real, LPL, BC4, BIO3, KIND_FIXED, false>(a, p, blocks, threads, st);
+    return launch_warp_t<real, LPL, BC4, BIO3, KIND_FIXED, false, ENS>(a, p, blocks, threads, st);
   }
   return a.nrepeat > 1
-             ? launch_warp_t<real, LPL, BC4, BIO3, KIND_ADAPT, true>(a, p, blocks, threads, st)
-             : launch_warp_t<real, LPL, BC4, BIO3, KIND_ADAPT, false>(a, p, blocks, threads, st);
+             ? launch_warp_t<real, LPL, BC4, BIO3, KIND_ADAPT, true, ENS>(a, p, blocks, threads, st)
+             : launch_warp_t<real, LPL, BC4, BIO3, KIND_ADAPT, false, ENS>(a, p, blocks, threads, st);
+}
+
+template <typename real, int LPL, bool BC4, bool BIO3>
+cudaError_t launch_warp_k(const ColumnArgs<real>& a, const Params<real>& p, int kind,
+                          int blocks, int threads, cudaStream_t st) {
+  return launch_warp_e<real, LPL, BC4, BIO3, false>(a, p, kind, blocks, threads, st);
+}
+template <typename real, int LPL, bool BC4, bool BIO3>
+cudaError_t launch_warp_ens(const ColumnArgs<real>& a, const Params<real>& p, int kind,
+                            int blocks, int threads, cudaStream_t st) {
+  return launch_warp_e<real, LPL, BC4, BIO3, true>(a, p, kind, blocks, threads, st);
 }
 
 template <typename real, int LPL, bool BC4, bool BIO3, int KIND, bool MULTI>
 static int warp_occupancy_t(int threads) {
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &nb, k_column_warp<real, LPL, BC4, BIO3, KIND, MULTI>, threads, 0) != cudaSuccess)
+          &nb, k_column_warp<real, LPL, BC4, BIO3, KIND, MULTI, false>, threads, 0) !=
+      cudaSuccess)
     return 0;
   return nb;
 }
@@ -1372,20 +1388,27 @@ int warp_occupancy_k(int kind, int threads) {
                   warp_occupancy_t<real, LPL, BC4, BIO3, KIND_ADAPT, true>(threads));
 }
 
+template <typename real, int LPL, bool BC4, bool BIO3>
+static cudaError_t launch_warp_any(const ColumnArgs<real>& a, const Params<real>& p, int kind,
+                                   int blocks, int threads, cudaStream_t st) {
+  return a.bgc ? launch_warp_ens<real, LPL, BC4, BIO3>(a, p, kind, blocks, threads, st)
+               : launch_warp_k<real, LPL, BC4, BIO3>(a, p, kind, blocks, threads, st);
+}
+
 template <typename real>
 cudaError_t launch_column_warp(const ColumnArgs<real>& a, const Params<real>& p, int lpl,
                                bool bc4, int kind, int blocks, int threads, cudaStream_t st) {
   const bool b3 = p.bio3 != 0;
   if (lpl == 1) {
-    if (bc4) return b3 ? launch_warp_k<real, 1, true, true>(a, p, kind, blocks, threads, st)
-                       : launch_warp_k<real, 1, true, false>(a, p, kind, blocks, threads, st);
-    return b3 ? launch_warp_k<real, 1, false, true>(a, p, kind, blocks, threads, st)
-              : launch_warp_k<real, 1, false, false>(a, p, kind, blocks, threads, st);
+    if (bc4) return b3 ? launch_warp_any<real, 1, true, true>(a, p, kind, blocks, threads, st)
+                       : launch_warp_any<real, 1, true, false>(a, p, kind, blocks, threads, st);
+    return b3 ? launch_warp_any<real, 1, false, true>(a, p, kind, blocks, threads, st)
+              : launch_warp_any<real, 1, false, false>(a, p, kind, blocks, threads, st);
   }
-  if (bc4) return b3 ? launch_warp_k<real, 2, true, true>(a, p, kind, blocks, threads, st)
-                     : launch_warp_k<real, 2, true, false>(a, p, kind, blocks, threads, st);
-  return b3 ? launch_warp_k<real, 2, false, true>(a, p, kind, blocks, threads, st)
-            : launch_warp_k<real, 2, false, false>(a, p, kind, blocks, threads, st);
+  if (bc4) return b3 ? launch_warp_any<real, 2, true, true>(a, p, kind, blocks, threads, st)
+                     : launch_warp_any<real, 2, true, false>(a, p, kind, blocks, threads, st);
+  return b3 ? launch_warp_any<real, 2, false, true>(a, p, kind, blocks, threads, st)
+            : launch_warp_any<real, 2, false, false>(a, p, kind, blocks, threads, st);
 }
 
 template <typename real>
@@ -1543,6 +1566,17 @@ cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
   prefix template int warp_occupancy_k<real, 1, true, BIO3>(int, int);          \
   prefix template int warp_occupancy_k<real, 2, false, BIO3>(int, int);         \
   prefix template int warp_occupancy_k<real, 2, true, BIO3>(int, int);
+
+// The warp-direct kernels with a parameter set per column.
+#define SED_WARP_ENS_VARIANT(prefix, real, BIO3)                                \
+  prefix template cudaError_t launch_warp_ens<real, 1, false, BIO3>(            \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t); \
+  prefix template cudaError_t launch_warp_ens<real, 1, true, BIO3>(             \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t); \
+  prefix template cudaError_t launch_warp_ens<real, 2, false, BIO3>(            \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t); \
+  prefix template cudaError_t launch_warp_ens<real, 2, true, BIO3>(             \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t);
 
 #define SED_INSTANTIATE(real)                                                   \
   template size_t tile_smem_bytes<real>(int, int, bool, int, bool);             \

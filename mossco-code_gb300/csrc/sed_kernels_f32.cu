@@ -7,5 +7,7 @@ namespace sed {
 SED_VARIANT(extern, float, true)
 SED_WARP_VARIANT(extern, float, false)
 SED_WARP_VARIANT(extern, float, true)
+SED_WARP_ENS_VARIANT(extern, float, false)
+SED_WARP_ENS_VARIANT(extern, float, true)
 SED_INSTANTIATE(float)
 }  // namespace sed

@@ -7,5 +7,7 @@ namespace sed {
 SED_VARIANT(extern, double, true)
 SED_WARP_VARIANT(extern, double, false)
 SED_WARP_VARIANT(extern, double, true)
+SED_WARP_ENS_VARIANT(extern, double, false)
+SED_WARP_ENS_VARIANT(extern, double, true)
 SED_INSTANTIATE(double)
 }  // namespace sed

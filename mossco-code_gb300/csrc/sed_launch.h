@@ -43,6 +43,9 @@ struct ColumnArgs {
   // warp-direct kernel: coupling steps per launch with constant forcing
   // (0 or 1: one); each warp keeps its column in registers between them
   int nrepeat;
+  // warp-direct kernel: per-slot OMEXDIA+P rate parameters [NBGC_DEV][nslot]
+  // (an ensemble of parameter sets), or null for the Params set
+  const real* bgc;
 };
 
 template <typename real>

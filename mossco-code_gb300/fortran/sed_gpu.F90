@@ -16,6 +16,7 @@ module sed_gpu
   private
 
   integer, parameter, public :: SED_NTR = 11
+  integer, parameter, public :: SED_NBGC = 17
   integer, parameter, public :: SED_OK = 0, SED_E_ARG = -1, SED_E_NAN = -2
   integer, parameter, public :: SED_E_SUBSTEP_CAP = -3, SED_E_CUDA = -4
   integer, parameter, public :: SED_E_STATE = -5, SED_E_NOMEM = -6
@@ -90,6 +91,12 @@ module sed_gpu
       integer(c_int), value :: method
       type(sed_stats_t), intent(out) :: st
     end function
+    !> an OMEXDIA+P parameter set per column, params(i,j,1:SED_NBGC) in
+    !! sed_params_t's order (c_null_ptr: the handle's set)
+    integer(c_int) function sed_set_column_bgc(h, params) bind(C, name='sed_set_column_bgc')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, params
+    end function
     integer(c_int) function sed_get_rhs(h, conc, rhs, fluxes) bind(C, name='sed_get_rhs')
       import :: c_int, c_ptr
       type(c_ptr), value :: h, conc, rhs, fluxes
@@ -151,7 +158,7 @@ module sed_gpu
   public :: sed_default_params, sed_gpu_init, sed_gpu_ode_solver, &
             sed_gpu_get_rhs, sed_gpu_finalize, sed_get_tuning, sed_set_tuning, &
             sed_autotune, sed_set_boundary, sed_get_boundary, sed_spinup, &
-            sed_get_min_dt
+            sed_get_min_dt, sed_set_column_bgc
 
 contains
 

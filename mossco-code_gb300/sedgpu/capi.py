@@ -106,6 +106,7 @@ _H = ctypes.c_void_p
 # name -> (restype, argtypes); must list every function of mossco_sed.h
 SIGNATURES = {
     "sed_default_params": (ctypes.c_int, [ctypes.POINTER(SedParams)]),
+    "sed_set_column_bgc": (ctypes.c_int, [_H, _dp]),
     "sed_create": (ctypes.c_int, [ctypes.POINTER(SedParams), ctypes.c_int,
                                   ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                   ctypes.POINTER(_H)]),
@@ -263,6 +264,16 @@ class Solver:
             _p(_f64(cs.flux_cap)),
             _p(np.ascontiguousarray(cs.kact, dtype=np.int32), _ip), None),
             "sed_set_grid")
+        if cs.bgc_col is not None:
+            self.set_column_bgc(cs.bgc_col)
+
+    def set_column_bgc(self, params: Optional[np.ndarray]):
+        """An OMEXDIA+P parameter set per column, [SED_NBGC][ncol] in
+        BGC_NAMES order (per-day units), or None for the handle's set."""
+        a = None if params is None else _f64(params)
+        if a is not None and a.shape != (len(BGC_NAMES), self.cs.ncol):
+            raise ValueError(f"params must be [{len(BGC_NAMES)}][{self.cs.ncol}]")
+        self._check(self.lib.sed_set_column_bgc(self.h, _p(a)), "sed_set_column_bgc")
 
     def _check(self, rc: int, what: str):
         if rc != SED_OK:

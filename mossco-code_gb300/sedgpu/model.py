@@ -129,10 +129,20 @@ class ColumnSet:
     nsteps: int = 1
     name: str = ""
     seed: int = 0
+    # per-column OMEXDIA+P parameter sets [len(BGC_NAMES)][ncol] (an
+    # ensemble), or None for the one set ``bgc``
+    bgc_col: Optional[np.ndarray] = None
 
     @property
     def ncol(self) -> int:
         return self.inum * self.jnum
+
+    def bgc_columns(self) -> np.ndarray:
+        """[len(BGC_NAMES)][ncol]: bgc_col, or ``bgc`` repeated."""
+        if self.bgc_col is not None:
+            return np.ascontiguousarray(self.bgc_col, dtype=np.float64)
+        v = np.array([self.bgc[n] for n in BGC_NAMES], dtype=np.float64)
+        return np.ascontiguousarray(np.repeat(v[:, None], self.ncol, axis=1))
 
     @property
     def n_active(self) -> int:
@@ -158,4 +168,6 @@ class ColumnSet:
                      "flux_cap", "bdys", "fluxes"):
             setattr(out, name, np.ascontiguousarray(getattr(self, name)[:, cols]))
         out.conc = np.ascontiguousarray(self.conc[:, :, cols])
+        if self.bgc_col is not None:
+            out.bgc_col = np.ascontiguousarray(self.bgc_col[:, cols])
         return out

@@ -75,6 +75,7 @@ class Model(ctypes.Structure):
         ("bioturb_k_l", ctypes.c_double), ("bioturb_L1", ctypes.c_double),
         ("bioturb_L2", ctypes.c_double), ("bioturb_beta", ctypes.c_double),
         ("bioturb_b", ctypes.c_double), ("bioturb_dry_density", ctypes.c_double),
+        ("bgc_col", ctypes.POINTER(Bgc)),
     ]
 
 
@@ -173,6 +174,11 @@ class OracleModel:
         for n in ("bioturb_k_l", "bioturb_L1", "bioturb_L2", "bioturb_beta",
                   "bioturb_b", "bioturb_dry_density"):
             setattr(m, n, float(getattr(d, n)))
+        if cs.bgc_col is not None:
+            # [ncol] structs: the transpose of the [param][col] table
+            tab = np.ascontiguousarray(np.asarray(cs.bgc_col, dtype=np.float64).T)
+            self._keep["bgc_col"] = tab
+            m.bgc_col = tab.ctypes.data_as(ctypes.POINTER(Bgc))
         self.m = m
 
     def get_rhs(self, conc: np.ndarray, fluxes: Optional[np.ndarray] = None):

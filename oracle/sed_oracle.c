@@ -321,7 +321,7 @@ static void get_rhs_col(const orc_model *m, int col, const double *conc,
   for (int k = 0; k < K; k++) {
     for (int n = 0; n < N; n++) w->cell[n] = conc[IDX(n, k, col, KM, nc)];
     double dn = 0.0;
-    orc_omexdia_p(&m->bgc, w->cell, w->rate, &dn);
+    orc_omexdia_p(m->bgc_col ? &m->bgc_col[col] : &m->bgc, w->cell, w->rate, &dn);
     for (int n = 0; n < N; n++)
       rhs[IDX(n, k, col, KM, nc)] = w->rate[n] + w->tr[(size_t)n * K + k];
     if (denit) denit[(size_t)k * nc + col] = dn;
@@ -503,6 +503,7 @@ static int step_one_column(const orc_model *m, col_ctx *c, int col,
   const int KM = m->kmax, N = m->ntr, K = m->kact[col];
   if (K <= 0) return 0;
   c->kact = K;
+  c->m1.bgc_col = m->bgc_col ? &m->bgc_col[col] : NULL;  /* the column's set */
   for (int k = 0; k < KM; k++) {
     c->dz[k] = m->dz[k * nc + col];
     c->phi[k] = m->phi[k * nc + col];

@@ -69,6 +69,8 @@ typedef struct {
   int bioturbation_profile;
   double bioturb_k_l, bioturb_L1, bioturb_L2, bioturb_beta, bioturb_b,
       bioturb_dry_density;
+  /* [ncol] a parameter set per column (an ensemble), or NULL for bgc */
+  const orc_bgc *bgc_col;
 } orc_model;
 
 typedef struct {
