@@ -20,6 +20,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdint>
@@ -545,6 +546,10 @@ struct pel_handle {
       d_work, d_stats, d_wcols;
   DevStats* h_stats = nullptr;  // pinned
   long long launches = 0;
+  std::vector<int> wcols;       // host copy of d_wcols
+  // pipelined host calls: copy-in, per-chunk step and copy-out streams
+  cudaStream_t s_in = nullptr, s_out = nullptr, s_cmp[8] = {};
+  cudaEvent_t e_start = nullptr, e_done = nullptr, e_in[8] = {}, e_cmp[8] = {};
 
   int fail(int code, const char* fmt, ...) {
     char buf[512];
@@ -562,6 +567,17 @@ struct pel_handle {
   size_t rsize() const { return fp64() ? sizeof(double) : sizeof(float); }
   size_t cells() const { return (size_t)K * ncol; }
   ~pel_handle() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (cudaStream_t st : {s_in, s_out})
+      if (st) { cudaStreamSynchronize(st); cudaStreamDestroy(st); }
+    for (cudaStream_t st : s_cmp)
+      if (st) { cudaStreamSynchronize(st); cudaStreamDestroy(st); }
+    for (cudaEvent_t ev : {e_start, e_done})
+      if (ev) cudaEventDestroy(ev);
+    for (int c = 0; c < 8; c++) {
+      if (e_in[c]) cudaEventDestroy(e_in[c]);
+      if (e_cmp[c]) cudaEventDestroy(e_cmp[c]);
+    }
     if (h_stats) cudaFreeHost(h_stats);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -715,21 +731,20 @@ int reset_stats(pel_handle* h) {
   return SED_OK;
 }
 
+// one thread per water column of a.wcols[0 .. a.nwater)
 template <typename real, typename store, bool LIGHT, bool EPI>
-void launch_run(pel_handle* h, const Args<real>& a, store* conc, int method) {
-  const dim3 g((h->water_cols + kThreads - 1) / kThreads > 0 ? (h->water_cols + kThreads - 1) / kThreads
-                                                              : 1),
-      b(kThreads);
+void launch_run(pel_handle* h, const Args<real>& a, store* conc, int method, cudaStream_t st) {
+  const dim3 g(a.nwater > 0 ? (a.nwater + kThreads - 1) / kThreads : 1), b(kThreads);
   switch (method) {
-    case SED_EULER: k_pel_run<real, store, SED_EULER, LIGHT, EPI><<<g, b, 0, h->stream>>>(a, conc); break;
+    case SED_EULER: k_pel_run<real, store, SED_EULER, LIGHT, EPI><<<g, b, 0, st>>>(a, conc); break;
     case SED_RUNGE_KUTTA_4:
-      k_pel_run<real, store, SED_RUNGE_KUTTA_4, LIGHT, EPI><<<g, b, 0, h->stream>>>(a, conc);
+      k_pel_run<real, store, SED_RUNGE_KUTTA_4, LIGHT, EPI><<<g, b, 0, st>>>(a, conc);
       break;
     case SED_ADAPTIVE_EULER:
-      k_pel_run<real, store, SED_ADAPTIVE_EULER, LIGHT, EPI><<<g, b, 0, h->stream>>>(a, conc);
+      k_pel_run<real, store, SED_ADAPTIVE_EULER, LIGHT, EPI><<<g, b, 0, st>>>(a, conc);
       break;
     default:
-      k_pel_run<real, store, SED_RUNGE_KUTTA_4_38, LIGHT, EPI><<<g, b, 0, h->stream>>>(a, conc);
+      k_pel_run<real, store, SED_RUNGE_KUTTA_4_38, LIGHT, EPI><<<g, b, 0, st>>>(a, conc);
       break;
   }
   h->launches++;
@@ -885,8 +900,8 @@ int run_on(pel_handle* h, store* conc, double t_couple, double dt, int method, b
     if (!same) convert<real, store>(h, st, conc, NTR * h->cells());
   } else {
     Args<real> a = make_args<real>(h, t_couple, dt);
-    if (light && epi) launch_run<real, store, true, true>(h, a, conc, method);
-    else launch_run<real, store, false, false>(h, a, conc, method);
+    if (light && epi) launch_run<real, store, true, true>(h, a, conc, method, h->stream);
+    else launch_run<real, store, false, false>(h, a, conc, method, h->stream);
     if (light) h->have_par = true;
   }
   PK(cudaGetLastError(), "pelagic kernels");
@@ -902,7 +917,71 @@ int check_method(pel_handle* h, int method, double t_couple, double dt) {
   return SED_OK;
 }
 
-// A call on the caller's host array conc: copy in, work, copy out.
+int ensure_pipeline(pel_handle* h) {
+  if (h->s_in) return SED_OK;
+  PK(cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking), "stream");
+  PK(cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking), "stream");
+  for (auto& st : h->s_cmp) PK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
+  PK(cudaEventCreateWithFlags(&h->e_start, cudaEventDisableTiming), "event");
+  PK(cudaEventCreateWithFlags(&h->e_done, cudaEventDisableTiming), "event");
+  for (int c = 0; c < 8; c++) {
+    PK(cudaEventCreateWithFlags(&h->e_in[c], cudaEventDisableTiming), "event");
+    PK(cudaEventCreateWithFlags(&h->e_cmp[c], cudaEventDisableTiming), "event");
+  }
+  return SED_OK;
+}
+
+// A Run or ode_solver call on the caller's host array with the copies in
+// flight: the grid is cut into 8 column ranges; range c's host->device copy
+// (one 2-D copy of its columns in every [tracer][layer] row), its step (on
+// its own stream) and its device->host copy are ordered by events, so one
+// range arrives while another is stepped and a third leaves.  The ranges
+// are disjoint in the staging array, in conc and in the water-column list.
+template <typename real>
+int host_pipelined(pel_handle* h, double* conc, double t_couple, double dt, int method,
+                   bool light, bool epi) {
+  int rc = ensure_pipeline(h);
+  if (rc) return rc;
+  const int nch = 8;
+  const size_t pitch = (size_t)h->ncol * sizeof(double), rows = (size_t)NTR * h->K;
+  double* stage = h->d_stage.as<double>();
+  PK(cudaEventRecord(h->e_start, h->stream), "event");
+  PK(cudaStreamWaitEvent(h->s_in, h->e_start, 0), "wait");
+  for (int c = 0; c < nch; c++) {
+    const int col0 = (int)((long long)h->ncol * c / nch);
+    const int col1 = (int)((long long)h->ncol * (c + 1) / nch);
+    const size_t width = (size_t)(col1 - col0) * sizeof(double);
+    if (width)
+      PK(cudaMemcpy2DAsync(stage + col0, pitch, conc + col0, pitch, width, rows,
+                           cudaMemcpyHostToDevice, h->s_in),
+         "conc range in");
+    PK(cudaEventRecord(h->e_in[c], h->s_in), "event");
+    PK(cudaStreamWaitEvent(h->s_cmp[c], h->e_in[c], 0), "wait");
+    const int w0 = (int)(std::lower_bound(h->wcols.begin(), h->wcols.end(), col0) - h->wcols.begin());
+    const int w1 = (int)(std::lower_bound(h->wcols.begin(), h->wcols.end(), col1) - h->wcols.begin());
+    if (w1 > w0) {
+      Args<real> a = make_args<real>(h, t_couple, dt);
+      a.wcols += w0;
+      a.nwater = w1 - w0;
+      if (light && epi) launch_run<real, double, true, true>(h, a, stage, method, h->s_cmp[c]);
+      else launch_run<real, double, false, false>(h, a, stage, method, h->s_cmp[c]);
+    }
+    PK(cudaEventRecord(h->e_cmp[c], h->s_cmp[c]), "event");
+    PK(cudaStreamWaitEvent(h->s_out, h->e_cmp[c], 0), "wait");
+    if (width)
+      PK(cudaMemcpy2DAsync(conc + col0, pitch, stage + col0, pitch, width, rows,
+                           cudaMemcpyDeviceToHost, h->s_out),
+         "conc range out");
+  }
+  PK(cudaEventRecord(h->e_done, h->s_out), "event");
+  PK(cudaStreamWaitEvent(h->stream, h->e_done, 0), "wait");
+  PK(cudaGetLastError(), "pelagic kernels");
+  if (light) h->have_par = true;
+  return SED_OK;
+}
+
+// A call on the caller's host array conc: copy in, work, copy out (in
+// flight for the per-cell steppers, in turn for the grid-wide cut).
 template <typename real>
 int host_call(pel_handle* h, double* conc, double t_couple, double dt, int method, bool light,
               bool epi, pel_stats* st) {
@@ -913,6 +992,11 @@ int host_call(pel_handle* h, double* conc, double t_couple, double dt, int metho
   const long long l0 = h->launches;
   long long host_att = 0;
   PK(cudaEventRecord(h->ev0, h->stream), "event");
+  if (!(method == SED_ADAPTIVE_EULER && h->prm.cut_scope == PEL_CUT_GLOBAL) && h->ncol >= 8) {
+    rc = host_pipelined<real>(h, conc, t_couple, dt, method, light, epi);
+    if (rc) return rc;
+    return finish_stats(h, st, host_att, l0, 1);
+  }
   PK(cudaMemcpyAsync(h->d_stage.p, conc, bytes, cudaMemcpyHostToDevice, h->stream), "conc in");
   rc = run_on<real, double>(h, h->d_stage.as<double>(), t_couple, dt, method, light, epi,
                             host_att);
@@ -1043,6 +1127,7 @@ int pel_set_grid(pel_handle* h, const double* layer_height, const int* mask) {
     if (wet) wcols.push_back(c);
   }
   h->water_cols = (int)wcols.size();
+  h->wcols = wcols;
   PK(h->d_wcols.alloc((wcols.size() + 1) * sizeof(int)), "water columns");
   if (!wcols.empty()) {
     PK(cudaMemcpyAsync(h->d_wcols.p, wcols.data(), wcols.size() * sizeof(int),

@@ -106,7 +106,7 @@ struct sed_handle {
   std::vector<int> seg_col;     // [nseg + 1] column bounds
   int pipe = 1;                 // sed_ode_solver pipeline chunks
   // pipelined sed_ode_solver: copy-in, two step, copy-out streams
-  cudaStream_t s_in = nullptr, s_out = nullptr, s_cmp[2] = {nullptr, nullptr};
+  cudaStream_t s_in = nullptr, s_out = nullptr, s_cmp[kMaxSeg] = {};
   cudaEvent_t pe_start = nullptr, pe_done = nullptr;
   cudaEvent_t pe_in[kMaxSeg] = {}, pe_cmp[kMaxSeg] = {};
   // device buffers
@@ -620,7 +620,9 @@ int ensure_pipeline(sed_handle* h) {
 // sed_ode_solver with the copies in flight: the columns are cut into
 // h->pipe chunks of whole segments.  Chunk c's host->device copy (one 2-D
 // copy of its column range in every [tracer][layer] row), its gather, step
-// and scatter (on one of two step streams, alternating), and its
+// and scatter (on its own step stream, so the steps of several chunks
+// overlap and a chunk's tail of slow columns shares the GPU with the next
+// chunk's step), and its
 // device->host copy are ordered by events, so chunk c+1 arrives while c is
 // stepped and c-1 leaves.  Each chunk writes a disjoint column range of the
 // staging array and of conc, and its own slots.
@@ -637,9 +639,9 @@ int ode_solver_pipelined(sed_handle* h, double* conc, double dt, int method) {
   double* stage = h->d_stage.as<double>();
   unsigned* q = h->d_queue.as<unsigned>();
   CK(cudaMemsetAsync(q, 0, kQueues * sizeof(unsigned), h->stream), "queue reset");
+  const int per = h->nseg / h->pipe;
   CK(cudaEventRecord(h->pe_start, h->stream), "event");
   CK(cudaStreamWaitEvent(h->s_in, h->pe_start, 0), "wait");
-  const int per = h->nseg / h->pipe;
   for (int c = 0; c < h->pipe; c++) {
     const int g0 = c * per, g1 = g0 + per;
     const int col0 = h->seg_col[g0], col1 = h->seg_col[g1];
@@ -648,7 +650,7 @@ int ode_solver_pipelined(sed_handle* h, double* conc, double dt, int method) {
       CK(cudaMemcpy2DAsync(stage + col0, pitch, conc + col0, pitch, width, rows,
                            cudaMemcpyHostToDevice, h->s_in), "conc chunk copy");
     CK(cudaEventRecord(h->pe_in[c], h->s_in), "event");
-    cudaStream_t cs = h->s_cmp[c & 1];
+    cudaStream_t cs = h->s_cmp[c];
     CK(cudaStreamWaitEvent(cs, h->pe_in[c], 0), "wait");
     for (int b = 0; b < 2; b++) {
       const Bin& bin = h->bins[b];
@@ -885,7 +887,9 @@ sed_handle::~sed_handle() {
   cudaSetDevice(device);
   if (stream) cudaStreamSynchronize(stream);
   reset_graph(this);
-  for (cudaStream_t st : {s_in, s_out, s_cmp[0], s_cmp[1]})
+  for (cudaStream_t st : {s_in, s_out})
+    if (st) { cudaStreamSynchronize(st); cudaStreamDestroy(st); }
+  for (cudaStream_t st : s_cmp)
     if (st) { cudaStreamSynchronize(st); cudaStreamDestroy(st); }
   for (cudaEvent_t ev : {pe_start, pe_done}) if (ev) cudaEventDestroy(ev);
   for (int c = 0; c < kMaxSeg; c++) {
