@@ -104,6 +104,27 @@ def test_ensemble_columns_equal_separate_runs_fp32(method):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("profile3,bc4", [(True, False), (False, True), (True, True)])
+def test_ensemble_with_profile3_and_cascade(profile3, bc4):
+    """The ENS kernels of the other template branches: TOC-dependent
+    bioturbation and the capped particulate flux cascade."""
+    cs = small(ncol=24, K=20, seed=28)
+    if profile3:
+        cs.driver.bioturbation_profile = 3
+    if bc4:   # a cap that binds, so the cascade moves material down
+        cs.driver.bcup_particulate = 4
+        cs.flux_cap[:] = 2e-5 * cs.dz / cs.dz[0]
+        for n in range(6):
+            cs.fluxes[n] *= 50.0
+    tab, which = ensemble(cs)
+    got, _ = gpu(cs, 2, capi.SED_FP32, table=tab)
+    for i, ov in enumerate(SETS):
+        ref, _ = gpu(with_set(cs, ov), 2, capi.SED_FP32)
+        cols = np.flatnonzero(which == i)
+        np.testing.assert_array_equal(got[:, :, cols], ref[:, :, cols])
+
+
+@pytest.mark.gpu
 def test_ensemble_fp64_matches_oracle(oracle_mod):
     cs = small(ncol=32, K=24, kmin=3, seed=25)
     cs.bgc_col, _ = ensemble(cs)
