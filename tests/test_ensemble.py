@@ -114,8 +114,10 @@ def test_ensemble_with_profile3_and_cascade(profile3, bc4):
     if bc4:   # a cap that binds, so the cascade moves material down
         cs.driver.bcup_particulate = 4
         cs.flux_cap[:] = 2e-5 * cs.dz / cs.dz[0]
+        # 50x deposition with profile 3 drives the reference algorithm (and
+        # the oracle) to NaN within two steps; profile 3 keeps the fluxes
         for n in range(6):
-            cs.fluxes[n] *= 50.0
+            cs.fluxes[n] *= 1.0 if profile3 else 50.0
     tab, which = ensemble(cs)
     got, _ = gpu(cs, 2, capi.SED_FP32, table=tab)
     for i, ov in enumerate(SETS):
