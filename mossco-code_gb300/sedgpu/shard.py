@@ -40,8 +40,16 @@ def shard(cs: ColumnSet, rank: int, world: int) -> Tuple[ColumnSet, Tuple[int, i
     return cs.subset(np.arange(c0, c1)), (c0, c1)
 
 
+def shard_pelagic(pcs, rank: int, world: int):
+    """The pelagic grid's share of one rank: a contiguous column range with
+    about equal water cells, as its own 1 x n grid, and the range."""
+    c0, c1 = partition(pcs.water().sum(axis=0), world)[rank]
+    return pcs.subset(np.arange(c0, c1)), (c0, c1)
+
+
 _SUM = ("attempts", "accepted", "column_steps", "capped_columns", "nan_cells",
-        "gpu_launches", "surrogate_columns")
+        "gpu_launches", "surrogate_columns", "capped_cells")
+_MAX = ("max_col_attempts", "max_cell_attempts", "device_ms")
 
 
 def reduce_stats(stats: Dict[str, float], group=None) -> Dict[str, float]:
@@ -54,8 +62,8 @@ def reduce_stats(stats: Dict[str, float], group=None) -> Dict[str, float]:
     dev = "cuda" if dist.get_backend(group) == "nccl" else "cpu"
     keys = [k for k in _SUM if k in stats]
     s = torch.tensor([float(stats[k]) for k in keys], dtype=torch.float64, device=dev)
-    mx = torch.tensor([float(stats.get("max_col_attempts", 0)),
-                       float(stats.get("device_ms", 0.0))], dtype=torch.float64, device=dev)
+    mkeys = [k for k in _MAX if k in stats] or ["max_col_attempts"]
+    mx = torch.tensor([float(stats.get(k, 0)) for k in mkeys], dtype=torch.float64, device=dev)
     mn = torch.tensor([float(stats.get("min_dt", np.inf))], dtype=torch.float64, device=dev)
     dist.all_reduce(s, op=dist.ReduceOp.SUM, group=group)
     dist.all_reduce(mx, op=dist.ReduceOp.MAX, group=group)
@@ -63,7 +71,7 @@ def reduce_stats(stats: Dict[str, float], group=None) -> Dict[str, float]:
     out = dict(stats)
     for k, v in zip(keys, s.tolist()):
         out[k] = int(v)
-    out["max_col_attempts"] = int(mx[0].item())
-    out["device_ms"] = float(mx[1].item())
+    for k, v in zip(mkeys, mx.tolist()):
+        out[k] = float(v) if k == "device_ms" else int(v)
     out["min_dt"] = float(mn[0].item())
     return out

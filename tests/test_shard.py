@@ -87,3 +87,55 @@ def test_two_gloo_ranks_equal_one_process(oracle_mod, tmp_path):
         assert int(d["column_steps"]) == int(np.count_nonzero(cs.kact)) * NSTEPS
         assert int(d["max_col"]) == sref["max_col_attempts"]
         assert float(d["min_dt"]) == sref["min_dt"]
+
+
+def _pel_rank_main(rank, world, port, outdir):
+    for p in (os.path.join(ROOT, "mossco-code_gb300"), os.path.join(ROOT, "oracle")):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    import torch.distributed as dist
+    import pel_oracle
+    from sedgpu import pelagic as pl
+    from sedgpu import shard as sh
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        pcs = pl.make_pelagic_workload("pelagic_cpu_16x16")
+        mine, (c0, c1) = sh.shard_pelagic(pcs, rank, world)
+        c = mine.conc.copy()
+        rc, st, _ = pel_oracle.PelOracle(mine).run(c, nthreads=1, nruns=2)
+        assert rc == 0
+        st["column_steps"] = mine.water_columns() * 2
+        red = sh.reduce_stats(st)
+        np.savez(os.path.join(outdir, f"pel{rank}.npz"), conc=c, c0=c0, c1=c1,
+                 attempts=red["attempts"], column_steps=red["column_steps"],
+                 max_cell=red["max_cell_attempts"])
+    finally:
+        dist.destroy_process_group()
+
+
+def test_pelagic_two_gloo_ranks_equal_one_process(tmp_path):
+    """The pelagic grid split the same way (columns balanced by water
+    cells): two ranks' Runs gathered equal one process's Runs."""
+    import pel_oracle
+    import torch.multiprocessing as mp
+    from sedgpu import pelagic
+    pel_oracle.build()
+    port = _free_port()
+    mp.spawn(_pel_rank_main, args=(2, port, str(tmp_path)), nprocs=2, join=True)
+    pcs = pelagic.make_pelagic_workload("pelagic_cpu_16x16")
+    ref = pcs.conc.copy()
+    rc, sref, _ = pel_oracle.PelOracle(pcs).run(ref, nthreads=1, nruns=2)
+    assert rc == 0
+    got = np.empty_like(ref)
+    for r in range(2):
+        d = np.load(tmp_path / f"pel{r}.npz")
+        got[:, :, int(d["c0"]):int(d["c1"])] = d["conc"]
+        assert int(d["attempts"]) == sref["attempts"]
+        assert int(d["column_steps"]) == 2 * pcs.water_columns()
+        assert int(d["max_cell"]) == sref["max_cell_attempts"]
+    np.testing.assert_array_equal(got, ref)
+    parts = shard.partition(pcs.water().sum(axis=0), 2)
+    w = [int(pcs.water()[:, a:b].sum()) for a, b in parts]
+    assert abs(w[0] - w[1]) <= pcs.knum
