@@ -362,3 +362,33 @@ def test_driver_mirror_sequence(po):
     ref = pcs.conc.copy()
     o.ode_solver(ref, rpar, 600.0, RUNGE_KUTTA_4)
     np.testing.assert_array_equal(pf.conc, ref)
+
+
+def column_stack(K, ncol=40, seed=5):
+    """ncol water columns of K layers (one masked column, one column with a
+    masked bottom segment), values in the synthetic workload's ranges."""
+    rng = np.random.default_rng(seed)
+    h = np.repeat(rng.uniform(0.2, 3.0, ncol)[None, :], K, axis=0)
+    conc = np.stack([rng.uniform(2, 10, (K, ncol)), rng.uniform(0.05, 2, (K, ncol)),
+                     rng.uniform(0.02, 0.5, (K, ncol)), rng.uniform(0.5, 3.5, (K, ncol))])
+    mask = np.zeros((K, ncol), dtype=np.int32)
+    mask[:, 3] = 1
+    mask[:K // 2, 7] = 1
+    bfl = np.zeros((4, ncol))
+    bfl[0] = rng.uniform(0, 3, ncol) / 86400.0
+    return pelagic.PelColumnSet(inum=ncol, jnum=1, knum=K, layer_height=h, conc=conc,
+                                I_0=rng.uniform(0, 250, ncol), mask=mask,
+                                albedo=rng.uniform(0.05, 0.1, ncol), bottom_flux=bfl)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("K", [1, 2, 33, 300])
+def test_layer_counts_fp64_bit_exact(po, K):
+    pcs = column_stack(K)
+    for method in (RUNGE_KUTTA_4, ADAPTIVE_EULER):
+        out, st = gpu_run(pcs, capi.SED_FP64, method=method)
+        ref, sref, _ = oracle_run(po, pcs, method=method)
+        w = pcs.water()
+        np.testing.assert_array_equal(out[:, w], ref[:, w])
+        np.testing.assert_array_equal(out[:, ~w], pcs.conc[:, ~w])
+        assert st["attempts"] == sref["attempts"]
