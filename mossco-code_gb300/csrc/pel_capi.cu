@@ -27,6 +27,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 namespace {
@@ -48,6 +49,7 @@ struct DevStats {
 template <typename real>
 struct Npzd {
   real p0, z0, kc, I_min, rmax, gmax, Iv2, alpha, rpn, rzn, rdn, rpdu, rpdl, rzd;
+  real nIv2L;  // -Iv^2 log2(e): the FP32 grazing exponent as a power of two
 };
 
 template <typename real>
@@ -111,6 +113,17 @@ __device__ __forceinline__ double pexp(double x) {
   return ldexp(s, (int)k);
 }
 __device__ __forceinline__ float pexp(float x) { return __expf(x); }
+// 2^x and 1/x by the hardware's approximate instructions (FP32 path)
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 __device__ __forceinline__ double pdiv(double a, double b) { return a / b; }
 __device__ __forceinline__ float pdiv(float a, float b) { return __fdividef(a, b); }
 // a*b + c: one fused multiply-add in FP32; in FP64 a product and a sum
@@ -139,8 +152,15 @@ template <typename real>
 __device__ __forceinline__ void rates(const Npzd<real>& m, const real (&c)[NTR], real L,
                                       real rpd, real (&r)[NTR]) {
   const real n = c[0], p = c[1], z = c[2], d = c[3];
-  const real fnp = pdiv(L * n, m.alpha + n) * (p + m.p0);
-  const real fpz = m.gmax * (real(1) - pexp(-(m.Iv2 * (p * p)))) * (z + m.z0);
+  real fnp, fpz;
+  if constexpr (std::is_same<real, float>::value) {
+    // exp(-Iv^2 p^2) = 2^(-Iv^2 log2(e) p^2); n/(alpha+n) by a reciprocal
+    fnp = L * n * rcp_approx(m.alpha + n) * (p + m.p0);
+    fpz = m.gmax * (1.0f - ex2_approx(m.nIv2L * (p * p))) * (z + m.z0);
+  } else {
+    fnp = pdiv(L * n, m.alpha + n) * (p + m.p0);
+    fpz = m.gmax * (real(1) - pexp(-(m.Iv2 * (p * p)))) * (z + m.z0);
+  }
   // each sum left to right: ((-fnp + rpn p) + rzn z) + rdn d, ...
   r[0] = fm(m.rdn, d, fm(m.rzn, z, fm(m.rpn, p, -fnp)));
   r[1] = fm(-rpd, p, fm(-m.rpn, p, fnp - fpz));
@@ -274,10 +294,9 @@ __device__ __forceinline__ void step_cell(const Args<real>& a, real (&c)[NTR], r
 template <typename real>
 __device__ __forceinline__ void epilogue_cell(const Args<real>& a, real (&c)[NTR], int k, int col,
                                               real hk, real dt, CellStats& s) {
-  bool nan = false;
-#pragma unroll
-  for (int n = 0; n < NTR; n++) nan |= c[n] != c[n];
-  s.nan += nan;
+  // a NaN in any tracer makes the sum NaN (one compare per cell)
+  const real sum = (c[0] + c[1]) + (c[2] + c[3]);
+  s.nan += sum != sum;
   if (k == 0 && a.bfl && hk > real(0)) {
 #pragma unroll
     for (int n = 0; n < NTR; n++) c[n] = c[n] + a.bfl[(size_t)n * a.ncol + col] * dt / hk;
@@ -682,6 +701,7 @@ Args<real> make_args(pel_handle* h, double t_couple, double dt) {
   a.m.rmax = (real)(p.rmax / day);
   a.m.gmax = (real)(p.gmax / day);
   a.m.Iv2 = (real)(p.Iv * p.Iv);
+  a.m.nIv2L = (real)(-(p.Iv * p.Iv) * 1.4426950408889634);
   a.m.alpha = (real)p.alpha;
   a.m.rpn = (real)(p.rpn / day);
   a.m.rzn = (real)(p.rzn / day);
