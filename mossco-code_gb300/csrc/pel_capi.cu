@@ -125,7 +125,11 @@ __device__ __forceinline__ float rcp_approx(float x) {
   return y;
 }
 __device__ __forceinline__ double pdiv(double a, double b) { return a / b; }
-__device__ __forceinline__ float pdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ float pdiv(float a, float b) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+  return a * r;
+}
 // a*b + c: one fused multiply-add in FP32; in FP64 a product and a sum
 // rounded separately, as the oracle's left-to-right statements are (the
 // unit is compiled without automatic contraction)

@@ -119,7 +119,14 @@ struct DevStats {
 
 // ---------------------------------------------------------------------------
 // division helpers: fast reciprocal in FP32, IEEE division in FP64
-__device__ __forceinline__ float sdiv(float a, float b) { return __fdividef(a, b); }
+// a/b as a times the hardware's approximate reciprocal of b (the
+// denominators here are Monod sums and positive rates, far from the range
+// where that loses accuracy)
+__device__ __forceinline__ float sdiv(float a, float b) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+  return a * r;
+}
 __device__ __forceinline__ double sdiv(double a, double b) { return a / b; }
 // Explicit fused multiply-add.  The kernels are compiled without automatic
 // contraction, so every FP32 rounding is the one written here, and results
