@@ -43,11 +43,9 @@ WORKLOAD = "plain_gpu_256x256"
 NTR, NCOEF, NFORCE, NDISS = 11, 4, 13, 5
 L2_BYTES = 129 * 1024 * 1024
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the hot
-# kernel from an ncu capture at day 10 of the run
-# (profiles/k_column_warp_plain_gpu_256x256.md)
+# kernel, from an ncu --set full capture of the launch at day 10 of the run
 MEASURED_TRAFFIC = {"plain_gpu_256x256": 168.4e6}
-# the same for one Run of the pelagic kernel
-# (profiles/k_pel_run_pelagic_1024x1024.md)
+# the same for one Run of the pelagic kernel (the first timed Run)
 PEL_TRAFFIC = {"pelagic_1024x1024": 1379.4e6}
 FALLBACK_HBM_GBS = 6800.0
 
