@@ -1,7 +1,7 @@
 """FP64 CPU reference of the surrogate MLP (forward, loss, gradients).
 
-TEST INFRASTRUCTURE ONLY: the checker of the GPU surrogate kernels in
-tests/.  Architecture: nin -> hidden (x nhidden, GELU, tanh form) -> nout,
+TEST INFRASTRUCTURE ONLY: the tests compare the GPU surrogate kernels with
+it.  Architecture: nin -> hidden (x nhidden, GELU, tanh form) -> nout,
 MSE loss over all outputs, parameters layer by layer as W[out][in] then
 b[out] (the layout of sed_sur_get_weights).
 """

@@ -1,7 +1,7 @@
 """ctypes front end of the FP64 CPU oracle (sed_oracle.c).
 
-TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
-the checker and by bench.py's CPU-baseline leg.  The product (the CUDA
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() to
+compare against and by bench.py's CPU-baseline leg.  The product (the CUDA
 library under mossco-code_gb300/) never imports it.
 
 Parity status: stepper and transport follow the reference source

@@ -1,8 +1,8 @@
 /*
  * pel_oracle.c -- FP64 CPU oracle for the MOSSCO pelagic driver path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA pelagic library and the
- * timed CPU baseline of its bench line.  Nothing in the product path links
+ * TEST INFRASTRUCTURE ONLY: the values the tests compare the CUDA pelagic
+ * library with, and the timed CPU baseline of its bench line.  Nothing in the product path links
  * or calls this file.
  *
  * Restates, in the reference's operation order:

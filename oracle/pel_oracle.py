@@ -1,7 +1,7 @@
 """ctypes front end of the FP64 CPU oracle of the pelagic path (pel_oracle.c).
 
-TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
-the checker and by bench.py's CPU-baseline leg of the pelagic line.  The
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() to
+compare against and by bench.py's CPU-baseline leg of the pelagic line.  The
 product (the CUDA library under mossco-code_gb300/) never imports it.
 
 Parity status: the stepper, light, Run loop and clip follow the reference

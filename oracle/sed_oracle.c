@@ -1,8 +1,8 @@
 /*
  * sed_oracle.c -- FP64 CPU oracle for the MOSSCO sediment-column hot path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA library and the timed
- * CPU baseline.  Nothing in the product path links or calls this file.
+ * TEST INFRASTRUCTURE ONLY: the values the tests compare the CUDA library
+ * with, and the timed CPU baseline.  Nothing in the product path links or calls this file.
  *
  * Restates, in the reference's own operation order:
  *   src/utilities/solver_library.F90:80-189      ode_solver (4 methods)
