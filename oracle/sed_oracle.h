@@ -2,8 +2,8 @@
  * sed_oracle.h -- FP64 CPU oracle for the MOSSCO sediment-column hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
- * algorithm, used by tests/, by __graft_entry__.smoke() as the checker and by
- * bench.py's CPU-baseline leg.  The product path (the CUDA library) never
+ * algorithm, which tests/ and __graft_entry__.smoke() compare against and
+ * bench.py's CPU-baseline leg times.  The product path (the CUDA library) never
  * links, loads or calls it.
  *
  * Parity status: the ODE stepper and the transport stencil follow the
