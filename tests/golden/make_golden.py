@@ -1,4 +1,5 @@
-"""Writes omexdia_p_example.json next to this script.
+"""Writes omexdia_p_example.json and gotm_npzd_example.json next to this
+script.
 
 The fixture is the reference's standalone one-column OMEXDIA+P example
 (examples/standalone/omexdia_p): the run and sediment namelists of
@@ -60,6 +61,11 @@ def main(ref: str) -> None:
     fixture["attempts"] = int(st["attempts"])
     with open(os.path.join(HERE, "omexdia_p_example.json"), "w") as f:
         json.dump(fixture, f, indent=1)
+    # the pelagic set-ups' FABM model: &gotm_npzd of the fabm0d examples
+    npzd = open(os.path.join(ref, "examples", "fabmsed_fabm0d", "fabm.nml")).read()
+    with open(os.path.join(HERE, "gotm_npzd_example.json"), "w") as f:
+        json.dump({"source": "examples/fabmsed_fabm0d/fabm.nml (gotm_npzd)",
+                   "gotm_npzd": namelist(npzd, "gotm_npzd")}, f, indent=1)
 
 
 if __name__ == "__main__":

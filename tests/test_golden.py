@@ -79,3 +79,15 @@ def test_fp64_device_reproduces_the_example(oracle_mod, fixture):
     gold = np.array(fixture["state"])
     scale = np.abs(gold).max(axis=1, keepdims=True) + 1e-300
     assert np.max(np.abs(out - gold) / scale) < 1e-9
+
+
+def test_pelagic_defaults_are_the_example_gotm_npzd():
+    """The pelagic path's gotm_npzd parameters and initial values are those
+    of the reference's fabm0d examples (tests/golden/gotm_npzd_example.json)."""
+    from sedgpu import pelagic
+    with open(os.path.join(HERE, "gotm_npzd_example.json")) as f:
+        nml = json.load(f)["gotm_npzd"]
+    for name in pelagic.NPZD_NAMES:
+        assert pelagic.NPZD_DEFAULTS[name] == nml[name], name
+    assert pelagic.NPZD_INITIAL == (nml["n_initial"], nml["p_initial"], nml["z_initial"],
+                                    nml["d_initial"])
