@@ -392,3 +392,20 @@ def test_layer_counts_fp64_bit_exact(po, K):
         np.testing.assert_array_equal(out[:, w], ref[:, w])
         np.testing.assert_array_equal(out[:, ~w], pcs.conc[:, ~w])
         assert st["attempts"] == sref["attempts"]
+
+
+@pytest.mark.gpu
+def test_soil_flux_guard_and_clip_fp64_bit_exact(po):
+    """The epilogue's third flux field (added unless the bottom cell would go
+    negative) and a nonzero clip floor on the device, against the oracle."""
+    pcs = small(64)
+    pcs.soil_flux = np.zeros((4, pcs.ncol))
+    pcs.soil_flux[3] = -0.5                   # removes more than some cells hold
+    pcs.soil_flux[0] = 2.0e-4
+    pcs.minimum = np.array([0.0, 0.3, 0.0, 0.0])
+    for method in (EULER, RUNGE_KUTTA_4):
+        out, _ = gpu_run(pcs, capi.SED_FP64, method=method, nruns=2)
+        ref, _, _ = oracle_run(po, pcs, method=method, nruns=2)
+        w = pcs.water()
+        np.testing.assert_array_equal(out[:, w], ref[:, w])
+        assert np.all(out[1][w] >= 0.3)
