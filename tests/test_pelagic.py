@@ -400,7 +400,7 @@ def test_soil_flux_guard_and_clip_fp64_bit_exact(po):
     negative) and a nonzero clip floor on the device, against the oracle."""
     pcs = small(64)
     pcs.soil_flux = np.zeros((4, pcs.ncol))
-    pcs.soil_flux[3] = -0.5                   # removes more than some cells hold
+    pcs.soil_flux[3] = -0.005                 # removes more than some cells hold
     pcs.soil_flux[0] = 2.0e-4
     pcs.minimum = np.array([0.0, 0.3, 0.0, 0.0])
     for method in (EULER, RUNGE_KUTTA_4):
