@@ -786,6 +786,7 @@ void convert(pel_handle* h, const void* in, void* out, size_t n) {
 template <typename real>
 int grid_adaptive(pel_handle* h, real* conc, double hs, long long& attempts) {
   Args<real> a = make_args<real>(h, hs, hs);
+  PK(h->d_rhs.alloc(NTR * h->cells() * sizeof(real)), "rhs buffer");  // grid path only
   real* rhs = h->d_rhs.as<real>();
   const int cb = cell_blocks(h);
   double dt_int = 0.0, dt_red = hs;
@@ -1112,8 +1113,7 @@ int pel_create(const pel_params* p, int inum, int jnum, int knum, int ntr, pel_h
   const size_t cells = h->cells();
   if (h->d_stats.alloc(sizeof(DevStats)) != cudaSuccess ||
       h->d_par.alloc(cells * h->rsize()) != cudaSuccess ||
-      h->d_state.alloc(NTR * cells * h->rsize()) != cudaSuccess ||
-      h->d_rhs.alloc(NTR * cells * h->rsize()) != cudaSuccess) {
+      h->d_state.alloc(NTR * cells * h->rsize()) != cudaSuccess) {
     delete h;
     return SED_E_NOMEM;
   }
