@@ -786,7 +786,7 @@ def run_pelagic(args) -> None:
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
     cpu = None
     if not args.no_cpu:
-        cpu = pel_cpu(pcs, 1, os.cpu_count() or 1, pcs.ncol)
+        cpu = pel_cpu(pcs, 1, os.cpu_count() or 1, args.pel_cpu_columns or pcs.ncol)
         for k in ("seconds", "status", "runs"):
             cpu.pop(k)
     line = {
@@ -829,7 +829,7 @@ def run_reference_pelagic(args) -> None:
     from sedgpu import pelagic
     pcs = pelagic.make_pelagic_workload(PEL_WORKLOAD, seed=args.seed)
     runs = args.steps or 1
-    cpu = pel_cpu(pcs, runs, os.cpu_count() or 1, pcs.ncol)
+    cpu = pel_cpu(pcs, runs, os.cpu_count() or 1, args.pel_cpu_columns or pcs.ncol)
     line = {
         "metric": PEL_METRIC, "value": cpu["value"], "unit": "column-runs/s",
         "n_gpus": args.gpus, "steps": cpu["runs"], "warmup": args.warmup,
@@ -878,6 +878,8 @@ def main():
                     help="with --spinup-years: spin up this many parameter sets at once")
     ap.add_argument("--path", default="sediment", choices=["sediment", "pelagic"],
                     help="pelagic: the fabm_pelagic driver path instead")
+    ap.add_argument("--pel-cpu-columns", type=int, default=0,
+                    help="pelagic CPU baseline: at most this many columns (0: the grid)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3

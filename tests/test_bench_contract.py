@@ -1,0 +1,41 @@
+"""The JSON line of bench.py's reference arm (the oracle on the host cores,
+no GPU needed) for both paths carries the keys of the benchmark contract."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+KEYS = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+        "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config")
+
+
+def run(*extra):
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                          "--steps", "2", "--warmup", "1", *extra],
+                         capture_output=True, text=True, check=True, timeout=600, cwd=ROOT)
+    return json.loads(out.stdout.strip().splitlines()[-1])
+
+
+def check(line):
+    for k in KEYS:
+        assert k in line, k
+    assert line["impl"] == "reference" and line["value"] > 0
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"]
+    assert set(("value", "unit", "sample")) <= set(cb)
+    e2e = line["e2e"]
+    assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
+    assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_sediment():
+    line = run("--cpu-columns", "32")
+    check(line)
+    assert line["unit"] == "column-steps/s" and line["config"]["workload"] == "plain_gpu_256x256"
+
+
+def test_reference_arm_pelagic():
+    line = run("--path", "pelagic", "--pel-cpu-columns", "256")
+    check(line)
+    assert line["unit"] == "column-runs/s" and line["config"]["model"] == "gotm_npzd"
