@@ -18,7 +18,8 @@ from .model import ColumnSet
 
 def partition(kact: np.ndarray, world: int) -> List[Tuple[int, int]]:
     """Contiguous column ranges [c0, c1), one per rank, with about equal
-    active-layer sums (land columns count as nothing)."""
+    active-layer sums (land columns count as nothing).  With more ranks than
+    columns some ranges are empty; such a rank has nothing to step."""
     kact = np.asarray(kact, dtype=np.int64)
     ncol = kact.size
     if world < 1:

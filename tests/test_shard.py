@@ -139,3 +139,15 @@ def test_pelagic_two_gloo_ranks_equal_one_process(tmp_path):
     parts = shard.partition(pcs.water().sum(axis=0), 2)
     w = [int(pcs.water()[:, a:b].sum()) for a, b in parts]
     assert abs(w[0] - w[1]) <= pcs.knum
+
+
+def test_partition_edge_cases():
+    """More ranks than columns, no active column, no column: the ranges stay
+    contiguous and cover the grid; a rank may get an empty range."""
+    for kact, world in ((np.array([5]), 3), (np.zeros(6, dtype=np.int32), 2),
+                        (np.ones(4, dtype=np.int32), 8), (np.array([], dtype=np.int32), 2)):
+        parts = shard.partition(kact, world)
+        assert len(parts) == world
+        assert parts[0][0] == 0 and parts[-1][1] == kact.size
+        assert all(a[1] == b[0] and a[0] <= a[1] for a, b in zip(parts, parts[1:]))
+        assert sum(b - a for a, b in parts) == kact.size
