@@ -29,7 +29,7 @@ SRC = os.path.join(HERE, "pel_oracle.c")
 _PKG = os.path.join(os.path.dirname(HERE), "mossco-code_gb300")
 if _PKG not in sys.path:
     sys.path.insert(0, _PKG)
-from sedgpu.pelagic import NPZD_NAMES, PEL_NTR, PelColumnSet  # noqa: E402
+from sedgpu.pelagic import NPZD_NAMES, PelColumnSet  # noqa: E402
 
 CFLAGS = ["-O3", "-std=gnu11", "-fPIC", "-shared", "-fopenmp",
           "-ffp-contract=off", "-fno-math-errno"]
