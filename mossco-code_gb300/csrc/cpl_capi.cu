@@ -1,0 +1,271 @@
+// cpl_capi.cu -- the pelagic -> soil coupling of include/mossco_cpl.h.
+//
+// One thread per horizontal column reads the pelagic state's bottom layer
+// (k = 0) and writes the sediment handle's boundary staging rows with the
+// arithmetic of pelagic_soil_connector's Run
+// (src/mediators/pelagic_soil_connector.F90:648-2058, 3-D pelagic fields and
+// 2-D soil fields, the branch the reference's set-ups take).  The sediment
+// handle then assembles bdys / fluxes from those rows as sed_set_boundary
+// does.  The work is a few dozen flops per column on about 12 doubles: a
+// pointwise, HBM-bound kernel.  Compiled with -fmad=false so that every
+// product and quotient rounds as the connector's Fortran expression does.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+
+#include "../../include/mossco_cpl.h"
+#include "cpl_internal.h"
+
+namespace {
+
+constexpr int NTR = SED_NTR;
+constexpr int NPART = 6;   // particulate tracers lead the sediment's order
+// sediment tracer rows (sed_tracer_name)
+constexpr int kLabC = 0, kSemC = 1, kLabN = 2, kSemN = 3, kLabP = 4, kOxy = 6, kNit = 7,
+              kAmm = 8, kOdu = 9, kPho = 10;
+
+struct Args {
+  const void* state;
+  int ncol, K;
+  int detN, detC, detP, din, nit, amm, oxy, odu;
+  double sf, sfmin, ncl, ncs, cN, cP, hsd, htke, crit;
+  int as_named;
+  const double* depth;  // null: no water_depth_at_soil_surface
+  const double* tke;    // null: no turbulent_kinetic_energy_at_soil_surface
+  double* surface;      // [NTR][ncol]
+  double* velocity;     // [NTR][ncol]
+};
+
+// Fortran max(0.0, x) of the connector's oxygen split (:830-832)
+__device__ __forceinline__ double pos(double x) { return x > 0.0 ? x : 0.0; }
+
+template <typename real>
+__global__ void k_pelagic_soil(Args a) {
+  const real* st = static_cast<const real*>(a.state);
+  const size_t layer = (size_t)a.K * a.ncol;  // one tracer's block
+  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < a.ncol;
+       col += gridDim.x * blockDim.x) {
+    auto B = [&](int n) { return (double)st[(size_t)n * layer + col]; };
+    double S[NTR];
+    for (int n = 0; n < NTR; n++) S[n] = 0.0;
+    double* V = a.velocity;
+    // ---- detritus (:1035-1236 factors, :1243-1590 fields)
+    if (a.detN >= 0 || a.detP >= 0) {
+      double fenv = 1.0;
+      if (a.depth && a.hsd > (double)1e-3f) {
+        const double d = a.depth[col];
+        fenv = fenv * (d * d) / (d * d + a.hsd * a.hsd);
+      }
+      if (a.tke && a.htke < (double)9e9f) fenv = fenv * a.htke / (a.tke[col] + a.htke);
+      fenv = fenv + a.sfmin / a.sf;
+      if (a.detC >= 0 && a.crit > (double)1e-3f && a.crit < (double)9e9f) {
+        const double t = B(a.detC) / a.crit;
+        const double t2 = t * t;
+        fenv = fenv * 1.0 / (1.0 + t2 * t2);
+      }
+      const double w = a.sf * fenv;
+      if (a.detN >= 0) {
+        const double N = B(a.detN);
+        if (a.as_named) {
+          double CN = 106.0 / 16.0;
+          if (a.detC >= 0) CN = B(a.detC) / ((double)1e-5f + N);
+          double fl = (1.0 - a.ncs * CN) / (a.ncl - a.ncs);
+          double rl = fl * a.ncl;
+          if (fl > CN) { fl = CN; rl = 1.0; }
+          if (fl < 0.0) { fl = 0.0; rl = 0.0; }
+          const double fs = CN - fl;
+          const double rs = 1.0 - rl;
+          S[kLabC] = fl * a.cN * N;
+          S[kSemC] = fs * a.cN * N;
+          S[kLabN] = rl * a.cN * N;
+          S[kSemN] = rs * a.cN * N;
+          for (int n = kLabC; n <= kSemN; n++) V[(size_t)n * a.ncol + col] = w * N;
+        } else {
+          for (int n = kLabC; n <= kSemN; n++) S[n] = w * N;
+        }
+        S[kLabP] = 1.0 / 16.0 * a.cN * N;
+        V[(size_t)kLabP * a.ncol + col] = w * N;
+      }
+      if (a.detP >= 0) S[kLabP] = B(a.detP);
+    }
+    // ---- oxygen and its deficit (:811-866)
+    if (a.oxy >= 0 && a.odu >= 0) {
+      S[kOxy] = B(a.oxy);
+      S[kOdu] = B(a.odu);
+    } else if (a.odu >= 0) {
+      const double x = B(a.odu);
+      S[kOxy] = pos(-x);
+      S[kOdu] = pos(x);
+    } else if (a.oxy >= 0) {
+      S[kOxy] = B(a.oxy);
+    }
+    // ---- dissolved nitrogen and phosphate (:1743-2003)
+    const bool hN = a.nit >= 0, hA = a.amm >= 0, hD = a.din >= 0;
+    const double Nt = hN ? B(a.nit) : 0.0;
+    const double A = hA ? B(a.amm) : 0.0;
+    const double D = hD ? B(a.din) : 0.0;
+    S[kAmm] = hA ? a.cN * A
+            : (hD && hN) ? a.cN * (D - Nt)
+            : hD ? a.cN * 0.5 * D
+            : a.cN * Nt;
+    S[kNit] = hN ? a.cN * Nt
+            : (hA && hD) ? a.cN * (D - A)
+            : hD ? a.cN * 0.5 * D
+            : a.cN * A;
+    const double din = hD ? D : (hA && hN) ? Nt + A : hA ? 2 * A : 2 * Nt;
+    S[kPho] = a.cP * (1.0 / 16.0 * a.cN * din);
+    for (int n = 0; n < NTR; n++) a.surface[(size_t)n * a.ncol + col] = S[n];
+  }
+}
+
+bool bad_index(int i) { return i < -1 || i >= PEL_NTR; }
+
+}  // namespace
+
+extern "C" {
+
+int cpl_default_params(cpl_params* p) {
+  if (!p) return SED_E_ARG;
+  memset(p, 0, sizeof *p);
+  // pelagic_soil_connector.F90:38-45; the literals without a kind suffix
+  // are default reals, so 0.02 and 0.1 are their single-precision values
+  p->sinking_factor = 0.3;
+  p->sinking_factor_min = (double)0.02f;
+  p->NC_ldet = 0.23;
+  p->NC_sdet = 0.01;
+  p->convertN = 1.0;
+  p->convertP = 1.0;
+  p->half_sedimentation_depth = (double)0.1f;
+  p->half_sedimentation_tke = 1.0e3;
+  p->critical_detritus = 60.0;
+  p->mode = CPL_AS_RUN;
+  return SED_OK;
+}
+
+int cpl_npzd_fields(cpl_fields* f) {
+  if (!f) return SED_E_ARG;
+  f->detN = 3;
+  f->detC = -1;
+  f->detP = -1;
+  f->din = 0;
+  f->nitrate = -1;
+  f->ammonium = -1;
+  f->oxygen = -1;
+  f->odu = -1;
+  return SED_OK;
+}
+
+int cpl_pelagic_soil(pel_handle* pel, sed_handle* sed, const cpl_params* p,
+                     const cpl_fields* f, const double* temperature,
+                     const double* water_depth, const double* tke,
+                     const double* velocity_in, double* surface_out,
+                     double* velocity_out, int* present_out) {
+  if (!sed) return SED_E_ARG;
+  if (!pel) return cpl::sed_fail(sed, SED_E_ARG, "pelagic handle is NULL");
+  if (!p || !f || !temperature)
+    return cpl::sed_fail(sed, SED_E_ARG, "params, fields and temperature are required");
+  for (int i : {f->detN, f->detC, f->detP, f->din, f->nitrate, f->ammonium, f->oxygen, f->odu})
+    if (bad_index(i)) return cpl::sed_fail(sed, SED_E_ARG, "field index out of range");
+  if (f->din < 0 && f->nitrate < 0 && f->ammonium < 0)
+    return cpl::sed_fail(sed, SED_E_ARG, "no nitrate, ammonium or DIN field");
+  if (p->mode != CPL_AS_RUN && p->mode != CPL_AS_NAMED)
+    return cpl::sed_fail(sed, SED_E_ARG, "mode must be CPL_AS_RUN or CPL_AS_NAMED");
+  if ((f->detN >= 0 || f->detP >= 0) && !(p->sinking_factor != 0.0))
+    return cpl::sed_fail(sed, SED_E_ARG, "sinking_factor must be nonzero");
+  cpl::PelView v;
+  if (int rc = cpl::pel_view(pel, &v)) {
+    std::string m = std::string("pelagic handle: ") + pel_last_error(pel);
+    return cpl::sed_fail(sed, rc, m.c_str());
+  }
+  cpl::SedStaging s;
+  if (int rc = cpl::sed_staging(sed, &s)) return rc;
+  if (v.ncol != s.ncol)
+    return cpl::sed_fail(sed, SED_E_ARG, "the handles' grids differ in inum*jnum");
+  if (v.device != s.device)
+    return cpl::sed_fail(sed, SED_E_ARG, "the handles are on different devices");
+  const size_t nc = (size_t)s.ncol;
+  cudaError_t e = cudaSuccess;
+  auto ok = [&](cudaError_t r) { if (e == cudaSuccess) e = r; return r == cudaSuccess; };
+  // the pelagic handle's pending work (a pel_step) before the reads
+  cudaEvent_t ev = nullptr;
+  ok(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  if (e == cudaSuccess) {
+    ok(cudaEventRecord(ev, v.stream));
+    ok(cudaStreamWaitEvent(s.stream, ev, 0));
+  }
+  if (ev) cudaEventDestroy(ev);
+  ok(cudaMemcpyAsync(s.temperature, temperature, nc * sizeof(double), cudaMemcpyHostToDevice,
+                     s.stream));
+  if (velocity_in)
+    ok(cudaMemcpyAsync(s.velocity, velocity_in, (size_t)NPART * nc * sizeof(double),
+                       cudaMemcpyHostToDevice, s.stream));
+  else
+    ok(cudaMemsetAsync(s.velocity, 0, (size_t)NPART * nc * sizeof(double), s.stream));
+  double* d_depth = s.spare;
+  double* d_tke = s.spare + nc;
+  if (water_depth)
+    ok(cudaMemcpyAsync(d_depth, water_depth, nc * sizeof(double), cudaMemcpyHostToDevice,
+                       s.stream));
+  if (tke)
+    ok(cudaMemcpyAsync(d_tke, tke, nc * sizeof(double), cudaMemcpyHostToDevice, s.stream));
+  if (e != cudaSuccess) {
+    std::string m = std::string("coupling copies: ") + cudaGetErrorString(e);
+    return cpl::sed_fail(sed, SED_E_CUDA, m.c_str());
+  }
+  Args a{};
+  a.state = v.state;
+  a.ncol = s.ncol;
+  a.K = v.K;
+  a.detN = f->detN; a.detC = f->detC; a.detP = f->detP; a.din = f->din;
+  a.nit = f->nitrate; a.amm = f->ammonium; a.oxy = f->oxygen; a.odu = f->odu;
+  a.sf = p->sinking_factor; a.sfmin = p->sinking_factor_min;
+  a.ncl = p->NC_ldet; a.ncs = p->NC_sdet; a.cN = p->convertN; a.cP = p->convertP;
+  a.hsd = p->half_sedimentation_depth; a.htke = p->half_sedimentation_tke;
+  a.crit = p->critical_detritus;
+  a.as_named = p->mode == CPL_AS_NAMED;
+  a.depth = water_depth ? d_depth : nullptr;
+  a.tke = tke ? d_tke : nullptr;
+  a.surface = s.surface;
+  a.velocity = s.velocity;
+  const int threads = 256;
+  long long blocks = ((long long)nc + threads - 1) / threads;
+  const long long cap = (long long)(s.sms > 0 ? s.sms : 1) * 8;
+  if (blocks > cap) blocks = cap;
+  if (v.fp64)
+    k_pelagic_soil<double><<<(int)blocks, threads, 0, s.stream>>>(a);
+  else
+    k_pelagic_soil<float><<<(int)blocks, threads, 0, s.stream>>>(a);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    std::string m = std::string("coupling kernel launch: ") + cudaGetErrorString(e);
+    return cpl::sed_fail(sed, SED_E_CUDA, m.c_str());
+  }
+  cpl::sed_count_launch(sed);
+  unsigned mask = (1u << kNit) | (1u << kAmm) | (1u << kPho);
+  if (f->detN >= 0) mask |= (1u << kLabC) | (1u << kSemC) | (1u << kLabN) | (1u << kSemN) |
+                           (1u << kLabP);
+  if (f->detP >= 0) mask |= 1u << kLabP;
+  if (f->oxygen >= 0 || f->odu >= 0) mask |= 1u << kOxy;
+  if (f->odu >= 0) mask |= 1u << kOdu;
+  if (int rc = cpl::sed_assemble_staged(sed, mask)) return rc;
+  if (surface_out)
+    ok(cudaMemcpyAsync(surface_out, s.surface, (size_t)NTR * nc * sizeof(double),
+                       cudaMemcpyDeviceToHost, s.stream));
+  if (velocity_out) {
+    ok(cudaMemsetAsync(s.velocity + (size_t)NPART * nc, 0, (size_t)(NTR - NPART) * nc *
+                       sizeof(double), s.stream));
+    ok(cudaMemcpyAsync(velocity_out, s.velocity, (size_t)NTR * nc * sizeof(double),
+                       cudaMemcpyDeviceToHost, s.stream));
+  }
+  ok(cudaStreamSynchronize(s.stream));
+  if (e != cudaSuccess) {
+    std::string m = std::string("coupling read-back: ") + cudaGetErrorString(e);
+    return cpl::sed_fail(sed, SED_E_CUDA, m.c_str());
+  }
+  if (present_out)
+    for (int n = 0; n < NTR; n++) present_out[n] = (mask >> n) & 1u;
+  return SED_OK;
+}
+
+}  // extern "C"

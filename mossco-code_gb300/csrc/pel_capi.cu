@@ -17,6 +17,7 @@
 // separate light / rhs / test / accept / epilogue kernels with the decision
 // read back on the host, as the parity mode.
 #include "mossco_pel.h"
+#include "cpl_internal.h"
 
 #include <cuda_runtime.h>
 
@@ -1336,3 +1337,15 @@ int pel_step(pel_handle* h, double t_couple, double dt, int method, int nruns,
 }
 
 }  // extern "C"
+
+int cpl::pel_view(pel_handle* h, PelView* v) {
+  if (!h || !v) return SED_E_ARG;
+  if (int rc = need(h, true, false, true, false)) return rc;
+  v->state = h->d_state.p;
+  v->fp64 = h->fp64();
+  v->ncol = h->ncol;
+  v->K = h->K;
+  v->device = h->device;
+  v->stream = h->stream;
+  return SED_OK;
+}

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/mossco_sed.h"
+#include "cpl_internal.h"
 #include "sed_launch.h"
 #include "sed_params.h"
 #include "sur_internal.h"
@@ -1685,22 +1686,53 @@ int sed_set_boundary(sed_handle* h, const double* temperature, const double* sur
   const unsigned part = (1u << NPART) - 1u;
   if ((mask & part) && !velocity)
     return h->fail(SED_E_ARG, "velocity is required for the particulate tracers present");
+  cpl::SedStaging s;
+  if (int rc = cpl::sed_staging(h, &s)) return rc;
+  const size_t nc = (size_t)h->ncol;
+  CK(cudaMemcpyAsync(s.temperature, temperature, nc * sizeof(double), cudaMemcpyHostToDevice,
+                     h->stream), "temperature copy");
+  CK(cudaMemcpyAsync(s.surface, surface, (size_t)NTR * nc * sizeof(double),
+                     cudaMemcpyHostToDevice, h->stream), "surface copy");
+  if (velocity)  // only the particulate rows are read
+    CK(cudaMemcpyAsync(s.velocity, velocity, (size_t)NPART * nc * sizeof(double),
+                       cudaMemcpyHostToDevice, h->stream), "velocity copy");
+  return cpl::sed_assemble_staged(h, mask);
+}
+
+}  // extern "C"
+
+int cpl::sed_staging(sed_handle* h, SedStaging* s) {
+  if (!h || !s) return SED_E_ARG;
+  if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
+  CK(cudaSetDevice(h->device), "set device");
+  const size_t nc = (size_t)h->ncol;
+  CK(h->d_bcin.alloc((3 + 2 * (size_t)NTR) * nc * sizeof(double)), "boundary staging");
+  s->temperature = h->d_bcin.as<double>();
+  s->surface = s->temperature + nc;
+  s->velocity = s->surface + (size_t)NTR * nc;
+  s->spare = s->velocity + (size_t)NTR * nc;
+  s->ncol = h->ncol;
+  s->device = h->device;
+  s->sms = h->sms;
+  s->stream = h->stream;
+  return SED_OK;
+}
+
+int cpl::sed_fail(sed_handle* h, int code, const char* msg) {
+  return h ? h->fail(code, "%s", msg) : code;
+}
+
+void cpl::sed_count_launch(sed_handle* h) { h->launches++; }
+
+int cpl::sed_assemble_staged(sed_handle* h, unsigned mask) {
+  const unsigned part = (1u << NPART) - 1u;
   if (h->prm.bcup_dissolved == 1 && (mask & ~part) && !h->have_state)
     return h->fail(SED_E_STATE, "the dissolved flux estimate needs the state: call "
                                 "sed_set_state first");
-  CK(cudaSetDevice(h->device), "set device");
   const size_t nc = (size_t)h->ncol;
-  CK(h->d_bcin.alloc((1 + 2 * (size_t)NTR) * nc * sizeof(double)), "boundary staging");
   double* bt = h->d_bcin.as<double>();
   double* bs = bt + nc;
   double* bv = bs + (size_t)NTR * nc;
-  CK(cudaMemcpyAsync(bt, temperature, nc * sizeof(double), cudaMemcpyHostToDevice, h->stream),
-     "temperature copy");
-  CK(cudaMemcpyAsync(bs, surface, (size_t)NTR * nc * sizeof(double), cudaMemcpyHostToDevice,
-                     h->stream), "surface copy");
-  if (velocity)  // only the particulate rows are read
-    CK(cudaMemcpyAsync(bv, velocity, (size_t)NPART * nc * sizeof(double),
-                       cudaMemcpyHostToDevice, h->stream), "velocity copy");
   cudaError_t e =
       h->fp64()
           ? launch_assemble_bc<double>(bt, bs, bv, mask, h->d_conc.as<double>(),
@@ -1733,6 +1765,8 @@ int sed_set_boundary(sed_handle* h, const double* temperature, const double* sur
   h->have_forcing = true;
   return SED_OK;
 }
+
+extern "C" {
 
 int sed_get_boundary(sed_handle* h, double* bdys, double* fluxes) {
   if (!h) return SED_E_ARG;

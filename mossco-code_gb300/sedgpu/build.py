@@ -24,7 +24,8 @@ LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 SOURCES = ["sed_kernels_f32.cu", "sed_kernels_f64.cu", "sed_kernels_f32_bio3.cu",
            "sed_kernels_f64_bio3.cu", "sed_kernels_warp.cu", "sed_kernels_warp_bio3.cu",
            "sed_capi.cu", "sed_noalloc.cu", "sur_kernels.cu", "sur_capi.cu", "sur_loop.cu",
-           "sed_kernels_warp_ens.cu", "sed_kernels_warp_ens_bio3.cu", "pel_capi.cu"]
+           "sed_kernels_warp_ens.cu", "sed_kernels_warp_ens_bio3.cu", "pel_capi.cu",
+           "cpl_capi.cu"]
 # The FP64 kernels evaluate the reference's arithmetic operation by
 # operation: no multiply-add contraction.
 # The FP32 kernels write every fused multiply-add explicitly (fmaf): without
@@ -38,9 +39,10 @@ EXTRA_FLAGS = {"sed_kernels_f64.cu": ["-fmad=false"],
                "sed_kernels_warp_bio3.cu": ["-fmad=false"],
                "sed_kernels_warp_ens.cu": ["-fmad=false"],
                "sed_kernels_warp_ens_bio3.cu": ["-fmad=false"],
-               "pel_capi.cu": ["-fmad=false"]}
+               "pel_capi.cu": ["-fmad=false"],
+               "cpl_capi.cu": ["-fmad=false"]}
 HEADERS = ["sed_device.cuh", "sed_kernels.cuh", "sed_launch.h", "sed_params.h",
-           "sur_kernels.h", "sur_internal.h", "sur_loop.h"]
+           "sur_kernels.h", "sur_internal.h", "sur_loop.h", "cpl_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no multiply-add contraction either (aarch64 g++ contracts by
 # default), so host-side FP64 forcing rows match the CPU restatement's
@@ -61,6 +63,7 @@ def _deps():
     files = [os.path.join(CSRC, f) for f in SOURCES + HEADERS]
     files.append(os.path.join(INCLUDE, "mossco_sed.h"))
     files.append(os.path.join(INCLUDE, "mossco_pel.h"))
+    files.append(os.path.join(INCLUDE, "mossco_cpl.h"))
     files.append(os.path.abspath(__file__))
     return files
 

@@ -1,0 +1,188 @@
+/*
+ * cpl_oracle.c -- FP64 CPU oracle of MOSSCO's pelagic_soil_connector Run.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Imported by tests/ (through pel_oracle.py) to
+ * check the device coupling; the product never links it.
+ *
+ * Restates src/mediators/pelagic_soil_connector.F90 Run (:176-2060) for 3-D
+ * pelagic fields and 2-D soil fields, statement by statement and in the
+ * Run's order: each whole-array Fortran assignment is one loop over the
+ * columns, and a field the Run writes twice is written twice here.  The ESMF
+ * lookups by name become the pelagic tracer indices of orc_cpl_fields; the
+ * bottom layer is k = 0 (the Run's lbnd(3)).  Literals without a kind
+ * suffix are default (single-precision) reals in the reference and appear
+ * here as float constants widened to double.
+ *
+ * Soil tracer rows (the sediment's OMEXDIA+P order): 0 labile C, 1
+ * semilabile C, 2 labile N, 3 semilabile N, 4 labile P, 5 adsorbed P, 6 O2,
+ * 7 NO3, 8 NH4, 9 ODU, 10 PO4.
+ *
+ * Parity: PINNED only to the reference's source text; the connector has no
+ * test and no example output in the reference tree.
+ */
+#include "cpl_oracle.h"
+
+#include <stdlib.h>
+
+enum { LC = 0, SC = 1, LN = 2, SN = 3, LP = 4, OX = 6, NI = 7, AM = 8, OD = 9, PH = 10 };
+
+void orc_cpl_defaults(orc_cpl *p) {
+  /* :38-45 */
+  p->sinking_factor = 0.3;
+  p->NC_ldet = 0.23;
+  p->NC_sdet = 0.01;
+  p->convertN = 1.0;
+  p->convertP = 1.0;
+  p->sinking_factor_min = (double)0.02f;
+  p->half_sedimentation_depth = (double)0.1f;
+  p->half_sedimentation_tke = 1.0e3;
+  p->critical_detritus = 60.0;
+  p->as_named = 0;
+}
+
+/* bottom-layer value of pelagic tracer n in column i */
+static double bot(const double *conc, int n, int ncol, int knum, int i) {
+  return conc[(size_t)n * knum * ncol + i];
+}
+
+int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
+                int ncol, int knum, const double *depth, const double *tke,
+                double *surface, double *velocity, int *present) {
+  const double one_e5 = (double)1e-5f, one_e3 = (double)1e-3f, nine_e9 = (double)9e9f;
+  double *CN = malloc(sizeof(double) * ncol), *fl = malloc(sizeof(double) * ncol),
+         *rl = malloc(sizeof(double) * ncol), *fs = malloc(sizeof(double) * ncol),
+         *rs = malloc(sizeof(double) * ncol), *fe = malloc(sizeof(double) * ncol),
+         *din = malloc(sizeof(double) * ncol);
+  int i, n;
+  for (n = 0; n < 11; n++) present[n] = 0;
+#define ROW(a, r) ((a) + (size_t)(r) * ncol)
+#define B(fld) bot(conc, (fld), ncol, knum, i)
+
+  /* oxygen and its deficit, :811-866 (both found / deficit only / oxygen
+   * only; the oxygen-only branch of the reference reads the deficit's
+   * pointers, which are not associated then: here oxygen alone is copied) */
+  if (f->oxygen >= 0 && f->odu >= 0) {
+    for (i = 0; i < ncol; i++) ROW(surface, OX)[i] = B(f->oxygen);
+    for (i = 0; i < ncol; i++) ROW(surface, OD)[i] = B(f->odu);
+    present[OX] = present[OD] = 1;
+  } else if (f->odu >= 0) {
+    for (i = 0; i < ncol; i++) {
+      const double x = -B(f->odu);
+      ROW(surface, OX)[i] = x > 0.0 ? x : 0.0;
+    }
+    for (i = 0; i < ncol; i++) {
+      const double x = B(f->odu);
+      ROW(surface, OD)[i] = x > 0.0 ? x : 0.0;
+    }
+    present[OX] = present[OD] = 1;
+  } else if (f->oxygen >= 0) {
+    for (i = 0; i < ncol; i++) ROW(surface, OX)[i] = B(f->oxygen);
+    present[OX] = 1;
+  }
+
+  /* C:N of the detritus, :1038-1072 */
+  for (i = 0; i < ncol; i++) CN[i] = 106.0 / 16.0;
+  if (f->detN >= 0 && f->detC >= 0)
+    for (i = 0; i < ncol; i++) CN[i] = B(f->detC) / (one_e5 + B(f->detN));
+
+  /* labile / semilabile factors, :1077-1098 */
+  for (i = 0; i < ncol; i++) fl[i] = (1.0 - p->NC_sdet * CN[i]) / (p->NC_ldet - p->NC_sdet);
+  for (i = 0; i < ncol; i++) rl[i] = fl[i] * p->NC_ldet;
+  for (i = 0; i < ncol; i++)
+    if (fl[i] > CN[i]) { fl[i] = CN[i]; rl[i] = 1.0; }
+  for (i = 0; i < ncol; i++)
+    if (fl[i] < 0.0) { fl[i] = 0.0; rl[i] = 0.0; }
+  for (i = 0; i < ncol; i++) fs[i] = CN[i] - fl[i];
+  for (i = 0; i < ncol; i++) rs[i] = 1.0 - rl[i];
+  for (i = 0; i < ncol; i++) fe[i] = 1.0;
+
+  /* water depth, :1126-1160 */
+  if (depth && p->half_sedimentation_depth > one_e3)
+    for (i = 0; i < ncol; i++)
+      fe[i] = fe[i] * (depth[i] * depth[i]) /
+              (depth[i] * depth[i] + p->half_sedimentation_depth * p->half_sedimentation_depth);
+  /* turbulence, :1164-1198 */
+  if (tke && p->half_sedimentation_tke < nine_e9)
+    for (i = 0; i < ncol; i++)
+      fe[i] = fe[i] * p->half_sedimentation_tke / (tke[i] + p->half_sedimentation_tke);
+  /* minimum sedimentation, :1202-1210 */
+  for (i = 0; i < ncol; i++) fe[i] = fe[i] + p->sinking_factor_min / p->sinking_factor;
+  /* detritus carbon above critical_detritus, :1213-1236 */
+  if (f->detC >= 0 && p->critical_detritus > one_e3 && p->critical_detritus < nine_e9)
+    for (i = 0; i < ncol; i++) {
+      const double x = B(f->detC) / p->critical_detritus;
+      const double x2 = x * x;
+      fe[i] = fe[i] * 1.0 / (1.0 + x2 * x2);
+    }
+
+  /* labile carbon, semilabile carbon, labile nitrogen, semilabile nitrogen,
+   * :1243-1490: the concentration, then the velocity formula into
+   * fieldList(1) again (the concentration: the Run as written) or into the
+   * z-velocity field (as_named) */
+  if (f->detN >= 0) {
+    const double *fac[4] = {fl, fs, rl, rs};
+    const int row[4] = {LC, SC, LN, SN};
+    int b;
+    for (b = 0; b < 4; b++) {
+      double *dst = ROW(surface, row[b]);
+      for (i = 0; i < ncol; i++) dst[i] = fac[b][i] * p->convertN * B(f->detN);
+      dst = p->as_named ? ROW(velocity, row[b]) : ROW(surface, row[b]);
+      for (i = 0; i < ncol; i++) dst[i] = p->sinking_factor * fe[i] * B(f->detN);
+      present[row[b]] = 1;
+    }
+  }
+  /* phosphorus, :1492-1590 */
+  if (f->detN >= 0) {
+    for (i = 0; i < ncol; i++) ROW(surface, LP)[i] = 1.0 / 16.0 * p->convertN * B(f->detN);
+    present[LP] = 1;
+  }
+  if (f->detP >= 0) {
+    for (i = 0; i < ncol; i++) ROW(surface, LP)[i] = B(f->detP);
+    present[LP] = 1;
+  }
+  if (f->detN >= 0)
+    for (i = 0; i < ncol; i++)
+      ROW(velocity, LP)[i] = p->sinking_factor * fe[i] * B(f->detN);
+
+  /* ammonium, :1743-1838 */
+  {
+    const int hN = f->nitrate >= 0, hA = f->ammonium >= 0, hD = f->din >= 0;
+    if (!hN && !hA && !hD) {
+      free(CN); free(fl); free(rl); free(fs); free(rs); free(fe); free(din);
+      return -1;
+    }
+    for (i = 0; i < ncol; i++) {
+      double v;
+      if (hA) v = p->convertN * B(f->ammonium);
+      else if (hD && hN) v = p->convertN * (B(f->din) - B(f->nitrate));
+      else if (hD) v = p->convertN * 0.5 * B(f->din);
+      else v = p->convertN * B(f->nitrate);
+      ROW(surface, AM)[i] = v;
+    }
+    /* nitrate, :1840-1935 */
+    for (i = 0; i < ncol; i++) {
+      double v;
+      if (hN) v = p->convertN * B(f->nitrate);
+      else if (hA && hD) v = p->convertN * (B(f->din) - B(f->ammonium));
+      else if (hD) v = p->convertN * 0.5 * B(f->din);
+      else v = p->convertN * B(f->ammonium);
+      ROW(surface, NI)[i] = v;
+    }
+    /* phosphate from DIN (a DIP field is overwritten, not read), :1938-2003 */
+    for (i = 0; i < ncol; i++) {
+      if (hD) din[i] = B(f->din);
+      else if (hA && hN) din[i] = B(f->nitrate) + B(f->ammonium);
+      else if (hA) din[i] = 2 * B(f->ammonium);
+      else din[i] = 2 * B(f->nitrate);
+    }
+    for (i = 0; i < ncol; i++) {
+      const double dip = 1.0 / 16.0 * p->convertN * din[i];
+      ROW(surface, PH)[i] = p->convertP * dip;
+    }
+    present[AM] = present[NI] = present[PH] = 1;
+  }
+#undef B
+#undef ROW
+  free(CN); free(fl); free(rl); free(fs); free(rs); free(fe); free(din);
+  return 0;
+}

@@ -25,26 +25,32 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libpeloracle.so")
 SRC = os.path.join(HERE, "pel_oracle.c")
+SRCS = [SRC, os.path.join(HERE, "cpl_oracle.c")]
 
 _PKG = os.path.join(os.path.dirname(HERE), "mossco-code_gb300")
 if _PKG not in sys.path:
     sys.path.insert(0, _PKG)
 from sedgpu.pelagic import NPZD_NAMES, PelColumnSet  # noqa: E402
 
+# pelagic_soil_connector's namelist and looked-up fields (cpl_oracle.h)
+CPL_PARAM_NAMES = ("sinking_factor", "sinking_factor_min", "NC_ldet", "NC_sdet", "convertN",
+                   "convertP", "half_sedimentation_depth", "half_sedimentation_tke",
+                   "critical_detritus")
+CPL_FIELD_NAMES = ("detN", "detC", "detP", "din", "nitrate", "ammonium", "oxygen", "odu")
+
 CFLAGS = ["-O3", "-std=gnu11", "-fPIC", "-shared", "-fopenmp",
           "-ffp-contract=off", "-fno-math-errno"]
 
 
 def build(force: bool = False) -> str:
-    """Compile the pelagic oracle with gcc into oracle/_build."""
+    """Compile the pelagic and connector oracles with gcc into oracle/_build."""
     os.makedirs(BUILD_DIR, exist_ok=True)
-    hdr = os.path.join(HERE, "pel_oracle.h")
+    deps = SRCS + [os.path.join(HERE, h) for h in ("pel_oracle.h", "cpl_oracle.h")]
     if (not force and os.path.exists(LIB_PATH)
-            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC)
-            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(hdr)):
+            and all(os.path.getmtime(LIB_PATH) >= os.path.getmtime(d) for d in deps)):
         return LIB_PATH
     tmp = LIB_PATH + f".tmp{os.getpid()}"
-    subprocess.check_call(["gcc", *CFLAGS, SRC, "-o", tmp, "-lm"])
+    subprocess.check_call(["gcc", *CFLAGS, *SRCS, "-o", tmp, "-lm"])
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
@@ -76,6 +82,14 @@ class PelStats(ctypes.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class OrcCpl(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in CPL_PARAM_NAMES] + [("as_named", ctypes.c_int)]
+
+
+class OrcCplFields(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in CPL_FIELD_NAMES]
+
+
 _lib = None
 
 
@@ -95,6 +109,11 @@ def lib():
         L.orc_pel_run.argtypes = [P(Pel), _dp, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_int, P(PelStats), _dp, ctypes.c_int]
         L.orc_pel_run.restype = ctypes.c_int
+        L.orc_cpl_defaults.argtypes = [P(OrcCpl)]
+        L.orc_cpl_defaults.restype = None
+        L.orc_cpl_run.argtypes = [P(OrcCpl), P(OrcCplFields), _dp, ctypes.c_int, ctypes.c_int,
+                                  _dp, _dp, _dp, _dp, P(ctypes.c_int)]
+        L.orc_cpl_run.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -198,3 +217,36 @@ class PelOracle:
             if rc:
                 break
         return rc, tot, par
+
+
+def cpl_defaults() -> dict:
+    p = OrcCpl()
+    lib().orc_cpl_defaults(ctypes.byref(p))
+    return {n: getattr(p, n) for n in CPL_PARAM_NAMES}
+
+
+def cpl_run(conc: np.ndarray, fields: dict, params: Optional[dict] = None,
+            as_named: bool = False, depth=None, tke=None, velocity_in=None):
+    """One pelagic_soil_connector Run on the pelagic state conc [ntr][knum][ncol].
+
+    Returns (rc, surface [11][ncol], velocity [11][ncol], present [11]); the
+    soil fields start at zero (velocity at velocity_in's particulate rows)."""
+    conc = np.ascontiguousarray(conc, dtype=np.float64)
+    ntr, knum, ncol = conc.shape
+    p = OrcCpl()
+    lib().orc_cpl_defaults(ctypes.byref(p))
+    for k, v in (params or {}).items():
+        setattr(p, k, float(v))
+    p.as_named = int(bool(as_named))
+    f = OrcCplFields(*[int(fields.get(n, -1)) for n in CPL_FIELD_NAMES])
+    surface = np.zeros((11, ncol))
+    velocity = np.zeros((11, ncol))
+    if velocity_in is not None:
+        velocity[:6] = np.asarray(velocity_in, dtype=np.float64)[:6]
+    present = np.zeros(11, dtype=np.int32)
+    f64 = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+    d, t = f64(depth), f64(tke)
+    rc = lib().orc_cpl_run(ctypes.byref(p), ctypes.byref(f), _ptr(conc), ncol, knum, _ptr(d),
+                           _ptr(t), _ptr(surface), _ptr(velocity),
+                           present.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return rc, surface, velocity, present
