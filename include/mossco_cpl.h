@@ -2,7 +2,7 @@
  * mossco_cpl.h -- C ABI of the pelagic -> soil coupling on the device.
  *
  * Replaces the Run of MOSSCO's pelagic_soil_connector
- * (src/mediators/pelagic_soil_connector.F90:176-2060) between a pelagic
+ * (src/mediators/pelagic_soil_connector.F90:176-2122) between a pelagic
  * handle (mossco_pel.h) and a sediment handle (mossco_sed.h) on the same
  * inum x jnum grid.  The pelagic state's bottom layer (k = 0, the
  * connector's lbnd(3)) becomes the sediment's "_at_soil_surface" fields,
@@ -31,7 +31,7 @@ extern "C" {
  * CPL_AS_RUN: as the connector's Run writes them.  For labile and
  *   semilabile carbon and nitrogen it looks up the concentration and the
  *   z-velocity field together and writes the velocity formula into
- *   fieldList(1) again (:1265-1273 and the three blocks after it); with
+ *   fieldList(1) again (:1287-1296 and the three blocks after it); with
  *   exact-name matching that is the concentration field in both ESMF item
  *   orders, so these concentrations carry sinking_factor*fac_env*detN and
  *   their velocities keep what the fields held (velocity_in, or 0 as the
@@ -87,7 +87,7 @@ int cpl_npzd_fields(cpl_fields *f);
  * The pelagic handle needs its state (pel_set_state or a step), the
  * sediment handle its grid, and with bcup_dissolved = 1 its state.  No
  * nitrate, ammonium or DIN field: SED_E_ARG (the Run returns
- * ESMF_RC_NOT_FOUND, :1834-1836).  Both handles on one device. */
+ * ESMF_RC_NOT_FOUND, :1806,1855).  Both handles on one device. */
 int cpl_pelagic_soil(pel_handle *pel, sed_handle *sed, const cpl_params *p,
                      const cpl_fields *f, const double *temperature,
                      const double *water_depth, const double *tke,

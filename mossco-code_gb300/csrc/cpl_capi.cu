@@ -3,7 +3,7 @@
 // One thread per horizontal column reads the pelagic state's bottom layer
 // (k = 0) and writes the sediment handle's boundary staging rows with the
 // arithmetic of pelagic_soil_connector's Run
-// (src/mediators/pelagic_soil_connector.F90:648-2058, 3-D pelagic fields and
+// (src/mediators/pelagic_soil_connector.F90:648-2110, 3-D pelagic fields and
 // 2-D soil fields, the branch the reference's set-ups take).  The sediment
 // handle then assembles bdys / fluxes from those rows as sed_set_boundary
 // does.  The work is a few dozen flops per column on about 12 doubles: a
@@ -37,7 +37,7 @@ struct Args {
   double* velocity;     // [NTR][ncol]
 };
 
-// Fortran max(0.0, x) of the connector's oxygen split (:830-832)
+// Fortran max(0.0, x) of the connector's oxygen split (:823-844)
 __device__ __forceinline__ double pos(double x) { return x > 0.0 ? x : 0.0; }
 
 template <typename real>
@@ -50,7 +50,7 @@ __global__ void k_pelagic_soil(Args a) {
     double S[NTR];
     for (int n = 0; n < NTR; n++) S[n] = 0.0;
     double* V = a.velocity;
-    // ---- detritus (:1035-1236 factors, :1243-1590 fields)
+    // ---- detritus (:1018-1236 factors, :1243-1646 fields)
     if (a.detN >= 0 || a.detP >= 0) {
       double fenv = 1.0;
       if (a.depth && a.hsd > (double)1e-3f) {
@@ -89,7 +89,7 @@ __global__ void k_pelagic_soil(Args a) {
       }
       if (a.detP >= 0) S[kLabP] = B(a.detP);
     }
-    // ---- oxygen and its deficit (:811-866)
+    // ---- oxygen and its deficit (:801-866)
     if (a.oxy >= 0 && a.odu >= 0) {
       S[kOxy] = B(a.oxy);
       S[kOdu] = B(a.odu);
@@ -100,7 +100,7 @@ __global__ void k_pelagic_soil(Args a) {
     } else if (a.oxy >= 0) {
       S[kOxy] = B(a.oxy);
     }
-    // ---- dissolved nitrogen and phosphate (:1743-2003)
+    // ---- dissolved nitrogen and phosphate (:1648-2110)
     const bool hN = a.nit >= 0, hA = a.amm >= 0, hD = a.din >= 0;
     const double Nt = hN ? B(a.nit) : 0.0;
     const double A = hA ? B(a.amm) : 0.0;

@@ -23,6 +23,9 @@ module sed_gpu
   integer, parameter, public :: SED_E_NODEVICE = -7
   integer, parameter, public :: SED_FP32 = 0, SED_FP64 = 1
   integer, parameter, public :: SED_CUT_PER_COLUMN = 0, SED_CUT_GLOBAL = 1
+  !> ode_solver methods (solver_library.F90:32-35)
+  integer, parameter, public :: SED_EULER = 0, SED_RUNGE_KUTTA_4 = 1, &
+                                SED_ADAPTIVE_EULER = 2, SED_RUNGE_KUTTA_4_38 = 3
 
   !> sed_params of mossco_sed.h (same member order and kinds)
   type, bind(C), public :: sed_params_t
@@ -105,6 +108,23 @@ module sed_gpu
       import :: c_int, c_ptr
       type(c_ptr), value :: h, bdys, fluxes
     end function
+    !> device-resident state for many coupling steps (a coupled run keeps
+    !! conc on the device between sed_step calls)
+    integer(c_int) function sed_set_state(h, conc) bind(C, name='sed_set_state')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, conc
+    end function
+    integer(c_int) function sed_get_state(h, conc) bind(C, name='sed_get_state')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, conc
+    end function
+    integer(c_int) function sed_step(h, dt, method, nsteps, st) bind(C, name='sed_step')
+      import :: c_int, c_ptr, c_double, sed_stats_t
+      type(c_ptr), value :: h
+      real(c_double), value :: dt
+      integer(c_int), value :: method, nsteps
+      type(sed_stats_t), intent(out) :: st
+    end function
     integer(c_int) function sed_spinup(h, mode, column, bdys1, fluxes1, dt, method, nsteps, st) &
         bind(C, name='sed_spinup')
       import :: c_int, c_ptr, c_double, c_long_long, sed_stats_t
@@ -158,7 +178,8 @@ module sed_gpu
   public :: sed_default_params, sed_gpu_init, sed_gpu_ode_solver, &
             sed_gpu_get_rhs, sed_gpu_finalize, sed_get_tuning, sed_set_tuning, &
             sed_autotune, sed_set_boundary, sed_get_boundary, sed_spinup, &
-            sed_get_min_dt, sed_set_column_bgc
+            sed_get_min_dt, sed_set_column_bgc, sed_set_state, sed_get_state, &
+            sed_step
 
 contains
 

@@ -4,7 +4,7 @@
  * TEST INFRASTRUCTURE ONLY.  Imported by tests/ (through pel_oracle.py) to
  * check the device coupling; the product never links it.
  *
- * Restates src/mediators/pelagic_soil_connector.F90 Run (:176-2060) for 3-D
+ * Restates src/mediators/pelagic_soil_connector.F90 Run (:176-2122) for 3-D
  * pelagic fields and 2-D soil fields, statement by statement and in the
  * Run's order: each whole-array Fortran assignment is one loop over the
  * columns, and a field the Run writes twice is written twice here.  The ESMF
@@ -58,7 +58,7 @@ int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
 #define ROW(a, r) ((a) + (size_t)(r) * ncol)
 #define B(fld) bot(conc, (fld), ncol, knum, i)
 
-  /* oxygen and its deficit, :811-866 (both found / deficit only / oxygen
+  /* oxygen and its deficit, :801-866 (both found / deficit only / oxygen
    * only; the oxygen-only branch of the reference reads the deficit's
    * pointers, which are not associated then: here oxygen alone is copied) */
   if (f->oxygen >= 0 && f->odu >= 0) {
@@ -80,12 +80,12 @@ int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
     present[OX] = 1;
   }
 
-  /* C:N of the detritus, :1038-1072 */
+  /* C:N of the detritus, :1018-1072 */
   for (i = 0; i < ncol; i++) CN[i] = 106.0 / 16.0;
   if (f->detN >= 0 && f->detC >= 0)
     for (i = 0; i < ncol; i++) CN[i] = B(f->detC) / (one_e5 + B(f->detN));
 
-  /* labile / semilabile factors, :1077-1098 */
+  /* labile / semilabile factors, :1074-1121 */
   for (i = 0; i < ncol; i++) fl[i] = (1.0 - p->NC_sdet * CN[i]) / (p->NC_ldet - p->NC_sdet);
   for (i = 0; i < ncol; i++) rl[i] = fl[i] * p->NC_ldet;
   for (i = 0; i < ncol; i++)
@@ -131,7 +131,7 @@ int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
       present[row[b]] = 1;
     }
   }
-  /* phosphorus, :1492-1590 */
+  /* phosphorus, :1492-1646 */
   if (f->detN >= 0) {
     for (i = 0; i < ncol; i++) ROW(surface, LP)[i] = 1.0 / 16.0 * p->convertN * B(f->detN);
     present[LP] = 1;
@@ -144,7 +144,7 @@ int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
     for (i = 0; i < ncol; i++)
       ROW(velocity, LP)[i] = p->sinking_factor * fe[i] * B(f->detN);
 
-  /* ammonium, :1743-1838 */
+  /* ammonium, :1685-1860 */
   {
     const int hN = f->nitrate >= 0, hA = f->ammonium >= 0, hD = f->din >= 0;
     if (!hN && !hA && !hD) {
@@ -159,7 +159,7 @@ int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
       else v = p->convertN * B(f->nitrate);
       ROW(surface, AM)[i] = v;
     }
-    /* nitrate, :1840-1935 */
+    /* nitrate, :1863-1985 */
     for (i = 0; i < ncol; i++) {
       double v;
       if (hN) v = p->convertN * B(f->nitrate);
@@ -168,7 +168,7 @@ int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
       else v = p->convertN * B(f->ammonium);
       ROW(surface, NI)[i] = v;
     }
-    /* phosphate from DIN (a DIP field is overwritten, not read), :1938-2003 */
+    /* phosphate from DIN (a DIP field is overwritten, not read), :1988-2110 */
     for (i = 0; i < ncol; i++) {
       if (hD) din[i] = B(f->din);
       else if (hA && hN) din[i] = B(f->nitrate) + B(f->ammonium);

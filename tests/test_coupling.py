@@ -2,7 +2,7 @@
 
 The reference maps the pelagic state's bottom layer to the soil's surface
 fields in pelagic_soil_connector's Run
-(src/mediators/pelagic_soil_connector.F90:176-2060) and the sediment
+(src/mediators/pelagic_soil_connector.F90:176-2122) and the sediment
 component turns them into bdys / fluxes (get_boundary_conditions,
 src/components/fabm_sediment_component.F90:1865-2030).  CPU tests check the
 oracle (oracle/cpl_oracle.c) against a vectorised restatement written here
