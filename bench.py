@@ -848,6 +848,182 @@ def run_reference_pelagic(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+CPL_METRIC = ("pelagic->soil coupling: horizontal columns mapped into the soil boundary per "
+              "second on 1 GB300 (pelagic_soil_connector Run + get_boundary_conditions)")
+CPL_PEL, CPL_SED = "pelagic_1024x1024", "soil_1024x1024"
+
+
+def cpl_bytes(ncol: int, as_named: bool, depth: bool, rsize: int = 4) -> int:
+    """Bytes one k_pelagic_soil launch must move for gotm_npzd's fields: the
+    bottom-layer detritus and nutrient values (2 r), the water depth (8 when
+    given), the eleven surface rows and the velocity rows the Run writes (8
+    each: phosphorus only as the Run is written, the five detritus rows as
+    named) per column."""
+    return int(ncol * (2 * rsize + (8 if depth else 0) + 8 * (11 + (5 if as_named else 1))))
+
+
+def cpl_cpu(conc, depth, target_s: float = 10.0):
+    """The connector oracle (one thread) on the whole grid, repeated for
+    about target_s seconds."""
+    import pel_oracle
+    fields = {"detN": 3, "din": 0}
+    t0 = time.perf_counter()
+    pel_oracle.cpl_run(conc, fields, None, False, depth)
+    one = max(time.perf_counter() - t0, 1e-6)
+    reps = max(1, int(target_s / one))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        rc, *_ = pel_oracle.cpl_run(conc, fields, None, False, depth)
+    secs = time.perf_counter() - t0
+    ncol = conc.shape[2]
+    return {"value": ncol * reps / secs, "unit": "columns/s", "cores": 1, "kind": "port",
+            "sample": f"the whole grid ({ncol} columns), {reps} calls, {secs:.1f} s",
+            "seconds": secs, "calls": reps, "status": rc}
+
+
+def cpl_bottom(pcs):
+    """The pelagic state the oracle needs: the bottom layer only (k = 0)."""
+    return np.ascontiguousarray(pcs.conc[:, :1, :])
+
+
+def run_coupling(args) -> None:
+    """The pelagic -> soil coupling on a 1024 x 1024 grid: the connector's
+    mapping from the FP32 pelagic state of pelagic_1024x1024 into the
+    boundary of the soil_1024x1024 sediment handle (gotm_npzd fields, the
+    Run as written, water depth from the pelagic layer heights), state
+    resident in HBM; bottom-water temperature and water depth come from
+    host arrays each call, as the API takes them."""
+    import torch
+    from sedgpu import capi, coupling, pelagic, synth
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    pcs = pelagic.make_pelagic_workload(CPL_PEL, seed=args.seed + 7919 * rank)
+    cs = synth.make_workload(CPL_SED, seed=args.seed + 7919 * rank)
+    assert pcs.ncol == cs.ncol
+    pp = pcs.params(capi.SED_FP32)
+    pp.device = local
+    pel = pelagic.PelagicSolver(pcs, params=pp)
+    pel.set_state(pcs.conc)
+    sed = capi.Solver(cs, params=capi.params_from(cs, capi.SED_FP32, device=local))
+    sed.set_state(cs.conc)
+    T = np.array(cs.bdys[0], dtype=np.float64, copy=True)
+    depth = np.ascontiguousarray(pcs.layer_height.sum(axis=0))
+    for a in (T, depth):
+        capi.host_register(a)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    calls = args.steps or 200
+    st = coupling.CplStats()
+    for _ in range(args.warmup):
+        coupling.pelagic_soil(pel, sed, T, depth, stats=st, read_back=False)
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    kern_ms = dev_ms = 0.0
+    launches = 0
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        flush.zero_()            # L2 flush between timed calls
+        torch.cuda.synchronize()
+        coupling.pelagic_soil(pel, sed, T, depth, stats=st, read_back=False)
+        kern_ms += st.kernel_ms
+        dev_ms += st.device_ms
+        launches += st.gpu_launches
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([dev_ms, kern_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms, kern_ms = (float(v) for v in t.tolist())
+        dist.barrier()
+    clk = clocks.stop()
+    e2e = None
+    if not args.no_e2e:
+        t1 = time.perf_counter()
+        for _ in range(calls):
+            _, _, present = coupling.pelagic_soil(pel, sed, T, depth, read_back=False)
+        e2e_s = time.perf_counter() - t1
+        e2e = {"value": world * cs.ncol * calls / e2e_s, "unit": "columns/s",
+               "h2d_bytes_per_step": int(T.nbytes + depth.nbytes),
+               "d2h_bytes_per_step": int(present.nbytes), "steps": calls,
+               "call": "cpl_pelagic_soil (host temperature and water depth in, the "
+                       "present flags out; the boundary stays on the device)"}
+    for a in (T, depth):
+        capi.host_unregister(a)
+    pel.close()
+    sed.close()
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    nbytes = cpl_bytes(cs.ncol, False, True)
+    peak, peak_kind = measured_peaks()
+    achieved = nbytes / (kern_ms / calls / 1e3) / 1e9
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpl_cpu(cpl_bottom(pcs), depth, args.cpl_cpu_seconds)
+        for k in ("seconds", "status", "calls"):
+            cpu.pop(k)
+    line = {
+        "metric": CPL_METRIC, "value": world * cs.ncol * calls / (dev_ms / 1e3),
+        "unit": "columns/s", "n_gpus": world, "steps": calls, "warmup": args.warmup,
+        "ms_per_step": dev_ms / calls, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 (from the f32 pelagic state)",
+        "data": "synthetic (seeded)",
+        "config": {"workload": f"{CPL_PEL} -> {CPL_SED}", "columns": cs.ncol,
+                   "fields": "gotm_npzd (detN = detritus, DIN = nutrients)",
+                   "mode": "CPL_AS_RUN", "water_depth": "given", "tke": "absent",
+                   "l2": "L2 flushed between timed calls"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                     "bytes_per_launch": nbytes, "kernel": "k_pelagic_soil<float>",
+                     "kernel_ms": kern_ms / calls},
+        "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches,
+        "clocks": clk, "wall_s": wall,
+        "note": ("ms_per_step and value: the call's device span (temperature and depth "
+                 "copies, the mapping, the boundary assembly and the forcing rows)"),
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_reference_coupling(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import pel_oracle
+    pel_oracle.build()
+    from sedgpu import pelagic
+    pcs = pelagic.make_pelagic_workload(CPL_PEL, seed=args.seed)
+    depth = np.ascontiguousarray(pcs.layer_height.sum(axis=0))
+    cpu = cpl_cpu(cpl_bottom(pcs), depth, args.cpl_cpu_seconds)
+    line = {
+        "metric": CPL_METRIC, "value": cpu["value"], "unit": "columns/s",
+        "n_gpus": args.gpus, "steps": cpu["calls"], "warmup": args.warmup,
+        "ms_per_step": cpu["seconds"] * 1e3 / cpu["calls"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+        "data": "synthetic (seeded)", "impl": "reference",
+        "config": {"workload": f"{CPL_PEL} -> {CPL_SED}", "columns": pcs.ncol,
+                   "fields": "gotm_npzd (detN = detritus, DIN = nutrients)",
+                   "mode": "CPL_AS_RUN", "water_depth": "given", "tke": "absent"},
+        "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": cpu["value"], "unit": "columns/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": ("the connector's Run as the C restatement on one host core (the "
+                 "mapping only); the Fortran reference and ESMF cannot be built here"),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -876,8 +1052,11 @@ def main():
     ap.add_argument("--spinup-cpu-steps", type=int, default=2000)
     ap.add_argument("--ensemble", type=int, default=0,
                     help="with --spinup-years: spin up this many parameter sets at once")
-    ap.add_argument("--path", default="sediment", choices=["sediment", "pelagic"],
-                    help="pelagic: the fabm_pelagic driver path instead")
+    ap.add_argument("--path", default="sediment", choices=["sediment", "pelagic", "coupling"],
+                    help="pelagic: the fabm_pelagic driver path instead; coupling: the "
+                         "pelagic -> soil connector")
+    ap.add_argument("--cpl-cpu-seconds", type=float, default=8.0,
+                    help="coupling CPU baseline: about this many seconds of oracle calls")
     ap.add_argument("--pel-cpu-columns", type=int, default=0,
                     help="pelagic CPU baseline: at most this many columns (0: the grid)")
     args = ap.parse_args()
@@ -888,6 +1067,11 @@ def main():
             run_reference_pelagic(args)
         else:
             run_pelagic(args)
+    elif args.path == "coupling":
+        if args.impl == "reference":
+            run_reference_coupling(args)
+        else:
+            run_coupling(args)
     elif args.impl == "reference":
         run_reference(args)
     elif args.spinup_years > 0 and args.ensemble > 0:

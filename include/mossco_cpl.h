@@ -67,6 +67,15 @@ typedef struct cpl_fields {
   int odu;      /* dissolved_reduced_substances_odu_in_water (:697-698) */
 } cpl_fields;
 
+/* what one cpl_pelagic_soil call did on the device */
+typedef struct cpl_stats {
+  int gpu_launches;      /* kernels this library launched for the call */
+  long long columns;     /* columns mapped */
+  double kernel_ms;      /* k_pelagic_soil alone (CUDA events) */
+  double device_ms;      /* the call's device span: copies, mapping and the
+                            sediment's boundary assembly (CUDA events) */
+} cpl_stats;
+
 int cpl_default_params(cpl_params *p);
 /* gotm_npzd's fields: detN = detritus (3), din = nutrients (0), others -1 */
 int cpl_npzd_fields(cpl_fields *f);
@@ -84,6 +93,7 @@ int cpl_npzd_fields(cpl_fields *f);
  *                call (host copies for inspection), or NULL
  *   present_out  [SED_NTR] 1 where the connector wrote the tracer's
  *                concentration field, or NULL
+ *   stats        or NULL
  * The pelagic handle needs its state (pel_set_state or a step), the
  * sediment handle its grid, and with bcup_dissolved = 1 its state.  No
  * nitrate, ammonium or DIN field: SED_E_ARG (the Run returns
@@ -92,7 +102,7 @@ int cpl_pelagic_soil(pel_handle *pel, sed_handle *sed, const cpl_params *p,
                      const cpl_fields *f, const double *temperature,
                      const double *water_depth, const double *tke,
                      const double *velocity_in, double *surface_out,
-                     double *velocity_out, int *present_out);
+                     double *velocity_out, int *present_out, cpl_stats *stats);
 
 #ifdef __cplusplus
 }

@@ -25,14 +25,23 @@ constexpr int NPART = 6;   // particulate tracers lead the sediment's order
 constexpr int kLabC = 0, kSemC = 1, kLabN = 2, kSemN = 3, kLabP = 4, kOxy = 6, kNit = 7,
               kAmm = 8, kOdu = 9, kPho = 10;
 
+// Per-launch constants are formed on the host in IEEE double, with the
+// same operations and rounding the Fortran expressions give them; the
+// kernel keeps only the per-column arithmetic (GB300's FP64 rate is a small
+// fraction of its FP32 rate, and the FP64 divisions bound this kernel).
 struct Args {
   const void* state;
   int ncol, K;
   int detN, detC, detP, din, nit, amm, oxy, odu;
-  double sf, sfmin, ncl, ncs, cN, cP, hsd, htke, crit;
+  double sf, ncl, ncs, cN, cP, htke, crit;
+  double hsd2;        // half_sedimentation_depth**2
+  double sfmin_sf;    // sinking_factor_min/sinking_factor
+  double c16N;        // 1.0d0/16.0d0 * convertN
+  double c05N;        // convertN*0.5d0
   int as_named;
-  const double* depth;  // null: no water_depth_at_soil_surface
-  const double* tke;    // null: no turbulent_kinetic_energy_at_soil_surface
+  int crit_on;        // detC present and 1e-3 < critical_detritus < 9e9
+  const double* depth;  // null: no water depth, or half_sedimentation_depth <= 1e-3
+  const double* tke;    // null: no turbulence field, or half_sedimentation_tke >= 9e9
   double* surface;      // [NTR][ncol]
   double* velocity;     // [NTR][ncol]
 };
@@ -53,13 +62,13 @@ __global__ void k_pelagic_soil(Args a) {
     // ---- detritus (:1018-1236 factors, :1243-1646 fields)
     if (a.detN >= 0 || a.detP >= 0) {
       double fenv = 1.0;
-      if (a.depth && a.hsd > (double)1e-3f) {
-        const double d = a.depth[col];
-        fenv = fenv * (d * d) / (d * d + a.hsd * a.hsd);
+      if (a.depth) {   // 1.0 * d**2 is d**2 exactly
+        const double d2 = a.depth[col] * a.depth[col];
+        fenv = d2 / (d2 + a.hsd2);
       }
-      if (a.tke && a.htke < (double)9e9f) fenv = fenv * a.htke / (a.tke[col] + a.htke);
-      fenv = fenv + a.sfmin / a.sf;
-      if (a.detC >= 0 && a.crit > (double)1e-3f && a.crit < (double)9e9f) {
+      if (a.tke) fenv = fenv * a.htke / (a.tke[col] + a.htke);
+      fenv = fenv + a.sfmin_sf;
+      if (a.crit_on) {
         const double t = B(a.detC) / a.crit;
         const double t2 = t * t;
         fenv = fenv * 1.0 / (1.0 + t2 * t2);
@@ -84,7 +93,7 @@ __global__ void k_pelagic_soil(Args a) {
         } else {
           for (int n = kLabC; n <= kSemN; n++) S[n] = w * N;
         }
-        S[kLabP] = 1.0 / 16.0 * a.cN * N;
+        S[kLabP] = a.c16N * N;
         V[(size_t)kLabP * a.ncol + col] = w * N;
       }
       if (a.detP >= 0) S[kLabP] = B(a.detP);
@@ -107,19 +116,44 @@ __global__ void k_pelagic_soil(Args a) {
     const double D = hD ? B(a.din) : 0.0;
     S[kAmm] = hA ? a.cN * A
             : (hD && hN) ? a.cN * (D - Nt)
-            : hD ? a.cN * 0.5 * D
+            : hD ? a.c05N * D
             : a.cN * Nt;
     S[kNit] = hN ? a.cN * Nt
             : (hA && hD) ? a.cN * (D - A)
-            : hD ? a.cN * 0.5 * D
+            : hD ? a.c05N * D
             : a.cN * A;
     const double din = hD ? D : (hA && hN) ? Nt + A : hA ? 2 * A : 2 * Nt;
-    S[kPho] = a.cP * (1.0 / 16.0 * a.cN * din);
+    S[kPho] = a.cP * (a.c16N * din);
     for (int n = 0; n < NTR; n++) a.surface[(size_t)n * a.ncol + col] = S[n];
   }
 }
 
 bool bad_index(int i) { return i < -1 || i >= PEL_NTR; }
+
+// CUDA events at marks 0..3 on one stream (none unless init was called)
+struct Timing {
+  cudaEvent_t ev[4] = {};
+  cudaStream_t st = nullptr;
+  bool on = false;
+  void init(cudaError_t* err, cudaStream_t s) {
+    st = s;
+    on = true;
+    for (auto& x : ev)
+      if (cudaEventCreate(&x) != cudaSuccess) { on = false; *err = cudaErrorMemoryAllocation; }
+  }
+  void mark(int i) {
+    if (on) cudaEventRecord(ev[i], st);
+  }
+  double ms(int a, int b) {
+    float t = 0.0f;
+    if (!on || cudaEventElapsedTime(&t, ev[a], ev[b]) != cudaSuccess) return 0.0;
+    return t;
+  }
+  ~Timing() {
+    for (auto& x : ev)
+      if (x) cudaEventDestroy(x);
+  }
+};
 
 }  // namespace
 
@@ -160,7 +194,8 @@ int cpl_pelagic_soil(pel_handle* pel, sed_handle* sed, const cpl_params* p,
                      const cpl_fields* f, const double* temperature,
                      const double* water_depth, const double* tke,
                      const double* velocity_in, double* surface_out,
-                     double* velocity_out, int* present_out) {
+                     double* velocity_out, int* present_out, cpl_stats* stats) {
+  if (stats) memset(stats, 0, sizeof *stats);
   if (!sed) return SED_E_ARG;
   if (!pel) return cpl::sed_fail(sed, SED_E_ARG, "pelagic handle is NULL");
   if (!p || !f || !temperature)
@@ -195,6 +230,9 @@ int cpl_pelagic_soil(pel_handle* pel, sed_handle* sed, const cpl_params* p,
     ok(cudaStreamWaitEvent(s.stream, ev, 0));
   }
   if (ev) cudaEventDestroy(ev);
+  Timing tm;
+  if (stats) tm.init(&e, s.stream);
+  tm.mark(0);
   ok(cudaMemcpyAsync(s.temperature, temperature, nc * sizeof(double), cudaMemcpyHostToDevice,
                      s.stream));
   if (velocity_in)
@@ -219,24 +257,34 @@ int cpl_pelagic_soil(pel_handle* pel, sed_handle* sed, const cpl_params* p,
   a.K = v.K;
   a.detN = f->detN; a.detC = f->detC; a.detP = f->detP; a.din = f->din;
   a.nit = f->nitrate; a.amm = f->ammonium; a.oxy = f->oxygen; a.odu = f->odu;
-  a.sf = p->sinking_factor; a.sfmin = p->sinking_factor_min;
+  a.sf = p->sinking_factor;
   a.ncl = p->NC_ldet; a.ncs = p->NC_sdet; a.cN = p->convertN; a.cP = p->convertP;
-  a.hsd = p->half_sedimentation_depth; a.htke = p->half_sedimentation_tke;
+  a.htke = p->half_sedimentation_tke;
   a.crit = p->critical_detritus;
+  a.hsd2 = p->half_sedimentation_depth * p->half_sedimentation_depth;
+  a.sfmin_sf = p->sinking_factor_min / p->sinking_factor;
+  a.c16N = 1.0 / 16.0 * p->convertN;
+  a.c05N = p->convertN * 0.5;
   a.as_named = p->mode == CPL_AS_NAMED;
-  a.depth = water_depth ? d_depth : nullptr;
-  a.tke = tke ? d_tke : nullptr;
+  // the Run's guards on the namelist values (:1150, :1181, :1215), with
+  // its default-real literals
+  a.crit_on = f->detC >= 0 && p->critical_detritus > (double)1e-3f &&
+              p->critical_detritus < (double)9e9f;
+  a.depth = water_depth && p->half_sedimentation_depth > (double)1e-3f ? d_depth : nullptr;
+  a.tke = tke && p->half_sedimentation_tke < (double)9e9f ? d_tke : nullptr;
   a.surface = s.surface;
   a.velocity = s.velocity;
   const int threads = 256;
   long long blocks = ((long long)nc + threads - 1) / threads;
   const long long cap = (long long)(s.sms > 0 ? s.sms : 1) * 8;
   if (blocks > cap) blocks = cap;
+  tm.mark(1);
   if (v.fp64)
     k_pelagic_soil<double><<<(int)blocks, threads, 0, s.stream>>>(a);
   else
     k_pelagic_soil<float><<<(int)blocks, threads, 0, s.stream>>>(a);
   e = cudaGetLastError();
+  tm.mark(2);
   if (e != cudaSuccess) {
     std::string m = std::string("coupling kernel launch: ") + cudaGetErrorString(e);
     return cpl::sed_fail(sed, SED_E_CUDA, m.c_str());
@@ -248,7 +296,9 @@ int cpl_pelagic_soil(pel_handle* pel, sed_handle* sed, const cpl_params* p,
   if (f->detP >= 0) mask |= 1u << kLabP;
   if (f->oxygen >= 0 || f->odu >= 0) mask |= 1u << kOxy;
   if (f->odu >= 0) mask |= 1u << kOdu;
+  const int before = cpl::sed_launches(sed);
   if (int rc = cpl::sed_assemble_staged(sed, mask)) return rc;
+  const int assembly = cpl::sed_launches(sed) - before;
   if (surface_out)
     ok(cudaMemcpyAsync(surface_out, s.surface, (size_t)NTR * nc * sizeof(double),
                        cudaMemcpyDeviceToHost, s.stream));
@@ -258,10 +308,17 @@ int cpl_pelagic_soil(pel_handle* pel, sed_handle* sed, const cpl_params* p,
     ok(cudaMemcpyAsync(velocity_out, s.velocity, (size_t)NTR * nc * sizeof(double),
                        cudaMemcpyDeviceToHost, s.stream));
   }
+  tm.mark(3);
   ok(cudaStreamSynchronize(s.stream));
   if (e != cudaSuccess) {
     std::string m = std::string("coupling read-back: ") + cudaGetErrorString(e);
     return cpl::sed_fail(sed, SED_E_CUDA, m.c_str());
+  }
+  if (stats) {
+    stats->gpu_launches = 1 + assembly;
+    stats->columns = (long long)nc;
+    stats->kernel_ms = tm.ms(1, 2);
+    stats->device_ms = tm.ms(0, 3);
   }
   if (present_out)
     for (int n = 0; n < NTR; n++) present_out[n] = (mask >> n) & 1u;

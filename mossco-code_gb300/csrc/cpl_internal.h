@@ -40,5 +40,7 @@ int sed_assemble_staged(sed_handle* h, unsigned present_mask);
 // records the message on the sediment handle and returns code
 int sed_fail(sed_handle* h, int code, const char* msg);
 void sed_count_launch(sed_handle* h);
+// kernels launched on the handle so far
+int sed_launches(const sed_handle* h);
 
 }  // namespace cpl

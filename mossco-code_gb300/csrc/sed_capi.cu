@@ -1724,6 +1724,8 @@ int cpl::sed_fail(sed_handle* h, int code, const char* msg) {
 
 void cpl::sed_count_launch(sed_handle* h) { h->launches++; }
 
+int cpl::sed_launches(const sed_handle* h) { return (int)h->launches; }
+
 int cpl::sed_assemble_staged(sed_handle* h, unsigned mask) {
   const unsigned part = (1u << NPART) - 1u;
   if (h->prm.bcup_dissolved == 1 && (mask & ~part) && !h->have_state)

@@ -32,6 +32,13 @@ module cpl_gpu
     integer(c_int) :: detN, detC, detP, din, nitrate, ammonium, oxygen, odu
   end type
 
+  !> cpl_stats of mossco_cpl.h
+  type, bind(C), public :: cpl_stats_t
+    integer(c_int)       :: gpu_launches
+    integer(c_long_long) :: columns
+    real(c_double)       :: kernel_ms, device_ms
+  end type
+
   interface
     integer(c_int) function cpl_default_params(p) bind(C, name='cpl_default_params')
       import :: c_int, cpl_params_t
@@ -42,14 +49,14 @@ module cpl_gpu
       type(cpl_fields_t), intent(out) :: f
     end function
     integer(c_int) function cpl_pelagic_soil(pel, sed, p, f, temperature, water_depth, &
-        tke, velocity_in, surface_out, velocity_out, present_out) &
+        tke, velocity_in, surface_out, velocity_out, present_out, stats) &
         bind(C, name='cpl_pelagic_soil')
       import :: c_int, c_ptr, cpl_params_t, cpl_fields_t
       type(c_ptr), value :: pel, sed
       type(cpl_params_t), intent(in) :: p
       type(cpl_fields_t), intent(in) :: f
       type(c_ptr), value :: temperature, water_depth, tke, velocity_in, &
-                            surface_out, velocity_out, present_out
+                            surface_out, velocity_out, present_out, stats
     end function
   end interface
 
@@ -75,7 +82,7 @@ contains
     if (present(water_depth)) d = c_loc(water_depth)
     if (present(tke)) t = c_loc(tke)
     rc = cpl_pelagic_soil(pgpu%h, sgpu%h, p, f, c_loc(temperature), d, t, c_null_ptr, &
-                          c_null_ptr, c_null_ptr, c_null_ptr)
+                          c_null_ptr, c_null_ptr, c_null_ptr, c_null_ptr)
   end subroutine
 
 end module cpl_gpu

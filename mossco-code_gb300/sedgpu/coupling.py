@@ -39,6 +39,14 @@ class CplFields(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in FIELD_NAMES]
 
 
+class CplStats(ctypes.Structure):
+    _fields_ = [("gpu_launches", ctypes.c_int), ("columns", ctypes.c_longlong),
+                ("kernel_ms", ctypes.c_double), ("device_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 _H = ctypes.c_void_p
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -48,7 +56,7 @@ CPL_SIGNATURES = {
     "cpl_npzd_fields": (ctypes.c_int, [ctypes.POINTER(CplFields)]),
     "cpl_pelagic_soil": (ctypes.c_int, [_H, _H, ctypes.POINTER(CplParams),
                                         ctypes.POINTER(CplFields), _dp, _dp, _dp, _dp, _dp,
-                                        _dp, _ip]),
+                                        _dp, _ip, ctypes.POINTER(CplStats)]),
 }
 
 _registered = False
@@ -101,13 +109,15 @@ def _p(a, t=_dp):
 
 def pelagic_soil(pel: PelagicSolver, sed: Solver, temperature, water_depth=None, tke=None,
                  velocity_in=None, params: Optional[CplParams] = None,
-                 fields: Optional[CplFields] = None
-                 ) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
+                 fields: Optional[CplFields] = None, stats: Optional[CplStats] = None,
+                 read_back: bool = True
+                 ) -> Tuple[Optional[np.ndarray], Optional[np.ndarray], np.ndarray]:
     """One connector Run from ``pel``'s device state into ``sed``'s boundary.
 
-    Returns the soil fields it wrote (host copies): surface [NTR][ncol],
-    velocity [NTR][ncol] and present [NTR] (1 where a concentration field
-    was written)."""
+    Returns the soil fields it wrote (host copies, None without
+    ``read_back``): surface [NTR][ncol], velocity [NTR][ncol], and present
+    [NTR] (1 where a concentration field was written).  ``stats``, when
+    given, receives the call's launches and device times."""
     L = load()
     ncol = sed.cs.ncol
     p = params or default_params()
@@ -119,11 +129,12 @@ def pelagic_soil(pel: PelagicSolver, sed: Solver, temperature, water_depth=None,
             raise ValueError(f"{name} must have {ncol} values")
     if v is not None and v.size < 6 * ncol:
         raise ValueError("velocity_in must hold the particulate rows [6][ncol]")
-    surface = np.zeros((NTR, ncol))
-    velocity = np.zeros((NTR, ncol))
+    surface = np.zeros((NTR, ncol)) if read_back else None
+    velocity = np.zeros((NTR, ncol)) if read_back else None
     present = np.zeros(NTR, dtype=np.int32)
     rc = L.cpl_pelagic_soil(pel.h, sed.h, ctypes.byref(p), ctypes.byref(f), _p(t), _p(d), _p(k),
-                            _p(v), _p(surface), _p(velocity), _p(present, _ip))
+                            _p(v), _p(surface), _p(velocity), _p(present, _ip),
+                            None if stats is None else ctypes.byref(stats))
     if rc != SED_OK:
         raise SedError(rc, "cpl_pelagic_soil: " + L.sed_last_error(sed.h).decode())
     return surface, velocity, present

@@ -135,6 +135,10 @@ WORKLOADS = {
     "surrogate_2048x2048": dict(inum=2048, jnum=2048, kmin=30, kmax=30,
                                 total=0.20, land=0.3, poc="loguniform",
                                 days=60),
+    # the soil under pelagic_1024x1024 for the coupling measurement: the
+    # 15 layers of examples/standalone/omexdia_p/run_sed.nml:34
+    "soil_1024x1024": dict(inum=1024, jnum=1024, kmin=15, kmax=15, total=0.18,
+                           land=0.3, poc="loguniform", days=1),
 }
 
 

@@ -1,5 +1,5 @@
 """The JSON line of bench.py's reference arm (the oracle on the host cores,
-no GPU needed) for both paths carries the keys of the benchmark contract."""
+no GPU needed) for every path carries the keys of the benchmark contract."""
 import json
 import os
 import subprocess
@@ -39,3 +39,10 @@ def test_reference_arm_pelagic():
     line = run("--path", "pelagic", "--pel-cpu-columns", "256")
     check(line)
     assert line["unit"] == "column-runs/s" and line["config"]["model"] == "gotm_npzd"
+
+
+def test_reference_arm_coupling():
+    line = run("--path", "coupling", "--cpl-cpu-seconds", "0.5")
+    check(line)
+    assert line["unit"] == "columns/s" and line["config"]["mode"] == "CPL_AS_RUN"
+    assert line["config"]["columns"] == 1024 * 1024

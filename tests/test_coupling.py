@@ -133,8 +133,11 @@ def test_defaults_are_the_connectors_literals(po):
 def test_null_handles_are_refused():
     L = coupling.load()
     p, f = coupling.default_params(), coupling.npzd_fields()
+    st = coupling.CplStats()
+    st.gpu_launches = 7
     assert L.cpl_pelagic_soil(None, None, p, f, None, None, None, None, None, None,
-                              None) == capi.SED_E_ARG
+                              None, st) == capi.SED_E_ARG
+    assert st.gpu_launches == 0   # cleared on entry
 
 
 @pytest.mark.parametrize("fields", FIELD_SETS)
@@ -252,7 +255,10 @@ def test_coupling_reads_the_stepped_device_state(po):
     T = np.full(256, 10.0)
     for _ in range(3):
         pel.step(2)
-        S, V, present = coupling.pelagic_soil(pel, sed, T)
+        st = coupling.CplStats()
+        S, V, present = coupling.pelagic_soil(pel, sed, T, stats=st)
+        assert st.gpu_launches == 3 and st.columns == 256   # mapping, assembly, forcing rows
+        assert 0.0 < st.kernel_ms <= st.device_ms
         rc, S0, V0, _ = po.cpl_run(pel.get_state(), NPZD, po.cpl_defaults(), False)
         np.testing.assert_array_equal(S, S0)
         np.testing.assert_array_equal(V[:6], V0[:6])
