@@ -151,3 +151,73 @@ def test_partition_edge_cases():
         assert parts[0][0] == 0 and parts[-1][1] == kact.size
         assert all(a[1] == b[0] and a[0] <= a[1] for a, b in zip(parts, parts[1:]))
         assert sum(b - a for a, b in parts) == kact.size
+
+
+def _cpl_rank_main(rank, world, port, outdir):
+    for p in (os.path.join(ROOT, "mossco-code_gb300"), os.path.join(ROOT, "oracle")):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    import torch
+    import torch.distributed as dist
+    import pel_oracle
+    from sedgpu import pelagic as pl
+    from sedgpu import shard as sh
+    from sedgpu import synth as sy
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        pcs = pl.make_pelagic_workload("pelagic_cpu_16x16")
+        cs = sy.make_columns(inum=16, jnum=16, kmin=5, kmax=15, total=0.18, land=0.2,
+                             poc="loguniform", days=1, seed=3, name="soil16")
+        pmine, smine, (c0, c1) = sh.shard_coupled(pcs, cs, rank, world)
+        assert pmine.ncol == smine.ncol == c1 - c0
+        rc, S, V, present = pel_oracle.cpl_run(pmine.conc, {"detN": 3, "din": 0})
+        assert rc == 0
+        # the only cross-rank traffic: one scalar, the columns mapped
+        n = torch.tensor([float(pmine.ncol)])
+        dist.all_reduce(n)
+        np.savez(os.path.join(outdir, f"cpl{rank}.npz"), S=S, V=V, c0=c0, c1=c1,
+                 total=float(n.item()))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_coupled_two_gloo_ranks_equal_one_process(tmp_path):
+    """A coupled pelagic / soil grid sharded by shard_coupled: each rank
+    maps its own columns (the same range of both grids) and the gathered
+    soil fields equal one process's connector Run."""
+    import pel_oracle
+    import torch.multiprocessing as mp
+    from sedgpu import pelagic
+    pel_oracle.build()
+    port = _free_port()
+    mp.spawn(_cpl_rank_main, args=(2, port, str(tmp_path)), nprocs=2, join=True)
+    pcs = pelagic.make_pelagic_workload("pelagic_cpu_16x16")
+    rc, S, V, _ = pel_oracle.cpl_run(pcs.conc, {"detN": 3, "din": 0})
+    assert rc == 0
+    gS, gV = np.full_like(S, np.nan), np.full_like(V, np.nan)
+    for r in range(2):
+        d = np.load(tmp_path / f"cpl{r}.npz")
+        a, b = int(d["c0"]), int(d["c1"])
+        gS[:, a:b], gV[:, a:b] = d["S"], d["V"]
+        assert float(d["total"]) == pcs.ncol
+    np.testing.assert_array_equal(gS, S)
+    np.testing.assert_array_equal(gV, V)
+
+
+def test_shard_coupled_balances_both_grids():
+    from sedgpu import pelagic
+    pcs = pelagic.make_pelagic_workload("pelagic_cpu_16x16")
+    cs = synth.make_columns(inum=16, jnum=16, kmin=5, kmax=15, total=0.18, land=0.2,
+                            poc="loguniform", days=1, seed=3, name="soil16")
+    work = cs.kact + shard.PEL_CELL_WEIGHT * pcs.water().sum(axis=0)
+    for world in (1, 2, 3, 7):
+        ranges = [shard.shard_coupled(pcs, cs, r, world)[2] for r in range(world)]
+        assert ranges[0][0] == 0 and ranges[-1][1] == cs.ncol
+        assert all(a[1] == b[0] for a, b in zip(ranges, ranges[1:]))
+        w = [work[a:b].sum() for a, b in ranges]
+        assert max(w) - min(w) <= 2 * work.max()
+    small = pcs.subset(np.arange(10))
+    with pytest.raises(ValueError):
+        shard.shard_coupled(small, cs, 0, 2)
