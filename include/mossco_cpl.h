@@ -65,6 +65,9 @@ typedef struct cpl_fields {
   int ammonium; /* ammonium_in_water, dissolved_ammonium_nh3_in_water */
   int oxygen;   /* dissolved_oxygen_in_water, ... (:652-656) */
   int odu;      /* dissolved_reduced_substances_odu_in_water (:697-698) */
+  int dip;      /* DIP_in_water, phosphate_in_water, ...: written by the
+                   reverse connector only (the forward Run overwrites it and
+                   never reads it, :2080-2094) */
 } cpl_fields;
 
 /* what one cpl_pelagic_soil call did on the device */
@@ -77,8 +80,20 @@ typedef struct cpl_stats {
 } cpl_stats;
 
 int cpl_default_params(cpl_params *p);
-/* gotm_npzd's fields: detN = detritus (3), din = nutrients (0), others -1 */
+/* gotm_npzd's fields: detN = detritus (3), din = nutrients (0), others -1
+ * (its bottom fluxes: nutrients_ and detritus_upward_flux_at_soil_surface) */
 int cpl_npzd_fields(cpl_fields *f);
+
+/* &soil_pelagic_connector (src/mediators/soil_pelagic_connector.F90:36-41,
+ * 140); NC_ldet and NC_sdet are read by the namelist and unused by the Run */
+typedef struct cpl_soil_params {
+  double dinflux_const;  /* mmol/m2/yr added to the DIN flux, 0 */
+  double dipflux_const;  /* mmol/m2/yr added to the phosphate flux, -1 */
+  double NC_ldet, NC_sdet; /* 0.2, 0.04 */
+  double convertN, convertP; /* 1, 1 */
+} cpl_soil_params;
+
+int cpl_soil_default_params(cpl_soil_params *p);
 
 /* One connector Run followed by the sediment's boundary assembly.
  *   temperature  [ncol] temperature_at_soil_surface (required; the pelagic
@@ -103,6 +118,25 @@ int cpl_pelagic_soil(pel_handle *pel, sed_handle *sed, const cpl_params *p,
                      const double *water_depth, const double *tke,
                      const double *velocity_in, double *surface_out,
                      double *velocity_out, int *present_out, cpl_stats *stats);
+
+/* The reverse direction: one Run of soil_pelagic_connector
+ * (src/mediators/soil_pelagic_connector.F90:179-965).  The sediment
+ * component exports every tracer's upward flux at the soil surface as
+ * -fluxes(:,:,n) (fabm_sediment_component.F90:1808-1815); the connector maps
+ * them to the pelagic fields' <name>_upward_flux_at_soil_surface, which the
+ * pelagic Run applies to its bottom layer (bfl, fabm_pelagic_component.F90
+ * :2093-2105).  This call reads the sediment handle's device fluxes after its
+ * last step and writes the pelagic handle's bottom-flux rows (as
+ * pel_set_forcing's bottom_flux) on the device; rows of fields the connector
+ * does not write keep their values (zeros if the handle had none).
+ *   bottom_flux_out  [PEL_NTR][ncol] the pelagic bottom fluxes after the
+ *                    call (host copy), or NULL
+ *   present_out      [PEL_NTR] 1 where the connector wrote the row, or NULL
+ * The sediment handle needs its forcing (a step's fluxes), the pelagic
+ * handle its grid. */
+int cpl_soil_pelagic(sed_handle *sed, pel_handle *pel, const cpl_soil_params *p,
+                     const cpl_fields *f, double *bottom_flux_out, int *present_out,
+                     cpl_stats *stats);
 
 #ifdef __cplusplus
 }

@@ -13,6 +13,7 @@
 
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "../../include/mossco_cpl.h"
 #include "cpl_internal.h"
@@ -128,6 +129,48 @@ __global__ void k_pelagic_soil(Args a) {
   }
 }
 
+// ---- the reverse direction: soil upward fluxes into the pelagic bottom
+// fluxes (soil_pelagic_connector.F90:179-965)
+
+struct SoilArgs {
+  const double* fluxes;  // the sediment's [NTR][ncol], downward positive
+  void* bfl;             // the pelagic handle's [PEL_NTR][ncol], its precision
+  int ncol;
+  int nit, amm, din, dip, oxy, odu, detN, detC, detP;  // pelagic rows, -1 absent
+  double cN, cP;
+  double dinc, dipc;     // dinflux_const/(86400.0*365.0), dipflux_const/(...)
+};
+
+template <typename real>
+__global__ void k_soil_pelagic(SoilArgs a) {
+  real* b = static_cast<real*>(a.bfl);
+  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < a.ncol;
+       col += gridDim.x * blockDim.x) {
+    // the soil's export: upward flux = -fluxes(:,:,n) (:1808-1815)
+    auto U = [&](int n) { return -a.fluxes[(size_t)n * a.ncol + col]; };
+    auto W = [&](int row, double v) { b[(size_t)row * a.ncol + col] = (real)v; };
+    const double no3 = U(kNit), nh4 = U(kAmm);
+    if (a.nit >= 0) W(a.nit, no3);                              // :352-356
+    if (a.amm >= 0) W(a.amm, a.cN * nh4);                       // :408-412
+    if (a.din >= 0) W(a.din, (nh4 + no3 + a.dinc) * a.cN);      // :467-473
+    if (a.dip >= 0) W(a.dip, a.cP * (U(kPho) + a.dipc));        // :528-534
+    const double o2 = U(kOxy), odu = U(kOdu);                   // :643-667
+    if (a.odu >= 0 && a.oxy >= 0) {
+      W(a.odu, odu);
+      W(a.oxy, o2);
+    } else if (a.odu >= 0) {
+      W(a.odu, odu - o2);
+    } else if (a.oxy >= 0) {
+      W(a.oxy, o2 - odu);
+    }
+    // detritus: zero, then every soil flux the Run's pattern matches, in
+    // ESMF's alphabetical item order (:734-960)
+    if (a.detN >= 0) W(a.detN, 0.0 + U(kLabN) + U(kSemN));
+    if (a.detC >= 0) W(a.detC, 0.0 + U(kLabC) + U(kSemC));
+    if (a.detP >= 0) W(a.detP, 0.0);
+  }
+}
+
 bool bad_index(int i) { return i < -1 || i >= PEL_NTR; }
 
 // CUDA events at marks 0..3 on one stream (none unless init was called)
@@ -187,6 +230,127 @@ int cpl_npzd_fields(cpl_fields* f) {
   f->ammonium = -1;
   f->oxygen = -1;
   f->odu = -1;
+  f->dip = -1;
+  return SED_OK;
+}
+
+int cpl_soil_default_params(cpl_soil_params* p) {
+  if (!p) return SED_E_ARG;
+  memset(p, 0, sizeof *p);
+  // soil_pelagic_connector.F90:36-41 (0.0 and -1. are default reals)
+  p->dinflux_const = (double)0.0f;
+  p->dipflux_const = (double)-1.0f;
+  p->NC_ldet = 0.20;
+  p->NC_sdet = 0.04;
+  p->convertP = 1.0;
+  p->convertN = 1.0;
+  return SED_OK;
+}
+
+int cpl_soil_pelagic(sed_handle* sed, pel_handle* pel, const cpl_soil_params* p,
+                     const cpl_fields* f, double* bottom_flux_out, int* present_out,
+                     cpl_stats* stats) {
+  if (stats) memset(stats, 0, sizeof *stats);
+  if (!sed) return SED_E_ARG;
+  if (!pel) return cpl::sed_fail(sed, SED_E_ARG, "pelagic handle is NULL");
+  if (!p || !f) return cpl::sed_fail(sed, SED_E_ARG, "params and fields are required");
+  const int rows[] = {f->nitrate, f->ammonium, f->din, f->dip, f->oxygen, f->odu,
+                      f->detN, f->detC, f->detP};
+  for (int i : rows)
+    if (bad_index(i)) return cpl::sed_fail(sed, SED_E_ARG, "field index out of range");
+  for (int i = 0; i < 9; i++)
+    for (int j = i + 1; j < 9; j++)
+      if (rows[i] >= 0 && rows[i] == rows[j])
+        return cpl::sed_fail(sed, SED_E_ARG, "two fields on one pelagic tracer");
+  void* bfl = nullptr;
+  if (int rc = cpl::pel_bottom_flux(pel, &bfl)) {
+    std::string m = std::string("pelagic handle: ") + pel_last_error(pel);
+    return cpl::sed_fail(sed, rc, m.c_str());
+  }
+  cpl::PelView v;
+  if (int rc = cpl::pel_view(pel, &v, false)) {
+    std::string m = std::string("pelagic handle: ") + pel_last_error(pel);
+    return cpl::sed_fail(sed, rc, m.c_str());
+  }
+  cpl::SedStaging s;
+  if (int rc = cpl::sed_staging(sed, &s)) return rc;
+  if (v.ncol != s.ncol)
+    return cpl::sed_fail(sed, SED_E_ARG, "the handles' grids differ in inum*jnum");
+  if (v.device != s.device)
+    return cpl::sed_fail(sed, SED_E_ARG, "the handles are on different devices");
+  const double* fl = nullptr;
+  if (int rc = cpl::sed_surface_fluxes(sed, &fl)) return rc;
+  cudaStream_t pst = v.stream;
+  const bool fp64 = v.fp64;
+  const size_t nc = (size_t)s.ncol;
+  cudaError_t e = cudaSuccess;
+  auto ok = [&](cudaError_t r) { if (e == cudaSuccess) e = r; return r == cudaSuccess; };
+  // the sediment's last step and flux scatter before the reads
+  cudaEvent_t ev = nullptr;
+  ok(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  if (e == cudaSuccess) {
+    ok(cudaEventRecord(ev, s.stream));
+    ok(cudaStreamWaitEvent(pst, ev, 0));
+  }
+  if (ev) cudaEventDestroy(ev);
+  Timing tm;
+  if (stats) tm.init(&e, pst);
+  SoilArgs a{};
+  a.fluxes = fl;
+  a.bfl = bfl;
+  a.ncol = s.ncol;
+  a.nit = f->nitrate; a.amm = f->ammonium; a.din = f->din; a.dip = f->dip;
+  a.oxy = f->oxygen; a.odu = f->odu; a.detN = f->detN; a.detC = f->detC; a.detP = f->detP;
+  a.cN = p->convertN;
+  a.cP = p->convertP;
+  // (86400.0*365.0) is a default-real product, 31536000 exactly
+  const double year = (double)(86400.0f * 365.0f);
+  a.dinc = p->dinflux_const / year;
+  a.dipc = p->dipflux_const / year;
+  const int threads = 256;
+  long long blocks = ((long long)nc + threads - 1) / threads;
+  const long long cap = (long long)(s.sms > 0 ? s.sms : 1) * 8;
+  if (blocks > cap) blocks = cap;
+  tm.mark(0);
+  tm.mark(1);
+  if (e == cudaSuccess) {
+    if (fp64)
+      k_soil_pelagic<double><<<(int)blocks, threads, 0, pst>>>(a);
+    else
+      k_soil_pelagic<float><<<(int)blocks, threads, 0, pst>>>(a);
+    e = cudaGetLastError();
+  }
+  tm.mark(2);
+  std::vector<float> tmp32;
+  if (bottom_flux_out && e == cudaSuccess) {
+    if (fp64) {
+      ok(cudaMemcpyAsync(bottom_flux_out, bfl, PEL_NTR * nc * sizeof(double),
+                         cudaMemcpyDeviceToHost, pst));
+    } else {
+      tmp32.resize(PEL_NTR * nc);
+      ok(cudaMemcpyAsync(tmp32.data(), bfl, PEL_NTR * nc * sizeof(float),
+                         cudaMemcpyDeviceToHost, pst));
+    }
+  }
+  tm.mark(3);
+  ok(cudaStreamSynchronize(pst));
+  if (e != cudaSuccess) {
+    std::string m = std::string("soil coupling: ") + cudaGetErrorString(e);
+    return cpl::sed_fail(sed, SED_E_CUDA, m.c_str());
+  }
+  if (bottom_flux_out && !fp64)
+    for (size_t i = 0; i < tmp32.size(); i++) bottom_flux_out[i] = (double)tmp32[i];
+  if (present_out) {
+    for (int n = 0; n < PEL_NTR; n++) present_out[n] = 0;
+    for (int i : rows)
+      if (i >= 0) present_out[i] = 1;
+  }
+  if (stats) {
+    stats->gpu_launches = 2;  // the sediment's flux scatter and the mapping
+    stats->columns = (long long)nc;
+    stats->kernel_ms = tm.ms(1, 2);
+    stats->device_ms = tm.ms(0, 3);
+  }
   return SED_OK;
 }
 
@@ -200,7 +364,8 @@ int cpl_pelagic_soil(pel_handle* pel, sed_handle* sed, const cpl_params* p,
   if (!pel) return cpl::sed_fail(sed, SED_E_ARG, "pelagic handle is NULL");
   if (!p || !f || !temperature)
     return cpl::sed_fail(sed, SED_E_ARG, "params, fields and temperature are required");
-  for (int i : {f->detN, f->detC, f->detP, f->din, f->nitrate, f->ammonium, f->oxygen, f->odu})
+  for (int i : {f->detN, f->detC, f->detP, f->din, f->nitrate, f->ammonium, f->oxygen, f->odu,
+                f->dip})
     if (bad_index(i)) return cpl::sed_fail(sed, SED_E_ARG, "field index out of range");
   if (f->din < 0 && f->nitrate < 0 && f->ammonium < 0)
     return cpl::sed_fail(sed, SED_E_ARG, "no nitrate, ammonium or DIN field");

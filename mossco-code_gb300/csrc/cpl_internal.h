@@ -19,8 +19,12 @@ struct PelView {
   cudaStream_t stream = nullptr;
 };
 // SED_E_STATE (with the message on the pelagic handle) when the handle
-// has no state yet.
-int pel_view(pel_handle* h, PelView* v);
+// has no grid, or no state yet and need_state is set (state is then null).
+int pel_view(pel_handle* h, PelView* v, bool need_state = true);
+// The handle's bottom-flux rows [PEL_NTR][ncol] in its precision, zeroed
+// and switched on when the handle had none (pel_set_forcing's
+// bottom_flux); SED_E_STATE without a grid.
+int pel_bottom_flux(pel_handle* h, void** bfl);
 
 // The sediment handle's boundary staging rows on the device, allocated on
 // first use: temperature [ncol], surface [SED_NTR][ncol], velocity
@@ -34,6 +38,10 @@ struct SedStaging {
   cudaStream_t stream = nullptr;
 };
 int sed_staging(sed_handle* h, SedStaging* s);
+// the handle's fluxes [SED_NTR][ncol] (FP64, downward positive) with the
+// surface fluxes of its last step scattered into the dissolved rows, as
+// sed_get_fluxes returns them; SED_E_STATE before any forcing
+int sed_surface_fluxes(sed_handle* h, const double** fluxes);
 // get_boundary_conditions on the staged rows: bdys / fluxes of the tracers
 // in present_mask, then the forcing rows of the next step.
 int sed_assemble_staged(sed_handle* h, unsigned present_mask);

@@ -1338,14 +1338,28 @@ int pel_step(pel_handle* h, double t_couple, double dt, int method, int nruns,
 
 }  // extern "C"
 
-int cpl::pel_view(pel_handle* h, PelView* v) {
+int cpl::pel_view(pel_handle* h, PelView* v, bool need_state) {
   if (!h || !v) return SED_E_ARG;
-  if (int rc = need(h, true, false, true, false)) return rc;
-  v->state = h->d_state.p;
+  if (int rc = need(h, true, false, need_state, false)) return rc;
+  v->state = h->have_state ? h->d_state.p : nullptr;
   v->fp64 = h->fp64();
   v->ncol = h->ncol;
   v->K = h->K;
   v->device = h->device;
   v->stream = h->stream;
+  return SED_OK;
+}
+
+int cpl::pel_bottom_flux(pel_handle* h, void** bfl) {
+  if (!h || !bfl) return SED_E_ARG;
+  if (int rc = need(h, true, false, false, false)) return rc;
+  if (!h->has_bfl) {
+    const size_t bytes = NTR * (size_t)h->ncol * h->rsize();
+    PK(h->d_bfl.alloc(bytes), "bottom flux");
+    PK(cudaMemsetAsync(h->d_bfl.p, 0, bytes, h->stream), "bottom flux");
+    PK(cudaStreamSynchronize(h->stream), "bottom flux");
+    h->has_bfl = true;
+  }
+  *bfl = h->d_bfl.p;
   return SED_OK;
 }

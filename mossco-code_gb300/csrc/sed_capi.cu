@@ -1718,6 +1718,16 @@ int cpl::sed_staging(sed_handle* h, SedStaging* s) {
   return SED_OK;
 }
 
+int cpl::sed_surface_fluxes(sed_handle* h, const double** fluxes) {
+  if (!h || !fluxes) return SED_E_ARG;
+  if (!h->have_forcing) return h->fail(SED_E_STATE, "the handle has no forcing yet");
+  CK(cudaSetDevice(h->device), "set device");
+  int rc = h->fp64() ? scatter_fluxes<double>(h) : scatter_fluxes<float>(h);
+  if (rc) return rc;
+  *fluxes = h->d_fluxes.as<double>();
+  return SED_OK;
+}
+
 int cpl::sed_fail(sed_handle* h, int code, const char* msg) {
   return h ? h->fail(code, "%s", msg) : code;
 }

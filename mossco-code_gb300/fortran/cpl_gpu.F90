@@ -6,7 +6,11 @@
 !! :176-2122) and the sediment component's get_boundary_conditions
 !! (src/components/fabm_sediment_component.F90:1865-2030) become one call,
 !! `call cpl_gpu_pelagic_soil(pgpu, sgpu, p, f, temperature, rc)`, from the
-!! pelagic handle's device state into the sediment handle's boundary.  The
+!! pelagic handle's device state into the sediment handle's boundary; the
+!! soil_pelagic_connector's Run (src/mediators/soil_pelagic_connector.F90
+!! :179-965) becomes `rc = cpl_soil_pelagic(sgpu%h, pgpu%h, sp, f, c_null_ptr,
+!! c_null_ptr, c_null_ptr)`, from the soil's fluxes into the pelagic handle's
+!! bottom fluxes.  The
 !! 2-D fields keep their Fortran layout: temperature(i,j) is the C ABI's
 !! [ncol] with col = i + inum*(j-1).
 module cpl_gpu
@@ -29,7 +33,12 @@ module cpl_gpu
 
   !> cpl_fields of mossco_cpl.h: 0-based pelagic tracer index, or -1
   type, bind(C), public :: cpl_fields_t
-    integer(c_int) :: detN, detC, detP, din, nitrate, ammonium, oxygen, odu
+    integer(c_int) :: detN, detC, detP, din, nitrate, ammonium, oxygen, odu, dip
+  end type
+
+  !> cpl_soil_params of mossco_cpl.h: the &soil_pelagic_connector namelist
+  type, bind(C), public :: cpl_soil_params_t
+    real(c_double) :: dinflux_const, dipflux_const, NC_ldet, NC_sdet, convertN, convertP
   end type
 
   !> cpl_stats of mossco_cpl.h
@@ -58,9 +67,24 @@ module cpl_gpu
       type(c_ptr), value :: temperature, water_depth, tke, velocity_in, &
                             surface_out, velocity_out, present_out, stats
     end function
+    integer(c_int) function cpl_soil_default_params(p) bind(C, name='cpl_soil_default_params')
+      import :: c_int, cpl_soil_params_t
+      type(cpl_soil_params_t), intent(out) :: p
+    end function
+    !> soil_pelagic_connector's Run: the soil handle's fluxes after its step
+    !! into the pelagic handle's bottom fluxes, on the device
+    integer(c_int) function cpl_soil_pelagic(sed, pel, p, f, bottom_flux_out, present_out, &
+        stats) bind(C, name='cpl_soil_pelagic')
+      import :: c_int, c_ptr, cpl_soil_params_t, cpl_fields_t
+      type(c_ptr), value :: sed, pel
+      type(cpl_soil_params_t), intent(in) :: p
+      type(cpl_fields_t), intent(in) :: f
+      type(c_ptr), value :: bottom_flux_out, present_out, stats
+    end function
   end interface
 
-  public :: cpl_default_params, cpl_npzd_fields, cpl_pelagic_soil, cpl_gpu_pelagic_soil
+  public :: cpl_default_params, cpl_npzd_fields, cpl_pelagic_soil, cpl_gpu_pelagic_soil, &
+            cpl_soil_default_params, cpl_soil_pelagic
 
 contains
 

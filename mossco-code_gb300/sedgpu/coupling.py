@@ -28,7 +28,9 @@ CPL_AS_NAMED = 1
 PARAM_NAMES = ("sinking_factor", "sinking_factor_min", "NC_ldet", "NC_sdet", "convertN",
                "convertP", "half_sedimentation_depth", "half_sedimentation_tke",
                "critical_detritus")
-FIELD_NAMES = ("detN", "detC", "detP", "din", "nitrate", "ammonium", "oxygen", "odu")
+FIELD_NAMES = ("detN", "detC", "detP", "din", "nitrate", "ammonium", "oxygen", "odu", "dip")
+SOIL_PARAM_NAMES = ("dinflux_const", "dipflux_const", "NC_ldet", "NC_sdet", "convertN",
+                    "convertP")
 
 
 class CplParams(ctypes.Structure):
@@ -37,6 +39,10 @@ class CplParams(ctypes.Structure):
 
 class CplFields(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in FIELD_NAMES]
+
+
+class CplSoilParams(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in SOIL_PARAM_NAMES]
 
 
 class CplStats(ctypes.Structure):
@@ -57,6 +63,10 @@ CPL_SIGNATURES = {
     "cpl_pelagic_soil": (ctypes.c_int, [_H, _H, ctypes.POINTER(CplParams),
                                         ctypes.POINTER(CplFields), _dp, _dp, _dp, _dp, _dp,
                                         _dp, _ip, ctypes.POINTER(CplStats)]),
+    "cpl_soil_default_params": (ctypes.c_int, [ctypes.POINTER(CplSoilParams)]),
+    "cpl_soil_pelagic": (ctypes.c_int, [_H, _H, ctypes.POINTER(CplSoilParams),
+                                        ctypes.POINTER(CplFields), _dp, _ip,
+                                        ctypes.POINTER(CplStats)]),
 }
 
 _registered = False
@@ -99,6 +109,15 @@ def npzd_fields(**overrides) -> CplFields:
     return f
 
 
+def soil_default_params(**overrides) -> CplSoilParams:
+    p = CplSoilParams()
+    if load().cpl_soil_default_params(ctypes.byref(p)) != SED_OK:
+        raise SedError(-1, "cpl_soil_default_params")
+    for k, v in overrides.items():
+        setattr(p, k, v)
+    return p
+
+
 def _f64(a):
     return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
 
@@ -138,3 +157,23 @@ def pelagic_soil(pel: PelagicSolver, sed: Solver, temperature, water_depth=None,
     if rc != SED_OK:
         raise SedError(rc, "cpl_pelagic_soil: " + L.sed_last_error(sed.h).decode())
     return surface, velocity, present
+
+
+def soil_pelagic(sed: Solver, pel: PelagicSolver, params: Optional[CplSoilParams] = None,
+                 fields: Optional[CplFields] = None, stats: Optional[CplStats] = None,
+                 read_back: bool = True) -> Tuple[Optional[np.ndarray], np.ndarray]:
+    """One soil_pelagic_connector Run from ``sed``'s fluxes after its last
+    step into ``pel``'s bottom-flux rows, on the device.  Returns the
+    pelagic bottom fluxes [PEL_NTR][ncol] (host copy, None without
+    ``read_back``) and present [PEL_NTR] (1 for the rows written)."""
+    from .pelagic import PEL_NTR
+    L = load()
+    p = params or soil_default_params()
+    f = fields or npzd_fields()
+    out = np.zeros((PEL_NTR, sed.cs.ncol)) if read_back else None
+    present = np.zeros(PEL_NTR, dtype=np.int32)
+    rc = L.cpl_soil_pelagic(sed.h, pel.h, ctypes.byref(p), ctypes.byref(f), _p(out),
+                            _p(present, _ip), None if stats is None else ctypes.byref(stats))
+    if rc != SED_OK:
+        raise SedError(rc, "cpl_soil_pelagic: " + L.sed_last_error(sed.h).decode())
+    return out, present

@@ -22,7 +22,9 @@
  */
 #include "cpl_oracle.h"
 
+#include <stdio.h>
 #include <stdlib.h>
+#include <string.h>
 
 enum { LC = 0, SC = 1, LN = 2, SN = 3, LP = 4, OX = 6, NI = 7, AM = 8, OD = 9, PH = 10 };
 
@@ -185,4 +187,114 @@ int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
 #undef ROW
   free(CN); free(fl); free(rl); free(fs); free(rs); free(fe); free(din);
   return 0;
+}
+
+/* ---- soil_pelagic_connector (src/mediators/soil_pelagic_connector.F90) */
+
+void orc_cpl_soil_defaults(orc_cpl_soil *p) {
+  /* :36-41; 0.0 and -1. are default-real literals */
+  p->dinflux_const = (double)0.0f;
+  p->dipflux_const = (double)-1.0f;
+  p->NC_ldet = 0.20;
+  p->NC_sdet = 0.04;
+  p->convertP = 1.0;
+  p->convertN = 1.0;
+}
+
+/* the soil's export names (the pelagic_soil_connector's own searches use
+ * them: :1243-1493, :1768, :1864, :2088, :740, :768) */
+static const char *const soil_names[11] = {
+    "detritus_labile_carbon",        "detritus_semilabile_carbon",
+    "detritus_labile_nitrogen",      "detritus_semilabile_nitrogen",
+    "detritus_labile_phosphorus",    "adsorbed_phosphorus",
+    "dissolved_oxygen",              "mole_concentration_of_nitrate",
+    "mole_concentration_of_ammonium", "dissolved_reduced_substances",
+    "mole_concentration_of_phosphate"};
+
+/* MOSSCO_StringMatchPattern (mossco_strings.F90:331-396) for a pattern
+ * with one inner asterisk: only the part after the asterisk is compared,
+ * as the end of the item */
+static int match_after_star(const char *item, const char *pattern) {
+  const char *star = strchr(pattern, '*');
+  size_t li = strlen(item), ls;
+  if (!star) return strcmp(item, pattern) == 0;
+  star++;
+  ls = strlen(star);
+  return li >= ls && strcmp(item + li - ls, star) == 0;
+}
+
+static int by_name(const void *a, const void *b) {
+  return strcmp(soil_names[*(const int *)a], soil_names[*(const int *)b]);
+}
+
+/* zero, then += every soil upward flux whose name the pattern matches, in
+ * ESMF's alphabetical item order (:776-805, :846-875, :915-944) */
+static void detritus_sum(const char *pattern, const double *fluxes, int ncol, double *dst) {
+  int order[11], i, n;
+  char item[96];
+  for (n = 0; n < 11; n++) order[n] = n;
+  qsort(order, 11, sizeof(int), by_name);
+  for (i = 0; i < ncol; i++) dst[i] = 0.0;
+  for (n = 0; n < 11; n++) {
+    snprintf(item, sizeof item, "%s_upward_flux_at_soil_surface", soil_names[order[n]]);
+    if (!match_after_star(item, pattern)) continue;
+    for (i = 0; i < ncol; i++) dst[i] = dst[i] + -fluxes[(size_t)order[n] * ncol + i];
+  }
+}
+
+void orc_cpl_soil_run(const orc_cpl_soil *p, const orc_cpl_soil_fields *f,
+                      const double *fluxes, int ncol, int ntr, double *bfl, int *present) {
+  /* the soil's export: upward flux = -fluxes(:,:,n) (fabm_sediment_component
+   * .F90:1808-1815) */
+  double *up = malloc(sizeof(double) * 11 * (size_t)ncol);
+  const double year = (double)(86400.0f * 365.0f);
+  int i, n;
+  for (n = 0; n < 11 * ncol; n++) up[n] = -fluxes[n];
+  for (n = 0; n < ntr; n++) present[n] = 0;
+#define UP(r) (up + (size_t)(r) * ncol)
+#define ROW(r) (bfl + (size_t)(r) * ncol)
+  if (f->nitrate >= 0) {  /* :352-356 */
+    for (i = 0; i < ncol; i++) ROW(f->nitrate)[i] = UP(NI)[i];
+    present[f->nitrate] = 1;
+  }
+  if (f->ammonium >= 0) {  /* :408-412 */
+    for (i = 0; i < ncol; i++) ROW(f->ammonium)[i] = p->convertN * UP(AM)[i];
+    present[f->ammonium] = 1;
+  }
+  if (f->din >= 0) {  /* :467-473 */
+    for (i = 0; i < ncol; i++)
+      ROW(f->din)[i] = (UP(AM)[i] + UP(NI)[i] + p->dinflux_const / year) * p->convertN;
+    present[f->din] = 1;
+  }
+  if (f->dip >= 0) {  /* :528-534 */
+    for (i = 0; i < ncol; i++)
+      ROW(f->dip)[i] = p->convertP * (UP(PH)[i] + p->dipflux_const / year);
+    present[f->dip] = 1;
+  }
+  if (f->odu >= 0 && f->oxygen >= 0) {  /* :643-667 */
+    for (i = 0; i < ncol; i++) ROW(f->odu)[i] = UP(OD)[i];
+    for (i = 0; i < ncol; i++) ROW(f->oxygen)[i] = UP(OX)[i];
+    present[f->odu] = present[f->oxygen] = 1;
+  } else if (f->odu >= 0) {
+    for (i = 0; i < ncol; i++) ROW(f->odu)[i] = UP(OD)[i] - UP(OX)[i];
+    present[f->odu] = 1;
+  } else if (f->oxygen >= 0) {
+    for (i = 0; i < ncol; i++) ROW(f->oxygen)[i] = UP(OX)[i] - UP(OD)[i];
+    present[f->oxygen] = 1;
+  }
+  if (f->detN >= 0) {
+    detritus_sum("detritus*nitrogen_upward_flux_at_soil_surface", fluxes, ncol, ROW(f->detN));
+    present[f->detN] = 1;
+  }
+  if (f->detC >= 0) {
+    detritus_sum("detritus*carbon_upward_flux_at_soil_surface", fluxes, ncol, ROW(f->detC));
+    present[f->detC] = 1;
+  }
+  if (f->detP >= 0) {
+    detritus_sum("detritus*phosphorous_upward_flux_at_soil_surface", fluxes, ncol, ROW(f->detP));
+    present[f->detP] = 1;
+  }
+#undef UP
+#undef ROW
+  free(up);
 }

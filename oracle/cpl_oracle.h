@@ -34,6 +34,25 @@ int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
                 int ncol, int knum, const double *depth, const double *tke,
                 double *surface, double *velocity, int *present);
 
+/* &soil_pelagic_connector (soil_pelagic_connector.F90:36-41) */
+typedef struct {
+  double dinflux_const, dipflux_const, NC_ldet, NC_sdet, convertN, convertP;
+} orc_cpl_soil;
+
+/* pelagic tracer row of each field the reverse Run writes, -1 = absent */
+typedef struct {
+  int nitrate, ammonium, din, dip, oxygen, odu, detN, detC, detP;
+} orc_cpl_soil_fields;
+
+void orc_cpl_soil_defaults(orc_cpl_soil *p);
+
+/* One soil_pelagic_connector Run: fluxes [11][ncol] are the sediment's
+ * (downward positive); bfl [ntr][ncol] holds the pelagic bottom fluxes
+ * before the Run and is updated where the Run writes; present [ntr] is set
+ * to 1 for every row written. */
+void orc_cpl_soil_run(const orc_cpl_soil *p, const orc_cpl_soil_fields *f,
+                      const double *fluxes, int ncol, int ntr, double *bfl, int *present);
+
 #ifdef __cplusplus
 }
 #endif

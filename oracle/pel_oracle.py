@@ -90,6 +90,20 @@ class OrcCplFields(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in CPL_FIELD_NAMES]
 
 
+CPL_SOIL_PARAM_NAMES = ("dinflux_const", "dipflux_const", "NC_ldet", "NC_sdet", "convertN",
+                        "convertP")
+CPL_SOIL_FIELD_NAMES = ("nitrate", "ammonium", "din", "dip", "oxygen", "odu", "detN", "detC",
+                        "detP")
+
+
+class OrcCplSoil(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in CPL_SOIL_PARAM_NAMES]
+
+
+class OrcCplSoilFields(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in CPL_SOIL_FIELD_NAMES]
+
+
 _lib = None
 
 
@@ -114,6 +128,11 @@ def lib():
         L.orc_cpl_run.argtypes = [P(OrcCpl), P(OrcCplFields), _dp, ctypes.c_int, ctypes.c_int,
                                   _dp, _dp, _dp, _dp, P(ctypes.c_int)]
         L.orc_cpl_run.restype = ctypes.c_int
+        L.orc_cpl_soil_defaults.argtypes = [P(OrcCplSoil)]
+        L.orc_cpl_soil_defaults.restype = None
+        L.orc_cpl_soil_run.argtypes = [P(OrcCplSoil), P(OrcCplSoilFields), _dp, ctypes.c_int,
+                                       ctypes.c_int, _dp, P(ctypes.c_int)]
+        L.orc_cpl_soil_run.restype = None
         _lib = L
     return _lib
 
@@ -250,3 +269,28 @@ def cpl_run(conc: np.ndarray, fields: dict, params: Optional[dict] = None,
                            _ptr(t), _ptr(surface), _ptr(velocity),
                            present.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
     return rc, surface, velocity, present
+
+
+def cpl_soil_defaults() -> dict:
+    p = OrcCplSoil()
+    lib().orc_cpl_soil_defaults(ctypes.byref(p))
+    return {n: getattr(p, n) for n in CPL_SOIL_PARAM_NAMES}
+
+
+def cpl_soil_run(fluxes: np.ndarray, fields: dict, params: Optional[dict] = None,
+                 bfl_in: Optional[np.ndarray] = None, ntr: int = 4):
+    """One soil_pelagic_connector Run on the sediment fluxes [11][ncol]
+    (downward positive).  Returns (bfl [ntr][ncol], present [ntr]); rows the
+    Run does not write keep bfl_in (zeros by default)."""
+    fl = np.ascontiguousarray(fluxes, dtype=np.float64)
+    ncol = fl.shape[1]
+    p = OrcCplSoil()
+    lib().orc_cpl_soil_defaults(ctypes.byref(p))
+    for k, v in (params or {}).items():
+        setattr(p, k, float(v))
+    f = OrcCplSoilFields(*[int(fields.get(n, -1)) for n in CPL_SOIL_FIELD_NAMES])
+    bfl = np.zeros((ntr, ncol)) if bfl_in is None else np.array(bfl_in, dtype=np.float64)
+    present = np.zeros(ntr, dtype=np.int32)
+    lib().orc_cpl_soil_run(ctypes.byref(p), ctypes.byref(f), _ptr(fl), ncol, ntr, _ptr(bfl),
+                           present.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return bfl, present

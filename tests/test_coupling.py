@@ -106,7 +106,8 @@ def numpy_run(conc, fields, p, as_named, depth=None, tke=None, velocity_in=None)
 def test_library_exports_coupling_abi():
     path = build.build()
     declared = coupling.header_functions()
-    assert declared == ["cpl_default_params", "cpl_npzd_fields", "cpl_pelagic_soil"]
+    assert declared == ["cpl_default_params", "cpl_npzd_fields", "cpl_pelagic_soil",
+                        "cpl_soil_default_params", "cpl_soil_pelagic"]
     out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True,
                          text=True, check=True).stdout
     exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
@@ -138,6 +139,10 @@ def test_null_handles_are_refused():
     assert L.cpl_pelagic_soil(None, None, p, f, None, None, None, None, None, None,
                               None, st) == capi.SED_E_ARG
     assert st.gpu_launches == 0   # cleared on entry
+    st.gpu_launches = 7
+    assert L.cpl_soil_pelagic(None, None, coupling.soil_default_params(), f, None, None,
+                              st) == capi.SED_E_ARG
+    assert st.gpu_launches == 0
 
 
 @pytest.mark.parametrize("fields", FIELD_SETS)
@@ -193,6 +198,69 @@ def test_oracle_run_as_written_overwrites_the_concentrations(po):
 def test_oracle_without_nitrogen_is_not_found(po):
     rc, *_ = po.cpl_run(pel_case(8).conc, dict(detN=3), po.cpl_defaults(), False)
     assert rc == -1
+
+
+# the reverse Run's field tables (pelagic rows of the fields it writes)
+SOIL_FIELD_SETS = [
+    NPZD,                                                   # gotm_npzd: DIN and detN
+    dict(nitrate=0, ammonium=1, dip=2, detC=3),
+    dict(din=0, oxygen=1, odu=2, detP=3),
+    dict(odu=1, detN=3),                                    # deficit as odu - oxygen
+    dict(oxygen=2, din=0),                                  # oxygen - odu
+]
+
+
+def numpy_soil_run(fluxes, fields, p, bfl_in):
+    """The reverse Run restated with whole-array numpy expressions."""
+    up = -fluxes
+    out = bfl_in.copy()
+    year = float(np.float32(86400.0) * np.float32(365.0))
+    g = {k: v for k, v in fields.items() if v >= 0}
+    if "nitrate" in g:
+        out[g["nitrate"]] = up[7]
+    if "ammonium" in g:
+        out[g["ammonium"]] = p["convertN"] * up[8]
+    if "din" in g:
+        out[g["din"]] = (up[8] + up[7] + p["dinflux_const"] / year) * p["convertN"]
+    if "dip" in g:
+        out[g["dip"]] = p["convertP"] * (up[10] + p["dipflux_const"] / year)
+    if "odu" in g and "oxygen" in g:
+        out[g["odu"]], out[g["oxygen"]] = up[9], up[6]
+    elif "odu" in g:
+        out[g["odu"]] = up[9] - up[6]
+    elif "oxygen" in g:
+        out[g["oxygen"]] = up[6] - up[9]
+    if "detN" in g:
+        out[g["detN"]] = 0.0 + up[2] + up[3]
+    if "detC" in g:
+        out[g["detC"]] = 0.0 + up[0] + up[1]
+    if "detP" in g:          # 'detritus*phosphorous': no soil name matches
+        out[g["detP"]] = 0.0
+    return out
+
+
+def test_soil_defaults_are_the_connectors_literals(po):
+    p = coupling.soil_default_params()
+    od = po.cpl_soil_defaults()
+    assert (p.dinflux_const, p.dipflux_const, p.convertN, p.convertP) == (0.0, -1.0, 1.0, 1.0)
+    assert (p.NC_ldet, p.NC_sdet) == (0.2, 0.04)
+    for n in coupling.SOIL_PARAM_NAMES:
+        assert getattr(p, n) == od[n], n
+
+
+@pytest.mark.parametrize("fields", SOIL_FIELD_SETS)
+def test_soil_oracle_matches_numpy_restatement(po, fields):
+    rng = np.random.default_rng(9)
+    ncol = 50
+    fluxes = rng.normal(0.0, 1e-5, (11, ncol))
+    bfl_in = rng.normal(0.0, 1e-6, (4, ncol))
+    p = po.cpl_soil_defaults()
+    p.update(convertN=1.3, convertP=0.7, dinflux_const=2.5)
+    got, present = po.cpl_soil_run(fluxes, fields, p, bfl_in)
+    np.testing.assert_array_equal(got, numpy_soil_run(fluxes, fields, p, bfl_in))
+    for name, row in fields.items():
+        assert present[row] == 1, name
+    assert present.sum() == len(fields)
 
 
 # ---------------------------------------------------------------- GPU
@@ -315,3 +383,75 @@ def test_coupling_errors():
     coupling.pelagic_soil(pel, sed, T)           # the handles still work
     for s in (pel, sed, fresh, other):
         s.close()
+
+
+def soil_fields_struct(d):
+    return coupling.CplFields(*[int(d.get(n, -1)) for n in coupling.FIELD_NAMES])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pel_precision", [capi.SED_FP64, capi.SED_FP32])
+@pytest.mark.parametrize("fields", SOIL_FIELD_SETS)
+def test_device_soil_to_pelagic_bit_exact(po, pel_precision, fields):
+    ncol = 300
+    pcs, cs, pel, sed = handles(ncol, pel_precision)
+    sed.set_forcing()
+    sed.step(1)
+    fl = sed.fluxes()                       # the fluxes the soil exports
+    p = coupling.soil_default_params(convertN=1.3, convertP=0.7, dinflux_const=2.5)
+    st = coupling.CplStats()
+    got, present = coupling.soil_pelagic(sed, pel, params=p, fields=soil_fields_struct(fields),
+                                         stats=st)
+    assert st.gpu_launches == 2 and st.columns == ncol
+    pp = {n: getattr(p, n) for n in coupling.SOIL_PARAM_NAMES}
+    ref, pres0 = po.cpl_soil_run(fl, fields, pp, pcs.bottom_flux)
+    if pel_precision == capi.SED_FP32:   # the handle keeps its rows in FP32
+        ref = ref.astype(np.float32).astype(np.float64)
+    np.testing.assert_array_equal(present, pres0)
+    np.testing.assert_array_equal(got, ref)
+    pel.close()
+    sed.close()
+
+
+@pytest.mark.gpu
+def test_two_way_coupled_loop_equals_host_route(po):
+    """pel_step -> cpl_pelagic_soil -> sed_step -> cpl_soil_pelagic for a
+    few coupling steps, all on the device, equals the loop that takes every
+    exchanged field through the host, maps it with the oracles and sets it
+    with sed_set_boundary and pel_set_forcing."""
+    ncol = 128
+    pcs, cs, pel, sed = handles(ncol, capi.SED_FP32, seed=8)
+    _, _, pel2, sed2 = handles(ncol, capi.SED_FP32, seed=8)
+    T = np.linspace(4.0, 16.0, ncol)
+    depth = np.linspace(1.0, 50.0, ncol)
+    bfl = pcs.bottom_flux.copy()
+    for _ in range(3):
+        pel.step(1)
+        coupling.pelagic_soil(pel, sed, T, depth, read_back=False)
+        sed.step(1)
+        coupling.soil_pelagic(sed, pel, read_back=False)
+        pel2.step(1)
+        rc, S0, V0, P0 = po.cpl_run(pel2.get_state(), NPZD, po.cpl_defaults(), False, depth)
+        sed2.set_boundary(T, S0, V0, P0)
+        sed2.step(1)
+        bfl, _ = po.cpl_soil_run(sed2.fluxes(), NPZD, None, bfl)
+        pel2.set_forcing(bottom_flux=bfl)
+    np.testing.assert_array_equal(pel.get_state(), pel2.get_state())
+    np.testing.assert_array_equal(sed.get_state(), sed2.get_state())
+    for s in (pel, sed, pel2, sed2):
+        s.close()
+
+
+@pytest.mark.gpu
+def test_soil_coupling_errors():
+    pcs, cs, pel, sed = handles(64, capi.SED_FP32)
+    with pytest.raises(capi.SedError) as e:     # no forcing and no step yet
+        coupling.soil_pelagic(sed, pel)
+    assert e.value.code == capi.SED_E_STATE
+    sed.set_forcing()
+    with pytest.raises(capi.SedError) as e:
+        coupling.soil_pelagic(sed, pel, fields=soil_fields_struct(dict(din=0, detN=0)))
+    assert e.value.code == capi.SED_E_ARG
+    coupling.soil_pelagic(sed, pel)
+    pel.close()
+    sed.close()
