@@ -1,14 +1,17 @@
-// cpl_capi.cu -- the pelagic -> soil coupling of include/mossco_cpl.h.
+// cpl_capi.cu -- the pelagic <-> soil coupling of include/mossco_cpl.h.
 //
-// One thread per horizontal column reads the pelagic state's bottom layer
-// (k = 0) and writes the sediment handle's boundary staging rows with the
-// arithmetic of pelagic_soil_connector's Run
+// k_pelagic_soil: one thread per horizontal column reads the pelagic
+// state's bottom layer (k = 0) and writes the sediment handle's boundary
+// staging rows with the arithmetic of pelagic_soil_connector's Run
 // (src/mediators/pelagic_soil_connector.F90:648-2110, 3-D pelagic fields and
 // 2-D soil fields, the branch the reference's set-ups take).  The sediment
 // handle then assembles bdys / fluxes from those rows as sed_set_boundary
-// does.  The work is a few dozen flops per column on about 12 doubles: a
-// pointwise, HBM-bound kernel.  Compiled with -fmad=false so that every
-// product and quotient rounds as the connector's Fortran expression does.
+// does.  k_soil_pelagic: the reverse, soil_pelagic_connector's Run, from the
+// sediment's fluxes into the pelagic handle's bottom-flux rows.
+// Both are pointwise: a few dozen FP64 operations per column on about a
+// dozen doubles, which GB300's FP64 pipe bounds before HBM does.  Compiled
+// with -fmad=false so that every product and quotient rounds as the
+// connectors' Fortran expressions do.
 #include <cuda_runtime.h>
 
 #include <cstring>
