@@ -976,12 +976,12 @@ def run_coupling(args) -> None:
         "metric": CPL_METRIC, "value": world * cs.ncol * calls / (dev_ms / 1e3),
         "unit": "columns/s", "n_gpus": world, "steps": calls, "warmup": args.warmup,
         "ms_per_step": dev_ms / calls, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64 (from the f32 pelagic state)",
+        "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded)",
         "config": {"workload": f"{CPL_PEL} -> {CPL_SED}", "columns": cs.ncol,
                    "fields": "gotm_npzd (detN = detritus, DIN = nutrients)",
                    "mode": "CPL_AS_RUN", "water_depth": "given", "tke": "absent",
-                   "l2": "L2 flushed between timed calls"},
+                   "pelagic_state": "f32", "l2": "L2 flushed between timed calls"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
                      "bytes_per_launch": nbytes, "kernel": "k_pelagic_soil<float>",
