@@ -39,6 +39,11 @@ module pel_gpu
   end type
 
   interface
+    !> the handle's last error message (a C string: read it with sed_c_string)
+    type(c_ptr) function pel_last_error(h) bind(C, name='pel_last_error')
+      import :: c_ptr
+      type(c_ptr), value :: h
+    end function
     integer(c_int) function pel_default_params(p) bind(C, name='pel_default_params')
       import :: c_int, pel_params_t
       type(pel_params_t), intent(out) :: p
@@ -103,7 +108,7 @@ module pel_gpu
 
   public :: pel_default_params, pel_create, pel_destroy, pel_set_grid, pel_set_forcing, &
             pel_set_state, pel_get_state, pel_light, pel_get_rhs, pel_ode_solver, &
-            pel_run, pel_step
+            pel_run, pel_step, pel_last_error
   public :: pel_gpu_init, pel_gpu_forcing, pel_gpu_run, pel_gpu_ode_solver, pel_gpu_finalize
 
 contains

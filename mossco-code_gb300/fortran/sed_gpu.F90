@@ -173,13 +173,73 @@ module sed_gpu
       import :: c_ptr
       type(c_ptr), value :: h
     end subroutine
+    !> diagnostics of the last step: surface fluxes [SED_NTR][ncol] (get_rhs
+    !! :692), attempts [ncol], FP64 budgets [4][ncol]
+    integer(c_int) function sed_get_fluxes(h, fluxes) bind(C, name='sed_get_fluxes')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, fluxes
+    end function
+    integer(c_int) function sed_get_attempts(h, attempts) bind(C, name='sed_get_attempts')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, attempts
+    end function
+    integer(c_int) function sed_get_budgets(h, budgets) bind(C, name='sed_get_budgets')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, budgets
+    end function
+    !> the handle's work on a caller's cudaStream_t (c_ptr)
+    integer(c_int) function sed_set_stream(h, stream) bind(C, name='sed_set_stream')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, stream
+    end function
+    integer(c_int) function sed_host_unregister(ptr) bind(C, name='sed_host_unregister')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ptr
+    end function
+    !> one drop-in coupling step without a handle and without allocation
+    integer(c_int) function sed_ode_solver_noalloc(p, inum, jnum, kmax, dz, dzc, phi, phi_i, &
+        biofac, flux_cap, kact, conc, bdys, fluxes, dt, method, st) &
+        bind(C, name='sed_ode_solver_noalloc')
+      import :: c_int, c_ptr, c_double, sed_params_t, sed_stats_t
+      type(sed_params_t), intent(in) :: p
+      integer(c_int), value :: inum, jnum, kmax
+      type(c_ptr), value :: dz, dzc, phi, phi_i, biofac, flux_cap, kact, conc, bdys, fluxes
+      real(c_double), value :: dt
+      integer(c_int), value :: method
+      type(sed_stats_t), intent(out) :: st
+    end function
+    !> C strings (const char*), read with sed_c_string
+    type(c_ptr) function sed_error_string(code) bind(C, name='sed_error_string')
+      import :: c_ptr, c_int
+      integer(c_int), value :: code
+    end function
+    type(c_ptr) function sed_last_error(h) bind(C, name='sed_last_error')
+      import :: c_ptr
+      type(c_ptr), value :: h
+    end function
+    type(c_ptr) function sed_tracer_name(n) bind(C, name='sed_tracer_name')
+      import :: c_ptr, c_int
+      integer(c_int), value :: n
+    end function
+    integer(c_int) function sed_tracer_is_particulate(n) bind(C, name='sed_tracer_is_particulate')
+      import :: c_int
+      integer(c_int), value :: n
+    end function
+    function c_strlen(s) bind(C, name='strlen')
+      import :: c_ptr, c_size_t
+      type(c_ptr), value :: s
+      integer(c_size_t) :: c_strlen
+    end function
   end interface
 
   public :: sed_default_params, sed_gpu_init, sed_gpu_ode_solver, &
             sed_gpu_get_rhs, sed_gpu_finalize, sed_get_tuning, sed_set_tuning, &
             sed_autotune, sed_set_boundary, sed_get_boundary, sed_spinup, &
             sed_get_min_dt, sed_set_column_bgc, sed_set_state, sed_get_state, &
-            sed_step
+            sed_step, sed_get_fluxes, sed_get_attempts, sed_get_budgets, sed_set_stream, &
+            sed_host_register, sed_host_unregister, sed_ode_solver_noalloc, &
+            sed_error_string, sed_last_error, sed_tracer_name, sed_tracer_is_particulate, &
+            sed_c_string
 
 contains
 
@@ -233,6 +293,25 @@ contains
     if (rc /= SED_OK) return
     rc = sed_get_rhs(gpu%h, c_loc(conc), c_loc(rhs), c_loc(fluxes))
   end subroutine
+
+  !> A C string of the library (sed_error_string, sed_last_error,
+  !! sed_tracer_name, pel_last_error) as a Fortran string.
+  function sed_c_string(p) result(str)
+    type(c_ptr), intent(in) :: p
+    character(len=:), allocatable :: str
+    character(kind=c_char), pointer :: chars(:)
+    integer :: i, n
+    if (.not. c_associated(p)) then
+      str = ''
+      return
+    end if
+    n = int(c_strlen(p))
+    call c_f_pointer(p, chars, [n])
+    allocate(character(len=n) :: str)
+    do i = 1, n
+      str(i:i) = chars(i)
+    end do
+  end function
 
   subroutine sed_gpu_finalize(gpu)
     type(sed_gpu_t), intent(inout) :: gpu
