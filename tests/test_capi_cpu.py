@@ -86,3 +86,9 @@ def test_synth_workload_shapes():
     assert 0.27 < land < 0.33
     act = cs.kact[cs.kact > 0]
     assert act.min() == 10 and act.max() == 60
+    # the soil under the pelagic grid of the coupling measurement: 15 layers
+    # (examples/standalone/omexdia_p/run_sed.nml:34), 0.18 m, 30 % land
+    cs = synth.make_workload("soil_1024x1024", cols=np.arange(20000))
+    assert cs.kmax == 15 and 0.27 < (cs.kact == 0).mean() < 0.33
+    assert set(np.unique(cs.kact)) <= {0, 15}
+    assert abs(cs.dz[:, np.flatnonzero(cs.kact)[0]].sum() - 0.18) < 1e-12
