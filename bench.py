@@ -939,10 +939,24 @@ def run_coupling(args) -> None:
         launches += st.gpu_launches
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
+    # the reverse direction (soil_pelagic_connector) on the fluxes of one
+    # soil step, timed the same way
+    sed.step(1)
+    for _ in range(args.warmup):
+        coupling.soil_pelagic(sed, pel, stats=st, read_back=False)
+    rev_kern = rev_dev = 0.0
+    for _ in range(calls):
+        flush.zero_()
+        torch.cuda.synchronize()
+        coupling.soil_pelagic(sed, pel, stats=st, read_back=False)
+        rev_kern += st.kernel_ms
+        rev_dev += st.device_ms
+        launches += st.gpu_launches
+    torch.cuda.synchronize()
     if dist:
-        t = torch.tensor([dev_ms, kern_ms], device="cuda")
+        t = torch.tensor([dev_ms, kern_ms, rev_dev, rev_kern], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms, kern_ms = (float(v) for v in t.tolist())
+        dev_ms, kern_ms, rev_dev, rev_kern = (float(v) for v in t.tolist())
         dist.barrier()
     clk = clocks.stop()
     e2e = None
@@ -965,6 +979,9 @@ def run_coupling(args) -> None:
             dist.destroy_process_group()
         return
     nbytes = cpl_bytes(cs.ncol, False, True)
+    # reverse, gotm_npzd: four soil flux rows read (8 B each), two pelagic
+    # bottom-flux rows written (4 B each) per column
+    rev_bytes = cs.ncol * (4 * 8 + 2 * 4)
     peak, peak_kind = measured_peaks()
     achieved = nbytes / (kern_ms / calls / 1e3) / 1e9
     cpu = None
@@ -986,10 +1003,19 @@ def run_coupling(args) -> None:
                      "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
                      "bytes_per_launch": nbytes, "kernel": "k_pelagic_soil<float>",
                      "kernel_ms": kern_ms / calls},
+        "reverse": {"kernel": "k_soil_pelagic<float>", "calls": calls,
+                    "kernel_ms": rev_kern / calls, "device_ms": rev_dev / calls,
+                    "bytes_per_launch": rev_bytes,
+                    "achieved_gbs": rev_bytes / (rev_kern / calls / 1e3) / 1e9,
+                    "frac": rev_bytes / (rev_kern / calls / 1e3) / 1e9 / peak,
+                    "note": ("cpl_soil_pelagic: the soil's flux scatter and the mapping of "
+                             "its nitrate, ammonium and detritus N fluxes into the pelagic "
+                             "nutrient and detritus bottom fluxes")},
         "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches,
         "clocks": clk, "wall_s": wall,
         "note": ("ms_per_step and value: the call's device span (temperature and depth "
-                 "copies, the mapping, the boundary assembly and the forcing rows)"),
+                 "copies, the mapping, the boundary assembly and the forcing rows); "
+                 "gpu_launches counts both directions"),
     }
     print(json.dumps(line), flush=True)
     if dist:

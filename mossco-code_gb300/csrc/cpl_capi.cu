@@ -152,19 +152,18 @@ __global__ void k_soil_pelagic(SoilArgs a) {
     // the soil's export: upward flux = -fluxes(:,:,n) (:1808-1815)
     auto U = [&](int n) { return -a.fluxes[(size_t)n * a.ncol + col]; };
     auto W = [&](int row, double v) { b[(size_t)row * a.ncol + col] = (real)v; };
-    const double no3 = U(kNit), nh4 = U(kAmm);
-    if (a.nit >= 0) W(a.nit, no3);                              // :352-356
-    if (a.amm >= 0) W(a.amm, a.cN * nh4);                       // :408-412
-    if (a.din >= 0) W(a.din, (nh4 + no3 + a.dinc) * a.cN);      // :467-473
+    // each soil flux is read only when a field that needs it is present
+    if (a.nit >= 0) W(a.nit, U(kNit));                          // :352-356
+    if (a.amm >= 0) W(a.amm, a.cN * U(kAmm));                   // :408-412
+    if (a.din >= 0) W(a.din, (U(kAmm) + U(kNit) + a.dinc) * a.cN);  // :467-473
     if (a.dip >= 0) W(a.dip, a.cP * (U(kPho) + a.dipc));        // :528-534
-    const double o2 = U(kOxy), odu = U(kOdu);                   // :643-667
-    if (a.odu >= 0 && a.oxy >= 0) {
-      W(a.odu, odu);
-      W(a.oxy, o2);
+    if (a.odu >= 0 && a.oxy >= 0) {                             // :643-667
+      W(a.odu, U(kOdu));
+      W(a.oxy, U(kOxy));
     } else if (a.odu >= 0) {
-      W(a.odu, odu - o2);
+      W(a.odu, U(kOdu) - U(kOxy));
     } else if (a.oxy >= 0) {
-      W(a.oxy, o2 - odu);
+      W(a.oxy, U(kOxy) - U(kOdu));
     }
     // detritus: zero, then every soil flux the Run's pattern matches, in
     // ESMF's alphabetical item order (:734-960)
