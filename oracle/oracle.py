@@ -93,6 +93,15 @@ class Stats(ctypes.Structure):
 _lib = None
 
 
+class Diag(ctypes.Structure):
+    """orc_diag: type_rhs_driver's last_min_dt and last_min_dt_grid_cell."""
+    _fields_ = [("last_min_dt", ctypes.c_double),
+                ("last_min_dt_grid_cell", ctypes.c_int * 4), ("inum", ctypes.c_int)]
+
+    def cell(self):
+        return tuple(self.last_min_dt_grid_cell)
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -108,6 +117,11 @@ def lib():
                               ctypes.c_int, P(Stats)]
         L.orc_run.restype = ctypes.c_int
         L.orc_epilogue.argtypes = [P(Model), _dp]
+        L.orc_diag_init.argtypes = [P(Diag), ctypes.c_int]
+        L.orc_diag_init.restype = None
+        L.orc_ode_solver_diag.argtypes = [P(Model), _dp, _dp, _dp, ctypes.c_double, P(Diag),
+                                          P(Stats)]
+        L.orc_ode_solver_diag.restype = ctypes.c_int
         L.orc_epilogue.restype = ctypes.c_int
         L.orc_omexdia_p.argtypes = [P(Bgc), _dp, _dp, _dp]
         L.orc_diff3d.argtypes = [ctypes.c_int, _dp, ctypes.c_double,
@@ -208,6 +222,27 @@ class OracleModel:
         rc = lib().orc_run(ctypes.byref(self.m), _ptr(conc), _ptr(bd),
                            _ptr(fl), float(dt), int(method), int(percol),
                            int(nsteps), int(nthreads), ctypes.byref(st))
+        return rc, st.as_dict(), fl
+
+    def new_diag(self) -> Diag:
+        """Diagnostics as a fresh driver holds them (last_min_dt 1e20, cell -99)."""
+        d = Diag()
+        lib().orc_diag_init(ctypes.byref(d), self.cs.inum)
+        return d
+
+    def ode_solver_diag(self, conc: np.ndarray, diag: Diag, dt: float = None,
+                        fluxes: Optional[np.ndarray] = None):
+        """One grid-wide ADAPTIVE_EULER call with adaptive_solver_diagnostics,
+        in place on ``conc``; ``diag`` carries across calls.  Returns
+        (status, stats dict, fluxes)."""
+        cs = self.cs
+        assert conc.dtype == np.float64 and conc.flags.c_contiguous
+        fl = np.array(cs.fluxes if fluxes is None else fluxes, dtype=np.float64, copy=True)
+        bd = np.ascontiguousarray(cs.bdys, dtype=np.float64)
+        st = Stats()
+        rc = lib().orc_ode_solver_diag(ctypes.byref(self.m), _ptr(conc), _ptr(bd), _ptr(fl),
+                                       float(cs.dt if dt is None else dt), ctypes.byref(diag),
+                                       ctypes.byref(st))
         return rc, st.as_dict(), fl
 
     def assemble_bc(self, conc, temperature, surface, velocity, present=None,

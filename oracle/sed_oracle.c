@@ -373,9 +373,41 @@ static void rhs_all(const orc_model *m, const double *conc, const double *bdys,
         body;                                                                \
       }
 
+/* minloc((c1 - c)/c) over the grid's whole (i,j,k,n) array in Fortran
+ * element order (i fastest), the diagnostic of solver_library.F90:133-134.
+ * Cells the solver does not step (land, masked tails) keep c1 = c, as the
+ * reference's rhs = 0 there leaves them.  NaN quotients (c = 0) are skipped,
+ * as gfortran's MINLOC skips them; with no other value the first element is
+ * returned.  Indices are 1-based. */
+static void minloc_relative_change(const orc_model *m, const double *conc,
+                                   const double *c1, int inum, int cell[4]) {
+  const int KM = m->kmax, nc = m->ncol;
+  int found = 0;
+  double best = 0.0;
+  size_t pos = 0, idx = 0;
+  for (int n = 0; n < m->ntr; n++)
+    for (int k = 0; k < KM; k++)
+      for (int col = 0; col < nc; col++, idx++) {
+        const size_t i = IDX(n, k, col, KM, nc);
+        const double c = conc[i];
+        const double v = (k < m->kact[col] ? c1[i] - c : c - c) / c;
+        if (v != v) continue;
+        if (!found || v < best) {
+          found = 1;
+          best = v;
+          pos = idx;
+        }
+      }
+  const size_t col = pos % (size_t)nc, kn = pos / (size_t)nc;
+  cell[0] = (int)(col % (size_t)inum) + 1;
+  cell[1] = (int)(col / (size_t)inum) + 1;
+  cell[2] = (int)(kn % (size_t)KM) + 1;
+  cell[3] = (int)(kn / (size_t)KM) + 1;
+}
+
 static int ode_solver_ws(const orc_model *m, double *conc, const double *bdys,
                          double *fluxes, double dt, int method, orc_stats *st,
-                         ode_ws *w) {
+                         ode_ws *w, orc_diag *diag) {
   const double third = 1.0 / 3.0;
   double *c1 = w->c1;
   switch (method) {
@@ -402,6 +434,11 @@ static int ode_solver_ws(const orc_model *m, double *conc, const double *bdys,
         dt_red = dt_red * 0.25;
         if (st) st->rejected++;
       } else {
+        /* adaptive_solver_diagnostics (:129-136), before conc = c1 */
+        if (diag && dt_red < diag->last_min_dt) {
+          diag->last_min_dt = dt_red;
+          minloc_relative_change(m, conc, c1, diag->inum, diag->last_min_dt_grid_cell);
+        }
         FOR_ACTIVE(m, conc[i_] = c1[i_]);
         dt_int = dt_int + dt_red;
         if (st) {
@@ -452,7 +489,23 @@ int orc_ode_solver(const orc_model *m, double *conc, const double *bdys,
                    double *fluxes, double dt, int method, orc_stats *st) {
   ode_ws w;
   ode_ws_alloc(&w, m);
-  int rc = ode_solver_ws(m, conc, bdys, fluxes, dt, method, st, &w);
+  int rc = ode_solver_ws(m, conc, bdys, fluxes, dt, method, st, &w, NULL);
+  ode_ws_free(&w);
+  return rc;
+}
+
+void orc_diag_init(orc_diag *d, int inum) {
+  d->last_min_dt = (double)1.e20f;  /* solver_library.F90:44: a default-real
+                                       literal widened to the driver's kind */
+  for (int i = 0; i < 4; i++) d->last_min_dt_grid_cell[i] = -99;  /* :45 */
+  d->inum = inum;
+}
+
+int orc_ode_solver_diag(const orc_model *m, double *conc, const double *bdys,
+                        double *fluxes, double dt, orc_diag *d, orc_stats *st) {
+  ode_ws w;
+  ode_ws_alloc(&w, m);
+  int rc = ode_solver_ws(m, conc, bdys, fluxes, dt, 2, st, &w, d);
   ode_ws_free(&w);
   return rc;
 }
@@ -516,7 +569,7 @@ static int step_one_column(const orc_model *m, col_ctx *c, int col,
     for (int k = 0; k < KM; k++) c->conc[n * KM + k] = conc[IDX(n, k, col, KM, nc)];
   for (int f = 0; f <= N; f++) c->bdys[f] = bdys[f * nc + col];
   for (int n = 0; n < N; n++) c->fluxes[n] = fluxes[n * nc + col];
-  int rc = ode_solver_ws(&c->m1, c->conc, c->bdys, c->fluxes, dt, method, st, &c->w);
+  int rc = ode_solver_ws(&c->m1, c->conc, c->bdys, c->fluxes, dt, method, st, &c->w, NULL);
   for (int n = 0; n < N; n++)
     for (int k = 0; k < KM; k++) conc[IDX(n, k, col, KM, nc)] = c->conc[n * KM + k];
   for (int n = 0; n < N; n++) fluxes[n * nc + col] = c->fluxes[n];
@@ -638,7 +691,7 @@ int orc_run(const orc_model *m, double *conc, const double *bdys,
   ode_ws_alloc(&w, m);
   int rc = 0;
   for (int s = 0; s < nsteps && rc == 0; s++) {
-    rc = ode_solver_ws(m, conc, bdys, fluxes, dt, method, st, &w);
+    rc = ode_solver_ws(m, conc, bdys, fluxes, dt, method, st, &w, NULL);
     int nan = orc_epilogue(m, conc);
     if (st) st->nan_cells += nan;
     if (nan && rc == 0) rc = -2;

@@ -124,6 +124,23 @@ void orc_get_rhs(const orc_model *m, const double *conc, const double *bdys,
 int orc_ode_solver(const orc_model *m, double *conc, const double *bdys,
                    double *fluxes, double dt, int method, orc_stats *st);
 
+/* type_rhs_driver's diagnostics of the adaptive method
+ * (solver_library.F90:43-45): the smallest accepted substep so far and the
+ * (i,j,k,n) cell (1-based) of the smallest relative change (c1-c)/c at the
+ * substep that set it.  They persist across calls, as on the driver. */
+typedef struct {
+  double last_min_dt;
+  int last_min_dt_grid_cell[4];
+  int inum;               /* grid columns along i (col = i + inum*j) */
+} orc_diag;
+
+void orc_diag_init(orc_diag *d, int inum);
+
+/* ADAPTIVE_EULER over the whole grid with adaptive_solver_diagnostics on
+ * (:129-136), updating d. */
+int orc_ode_solver_diag(const orc_model *m, double *conc, const double *bdys,
+                        double *fluxes, double dt, orc_diag *d, orc_stats *st);
+
 /* Same stepper applied to every column as its own 1-column grid (the
  * per-column refinement the reference's TODO at solver_library.F90:113-116
  * asks for).  OpenMP over columns with nthreads threads (<=0: default). */

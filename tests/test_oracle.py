@@ -269,3 +269,74 @@ def test_assemble_bc_matches_reference_formulas(oracle_mod):
     cs.driver.bcup_dissolved = 2
     _, fl2 = oracle_mod.OracleModel(cs).assemble_bc(cs.conc, T, surf, vel)
     assert np.all(fl2[6:] == 0.0)
+
+
+def numpy_adaptive_diag(om, cs, conc, dt, last_min_dt, cell):
+    """Grid-wide ADAPTIVE_EULER with adaptive_solver_diagnostics restated in
+    numpy over the oracle's right-hand side (solver_library.F90:104-140):
+    on an accepted substep with dt_red < last_min_dt, last_min_dt = dt_red
+    and the cell is minloc((c1 - c)/c) over the whole (i,j,k,n) array,
+    NaN quotients skipped (gfortran's MINLOC)."""
+    m = om.m
+    keep = 1.0 + m.relative_change_min
+    active = (np.arange(cs.kmax)[:, None] < cs.kact[None, :])[None].repeat(NTR, axis=0)
+    fl = np.array(cs.fluxes, dtype=np.float64, copy=True)
+    dt_int, dt_red = 0.0, dt
+    while dt_int < dt:
+        rhs, fl, _ = om.get_rhs(conc, fl)
+        c1 = np.where(active, conc + dt_red * rhs, conc)
+        reject = bool(np.any((c1 - keep * conc < -m.atol) & active))
+        if reject and dt_red > m.dt_min:
+            dt_red = dt_red * 0.25
+            continue
+        if dt_red < last_min_dt:
+            last_min_dt = dt_red
+            with np.errstate(divide="ignore", invalid="ignore"):
+                v = (c1 - conc) / conc
+            shape = (NTR, cs.kmax, cs.jnum, cs.inum)
+            flat = v.reshape(shape).ravel()
+            pos = 0 if np.isnan(flat).all() else int(np.nanargmin(flat))
+            n, k, j, i = np.unravel_index(pos, shape)
+            cell = (int(i) + 1, int(j) + 1, int(k) + 1, int(n) + 1)
+        conc[active] = c1[active]
+        dt_int = dt_int + dt_red
+    return last_min_dt, cell
+
+
+def test_last_min_dt_grid_cell_matches_numpy_restatement(oracle_mod):
+    """a1: type_rhs_driver's last_min_dt and last_min_dt_grid_cell, carried
+    across calls, with land columns (zero state: NaN quotients) and masked
+    bottom tails in the grid."""
+    cs = synth.make_columns(inum=5, jnum=3, kmin=6, kmax=10, total=0.18, land=0.25,
+                            poc="loguniform", days=1, seed=41, name="diag5x3")
+    cs.conc[:, :, cs.kact == 0] = 0.0
+    om = oracle_mod.OracleModel(cs)
+    d = om.new_diag()
+    assert d.cell() == (-99, -99, -99, -99)
+    assert d.last_min_dt == float(np.float32(1e20))
+    got = cs.conc.copy()
+    ref = cs.conc.copy()
+    last, cell = d.last_min_dt, d.cell()
+    for step in range(4):
+        rc, st, _ = om.ode_solver_diag(got, d)
+        assert rc == 0
+        last, cell = numpy_adaptive_diag(om, cs, ref, cs.dt, last, cell)
+        np.testing.assert_array_equal(got, ref)
+        assert d.last_min_dt == last and d.cell() == cell, (step, d.cell(), cell)
+    assert d.last_min_dt < cs.dt                 # the grid did cut
+    i, j, k, n = d.cell()
+    assert cs.kact[(i - 1) + cs.inum * (j - 1)] >= k   # an active cell
+
+
+def test_last_min_dt_grid_cell_of_a_uniform_decay(oracle_mod):
+    """Labile carbon alone decays at lam with lam*dt = 8: the cut sequence
+    is fixed (dt/16 is the first accepted substep), and the smallest
+    relative change is labile carbon's (tracer 1)."""
+    cs = decay_case(ncol=4, K=3, lam_dt=8.0)
+    om = oracle_mod.OracleModel(cs)
+    d = om.new_diag()
+    c = cs.conc.copy()
+    rc, st, _ = om.ode_solver_diag(c, d)
+    assert rc == 0
+    assert d.last_min_dt == cs.dt / 16.0
+    assert d.cell()[3] in (1, 3)    # labile detritus C or N (the same rate)
