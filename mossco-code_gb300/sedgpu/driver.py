@@ -27,7 +27,7 @@ from .model import (ADAPTIVE_EULER, BGC_DEFAULTS, EULER, NTR, RUNGE_KUTTA_4,
                     RUNGE_KUTTA_4_38, ColumnSet, DriverParams)
 
 __all__ = ["TypeSed", "SedGrid", "init_grid", "initialize",
-           "init_concentrations", "update_porosity", "ode_solver", "get_rhs",
+           "init_concentrations", "update_porosity", "ode_solver", "get_rhs", "update_min_dt",
            "EULER", "RUNGE_KUTTA_4", "ADAPTIVE_EULER", "RUNGE_KUTTA_4_38"]
 
 
@@ -87,6 +87,11 @@ class TypeSed:
         self.fluxes = np.zeros((NTR, inum * jnum))
         self.cut_scope = SED_CUT_PER_COLUMN
         self.precision = SED_FP32
+        # type_rhs_driver's diagnostics (solver_library.F90:43-45): kept
+        # across ode_solver calls while adaptive_solver_diagnostics is set
+        self.adaptive_solver_diagnostics = False
+        self.last_min_dt = float(np.float32(1.0e20))
+        self.last_min_dt_grid_cell = [-99, -99, -99, -99]
         self._solver: Optional[Solver] = None
         self._solver_key = None
 
@@ -258,13 +263,33 @@ def init_concentrations(sed: TypeSed, initial_values=None) -> None:
     sed.conc = np.ascontiguousarray(conc)
 
 
+def update_min_dt(rhs_driver: TypeSed, min_dt: np.ndarray) -> None:
+    """last_min_dt / last_min_dt_grid_cell (solver_library.F90:129-136) from
+    the smallest accepted substep of every column in the last call ([ncol],
+    0 where a column accepted none).  The substep is the grid's smallest;
+    its cell is (i, j) of the first column in Fortran order that took it,
+    with the layer and tracer not recorded by the device (-99)."""
+    md = np.asarray(min_dt, dtype=np.float64)
+    pos = np.where(md > 0.0, md, np.inf)
+    if not np.isfinite(pos).any():
+        return
+    col = int(np.argmin(pos))
+    if pos[col] < rhs_driver.last_min_dt:
+        rhs_driver.last_min_dt = float(pos[col])
+        rhs_driver.last_min_dt_grid_cell = [col % rhs_driver.inum + 1,
+                                            col // rhs_driver.inum + 1, -99, -99]
+
+
 def ode_solver(rhs_driver: TypeSed, dt: float, method: int) -> None:
     """solver_library ode_solver (src/utilities/solver_library.F90:80-189):
     advances rhs_driver.conc in place by dt with the given method, followed
     by the component's NaN check and clamp.  Raises SedError on NaN, on the
-    substep cap or on a CUDA error."""
+    substep cap or on a CUDA error.  With adaptive_solver_diagnostics and
+    ADAPTIVE_EULER it updates last_min_dt and last_min_dt_grid_cell."""
     s = rhs_driver.solver()
     s.ode_solver(rhs_driver.conc, rhs_driver.bdys, rhs_driver.fluxes, dt, method)
+    if rhs_driver.adaptive_solver_diagnostics and method == ADAPTIVE_EULER:
+        update_min_dt(rhs_driver, s.min_dt())
 
 
 def get_rhs(rhs_driver: TypeSed) -> np.ndarray:

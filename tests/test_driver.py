@@ -269,3 +269,25 @@ def test_driver_ode_solver_fp32_close_to_oracle(oracle_mod):
     scale = np.abs(want).max(axis=1, keepdims=True) + 1e-30
     assert np.max(np.abs(got - want) / scale) < 1e-3
     sed.solver().close()
+
+
+def test_last_min_dt_diagnostics_mirror():
+    """type_rhs_driver's last_min_dt starts at the default-real 1e20 and the
+    cell at -99 (solver_library.F90:44-45); a call lowers it to the grid's
+    smallest accepted substep, at (i, j) of the first column in Fortran
+    order that took it, and a later call with larger substeps keeps it."""
+    from sedgpu import driver
+    sed = driver.TypeSed(4, 3, 10)
+    assert sed.last_min_dt == float(np.float32(1e20))
+    assert sed.last_min_dt_grid_cell == [-99, -99, -99, -99]
+    assert sed.adaptive_solver_diagnostics is False
+    md = np.full(12, 900.0)
+    md[[2, 7]] = 0.0          # land, or no accepted substep
+    md[6] = 56.25             # col 6 = (i 3, j 2)
+    md[9] = 56.25
+    driver.update_min_dt(sed, md)
+    assert sed.last_min_dt == 56.25 and sed.last_min_dt_grid_cell == [3, 2, -99, -99]
+    driver.update_min_dt(sed, np.full(12, 225.0))
+    assert sed.last_min_dt == 56.25 and sed.last_min_dt_grid_cell == [3, 2, -99, -99]
+    driver.update_min_dt(sed, np.zeros(12))
+    assert sed.last_min_dt == 56.25
