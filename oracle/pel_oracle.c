@@ -295,7 +295,8 @@ int orc_pel_ode_solver(const orc_pel *m, double *conc, const double *par,
 
 /* The component's per-step epilogue on one column (:2093-2105, :2188-2203,
  * :2238): bottom upward fluxes where the bottom layer has a height,
- * external surface fluxes into the top layer, soil-surface fluxes into the
+ * open-boundary values (:2115-2155), external surface fluxes into the top
+ * layer, soil-surface fluxes into the
  * bottom layer unless they would make it negative, then the clip.  Returns
  * the NaN cells seen after ode_solver. */
 static int epilogue_column(const orc_pel *m, double *conc, int col, double dt) {
@@ -314,6 +315,15 @@ static int epilogue_column(const orc_pel *m, double *conc, int col, double dt) {
     for (int n = 0; n < NTR; n++) {
       double *c = &conc[AT(n, 0, col, K, nc)];
       *c = *c + m->bottom_flux[(size_t)n * nc + col] * dt / hb;
+    }
+  /* vertically homogeneous boundary values (:2115-2155); masked cells are
+   * not written, as everywhere in this restatement */
+  if (m->open_boundary && m->open_boundary[col])
+    for (int n = 0; n < NTR; n++) {
+      if (!m->has_boundary_value[n]) continue;
+      for (int k = 0; k < K; k++)
+        if (!masked(m, k, col))
+          conc[AT(n, k, col, K, nc)] = m->boundary_value[(size_t)n * nc + col];
     }
   if (!masked(m, K - 1, col) && m->surface_flux)
     for (int n = 0; n < NTR; n++) {

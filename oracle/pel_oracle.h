@@ -39,6 +39,13 @@ typedef struct {
   long max_attempts;
   int cut_scope;                /* 0 per cell, 1 the reference's grid-wide any() */
   orc_npzd bgc;
+  /* open boundaries (fabm_pelagic_component.F90:2115-2155): columns with
+   * open_boundary[col] set take boundary_value[n][col] in every layer, for
+   * each tracer n with has_boundary_value[n], after the bottom fluxes of
+   * every internal step; NULL = none */
+  const unsigned char *open_boundary;   /* [ncol] */
+  const double *boundary_value;         /* [ntr][ncol] */
+  const int *has_boundary_value;        /* [ntr] */
 } orc_pel;
 
 typedef struct {

@@ -70,7 +70,9 @@ class Pel(ctypes.Structure):
                 ("background_extinction", ctypes.c_double),
                 ("dt_min", ctypes.c_double), ("relative_change_min", ctypes.c_double),
                 ("atol", ctypes.c_double), ("max_attempts", ctypes.c_long),
-                ("cut_scope", ctypes.c_int), ("bgc", Npzd)]
+                ("cut_scope", ctypes.c_int), ("bgc", Npzd),
+                ("open_boundary", ctypes.POINTER(ctypes.c_ubyte)), ("boundary_value", _dp),
+                ("has_boundary_value", ctypes.POINTER(ctypes.c_int))]
 
 
 class PelStats(ctypes.Structure):
@@ -161,7 +163,12 @@ def pel_exp(x: float) -> float:
 class PelOracle:
     """Keeps the numpy arrays behind an orc_pel alive."""
 
-    def __init__(self, pcs: PelColumnSet, cut_scope: int = 0):
+    def __init__(self, pcs: PelColumnSet, cut_scope: int = 0, open_boundary=None,
+                 boundary_value=None):
+        """open_boundary [ncol] (nonzero: an open-boundary column) and
+        boundary_value [ntr][ncol] with NaN rows for tracers without a
+        <name>_boundary_value_hz field (fabm_pelagic_component.F90
+        :2115-2155); None: no open boundary."""
         self.pcs = pcs
         f = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
         self._keep = dict(
@@ -182,6 +189,14 @@ class PelOracle:
         m.max_attempts = int(pcs.max_attempts)
         m.cut_scope = cut_scope
         m.bgc = npzd_struct(pcs.npzd)
+        if open_boundary is not None:
+            bv = np.ascontiguousarray(boundary_value, dtype=np.float64)
+            has = np.ascontiguousarray(~np.isnan(bv).all(axis=1), dtype=np.int32)
+            ob = np.ascontiguousarray(np.asarray(open_boundary) != 0, dtype=np.uint8)
+            k.update(ob=ob, bv=np.nan_to_num(bv), has=has)
+            m.open_boundary = k["ob"].ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte))
+            m.boundary_value = _ptr(k["bv"])
+            m.has_boundary_value = k["has"].ctypes.data_as(ctypes.POINTER(ctypes.c_int))
         self.m = m
 
     def light(self, conc: np.ndarray) -> np.ndarray:

@@ -216,6 +216,41 @@ def test_workload_is_seeded_and_column_addressable():
     assert 0.1 < 1 - a.water_columns() / a.ncol < 0.35
 
 
+def test_open_boundary_values_in_the_oracle(po):
+    """The Run's vertically homogeneous boundary values
+    (fabm_pelagic_component.F90:2115-2155): an open-boundary column takes the
+    value of every tracer that has one after each internal step's bottom
+    fluxes, before the surface fluxes and the clip; other columns, and
+    tracers without a value, are stepped as without boundaries."""
+    pcs = small(32, seed=4)
+    assert pcs.soil_flux is None and pcs.surface_flux is not None
+    water = np.flatnonzero(pcs.water().all(axis=0))
+    obc = water[[0, 3, 7]]
+    ob = np.zeros(pcs.ncol, dtype=np.int32)
+    ob[obc] = 1
+    bv = np.full((4, pcs.ncol), np.nan)
+    bv[0], bv[3] = 7.5, 0.25
+    for cut in (0, 1):
+        ref = pcs.conc.copy()
+        assert po.PelOracle(pcs, cut_scope=cut).run(ref, nthreads=1)[0] == 0
+        got = pcs.conc.copy()
+        assert po.PelOracle(pcs, cut_scope=cut, open_boundary=ob,
+                            boundary_value=bv).run(got, nthreads=1)[0] == 0
+        rest = np.setdiff1d(np.arange(pcs.ncol), obc)
+        if cut == 0:    # per-cell cuts: the other columns do not see them
+            np.testing.assert_array_equal(got[:, :, rest], ref[:, :, rest])
+        K = pcs.knum
+        top = K - 1
+        h = pcs.dt if pcs.t_couple % pcs.dt == 0 else pcs.t_couple % pcs.dt
+        for c in obc:
+            np.testing.assert_array_equal(got[0, :top, c], 7.5)
+            np.testing.assert_array_equal(got[3, :top, c], 0.25)
+            ht = pcs.layer_height[top, c]
+            assert got[0, top, c] == 7.5 + pcs.surface_flux[0, c] * h / ht
+            assert got[3, top, c] == 0.25 + pcs.surface_flux[3, c] * h / ht
+            assert not np.array_equal(got[1, :, c], pcs.conc[1, :, c])
+
+
 # ---------------------------------------------------------------- GPU
 
 def gpu_run(pcs, precision, cut=pelagic.PEL_CUT_PER_CELL, nruns=1, method=None):
