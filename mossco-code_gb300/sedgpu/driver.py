@@ -28,7 +28,8 @@ from .model import (ADAPTIVE_EULER, BGC_DEFAULTS, EULER, NTR, RUNGE_KUTTA_4,
 
 __all__ = ["TypeSed", "SedGrid", "init_grid", "initialize",
            "init_concentrations", "update_porosity", "ode_solver", "get_rhs", "update_min_dt",
-           "EULER", "RUNGE_KUTTA_4", "ADAPTIVE_EULER", "RUNGE_KUTTA_4_38"]
+           "EULER", "RUNGE_KUTTA_4", "ADAPTIVE_EULER", "RUNGE_KUTTA_4_38",
+           "SED_CUT_GLOBAL", "SED_CUT_PER_COLUMN"]
 
 
 @dataclasses.dataclass
