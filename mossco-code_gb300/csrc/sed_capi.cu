@@ -633,7 +633,6 @@ int ode_solver_pipelined(sed_handle* h, double* conc, double dt, int method) {
   if (rc) return rc;
   Params<real> p = make_params<real>(h->prm);
   set_clock(p, dt, h->prm.dt_min);
-  const bool bc4 = h->prm.bcup_particulate == 4;
   const int kind = method == SED_ADAPTIVE_EULER ? KIND_ADAPT : KIND_FIXED;
   const size_t pitch = (size_t)h->ncol * sizeof(double);
   const size_t rows = (size_t)NTR * h->kmax;
