@@ -36,9 +36,13 @@ extern "C" {
  *   orders, so these concentrations carry sinking_factor*fac_env*detN and
  *   their velocities keep what the fields held (velocity_in, or 0 as the
  *   sediment component initialises them, fabm_sediment_component.F90:1180).
+ *   Likewise the nitrate block (:1863-1935) looks the nitrate field up but
+ *   writes through the ammonium field's pointer, so ammonium takes the
+ *   nitrate value and the nitrate field is not written: its row keeps the
+ *   sediment handle's previous boundary (present_out[7] = 0).
  * CPL_AS_NAMED: each formula into the field its comment names: the C:N
  *   split into the concentrations, sinking_factor*fac_env*detN into the
- *   z-velocities. */
+ *   z-velocities, ammonium and nitrate into their own fields. */
 #define CPL_AS_RUN 0
 #define CPL_AS_NAMED 1
 

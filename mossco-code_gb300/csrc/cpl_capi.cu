@@ -20,156 +20,54 @@
 
 #include "../../include/mossco_cpl.h"
 #include "cpl_internal.h"
+#include "cpl_map.cuh"
 
 namespace {
 
-constexpr int NTR = SED_NTR;
-constexpr int NPART = 6;   // particulate tracers lead the sediment's order
-// sediment tracer rows (sed_tracer_name)
-constexpr int kLabC = 0, kSemC = 1, kLabN = 2, kSemN = 3, kLabP = 4, kOxy = 6, kNit = 7,
-              kAmm = 8, kOdu = 9, kPho = 10;
+using namespace cplmap;
 
-// Per-launch constants are formed on the host in IEEE double, with the
-// same operations and rounding the Fortran expressions give them; the
-// kernel keeps only the per-column arithmetic (GB300's FP64 rate is a small
-// fraction of its FP32 rate, and the FP64 divisions bound this kernel).
-struct Args {
-  const void* state;
+// Device buffers of one forward launch
+struct ForwardBufs {
+  const void* state;   // the pelagic state [PEL_NTR][K][ncol]
   int ncol, K;
-  int detN, detC, detP, din, nit, amm, oxy, odu;
-  double sf, ncl, ncs, cN, cP, htke, crit;
-  double hsd2;        // half_sedimentation_depth**2
-  double sfmin_sf;    // sinking_factor_min/sinking_factor
-  double c16N;        // 1.0d0/16.0d0 * convertN
-  double c05N;        // convertN*0.5d0
-  int as_named;
-  int crit_on;        // detC present and 1e-3 < critical_detritus < 9e9
-  const double* depth;  // null: no water depth, or half_sedimentation_depth <= 1e-3
-  const double* tke;    // null: no turbulence field, or half_sedimentation_tke >= 9e9
-  double* surface;      // [NTR][ncol]
+  const double* depth;  // [ncol] when a.use_depth
+  const double* tke;    // [ncol] when a.use_tke
+  double* surface;      // the sediment's staging rows [NTR][ncol]
   double* velocity;     // [NTR][ncol]
 };
 
-// Fortran max(0.0, x) of the connector's oxygen split (:823-844)
-__device__ __forceinline__ double pos(double x) { return x > 0.0 ? x : 0.0; }
-
 template <typename real>
-__global__ void k_pelagic_soil(Args a) {
-  const real* st = static_cast<const real*>(a.state);
-  const size_t layer = (size_t)a.K * a.ncol;  // one tracer's block
-  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < a.ncol;
+__global__ void k_pelagic_soil(Forward a, ForwardBufs b) {
+  const real* st = static_cast<const real*>(b.state);
+  const size_t layer = (size_t)b.K * b.ncol;  // one tracer's block
+  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < b.ncol;
        col += gridDim.x * blockDim.x) {
     auto B = [&](int n) { return (double)st[(size_t)n * layer + col]; };
-    double S[NTR];
-    for (int n = 0; n < NTR; n++) S[n] = 0.0;
-    double* V = a.velocity;
-    // ---- detritus (:1018-1236 factors, :1243-1646 fields)
-    if (a.detN >= 0 || a.detP >= 0) {
-      double fenv = 1.0;
-      if (a.depth) {   // 1.0 * d**2 is d**2 exactly
-        const double d2 = a.depth[col] * a.depth[col];
-        fenv = d2 / (d2 + a.hsd2);
-      }
-      if (a.tke) fenv = fenv * a.htke / (a.tke[col] + a.htke);
-      fenv = fenv + a.sfmin_sf;
-      if (a.crit_on) {
-        const double t = B(a.detC) / a.crit;
-        const double t2 = t * t;
-        fenv = fenv * 1.0 / (1.0 + t2 * t2);
-      }
-      const double w = a.sf * fenv;
-      if (a.detN >= 0) {
-        const double N = B(a.detN);
-        if (a.as_named) {
-          double CN = 106.0 / 16.0;
-          if (a.detC >= 0) CN = B(a.detC) / ((double)1e-5f + N);
-          double fl = (1.0 - a.ncs * CN) / (a.ncl - a.ncs);
-          double rl = fl * a.ncl;
-          if (fl > CN) { fl = CN; rl = 1.0; }
-          if (fl < 0.0) { fl = 0.0; rl = 0.0; }
-          const double fs = CN - fl;
-          const double rs = 1.0 - rl;
-          S[kLabC] = fl * a.cN * N;
-          S[kSemC] = fs * a.cN * N;
-          S[kLabN] = rl * a.cN * N;
-          S[kSemN] = rs * a.cN * N;
-          for (int n = kLabC; n <= kSemN; n++) V[(size_t)n * a.ncol + col] = w * N;
-        } else {
-          for (int n = kLabC; n <= kSemN; n++) S[n] = w * N;
-        }
-        S[kLabP] = a.c16N * N;
-        V[(size_t)kLabP * a.ncol + col] = w * N;
-      }
-      if (a.detP >= 0) S[kLabP] = B(a.detP);
-    }
-    // ---- oxygen and its deficit (:801-866)
-    if (a.oxy >= 0 && a.odu >= 0) {
-      S[kOxy] = B(a.oxy);
-      S[kOdu] = B(a.odu);
-    } else if (a.odu >= 0) {
-      const double x = B(a.odu);
-      S[kOxy] = pos(-x);
-      S[kOdu] = pos(x);
-    } else if (a.oxy >= 0) {
-      S[kOxy] = B(a.oxy);
-    }
-    // ---- dissolved nitrogen and phosphate (:1648-2110)
-    const bool hN = a.nit >= 0, hA = a.amm >= 0, hD = a.din >= 0;
-    const double Nt = hN ? B(a.nit) : 0.0;
-    const double A = hA ? B(a.amm) : 0.0;
-    const double D = hD ? B(a.din) : 0.0;
-    S[kAmm] = hA ? a.cN * A
-            : (hD && hN) ? a.cN * (D - Nt)
-            : hD ? a.c05N * D
-            : a.cN * Nt;
-    S[kNit] = hN ? a.cN * Nt
-            : (hA && hD) ? a.cN * (D - A)
-            : hD ? a.c05N * D
-            : a.cN * A;
-    const double din = hD ? D : (hA && hN) ? Nt + A : hA ? 2 * A : 2 * Nt;
-    S[kPho] = a.cP * (a.c16N * din);
-    for (int n = 0; n < NTR; n++) a.surface[(size_t)n * a.ncol + col] = S[n];
+    const ForwardOut o = pelagic_soil_column(a, B, a.use_depth ? b.depth[col] : 0.0,
+                                             a.use_tke ? b.tke[col] : 0.0);
+    for (int n = 0; n < NTR; n++) b.surface[(size_t)n * b.ncol + col] = o.S[n];
+    for (int n = 0; n < NPART; n++)
+      if ((o.vrows >> n) & 1u) b.velocity[(size_t)n * b.ncol + col] = o.w;
   }
 }
 
 // ---- the reverse direction: soil upward fluxes into the pelagic bottom
 // fluxes (soil_pelagic_connector.F90:179-965)
 
-struct SoilArgs {
+struct ReverseBufs {
   const double* fluxes;  // the sediment's [NTR][ncol], downward positive
   void* bfl;             // the pelagic handle's [PEL_NTR][ncol], its precision
   int ncol;
-  int nit, amm, din, dip, oxy, odu, detN, detC, detP;  // pelagic rows, -1 absent
-  double cN, cP;
-  double dinc, dipc;     // dinflux_const/(86400.0*365.0), dipflux_const/(...)
 };
 
 template <typename real>
-__global__ void k_soil_pelagic(SoilArgs a) {
-  real* b = static_cast<real*>(a.bfl);
-  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < a.ncol;
+__global__ void k_soil_pelagic(Reverse a, ReverseBufs b) {
+  real* out = static_cast<real*>(b.bfl);
+  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < b.ncol;
        col += gridDim.x * blockDim.x) {
-    // the soil's export: upward flux = -fluxes(:,:,n) (:1808-1815)
-    auto U = [&](int n) { return -a.fluxes[(size_t)n * a.ncol + col]; };
-    auto W = [&](int row, double v) { b[(size_t)row * a.ncol + col] = (real)v; };
-    // each soil flux is read only when a field that needs it is present
-    if (a.nit >= 0) W(a.nit, U(kNit));                          // :352-356
-    if (a.amm >= 0) W(a.amm, a.cN * U(kAmm));                   // :408-412
-    if (a.din >= 0) W(a.din, (U(kAmm) + U(kNit) + a.dinc) * a.cN);  // :467-473
-    if (a.dip >= 0) W(a.dip, a.cP * (U(kPho) + a.dipc));        // :528-534
-    if (a.odu >= 0 && a.oxy >= 0) {                             // :643-667
-      W(a.odu, U(kOdu));
-      W(a.oxy, U(kOxy));
-    } else if (a.odu >= 0) {
-      W(a.odu, U(kOdu) - U(kOxy));
-    } else if (a.oxy >= 0) {
-      W(a.oxy, U(kOxy) - U(kOdu));
-    }
-    // detritus: zero, then every soil flux the Run's pattern matches, in
-    // ESMF's alphabetical item order (:734-960)
-    if (a.detN >= 0) W(a.detN, 0.0 + U(kLabN) + U(kSemN));
-    if (a.detC >= 0) W(a.detC, 0.0 + U(kLabC) + U(kSemC));
-    if (a.detP >= 0) W(a.detP, 0.0);
+    auto U = [&](int n) { return -b.fluxes[(size_t)n * b.ncol + col]; };
+    auto W = [&](int row, double v) { out[(size_t)row * b.ncol + col] = (real)v; };
+    soil_pelagic_column(a, U, W);
   }
 }
 
@@ -297,18 +195,8 @@ int cpl_soil_pelagic(sed_handle* sed, pel_handle* pel, const cpl_soil_params* p,
   if (ev) cudaEventDestroy(ev);
   Timing tm;
   if (stats) tm.init(&e, pst);
-  SoilArgs a{};
-  a.fluxes = fl;
-  a.bfl = bfl;
-  a.ncol = s.ncol;
-  a.nit = f->nitrate; a.amm = f->ammonium; a.din = f->din; a.dip = f->dip;
-  a.oxy = f->oxygen; a.odu = f->odu; a.detN = f->detN; a.detC = f->detC; a.detP = f->detP;
-  a.cN = p->convertN;
-  a.cP = p->convertP;
-  // (86400.0*365.0) is a default-real product, 31536000 exactly
-  const double year = (double)(86400.0f * 365.0f);
-  a.dinc = p->dinflux_const / year;
-  a.dipc = p->dipflux_const / year;
+  const Reverse a = make_reverse(p, f);
+  ReverseBufs rb{fl, bfl, s.ncol};
   const int threads = 256;
   long long blocks = ((long long)nc + threads - 1) / threads;
   const long long cap = (long long)(s.sms > 0 ? s.sms : 1) * 8;
@@ -317,9 +205,9 @@ int cpl_soil_pelagic(sed_handle* sed, pel_handle* pel, const cpl_soil_params* p,
   tm.mark(1);
   if (e == cudaSuccess) {
     if (fp64)
-      k_soil_pelagic<double><<<(int)blocks, threads, 0, pst>>>(a);
+      k_soil_pelagic<double><<<(int)blocks, threads, 0, pst>>>(a, rb);
     else
-      k_soil_pelagic<float><<<(int)blocks, threads, 0, pst>>>(a);
+      k_soil_pelagic<float><<<(int)blocks, threads, 0, pst>>>(a, rb);
     e = cudaGetLastError();
   }
   tm.mark(2);
@@ -418,38 +306,17 @@ int cpl_pelagic_soil(pel_handle* pel, sed_handle* sed, const cpl_params* p,
     std::string m = std::string("coupling copies: ") + cudaGetErrorString(e);
     return cpl::sed_fail(sed, SED_E_CUDA, m.c_str());
   }
-  Args a{};
-  a.state = v.state;
-  a.ncol = s.ncol;
-  a.K = v.K;
-  a.detN = f->detN; a.detC = f->detC; a.detP = f->detP; a.din = f->din;
-  a.nit = f->nitrate; a.amm = f->ammonium; a.oxy = f->oxygen; a.odu = f->odu;
-  a.sf = p->sinking_factor;
-  a.ncl = p->NC_ldet; a.ncs = p->NC_sdet; a.cN = p->convertN; a.cP = p->convertP;
-  a.htke = p->half_sedimentation_tke;
-  a.crit = p->critical_detritus;
-  a.hsd2 = p->half_sedimentation_depth * p->half_sedimentation_depth;
-  a.sfmin_sf = p->sinking_factor_min / p->sinking_factor;
-  a.c16N = 1.0 / 16.0 * p->convertN;
-  a.c05N = p->convertN * 0.5;
-  a.as_named = p->mode == CPL_AS_NAMED;
-  // the Run's guards on the namelist values (:1150, :1181, :1215), with
-  // its default-real literals
-  a.crit_on = f->detC >= 0 && p->critical_detritus > (double)1e-3f &&
-              p->critical_detritus < (double)9e9f;
-  a.depth = water_depth && p->half_sedimentation_depth > (double)1e-3f ? d_depth : nullptr;
-  a.tke = tke && p->half_sedimentation_tke < (double)9e9f ? d_tke : nullptr;
-  a.surface = s.surface;
-  a.velocity = s.velocity;
+  const Forward a = make_forward(p, f, water_depth != nullptr, tke != nullptr);
+  ForwardBufs fb{v.state, s.ncol, v.K, d_depth, d_tke, s.surface, s.velocity};
   const int threads = 256;
   long long blocks = ((long long)nc + threads - 1) / threads;
   const long long cap = (long long)(s.sms > 0 ? s.sms : 1) * 8;
   if (blocks > cap) blocks = cap;
   tm.mark(1);
   if (v.fp64)
-    k_pelagic_soil<double><<<(int)blocks, threads, 0, s.stream>>>(a);
+    k_pelagic_soil<double><<<(int)blocks, threads, 0, s.stream>>>(a, fb);
   else
-    k_pelagic_soil<float><<<(int)blocks, threads, 0, s.stream>>>(a);
+    k_pelagic_soil<float><<<(int)blocks, threads, 0, s.stream>>>(a, fb);
   e = cudaGetLastError();
   tm.mark(2);
   if (e != cudaSuccess) {
@@ -457,12 +324,7 @@ int cpl_pelagic_soil(pel_handle* pel, sed_handle* sed, const cpl_params* p,
     return cpl::sed_fail(sed, SED_E_CUDA, m.c_str());
   }
   cpl::sed_count_launch(sed);
-  unsigned mask = (1u << kNit) | (1u << kAmm) | (1u << kPho);
-  if (f->detN >= 0) mask |= (1u << kLabC) | (1u << kSemC) | (1u << kLabN) | (1u << kSemN) |
-                           (1u << kLabP);
-  if (f->detP >= 0) mask |= 1u << kLabP;
-  if (f->oxygen >= 0 || f->odu >= 0) mask |= 1u << kOxy;
-  if (f->odu >= 0) mask |= 1u << kOdu;
+  const unsigned mask = forward_rows(a);
   const int before = cpl::sed_launches(sed);
   if (int rc = cpl::sed_assemble_staged(sed, mask)) return rc;
   const int assembly = cpl::sed_launches(sed) - before;

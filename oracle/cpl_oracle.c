@@ -161,14 +161,20 @@ int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
       else v = p->convertN * B(f->nitrate);
       ROW(surface, AM)[i] = v;
     }
-    /* nitrate, :1863-1985 */
-    for (i = 0; i < ncol; i++) {
-      double v;
-      if (hN) v = p->convertN * B(f->nitrate);
-      else if (hA && hD) v = p->convertN * (B(f->din) - B(f->ammonium));
-      else if (hD) v = p->convertN * 0.5 * B(f->din);
-      else v = p->convertN * B(f->ammonium);
-      ROW(surface, NI)[i] = v;
+    /* nitrate, :1863-1935: the block looks the nitrate field up (:1863)
+     * but writes through fieldList(1) (rank 1, :1872) or farrayPtr2 (rank
+     * 2, :1924), both still the ammonium field of :1766-1806; so the Run
+     * as written overwrites ammonium and leaves the nitrate field alone */
+    {
+      double *dst = p->as_named ? ROW(surface, NI) : ROW(surface, AM);
+      for (i = 0; i < ncol; i++) {
+        double v;
+        if (hN) v = p->convertN * B(f->nitrate);
+        else if (hA && hD) v = p->convertN * (B(f->din) - B(f->ammonium));
+        else if (hD) v = p->convertN * 0.5 * B(f->din);
+        else v = p->convertN * B(f->ammonium);
+        dst[i] = v;
+      }
     }
     /* phosphate from DIN (a DIP field is overwritten, not read), :1988-2110 */
     for (i = 0; i < ncol; i++) {
@@ -181,7 +187,8 @@ int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
       const double dip = 1.0 / 16.0 * p->convertN * din[i];
       ROW(surface, PH)[i] = p->convertP * dip;
     }
-    present[AM] = present[NI] = present[PH] = 1;
+    present[AM] = present[PH] = 1;
+    if (p->as_named) present[NI] = 1;
   }
 #undef B
 #undef ROW

@@ -11,6 +11,7 @@ library's exports.  GPU tests check the device coupling bit for bit against
 the oracle for FP64 and FP32 pelagic state, after device-resident steps, and
 a coupled pelagic / soil loop against the same loop routed through the host.
 """
+import os
 import subprocess
 
 import numpy as np
@@ -95,7 +96,11 @@ def numpy_run(conc, fields, p, as_named, depth=None, tke=None, velocity_in=None)
     z = np.zeros(ncol)
     Nt, A, D = b.get("nitrate", z), b.get("ammonium", z), b.get("din", z)
     S[8] = (cN * A if hA else cN * (D - Nt) if hD and hN else cN * 0.5 * D if hD else cN * Nt)
-    S[7] = (cN * Nt if hN else cN * (D - A) if hA and hD else cN * 0.5 * D if hD else cN * A)
+    nit = (cN * Nt if hN else cN * (D - A) if hA and hD else cN * 0.5 * D if hD else cN * A)
+    if as_named:
+        S[7] = nit
+    else:        # the nitrate block writes through the ammonium field
+        S[8] = nit
     din = D if hD else Nt + A if hA and hN else 2 * A if hA else 2 * Nt
     S[10] = cP * (1.0 / 16.0 * cN * din)
     return S, V
@@ -164,7 +169,7 @@ def test_oracle_matches_numpy_restatement(po, fields, as_named):
         S2, V2 = numpy_run(conc, fields, p, as_named, d, t, vin)
         np.testing.assert_array_equal(S, S2)
         np.testing.assert_array_equal(V, V2)
-        assert present[7] == present[8] == present[10] == 1
+        assert present[8] == present[10] == 1 and present[7] == int(as_named)
         assert present[5] == 0
         assert present[0] == ("detN" in fields)
 
@@ -193,6 +198,15 @@ def test_oracle_run_as_written_overwrites_the_concentrations(po):
     np.testing.assert_array_equal(S[7], 0.5 * pcs.conc[0, 0])
     np.testing.assert_array_equal(S[8], S[7])
     np.testing.assert_array_equal(S[10], 1.0 / 16.0 * pcs.conc[0, 0])
+    # as written, the nitrate value lands in the ammonium field and the
+    # nitrate field is not written (pelagic_soil_connector.F90:1863-1935)
+    rc, S, V, present = po.cpl_run(pcs.conc, dict(din=0, nitrate=1), p, False)
+    np.testing.assert_array_equal(S[8], pcs.conc[1, 0])
+    assert not S[7].any() and present[7] == 0 and present[8] == 1
+    rc, S, V, present = po.cpl_run(pcs.conc, dict(din=0, nitrate=1), p, True)
+    np.testing.assert_array_equal(S[7], pcs.conc[1, 0])
+    np.testing.assert_array_equal(S[8], pcs.conc[0, 0] - pcs.conc[1, 0])
+    assert present[7] == present[8] == 1
 
 
 def test_oracle_without_nitrogen_is_not_found(po):
@@ -261,6 +275,99 @@ def test_soil_oracle_matches_numpy_restatement(po, fields):
     for name, row in fields.items():
         assert present[row] == 1, name
     assert present.sum() == len(fields)
+
+
+HARNESS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "cpl_map_harness.cu")
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    """The kernels' per-column functions (csrc/cpl_map.cuh) compiled for the
+    host with nvcc, as tests/cpl_map_harness.cu drives them."""
+    exe = tmp_path_factory.mktemp("cplmap") / "harness"
+    r = subprocess.run([build.nvcc(), *build.ARCH, "-std=c++17", "-O2", "-Xcompiler",
+                        "-ffp-contract=off", "-I", build.CSRC, HARNESS, "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return str(exe)
+
+
+def _hex(values):
+    return " ".join(float(v).hex() for v in np.ravel(values))
+
+
+def _fields_line(d):
+    return " ".join(str(int(d.get(n, -1))) for n in coupling.FIELD_NAMES)
+
+
+@pytest.mark.parametrize("as_named", [False, True])
+def test_kernel_arithmetic_on_the_host_matches_the_oracle(po, harness, as_named):
+    """The forward kernel's per-column function, run on the host, equals the
+    connector oracle bit for bit over every field table, with and without
+    water depth and turbulence."""
+    pcs = pel_case(40, seed=5)
+    conc = pcs.conc.copy()
+    rng = np.random.default_rng(8)
+    conc[2, 0] *= rng.uniform(0.0, 40.0, conc.shape[2])
+    conc[1, 0] -= 1.5
+    ncol = conc.shape[2]
+    depth = rng.uniform(0.02, 40.0, ncol)
+    tke = rng.uniform(0.0, 3e3, ncol)
+    vin = rng.uniform(-1e-4, 0.0, (6, ncol))
+    p = po.cpl_defaults()
+    p.update(convertN=1.1, convertP=0.9)
+    cases, refs = [], []
+    for fields in FIELD_SETS:
+        for d, t in ((None, None), (depth, tke)):
+            lines = ["F", _hex([p[n] for n in coupling.PARAM_NAMES]) + f" {int(as_named)}",
+                     _fields_line(fields), f"{int(d is not None)} {int(t is not None)} {ncol}"]
+            for c in range(ncol):
+                lines.append(_hex(list(conc[:, 0, c]) + [0.0 if d is None else d[c],
+                                                          0.0 if t is None else t[c]]))
+            cases.append("\n".join(lines))
+            refs.append(po.cpl_run(conc, fields, p, as_named, d, t, vin))
+    out = subprocess.run([harness], input="\n".join(cases) + "\n", capture_output=True,
+                         text=True, check=True).stdout.split("\n")
+    row = 0
+    for rc, S, V, present in refs:
+        assert rc == 0
+        for c in range(ncol):
+            tok = out[row].split()
+            row += 1
+            got = np.array([float.fromhex(x) for x in tok[:11]])
+            srows, w, vrows = int(tok[11]), float.fromhex(tok[12]), int(tok[13])
+            np.testing.assert_array_equal(got, S[:, c])
+            assert [int((srows >> n) & 1) for n in range(11)] == list(present)
+            v = vin[:, c].copy()
+            for n in range(6):
+                if (vrows >> n) & 1:
+                    v[n] = w
+            np.testing.assert_array_equal(v, V[:6, c])
+
+
+def test_reverse_kernel_arithmetic_on_the_host_matches_the_oracle(po, harness):
+    rng = np.random.default_rng(12)
+    ncol = 30
+    fluxes = rng.normal(0.0, 1e-5, (11, ncol))
+    bfl_in = rng.normal(0.0, 1e-6, (4, ncol))
+    p = po.cpl_soil_defaults()
+    p.update(convertN=1.3, convertP=0.7, dinflux_const=2.5)
+    cases, refs = [], []
+    for fields in SOIL_FIELD_SETS:
+        lines = ["R", _hex([p[n] for n in coupling.SOIL_PARAM_NAMES]), _fields_line(fields),
+                 str(ncol)]
+        for c in range(ncol):
+            lines.append(_hex(list(fluxes[:, c]) + list(bfl_in[:, c])))
+        cases.append("\n".join(lines))
+        refs.append(po.cpl_soil_run(fluxes, fields, p, bfl_in)[0])
+    out = subprocess.run([harness], input="\n".join(cases) + "\n", capture_output=True,
+                         text=True, check=True).stdout.split("\n")
+    row = 0
+    for ref in refs:
+        for c in range(ncol):
+            got = [float.fromhex(x) for x in out[row].split()]
+            row += 1
+            np.testing.assert_array_equal(got, ref[:, c])
 
 
 # ---------------------------------------------------------------- GPU
