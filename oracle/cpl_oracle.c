@@ -28,6 +28,14 @@
 
 enum { LC = 0, SC = 1, LN = 2, SN = 3, LP = 4, OX = 6, NI = 7, AM = 8, OD = 9, PH = 10 };
 
+/* Every column is independent: large grids split each whole-array loop over
+ * the host threads (elementwise, so the result does not depend on them). */
+#ifdef _OPENMP
+#define PFOR _Pragma("omp parallel for schedule(static) if(ncol > 65536)")
+#else
+#define PFOR
+#endif
+
 void orc_cpl_defaults(orc_cpl *p) {
   /* :38-45 */
   p->sinking_factor = 0.3;
@@ -64,53 +72,71 @@ int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
    * only; the oxygen-only branch of the reference reads the deficit's
    * pointers, which are not associated then: here oxygen alone is copied) */
   if (f->oxygen >= 0 && f->odu >= 0) {
+    PFOR
     for (i = 0; i < ncol; i++) ROW(surface, OX)[i] = B(f->oxygen);
+    PFOR
     for (i = 0; i < ncol; i++) ROW(surface, OD)[i] = B(f->odu);
     present[OX] = present[OD] = 1;
   } else if (f->odu >= 0) {
+    PFOR
     for (i = 0; i < ncol; i++) {
       const double x = -B(f->odu);
       ROW(surface, OX)[i] = x > 0.0 ? x : 0.0;
     }
+    PFOR
     for (i = 0; i < ncol; i++) {
       const double x = B(f->odu);
       ROW(surface, OD)[i] = x > 0.0 ? x : 0.0;
     }
     present[OX] = present[OD] = 1;
   } else if (f->oxygen >= 0) {
+    PFOR
     for (i = 0; i < ncol; i++) ROW(surface, OX)[i] = B(f->oxygen);
     present[OX] = 1;
   }
 
   /* C:N of the detritus, :1018-1072 */
+  PFOR
   for (i = 0; i < ncol; i++) CN[i] = 106.0 / 16.0;
   if (f->detN >= 0 && f->detC >= 0)
+    PFOR
     for (i = 0; i < ncol; i++) CN[i] = B(f->detC) / (one_e5 + B(f->detN));
 
   /* labile / semilabile factors, :1074-1121 */
+  PFOR
   for (i = 0; i < ncol; i++) fl[i] = (1.0 - p->NC_sdet * CN[i]) / (p->NC_ldet - p->NC_sdet);
+  PFOR
   for (i = 0; i < ncol; i++) rl[i] = fl[i] * p->NC_ldet;
+  PFOR
   for (i = 0; i < ncol; i++)
     if (fl[i] > CN[i]) { fl[i] = CN[i]; rl[i] = 1.0; }
+  PFOR
   for (i = 0; i < ncol; i++)
     if (fl[i] < 0.0) { fl[i] = 0.0; rl[i] = 0.0; }
+  PFOR
   for (i = 0; i < ncol; i++) fs[i] = CN[i] - fl[i];
+  PFOR
   for (i = 0; i < ncol; i++) rs[i] = 1.0 - rl[i];
+  PFOR
   for (i = 0; i < ncol; i++) fe[i] = 1.0;
 
   /* water depth, :1126-1160 */
   if (depth && p->half_sedimentation_depth > one_e3)
+    PFOR
     for (i = 0; i < ncol; i++)
       fe[i] = fe[i] * (depth[i] * depth[i]) /
               (depth[i] * depth[i] + p->half_sedimentation_depth * p->half_sedimentation_depth);
   /* turbulence, :1164-1198 */
   if (tke && p->half_sedimentation_tke < nine_e9)
+    PFOR
     for (i = 0; i < ncol; i++)
       fe[i] = fe[i] * p->half_sedimentation_tke / (tke[i] + p->half_sedimentation_tke);
   /* minimum sedimentation, :1202-1210 */
+  PFOR
   for (i = 0; i < ncol; i++) fe[i] = fe[i] + p->sinking_factor_min / p->sinking_factor;
   /* detritus carbon above critical_detritus, :1213-1236 */
   if (f->detC >= 0 && p->critical_detritus > one_e3 && p->critical_detritus < nine_e9)
+    PFOR
     for (i = 0; i < ncol; i++) {
       const double x = B(f->detC) / p->critical_detritus;
       const double x2 = x * x;
@@ -127,22 +153,27 @@ int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
     int b;
     for (b = 0; b < 4; b++) {
       double *dst = ROW(surface, row[b]);
+      PFOR
       for (i = 0; i < ncol; i++) dst[i] = fac[b][i] * p->convertN * B(f->detN);
       dst = p->as_named ? ROW(velocity, row[b]) : ROW(surface, row[b]);
+      PFOR
       for (i = 0; i < ncol; i++) dst[i] = p->sinking_factor * fe[i] * B(f->detN);
       present[row[b]] = 1;
     }
   }
   /* phosphorus, :1492-1646 */
   if (f->detN >= 0) {
+    PFOR
     for (i = 0; i < ncol; i++) ROW(surface, LP)[i] = 1.0 / 16.0 * p->convertN * B(f->detN);
     present[LP] = 1;
   }
   if (f->detP >= 0) {
+    PFOR
     for (i = 0; i < ncol; i++) ROW(surface, LP)[i] = B(f->detP);
     present[LP] = 1;
   }
   if (f->detN >= 0)
+    PFOR
     for (i = 0; i < ncol; i++)
       ROW(velocity, LP)[i] = p->sinking_factor * fe[i] * B(f->detN);
 
@@ -153,6 +184,7 @@ int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
       free(CN); free(fl); free(rl); free(fs); free(rs); free(fe); free(din);
       return -1;
     }
+    PFOR
     for (i = 0; i < ncol; i++) {
       double v;
       if (hA) v = p->convertN * B(f->ammonium);
@@ -167,6 +199,7 @@ int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
      * as written overwrites ammonium and leaves the nitrate field alone */
     {
       double *dst = p->as_named ? ROW(surface, NI) : ROW(surface, AM);
+      PFOR
       for (i = 0; i < ncol; i++) {
         double v;
         if (hN) v = p->convertN * B(f->nitrate);
@@ -177,12 +210,14 @@ int orc_cpl_run(const orc_cpl *p, const orc_cpl_fields *f, const double *conc,
       }
     }
     /* phosphate from DIN (a DIP field is overwritten, not read), :1988-2110 */
+    PFOR
     for (i = 0; i < ncol; i++) {
       if (hD) din[i] = B(f->din);
       else if (hA && hN) din[i] = B(f->nitrate) + B(f->ammonium);
       else if (hA) din[i] = 2 * B(f->ammonium);
       else din[i] = 2 * B(f->nitrate);
     }
+    PFOR
     for (i = 0; i < ncol; i++) {
       const double dip = 1.0 / 16.0 * p->convertN * din[i];
       ROW(surface, PH)[i] = p->convertP * dip;
@@ -241,10 +276,12 @@ static void detritus_sum(const char *pattern, const double *fluxes, int ncol, do
   char item[96];
   for (n = 0; n < 11; n++) order[n] = n;
   qsort(order, 11, sizeof(int), by_name);
+  PFOR
   for (i = 0; i < ncol; i++) dst[i] = 0.0;
   for (n = 0; n < 11; n++) {
     snprintf(item, sizeof item, "%s_upward_flux_at_soil_surface", soil_names[order[n]]);
     if (!match_after_star(item, pattern)) continue;
+    PFOR
     for (i = 0; i < ncol; i++) dst[i] = dst[i] + -fluxes[(size_t)order[n] * ncol + i];
   }
 }
@@ -261,31 +298,39 @@ void orc_cpl_soil_run(const orc_cpl_soil *p, const orc_cpl_soil_fields *f,
 #define UP(r) (up + (size_t)(r) * ncol)
 #define ROW(r) (bfl + (size_t)(r) * ncol)
   if (f->nitrate >= 0) {  /* :352-356 */
+    PFOR
     for (i = 0; i < ncol; i++) ROW(f->nitrate)[i] = UP(NI)[i];
     present[f->nitrate] = 1;
   }
   if (f->ammonium >= 0) {  /* :408-412 */
+    PFOR
     for (i = 0; i < ncol; i++) ROW(f->ammonium)[i] = p->convertN * UP(AM)[i];
     present[f->ammonium] = 1;
   }
   if (f->din >= 0) {  /* :467-473 */
+    PFOR
     for (i = 0; i < ncol; i++)
       ROW(f->din)[i] = (UP(AM)[i] + UP(NI)[i] + p->dinflux_const / year) * p->convertN;
     present[f->din] = 1;
   }
   if (f->dip >= 0) {  /* :528-534 */
+    PFOR
     for (i = 0; i < ncol; i++)
       ROW(f->dip)[i] = p->convertP * (UP(PH)[i] + p->dipflux_const / year);
     present[f->dip] = 1;
   }
   if (f->odu >= 0 && f->oxygen >= 0) {  /* :643-667 */
+    PFOR
     for (i = 0; i < ncol; i++) ROW(f->odu)[i] = UP(OD)[i];
+    PFOR
     for (i = 0; i < ncol; i++) ROW(f->oxygen)[i] = UP(OX)[i];
     present[f->odu] = present[f->oxygen] = 1;
   } else if (f->odu >= 0) {
+    PFOR
     for (i = 0; i < ncol; i++) ROW(f->odu)[i] = UP(OD)[i] - UP(OX)[i];
     present[f->odu] = 1;
   } else if (f->oxygen >= 0) {
+    PFOR
     for (i = 0; i < ncol; i++) ROW(f->oxygen)[i] = UP(OX)[i] - UP(OD)[i];
     present[f->oxygen] = 1;
   }
