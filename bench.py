@@ -175,6 +175,31 @@ def cpu_window(workload: str, seed: int, warmup: int, steps: int, threads: int,
             "sample": sample, "seconds": secs}
 
 
+def host_cpu() -> dict:
+    """The host's CPU model (as /proc/cpuinfo names it) and core count."""
+    import platform
+    model = ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu part") and ":" in line:
+                    model = line.split(":", 1)[1].strip()
+                    if key == "model name":
+                        break
+    except OSError:
+        pass
+    return {"machine": platform.machine(), "model": model, "nproc": os.cpu_count() or 1}
+
+
+def cpu_context(workload: str, seed: int, warmup: int, steps: int, max_columns: int) -> dict:
+    """The host beside the all-core baseline, and the same window on one
+    core (about 5 s of work)."""
+    one = cpu_window(workload, seed, warmup, steps, 1, max_columns, target_s=5.0)
+    return {"host": host_cpu(),
+            "one_core": {"value": one["value"], "unit": one["unit"], "sample": one["sample"]}}
+
+
 def days(step0: int, step1: int, dt: float) -> str:
     return f"{step0 * dt / 86400.0:.3f}..{step1 * dt / 86400.0:.3f}"
 
@@ -200,7 +225,9 @@ def run_reference(args) -> None:
         "config": {"workload": args.workload, "tracers": NTR, "dt_s": full.dt,
                    "method": "adaptive_euler", "cut": "per_column",
                    "simulated_days_timed": days(args.warmup, args.warmup + steps, full.dt)},
-        "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "cpu_baseline": dict({k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                             **cpu_context(args.workload, args.seed, args.warmup, steps,
+                                           args.cpu_columns)),
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "note": ("reference algorithm as the FP64 C restatement on the host "
@@ -604,6 +631,7 @@ def run_gpu(args) -> None:
         cpu = cpu_window(args.workload, args.seed, args.warmup, steps, os.cpu_count() or 1,
                          args.cpu_columns)
         cpu.pop("seconds")
+        cpu.update(cpu_context(args.workload, args.seed, args.warmup, steps, args.cpu_columns))
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,

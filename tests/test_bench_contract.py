@@ -33,6 +33,10 @@ def test_reference_arm_sediment():
     line = run("--cpu-columns", "32")
     check(line)
     assert line["unit"] == "column-steps/s" and line["config"]["workload"] == "plain_gpu_256x256"
+    # the host beside the all-core figure, and the same window on one core
+    cb = line["cpu_baseline"]
+    assert cb["host"]["nproc"] >= 1 and cb["host"]["machine"]
+    assert cb["one_core"]["value"] > 0 and cb["one_core"]["unit"] == "column-steps/s"
 
 
 def test_reference_arm_pelagic():
