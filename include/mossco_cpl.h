@@ -109,7 +109,9 @@ int cpl_soil_default_params(cpl_soil_params *p);
  *   velocity_in  [SED_NTR][ncol] the z-velocity fields' contents before the
  *                call, or NULL (zeros); only particulate rows are read
  *   surface_out, velocity_out  [SED_NTR][ncol] the export fields after the
- *                call (host copies for inspection), or NULL
+ *                call (host copies for inspection), or NULL; surface rows
+ *                the Run does not write read 0, velocity rows velocity_in's
+ *                (non-particulate rows 0)
  *   present_out  [SED_NTR] 1 where the connector wrote the tracer's
  *                concentration field, or NULL
  *   stats        or NULL
