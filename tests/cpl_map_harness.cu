@@ -19,6 +19,19 @@
 
 using namespace cplmap;
 
+struct Bottom {
+  const double* b;
+  CPL_HD double operator()(int n) const { return b[n]; }
+};
+struct Up {
+  const double* fl;
+  CPL_HD double operator()(int n) const { return -fl[n]; }
+};
+struct Put {
+  double* out;
+  CPL_HD void operator()(int row, double v) const { out[row] = v; }
+};
+
 static int read_fields(cpl_fields* f) {
   return scanf("%d %d %d %d %d %d %d %d %d", &f->detN, &f->detC, &f->detP, &f->din,
                &f->nitrate, &f->ammonium, &f->oxygen, &f->odu, &f->dip) == 9;
@@ -38,7 +51,7 @@ static int forward() {
     double b[4], depth, tke;
     if (scanf("%lf %lf %lf %lf %lf %lf", &b[0], &b[1], &b[2], &b[3], &depth, &tke) != 6)
       return 1;
-    const ForwardOut o = pelagic_soil_column(a, [&](int n) { return b[n]; }, depth, tke);
+    const ForwardOut o = pelagic_soil_column(a, Bottom{b}, depth, tke);
     for (int n = 0; n < NTR; n++) printf("%a ", o.S[n]);
     printf("%u %a %u\n", o.srows, o.w, o.vrows);
   }
@@ -60,8 +73,7 @@ static int reverse() {
       if (scanf("%lf", &fl[n]) != 1) return 1;
     for (int n = 0; n < PEL_NTR; n++)
       if (scanf("%lf", &out[n]) != 1) return 1;
-    soil_pelagic_column(a, [&](int n) { return -fl[n]; },
-                        [&](int row, double v) { out[row] = v; });
+    soil_pelagic_column(a, Up{fl}, Put{out});
     for (int n = 0; n < PEL_NTR; n++) printf("%a ", out[n]);
     printf("\n");
   }
