@@ -42,7 +42,6 @@ extern "C" {
 #define SED_E_STATE (-5)        /* call order: grid / forcing / state missing */
 #define SED_E_NOMEM (-6)        /* device or pinned allocation failed */
 #define SED_E_NODEVICE (-7)     /* no CUDA device */
-#define SED_E_TIMEOUT (-8)      /* a bounded device wait gave up */
 #define SED_E_TOO_LARGE (-9)    /* grid exceeds the no-allocation scratch */
 
 /* Size of the device array behind sed_ode_solver_noalloc (64 MiB). */
@@ -303,11 +302,17 @@ int sed_autotune(sed_handle *h, double dt, int method, int flags,
  * and fluxes updated in place); p must ask for SED_FP32 state and
  * per-column cuts, and budgets are not computed.  A grid whose buffers do
  * not fit the array (about 4.7 KB per column at 30 layers, so ~14 000
- * columns) is rejected with SED_E_TOO_LARGE.  The first call on a device
- * looks up the array's device address; make that first call before any
- * stream capture.  All calls share the array, so calls that overlap on the
- * GPU (from several host threads) race; the work runs on the legacy
- * default stream and the call returns when it is done. */
+ * columns) is rejected with SED_E_TOO_LARGE.  The call runs the tile form
+ * of the column kernel on the array; its results equal sed_ode_solver's bit
+ * for bit.  Every call looks up the array's device address in the current
+ * context of p->device (the first call in a context loads the module; make
+ * that first call before any stream capture), so a cudaDeviceReset by the
+ * caller between calls is harmless.  All calls share the array, so calls
+ * that overlap on the GPU (from several host threads of one process) race.
+ * The work runs on the calling thread's per-thread default stream
+ * (cudaStreamPerThread), so it does not wait for other streams of the
+ * device, and the call returns when it is done.  After an error return the
+ * caller's conc and fluxes are unchanged. */
 int sed_ode_solver_noalloc(const sed_params *p, int inum, int jnum, int kmax,
                            const double *dz, const double *dzc,
                            const double *phi, const double *phi_i,

@@ -1881,7 +1881,6 @@ const char* sed_error_string(int code) {
     case SED_E_STATE: return "call order: grid, forcing or state missing";
     case SED_E_NOMEM: return "out of memory";
     case SED_E_NODEVICE: return "no CUDA device";
-    case SED_E_TIMEOUT: return "bounded device wait gave up";
     case SED_E_TOO_LARGE: return "grid exceeds the no-allocation scratch array";
     default: return "unknown error";
   }

@@ -4,26 +4,29 @@
 // Some callers cannot allocate device memory: a component whose host
 // framework owns the GPU's memory pool and forbids other allocators, or a
 // call site that cannot keep a solver handle (and the buffers it allocates)
-// alive between calls.  This entry point runs the same column kernel as
-// sed_ode_solver, but every device buffer it needs -- the staging of the
-// caller's FP64 arrays, the FP32 state, coefficients and forcing, the tile
-// work counter and the step statistics -- lives in one file-scope
-// __device__ array of SED_NOALLOC_SCRATCH_BYTES.  Every GPU that loads the
-// library holds that array until the process exits.
+// alive between calls.  This entry point runs the tile form of the column
+// kernel (k_column: 32- or 16-column tiles, 256 threads), with every device
+// buffer it needs -- the staging of the caller's FP64 arrays, the FP32 state,
+// coefficients and forcing, the tile work counter and the step statistics --
+// in one file-scope __device__ array of SED_NOALLOC_SCRATCH_BYTES.  Every GPU
+// that loads the library holds that array until the process exits.  The
+// per-column arithmetic is the one of every other FP32 kernel of the
+// library, so the results equal sed_ode_solver's bit for bit.
 //
 // The array's host-side name is only a stand-in: host code obtains its
-// device address with cudaGetSymbolAddress, once per device, with that
-// device current (done by the first call on the device), and passes that
-// address to the kernels.  All calls share the array and it keeps the last
-// call's contents; each call re-initialises what it reads (work counter,
-// statistics, staged inputs).  Calls that overlap on the GPU -- from several
-// host threads, or on one device from several processes' views of the same
-// library state -- race on the shared array.
+// device address with cudaGetSymbolAddress, with the call's device current,
+// and passes that address to the kernels.  Every call looks the address up
+// again (the runtime answers from its own table after the first call in a
+// context), so a context that was destroyed and created again -- a
+// cudaDeviceReset by the caller -- gets the array's new address.  All calls
+// share the array and it keeps the last call's contents; each call
+// re-initialises what it reads (work counter, statistics, staged inputs).
+// Calls that overlap on the GPU from several host threads of one process
+// race on the shared array.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstring>
-#include <mutex>
 
 #include "../../include/mossco_sed.h"
 #include "sed_launch.h"
@@ -34,10 +37,6 @@ using namespace sed;
 static __device__ __align__(256) unsigned char g_sed_noalloc_scratch[SED_NOALLOC_SCRATCH_BYTES];
 
 namespace {
-
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-unsigned char* g_scratch_addr[kMaxDevices];  // device address per device
 
 size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -143,20 +142,17 @@ extern "C" int sed_ode_solver_noalloc(const sed_params* p, int inum, int jnum,
     cudaGetLastError();
     return SED_E_NODEVICE;
   }
-  if (p->device < 0 || p->device >= ndev || p->device >= kMaxDevices) return SED_E_ARG;
+  if (p->device < 0 || p->device >= ndev) return SED_E_ARG;
   if (cudaSetDevice(p->device) != cudaSuccess) return SED_E_CUDA;
+  // the array's device address in the current context of this device
   unsigned char* base = nullptr;
   {
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[p->device]) {
-      void* addr = nullptr;
-      if (cudaGetSymbolAddress(&addr, g_sed_noalloc_scratch) != cudaSuccess || !addr) {
-        cudaGetLastError();
-        return SED_E_CUDA;
-      }
-      g_scratch_addr[p->device] = static_cast<unsigned char*>(addr);
+    void* addr = nullptr;
+    if (cudaGetSymbolAddress(&addr, g_sed_noalloc_scratch) != cudaSuccess || !addr) {
+      cudaGetLastError();
+      return SED_E_CUDA;
     }
-    base = g_scratch_addr[p->device];
+    base = static_cast<unsigned char*>(addr);
   }
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess)
@@ -165,7 +161,9 @@ extern "C" int sed_ode_solver_noalloc(const sed_params* p, int inum, int jnum,
   const int occ = column_blocks_per_sm<float>(tc, lpl, bc4, kind, 256, false);
   if (occ <= 0) return SED_E_CUDA;
 
-  cudaStream_t st = 0;
+  // the calling thread's default stream: ordered with this thread's other
+  // default-stream work, not with the device's other streams
+  cudaStream_t st = cudaStreamPerThread;
   int launches = 0;
   cudaError_t e = cudaSuccess;
   auto ok = [&](cudaError_t r) { if (e == cudaSuccess) e = r; return e == cudaSuccess; };
@@ -265,10 +263,13 @@ extern "C" int sed_ode_solver_noalloc(const sed_params* p, int inum, int jnum,
                                   slot_k, ncol, nslot, sms, st));
     launches += 2;
   }
-  ok(cudaMemcpyAsync(conc, stage, (size_t)NTR * cells * sizeof(double),
-                     cudaMemcpyDeviceToHost, st));
-  ok(cudaMemcpyAsync(fluxes, base + L.fluxes, (size_t)NTR * ncol * sizeof(double),
-                     cudaMemcpyDeviceToHost, st));
+  // the caller's arrays are written only when every step before succeeded
+  if (ok(cudaSuccess)) {
+    ok(cudaMemcpyAsync(conc, stage, (size_t)NTR * cells * sizeof(double),
+                       cudaMemcpyDeviceToHost, st));
+    ok(cudaMemcpyAsync(fluxes, base + L.fluxes, (size_t)NTR * ncol * sizeof(double),
+                       cudaMemcpyDeviceToHost, st));
+  }
   DevStats s{};
   ok(cudaMemcpyAsync(&s, base + L.stats, sizeof s, cudaMemcpyDeviceToHost, st));
   ok(cudaStreamSynchronize(st));

@@ -19,7 +19,7 @@ from .model import BGC_NAMES, NTR, ColumnSet
 
 SED_OK, SED_E_ARG, SED_E_NAN, SED_E_SUBSTEP_CAP = 0, -1, -2, -3
 SED_E_CUDA, SED_E_STATE, SED_E_NOMEM, SED_E_NODEVICE = -4, -5, -6, -7
-SED_E_TIMEOUT, SED_E_TOO_LARGE = -8, -9
+SED_E_TOO_LARGE = -9
 SED_FP32, SED_FP64 = 0, 1
 SED_CUT_PER_COLUMN, SED_CUT_GLOBAL = 0, 1
 SED_KMAX_LIMIT = 63

@@ -10,7 +10,7 @@ reference itself cannot be built (Fortran, FABM), so the state is the
 oracle's: it pins regressions of the oracle and of the FP64 device path to
 the reference's own example configuration.
 
-    python tests/golden/make_golden.py [path-to-reference-checkout]
+    python tests/golden/make_golden.py <path-to-reference-checkout>
 """
 import json
 import os
@@ -69,4 +69,6 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of the reference source tree>")
+    main(sys.argv[1])
