@@ -350,14 +350,38 @@ const char *sed_sur_last_error(const sed_surrogate *s);
  * c0[11] | mu_x[nin] | sd_x[nin] | mu_d[nout] | sd_d[nout], with nin =
  * 11 K + 13 and nout = 11 K for a grid of K layers. */
 int sed_sur_set_norm(sed_surrogate *s, const float *norm, int n);
-/* nsteps coupling steps with the surrogate proposing every column's state;
- * a column is accepted when its backward-Euler defect
- * max |C' - C - dt f(C')| / (|C'| + |C| + dt |f(C')| + res_atol) <= tol,
- * every other column is advanced by the plain adaptive solver.  FP32 state,
- * all active columns at kmax layers.  stats.surrogate_columns counts the
- * accepted column-steps. */
+/* nsteps coupling steps of the handle's device state with the surrogate
+ * (FP32 state, per-column cuts, every active column at kmax layers).  Each
+ * step runs:
+ *   1. the gate: every column's first adaptive attempt, the whole step at
+ *      once.  A column whose attempt is accepted is done, with exactly the
+ *      plain step's result (most columns, most steps); the others -- whose
+ *      plain step would take many substeps -- are listed;
+ *   2. the network's proposal for the listed columns;
+ *   3. the residual test of each proposal P with the plain right-hand side:
+ *      P is taken when dt |f(P)| <= tol (|P| + res_atol) in every cell (a
+ *      state the plain dynamics would move by at most tol of its value over
+ *      a step); NaN fails;
+ *   4. the plain adaptive solver on the listed columns whose proposal failed.
+ * With tol = 0 nothing is taken and the result equals sed_step's bit for
+ * bit.  stats.surrogate_columns counts the column-steps taken from the
+ * network; their attempts count 0 and their budgets are zero. */
 int sed_step_surrogate(sed_handle *h, sed_surrogate *s, double dt, int nsteps,
                        double tol, double res_atol, sed_stats *stats);
+/* Training rows from the plain solver: one plain adaptive coupling step of
+ * the handle's device state (FP32, per-column cuts, every active column at
+ * kmax layers), then a row for every column whose step took more than one
+ * attempt -- the columns step 1 of sed_step_surrogate hands to the network.
+ * Rows go to caller device arrays (FP32), starting at row *count:
+ *   x[row][0 .. 11 K)        log(max(C, 0) + c0[n]) before the step,
+ *                            tracer-major (n K + k)
+ *   x[row][11 K .. 11 K+13)  the column's 13 forcing rows
+ *   y[row][0 .. 11 K)        log(max(C', 0) + c0[n]) - the same before
+ * with row pitches pitch_x, pitch_y (floats).  Rows past capacity are
+ * dropped; *count returns min(rows so far, capacity). */
+int sed_sur_collect(sed_handle *h, const float *c0, double dt, float *x_dev,
+                    float *y_dev, int pitch_x, int pitch_y,
+                    long long capacity, long long *count, sed_stats *stats);
 void sed_sur_destroy(sed_surrogate *s);
 
 const char *sed_error_string(int code);

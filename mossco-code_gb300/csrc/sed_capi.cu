@@ -116,9 +116,12 @@ struct sed_handle {
       d_budget, d_nsub, d_queue, d_stats, d_flag, d_stage, d_bdys, d_fluxes,
       d_rhs, d_rhs_stage, d_grid, d_force64, d_prop, d_skip, d_xfeat, d_yhat, d_backup,
       d_col_slot, d_top, d_bcin, d_mindt;
+  // surrogate step: heavy-column slot list, its counter, hidden activations
+  DevBuf d_list, d_gate, d_act;
   std::vector<double> force64;  // host forcing rows (FP64 state)
   DevStats* h_stats = nullptr;  // pinned
   int* h_flag = nullptr;        // pinned
+  unsigned long long* h_count = nullptr;  // pinned
   // graph of one coupling step
   cudaGraphExec_t graph = nullptr;
   double graph_dt = -1.0;
@@ -898,6 +901,7 @@ sed_handle::~sed_handle() {
   }
   if (h_stats) cudaFreeHost(h_stats);
   if (h_flag) cudaFreeHost(h_flag);
+  if (h_count) cudaFreeHost(h_count);
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
   if (own_stream) cudaStreamDestroy(own_stream);
@@ -983,6 +987,8 @@ int sed_create(const sed_params* p, int inum, int jnum, int kmax, int ntr,
     CK(cudaEventCreate(&h->ev1), "event");
     CK(cudaHostAlloc((void**)&h->h_stats, sizeof(DevStats), cudaHostAllocDefault), "pinned stats");
     CK(cudaHostAlloc((void**)&h->h_flag, sizeof(int), cudaHostAllocDefault), "pinned flag");
+    CK(cudaHostAlloc((void**)&h->h_count, sizeof(unsigned long long), cudaHostAllocDefault),
+       "pinned counter");
     CK(h->d_queue.alloc(kQueues * sizeof(unsigned)), "queue");
     CK(h->d_stats.alloc(sizeof(DevStats)), "stats");
     CK(h->d_flag.alloc(sizeof(int)), "flag");
@@ -1314,6 +1320,29 @@ int sed_sur_set_norm(sed_surrogate* s, const float* norm, int n) {
   return SED_OK;
 }
 
+// The depth class holding every active column of a surrogate handle (all
+// active columns have kmax layers); -1 if the columns are not all there.
+static int surrogate_bin(sed_handle* h) {
+  for (int i = 0; i < h->nslot; i++)
+    if (h->slot_col[i] >= 0 && h->slot_k[i] != h->kmax) return -1;
+  const int b = h->kmax > 31 ? 1 : 0;
+  return h->bins[b].nslots > 0 ? b : -1;
+}
+
+// Warp-direct launch of one class's kernel over a's columns (a.ntiles of
+// them: the class's slot range, or a slot list).
+static cudaError_t launch_warp_columns(sed_handle* h, const ColumnArgs<float>& a,
+                                       const Params<float>& p, const Bin& bin, int kind) {
+  const bool bc4 = h->prm.bcup_particulate == 4;
+  const int threads = bin.threads;
+  const int occ = column_warp_blocks_per_sm<float>(
+      bin.lpl, bc4, kind == KIND_FIXED ? KIND_FIXED : KIND_ADAPT, threads, p.bio3 != 0);
+  const int warps = threads / 32;
+  const int blocks =
+      std::max(1, std::min(std::max(occ, 1) * h->sms, (a.ntiles + warps - 1) / warps));
+  return launch_column_warp<float>(a, p, bin.lpl, bc4, kind, blocks, threads, h->stream);
+}
+
 int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, double tol,
                        double res_atol, sed_stats* stats) {
   int rc = ready(h);
@@ -1322,84 +1351,145 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
   if (h->has_bgc) return h->fail(SED_E_STATE, "the surrogate has no per-column parameter sets");
   if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");
   if (h->fp64()) return h->fail(SED_E_ARG, "the surrogate step runs on FP32 state");
+  if (h->prm.cut_scope != SED_CUT_PER_COLUMN)
+    return h->fail(SED_E_ARG, "the surrogate step cuts substeps per column");
   if (s->device != h->device) return h->fail(SED_E_ARG, "surrogate on another device");
   const int K = h->kmax;
   if (s->nin != NTR * K + NFORCE || s->nout != NTR * K)
     return h->fail(SED_E_ARG, "surrogate sized for %d inputs / %d outputs, grid needs %d / %d",
                    s->nin, s->nout, NTR * K + NFORCE, NTR * K);
   if (!s->norm) return h->fail(SED_E_STATE, "sed_sur_set_norm has not been called");
-  for (int i = 0; i < h->nslot; i++)
-    if (h->slot_col[i] >= 0 && h->slot_k[i] != K)
-      return h->fail(SED_E_ARG, "the surrogate needs every active column at %d layers", K);
-  if (!(dt > 0.0) || nsteps < 0 || !(tol > 0.0) || !(res_atol >= 0.0))
+  const int b = surrogate_bin(h);
+  if (b < 0) return h->fail(SED_E_ARG, "the surrogate needs every active column at %d layers", K);
+  if (!(dt > 0.0) || nsteps < 0 || !(tol >= 0.0) || !(res_atol >= 0.0))
     return h->fail(SED_E_ARG, "bad dt, nsteps, tol or res_atol");
   CK(cudaSetDevice(h->device), "set device");
+  const Bin& bin = h->bins[b];
   const size_t ns = h->nslot;
-  const int rows = pad128(h->nslot);
+  const int maxrows = pad128(bin.nslots);
   CK(h->d_prop.alloc((size_t)NTR * K * ns * sizeof(float)), "proposal");
   CK(h->d_skip.alloc(ns * sizeof(int)), "skip flags");
-  CK(h->d_xfeat.alloc((size_t)rows * s->pin[0] * sizeof(bf16)), "features");
-  CK(h->d_yhat.alloc((size_t)rows * s->pout[s->L - 1] * sizeof(float)), "predictions");
+  CK(h->d_list.alloc((size_t)bin.nslots * sizeof(int)), "heavy list");
+  CK(h->d_gate.alloc(128), "heavy counter");
+  CK(h->d_xfeat.alloc((size_t)maxrows * s->pin[0] * sizeof(bf16)), "features");
+  CK(h->d_yhat.alloc((size_t)maxrows * s->pout[s->L - 1] * sizeof(float)), "predictions");
+  CK(h->d_act.alloc((size_t)2 * maxrows * s->pout[0] * sizeof(bf16)), "activations");
   const long long l0 = h->launches;
   if ((rc = stats_reset(h))) return rc;
   Params<float> p = make_params<float>(h->prm);
   set_clock(p, dt, h->prm.dt_min);
-  const bool bc4 = h->prm.bcup_particulate == 4;
+  unsigned* nheavy = h->d_gate.as<unsigned>();
+  int* list = h->d_list.as<int>();
+  bf16* act0 = h->d_act.as<bf16>();
+  bf16* act1 = act0 + (size_t)maxrows * s->pout[0];
   CK(cudaEventRecord(h->ev0, h->stream), "event");
   for (int step = 0; step < nsteps; step++) {
-    CK(sur::features(h->d_conc.as<float>(), h->d_force.as<float>(), s->norm, K, h->kmax,
-                     h->nslot, rows, s->nin, s->pin[0], h->d_xfeat.as<bf16>(), h->stream),
-       "features");
+    // 1. gate: every column's first (whole-step) attempt; columns that pass
+    //    are done, exactly as the plain step; the others are listed
+    CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
+    CK(cudaMemsetAsync(nheavy, 0, sizeof(unsigned), h->stream), "counter reset");
+    ColumnArgs<float> a = column_args<float>(h, bin, b, dt, SED_ADAPTIVE_EULER);
+    a.ntiles = bin.nslots;
+    a.heavy = list;
+    a.nheavy = nheavy;
+    CK(launch_warp_columns(h, a, p, bin, KIND_PROBE), "gate launch");
     h->launches++;
-    CK(cudaStreamSynchronize(h->stream), "features");
-    rc = sed_sur_forward_device(s, h->d_xfeat.p, h->d_yhat.p, rows);
+    CK(cudaMemcpyAsync(h->h_count, nheavy, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream),
+       "counter copy");
+    CK(cudaStreamSynchronize(h->stream), "gate");
+    unsigned nh_u = 0;
+    memcpy(&nh_u, h->h_count, sizeof nh_u);
+    const int nh = (int)nh_u;
+    if (nh <= 0) continue;
+    // 2. the network's proposal for the listed columns
+    const int rows = pad128(nh);
+    CK(sur::features(h->d_conc.as<float>(), h->d_force.as<float>(), s->norm, list, nh, K,
+                     h->kmax, h->nslot, rows, s->nin, s->pin[0], h->d_xfeat.as<bf16>(),
+                     h->stream),
+       "features");
+    rc = sur_infer_rows(s, h->d_xfeat.as<bf16>(), h->d_yhat.as<float>(), rows, act0, act1,
+                        h->stream);
     if (rc) return h->fail(rc, "surrogate forward: %s", s->err.c_str());
-    h->launches += 1 + 3 * s->L;
-    CK(sur::apply(h->d_yhat.as<float>(), h->d_conc.as<float>(), s->norm, K, h->kmax,
+    CK(sur::apply(h->d_yhat.as<float>(), h->d_conc.as<float>(), s->norm, list, nh, K, h->kmax,
                   h->nslot, s->nin, s->nout, s->pout[s->L - 1], h->d_prop.as<float>(),
                   h->stream),
        "apply");
-    h->launches++;
-    // residual test of every column, then the plain solver on the rejected
-    for (int kind : {KIND_RESID, KIND_ADAPT}) {
-      CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
-      for (int b = 0; b < 2; b++) {
-        const Bin& bin = h->bins[b];
-        if (bin.nslots == 0) continue;
-        ColumnArgs<float> a = column_args<float>(h, bin, b, dt, SED_ADAPTIVE_EULER);
-        a.out = h->d_prop.as<float>();
-        a.skip = h->d_skip.as<int>();
-        a.res_tol = tol;
-        a.res_atol = res_atol;
-        if (kind == KIND_ADAPT) {
-          CK(launch_bin<float>(h, a, p, bin, kind, h->stream), "surrogate step launch");
-          h->launches++;
-          continue;
-        }
-        int blocks = 1;
-        {
-          // two states per tile: the widest tile up to the class's that fits,
-          // staging every layer of the class
-          int tc = bin.tc ? bin.tc : 32, occ = 0;
-          for (; tc >= 8; tc /= 2)
-            if ((occ = column_blocks_per_sm<float>(tc, bin.lpl, bc4, kind, bin.threads,
-                                                   p.bio3 != 0)) > 0)
-              break;
-          if (occ <= 0) return h->fail(SED_E_CUDA, "residual kernel does not fit");
-          a.tc = tc;
-          a.tile_k = nullptr;
-          a.tile0 = 0;
-          a.ntiles = bin.nslots / tc;
-          blocks = std::max(1, std::min(a.ntiles, occ * h->sms));
-        }
-        CK(launch_column<float>(a, p, bin.lpl, bc4, kind, blocks, bin.threads, h->stream),
-           "surrogate step launch");
-        h->launches++;
-      }
-    }
+    h->launches += 2 + s->L;
+    // 3. residual test of every proposal; passing ones replace the state
+    ColumnArgs<float> r = column_args<float>(h, bin, b, dt, SED_ADAPTIVE_EULER);
+    r.list = list;
+    r.ntiles = nh;
+    r.out = h->d_prop.as<float>();
+    r.skip = h->d_skip.as<int>();
+    r.res_tol = tol;
+    r.res_atol = res_atol;
+    CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
+    CK(launch_warp_columns(h, r, p, bin, KIND_RESID), "residual launch");
+    // 4. the plain solver on the listed columns that failed it
+    ColumnArgs<float> f = column_args<float>(h, bin, b, dt, SED_ADAPTIVE_EULER);
+    f.list = list;
+    f.ntiles = nh;
+    f.skip = h->d_skip.as<int>();
+    CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
+    CK(launch_warp_columns(h, f, p, bin, KIND_ADAPT), "fallback launch");
+    h->launches += 2;
   }
   CK(cudaEventRecord(h->ev1, h->stream), "event");
   return stats_fetch(h, stats, l0, true);
+}
+
+int sed_sur_collect(sed_handle* h, const float* c0, double dt, float* x_dev, float* y_dev,
+                    int pitch_x, int pitch_y, long long capacity, long long* count,
+                    sed_stats* stats) {
+  int rc = ready(h);
+  if (rc) return rc;
+  if (!c0 || !x_dev || !y_dev || !count || capacity < 0 || *count < 0)
+    return h->fail(SED_E_ARG, "c0, x, y and count are required");
+  if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");
+  if (h->fp64()) return h->fail(SED_E_ARG, "training rows come from FP32 state");
+  if (h->has_bgc) return h->fail(SED_E_STATE, "training rows use the handle's parameter set");
+  if (h->prm.cut_scope != SED_CUT_PER_COLUMN)
+    return h->fail(SED_E_ARG, "training rows come from per-column cuts");
+  const int K = h->kmax;
+  if (pitch_x < NTR * K + NFORCE || pitch_y < NTR * K)
+    return h->fail(SED_E_ARG, "row pitches %d / %d below %d / %d", pitch_x, pitch_y,
+                   NTR * K + NFORCE, NTR * K);
+  const int b = surrogate_bin(h);
+  if (b < 0) return h->fail(SED_E_ARG, "training rows need every active column at %d layers", K);
+  if (!(dt > 0.0)) return h->fail(SED_E_ARG, "bad dt");
+  CK(cudaSetDevice(h->device), "set device");
+  const size_t state = (size_t)NTR * K * h->nslot * sizeof(float);
+  CK(h->d_backup.alloc(state), "state copy");
+  // d_gate: the row counter, then the log offsets c0 at byte 64
+  CK(h->d_gate.alloc(128), "row counter");
+  const long long l0 = h->launches;
+  if ((rc = stats_reset(h))) return rc;
+  float* d_c0 = reinterpret_cast<float*>(h->d_gate.as<unsigned char>() + 64);
+  CK(cudaMemcpyAsync(d_c0, c0, NTR * sizeof(float), cudaMemcpyHostToDevice, h->stream),
+     "c0 copy");
+  unsigned long long* cnt = reinterpret_cast<unsigned long long*>(h->d_gate.p);
+  *h->h_count = (unsigned long long)*count;
+  CK(cudaMemcpyAsync(cnt, h->h_count, sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                     h->stream),
+     "counter copy");
+  CK(cudaMemcpyAsync(h->d_backup.p, h->d_conc.p, state, cudaMemcpyDeviceToDevice, h->stream),
+     "state copy");
+  CK(cudaEventRecord(h->ev0, h->stream), "event");
+  if ((rc = enqueue_columns<float>(h, dt, SED_ADAPTIVE_EULER, KIND_ADAPT))) return rc;
+  CK(cudaEventRecord(h->ev1, h->stream), "event");
+  const Bin& bin = h->bins[b];
+  CK(sur::collect(h->d_backup.as<float>(), h->d_conc.as<float>(), h->d_force.as<float>(),
+                  h->d_kact.as<int>(), h->d_nsub.as<int>(), d_c0, K, h->kmax, h->nslot,
+                  bin.slot0, bin.nslots, x_dev, pitch_x, y_dev, pitch_y, cnt, capacity, h->sms,
+                  h->stream),
+     "collect");
+  h->launches++;
+  CK(cudaMemcpyAsync(h->h_count, cnt, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                     h->stream),
+     "counter copy");
+  if ((rc = stats_fetch(h, stats, l0, true))) return rc;
+  *count = std::min((long long)*h->h_count, capacity);
+  return SED_OK;
 }
 
 int sed_get_rhs(sed_handle* h, const double* conc, double* rhs, double* fluxes) {

@@ -28,14 +28,12 @@ namespace sed {
 template <typename real>
 struct TileLayout {
   int tcp, kt;
-  size_t conc, conc2, coef, cap, force, sflux, bud, nsub, total;
-  __host__ __device__ TileLayout(int tc, int kt_, bool bc4, bool two_states, int ncoef)
-      : kt(kt_) {
+  size_t conc, coef, cap, force, sflux, bud, nsub, total;
+  __host__ __device__ TileLayout(int tc, int kt_, bool bc4, int ncoef) : kt(kt_) {
     tcp = tc + 16 / (int)sizeof(real);  // row pad keeps 16-byte alignment
     size_t r = sizeof(real);
     conc = 0;
-    conc2 = conc + (size_t)NTR * kt * tcp * r;
-    coef = conc2 + (two_states ? (size_t)NTR * kt * tcp * r : 0);
+    coef = conc + (size_t)NTR * kt * tcp * r;
     cap = coef + (size_t)ncoef * kt * tcp * r;
     force = cap + (bc4 ? (size_t)kt * tcp * r : 0);
     sflux = force + (size_t)NFORCE * tcp * r;
@@ -49,7 +47,8 @@ struct TileLayout {
 
 template <typename real>
 size_t tile_smem_bytes(int tc, int lpl, bool bc4, int kind, bool bio3) {
-  return TileLayout<real>(tc, 32 * lpl, bc4, kind == KIND_RESID, coef_rows<real>(bio3)).total;
+  (void)kind;
+  return TileLayout<real>(tc, 32 * lpl, bc4, coef_rows<real>(bio3)).total;
 }
 
 // Copy `rows` rows of tc reals between global (row stride gstride, first
@@ -413,7 +412,12 @@ __device__ __forceinline__ int epilogue(const Params<real>& p, int lane, int K,
 // exact in FP64 (p.ticks), the same decisions are taken with integer ticks
 // of dt/4^mstop (mstop = first level with dt/4^m <= dt_min), which keeps the
 // loop off the FP64 pipe; otherwise the FP64 sums are kept.
-template <typename real, int LPL, bool BC4, bool BIO3, bool TICKS>
+//
+// PROBE: the gate of the surrogate step.  A column whose first attempt (the
+// whole coupling step at once) is accepted finishes exactly as without
+// PROBE; a column whose first attempt is rejected returns at once with
+// attempts = -1, its state C untouched, and no budget or epilogue work.
+template <typename real, int LPL, bool BC4, bool BIO3, bool TICKS, bool PROBE = false>
 __device__ __forceinline__ ColResult solve_adaptive(
     const Params<real>& p, const Lane<real, LPL, BC4>& lc, int lane, int K,
     real (&C)[LPL][NTR], real (&ftop)[NTR], double dt, double (&bud)[4]) {
@@ -459,6 +463,10 @@ __device__ __forceinline__ ColResult solve_adaptive(
     }
     const bool reject = __any_sync(FULL, bad);
     const bool can_cut = TICKS ? (m < p.mstop) : (dt_red > p.dt_min);
+    if (PROBE && reject && can_cut) {
+      res.attempts = -1;
+      return res;
+    }
     if (reject && can_cut) {
       m++;
       dtr = dtr * real(0.25);
@@ -588,10 +596,9 @@ k_column(ColumnArgs<real> a, Params<real> p) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int tc = a.tc;
   constexpr int KT = 32 * LPL;
-  TileLayout<real> L(tc, KT, BC4, KIND == KIND_RESID, NCO);
+  TileLayout<real> L(tc, KT, BC4, NCO);
   const int tcp = L.tcp;
   real* s_conc = reinterpret_cast<real*>(smem + L.conc);
-  real* s_conc2 = reinterpret_cast<real*>(smem + L.conc2);
   real* s_coef = reinterpret_cast<real*>(smem + L.coef);
   real* s_cap = reinterpret_cast<real*>(smem + L.cap);
   real* s_force = reinterpret_cast<real*>(smem + L.force);
@@ -599,13 +606,13 @@ k_column(ColumnArgs<real> a, Params<real> p) {
   double* s_bud = reinterpret_cast<double*>(smem + L.bud);
   int* s_nsub = reinterpret_cast<int*>(smem + L.nsub);
   __shared__ int s_tile, s_next;
-  __shared__ unsigned long long b_att, b_acc, b_cols, b_mindt, b_sur;
+  __shared__ unsigned long long b_att, b_acc, b_cols, b_mindt;
   __shared__ int b_maxatt, b_cap, b_nan;
 
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lane = tid & 31;
   if (tid == 0) {
-    b_att = 0; b_acc = 0; b_cols = 0; b_sur = 0; b_mindt = 0x7FF0000000000000ull;
+    b_att = 0; b_acc = 0; b_cols = 0; b_mindt = 0x7FF0000000000000ull;
     b_maxatt = 0; b_cap = 0; b_nan = 0;
   }
   const size_t ns = (size_t)a.nslot;
@@ -617,12 +624,8 @@ k_column(ColumnArgs<real> a, Params<real> p) {
     if (tile >= a.ntiles) break;
     const int slot0 = a.slot0 + tile * tc;
     const int kt = a.tile_k ? a.tile_k[a.tile0 + tile] : (a.kmax < KT ? a.kmax : KT);
-    // stage in (KIND_RESID: the proposed state, and the start state)
-    copy_grouped<real, true>(s_conc, (KIND == KIND_RESID ? a.out : a.conc) + slot0, NTR,
-                             kt, KT, a.kmax, ns, tc, tcp, tid, nthr);
-    if (KIND == KIND_RESID)
-      copy_grouped<real, true>(s_conc2, a.conc + slot0, NTR, kt, KT, a.kmax, ns, tc,
-                               tcp, tid, nthr);
+    copy_grouped<real, true>(s_conc, a.conc + slot0, NTR, kt, KT, a.kmax, ns, tc, tcp, tid,
+                             nthr);
     copy_grouped<real, true>(s_coef, const_cast<real*>(a.coef) + slot0, NCO, kt, KT,
                              a.kmax, ns, tc, tcp, tid, nthr);
     if (BC4)
@@ -638,22 +641,10 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       j = __shfl_sync(FULL, j, 0);
       if (j >= tc) break;
       const int K = a.kact[slot0 + j];
-      if (KIND != KIND_RESID && K > 0 && a.skip && a.skip[slot0 + j]) {
-        // accepted surrogate step: state and surface flux already in place
-        if (lane == 0) {
-          s_nsub[j] = 0;
-          if (a.mindt) a.mindt[slot0 + j] = 0.0;
-#pragma unroll
-          for (int d = 0; d < NDISS; d++) s_sflux[d * tcp + j] = a.sflux[d * ns + slot0 + j];
-          for (int b = 0; b < 4; b++) s_bud[b * tc + j] = 0.0;
-        }
-        continue;
-      }
       if (K <= 0) {
-        if (KIND == KIND_RESID && lane == 0) a.skip[slot0 + j] = 0;
         if (lane == 0) {
           s_nsub[j] = 0;
-          if (mode == 0 && KIND != KIND_RESID && a.mindt) a.mindt[slot0 + j] = 0.0;
+          if (mode == 0 && a.mindt) a.mindt[slot0 + j] = 0.0;
 #pragma unroll
           for (int d = 0; d < NDISS; d++) s_sflux[d * tcp + j] = real(0);
           for (int b = 0; b < 4; b++) s_bud[b * tc + j] = 0.0;
@@ -667,53 +658,6 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       real ftop[NTR];
 #pragma unroll
       for (int n = 0; n < NTR; n++) ftop[n] = real(0);
-      if (KIND == KIND_RESID) {
-        // backward-Euler defect of the proposed state C' over the step:
-        // |C' - C - dt f(C')| / (|C'| + |C| + dt |f(C')| + atol)
-        real R[LPL][NTR];
-        real dn[LPL];
-        rhs_any<real, LPL, BC4, BIO3>(p, lc, lane, K, C, R, ftop, dn);
-        const real dtr = (real)a.dt, at = (real)a.res_atol;
-        real rho = real(0);
-#pragma unroll
-        for (int s = 0; s < LPL; s++) {
-          const int Ll = s * 32 + lane;
-          if (Ll < K) {
-#pragma unroll
-            for (int n = 0; n < NTR; n++) {
-              const real c0 = s_conc2[(n * KT + Ll) * tcp + j];
-              const real num = fabs(C[s][n] - c0 - dtr * R[s][n]);
-              const real den = fabs(C[s][n]) + fabs(c0) + dtr * fabs(R[s][n]) + at;
-              rho = fmax(rho, num / den);
-            }
-          }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) rho = fmax(rho, __shfl_xor_sync(FULL, rho, o));
-        const bool pass = rho <= (real)a.res_tol;  // NaN fails
-        if (!pass) {  // hand the start state back for the fallback step
-#pragma unroll
-          for (int s = 0; s < LPL; s++) {
-            const int Ll = s * 32 + lane;
-            if (Ll < K)
-#pragma unroll
-              for (int n = 0; n < NTR; n++)
-                s_conc[(n * KT + Ll) * tcp + j] = s_conc2[(n * KT + Ll) * tcp + j];
-          }
-        }
-        if (lane == 0) {
-          a.skip[slot0 + j] = pass ? 1 : 0;
-#pragma unroll
-          for (int d = 0; d < NDISS; d++) s_sflux[d * tcp + j] = ftop[NPART + d];
-          s_nsub[j] = 0;
-          for (int b = 0; b < 4; b++) s_bud[b * tc + j] = 0.0;
-          if (pass) {
-            atomicAdd(&b_sur, 1ull);
-            atomicAdd(&b_cols, 1ull);
-          }
-        }
-        continue;
-      }
       if (KIND == KIND_RHS) {
         real R[LPL][NTR];
         real dn[LPL];
@@ -778,7 +722,6 @@ k_column(ColumnArgs<real> a, Params<real> p) {
   }
   __syncthreads();
   if (tid == 0 && mode == 0) {
-    atomicAdd(&a.stats->surrogate, b_sur);
     atomicAdd(&a.stats->attempts, b_att);
     atomicAdd(&a.stats->accepted, b_acc);
     atomicAdd(&a.stats->column_steps, b_cols);
@@ -804,11 +747,11 @@ template <typename real, int LPL, bool BC4, bool BIO3, int KIND, bool MULTI, boo
 __global__ void __launch_bounds__(256, (MinBlocks<real, LPL>::value))
 k_column_warp(ColumnArgs<real> a, Params<real> p) {
   __shared__ real s_bnd[8][NFORCE];
-  __shared__ unsigned long long b_att, b_acc, b_cols, b_mindt;
+  __shared__ unsigned long long b_att, b_acc, b_cols, b_mindt, b_sur;
   __shared__ int b_maxatt, b_cap, b_nan;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) {
-    b_att = 0; b_acc = 0; b_cols = 0; b_mindt = 0x7FF0000000000000ull;
+    b_att = 0; b_acc = 0; b_cols = 0; b_sur = 0; b_mindt = 0x7FF0000000000000ull;
     b_maxatt = 0; b_cap = 0; b_nan = 0;
   }
   __syncthreads();
@@ -819,9 +762,12 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
     if (lane == 0) j = (int)atomicAdd(a.queue, 1u);
     j = __shfl_sync(FULL, j, 0);
     if (j >= a.ntiles) break;
-    const int slot = a.slot0 + j;
+    // the launch's j-th column: of a slot list (the surrogate step's heavy
+    // columns), or of the slot range
+    const int slot = a.list ? a.list[j] : a.slot0 + j;
     const int K = a.kact[slot];
-    const bool skipped = a.skip && K > 0 && a.skip[slot];
+    // (KIND_RESID writes the skip flags; the stepping kinds read them)
+    const bool skipped = KIND != KIND_RESID && a.skip && K > 0 && a.skip[slot];
     if (K <= 0 || skipped) {
       // land or padding: zero outputs; accepted surrogate step: the state
       // and surface flux are already in place
@@ -842,13 +788,63 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
     // global arrays in load_lane's (row, column) form: rows of kmax layers
     // per tracer / coefficient, columns of stride nslot; then the surface
     // values the substeps read come from the warp's shared copy
-    load_lane<real, LPL, BC4, BIO3>(lc, C, a.conc, a.coef, a.cap, a.force, slot, a.kmax,
-                                    (int)ns, lane, K, p.mol_mode);
+    // KIND_RESID reads the surrogate's proposed state (a.out)
+    load_lane<real, LPL, BC4, BIO3>(lc, C, KIND == KIND_RESID ? a.out : a.conc, a.coef, a.cap,
+                                    a.force, slot, a.kmax, (int)ns, lane, K, p.mol_mode);
     lc.bnd_s = sb + 2;
     lc.bnd_stride = 1;
     Params<real> pc = p;
     if (ENS) load_bgc(pc, a.bgc, ns, slot);
     real ftop[NTR];
+    if (KIND == KIND_RESID) {
+      // Quasi-steady test of the proposal P: the plain right-hand side at P
+      // may change no cell by more than res_tol of its value over one step,
+      // dt |f(P)| <= res_tol (|P| + res_atol) in every active cell.  At the
+      // end of a column's heavy steps the plain solver's own states change
+      // by about 1 % per step this way; a proposal off the slow manifold of
+      // the stiff cells fails by orders of magnitude.  NaN fails.
+      epilogue<real, LPL>(pc, lane, K, C);
+      real R[LPL][NTR];
+      real dn[LPL];
+#pragma unroll
+      for (int n = 0; n < NTR; n++) ftop[n] = real(0);
+      rhs_any<real, LPL, BC4, BIO3>(pc, lc, lane, K, C, R, ftop, dn);
+      const real dtr = (real)a.dt, at = (real)a.res_atol, tol = (real)a.res_tol;
+      bool ok = true;
+#pragma unroll
+      for (int s = 0; s < LPL; s++) {
+        const int L = s * 32 + lane;
+        if (L < K)
+#pragma unroll
+          for (int n = 0; n < NTR; n++)
+            ok = ok && (dtr * fabs(R[s][n]) <= tol * (fabs(C[s][n]) + at));
+      }
+      const bool pass = __all_sync(FULL, ok);
+      if (pass) {
+#pragma unroll
+        for (int s = 0; s < LPL; s++) {
+          const int L = s * 32 + lane;
+          if (L < K)
+#pragma unroll
+            for (int n = 0; n < NTR; n++) a.conc[((size_t)n * a.kmax + L) * ns + slot] = C[s][n];
+        }
+      }
+      if (lane == 0) {
+        a.skip[slot] = pass ? 1 : 0;
+        if (pass) {
+#pragma unroll
+          for (int d = 0; d < NDISS; d++) a.sflux[d * ns + slot] = ftop[NPART + d];
+          a.nsub[slot] = 0;
+          if (a.mindt) a.mindt[slot] = 0.0;
+          if (a.budget)
+            for (int b = 0; b < 4; b++) a.budget[b * ns + slot] = 0.0;
+          atomicAdd(&b_sur, 1ull);
+          atomicAdd(&b_cols, 1ull);
+        }
+      }
+      __syncwarp();
+      continue;
+    }
     double bud[4];
     ColResult r;
     // MULTI: a.nrepeat steps in a row (the loop costs registers, so the
@@ -858,12 +854,15 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
 #pragma unroll
       for (int n = 0; n < NTR; n++) ftop[n] = real(0);
       for (int b = 0; b < 4; b++) bud[b] = 0.0;
-      if (KIND == KIND_ADAPT)
-        r = pc.ticks
-                ? solve_adaptive<real, LPL, BC4, BIO3, true>(pc, lc, lane, K, C, ftop, a.dt, bud)
-                : solve_adaptive<real, LPL, BC4, BIO3, false>(pc, lc, lane, K, C, ftop, a.dt, bud);
+      constexpr bool PROBE = KIND == KIND_PROBE;
+      if (KIND == KIND_ADAPT || PROBE)
+        r = pc.ticks ? solve_adaptive<real, LPL, BC4, BIO3, true, PROBE>(pc, lc, lane, K, C, ftop,
+                                                                        a.dt, bud)
+                     : solve_adaptive<real, LPL, BC4, BIO3, false, PROBE>(pc, lc, lane, K, C, ftop,
+                                                                         a.dt, bud);
       else
         r = solve_fixed<real, LPL, BC4, BIO3>(pc, lc, lane, K, C, ftop, a.dt, a.method, bud);
+      if (PROBE && r.attempts < 0) break;
       if (lane == 0) {
         atomicAdd(&b_att, (unsigned long long)r.attempts);
         atomicAdd(&b_acc, (unsigned long long)r.accepted);
@@ -874,6 +873,11 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
         if (r.accepted > 0)
           atomicMin(&b_mindt, (unsigned long long)__double_as_longlong(r.min_dt));
       }
+    }
+    if (KIND == KIND_PROBE && r.attempts < 0) {
+      // first attempt rejected: a heavy column, left as it was
+      if (lane == 0) a.heavy[atomicAdd(a.nheavy, 1u)] = slot;
+      continue;
     }
 #pragma unroll
     for (int s = 0; s < LPL; s++) {
@@ -894,6 +898,7 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
   }
   __syncthreads();
   if (tid == 0) {
+    if (b_sur) atomicAdd(&a.stats->surrogate, b_sur);
     atomicAdd(&a.stats->attempts, b_att);
     atomicAdd(&a.stats->accepted, b_acc);
     atomicAdd(&a.stats->column_steps, b_cols);
@@ -1268,8 +1273,6 @@ cudaError_t launch_column_k(const ColumnArgs<real>& a, const Params<real>& p,
     return launch_column_t<real, LPL, BC4, BIO3, KIND_ADAPT>(a, p, blocks, threads, st);
   if (kind == KIND_FIXED)
     return launch_column_t<real, LPL, BC4, BIO3, KIND_FIXED>(a, p, blocks, threads, st);
-  if (kind == KIND_RESID)
-    return launch_column_t<real, LPL, BC4, BIO3, KIND_RESID>(a, p, blocks, threads, st);
   return launch_column_t<real, LPL, BC4, BIO3, KIND_RHS>(a, p, blocks, threads, st);
 }
 
@@ -1320,7 +1323,6 @@ template <typename real, int LPL, bool BC4, bool BIO3>
 int occupancy_k(int tc, int kind, int threads) {
   if (kind == KIND_ADAPT) return occupancy_t<real, LPL, BC4, BIO3, KIND_ADAPT>(tc, threads);
   if (kind == KIND_FIXED) return occupancy_t<real, LPL, BC4, BIO3, KIND_FIXED>(tc, threads);
-  if (kind == KIND_RESID) return occupancy_t<real, LPL, BC4, BIO3, KIND_RESID>(tc, threads);
   return occupancy_t<real, LPL, BC4, BIO3, KIND_RHS>(tc, threads);
 }
 
@@ -1351,6 +1353,18 @@ static cudaError_t launch_warp_t(const ColumnArgs<real>& a, const Params<real>& 
 template <typename real, int LPL, bool BC4, bool BIO3, bool ENS>
 cudaError_t launch_warp_e(const ColumnArgs<real>& a, const Params<real>& p, int kind,
                           int blocks, int threads, cudaStream_t st) {
+  if (kind == KIND_PROBE || kind == KIND_RESID) {
+    // the surrogate step's gate and residual test: FP32 state, one set
+    if constexpr (std::is_same<real, float>::value && !ENS) {
+      if (a.nrepeat > 1) return cudaErrorInvalidValue;
+      return kind == KIND_PROBE
+                 ? launch_warp_t<real, LPL, BC4, BIO3, KIND_PROBE, false, ENS>(a, p, blocks,
+                                                                              threads, st)
+                 : launch_warp_t<real, LPL, BC4, BIO3, KIND_RESID, false, ENS>(a, p, blocks,
+                                                                              threads, st);
+    }
+    return cudaErrorInvalidValue;
+  }
   if (kind == KIND_FIXED) {
     if (a.nrepeat > 1) return cudaErrorInvalidValue;
     return launch_warp_t<real, LPL, BC4, BIO3, KIND_FIXED, false, ENS>(a, p, blocks, threads, st);

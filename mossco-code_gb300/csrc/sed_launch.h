@@ -8,7 +8,9 @@
 
 namespace sed {
 
-enum : int { KIND_ADAPT = 0, KIND_FIXED = 1, KIND_RHS = 2, KIND_RESID = 3 };
+// KIND_PROBE and KIND_RESID are the surrogate step's gate and residual test
+// (warp-direct kernel only)
+enum : int { KIND_ADAPT = 0, KIND_FIXED = 1, KIND_RHS = 2, KIND_RESID = 3, KIND_PROBE = 4 };
 
 // Arguments of the tile kernel.  Device layouts (slot = compacted column):
 //   conc  [NTR][kmax][nslot]     coef  [coef_rows][kmax][nslot]
@@ -36,10 +38,17 @@ struct ColumnArgs {
   double dt;
   int method;
   // surrogate coupling step: per-slot flags (1 = the surrogate's state was
-  // accepted, the step kernels skip the column) and the residual test of
-  // KIND_RESID (out = proposed state, conc = state at the start of the step)
+  // accepted, the step kernels skip the column) and the tolerances of the
+  // residual test (KIND_RESID: out = proposed state, written into conc when
+  // it passes)
   int* skip;
   double res_tol, res_atol;
+  // warp-direct kernel: the launch's columns are list[0 .. ntiles) (slots)
+  // instead of the slot range; KIND_PROBE appends the slot of every column
+  // whose first attempt was rejected to heavy[atomicAdd(nheavy, 1)]
+  const int* list;
+  int* heavy;
+  unsigned* nheavy;
   // warp-direct kernel: coupling steps per launch with constant forcing
   // (0 or 1: one); each warp keeps its column in registers between them
   int nrepeat;

@@ -41,6 +41,21 @@ int sur_forward_rows(sed_surrogate* s, int m) {
   return SED_OK;
 }
 
+int sur_infer_rows(sed_surrogate* s, const bf16* x, float* y, int m, bf16* act0, bf16* act1,
+                   cudaStream_t st) {
+  const bf16* in = x;
+  for (int l = 0; l < s->L; l++) {
+    const bool last = l == s->L - 1;
+    bf16* out = (l & 1) ? act1 : act0;
+    SCK(sur::gemm_nt(last ? sur::EPI_BIAS : sur::EPI_GELU, in, s->wb[l], m, s->pout[l],
+                     s->pin[l], s->b[l], last ? y : nullptr, last ? nullptr : out, nullptr,
+                     s->pout[l], st),
+        "inference gemm");
+    in = out;
+  }
+  return SED_OK;
+}
+
 namespace {
 
 // loss + backward over m rows (targets in s->y); gradients in gw/gb

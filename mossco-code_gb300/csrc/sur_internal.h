@@ -67,3 +67,7 @@ struct sed_surrogate {
 
 // forward pass over m rows already in s->x; output pre-activation in z[L-1]
 int sur_forward_rows(sed_surrogate* s, int m);
+// inference over m rows (a multiple of 128): x BF16 [m][pin[0]] -> y FP32
+// [m][pout[L-1]], hidden activations in act0 / act1 (BF16 [m][hidden padded])
+int sur_infer_rows(sed_surrogate* s, const bf16* x, float* y, int m, bf16* act0, bf16* act1,
+                   cudaStream_t st);

@@ -68,7 +68,8 @@ __device__ __forceinline__ float gelu_grad(float z) {
 }
 
 // Epilogues.  EPI_BIAS_GELU: Z = acc + bias -> store Z (fp32) and GELU(Z)
-// (bf16).  EPI_BIAS: out = acc + bias (fp32, and bf16 if out_bf16).
+// (bf16).  EPI_GELU: GELU(acc + bias) (bf16 only).  EPI_BIAS: out = acc +
+// bias (fp32).
 // EPI_F32: out = acc (fp32).  EPI_GELU_BWD: out = acc * GELU'(Zprev)
 // (bf16), the gradient through the previous layer's activation.
 template <int EPI>
@@ -159,6 +160,11 @@ k_gemm_nt(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restrict__
           v0 += bias[col];
           v1 += bias[col + 1];
           *reinterpret_cast<float2*>(out_f32 + o) = make_float2(v0, v1);
+          *reinterpret_cast<__nv_bfloat162*>(out_bf16 + o) =
+              __floats2bfloat162_rn(gelu(v0), gelu(v1));
+        } else if (EPI == EPI_GELU) {
+          v0 += bias[col];
+          v1 += bias[col + 1];
           *reinterpret_cast<__nv_bfloat162*>(out_bf16 + o) =
               __floats2bfloat162_rn(gelu(v0), gelu(v1));
         } else if (EPI == EPI_BIAS) {
@@ -273,6 +279,9 @@ cudaError_t gemm_nt(int epi, const __nv_bfloat16* A, const __nv_bfloat16* B, int
       break;
     case EPI_BIAS:
       k_gemm_nt<EPI_BIAS><<<grid, 128, 0, st>>>(A, B, M, N, K, bias, out_f32, out_bf16, zprev, ld_out);
+      break;
+    case EPI_GELU:
+      k_gemm_nt<EPI_GELU><<<grid, 128, 0, st>>>(A, B, M, N, K, bias, out_f32, out_bf16, zprev, ld_out);
       break;
     case EPI_F32:
       k_gemm_nt<EPI_F32><<<grid, 128, 0, st>>>(A, B, M, N, K, bias, out_f32, out_bf16, zprev, ld_out);

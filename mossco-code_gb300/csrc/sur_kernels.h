@@ -6,7 +6,8 @@
 
 namespace sur {
 
-enum : int { EPI_BIAS_GELU = 0, EPI_BIAS = 1, EPI_F32 = 2, EPI_GELU_BWD = 3 };
+// EPI_GELU: GELU(acc + bias) to BF16 only (inference: no pre-activations kept)
+enum : int { EPI_BIAS_GELU = 0, EPI_BIAS = 1, EPI_F32 = 2, EPI_GELU_BWD = 3, EPI_GELU = 4 };
 
 // C[M x N] = A[M x K] . B[N x K]^T; M % 128 == 0, N % 64 == 0, K % 32 == 0
 cudaError_t gemm_nt(int epi, const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N,

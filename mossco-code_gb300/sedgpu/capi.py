@@ -158,6 +158,10 @@ SIGNATURES = {
     "sed_step_surrogate": (ctypes.c_int, [_H, _H, ctypes.c_double, ctypes.c_int,
                                           ctypes.c_double, ctypes.c_double,
                                           ctypes.POINTER(SedStats)]),
+    "sed_sur_collect": (ctypes.c_int, [_H, _fp, ctypes.c_double, _vp, _vp, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_longlong,
+                                       ctypes.POINTER(ctypes.c_longlong),
+                                       ctypes.POINTER(SedStats)]),
     "sed_error_string": (ctypes.c_char_p, [ctypes.c_int]),
     "sed_last_error": (ctypes.c_char_p, [_H]),
     "sed_tracer_name": (ctypes.c_char_p, [ctypes.c_int]),

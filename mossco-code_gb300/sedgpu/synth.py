@@ -256,6 +256,17 @@ def make_columns(inum: int, jnum: int, kmin: int, kmax: int, total: float,
     return cs
 
 
+def active_columns(name: str, seed: int = 1234) -> np.ndarray:
+    """Global ids of the active (non-land) columns of a named workload,
+    without building its arrays (the land mask is one counter-based draw per
+    column, as in make_columns)."""
+    spec = WORKLOADS[name]
+    gid = np.arange(spec["inum"] * spec["jnum"], dtype=np.int64)
+    if spec["land"] <= 0:
+        return gid
+    return gid[~(uniform(seed, F_LAND, gid) < spec["land"])]
+
+
 def make_workload(name: str, seed: int = 1234,
                   cols: Optional[np.ndarray] = None, **over) -> ColumnSet:
     """One of the named workloads (``WORKLOADS``), optionally a column

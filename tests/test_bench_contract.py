@@ -29,8 +29,21 @@ def check(line):
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
 
 
-def test_reference_arm_sediment():
-    line = run("--cpu-columns", "32")
+def test_reference_arm_headline():
+    """The default sediment arm: the reference algorithm over the headline's
+    window (a column sample of the 2048 x 2048 workload, brought to the
+    window's start day untimed)."""
+    line = run("--start-day", "0.25", "--ref-columns", "24")
+    check(line)
+    assert line["unit"] == "column-steps/s"
+    cfg = line["config"]
+    assert cfg["workload"] == "surrogate_2048x2048" and cfg["columns"] == 2936778
+    assert cfg["simulated_days_timed"] == "0.250..0.333"
+    assert "of 2936778 active columns" in line["cpu_baseline"]["sample"]
+
+
+def test_reference_arm_sediment_plain():
+    line = run("--solver", "plain", "--cpu-columns", "32")
     check(line)
     assert line["unit"] == "column-steps/s" and line["config"]["workload"] == "plain_gpu_256x256"
     # the host beside the all-core figure, and the same window on one core
