@@ -267,10 +267,41 @@ def active_columns(name: str, seed: int = 1234) -> np.ndarray:
     return gid[~(uniform(seed, F_LAND, gid) < spec["land"])]
 
 
+# per-column arrays of a ColumnSet: the column is the last axis
+_COLUMN_FIELDS = ("kact", "dz", "dzc", "zc", "zi", "phi", "phi_i", "biofac", "flux_cap",
+                  "bdys", "fluxes", "conc")
+CHUNK_COLUMNS = 1 << 17
+
+
 def make_workload(name: str, seed: int = 1234,
-                  cols: Optional[np.ndarray] = None, **over) -> ColumnSet:
+                  cols: Optional[np.ndarray] = None, threads: Optional[int] = None,
+                  **over) -> ColumnSet:
     """One of the named workloads (``WORKLOADS``), optionally a column
-    subset; keyword overrides replace entries of the workload table."""
+    subset; keyword overrides replace entries of the workload table.
+
+    Grids of more than CHUNK_COLUMNS columns are built in column chunks on a
+    thread pool (numpy releases the interpreter lock inside its array
+    operations); every value is a function of its column id alone, so the
+    result is the same as one pass over all columns."""
     spec = dict(WORKLOADS[name])
     spec.update(over)
-    return make_columns(seed=seed, cols=cols, name=name, **spec)
+    n = spec["inum"] * spec["jnum"] if cols is None else len(cols)
+    if n <= CHUNK_COLUMNS:
+        return make_columns(seed=seed, cols=cols, name=name, **spec)
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+    gid = np.arange(n, dtype=np.int64) if cols is None else np.asarray(cols, dtype=np.int64)
+    parts = [gid[i:i + CHUNK_COLUMNS] for i in range(0, n, CHUNK_COLUMNS)]
+    workers = threads or min(len(parts), os.cpu_count() or 1)
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        sets = list(ex.map(lambda c: make_columns(seed=seed, cols=c, name=name, **spec),
+                           parts))
+    out = sets[0]
+    for f in _COLUMN_FIELDS:
+        setattr(out, f, np.ascontiguousarray(
+            np.concatenate([getattr(cs, f) for cs in sets], axis=-1)))
+    if cols is None:
+        out.inum, out.jnum = spec["inum"], spec["jnum"]
+    else:
+        out.inum, out.jnum = n, 1
+    return out
