@@ -245,18 +245,21 @@ contains
 
   !> Create a handle for the driver's grid (after type_sed%initialize):
   !! grid%dz, grid%dzc, porosity, intf_porosity, bioturbation_factor,
-  !! flux_cap and mask (masked columns, or masked bottom layers only).
-  subroutine sed_gpu_init(gpu, p, inum, jnum, knum, dz, dzc, porosity, &
+  !! flux_cap and mask (masked columns, or masked bottom layers only).  ntr
+  !! is the driver's nvar, the tracer planes of its conc array
+  !! (fabm_sediment_driver.F90:353); the library refuses any count but
+  !! SED_NTR with SED_E_ARG, so it never reads past the caller's arrays.
+  subroutine sed_gpu_init(gpu, p, inum, jnum, knum, ntr, dz, dzc, porosity, &
                           intf_porosity, bioturbation_factor, flux_cap, mask, rc)
     type(sed_gpu_t), intent(out) :: gpu
     type(sed_params_t), intent(in) :: p
-    integer, intent(in) :: inum, jnum, knum
+    integer, intent(in) :: inum, jnum, knum, ntr
     real(c_double), dimension(:,:,:), intent(in), target, contiguous :: &
       dz, dzc, porosity, intf_porosity, bioturbation_factor, flux_cap
     integer(c_int), dimension(:,:,:), intent(in), target, contiguous :: mask
     integer, intent(out) :: rc
     rc = sed_create(p, int(inum, c_int), int(jnum, c_int), int(knum, c_int), &
-                    int(SED_NTR, c_int), gpu%h)
+                    int(ntr, c_int), gpu%h)
     if (rc /= SED_OK) return
     rc = sed_set_grid(gpu%h, c_loc(dz), c_loc(dzc), c_loc(porosity), &
                       c_loc(intf_porosity), c_loc(bioturbation_factor), &
