@@ -604,6 +604,102 @@ def run_reference_headline(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+MLP_METRIC = ("surrogate MLP inference on 1 GB300: rows/s of the 343->256x4->330 network "
+              "(BF16 products, FP32 accumulation)")
+
+
+def mlp_flops_per_row(K: int = 30) -> int:
+    """Algorithmic multiply-adds x 2 of one row, unpadded widths."""
+    dims = [NTR * K + NFORCE] + [256] * 4 + [NTR * K]
+    return 2 * sum(dims[i] * dims[i + 1] for i in range(len(dims) - 1))
+
+
+def run_mlp(args) -> None:
+    """Inference of the surrogate network on the rows of the 2048 x 2048
+    workload's active columns (2 936 778, padded to 128), with random
+    weights: the fused tcgen05 kernel and the mma.sync GEMMs, each timed with
+    CUDA events on the stream it runs on, inputs larger than L2."""
+    import ctypes
+    import torch
+    from sedgpu import capi
+    from sedgpu import surrogate as S
+    torch.cuda.set_device(0)
+    lib = capi.load()
+    K = 30
+    m = S.pad128(args.mlp_rows)
+    sur = S.Surrogate(K, batch=8192, seed=3)
+    n = lib.sed_sur_num_params(sur.h)
+    rng = np.random.default_rng(4)
+    w = rng.normal(0, 1, n).astype(np.float32)
+    dims = [sur.nin] + [S.HIDDEN] * S.NHIDDEN + [sur.nout]
+    o = 0
+    for i in range(len(dims) - 1):
+        w[o:o + dims[i] * dims[i + 1]] /= np.sqrt(dims[i])
+        o += dims[i] * dims[i + 1] + dims[i + 1]
+    sur.set_weights(w)
+    X = torch.zeros((m, sur.pin), dtype=torch.bfloat16, device="cuda")
+    X[:, :sur.nin] = torch.randn((m, sur.nin), device="cuda").to(torch.bfloat16)
+    Y = torch.empty((m, sur.pout), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    lib.sed_sur_set_stream(sur.h, ctypes.c_void_p(stream.cuda_stream))
+    flops = mlp_flops_per_row(K) * m
+    peak = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+    except Exception:
+        peak = 1900.0
+    out = {}
+    clk = None
+    for name, tc in (("tcgen05_fused", 1), ("mma_sync_gemms", 0)):
+        got = lib.sed_sur_set_tensor_cores(sur.h, tc)
+        if tc and got != 1:
+            out[name] = {"unavailable": "network shape or tensor-map encoder"}
+            continue
+
+        def call():
+            rc = lib.sed_sur_forward_device(sur.h, ctypes.c_void_p(X.data_ptr()),
+                                            ctypes.c_void_p(Y.data_ptr()), m)
+            if rc != 0:
+                raise capi.SedError(rc, lib.sed_sur_last_error(sur.h).decode())
+        for _ in range(args.warmup):
+            call()
+        clocks = ClockSampler(0) if tc else None
+        if clocks:
+            clocks.start()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps or 10)]
+        for e0, e1 in ev:
+            e0.record(stream)
+            call()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        if clocks:
+            clk = clocks.stop()
+        ms = [e0.elapsed_time(e1) for e0, e1 in ev]
+        med = statistics.median(ms)
+        out[name] = {"ms": med, "rows_per_s": m / (med / 1e3),
+                     "tflops": flops / (med / 1e3) / 1e12,
+                     "frac_of_measured_bf16_peak": flops / (med / 1e3) / 1e12 / peak}
+    lib.sed_sur_set_stream(sur.h, None)
+    sur.close()
+    fast = out["tcgen05_fused"]
+    line = {"metric": MLP_METRIC, "value": fast.get("rows_per_s"), "unit": "rows/s",
+            "n_gpus": 1, "steps": args.steps or 10, "warmup": args.warmup,
+            "ms_per_step": fast.get("ms"), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16", "data": "synthetic (random weights and rows)",
+            "config": {"workload": "surrogate_mlp_2048x2048", "rows": m,
+                       "network": "343->256x4->330 (padded 384/384)",
+                       "flops_per_row": mlp_flops_per_row(K),
+                       "l2": "inputs larger than L2 (rows 2.2 GB)"},
+            "roofline": {"bound": "tensor", "achieved": fast.get("tflops"), "peak": peak,
+                         "unit": "TFLOP/s",
+                         "frac": fast.get("frac_of_measured_bf16_peak"),
+                         "peak_kind": "measured (cuBLAS bf16 burst)"},
+            "engines": out, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def run_spinup(args) -> None:
     """Spin-up of the reference's 1-column model (sed1d, hourly steps for
     --spinup-years) through sed_spinup's column mode, against the oracle's
@@ -1417,7 +1513,10 @@ def main():
     ap.add_argument("--spinup-cpu-steps", type=int, default=2000)
     ap.add_argument("--ensemble", type=int, default=0,
                     help="with --spinup-years: spin up this many parameter sets at once")
-    ap.add_argument("--path", default="sediment", choices=["sediment", "pelagic", "coupling"],
+    ap.add_argument("--mlp-rows", type=int, default=2936778,
+                    help="--path mlp: rows of the inference batch")
+    ap.add_argument("--path", default="sediment",
+                    choices=["sediment", "pelagic", "coupling", "mlp"],
                     help="pelagic: the fabm_pelagic driver path instead; coupling: the "
                          "pelagic -> soil connector")
     ap.add_argument("--cpl-cpu-seconds", type=float, default=8.0,
@@ -1431,6 +1530,9 @@ def main():
                 and args.spinup_years <= 0)
     if not args.workload:
         args.workload = HEADLINE if headline else WORKLOAD
+    if args.path == "mlp":
+        run_mlp(args)
+        return
     if args.path == "pelagic":
         if args.impl == "reference":
             run_reference_pelagic(args)

@@ -1373,7 +1373,8 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
   CK(h->d_gate.alloc(128), "heavy counter");
   CK(h->d_xfeat.alloc((size_t)maxrows * s->pin[0] * sizeof(bf16)), "features");
   CK(h->d_yhat.alloc((size_t)maxrows * s->pout[s->L - 1] * sizeof(float)), "predictions");
-  CK(h->d_act.alloc((size_t)2 * maxrows * s->pout[0] * sizeof(bf16)), "activations");
+  if (!sur_uses_tc(s))
+    CK(h->d_act.alloc((size_t)2 * maxrows * s->pout[0] * sizeof(bf16)), "activations");
   const long long l0 = h->launches;
   if ((rc = stats_reset(h))) return rc;
   Params<float> p = make_params<float>(h->prm);
@@ -1410,6 +1411,8 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
     rc = sur_infer_rows(s, h->d_xfeat.as<bf16>(), h->d_yhat.as<float>(), rows, act0, act1,
                         h->stream);
     if (rc) return h->fail(rc, "surrogate forward: %s", s->err.c_str());
+    // one fused kernel, or one GEMM per layer
+    h->launches -= sur_uses_tc(s) ? s->L - 1 : 0;
     CK(sur::apply(h->d_yhat.as<float>(), h->d_conc.as<float>(), s->norm, list, nh, K, h->kmax,
                   h->nslot, s->nin, s->nout, s->pout[s->L - 1], h->d_prop.as<float>(),
                   h->stream),
@@ -1435,7 +1438,10 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
     h->launches += 2;
   }
   CK(cudaEventRecord(h->ev1, h->stream), "event");
-  return stats_fetch(h, stats, l0, true);
+  rc = stats_fetch(h, stats, l0, true);
+  if (rc) return rc;
+  if (sur_uses_tc(s) && (rc = sur_check_tc(s))) return h->fail(rc, "%s", s->err.c_str());
+  return SED_OK;
 }
 
 int sed_sur_collect(sed_handle* h, const float* c0, double dt, float* x_dev, float* y_dev,

@@ -19,6 +19,7 @@
 #include "../../include/mossco_sed.h"
 #include "sur_internal.h"
 #include "sur_kernels.h"
+#include "sur_tc.h"
 
 #define SCK(expr, what)                                                        \
   do {                                                                         \
@@ -41,8 +42,24 @@ int sur_forward_rows(sed_surrogate* s, int m) {
   return SED_OK;
 }
 
+bool sur_uses_tc(const sed_surrogate* s) { return s->use_tc && sur::tc_supported(s); }
+
+int sur_check_tc(sed_surrogate* s) {
+  int e = 0;
+  SCK(cudaMemcpy(&e, s->d_err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+  if (e) {
+    cudaMemset(s->d_err, 0, sizeof(int));
+    return s->fail(SED_E_CUDA, "tensor-core MLP kernel gave up waiting (code %d)", e);
+  }
+  return SED_OK;
+}
+
 int sur_infer_rows(sed_surrogate* s, const bf16* x, float* y, int m, bf16* act0, bf16* act1,
                    cudaStream_t st) {
+  if (sur_uses_tc(s)) {
+    SCK(sur::infer_tc(s, x, y, m, s->d_err, st), "tensor-core inference");
+    return SED_OK;
+  }
   const bf16* in = x;
   for (int l = 0; l < s->L; l++) {
     const bool last = l == s->L - 1;
@@ -136,8 +153,9 @@ int sed_sur_create(int nin, int nout, int hidden, int nhidden, int max_batch,
   s->max_batch = pad128(max_batch);
   auto bail = [&](int rc) { delete s; return rc; };
   if (cudaSetDevice(device) != cudaSuccess) return bail(SED_E_CUDA);
-  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking) != cudaSuccess)
     return bail(SED_E_CUDA);
+  s->stream = s->own_stream;
   int maxd = 0;
   for (int l = 0; l < s->L; l++) {
     s->din[l] = l == 0 ? nin : hidden;
@@ -163,7 +181,7 @@ int sed_sur_create(int nin, int nout, int hidden, int nhidden, int max_batch,
        s->alloc(&s->dz, B * maxd) == cudaSuccess && s->alloc(&s->dz2, B * maxd) == cudaSuccess &&
        s->alloc(&s->dzt, B * maxd) == cudaSuccess && s->alloc(&s->at, B * maxd) == cudaSuccess &&
        s->alloc(&s->mask, (size_t)s->pout[s->L - 1]) == cudaSuccess &&
-       s->alloc(&s->loss, 4) == cudaSuccess;
+       s->alloc(&s->loss, 4) == cudaSuccess && s->alloc(&s->d_err, 1) == cudaSuccess;
   if (!ok) return bail(SED_E_NOMEM);
   // output mask; initial weights U(-1/sqrt(in), 1/sqrt(in)), zero biases
   std::vector<float> mask(s->pout[s->L - 1], 0.0f);
@@ -264,6 +282,14 @@ int sed_sur_forward(sed_surrogate* s, const float* x, float* y, int m) {
 int sed_sur_forward_device(sed_surrogate* s, const void* x_dev, void* y_dev, int m) {
   if (!s || !x_dev || !y_dev || m <= 0 || m % 128) return SED_E_ARG;
   SCK(cudaSetDevice(s->device), "set device");
+  if (sur_uses_tc(s)) {
+    // the fused kernel reads and writes the caller's rows directly
+    int rc = sur_infer_rows(s, static_cast<const bf16*>(x_dev), static_cast<float*>(y_dev), m,
+                            nullptr, nullptr, s->stream);
+    if (rc) return rc;
+    SCK(cudaStreamSynchronize(s->stream), "forward");
+    return sur_check_tc(s);
+  }
   const int nlast = s->pout[s->L - 1];
   for (int r0 = 0; r0 < m; r0 += s->max_batch) {
     const int mm = std::min(s->max_batch, m - r0);
@@ -323,6 +349,20 @@ int sed_sur_grads(sed_surrogate* s, const float* x, const float* y, int m, float
   if ((rc = backward(s, mp, m))) return rc;
   if (loss) SCK(cudaMemcpyAsync(loss, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->stream), "loss");
   return fetch_params(s, s->gw, s->gb, grads);
+}
+
+int sed_sur_set_stream(sed_surrogate* s, void* stream) {
+  if (!s) return SED_E_ARG;
+  SCK(cudaSetDevice(s->device), "set device");
+  SCK(cudaStreamSynchronize(s->stream), "stream switch");
+  s->stream = stream ? static_cast<cudaStream_t>(stream) : s->own_stream;
+  return SED_OK;
+}
+
+int sed_sur_set_tensor_cores(sed_surrogate* s, int on) {
+  if (!s) return SED_E_ARG;
+  s->use_tc = on != 0;
+  return sur_uses_tc(s) ? 1 : 0;
 }
 
 const char* sed_sur_last_error(const sed_surrogate* s) { return s ? s->err.c_str() : ""; }

@@ -18,7 +18,8 @@ inline int pad128(int x) { return (x + 127) / 128 * 128; }
 
 struct sed_surrogate {
   int device = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;      // stream in use
+  cudaStream_t own_stream = nullptr;  // stream created by the handle
   int nin = 0, nout = 0, hidden = 0, nhidden = 0, L = 0, max_batch = 0;
   int din[kSurMaxLayers], dout[kSurMaxLayers], pin[kSurMaxLayers], pout[kSurMaxLayers];
   float *w[kSurMaxLayers] = {}, *b[kSurMaxLayers] = {}, *gw[kSurMaxLayers] = {}, *gb[kSurMaxLayers] = {};
@@ -33,6 +34,10 @@ struct sed_surrogate {
   // c0[11] | mu_x[nin] | sd_x[nin] | mu_d[nout] | sd_d[nout]
   float* norm = nullptr;
   int norm_len = 0;
+  // inference on the tcgen05 fused kernel (when the shape fits) or on the
+  // mma.sync GEMMs; d_err: the fused kernel's barrier-timeout code
+  bool use_tc = true;
+  int* d_err = nullptr;
   std::vector<void*> allocs;
   std::string err;
 
@@ -60,7 +65,7 @@ struct sed_surrogate {
     cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
     for (void* p : allocs) cudaFree(p);
-    if (stream) cudaStreamDestroy(stream);
+    if (own_stream) cudaStreamDestroy(own_stream);
   }
 };
 
@@ -68,6 +73,13 @@ struct sed_surrogate {
 // forward pass over m rows already in s->x; output pre-activation in z[L-1]
 int sur_forward_rows(sed_surrogate* s, int m);
 // inference over m rows (a multiple of 128): x BF16 [m][pin[0]] -> y FP32
-// [m][pout[L-1]], hidden activations in act0 / act1 (BF16 [m][hidden padded])
+// [m][pout[L-1]]: the fused tcgen05 kernel when s->use_tc and the shape
+// fits, else the mma.sync GEMMs with the hidden activations in act0 / act1
+// (BF16 [m][hidden padded]; unused by the fused kernel, may be null then)
 int sur_infer_rows(sed_surrogate* s, const bf16* x, float* y, int m, bf16* act0, bf16* act1,
                    cudaStream_t st);
+// whether sur_infer_rows takes the fused tcgen05 kernel
+bool sur_uses_tc(const sed_surrogate* s);
+// the fused kernel's error flag: reset before, checked after a synchronised
+// call (SED_E_CUDA with a message when the kernel gave up waiting)
+int sur_check_tc(sed_surrogate* s);

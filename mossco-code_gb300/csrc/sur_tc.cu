@@ -1,0 +1,433 @@
+// sur_tc.cu -- the surrogate network's inference pass on the 5th-generation
+// tensor cores: one fused kernel for the whole MLP (all layers, bias and
+// GELU), tcgen05.mma with accumulators in tensor memory (TMEM), operands
+// staged in shared memory by TMA (cp.async.bulk.tensor) with the 128-byte
+// swizzle the MMA descriptors read.
+//
+// A persistent CTA per SM walks tiles of 128 rows.  Per tile:
+//   X tile [128][K0] (BF16)  --TMA-->  shared memory (6 chunks of 64 columns)
+//   layer l: acc[128][N_l] (FP32, TMEM) = A[128][K_l] . W_l^T, the weights
+//            streamed through a ring of NST stages of [256][64] by TMA
+//   epilogue: acc + b, GELU -> BF16 back into the same shared buffer, in
+//            the swizzled layout of the next layer's A operand; the last
+//            layer's acc + b goes to global memory (FP32 rows).
+// Roles (192 threads): warps 0-3 run the epilogue (warp w reads TMEM lanes
+// 32w..32w+31, one row per thread), warp 4 issues the TMA loads, warp 5
+// issues the MMAs.  Every wait on an mbarrier is bounded: after ~1 s the
+// kernel records an error code, stops issuing work, waits (bounded) for its
+// outstanding copies and MMAs, frees its TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "sur_internal.h"
+#include "sur_tc.h"
+
+namespace sur {
+namespace tc {
+
+constexpr int BM = 128;                  // rows per tile (MMA M)
+constexpr int BK = 64;                   // K per chunk: 128 bytes of BF16
+constexpr int CHUNK = BM * BK * 2;       // one [128][64] BF16 box: 16 KB
+constexpr int KMAX0 = 384;               // widest input the X buffer holds
+constexpr int XBUF = (KMAX0 / BK) * CHUNK;  // 96 KB
+constexpr int STAGE = 2 * CHUNK;         // [256][64] weights: 32 KB
+constexpr int NST = 3;                   // weight ring stages
+constexpr int HID = 256;                 // hidden width (TMEM columns used)
+constexpr int TMEM_COLS = 512;
+constexpr int NTHREADS = 192;
+constexpr long long WAIT_CYCLES = 2000000000ll;  // ~1 s at 2 GHz
+
+struct Layers {
+  CUtensorMap w[kSurMaxLayers];  // [nout][nin] BF16, box [128][64]
+  const float* bias[kSurMaxLayers];
+  int nout[kSurMaxLayers];
+  int L, k0;
+};
+
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t saddr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Bounded wait: false (with the error recorded) when the phase does not
+// complete within WAIT_CYCLES or another role has given up.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort,
+                                          int* err, int code) {
+  const long long t0 = clock64();
+  for (;;) {
+    if (mbar_test(bar, parity)) return true;
+    if (*abort) return false;
+    if (clock64() - t0 > WAIT_CYCLES) {
+      *abort = 1;
+      atomicCAS(err, 0, code);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major operand in the 128-byte
+// swizzled layout TMA writes: rows of 128 bytes, 8-row atoms of 1024 bytes
+// (stride byte offset 1024), descriptor version 1, swizzle mode 2.
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulation, BF16 A and B,
+// both K-major, M = 128, N = n.
+__device__ __forceinline__ uint32_t idesc_bf16(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// 32 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// tanh form of GELU with the hardware tanh approximation
+__device__ __forceinline__ float gelu_fast(float z) {
+  const float u = 0.7978845608028654f * fmaf(0.044715f * z * z, z, z);
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+  return 0.5f * z * (1.0f + t);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&h);
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers P,
+         float* __restrict__ y, int ldy, int ntiles, int* err) {
+  extern __shared__ unsigned char smem_raw[];
+  // 1024-byte alignment for the swizzle atoms
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  unsigned char* xbuf = smem;                 // X tile, then the activations
+  unsigned char* wbuf = smem + XBUF;          // weight ring
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + XBUF + NST * STAGE);
+  // bars: full[NST], empty[NST], xfull, xempty, accfull, epidone
+  __shared__ uint32_t s_tmem;
+  __shared__ volatile int s_abort;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t b_full = saddr(bars), b_empty = saddr(bars + NST);
+  const uint32_t b_xfull = saddr(bars + 2 * NST), b_xempty = saddr(bars + 2 * NST + 1);
+  const uint32_t b_acc = saddr(bars + 2 * NST + 2), b_epi = saddr(bars + 2 * NST + 3);
+
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    for (int i = 0; i < NST; i++) {
+      mbar_init(b_full + 8 * i, 1);
+      mbar_init(b_empty + 8 * i, 1);
+    }
+    mbar_init(b_xfull, 1);
+    mbar_init(b_xempty, 1);
+    mbar_init(b_acc, 1);
+    mbar_init(b_epi, 4 * 32);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     saddr(&s_tmem)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (warp == 4 && lane == 0) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tx)) : "memory");
+    for (int l = 0; l < P.L; l++)
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&P.w[l]))
+                   : "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = s_tmem;
+
+  if (warp == 4) {
+    // ---- TMA producer (one lane)
+    if (lane == 0) {
+      uint32_t g = 0;   // weight chunks issued
+      uint32_t it = 0;  // tiles issued
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, it++) {
+        if (it > 0) ok = mbar_wait(b_xempty, (it - 1) & 1, &s_abort, err, 1);
+        if (!ok) break;
+        mbar_expect_tx(b_xfull, (uint32_t)(P.k0 / BK) * CHUNK);
+        for (int kc = 0; kc < P.k0 / BK; kc++)
+          tma_load_2d(saddr(xbuf + kc * CHUNK), &tx, kc * BK, tile * BM, b_xfull);
+        for (int l = 0; l < P.L && ok; l++) {
+          const int K = l == 0 ? P.k0 : HID;
+          for (int n0 = 0; n0 < P.nout[l] && ok; n0 += HID) {
+            const int nn = min(HID, P.nout[l] - n0);
+            for (int kc = 0; kc < K / BK; kc++, g++) {
+              const uint32_t s = g % NST;
+              if (g >= NST) {
+                ok = mbar_wait(b_empty + 8 * s, ((g / NST) - 1) & 1, &s_abort, err, 2);
+                if (!ok) break;
+              }
+              mbar_expect_tx(b_full + 8 * s, (uint32_t)nn * BK * 2);
+              for (int r = 0; r < nn; r += BM)
+                tma_load_2d(saddr(wbuf + s * STAGE + r * BK * 2), &P.w[l], kc * BK, n0 + r,
+                            b_full + 8 * s);
+            }
+          }
+        }
+      }
+      if (!ok) {
+        // let the copies already issued land before the CTA's memory goes
+        for (uint32_t k = 0; k < NST && k < g; k++) {
+          const uint32_t gg = g - 1 - k, s = gg % NST;
+          const long long t0 = clock64();
+          while (!mbar_test(b_full + 8 * s, (gg / NST) & 1) && clock64() - t0 < WAIT_CYCLES) {
+          }
+        }
+      }
+    }
+  } else if (warp == 5) {
+    // ---- MMA issuer (one lane)
+    if (lane == 0) {
+      uint32_t g = 0, it = 0, e = 0;
+      bool ok = true, issued = false;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, it++) {
+        ok = mbar_wait(b_xfull, it & 1, &s_abort, err, 3);
+        for (int l = 0; l < P.L && ok; l++) {
+          if (it > 0 || l > 0) {
+            // the previous layer's epilogue: A operand written, TMEM read
+            ok = mbar_wait(b_epi, e & 1, &s_abort, err, 4);
+            e++;
+            if (!ok) break;
+          }
+          fence_after();
+          const int K = l == 0 ? P.k0 : HID;
+          for (int n0 = 0; n0 < P.nout[l] && ok; n0 += HID) {
+            const int nn = min(HID, P.nout[l] - n0);
+            const uint32_t idesc = idesc_bf16(nn);
+            for (int kc = 0; kc < K / BK; kc++, g++) {
+              const uint32_t s = g % NST;
+              ok = mbar_wait(b_full + 8 * s, (g / NST) & 1, &s_abort, err, 5);
+              if (!ok) break;
+              fence_after();
+              const uint32_t a0 = saddr(xbuf + kc * CHUNK);
+              const uint32_t b0 = saddr(wbuf + s * STAGE);
+#pragma unroll
+              for (int k = 0; k < BK / 16; k++)
+                mma_bf16(tmem + (uint32_t)n0, desc_sw128(a0 + 32 * k), desc_sw128(b0 + 32 * k),
+                         idesc, (kc > 0 || k > 0) ? 1u : 0u);
+              mma_commit(b_empty + 8 * s);  // the stage is free once these complete
+              issued = true;
+            }
+          }
+          if (ok) mma_commit(b_acc);  // the layer's accumulator is complete
+        }
+        if (ok) mma_commit(b_xempty);  // the A buffer is free for the next tile
+      }
+      if (issued) {
+        // the MMAs in flight complete before the TMEM is released
+        const long long t0 = clock64();
+        while (!mbar_test(b_empty + 8 * ((g - 1) % NST), ((g - 1) / NST) & 1) &&
+               clock64() - t0 < WAIT_CYCLES) {
+        }
+      }
+    }
+  } else {
+    // ---- epilogue (warps 0-3: one row per thread)
+    const int row = warp * 32 + lane;
+    const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+    uint32_t a = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      for (int l = 0; l < P.L; l++) {
+        ok = mbar_wait(b_acc, a & 1, &s_abort, err, 6);
+        a++;
+        if (!ok) break;
+        fence_after();
+        const bool last = l == P.L - 1;
+        const float* bias = P.bias[l];
+        for (int c0 = 0; c0 < P.nout[l]; c0 += 32) {
+          float v[32];
+          tmem_ld32(tl + (uint32_t)c0, v);
+#pragma unroll
+          for (int i = 0; i < 32; i += 4) {
+            const float4 b = __ldg(reinterpret_cast<const float4*>(bias + c0 + i));
+            v[i] += b.x;
+            v[i + 1] += b.y;
+            v[i + 2] += b.z;
+            v[i + 3] += b.w;
+          }
+          if (last) {
+            float* dst = y + (size_t)(tile * BM + row) * ldy + c0;
+#pragma unroll
+            for (int i = 0; i < 32; i += 4)
+              *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+          } else {
+            // BF16 GELU into the next layer's A operand: chunk c0/64, row
+            // `row`, 16-byte pieces j0..j0+3 at (j ^ row % 8)
+            unsigned char* rbase = xbuf + (c0 / BK) * CHUNK + row * 128;
+            const int j0 = (c0 % BK) / 8;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              uint4 w;
+              w.x = pack_bf16(gelu_fast(v[8 * q + 0]), gelu_fast(v[8 * q + 1]));
+              w.y = pack_bf16(gelu_fast(v[8 * q + 2]), gelu_fast(v[8 * q + 3]));
+              w.z = pack_bf16(gelu_fast(v[8 * q + 4]), gelu_fast(v[8 * q + 5]));
+              w.w = pack_bf16(gelu_fast(v[8 * q + 6]), gelu_fast(v[8 * q + 7]));
+              *reinterpret_cast<uint4*>(rbase + (((j0 + q) ^ (row & 7)) << 4)) = w;
+            }
+          }
+        }
+        fence_before();
+        if (!last) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive(b_epi);
+      }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// [rows][cols] BF16 (row pitch cols), boxes of [128 rows][64 columns],
+// 128-byte swizzle
+bool encode_bf16(CUtensorMap* m, const void* base, int rows, int cols) {
+  auto fn = encoder();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)BM};
+  cuuint32_t estr[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
+
+size_t smem_bytes() { return 1024 + XBUF + NST * STAGE + 8 * (2 * NST + 4); }
+
+}  // namespace tc
+
+bool tc_supported(const sed_surrogate* s) {
+  if (s->L < 2 || s->L > kSurMaxLayers) return false;
+  if (s->pin[0] % tc::BK || s->pin[0] > tc::KMAX0) return false;
+  for (int l = 0; l < s->L - 1; l++)
+    if (s->pout[l] != tc::HID) return false;
+  for (int l = 1; l < s->L; l++)
+    if (s->pin[l] != tc::HID) return false;
+  const int nlast = s->pout[s->L - 1];
+  return nlast % 128 == 0 && nlast <= tc::TMEM_COLS && tc::encoder() != nullptr;
+}
+
+cudaError_t infer_tc(sed_surrogate* s, const __nv_bfloat16* x, float* y, int m, int* err,
+                     cudaStream_t st) {
+  if (m <= 0 || m % tc::BM || !tc_supported(s)) return cudaErrorInvalidValue;
+  tc::Layers P{};
+  P.L = s->L;
+  P.k0 = s->pin[0];
+  for (int l = 0; l < s->L; l++) {
+    if (!tc::encode_bf16(&P.w[l], s->wb[l], s->pout[l], s->pin[l])) return cudaErrorInvalidValue;
+    P.bias[l] = s->b[l];
+    P.nout[l] = s->pout[l];
+  }
+  CUtensorMap tx;
+  if (!tc::encode_bf16(&tx, x, m, s->pin[0])) return cudaErrorInvalidValue;
+  const size_t smem = tc::smem_bytes();
+  cudaError_t e = cudaFuncSetAttribute(tc::k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int ntiles = m / tc::BM;
+  const int grid = std::max(1, std::min(ntiles, sms));
+  tc::k_mlp_tc<<<grid, tc::NTHREADS, smem, st>>>(tx, P, y, s->pout[s->L - 1], ntiles, err);
+  return cudaGetLastError();
+}
+
+}  // namespace sur

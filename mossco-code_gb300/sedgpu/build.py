@@ -25,7 +25,7 @@ SOURCES = ["sed_kernels_f32.cu", "sed_kernels_f64.cu", "sed_kernels_f32_bio3.cu"
            "sed_kernels_f64_bio3.cu", "sed_kernels_warp.cu", "sed_kernels_warp_bio3.cu",
            "sed_capi.cu", "sed_noalloc.cu", "sur_kernels.cu", "sur_capi.cu", "sur_loop.cu",
            "sed_kernels_warp_ens.cu", "sed_kernels_warp_ens_bio3.cu", "pel_capi.cu",
-           "cpl_capi.cu"]
+           "cpl_capi.cu", "sur_tc.cu"]
 # The FP64 kernels evaluate the reference's arithmetic operation by
 # operation: no multiply-add contraction.
 # The FP32 kernels write every fused multiply-add explicitly (fmaf): without
@@ -43,7 +43,7 @@ EXTRA_FLAGS = {"sed_kernels_f64.cu": ["-fmad=false"],
                "cpl_capi.cu": ["-fmad=false"]}
 HEADERS = ["sed_device.cuh", "sed_kernels.cuh", "sed_launch.h", "sed_params.h",
            "sur_kernels.h", "sur_internal.h", "sur_loop.h", "cpl_internal.h",
-           "cpl_map.cuh"]
+           "cpl_map.cuh", "sur_tc.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no multiply-add contraction either (aarch64 g++ contracts by
 # default), so host-side FP64 forcing rows match the CPU restatement's

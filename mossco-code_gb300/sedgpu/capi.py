@@ -153,6 +153,8 @@ SIGNATURES = {
                                           ctypes.c_float, _fp]),
     "sed_sur_grads": (ctypes.c_int, [_H, _fp, _fp, ctypes.c_int, _fp, _fp]),
     "sed_sur_last_error": (ctypes.c_char_p, [_H]),
+    "sed_sur_set_tensor_cores": (ctypes.c_int, [_H, ctypes.c_int]),
+    "sed_sur_set_stream": (ctypes.c_int, [_H, _vp]),
     "sed_sur_destroy": (None, [_H]),
     "sed_sur_set_norm": (ctypes.c_int, [_H, _fp, ctypes.c_int]),
     "sed_step_surrogate": (ctypes.c_int, [_H, _H, ctypes.c_double, ctypes.c_int,

@@ -128,3 +128,62 @@ def test_gpu_training_reduces_loss():
         assert losses[-1] < 0.33 * losses[0], losses
     finally:
         lib.sed_sur_destroy(h)
+
+
+def _device_forward(lib, h, x, tc):
+    """sed_sur_forward_device on BF16 rows of x with the fused tcgen05
+    kernel (tc) or the mma.sync GEMMs; returns the FP32 outputs."""
+    import torch
+    m = x.shape[0]
+    xp = np.zeros((m, 384), dtype=np.float32)
+    xp[:, :x.shape[1]] = x
+    xd = torch.tensor(xp, device="cuda").to(torch.bfloat16).contiguous()
+    yd = torch.zeros((m, 384), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    assert lib.sed_sur_set_tensor_cores(h, 1 if tc else 0) == (1 if tc else 0)
+    rc = lib.sed_sur_forward_device(h, ctypes.c_void_p(xd.data_ptr()),
+                                    ctypes.c_void_p(yd.data_ptr()), m)
+    assert rc == 0, lib.sed_sur_last_error(h)
+    return yd[:, :SHAPE["nout"]].cpu().numpy().astype(np.float64)
+
+
+@pytest.mark.gpu
+def test_tensor_core_inference_matches_fp64_reference():
+    """The fused tcgen05 inference kernel (TMEM accumulators, TMA-staged
+    operands) against the FP64 MLP on the same BF16-rounded operands, at the
+    bar of the GEMM path above; and against the GEMM path on a batch of 400
+    tiles of 128 rows, so that every CTA of the persistent grid walks
+    several tiles through its barrier phases."""
+    lib, h = _sur(**SHAPE, batch=256, seed=5)
+    try:
+        shapes = M.layer_shapes(**SHAPE)
+        n = lib.sed_sur_num_params(h)
+        rng = np.random.default_rng(3)
+        params = rng.normal(0, 1, n).astype(np.float32)
+        o = 0
+        for r, c in shapes:
+            params[o:o + r * c] *= 1.0 / np.sqrt(c)
+            params[o + r * c:o + r * c + r] *= 0.1
+            o += r * c + r
+        assert lib.sed_sur_set_weights(h, _fp(params)) == 0
+        pb = params.astype(np.float64).copy()
+        o = 0
+        for r, c in shapes:
+            pb[o:o + r * c] = M.bf16_round(params[o:o + r * c])
+            o += r * c + r
+        x = rng.normal(0, 1, (256, SHAPE["nin"])).astype(np.float32)
+        yref, _, _ = M.forward(pb, shapes, M.bf16_round(x))
+        for tc in (True, False):
+            yg = _device_forward(lib, h, x, tc)
+            rel = np.linalg.norm(yg - yref) / np.linalg.norm(yref)
+            assert rel < 1e-2, (tc, rel)
+        xl = rng.normal(0, 1, (128 * 400, SHAPE["nin"])).astype(np.float32)
+        a = _device_forward(lib, h, xl, True)
+        b = _device_forward(lib, h, xl, False)
+        rel = np.linalg.norm(a - b) / np.linalg.norm(b)
+        assert rel < 1e-2, rel
+        # row by row: no tile is missing or misplaced
+        rrow = np.linalg.norm(a - b, axis=1) / np.linalg.norm(b, axis=1)
+        assert rrow.max() < 5e-2, rrow.max()
+    finally:
+        lib.sed_sur_destroy(h)
