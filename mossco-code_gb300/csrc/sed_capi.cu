@@ -1389,11 +1389,12 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
     //    are done, exactly as the plain step; the others are listed
     CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
     CK(cudaMemsetAsync(nheavy, 0, sizeof(unsigned), h->stream), "counter reset");
+    // (the tile kernel: one attempt per column is uniform work, staged with
+    // coalesced loads, one list reservation per tile)
     ColumnArgs<float> a = column_args<float>(h, bin, b, dt, SED_ADAPTIVE_EULER);
-    a.ntiles = bin.nslots;
     a.heavy = list;
     a.nheavy = nheavy;
-    CK(launch_warp_columns(h, a, p, bin, KIND_PROBE), "gate launch");
+    CK(launch_bin<float>(h, a, p, bin, KIND_PROBE, h->stream), "gate launch");
     h->launches++;
     CK(cudaMemcpyAsync(h->h_count, nheavy, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream),
        "counter copy");

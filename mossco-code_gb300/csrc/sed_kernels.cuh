@@ -606,6 +606,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
   double* s_bud = reinterpret_cast<double*>(smem + L.bud);
   int* s_nsub = reinterpret_cast<int*>(smem + L.nsub);
   __shared__ int s_tile, s_next;
+  __shared__ int s_heavy[64];  // KIND_PROBE: the tile's columns the gate rejects
   __shared__ unsigned long long b_att, b_acc, b_cols, b_mindt;
   __shared__ int b_maxatt, b_cap, b_nan;
 
@@ -641,6 +642,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       j = __shfl_sync(FULL, j, 0);
       if (j >= tc) break;
       const int K = a.kact[slot0 + j];
+      if (KIND == KIND_PROBE && lane == 0) s_heavy[j] = 0;
       if (K <= 0) {
         if (lane == 0) {
           s_nsub[j] = 0;
@@ -678,12 +680,26 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       }
       double bud[4] = {0.0, 0.0, 0.0, 0.0};
       ColResult r;
-      if (KIND == KIND_ADAPT)
-        r = p.ticks ? solve_adaptive<real, LPL, BC4, BIO3, true>(p, lc, lane, K, C, ftop, a.dt, bud)
-                    : solve_adaptive<real, LPL, BC4, BIO3, false>(p, lc, lane, K, C, ftop, a.dt, bud);
+      constexpr bool PROBE = KIND == KIND_PROBE;
+      if (KIND == KIND_ADAPT || PROBE)
+        r = p.ticks ? solve_adaptive<real, LPL, BC4, BIO3, true, PROBE>(p, lc, lane, K, C, ftop,
+                                                                       a.dt, bud)
+                    : solve_adaptive<real, LPL, BC4, BIO3, false, PROBE>(p, lc, lane, K, C, ftop,
+                                                                        a.dt, bud);
       else
         r = solve_fixed<real, LPL, BC4, BIO3>(p, lc, lane, K, C, ftop, a.dt, a.method,
                                               bud);
+      if (PROBE && r.attempts < 0) {
+        // the gate rejects the column: its staged state goes back as it was
+        if (lane == 0) {
+          s_heavy[j] = 1;
+          s_nsub[j] = 0;
+#pragma unroll
+          for (int d = 0; d < NDISS; d++) s_sflux[d * tcp + j] = real(0);
+          for (int b = 0; b < 4; b++) s_bud[b * tc + j] = 0.0;
+        }
+        continue;
+      }
 #pragma unroll
       for (int s = 0; s < LPL; s++) {
         const int Ll = s * 32 + lane;
@@ -708,6 +724,16 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       }
     }
     __syncthreads();
+    if (KIND == KIND_PROBE && tid == 0) {
+      // the tile's rejected columns into the list: one reservation per tile
+      int n = 0;
+      for (int q = 0; q < tc; q++) n += s_heavy[q];
+      if (n > 0) {
+        unsigned at = atomicAdd(a.nheavy, (unsigned)n);
+        for (int q = 0; q < tc; q++)
+          if (s_heavy[q]) a.heavy[at++] = slot0 + q;
+      }
+    }
     // stage out
     real* dst = (mode == 1) ? a.out : a.conc;
     copy_grouped<real, false>(s_conc, dst + slot0, NTR, kt, KT, a.kmax, ns, tc,
@@ -854,15 +880,12 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
 #pragma unroll
       for (int n = 0; n < NTR; n++) ftop[n] = real(0);
       for (int b = 0; b < 4; b++) bud[b] = 0.0;
-      constexpr bool PROBE = KIND == KIND_PROBE;
-      if (KIND == KIND_ADAPT || PROBE)
-        r = pc.ticks ? solve_adaptive<real, LPL, BC4, BIO3, true, PROBE>(pc, lc, lane, K, C, ftop,
-                                                                        a.dt, bud)
-                     : solve_adaptive<real, LPL, BC4, BIO3, false, PROBE>(pc, lc, lane, K, C, ftop,
-                                                                         a.dt, bud);
+      if (KIND == KIND_ADAPT)
+        r = pc.ticks
+                ? solve_adaptive<real, LPL, BC4, BIO3, true>(pc, lc, lane, K, C, ftop, a.dt, bud)
+                : solve_adaptive<real, LPL, BC4, BIO3, false>(pc, lc, lane, K, C, ftop, a.dt, bud);
       else
         r = solve_fixed<real, LPL, BC4, BIO3>(pc, lc, lane, K, C, ftop, a.dt, a.method, bud);
-      if (PROBE && r.attempts < 0) break;
       if (lane == 0) {
         atomicAdd(&b_att, (unsigned long long)r.attempts);
         atomicAdd(&b_acc, (unsigned long long)r.accepted);
@@ -873,11 +896,6 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
         if (r.accepted > 0)
           atomicMin(&b_mindt, (unsigned long long)__double_as_longlong(r.min_dt));
       }
-    }
-    if (KIND == KIND_PROBE && r.attempts < 0) {
-      // first attempt rejected: a heavy column, left as it was
-      if (lane == 0) a.heavy[atomicAdd(a.nheavy, 1u)] = slot;
-      continue;
     }
 #pragma unroll
     for (int s = 0; s < LPL; s++) {
@@ -1273,6 +1291,11 @@ cudaError_t launch_column_k(const ColumnArgs<real>& a, const Params<real>& p,
     return launch_column_t<real, LPL, BC4, BIO3, KIND_ADAPT>(a, p, blocks, threads, st);
   if (kind == KIND_FIXED)
     return launch_column_t<real, LPL, BC4, BIO3, KIND_FIXED>(a, p, blocks, threads, st);
+  if (kind == KIND_PROBE) {
+    if constexpr (std::is_same<real, float>::value)
+      return launch_column_t<real, LPL, BC4, BIO3, KIND_PROBE>(a, p, blocks, threads, st);
+    return cudaErrorInvalidValue;
+  }
   return launch_column_t<real, LPL, BC4, BIO3, KIND_RHS>(a, p, blocks, threads, st);
 }
 
@@ -1323,6 +1346,11 @@ template <typename real, int LPL, bool BC4, bool BIO3>
 int occupancy_k(int tc, int kind, int threads) {
   if (kind == KIND_ADAPT) return occupancy_t<real, LPL, BC4, BIO3, KIND_ADAPT>(tc, threads);
   if (kind == KIND_FIXED) return occupancy_t<real, LPL, BC4, BIO3, KIND_FIXED>(tc, threads);
+  if (kind == KIND_PROBE) {
+    if constexpr (std::is_same<real, float>::value)
+      return occupancy_t<real, LPL, BC4, BIO3, KIND_PROBE>(tc, threads);
+    return 0;
+  }
   return occupancy_t<real, LPL, BC4, BIO3, KIND_RHS>(tc, threads);
 }
 
@@ -1353,15 +1381,12 @@ static cudaError_t launch_warp_t(const ColumnArgs<real>& a, const Params<real>& 
 template <typename real, int LPL, bool BC4, bool BIO3, bool ENS>
 cudaError_t launch_warp_e(const ColumnArgs<real>& a, const Params<real>& p, int kind,
                           int blocks, int threads, cudaStream_t st) {
-  if (kind == KIND_PROBE || kind == KIND_RESID) {
-    // the surrogate step's gate and residual test: FP32 state, one set
+  if (kind == KIND_RESID) {
+    // the surrogate step's residual test: FP32 state, one parameter set
     if constexpr (std::is_same<real, float>::value && !ENS) {
       if (a.nrepeat > 1) return cudaErrorInvalidValue;
-      return kind == KIND_PROBE
-                 ? launch_warp_t<real, LPL, BC4, BIO3, KIND_PROBE, false, ENS>(a, p, blocks,
-                                                                              threads, st)
-                 : launch_warp_t<real, LPL, BC4, BIO3, KIND_RESID, false, ENS>(a, p, blocks,
-                                                                              threads, st);
+      return launch_warp_t<real, LPL, BC4, BIO3, KIND_RESID, false, ENS>(a, p, blocks, threads,
+                                                                        st);
     }
     return cudaErrorInvalidValue;
   }

@@ -8,8 +8,8 @@
 
 namespace sed {
 
-// KIND_PROBE and KIND_RESID are the surrogate step's gate and residual test
-// (warp-direct kernel only)
+// KIND_PROBE and KIND_RESID are the surrogate step's gate (tile kernel) and
+// residual test (warp-direct kernel), FP32 state only
 enum : int { KIND_ADAPT = 0, KIND_FIXED = 1, KIND_RHS = 2, KIND_RESID = 3, KIND_PROBE = 4 };
 
 // Arguments of the tile kernel.  Device layouts (slot = compacted column):
@@ -44,8 +44,9 @@ struct ColumnArgs {
   int* skip;
   double res_tol, res_atol;
   // warp-direct kernel: the launch's columns are list[0 .. ntiles) (slots)
-  // instead of the slot range; KIND_PROBE appends the slot of every column
-  // whose first attempt was rejected to heavy[atomicAdd(nheavy, 1)]
+  // instead of the slot range.  KIND_PROBE (tile kernel) appends the slot of
+  // every column whose first attempt was rejected to heavy[], reserving each
+  // tile's entries with one atomicAdd on *nheavy
   const int* list;
   int* heavy;
   unsigned* nheavy;
