@@ -114,7 +114,7 @@ struct sed_handle {
   DevBuf d_bgc;  // [NBGC_DEV][nslot] derived per-slot rate parameters
   DevBuf d_slot_col, d_kact, d_tile_k, d_conc, d_coef, d_cap, d_force, d_sflux,
       d_budget, d_nsub, d_queue, d_stats, d_flag, d_stage, d_bdys, d_fluxes,
-      d_rhs, d_rhs_stage, d_grid, d_force64, d_prop, d_skip, d_xfeat, d_yhat, d_backup,
+      d_rhs, d_rhs_stage, d_grid, d_force64, d_skip, d_xfeat, d_yhat, d_backup,
       d_col_slot, d_top, d_bcin, d_mindt;
   // surrogate step: heavy-column slot list, its counter, hidden activations
   DevBuf d_list, d_gate, d_act;
@@ -1367,7 +1367,6 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
   const Bin& bin = h->bins[b];
   const size_t ns = h->nslot;
   const int maxrows = pad128(bin.nslots);
-  CK(h->d_prop.alloc((size_t)NTR * K * ns * sizeof(float)), "proposal");
   CK(h->d_skip.alloc(ns * sizeof(int)), "skip flags");
   CK(h->d_list.alloc((size_t)bin.nslots * sizeof(int)), "heavy list");
   CK(h->d_gate.alloc(128), "heavy counter");
@@ -1379,6 +1378,14 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
   if ((rc = stats_reset(h))) return rc;
   Params<float> p = make_params<float>(h->prm);
   set_clock(p, dt, h->prm.dt_min);
+  // the gate's tile kernel: the class's tile width (or, for a warp-direct
+  // class, the width its other kinds use); the occupancy query also raises
+  // the kernel's shared-memory limit, before any launch
+  const bool bc4 = h->prm.bcup_particulate == 4;
+  const int gate_tc = bin.tc ? bin.tc : bin.tc_fb;
+  const int gate_occ =
+      column_blocks_per_sm<float>(gate_tc, bin.lpl, bc4, KIND_PROBE, bin.threads, p.bio3 != 0);
+  if (gate_occ <= 0) return h->fail(SED_E_CUDA, "the gate's tile kernel does not fit");
   unsigned* nheavy = h->d_gate.as<unsigned>();
   int* list = h->d_list.as<int>();
   bf16* act0 = h->d_act.as<bf16>();
@@ -1394,7 +1401,16 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
     ColumnArgs<float> a = column_args<float>(h, bin, b, dt, SED_ADAPTIVE_EULER);
     a.heavy = list;
     a.nheavy = nheavy;
-    CK(launch_bin<float>(h, a, p, bin, KIND_PROBE, h->stream), "gate launch");
+    a.tc = gate_tc;
+    if (!bin.tc) {  // whole tiles of the class, all layers staged
+      a.tile_k = nullptr;
+      a.tile0 = 0;
+    }
+    a.ntiles = bin.nslots / gate_tc;
+    CK(launch_column<float>(a, p, bin.lpl, bc4, KIND_PROBE,
+                            std::max(1, std::min(a.ntiles, gate_occ * h->sms)), bin.threads,
+                            h->stream),
+       "gate launch");
     h->launches++;
     CK(cudaMemcpyAsync(h->h_count, nheavy, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream),
        "counter copy");
@@ -1414,16 +1430,17 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
     if (rc) return h->fail(rc, "surrogate forward: %s", s->err.c_str());
     // one fused kernel, or one GEMM per layer
     h->launches -= sur_uses_tc(s) ? s->L - 1 : 0;
-    CK(sur::apply(h->d_yhat.as<float>(), h->d_conc.as<float>(), s->norm, list, nh, K, h->kmax,
-                  h->nslot, s->nin, s->nout, s->pout[s->L - 1], h->d_prop.as<float>(),
-                  h->stream),
-       "apply");
-    h->launches += 2 + s->L;
-    // 3. residual test of every proposal; passing ones replace the state
+    h->launches += 1 + s->L;
+    // 3. each column's proposal from its prediction row and its residual
+    //    test; passing ones replace the state
     ColumnArgs<float> r = column_args<float>(h, bin, b, dt, SED_ADAPTIVE_EULER);
     r.list = list;
     r.ntiles = nh;
-    r.out = h->d_prop.as<float>();
+    r.yhat = h->d_yhat.as<float>();
+    r.ldy = s->pout[s->L - 1];
+    r.norm = s->norm;
+    r.nin = s->nin;
+    r.nout = s->nout;
     r.skip = h->d_skip.as<int>();
     r.res_tol = tol;
     r.res_atol = res_atol;

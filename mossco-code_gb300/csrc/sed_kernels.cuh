@@ -814,17 +814,36 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
     // global arrays in load_lane's (row, column) form: rows of kmax layers
     // per tracer / coefficient, columns of stride nslot; then the surface
     // values the substeps read come from the warp's shared copy
-    // KIND_RESID reads the surrogate's proposed state (a.out)
-    load_lane<real, LPL, BC4, BIO3>(lc, C, KIND == KIND_RESID ? a.out : a.conc, a.coef, a.cap,
-                                    a.force, slot, a.kmax, (int)ns, lane, K, p.mol_mode);
+    load_lane<real, LPL, BC4, BIO3>(lc, C, a.conc, a.coef, a.cap, a.force, slot, a.kmax,
+                                    (int)ns, lane, K, p.mol_mode);
     lc.bnd_s = sb + 2;
     lc.bnd_stride = 1;
     Params<real> pc = p;
     if (ENS) load_bgc(pc, a.bgc, ns, slot);
     real ftop[NTR];
-    if (KIND == KIND_RESID) {
-      // Quasi-steady test of the proposal P: the plain right-hand side at P
-      // may change no cell by more than res_tol of its value over one step,
+    if constexpr (KIND == KIND_RESID) {
+      // The network's proposal P from the state C and prediction row j:
+      // P = max(exp(log(max(C, 0) + c0) + mu_d + sd_d y) - c0, 0), cell
+      // (n, k) at feature n K + k (every column has K = kmax layers here).
+      {
+        const float* yr = a.yhat + (size_t)j * a.ldy;
+        const float* c0 = a.norm;
+        const float* mud = a.norm + NTR + 2 * a.nin;
+        const float* sdd = mud + a.nout;
+#pragma unroll
+        for (int s = 0; s < LPL; s++) {
+          const int L = s * 32 + lane;
+          if (L < K)
+#pragma unroll
+            for (int n = 0; n < NTR; n++) {
+              const int f = n * K + L;
+              const float u = logf(fmaxf((float)C[s][n], 0.0f) + c0[n]) + mud[f] + sdd[f] * yr[f];
+              C[s][n] = (real)fmaxf(expf(u) - c0[n], 0.0f);
+            }
+        }
+      }
+      // Quasi-steady test of P: the plain right-hand side at P may change no
+      // cell by more than res_tol of its value over one step,
       // dt |f(P)| <= res_tol (|P| + res_atol) in every active cell.  At the
       // end of a column's heavy steps the plain solver's own states change
       // by about 1 % per step this way; a proposal off the slow manifold of

@@ -39,8 +39,8 @@ struct ColumnArgs {
   int method;
   // surrogate coupling step: per-slot flags (1 = the surrogate's state was
   // accepted, the step kernels skip the column) and the tolerances of the
-  // residual test (KIND_RESID: out = proposed state, written into conc when
-  // it passes)
+  // residual test (KIND_RESID: the proposal, formed from yhat, is written
+  // into conc when it passes)
   int* skip;
   double res_tol, res_atol;
   // warp-direct kernel: the launch's columns are list[0 .. ntiles) (slots)
@@ -50,6 +50,12 @@ struct ColumnArgs {
   const int* list;
   int* heavy;
   unsigned* nheavy;
+  // KIND_RESID: the network's prediction rows (row j for the list's j-th
+  // column, pitch ldy) and its normalisation c0[11] | mu_x[nin] | sd_x[nin] |
+  // mu_d[nout] | sd_d[nout]
+  const float* yhat;
+  const float* norm;
+  int ldy, nin, nout;
   // warp-direct kernel: coupling steps per launch with constant forcing
   // (0 or 1: one); each warp keeps its column in registers between them
   int nrepeat;

@@ -8,10 +8,9 @@
 // (the 13 per-column forcing rows of the solver: bioturbation x f_T, the
 // molecular multiplier and the 11 surface values), zero in padded rows and
 // columns.  The network predicts the standardised change of log(C + c0)
-// over one coupling step; the proposed state is
-// max(exp(log(max(C, 0) + c0) + mu_d + sd_d y) - c0, 0).  Features and apply
-// are 32 x 32 tiled transposes (row tiles on blockIdx.x, feature tiles on
-// blockIdx.y).
+// over one coupling step; the surrogate step's residual kernel forms the
+// proposed state from it.  The features kernel is a 32 x 32 tiled transpose
+// (row tiles on blockIdx.x, feature tiles on blockIdx.y).
 //
 // Training rows (k_collect): for every column whose plain step took more
 // than one attempt (its first, whole-step attempt was rejected: the columns
@@ -64,36 +63,6 @@ __global__ void k_features(const float* __restrict__ conc, const float* __restri
   }
 }
 
-__global__ void k_apply(const float* __restrict__ yhat, const float* __restrict__ conc,
-                        const float* __restrict__ norm, const int* __restrict__ list, int nrows,
-                        int K, int kmax, int nslot, int nin, int nout, int pout,
-                        float* __restrict__ prop) {
-  __shared__ float tile[32][33];
-  const int f0 = blockIdx.y * 32, r0 = blockIdx.x * 32;
-  const float* c0 = norm;
-  const float* mud = norm + NTR + 2 * nin;
-  const float* sdd = mud + nout;
-  // read: rows, outputs contiguous
-  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
-    const int r = r0 + y, f = f0 + threadIdx.x;
-    tile[y][threadIdx.x] = (r < nrows && f < nout) ? yhat[(size_t)r * pout + f] : 0.0f;
-  }
-  __syncthreads();
-  // write: state rows of the row's slot
-  const int r = r0 + threadIdx.x;
-  if (r >= nrows) return;
-  const int slot = list[r];
-  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
-    const int f = f0 + y;
-    if (f < nout) {
-      const int n = f / K, k = f - n * K;
-      const size_t i = ((size_t)n * kmax + k) * nslot + slot;
-      const float u = logf(fmaxf(conc[i], 0.0f) + c0[n]) + mud[f] + sdd[f] * tile[threadIdx.x][y];
-      prop[i] = fmaxf(expf(u) - c0[n], 0.0f);
-    }
-  }
-}
-
 // One warp per slot of the class range [slot0, slot0 + nslots).
 __global__ void k_collect(const float* __restrict__ conc0, const float* __restrict__ conc1,
                           const float* __restrict__ force, const int* __restrict__ kact,
@@ -131,16 +100,6 @@ cudaError_t features(const float* conc, const float* force, const float* norm, c
   dim3 grid((rows + 31) / 32, (pin + 31) / 32);
   k_features<<<grid, dim3(32, 8), 0, st>>>(conc, force, norm, list, nrows, K, kmax, nslot, rows,
                                            nin, pin, x);
-  return cudaGetLastError();
-}
-
-cudaError_t apply(const float* yhat, const float* conc, const float* norm, const int* list,
-                  int nrows, int K, int kmax, int nslot, int nin, int nout, int pout,
-                  float* prop, cudaStream_t st) {
-  if (nrows <= 0) return cudaSuccess;
-  dim3 grid((nrows + 31) / 32, (nout + 31) / 32);
-  k_apply<<<grid, dim3(32, 8), 0, st>>>(yhat, conc, norm, list, nrows, K, kmax, nslot, nin,
-                                        nout, pout, prop);
   return cudaGetLastError();
 }
 

@@ -13,10 +13,6 @@ namespace sur {
 cudaError_t features(const float* conc, const float* force, const float* norm, const int* list,
                      int nrows, int K, int kmax, int nslot, int rows, int nin, int pin,
                      __nv_bfloat16* x, cudaStream_t st);
-// the proposed state of the column in slot list[r] from prediction row r
-cudaError_t apply(const float* yhat, const float* conc, const float* norm, const int* list,
-                  int nrows, int K, int kmax, int nslot, int nin, int nout, int pout,
-                  float* prop, cudaStream_t st);
 // training rows of the columns of slots [slot0, slot0 + nslots) whose step
 // took more than one attempt (conc0: state before the step, conc1: after)
 cudaError_t collect(const float* conc0, const float* conc1, const float* force, const int* kact,

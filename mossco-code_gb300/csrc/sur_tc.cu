@@ -11,11 +11,9 @@
 //   epilogue: acc + b, GELU -> BF16 back into the same shared buffer, in
 //            the swizzled layout of the next layer's A operand; the last
 //            layer's acc + b goes to global memory (FP32 rows).
-// Roles (192 threads): warps 0-3 run the epilogue (warp w reads TMEM lanes
-// 32w..32w+31, one row per thread), warp 4 issues the TMA loads, warp 5
-// issues the MMAs.  Every wait on an mbarrier is bounded: after ~1 s the
-// kernel records an error code, stops issuing work, waits (bounded) for its
-// outstanding copies and MMAs, frees its TMEM and returns.
+// Every wait on an mbarrier is bounded: after ~1 s the kernel records an
+// error code, stops issuing work, waits (bounded) for its outstanding copies
+// and MMAs, frees its TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -39,7 +37,9 @@ constexpr int STAGE = 2 * CHUNK;         // [256][64] weights: 32 KB
 constexpr int NST = 3;                   // weight ring stages
 constexpr int HID = 256;                 // hidden width (TMEM columns used)
 constexpr int TMEM_COLS = 512;
-constexpr int NTHREADS = 192;
+constexpr int EPI_THREADS = 256;         // warps 0-7
+constexpr int PRODUCER = 8, MMA = 9;     // warps
+constexpr int NTHREADS = 320;
 constexpr long long WAIT_CYCLES = 2000000000ll;  // ~1 s at 2 GHz
 
 struct Layers {
@@ -164,6 +164,19 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   return *reinterpret_cast<uint32_t*>(&h);
 }
 
+// Roles of the 320 threads: warps 0-7 run the epilogue (warp w reads the
+// TMEM lanes 32 (w % 4) .. +31, one row per thread, and the columns
+// 32 (w / 4) .. +31 of every 64-column chunk), warp 8 issues the TMA loads,
+// warp 9 the MMAs.
+//
+// Overlap.  Hidden layer l accumulates in TMEM region l % 2 (columns
+// 256 (l % 2) .. +255), so layer l+1's MMAs run while the epilogue still
+// reads layer l's accumulator; the epilogue releases the next layer's A
+// operand 64 columns at a time (barrier actc[kc]), so layer l+1 starts on
+// chunk 0 while chunks 1-3 are being produced.  The last layer's output
+// columns 0..255 accumulate in region 0 and 256.. in region 1 (its TMEM
+// column is its output column); the next tile's layer 0 waits only for the
+// epilogue to have read region 0 (barrier lastepi).
 __global__ void __launch_bounds__(NTHREADS, 1)
 k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers P,
          float* __restrict__ y, int ldy, int ntiles, int* err) {
@@ -174,13 +187,18 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
   unsigned char* xbuf = smem;                 // X tile, then the activations
   unsigned char* wbuf = smem + XBUF;          // weight ring
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + XBUF + NST * STAGE);
-  // bars: full[NST], empty[NST], xfull, xempty, accfull, epidone
+  // bars: full[NST], empty[NST], xfull, xempty, acc[2], lastepi, actc[4]
+  // (accumulators complete alternately on acc[0] and acc[1], so neither
+  // runs two phases ahead of the epilogue when the last layer's two parts
+  // complete back to back)
   __shared__ uint32_t s_tmem;
   __shared__ volatile int s_abort;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t b_full = saddr(bars), b_empty = saddr(bars + NST);
   const uint32_t b_xfull = saddr(bars + 2 * NST), b_xempty = saddr(bars + 2 * NST + 1);
-  const uint32_t b_acc = saddr(bars + 2 * NST + 2), b_epi = saddr(bars + 2 * NST + 3);
+  const uint32_t b_acc = saddr(bars + 2 * NST + 2);   // 2 barriers, 8 bytes apart
+  const uint32_t b_last = saddr(bars + 2 * NST + 4);
+  const uint32_t b_actc = saddr(bars + 2 * NST + 5);  // 4 barriers, 8 bytes apart
 
   if (threadIdx.x == 0) {
     s_abort = 0;
@@ -191,7 +209,9 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
     mbar_init(b_xfull, 1);
     mbar_init(b_xempty, 1);
     mbar_init(b_acc, 1);
-    mbar_init(b_epi, 4 * 32);
+    mbar_init(b_acc + 8, 1);
+    mbar_init(b_last, EPI_THREADS);
+    for (int i = 0; i < HID / BK; i++) mbar_init(b_actc + 8 * i, EPI_THREADS);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -201,7 +221,7 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  if (warp == 4 && lane == 0) {
+  if (warp == PRODUCER && lane == 0) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tx)) : "memory");
     for (int l = 0; l < P.L; l++)
       asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&P.w[l]))
@@ -211,8 +231,9 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
   __syncthreads();
   fence_after();
   const uint32_t tmem = s_tmem;
+  const int last = P.L - 1;
 
-  if (warp == 4) {
+  if (warp == PRODUCER) {
     // ---- TMA producer (one lane)
     if (lane == 0) {
       uint32_t g = 0;   // weight chunks issued
@@ -252,26 +273,30 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
         }
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == MMA) {
     // ---- MMA issuer (one lane)
     if (lane == 0) {
-      uint32_t g = 0, it = 0, e = 0;
+      uint32_t g = 0, it = 0, u = 0;
+      uint32_t ph_act[HID / BK] = {0, 0, 0, 0};
       bool ok = true, issued = false;
       for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, it++) {
         ok = mbar_wait(b_xfull, it & 1, &s_abort, err, 3);
+        // region 0 is free once the previous tile's last epilogue read it
+        if (ok && it > 0) ok = mbar_wait(b_last, (it - 1) & 1, &s_abort, err, 4);
         for (int l = 0; l < P.L && ok; l++) {
-          if (it > 0 || l > 0) {
-            // the previous layer's epilogue: A operand written, TMEM read
-            ok = mbar_wait(b_epi, e & 1, &s_abort, err, 4);
-            e++;
-            if (!ok) break;
-          }
-          fence_after();
           const int K = l == 0 ? P.k0 : HID;
           for (int n0 = 0; n0 < P.nout[l] && ok; n0 += HID) {
             const int nn = min(HID, P.nout[l] - n0);
             const uint32_t idesc = idesc_bf16(nn);
+            // hidden layer l: region l % 2; last layer: its output columns
+            const uint32_t dcol = l == last ? (uint32_t)n0 : (uint32_t)(HID * (l & 1));
             for (int kc = 0; kc < K / BK; kc++, g++) {
+              if (l > 0 && n0 == 0) {
+                // the epilogue has written this chunk of the A operand
+                ok = mbar_wait(b_actc + 8 * kc, ph_act[kc] & 1, &s_abort, err, 7);
+                ph_act[kc]++;
+                if (!ok) break;
+              }
               const uint32_t s = g % NST;
               ok = mbar_wait(b_full + 8 * s, (g / NST) & 1, &s_abort, err, 5);
               if (!ok) break;
@@ -280,13 +305,13 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
               const uint32_t b0 = saddr(wbuf + s * STAGE);
 #pragma unroll
               for (int k = 0; k < BK / 16; k++)
-                mma_bf16(tmem + (uint32_t)n0, desc_sw128(a0 + 32 * k), desc_sw128(b0 + 32 * k),
-                         idesc, (kc > 0 || k > 0) ? 1u : 0u);
+                mma_bf16(tmem + dcol, desc_sw128(a0 + 32 * k), desc_sw128(b0 + 32 * k), idesc,
+                         (kc > 0 || k > 0) ? 1u : 0u);
               mma_commit(b_empty + 8 * s);  // the stage is free once these complete
               issued = true;
             }
+            if (ok) mma_commit(b_acc + 8 * (u++ & 1));  // this accumulator (part) is complete
           }
-          if (ok) mma_commit(b_acc);  // the layer's accumulator is complete
         }
         if (ok) mma_commit(b_xempty);  // the A buffer is free for the next tile
       }
@@ -299,54 +324,65 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
       }
     }
   } else {
-    // ---- epilogue (warps 0-3: one row per thread)
-    const int row = warp * 32 + lane;
-    const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+    // ---- epilogue (warps 0-7)
+    const int q = warp & 3, h = warp >> 2;
+    const int row = q * 32 + lane;
+    const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16);
     uint32_t a = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-      for (int l = 0; l < P.L; l++) {
-        ok = mbar_wait(b_acc, a & 1, &s_abort, err, 6);
-        a++;
-        if (!ok) break;
-        fence_after();
-        const bool last = l == P.L - 1;
+      for (int l = 0; l < P.L && ok; l++) {
         const float* bias = P.bias[l];
-        for (int c0 = 0; c0 < P.nout[l]; c0 += 32) {
-          float v[32];
-          tmem_ld32(tl + (uint32_t)c0, v);
+        const bool is_last = l == last;
+        for (int n0 = 0; n0 < P.nout[l] && ok; n0 += HID) {
+          ok = mbar_wait(b_acc + 8 * (a & 1), (a >> 1) & 1, &s_abort, err, 6);
+          a++;
+          if (!ok) break;
+          fence_after();
+          const int nn = min(HID, P.nout[l] - n0);
+          for (int kc = 0; kc < nn / BK; kc++) {
+            const int c0 = n0 + kc * BK + 32 * h;  // output column
+            const uint32_t tcol = is_last ? (uint32_t)c0 : (uint32_t)(HID * (l & 1) + c0);
+            float v[32];
+            tmem_ld32(tl + tcol, v);
 #pragma unroll
-          for (int i = 0; i < 32; i += 4) {
-            const float4 b = __ldg(reinterpret_cast<const float4*>(bias + c0 + i));
-            v[i] += b.x;
-            v[i + 1] += b.y;
-            v[i + 2] += b.z;
-            v[i + 3] += b.w;
-          }
-          if (last) {
-            float* dst = y + (size_t)(tile * BM + row) * ldy + c0;
+            for (int i = 0; i < 32; i += 4) {
+              const float4 b = __ldg(reinterpret_cast<const float4*>(bias + c0 + i));
+              v[i] += b.x;
+              v[i + 1] += b.y;
+              v[i + 2] += b.z;
+              v[i + 3] += b.w;
+            }
+            if (is_last) {
+              float* dst = y + (size_t)(tile * BM + row) * ldy + c0;
 #pragma unroll
-            for (int i = 0; i < 32; i += 4)
-              *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
-          } else {
-            // BF16 GELU into the next layer's A operand: chunk c0/64, row
-            // `row`, 16-byte pieces j0..j0+3 at (j ^ row % 8)
-            unsigned char* rbase = xbuf + (c0 / BK) * CHUNK + row * 128;
-            const int j0 = (c0 % BK) / 8;
+              for (int i = 0; i < 32; i += 4)
+                *reinterpret_cast<float4*>(dst + i) =
+                    make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+            } else {
+              // BF16 GELU into chunk kc of the next layer's A operand: row
+              // `row`, 16-byte pieces 4h .. 4h+3 at (piece ^ row % 8)
+              unsigned char* rbase = xbuf + kc * CHUNK + row * 128;
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-              uint4 w;
-              w.x = pack_bf16(gelu_fast(v[8 * q + 0]), gelu_fast(v[8 * q + 1]));
-              w.y = pack_bf16(gelu_fast(v[8 * q + 2]), gelu_fast(v[8 * q + 3]));
-              w.z = pack_bf16(gelu_fast(v[8 * q + 4]), gelu_fast(v[8 * q + 5]));
-              w.w = pack_bf16(gelu_fast(v[8 * q + 6]), gelu_fast(v[8 * q + 7]));
-              *reinterpret_cast<uint4*>(rbase + (((j0 + q) ^ (row & 7)) << 4)) = w;
+              for (int p = 0; p < 4; p++) {
+                uint4 w;
+                w.x = pack_bf16(gelu_fast(v[8 * p + 0]), gelu_fast(v[8 * p + 1]));
+                w.y = pack_bf16(gelu_fast(v[8 * p + 2]), gelu_fast(v[8 * p + 3]));
+                w.z = pack_bf16(gelu_fast(v[8 * p + 4]), gelu_fast(v[8 * p + 5]));
+                w.w = pack_bf16(gelu_fast(v[8 * p + 6]), gelu_fast(v[8 * p + 7]));
+                *reinterpret_cast<uint4*>(rbase + (((4 * h + p) ^ (row & 7)) << 4)) = w;
+              }
+              fence_before();
+              asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+              mbar_arrive(b_actc + 8 * kc);
             }
           }
+          if (is_last && n0 == 0) {
+            // region 0 read: the next tile's first layer may start
+            fence_before();
+            mbar_arrive(b_last);
+          }
         }
-        fence_before();
-        if (!last) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_arrive(b_epi);
       }
     }
   }
@@ -389,12 +425,14 @@ bool encode_bf16(CUtensorMap* m, const void* base, int rows, int cols) {
          CUDA_SUCCESS;
 }
 
-size_t smem_bytes() { return 1024 + XBUF + NST * STAGE + 8 * (2 * NST + 4); }
+size_t smem_bytes() { return 1024 + XBUF + NST * STAGE + 8 * (2 * NST + 5 + HID / BK); }
 
 }  // namespace tc
 
 bool tc_supported(const sed_surrogate* s) {
-  if (s->L < 2 || s->L > kSurMaxLayers) return false;
+  // an even number of hidden layers: the last layer's first 256 outputs then
+  // accumulate in region 0, away from the last hidden layer's region 1
+  if (s->L < 3 || s->L > kSurMaxLayers || (s->L - 1) % 2) return false;
   if (s->pin[0] % tc::BK || s->pin[0] > tc::KMAX0) return false;
   for (int l = 0; l < s->L - 1; l++)
     if (s->pout[l] != tc::HID) return false;
