@@ -41,6 +41,10 @@ constexpr int EPI_THREADS = 256;         // warps 0-7
 constexpr int PRODUCER = 8, MMA = 9;     // warps
 constexpr int NTHREADS = 320;
 constexpr long long WAIT_CYCLES = 2000000000ll;  // ~1 s at 2 GHz
+// shared memory after the weight ring: 2 NST + 9 barriers, then the biases
+constexpr int BAR_OFF = XBUF + NST * STAGE;
+constexpr int BIAS_OFF = BAR_OFF + 8 * (2 * NST + 9);
+constexpr int BIAS_MAX = 4096;  // floats: the sum of every layer's padded width
 
 struct Layers {
   CUtensorMap w[kSurMaxLayers];  // [nout][nin] BF16, box [128][64]
@@ -133,9 +137,9 @@ __device__ __forceinline__ void fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// 32 consecutive FP32 columns of this thread's TMEM lane
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-  uint32_t r[32];
+// 32 consecutive FP32 columns of this thread's TMEM lane, issued without
+// waiting: the registers hold the values only after tmem_wait(r)
+__device__ __forceinline__ void tmem_ld32_async(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
       "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -146,17 +150,29 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
         "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
         "=r"(r[31])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+// Wait for the thread's TMEM loads; the registers are operands, so no use
+// of them moves above the wait.
+__device__ __forceinline__ void tmem_wait(uint32_t (&r)[32]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                 "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                 "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]),
+                 "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]),
+                 "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]),
+                 "+r"(r[30]), "+r"(r[31])
+               :
+               : "memory");
 }
 
-// tanh form of GELU with the hardware tanh approximation
+// tanh form of GELU, 0.5 z (1 + tanh(k0 (z + k1 z^3))), with the hardware
+// tanh approximation: z2 = z z; u = z (k0 + k0 k1 z2); h = z / 2; h + h t
 __device__ __forceinline__ float gelu_fast(float z) {
-  const float u = 0.7978845608028654f * fmaf(0.044715f * z * z, z, z);
+  const float w = fmaf(0.035677408136300125f, z * z, 0.7978845608028654f);
   float t;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
-  return 0.5f * z * (1.0f + t);
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(z * w));
+  const float hz = 0.5f * z;
+  return fmaf(hz, t, hz);
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
@@ -186,7 +202,7 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   unsigned char* xbuf = smem;                 // X tile, then the activations
   unsigned char* wbuf = smem + XBUF;          // weight ring
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + XBUF + NST * STAGE);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + BAR_OFF);
   // bars: full[NST], empty[NST], xfull, xempty, acc[2], lastepi, actc[4]
   // (accumulators complete alternately on acc[0] and acc[1], so neither
   // runs two phases ahead of the epilogue when the last layer's two parts
@@ -226,6 +242,17 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
     for (int l = 0; l < P.L; l++)
       asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&P.w[l]))
                    : "memory");
+  }
+  // every layer's bias in shared memory (layer l at boff[l])
+  float* s_bias = reinterpret_cast<float*>(smem + BIAS_OFF);
+  int boff[kSurMaxLayers];
+  {
+    int o = 0;
+    for (int l = 0; l < P.L; l++) {
+      boff[l] = o;
+      for (int i = threadIdx.x; i < P.nout[l]; i += blockDim.x) s_bias[o + i] = P.bias[l][i];
+      o += P.nout[l];
+    }
   }
   fence_before();
   __syncthreads();
@@ -332,27 +359,34 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
     bool ok = true;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
       for (int l = 0; l < P.L && ok; l++) {
-        const float* bias = P.bias[l];
+        const float* bias = s_bias + boff[l];
         const bool is_last = l == last;
         for (int n0 = 0; n0 < P.nout[l] && ok; n0 += HID) {
           ok = mbar_wait(b_acc + 8 * (a & 1), (a >> 1) & 1, &s_abort, err, 6);
           a++;
           if (!ok) break;
           fence_after();
-          const int nn = min(HID, P.nout[l] - n0);
-          for (int kc = 0; kc < nn / BK; kc++) {
-            const int c0 = n0 + kc * BK + 32 * h;  // output column
-            const uint32_t tcol = is_last ? (uint32_t)c0 : (uint32_t)(HID * (l & 1) + c0);
-            float v[32];
-            tmem_ld32(tl + tcol, v);
+          const int nchunk = min(HID, P.nout[l] - n0) / BK;
+          // TMEM column of chunk kc: the output column for the last layer,
+          // region l % 2 for a hidden one
+          auto tcol = [&](int kc) {
+            const int c0 = n0 + kc * BK + 32 * h;
+            return is_last ? (uint32_t)c0 : (uint32_t)(HID * (l & 1) + c0);
+          };
+          uint32_t ra[32], rb[32];
+          tmem_ld32_async(tl + tcol(0), ra);
+          tmem_wait(ra);
 #pragma unroll
-            for (int i = 0; i < 32; i += 4) {
-              const float4 b = __ldg(reinterpret_cast<const float4*>(bias + c0 + i));
-              v[i] += b.x;
-              v[i + 1] += b.y;
-              v[i + 2] += b.z;
-              v[i + 3] += b.w;
-            }
+          for (int kc = 0; kc < HID / BK; kc++) {
+            if (kc >= nchunk) break;
+            uint32_t(&cur)[32] = (kc & 1) ? rb : ra;
+            uint32_t(&nxt)[32] = (kc & 1) ? ra : rb;
+            // the next chunk's load runs while this one is processed
+            if (kc + 1 < nchunk) tmem_ld32_async(tl + tcol(kc + 1), nxt);
+            const int c0 = n0 + kc * BK + 32 * h;  // output column
+            float v[32];
+#pragma unroll
+            for (int i = 0; i < 32; i++) v[i] = __uint_as_float(cur[i]) + bias[c0 + i];
             if (is_last) {
               float* dst = y + (size_t)(tile * BM + row) * ldy + c0;
 #pragma unroll
@@ -376,6 +410,7 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
               asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
               mbar_arrive(b_actc + 8 * kc);
             }
+            if (kc + 1 < nchunk) tmem_wait(nxt);
           }
           if (is_last && n0 == 0) {
             // region 0 read: the next tile's first layer may start
@@ -425,7 +460,7 @@ bool encode_bf16(CUtensorMap* m, const void* base, int rows, int cols) {
          CUDA_SUCCESS;
 }
 
-size_t smem_bytes() { return 1024 + XBUF + NST * STAGE + 8 * (2 * NST + 5 + HID / BK); }
+size_t smem_bytes() { return 1024 + BIAS_OFF + 4 * BIAS_MAX; }
 
 }  // namespace tc
 
@@ -439,7 +474,10 @@ bool tc_supported(const sed_surrogate* s) {
   for (int l = 1; l < s->L; l++)
     if (s->pin[l] != tc::HID) return false;
   const int nlast = s->pout[s->L - 1];
-  return nlast % 128 == 0 && nlast <= tc::TMEM_COLS && tc::encoder() != nullptr;
+  int nbias = 0;
+  for (int l = 0; l < s->L; l++) nbias += s->pout[l];
+  return nlast % 128 == 0 && nlast <= tc::TMEM_COLS && nbias <= tc::BIAS_MAX &&
+         tc::encoder() != nullptr;
 }
 
 cudaError_t infer_tc(sed_surrogate* s, const __nv_bfloat16* x, float* y, int m, int* err,
