@@ -332,6 +332,14 @@ int sed_sur_create(int nin, int nout, int hidden, int nhidden, int max_batch,
 int sed_sur_num_params(const sed_surrogate *s);
 int sed_sur_set_weights(sed_surrogate *s, const float *params);
 int sed_sur_get_weights(sed_surrogate *s, float *params);
+/* Checkpoint of the training state: state[sed_sur_state_size(s)] holds the
+ * parameters, then Adam's first and second moments (each in the layout of
+ * sed_sur_get_weights), and *step Adam's step count.  Training resumed from
+ * a checkpoint on the same batches gives the same parameters, bit for bit,
+ * as training without the interruption. */
+int sed_sur_state_size(const sed_surrogate *s);
+int sed_sur_get_state(sed_surrogate *s, float *state, long long *step);
+int sed_sur_set_state(sed_surrogate *s, const float *state, long long step);
 /* host rows x[m][nin] -> y[m][nout] */
 int sed_sur_forward(sed_surrogate *s, const float *x, float *y, int m);
 /* device rows: x BF16 [m][pad128(nin)] -> y FP32 [m][pad128(nout)],

@@ -235,6 +235,22 @@ int sed_sur_set_weights(sed_surrogate* s, const float* params) {
   return SED_OK;
 }
 
+// params (unpadded, the layout of sed_sur_get_weights) into padded device
+// arrays, zero in the padding
+static int store_params(sed_surrogate* s, float* const* dst_w, float* const* dst_b,
+                        const float* params) {
+  size_t o = 0;
+  for (int l = 0; l < s->L; l++) {
+    std::vector<float> w((size_t)s->pout[l] * s->pin[l], 0.0f), b(s->pout[l], 0.0f);
+    for (int r = 0; r < s->dout[l]; r++)
+      for (int c = 0; c < s->din[l]; c++) w[(size_t)r * s->pin[l] + c] = params[o++];
+    for (int r = 0; r < s->dout[l]; r++) b[r] = params[o++];
+    SCK(cudaMemcpy(dst_w[l], w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice), "w");
+    SCK(cudaMemcpy(dst_b[l], b.data(), b.size() * sizeof(float), cudaMemcpyHostToDevice), "b");
+  }
+  return SED_OK;
+}
+
 static int fetch_params(sed_surrogate* s, float* const* src_w, float* const* src_b, float* out) {
   SCK(cudaStreamSynchronize(s->stream), "sync");
   size_t o = 0;
@@ -246,6 +262,37 @@ static int fetch_params(sed_surrogate* s, float* const* src_w, float* const* src
       for (int c = 0; c < s->din[l]; c++) out[o++] = w[(size_t)r * s->pin[l] + c];
     for (int r = 0; r < s->dout[l]; r++) out[o++] = b[r];
   }
+  return SED_OK;
+}
+
+int sed_sur_state_size(const sed_surrogate* s) {
+  if (!s) return SED_E_ARG;
+  return 3 * sed_sur_num_params(s);
+}
+
+// The training state: parameters, Adam's first and second moments (each in
+// the layout of sed_sur_get_weights) and Adam's step count.
+int sed_sur_get_state(sed_surrogate* s, float* state, long long* step) {
+  if (!s || !state || !step) return SED_E_ARG;
+  SCK(cudaSetDevice(s->device), "set device");
+  const int n = sed_sur_num_params(s);
+  int rc = fetch_params(s, s->w, s->b, state);
+  if (!rc) rc = fetch_params(s, s->mw, s->mb, state + n);
+  if (!rc) rc = fetch_params(s, s->vw, s->vb, state + 2 * (size_t)n);
+  if (rc) return rc;
+  *step = s->step;
+  return SED_OK;
+}
+
+int sed_sur_set_state(sed_surrogate* s, const float* state, long long step) {
+  if (!s || !state || step < 0) return SED_E_ARG;
+  SCK(cudaSetDevice(s->device), "set device");
+  const int n = sed_sur_num_params(s);
+  int rc = store_params(s, s->mw, s->mb, state + n);
+  if (!rc) rc = store_params(s, s->vw, s->vb, state + 2 * (size_t)n);
+  if (!rc) rc = sed_sur_set_weights(s, state);  // also the BF16 copies
+  if (rc) return rc;
+  s->step = (int)step;
   return SED_OK;
 }
 

@@ -147,6 +147,9 @@ SIGNATURES = {
     "sed_sur_num_params": (ctypes.c_int, [_H]),
     "sed_sur_set_weights": (ctypes.c_int, [_H, _fp]),
     "sed_sur_get_weights": (ctypes.c_int, [_H, _fp]),
+    "sed_sur_state_size": (ctypes.c_int, [_H]),
+    "sed_sur_get_state": (ctypes.c_int, [_H, _fp, ctypes.POINTER(ctypes.c_longlong)]),
+    "sed_sur_set_state": (ctypes.c_int, [_H, _fp, ctypes.c_longlong]),
     "sed_sur_forward": (ctypes.c_int, [_H, _fp, _fp, ctypes.c_int]),
     "sed_sur_forward_device": (ctypes.c_int, [_H, _vp, _vp, ctypes.c_int]),
     "sed_sur_train_step": (ctypes.c_int, [_H, _vp, _vp, ctypes.c_int,

@@ -237,15 +237,38 @@ class Surrogate:
         self._check(self.lib.sed_sur_set_weights(
             self.h, w.ctypes.data_as(ctypes.POINTER(ctypes.c_float))), "set weights")
 
+    def checkpoint(self) -> dict:
+        """The training state: parameters, Adam moments and step count
+        (sed_sur_get_state), with the normalisation."""
+        n = self.lib.sed_sur_state_size(self.h)
+        st = np.zeros(n, dtype=np.float32)
+        step = ctypes.c_longlong(0)
+        self._check(self.lib.sed_sur_get_state(
+            self.h, st.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(step)),
+            "get state")
+        return {"state": st, "step": int(step.value),
+                "norm": None if self.norm is None else self.norm.pack(), "K": self.K}
+
+    def restore(self, ck: dict):
+        st = np.ascontiguousarray(ck["state"], dtype=np.float32)
+        self._check(self.lib.sed_sur_set_state(
+            self.h, st.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), int(ck["step"])),
+            "set state")
+        if ck.get("norm") is not None:
+            self.set_norm(Normalizer.unpack(ck["norm"], int(ck["K"])))
+
     def save(self, path: str):
-        np.savez_compressed(path, weights=self.weights(), norm=self.norm.pack(), K=self.K)
+        """Parameters, Adam state and normalisation to an .npz file."""
+        ck = self.checkpoint()
+        np.savez_compressed(path, state=ck["state"], step=ck["step"], norm=ck["norm"],
+                            K=self.K)
 
     @staticmethod
     def load(path: str, batch: int = 8192) -> "Surrogate":
         d = np.load(path)
         s = Surrogate(int(d["K"]), batch=batch)
-        s.set_weights(d["weights"])
-        s.set_norm(Normalizer.unpack(d["norm"], int(d["K"])))
+        s.restore({"state": d["state"], "step": int(d["step"]), "norm": d["norm"],
+                   "K": int(d["K"])})
         return s
 
     def train(self, X, Y, steps: int, lr: float = 1e-3, lr_final: float = 2e-5,
