@@ -1492,7 +1492,8 @@ def main():
                     help="surrogate: simulated day the timed window starts at")
     ap.add_argument("--sur-tol", type=float, default=1e-3)
     ap.add_argument("--sur-res-atol", type=float, default=1e-2)
-    ap.add_argument("--sur-sweep", type=float, nargs="*", default=[1e-2, 1e-1, 1.0])
+    ap.add_argument("--sur-sweep", type=float, nargs="*", default=[1e-2, 1e-1, 1.0, 1e30],
+                    help="residual tolerances of the sweep (1e30: every proposal taken)")
     ap.add_argument("--sur-train-columns", type=int, default=200000)
     ap.add_argument("--sur-test-columns", type=int, default=20000)
     ap.add_argument("--sur-every", type=int, default=15,
