@@ -98,6 +98,17 @@ typedef struct sed_params {
   int bioturbation_profile;
   double bioturb_k_l, bioturb_L1, bioturb_L2, bioturb_beta, bioturb_b,
       bioturb_dry_density;
+  /* Temperature dependence of the microbial rates (K).  The reference hands
+   * the column temperature to the reaction model at every right-hand side
+   * (fabm_sediment_driver.F90:613); with temp_activation > 0, rLabile,
+   * rSemilabile, CprodMax, rnit and rODUox are multiplied in each column by
+   * exp(-temp_activation (1/(T+273) - 1/288)), T = bdys[0] in degC: the
+   * Arrhenius form and reference temperature the driver applies to
+   * bioturbation (:648, with 4500 K).  0 (default): rates independent of
+   * temperature.  > 0 steps with per-column cuts and the warp-direct
+   * kernels, as per-column parameter sets do; the surrogate, training rows,
+   * sed_get_rhs and sed_ode_solver_noalloc refuse it. */
+  double temp_activation;
 } sed_params;
 
 typedef struct sed_stats {

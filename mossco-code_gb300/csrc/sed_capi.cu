@@ -98,6 +98,10 @@ struct sed_handle {
   bool have_grid = false, have_forcing = false, have_state = false;
   // per-column OMEXDIA+P parameter sets (sed_set_column_bgc), [SED_NBGC][ncol]
   bool has_bgc = false;
+  // temperature-dependent rates: the per-slot table is d_bgc_base scaled by
+  // each column's factor whenever the forcing changes; rfac_host: d_rfac
+  // holds the factors of the current forcing formed on the host (FP64)
+  bool rfac_host = false;
   std::vector<double> bgc_cols;
   // slots: depth class, then column segment, then active layers
   int nslot = 0, nactive = 0;
@@ -112,6 +116,7 @@ struct sed_handle {
   cudaEvent_t pe_in[kMaxSeg] = {}, pe_cmp[kMaxSeg] = {};
   // device buffers
   DevBuf d_bgc;  // [NBGC_DEV][nslot] derived per-slot rate parameters
+  DevBuf d_bgc_base, d_rfac;  // its unscaled form; [ncol] rate factors
   DevBuf d_slot_col, d_kact, d_tile_k, d_conc, d_coef, d_cap, d_force, d_sflux,
       d_budget, d_nsub, d_queue, d_stats, d_flag, d_stage, d_bdys, d_fluxes,
       d_rhs, d_rhs_stage, d_grid, d_force64, d_skip, d_xfeat, d_yhat, d_backup,
@@ -119,6 +124,7 @@ struct sed_handle {
   // surrogate step: heavy-column slot list, its counter, hidden activations
   DevBuf d_list, d_gate, d_act;
   std::vector<double> force64;  // host forcing rows (FP64 state)
+  std::vector<double> rfac64;   // host rate factors (FP64 state)
   DevStats* h_stats = nullptr;  // pinned
   int* h_flag = nullptr;        // pinned
   unsigned long long* h_count = nullptr;  // pinned
@@ -142,6 +148,9 @@ struct sed_handle {
     return fail(SED_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
   }
   bool fp64() const { return prm.precision == SED_FP64; }
+  bool temp_rates() const { return prm.temp_activation > 0.0; }
+  // the kernels read a per-slot parameter table
+  bool table() const { return has_bgc || temp_rates(); }
   size_t rsize() const { return fp64() ? sizeof(double) : sizeof(float); }
   ~sed_handle();
 };
@@ -170,6 +179,10 @@ int check_params(sed_handle* h, const sed_params& p) {
   if (p.bioturbation_profile == 3 &&
       !(p.bioturb_dry_density > 0.0 && p.bioturb_b > 0.0 && p.bioturb_L1 + p.bioturb_L2 > 0.0))
     return h->fail(SED_E_ARG, "bioturbation profile 3 needs dry density > 0, b > 0, L1+L2 > 0");
+  if (!(p.temp_activation >= 0.0) || !std::isfinite(p.temp_activation))
+    return h->fail(SED_E_ARG, "temp_activation must be >= 0 and finite");
+  if (p.temp_activation > 0.0 && p.cut_scope == SED_CUT_GLOBAL)
+    return h->fail(SED_E_ARG, "temperature-dependent rates need per-column cuts");
   return SED_OK;
 }
 
@@ -205,7 +218,7 @@ ColumnArgs<real> column_args(sed_handle* h, const Bin& b, int bin_index,
   a.ntiles = b.tc ? b.nslots / b.tc : b.nslots;
   a.dt = dt;
   a.method = method;
-  a.bgc = h->has_bgc ? h->d_bgc.as<real>() : nullptr;
+  a.bgc = h->table() ? h->d_bgc.as<real>() : nullptr;
   return a;
 }
 
@@ -404,8 +417,10 @@ int step_global(sed_handle* h, double dt) {
 template <typename real>
 int step_any(sed_handle* h, double dt, int method) {
   if (method == SED_ADAPTIVE_EULER && h->prm.cut_scope == SED_CUT_GLOBAL) {
-    if (h->has_bgc)
-      return h->fail(SED_E_STATE, "per-column parameter sets need per-column cuts");
+    if (h->table())
+      return h->fail(SED_E_STATE,
+                     "per-column parameter sets and temperature-dependent rates need "
+                     "per-column cuts");
     return step_global<real>(h, dt);
   }
   return step_percol<real>(h, dt, method);
@@ -442,6 +457,20 @@ int scatter_fluxes(sed_handle* h) {
   return SED_OK;
 }
 
+// Temperature-dependent rates: the per-slot table from its base, the
+// microbial rate constants scaled by the column's factor (the host's, in
+// d_rfac, when rfac_host; else formed on the device from bdys[0]).
+template <typename real>
+int rate_table(sed_handle* h) {
+  CK(launch_rate_temperature<real>(h->d_bgc_base.as<real>(), h->d_bgc.as<real>(),
+                                   h->d_slot_col.as<int>(), h->d_bdys.as<double>(),
+                                   h->rfac_host ? h->d_rfac.as<double>() : nullptr,
+                                   h->prm.temp_activation, h->nslot, h->sms, h->stream),
+     "rate factor launch");
+  h->launches++;
+  return SED_OK;
+}
+
 template <typename real>
 int prep_force(sed_handle* h) {
   CK(launch_prep_force<real>(h->d_bdys.as<double>(), h->d_fluxes.as<double>(),
@@ -451,7 +480,8 @@ int prep_force(sed_handle* h) {
                              h->prm.bioturbation_profile == 3 ? 1 : 0, h->sms, h->stream),
      "forcing launch");
   h->launches++;
-  return SED_OK;
+  h->rfac_host = false;
+  return h->temp_rates() ? rate_table<real>(h) : SED_OK;
 }
 
 // FP64 state: the per-column forcing rows are formed on the host with the
@@ -482,7 +512,17 @@ int prep_force_host64(sed_handle* h, const double* bdys, const double* fluxes) {
                            h->d_slot_col.as<int>(), NFORCE, 1, ncol, h->nslot, h->sms,
                            h->stream), "forcing gather");
   h->launches++;
-  return SED_OK;
+  h->rfac_host = false;
+  if (!h->temp_rates()) return SED_OK;
+  // the rate factors with the host's exp, as the CPU restatement forms them
+  std::vector<double>& fr = h->rfac64;
+  fr.resize(ncol);
+  for (int c = 0; c < ncol; c++) fr[c] = rate_factor(h->prm.temp_activation, bdys[c]);
+  CK(h->d_rfac.alloc((size_t)ncol * sizeof(double)), "rate factors");
+  CK(cudaMemcpyAsync(h->d_rfac.p, fr.data(), (size_t)ncol * sizeof(double),
+                     cudaMemcpyHostToDevice, h->stream), "rate factors copy");
+  h->rfac_host = true;
+  return rate_table<double>(h);
 }
 
 int upload_forcing(sed_handle* h, const double* bdys, const double* fluxes) {
@@ -530,9 +570,11 @@ int class_occupancy(sed_handle* h, const Bin& b, int tc, int threads) {
 
 // Occupancy and per-tile layer counts of the current tuning; raises the
 // kernels' shared-memory limit before any capture and drops the step graph.
-// The per-slot table of derived rate parameters of the ensemble: each
-// column's sed_params set through make_params, so a column with the
-// handle's own set gets the bits of the uniform path.
+// The per-slot table of derived rate parameters: each column's sed_params
+// set (its own with sed_set_column_bgc, else the handle's) through
+// make_params, so a column with the handle's own set gets the bits of the
+// uniform path.  With temperature-dependent rates this is the unscaled
+// base, scaled by rate_table once the forcing is known.
 template <typename real>
 int upload_bgc(sed_handle* h) {
   const int ns = h->nslot, nc = h->ncol;
@@ -541,7 +583,7 @@ int upload_bgc(sed_handle* h) {
   for (int s = 0; s < ns; s++) {
     const int c = h->slot_col[s];
     Params<real> q = base;
-    if (c >= 0) {
+    if (c >= 0 && h->has_bgc) {
       sed_params sp = h->prm;
       double* f[SED_NBGC] = {&sp.rLabile, &sp.rSemilabile, &sp.NCrLdet, &sp.NCrSdet,
                              &sp.PAds, &sp.PAdsODU, &sp.NH3Ads, &sp.CprodMax, &sp.rnit,
@@ -552,11 +594,14 @@ int upload_bgc(sed_handle* h) {
     }
     for (int i = 0; i < NBGC_DEV; i++) tab[(size_t)i * ns + s] = *bgc_field(q, i);
   }
+  DevBuf& dst = h->temp_rates() ? h->d_bgc_base : h->d_bgc;
   CK(h->d_bgc.alloc(tab.size() * sizeof(real)), "parameter sets");
-  CK(cudaMemcpyAsync(h->d_bgc.p, tab.data(), tab.size() * sizeof(real), cudaMemcpyHostToDevice,
+  CK(dst.alloc(tab.size() * sizeof(real)), "parameter sets");
+  CK(cudaMemcpyAsync(dst.p, tab.data(), tab.size() * sizeof(real), cudaMemcpyHostToDevice,
                      h->stream),
      "parameter sets copy");
   CK(cudaStreamSynchronize(h->stream), "parameter sets copy");
+  if (h->temp_rates() && h->have_forcing) return rate_table<real>(h);
   return SED_OK;
 }
 
@@ -790,7 +835,7 @@ int autotune_t(sed_handle* h, double dt, int method, int flags, sed_tuning* out)
     float best_ms = 1e30f;
     for (int tc : tcs)
       for (int th : thr) {
-        if (tc > 0 && h->has_bgc) continue;  // ensembles step warp-direct only
+        if (tc > 0 && h->table()) continue;  // per-slot tables step warp-direct only
         if (tc > 0) {
           const int occ = class_occupancy(h, bin, tc, th);
           if (occ <= 0 || bin.nslots < tc) continue;
@@ -951,6 +996,7 @@ int sed_default_params(sed_params* p) {
   p->bioturb_beta = 0.22;
   p->bioturb_b = 1.334;
   p->bioturb_dry_density = 1000.0;
+  p->temp_activation = 0.0;
   return SED_OK;
 }
 
@@ -1137,7 +1183,7 @@ int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
     CK(cudaStreamSynchronize(h->stream), "column map");
   }
   CK(h->d_tile_k.alloc((size_t)(h->nslot / 8 + 1) * sizeof(int)), "tile_k");
-  if (h->has_bgc) {  // the ensemble's table follows the new layout
+  if (h->table()) {  // the per-slot table follows the new layout
     h->bins[0].tc = h->bins[1].tc = 0;
     int rc = h->fp64() ? upload_bgc<double>(h) : upload_bgc<float>(h);
     if (rc) return rc;
@@ -1348,7 +1394,10 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
   int rc = ready(h);
   if (rc) return rc;
   if (!s) return h->fail(SED_E_ARG, "no surrogate");
-  if (h->has_bgc) return h->fail(SED_E_STATE, "the surrogate has no per-column parameter sets");
+  if (h->table())
+    return h->fail(SED_E_STATE,
+                   "the surrogate has no per-column parameter sets or temperature-dependent "
+                   "rates");
   if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");
   if (h->fp64()) return h->fail(SED_E_ARG, "the surrogate step runs on FP32 state");
   if (h->prm.cut_scope != SED_CUT_PER_COLUMN)
@@ -1471,7 +1520,9 @@ int sed_sur_collect(sed_handle* h, const float* c0, double dt, float* x_dev, flo
     return h->fail(SED_E_ARG, "c0, x, y and count are required");
   if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");
   if (h->fp64()) return h->fail(SED_E_ARG, "training rows come from FP32 state");
-  if (h->has_bgc) return h->fail(SED_E_STATE, "training rows use the handle's parameter set");
+  if (h->table())
+    return h->fail(SED_E_STATE, "training rows use the handle's parameter set, without "
+                                "temperature-dependent rates");
   if (h->prm.cut_scope != SED_CUT_PER_COLUMN)
     return h->fail(SED_E_ARG, "training rows come from per-column cuts");
   const int K = h->kmax;
@@ -1521,7 +1572,9 @@ int sed_get_rhs(sed_handle* h, const double* conc, double* rhs, double* fluxes) 
   if (!h) return SED_E_ARG;
   if ((rc = ready(h))) return rc;
   if (!conc || !rhs) return h->fail(SED_E_ARG, "conc and rhs are required");
-  if (h->has_bgc) return h->fail(SED_E_STATE, "sed_get_rhs has no per-column parameter sets");
+  if (h->table())
+    return h->fail(SED_E_STATE, "sed_get_rhs has no per-column parameter sets or "
+                                "temperature-dependent rates");
   CK(cudaSetDevice(h->device), "set device");
   const size_t n = (size_t)NTR * h->kmax * h->nslot * h->rsize();
   CK(h->d_rhs.alloc(n), "rhs buffer");
@@ -1596,9 +1649,13 @@ int sed_set_column_bgc(sed_handle* h, const double* params) {
   if (!params) {
     h->has_bgc = false;
     h->bgc_cols.clear();
-    h->d_bgc.release();
     reset_graph(h);
-    return SED_OK;
+    if (!h->temp_rates()) {
+      h->d_bgc.release();
+      return SED_OK;
+    }
+    // the handle's own set, scaled by temperature
+    return h->fp64() ? upload_bgc<double>(h) : upload_bgc<float>(h);
   }
   const size_t nc = (size_t)h->ncol;
   for (int i = 0; i < SED_NBGC; i++)
@@ -1745,10 +1802,28 @@ int spinup_t(sed_handle* h, int mode, int column, const double* bdys1, const dou
                        h->stream), "forcing save");
   CK(cudaMemcpy2DAsync(fcol, pitch, spin.data(), rs, rs, NFORCE, cudaMemcpyHostToDevice,
                        h->stream), "spin-up forcing");
+  // with temperature-dependent rates, the column's rates at the spin-up
+  // temperature in place of its own, put back after
+  std::vector<real> saved_tab(NBGC_DEV), spin_tab(NBGC_DEV);
+  real* tcol = h->temp_rates() ? h->d_bgc.as<real>() + slot : nullptr;
+  if (tcol) {
+    CK(cudaMemcpy2DAsync(spin_tab.data(), rs, h->d_bgc_base.as<real>() + slot, pitch, rs,
+                         NBGC_DEV, cudaMemcpyDeviceToHost, h->stream), "rates read");
+    CK(cudaMemcpy2DAsync(saved_tab.data(), rs, tcol, pitch, rs, NBGC_DEV,
+                         cudaMemcpyDeviceToHost, h->stream), "rates save");
+    CK(cudaStreamSynchronize(h->stream), "rates read");
+    const double fr = rate_factor(h->prm.temp_activation, bdys1[0]);
+    for (int i = 0; i < NRATE_TEMP; i++) spin_tab[i] = (real)((double)spin_tab[i] * fr);
+    CK(cudaMemcpy2DAsync(tcol, pitch, spin_tab.data(), rs, rs, NBGC_DEV,
+                         cudaMemcpyHostToDevice, h->stream), "spin-up rates");
+  }
   int rc = spin_range<real>(h, h->bins[b], b, slot, slot + 1, dt, method, nsteps, 1, 32);
   if (rc) return rc;
   CK(cudaMemcpy2DAsync(fcol, pitch, saved.data(), rs, rs, NFORCE, cudaMemcpyHostToDevice,
                        h->stream), "forcing restore");
+  if (tcol)
+    CK(cudaMemcpy2DAsync(tcol, pitch, saved_tab.data(), rs, rs, NBGC_DEV,
+                         cudaMemcpyHostToDevice, h->stream), "rates restore");
   CK(launch_broadcast<real>(h->d_conc.as<real>(), h->d_kact.as<int>(), slot, h->nslot, h->kmax,
                             h->sms, h->stream), "broadcast launch");
   h->launches++;
@@ -1930,8 +2005,9 @@ int sed_set_tuning(sed_handle* h, const sed_tuning* t) {
       return h->fail(SED_E_ARG, "tile_columns[%d]=%d: 0 (warp-direct), 8, 16, 32 or 64", b, tc);
     if (th < 64 || th > 256 || th % 64 != 0)
       return h->fail(SED_E_ARG, "threads[%d]=%d: 64, 128, 192 or 256", b, th);
-    if (tc != 0 && h->has_bgc)
-      return h->fail(SED_E_ARG, "per-column parameter sets step warp-direct only (tile 0)");
+    if (tc != 0 && h->table())
+      return h->fail(SED_E_ARG, "per-column parameter sets and temperature-dependent rates "
+                                "step warp-direct only (tile 0)");
     if (t->blocks_per_sm[b] < 0) return h->fail(SED_E_ARG, "blocks_per_sm[%d] < 0", b);
   }
   const int pc = t->pipeline_chunks;

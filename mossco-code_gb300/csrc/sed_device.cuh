@@ -72,8 +72,17 @@ struct Params {
 };
 
 // The rate parameters of Params that a per-column parameter set replaces,
-// in the order of the per-slot table.
+// in the order of the per-slot table; the first NRATE_TEMP of them (rF, rS,
+// cmax, rnit, rodu) are the microbial rates that temperature scales.
 constexpr int NBGC_DEV = 16;
+constexpr int NRATE_TEMP = 5;
+
+// Temperature factor of the microbial rates at T degC for activation
+// temperature Ta (K): the Arrhenius form and 288 K reference the driver
+// applies to bioturbation (fabm_sediment_driver.F90:648).
+__host__ __device__ inline double rate_factor(double Ta, double T) {
+  return exp(-Ta * (1.0 / (T + 273.0) - (1.0 / 288.0)));
+}
 
 template <typename real>
 __host__ __device__ __forceinline__ real* bgc_field(Params<real>& p, int i) {

@@ -1212,6 +1212,28 @@ __global__ void k_prep_force(const double* __restrict__ bdys,
   }
 }
 
+// Temperature-dependent rates: the per-slot parameter table from its base,
+// the microbial rate constants (rows 0-4 of the table: rF, rS, cmax, rnit,
+// rodu) multiplied by the column's factor -- fac[col] when given (formed on
+// the host), else rate_factor of the column's temperature bdys[col].  Land
+// slots keep the base.
+template <typename real>
+__global__ void k_rate_temperature(const real* __restrict__ base, real* __restrict__ tab,
+                                   const int* __restrict__ slot_col,
+                                   const double* __restrict__ bdys,
+                                   const double* __restrict__ fac, double Ta, int nslot) {
+  for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < nslot;
+       slot += gridDim.x * blockDim.x) {
+    const int col = slot_col[slot];
+    const double f = col < 0 ? 1.0 : (fac ? fac[col] : rate_factor(Ta, bdys[col]));
+#pragma unroll
+    for (int i = 0; i < NBGC_DEV; i++) {
+      const real b = base[(size_t)i * nslot + slot];
+      tab[(size_t)i * nslot + slot] = i < NRATE_TEMP ? (real)((double)b * f) : b;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 static int grid_for(size_t total, int block, int sms) {
@@ -1593,6 +1615,15 @@ cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
   return cudaGetLastError();
 }
 
+template <typename real>
+cudaError_t launch_rate_temperature(const real* base, real* tab, const int* slot_col,
+                                    const double* bdys, const double* fac, double Ta,
+                                    int nslot, int sms, cudaStream_t st) {
+  k_rate_temperature<real><<<grid_for(nslot, 256, sms), 256, 0, st>>>(base, tab, slot_col,
+                                                                     bdys, fac, Ta, nslot);
+  return cudaGetLastError();
+}
+
 // The kernels of one profile-3 setting for every layers-per-lane / BcUp-4
 // combination: the BIO3 = true set is compiled in its own translation unit
 // (declared extern where the dispatchers are instantiated).
@@ -1674,6 +1705,9 @@ cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
                                                const int*, real*, int, int,     \
                                                double, double, int, int, int,   \
                                                int, cudaStream_t);              \
+  template cudaError_t launch_rate_temperature<real>(                           \
+      const real*, real*, const int*, const double*, const double*, double,     \
+      int, int, cudaStream_t);                                                  \
   template cudaError_t launch_assemble_bc<real>(                                \
       const double*, const double*, const double*, unsigned, const real*,       \
       const int*, const double*, double*, double*, int, int, int, int, double,  \

@@ -141,6 +141,14 @@ cudaError_t launch_prep_force(const double* bdys, const double* fluxes,
                               int nslot, double bio, double diffusivity,
                               int mode, int bcup_d, int bio3, int sms, cudaStream_t st);
 
+// temperature-dependent rates: tab = base with the microbial rate rows
+// scaled by each column's factor (fac[ncol] from the host, or NULL to form
+// it from the temperature row bdys[0][ncol])
+template <typename real>
+cudaError_t launch_rate_temperature(const real* base, real* tab, const int* slot_col,
+                                    const double* bdys, const double* fac, double Ta,
+                                    int nslot, int sms, cudaStream_t st);
+
 // spin-up: the profile of slot src into every other active slot
 template <typename real>
 cudaError_t launch_broadcast(real* conc, const int* kact, int src, int nslot, int kmax, int sms,

@@ -115,6 +115,7 @@ extern "C" int sed_ode_solver_noalloc(const sed_params* p, int inum, int jnum,
   if (p->mol_diff_mode != 0 && p->mol_diff_mode != 1) return SED_E_ARG;
   if (p->max_attempts <= 0 || !(p->atol >= 0.0)) return SED_E_ARG;
   if (p->bioturbation_profile == 3) return SED_E_ARG;  // static biofac only
+  if (p->temp_activation != 0.0) return SED_E_ARG;     // the handle's rate set only
   if (method < 0 || method > 3 || !(dt > 0.0)) return SED_E_ARG;
   const int ncol = inum * jnum;
   // the same domain checks as sed_set_grid (fabm_sediment_driver.F90:503-530)

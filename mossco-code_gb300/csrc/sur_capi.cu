@@ -94,8 +94,7 @@ int backward(sed_surrogate* s, int m, int m_valid) {
     SCK(sur::gemm_nt(sur::EPI_F32, s->dzt, s->at, po, pi, m, nullptr, s->gw[l], nullptr,
                      nullptr, pi, s->stream),
         "weight gradient gemm");
-    SCK(cudaMemsetAsync(s->gb[l], 0, po * sizeof(float), s->stream), "gb reset");
-    SCK(sur::bias_grad(dcur, m, po, s->gb[l], s->stream), "bias gradient");
+    SCK(sur::bias_grad(dcur, m, po, s->gpart, s->gb[l], s->stream), "bias gradient");
     if (l > 0) {
       // dZ_{l-1} = (dZ_l W_l) * GELU'(Z_{l-1}) : A = dZ [m x po], B = W^T [pi x po]
       SCK(sur::gemm_nt(sur::EPI_GELU_BWD, dcur, s->wbt[l], m, pi, po, nullptr, nullptr, dnext,
@@ -181,7 +180,8 @@ int sed_sur_create(int nin, int nout, int hidden, int nhidden, int max_batch,
        s->alloc(&s->dz, B * maxd) == cudaSuccess && s->alloc(&s->dz2, B * maxd) == cudaSuccess &&
        s->alloc(&s->dzt, B * maxd) == cudaSuccess && s->alloc(&s->at, B * maxd) == cudaSuccess &&
        s->alloc(&s->mask, (size_t)s->pout[s->L - 1]) == cudaSuccess &&
-       s->alloc(&s->loss, 4) == cudaSuccess && s->alloc(&s->d_err, 1) == cudaSuccess;
+       s->alloc(&s->loss, 4) == cudaSuccess && s->alloc(&s->d_err, 1) == cudaSuccess &&
+       s->alloc(&s->gpart, (size_t)sur::bias_grad_parts() * maxd) == cudaSuccess;
   if (!ok) return bail(SED_E_NOMEM);
   // output mask; initial weights U(-1/sqrt(in), 1/sqrt(in)), zero biases
   std::vector<float> mask(s->pout[s->L - 1], 0.0f);

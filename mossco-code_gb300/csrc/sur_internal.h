@@ -29,6 +29,7 @@ struct sed_surrogate {
   bf16* a[kSurMaxLayers] = {};   // GELU activations of hidden layers
   bf16 *x = nullptr, *y = nullptr, *dz = nullptr, *dz2 = nullptr, *dzt = nullptr, *at = nullptr;
   float *mask = nullptr, *loss = nullptr;
+  float* gpart = nullptr;  // bias-gradient partial sums [bias_grad_parts()][maxd]
   int step = 0;
   // feature and increment normalisation of the column surrogate:
   // c0[11] | mu_x[nin] | sd_x[nin] | mu_d[nout] | sd_d[nout]

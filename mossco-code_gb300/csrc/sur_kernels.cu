@@ -219,14 +219,36 @@ __global__ void k_mse(const float* __restrict__ yhat, const __nv_bfloat16* __res
   if ((threadIdx.x & 31) == 0) atomicAdd(loss, s * inv_count);
 }
 
-// db[n] = sum_m dZ[m][n]; dZ bf16 [M][N]
-__global__ void k_bias_grad(const __nv_bfloat16* __restrict__ dz, int M, int N,
-                            float* __restrict__ db) {
+// db[n] = sum_m dZ[m][n]; dZ bf16 [M][N], in a fixed order so that training
+// is reproducible bit for bit: block (x, y) sums rows y, y + gridDim.y, ...
+// of 32 columns (8 row phases per block, reduced in order) into
+// part[y][n]; k_bias_sum then adds the gridDim.y partials in order.
+constexpr int kBiasRowBlocks = 64;
+
+__global__ void k_bias_part(const __nv_bfloat16* __restrict__ dz, int M, int N,
+                            float* __restrict__ part) {
+  __shared__ float red[8][33];
+  const int n = blockIdx.x * 32 + threadIdx.x;
+  float s = 0.0f;
+  if (n < N)
+    for (int m = blockIdx.y * 8 + threadIdx.y; m < M; m += gridDim.y * 8)
+      s += __bfloat162float(dz[(size_t)m * N + n]);
+  red[threadIdx.y][threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.y == 0 && n < N) {
+    float t = red[0][threadIdx.x];
+    for (int r = 1; r < 8; r++) t += red[r][threadIdx.x];
+    part[(size_t)blockIdx.y * N + n] = t;
+  }
+}
+
+__global__ void k_bias_sum(const float* __restrict__ part, int N, int nparts,
+                           float* __restrict__ db) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
-  float s = 0.0f;
-  for (int m = blockIdx.y; m < M; m += gridDim.y) s += __bfloat162float(dz[(size_t)m * N + n]);
-  atomicAdd(db + n, s);
+  float t = 0.0f;
+  for (int g = 0; g < nparts; g++) t += part[(size_t)g * N + n];
+  db[n] = t;
 }
 
 // Adam on FP32 master weights; refreshes the BF16 copy W and its transpose.
@@ -309,11 +331,14 @@ cudaError_t mse(const float* yhat, const __nv_bfloat16* y, const float* mask, in
   return cudaGetLastError();
 }
 
-cudaError_t bias_grad(const __nv_bfloat16* dz, int M, int N, float* db, cudaStream_t st) {
-  dim3 grid((N + 127) / 128, 256);
-  k_bias_grad<<<grid, 128, 0, st>>>(dz, M, N, db);
+cudaError_t bias_grad(const __nv_bfloat16* dz, int M, int N, float* part, float* db,
+                      cudaStream_t st) {
+  k_bias_part<<<dim3((N + 31) / 32, kBiasRowBlocks), dim3(32, 8), 0, st>>>(dz, M, N, part);
+  k_bias_sum<<<(N + 127) / 128, 128, 0, st>>>(part, N, kBiasRowBlocks, db);
   return cudaGetLastError();
 }
+
+int bias_grad_parts() { return kBiasRowBlocks; }
 
 cudaError_t adam(float* w, float* m, float* v, const float* g, int n, float lr, float b1,
                  float b2, float eps, int step, __nv_bfloat16* wb, __nv_bfloat16* wbt,

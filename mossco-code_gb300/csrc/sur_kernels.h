@@ -18,7 +18,10 @@ cudaError_t transpose_bf16(const __nv_bfloat16* in, __nv_bfloat16* out, int rows
 cudaError_t mse(const float* yhat, const __nv_bfloat16* y, const float* mask, int M, int N,
                 int m_valid, float inv_count, __nv_bfloat16* dy, float* loss,
                 cudaStream_t st);
-cudaError_t bias_grad(const __nv_bfloat16* dz, int M, int N, float* db, cudaStream_t st);
+// db[N] = column sums of dz[M][N] in a fixed order; part: bias_grad_parts() x N
+cudaError_t bias_grad(const __nv_bfloat16* dz, int M, int N, float* part, float* db,
+                      cudaStream_t st);
+int bias_grad_parts();
 cudaError_t adam(float* w, float* m, float* v, const float* g, int n, float lr, float b1,
                  float b2, float eps, int step, __nv_bfloat16* wb, __nv_bfloat16* wbt,
                  int rows, int cols, cudaStream_t st);

@@ -44,6 +44,8 @@ module sed_gpu
     integer(c_int)  :: bioturbation_profile
     real(c_double)  :: bioturb_k_l, bioturb_L1, bioturb_L2, bioturb_beta, &
                        bioturb_b, bioturb_dry_density
+    !> > 0: microbial rates times exp(-temp_activation (1/(T+273) - 1/288))
+    real(c_double)  :: temp_activation
   end type
 
   type, bind(C), public :: sed_stats_t

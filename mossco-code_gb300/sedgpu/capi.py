@@ -55,7 +55,8 @@ class SedParams(ctypes.Structure):
                    ("bioturb_L2", ctypes.c_double),
                    ("bioturb_beta", ctypes.c_double),
                    ("bioturb_b", ctypes.c_double),
-                   ("bioturb_dry_density", ctypes.c_double)])
+                   ("bioturb_dry_density", ctypes.c_double),
+                   ("temp_activation", ctypes.c_double)])
 
 
 class SedStats(ctypes.Structure):
@@ -242,6 +243,7 @@ def params_from(cs: ColumnSet, precision: int = SED_FP32, budgets: bool = False,
     for n in ("bioturb_k_l", "bioturb_L1", "bioturb_L2", "bioturb_beta", "bioturb_b",
               "bioturb_dry_density"):
         setattr(p, n, float(getattr(d, n)))
+    p.temp_activation = float(getattr(d, "temp_activation", 0.0))
     return p
 
 

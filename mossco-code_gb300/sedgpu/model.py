@@ -87,6 +87,10 @@ class DriverParams:
     bioturb_beta: float = 0.22
     bioturb_b: float = 1.334
     bioturb_dry_density: float = 1000.0
+    # > 0: the microbial rates (rLabile, rSemilabile, CprodMax, rnit, rODUox)
+    # times exp(-temp_activation (1/(T+273) - 1/288)) in each column, the
+    # Arrhenius form of the driver's bioturbation factor f_T (:648); 0: none
+    temp_activation: float = 0.0
 
     def minimum_array(self) -> np.ndarray:
         if self.minimum is None:

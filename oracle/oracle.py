@@ -76,6 +76,7 @@ class Model(ctypes.Structure):
         ("bioturb_L2", ctypes.c_double), ("bioturb_beta", ctypes.c_double),
         ("bioturb_b", ctypes.c_double), ("bioturb_dry_density", ctypes.c_double),
         ("bgc_col", ctypes.POINTER(Bgc)),
+        ("temp_activation", ctypes.c_double),
     ]
 
 
@@ -123,7 +124,7 @@ def lib():
                                           P(Stats)]
         L.orc_ode_solver_diag.restype = ctypes.c_int
         L.orc_epilogue.restype = ctypes.c_int
-        L.orc_omexdia_p.argtypes = [P(Bgc), _dp, _dp, _dp]
+        L.orc_omexdia_p.argtypes = [P(Bgc), ctypes.c_double, _dp, _dp, _dp]
         L.orc_diff3d.argtypes = [ctypes.c_int, _dp, ctypes.c_double,
                                  ctypes.c_double, ctypes.c_double,
                                  ctypes.c_double, ctypes.c_int, ctypes.c_int,
@@ -188,6 +189,7 @@ class OracleModel:
         for n in ("bioturb_k_l", "bioturb_L1", "bioturb_L2", "bioturb_beta",
                   "bioturb_b", "bioturb_dry_density"):
             setattr(m, n, float(getattr(d, n)))
+        m.temp_activation = float(d.temp_activation)
         if cs.bgc_col is not None:
             # [ncol] structs: the transpose of the [param][col] table
             tab = np.ascontiguousarray(np.asarray(cs.bgc_col, dtype=np.float64).T)
@@ -269,12 +271,13 @@ class OracleModel:
         return inv
 
 
-def omexdia_rates(bgc: dict, cell: np.ndarray):
+def omexdia_rates(bgc: dict, cell: np.ndarray, fr: float = 1.0):
+    """Local rates of one cell; fr multiplies the microbial rate constants."""
     b = Bgc(*[float(bgc[n]) for n in BGC_NAMES])
     c = np.ascontiguousarray(cell, dtype=np.float64)
     r = np.zeros(NTR)
     dn = np.zeros(1)
-    lib().orc_omexdia_p(ctypes.byref(b), _ptr(c), _ptr(r), _ptr(dn))
+    lib().orc_omexdia_p(ctypes.byref(b), float(fr), _ptr(c), _ptr(r), _ptr(dn))
     return r, float(dn[0])
 
 

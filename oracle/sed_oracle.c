@@ -98,21 +98,22 @@ void orc_init_profiles(int kmax, const double *zc, const double *zi,
  * with an explicit adsorbed-P pool at rate PAds, the sorbing share being
  * PAdsODU/(PAdsODU+ODU) (iron-bound P released as reduced substances
  * accumulate).  CprodMax caps total carbon mineralisation (per day). */
-void orc_omexdia_p(const orc_bgc *p, const double *c, double *r,
+void orc_omexdia_p(const orc_bgc *p, double fr, const double *c, double *r,
                    double *denit) {
   const double spd = 86400.0;
   double fdetC = c[0], sdetC = c[1], fdetN = c[2], sdetN = c[3], fdetP = c[4];
   double adsP = c[5], O2 = c[6], NO3 = c[7], NH4 = c[8], ODU = c[9];
   double PO4 = c[10];
-  double rF = p->rLabile / spd;
-  double rS = p->rSemilabile / spd;
+  /* fr: the temperature factor of the microbial rates (1 without) */
+  double rF = p->rLabile / spd * fr;
+  double rS = p->rSemilabile / spd * fr;
   double CprodF = rF * fdetC;
   double CprodS = rS * sdetC;
   double NprodF = rF * fdetN;
   double NprodS = rS * sdetN;
   double Pprod = rF * fdetP;
   double Cprod = CprodF + CprodS;
-  double cmax = p->CprodMax / spd;
+  double cmax = p->CprodMax / spd * fr;
   double lim = 1.0;
   if (Cprod > cmax) lim = cmax / Cprod;
   double oxlim = O2 / (O2 + p->ksO2oxic);
@@ -123,8 +124,10 @@ void orc_omexdia_p(const orc_bgc *p, const double *c, double *r,
   double OxicMin = Cmin * oxlim * rescale;
   double Denit = Cmin * dnlim * rescale;
   double AnoxicMin = Cmin * anlim * rescale;
-  double Nitri = p->rnit / spd * NH4 * (O2 / (O2 + p->ksO2nitri));
-  double OduOx = p->rODUox / spd * ODU * (O2 / (O2 + p->ksO2oduox));
+  double rnit = p->rnit / spd * fr;
+  double rodu = p->rODUox / spd * fr;
+  double Nitri = rnit * NH4 * (O2 / (O2 + p->ksO2nitri));
+  double OduOx = rodu * ODU * (O2 / (O2 + p->ksO2oduox));
   double fox = p->PAdsODU / (p->PAdsODU + ODU);
   double Rads = p->PAds / spd * (fox * PO4 - (1.0 - fox) * adsP);
   r[0] = -(lim * CprodF);
@@ -272,6 +275,11 @@ static void get_rhs_col(const orc_model *m, int col, const double *conc,
    * the factor is recomputed from the state */
   double f_T = 1.0 * exp(-4500.0 * (1.0 / (T + 273.0) - (1.0 / 288.0)));
   double bioturbation = m->bioturbation;
+  /* temperature factor of the microbial rates (sed_params.temp_activation):
+   * the same Arrhenius form and 288 K reference as f_T */
+  const double fr = m->temp_activation > 0.0
+                        ? exp(-m->temp_activation * (1.0 / (T + 273.0) - (1.0 / 288.0)))
+                        : 1.0;
   if (m->bioturbation_profile == 3) {
     for (int k = 0; k < K; k++) {
       w->cin[k] = conc[IDX(0, k, col, KM, nc)];
@@ -321,7 +329,7 @@ static void get_rhs_col(const orc_model *m, int col, const double *conc,
   for (int k = 0; k < K; k++) {
     for (int n = 0; n < N; n++) w->cell[n] = conc[IDX(n, k, col, KM, nc)];
     double dn = 0.0;
-    orc_omexdia_p(m->bgc_col ? &m->bgc_col[col] : &m->bgc, w->cell, w->rate, &dn);
+    orc_omexdia_p(m->bgc_col ? &m->bgc_col[col] : &m->bgc, fr, w->cell, w->rate, &dn);
     for (int n = 0; n < N; n++)
       rhs[IDX(n, k, col, KM, nc)] = w->rate[n] + w->tr[(size_t)n * K + k];
     if (denit) denit[(size_t)k * nc + col] = dn;

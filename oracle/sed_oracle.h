@@ -71,6 +71,10 @@ typedef struct {
       bioturb_dry_density;
   /* [ncol] a parameter set per column (an ensemble), or NULL for bgc */
   const orc_bgc *bgc_col;
+  /* > 0: rLabile, rSemilabile, CprodMax, rnit and rODUox multiplied by
+   * exp(-temp_activation (1/(T+273) - 1/288)), T the column's temperature
+   * (the Arrhenius form of f_T, fabm_sediment_driver.F90:648); 0: none */
+  double temp_activation;
 } orc_model;
 
 typedef struct {
@@ -101,8 +105,9 @@ void orc_init_profiles(int kmax, const double *zc, const double *zi,
 /* Interface porosity only (update_porosity :434-435). */
 void orc_interface_porosity(int kmax, const double *phi, double *phi_i);
 
-/* a11: OMEXDIA+P local rates for one cell, per second. */
-void orc_omexdia_p(const orc_bgc *p, const double *c, double *r,
+/* a11: OMEXDIA+P local rates for one cell, per second; fr multiplies the
+ * microbial rate constants (the temperature factor; 1 for none). */
+void orc_omexdia_p(const orc_bgc *p, double fr, const double *c, double *r,
                    double *denit);
 
 /* a10: diff3d for one column (fabm_sediment_driver.F90:739-825); all
