@@ -1,0 +1,98 @@
+"""Profiling cases: the launches of one coupling step in a stated regime,
+bracketed by cudaProfilerStart / cudaProfilerStop so that
+``ncu --profile-from-start off`` captures them and nothing of the set-up.
+
+    python -m sedgpu.profcase plain --columns 262144 --day 10
+        one plain FP32 step (budgets on) of the first COLUMNS columns of the
+        2048 x 2048 workload, from the state DAY simulated days in
+    python -m sedgpu.profcase surrogate --day 10
+        the whole 2048 x 2048 workload at day DAY: one plain step, then one
+        gated surrogate step (tolerance 1e-3) with a briefly trained network
+
+The tuning is the workload's autotuned one at DAY.  Run from the repository
+root with ``mossco-code_gb300`` on the path (``python -m`` from that folder,
+or PYTHONPATH)."""
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import capi, synth
+
+
+def _develop(cs, day: float):
+    s = capi.Solver(cs, budgets=True)
+    s.set_forcing()
+    s.set_state(cs.conc)
+    n = int(round(day * 86400.0 / cs.dt))
+    done = 0
+    while done < n:
+        k = min(24, n - done)
+        s.step(k)
+        done += k
+    s.autotune()
+    return s
+
+
+def plain(columns: int, day: float) -> dict:
+    import torch
+    cs = synth.make_workload("surrogate_2048x2048", cols=np.arange(columns))
+    s = _develop(cs, day)
+    s.step(1)   # the graph and tuning in place
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    st = s.step(1)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    t = s.tuning().as_dict()
+    s.close()
+    return {"case": "plain", "columns": int(cs.n_active), "day": day,
+            "tuning": {k: t[k] for k in ("tile_columns", "threads")},
+            "attempts": st["attempts"], "accepted": st["accepted"],
+            "column_steps": st["column_steps"], "device_ms": st["device_ms"]}
+
+
+def surrogate(day: float, train_steps: int = 300) -> dict:
+    import torch
+    from . import surrogate as S
+    train = synth.make_workload("surrogate_200k", cols=np.arange(8192))
+    sur, _ = S.train_surrogate(train, None, nsteps=48, every=3, warm=12,
+                               train_steps=train_steps, batch=2048, log_every=100)
+    cs = synth.make_workload("surrogate_2048x2048")
+    s = _develop(cs, day)
+    s0 = s.get_state()
+    # one untimed pass of each, then the profiled pair from the same state
+    s.step(1)
+    s.set_state(s0)
+    S.step_surrogate(s, sur, 1, tol=1e-3)
+    s.set_state(s0)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    p = s.step(1)
+    s.set_state(s0)
+    q = S.step_surrogate(s, sur, 1, tol=1e-3)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    s.close()
+    sur.close()
+    return {"case": "surrogate", "columns": int(cs.n_active), "day": day,
+            "plain_ms": p["device_ms"], "surrogate_ms": q["device_ms"],
+            "surrogate_columns": q["surrogate_columns"],
+            "launches": {"plain": p["gpu_launches"], "surrogate": q["gpu_launches"]}}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("case", choices=("plain", "surrogate"))
+    ap.add_argument("--columns", type=int, default=262144)
+    ap.add_argument("--day", type=float, default=10.0)
+    a = ap.parse_args(argv)
+    t = time.perf_counter()
+    out = plain(a.columns, a.day) if a.case == "plain" else surrogate(a.day)
+    out["wall_s"] = round(time.perf_counter() - t, 1)
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()
