@@ -247,6 +247,13 @@ struct Lane {
   int bnd_stride;
   __device__ __forceinline__ real bnd(int n) const { return bnd_s[n * bnd_stride]; }
   real src[BC4 ? LPL : 1][BC4 ? NPART : 1];  // capped-flux cascade sources
+  // FP32 form: the surface interface (upper interface of layer 0) carries
+  // no conductance; its flux is alpha b - beta C0 with b the tracer's
+  // surface value, alpha and beta zero on every lane but lane 0.  There:
+  // particulates (a flux condition) alpha_p = 1; dissolved tracers
+  // alpha_d = beta = ad0 (concentration condition, ad0 the dissolved
+  // surface conductance), alpha_d = 1, beta = 0 (flux), or both 0 (none)
+  real alpha_p, alpha_d, beta;
   // FP64 reference-order path (diff3d's own operands)
   real dz[LPL], len[LPL], Dp[LPL], Dd[LPL];
   real ext_a[BC4 ? LPL : 1][BC4 ? NPART : 1];  // cascade additions in the loop
@@ -266,12 +273,16 @@ struct Lane {
 // biomass and the factor beta biomass^b / TOC, folded into the particulate
 // (ap) and dissolved (ad) interface conductances.  Lanes past the column
 // get zero conductances.
+//
+// As in the static form, the surface interface carries no conductance: its
+// dissolved value (lane 0) is returned in ad_top.
 template <typename real, int LPL, bool BC4>
 __device__ __forceinline__ void bio3_conductances(const Params<real>& p,
                                                   const Lane<real, LPL, BC4>& lc,
                                                   int lane, int K,
                                                   const real (&C)[LPL][NTR],
-                                                  real (&ap)[LPL], real (&ad)[LPL]) {
+                                                  real (&ap)[LPL], real (&ad)[LPL],
+                                                  real& ad_top) {
   real wt[LPL];
   real part = real(0);
 #pragma unroll
@@ -285,48 +296,40 @@ __device__ __forceinline__ void bio3_conductances(const Params<real>& p,
   for (int s = 0; s < LPL; s++) {
     const real biomass = wt[s] * lc.gz[s] * part;
     const real fac = sdiv(p.bio_beta * __powf(biomass, p.bio_b), wt[s]);
-    const bool act = s * 32 + lane < K;
-    ap[s] = act ? lc.gb3[s] * fac : real(0);
-    ad[s] = act ? ap[s] + lc.dm[s] : real(0);
+    const int L = s * 32 + lane;
+    const bool inner = L < K && L != 0;
+    const real a = lc.gb3[s] * fac;
+    const real d = a + lc.dm[s];
+    ap[s] = inner ? a : real(0);
+    ad[s] = inner ? d : real(0);
+    if (s == 0) ad_top = L == 0 ? d : real(0);
   }
 }
 
 // diff3d transport of tracer n added to R (FP32 folded form): interface
-// fluxes F = a (C_above - C) with the surface boundary on lane 0, then
-// dC = (F - F_below) / (phi dz).  Branch-free: lanes past the column hold
-// zero state and conductances; the no-flux bottom drops F_below at K-1.
-template <typename real, int LPL, bool BC4>
-__device__ __forceinline__ void transport_one(const Lane<real, LPL, BC4>& lc, int n,
-                                              const real (&apv)[LPL], const real (&adv)[LPL],
-                                              const bool (&bottom)[LPL], bool top,
-                                              bool dirichlet, bool fluxbc, int lane,
-                                              const real (&C)[LPL][NTR], real (&R)[LPL][NTR],
-                                              real (&ftop)[NTR]) {
-  const bool part = n < NPART;
-  real v[LPL], vm[LPL], F[LPL], Fb[LPL];
+// fluxes F = a (C_above - C), the surface interface's flux alpha b - beta C
+// on lane 0 (a = 0 there), then dC = (F - F_below) / (phi dz).  Branch- and
+// select-free: lanes past the column hold zero state and conductances; the
+// no-flux bottom drops F_below at K-1 by the zero conductance below it.
+template <int LPL, bool BC4, bool PART>
+__device__ __forceinline__ void transport_one(const Lane<float, LPL, BC4>& lc, int n,
+                                              const float (&a)[LPL], float alpha, float beta,
+                                              int lane, const float (&C)[LPL][NTR],
+                                              float (&R)[LPL][NTR], float (&ftop)[NTR]) {
+  float v[LPL], vm[LPL], F[LPL], Fb[LPL];
 #pragma unroll
-  for (int s = 0; s < LPL; s++) v[s] = part ? lc.phi[s] * C[s][n] : C[s][n];
-  from_above<real, LPL>(v, vm, lane);
-  const real b = lc.bnd(n);
-  if (part) {
+  for (int s = 0; s < LPL; s++) v[s] = PART ? lc.phi[s] * C[s][n] : C[s][n];
+  from_above<float, LPL>(v, vm, lane);
+  const float ab = alpha * lc.bnd(n);
+  const float top = PART ? ab : fm(-beta, v[0], ab);
 #pragma unroll
-    for (int s = 0; s < LPL; s++) F[s] = apv[s] * (vm[s] - v[s]);
-    F[0] = top ? b : F[0];  // downward flux through the surface (BcUp 1)
-  } else {
-    // Dirichlet (BcUp 2): the surface interface sees the bottom water
-    vm[0] = (top && dirichlet) ? b : vm[0];
-#pragma unroll
-    for (int s = 0; s < LPL; s++) F[s] = adv[s] * (vm[s] - v[s]);
-    F[0] = (top && !dirichlet) ? (fluxbc ? b : real(0)) : F[0];
-  }
+  for (int s = 0; s < LPL; s++) F[s] = s == 0 ? fm(a[s], vm[s] - v[s], top) : a[s] * (vm[s] - v[s]);
   ftop[n] = F[0];
-  from_below<real, LPL>(F, Fb, lane);
+  from_below<float, LPL>(F, Fb, lane);
 #pragma unroll
   for (int s = 0; s < LPL; s++) {
-    // the flux below the last layer is zero by construction: the lane
-    // below holds zero conductance (columns leave the warp's last lane free)
-    const real div = F[s] - Fb[s];
-    if (BC4 && part)
+    const float div = F[s] - Fb[s];
+    if (BC4 && PART)
       R[s][n] = R[s][n] + fm(div, lc.ivol[s], lc.src[BC4 ? s : 0][BC4 ? n : 0]);
     else
       R[s][n] = fm(div, lc.ivol[s], R[s][n]);
@@ -341,10 +344,9 @@ __device__ __forceinline__ float2 splat(float a) { return make_float2(a, a); }
 // scalar operation does), halving the arithmetic instructions.
 template <int LPL, bool BC4, bool PART>
 __device__ __forceinline__ void transport_pair(const Lane<float, LPL, BC4>& lc, int n,
-                                               const float (&a)[LPL], const bool (&bottom)[LPL],
-                                               bool top, bool dirichlet, bool fluxbc, int lane,
-                                               const float (&C)[LPL][NTR], float (&R)[LPL][NTR],
-                                               float (&ftop)[NTR]) {
+                                               const float (&a)[LPL], float alpha, float beta,
+                                               int lane, const float (&C)[LPL][NTR],
+                                               float (&R)[LPL][NTR], float (&ftop)[NTR]) {
   float vx[LPL], vy[LPL], mx[LPL], my[LPL];
   float2 v[LPL], F[LPL];
 #pragma unroll
@@ -356,20 +358,12 @@ __device__ __forceinline__ void transport_pair(const Lane<float, LPL, BC4>& lc, 
   }
   from_above<float, LPL>(vx, mx, lane);
   from_above<float, LPL>(vy, my, lane);
-  const float b0 = lc.bnd(n), b1 = lc.bnd(n + 1);
-  if (!PART) {
-    mx[0] = (top && dirichlet) ? b0 : mx[0];
-    my[0] = (top && dirichlet) ? b1 : my[0];
-  }
+  const float2 ab = __fmul2_rn(splat(alpha), make_float2(lc.bnd(n), lc.bnd(n + 1)));
+  const float2 top = PART ? ab : __ffma2_rn(splat(-beta), v[0], ab);
 #pragma unroll
-  for (int s = 0; s < LPL; s++)
-    F[s] = __fmul2_rn(splat(a[s]), __fadd2_rn(make_float2(mx[s], my[s]), neg2(v[s])));
-  if (PART) {
-    F[0].x = top ? b0 : F[0].x;
-    F[0].y = top ? b1 : F[0].y;
-  } else {
-    F[0].x = (top && !dirichlet) ? (fluxbc ? b0 : 0.0f) : F[0].x;
-    F[0].y = (top && !dirichlet) ? (fluxbc ? b1 : 0.0f) : F[0].y;
+  for (int s = 0; s < LPL; s++) {
+    const float2 d = __fadd2_rn(make_float2(mx[s], my[s]), neg2(v[s]));
+    F[s] = s == 0 ? __ffma2_rn(splat(a[s]), d, top) : __fmul2_rn(splat(a[s]), d);
   }
   ftop[n] = F[0].x;
   ftop[n + 1] = F[0].y;
@@ -393,12 +387,12 @@ __device__ __forceinline__ void transport_pair(const Lane<float, LPL, BC4>& lc, 
   }
 }
 
-// Right-hand side of one column: OMEXDIA+P rates plus diff3d transport.
-// ftop receives the flux through the sediment surface (lane 0 only).
-// Branch-free: lanes beyond the column's K layers hold zero state and zero
-// conductances, so their rates and fluxes vanish by construction; the
-// surface boundary enters by selects on lane 0, the no-flux bottom by
-// dropping the flux from below at layer K-1.
+// Right-hand side of one column (FP32 form): OMEXDIA+P rates plus diff3d
+// transport.  ftop receives the flux through the sediment surface (lane 0
+// only).  Branch-free: lanes beyond the column's K layers hold zero state
+// and zero conductances, so their rates and fluxes vanish by construction;
+// the surface boundary enters through the lane coefficients ab / beta, the
+// no-flux bottom by the zero conductance below layer K-1.
 template <typename real, int LPL, bool BC4, bool BIO3>
 __device__ __forceinline__ void column_rhs(const Params<real>& p,
                                            const Lane<real, LPL, BC4>& lc,
@@ -407,36 +401,30 @@ __device__ __forceinline__ void column_rhs(const Params<real>& p,
                                            real (&R)[LPL][NTR],
                                            real (&ftop)[NTR],
                                            real (&dn)[LPL]) {
+  static_assert(std::is_same<real, float>::value, "FP32 form");
   real apv[LPL], adv[LPL];
+  real alpha_d = lc.alpha_d, beta = lc.beta;
   if constexpr (BIO3) {
-    bio3_conductances<real, LPL, BC4>(p, lc, lane, K, C, apv, adv);
+    real ad_top;
+    bio3_conductances<real, LPL, BC4>(p, lc, lane, K, C, apv, adv, ad_top);
+    if (p.bcup_d == 2) {  // concentration condition, this rhs's conductance
+      alpha_d = ad_top;
+      beta = ad_top;
+    }
   } else {
 #pragma unroll
     for (int s = 0; s < LPL; s++) { apv[s] = lc.ap[s]; adv[s] = lc.ad[s]; }
   }
 #pragma unroll
   for (int s = 0; s < LPL; s++) omexdia_p<real>(p, C[s], R[s], dn[s]);
-  const bool top = lane == 0;
-  const bool dirichlet = p.bcup_d == 2;
-  const bool fluxbc = p.bcup_d == 1;
-  bool bottom[LPL];  // unused by the FP32 form (see transport_one)
-#pragma unroll
-  for (int s = 0; s < LPL; s++) bottom[s] = false;
-  if constexpr (std::is_same<real, float>::value) {
-    // tracer pairs of one class in packed FP32x2 arithmetic, tracer 10 alone
-    transport_pair<LPL, BC4, true>(lc, 0, apv, bottom, top, dirichlet, fluxbc, lane, C, R, ftop);
-    transport_pair<LPL, BC4, true>(lc, 2, apv, bottom, top, dirichlet, fluxbc, lane, C, R, ftop);
-    transport_pair<LPL, BC4, true>(lc, 4, apv, bottom, top, dirichlet, fluxbc, lane, C, R, ftop);
-    transport_pair<LPL, BC4, false>(lc, 6, adv, bottom, top, dirichlet, fluxbc, lane, C, R, ftop);
-    transport_pair<LPL, BC4, false>(lc, 8, adv, bottom, top, dirichlet, fluxbc, lane, C, R, ftop);
-    transport_one<real, LPL, BC4>(lc, NTR - 1, apv, adv, bottom, top, dirichlet, fluxbc, lane, C,
-                                  R, ftop);
-  } else {
-#pragma unroll
-    for (int n = 0; n < NTR; n++)
-      transport_one<real, LPL, BC4>(lc, n, apv, adv, bottom, top, dirichlet, fluxbc, lane, C,
-                                    R, ftop);
-  }
+  // tracer pairs of one class in packed FP32x2 arithmetic, tracer 10 alone
+  const real alpha_p = lc.alpha_p;
+  transport_pair<LPL, BC4, true>(lc, 0, apv, alpha_p, 0.0f, lane, C, R, ftop);
+  transport_pair<LPL, BC4, true>(lc, 2, apv, alpha_p, 0.0f, lane, C, R, ftop);
+  transport_pair<LPL, BC4, true>(lc, 4, apv, alpha_p, 0.0f, lane, C, R, ftop);
+  transport_pair<LPL, BC4, false>(lc, 6, adv, alpha_d, beta, lane, C, R, ftop);
+  transport_pair<LPL, BC4, false>(lc, 8, adv, alpha_d, beta, lane, C, R, ftop);
+  transport_one<LPL, BC4, false>(lc, NTR - 1, adv, alpha_d, beta, lane, C, R, ftop);
 }
 
 // ---------------------------------------------------------------------------

@@ -106,7 +106,7 @@ __device__ __forceinline__ void load_lane(Lane<real, LPL, BC4>& lc,
                                           const real* s_cap,
                                           const real* s_force, int j, int KT,
                                           int tcp, int lane, int K,
-                                          int mol_mode) {
+                                          int mol_mode, int bcup_d) {
   const real bioT = s_force[0 * tcp + j];
   const real dmul = s_force[1 * tcp + j];
 #pragma unroll
@@ -115,6 +115,7 @@ __device__ __forceinline__ void load_lane(Lane<real, LPL, BC4>& lc,
     lc.bnd_stride = tcp;
   }
   real cap[LPL];
+  real ad0 = real(0);  // the dissolved surface conductance (FP32 form, lane 0)
 #pragma unroll
   for (int s = 0; s < LPL; s++) {
     const int L = s * 32 + lane;
@@ -146,11 +147,16 @@ __device__ __forceinline__ void load_lane(Lane<real, LPL, BC4>& lc,
       lc.ap[s] = 0.0;
     } else {
       const real phi = row(0), vol = row(1), gb = row(2), gm = row(3);
+      // the surface interface (L = 0) carries no conductance: its flux is
+      // the lane's ab - beta C (below)
+      const bool inner = act && L != 0;
+      const real d = fm(bioT, gb, dmul * gm);
       lc.phi[s] = act ? phi : real(0);
       lc.vol[s] = act ? vol : real(0);
       lc.ivol[s] = act ? real(1) / vol : real(0);
-      lc.ap[s] = act ? bioT * gb : real(0);
-      lc.ad[s] = act ? fm(bioT, gb, dmul * gm) : real(0);
+      lc.ap[s] = inner ? bioT * gb : real(0);
+      lc.ad[s] = inner ? d : real(0);
+      if (s == 0 && L == 0) ad0 = d;
       if constexpr (BIO3) {
         lc.wc[s] = act ? phi / (real(1) - phi) : real(0);
         lc.gz[s] = act ? row(NCOEF) : real(0);
@@ -164,10 +170,17 @@ __device__ __forceinline__ void load_lane(Lane<real, LPL, BC4>& lc,
     for (int n = 0; n < NTR; n++)
       C[s][n] = act ? s_conc[(n * KT + Lc) * tcp + j] : real(0);
   }
-  if constexpr (std::is_same<real, double>::value)
+  if constexpr (std::is_same<real, double>::value) {
     cascade_ref<LPL, BC4>(lc, cap, lane, K);
-  else
+  } else {
     cascade_sources<real, LPL, BC4>(lc, cap, lane, K);
+    // surface fluxes: particulates and BcUp 1 the given flux, BcUp 2 the
+    // conductance times (bottom water - C0), BcUp 3 none
+    const bool top = lane == 0;
+    lc.alpha_p = top ? real(1) : real(0);
+    lc.alpha_d = !top ? real(0) : (bcup_d == 2 ? ad0 : (bcup_d == 1 ? real(1) : real(0)));
+    lc.beta = (top && bcup_d == 2) ? ad0 : real(0);
+  }
 }
 
 // The right-hand side used by the steppers: folded FP32 form, or the
@@ -266,20 +279,25 @@ struct ColResult {
   double min_dt;
 };
 
-// Compensated running sum (Knuth's TwoSum): FP32 operations carrying the
-// rounding error along, so the per-substep surface-flux integral needs no
-// FP64 arithmetic inside the substep loop.
-template <typename real>
-struct CompSum {
-  real s, c;
-  __device__ __forceinline__ void zero() { s = real(0); c = real(0); }
-  __device__ __forceinline__ void add(real x) {
-    const real t = s + x;
-    const real bp = t - s;
-    c += (s - (t - bp)) + (x - bp);
+// Two compensated running sums (Knuth's TwoSum: t = s + x, bp = t - s,
+// c += (s - (t - bp)) + (x - bp), s = t) in packed FP32x2 arithmetic, each
+// component rounding as the scalar operation would: the per-substep
+// surface-flux integrals of the P and N pools carry their rounding error
+// along without FP64 arithmetic inside the substep loop.
+struct CompSum2 {
+  float2 s, c;
+  __device__ __forceinline__ void zero() { s = make_float2(0.0f, 0.0f); c = s; }
+  __device__ __forceinline__ void add(float2 x) {
+    const float2 t = __fadd2_rn(s, x);
+    const float2 bp = __fadd2_rn(t, make_float2(-s.x, -s.y));
+    const float2 tb = __fadd2_rn(t, make_float2(-bp.x, -bp.y));
+    const float2 e = __fadd2_rn(__fadd2_rn(s, make_float2(-tb.x, -tb.y)),
+                                __fadd2_rn(x, make_float2(-bp.x, -bp.y)));
+    c = __fadd2_rn(c, e);
     s = t;
   }
-  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+  __device__ __forceinline__ double value_x() const { return (double)s.x + (double)c.x; }
+  __device__ __forceinline__ double value_y() const { return (double)s.y + (double)c.y; }
 };
 
 // Budget bookkeeping of one column over one coupling step: column
@@ -335,12 +353,12 @@ struct Budget<double, LPL, BC4> {
 template <int LPL, bool BC4>
 struct Budget<float, LPL, BC4> {
   DW inv0P, inv0N;
-  CompSum<float> inP, inN;
+  CompSum2 inPN;  // surface inflow of the P (x) and N (y) pools
   float n2[LPL];
   __device__ __forceinline__ void start(const Params<float>& p,
                                         const Lane<float, LPL, BC4>& lc,
                                         const float (&C)[LPL][NTR]) {
-    inP.zero(); inN.zero();
+    inPN.zero();
 #pragma unroll
     for (int s = 0; s < LPL; s++) n2[s] = 0.0f;
     if (p.budgets) {
@@ -354,8 +372,11 @@ struct Budget<float, LPL, BC4> {
                                           const float (&ftop)[NTR],
                                           const float (&dn)[LPL]) {
     if (!p.budgets) return;
-    inP.add(w * (ftop[T_FDETP] + ftop[T_ADSP] + ftop[T_PO4]));
-    inN.add(w * (ftop[T_FDETN] + ftop[T_SDETN] + ftop[T_NO3] + ftop[T_NH4]));
+    // P: (FDETP + ADSP) + PO4, N: ((FDETN + SDETN) + NO3) + NH4, in pairs
+    const float2 a = __fadd2_rn(make_float2(ftop[T_FDETP], ftop[T_FDETN]),
+                                make_float2(ftop[T_ADSP], ftop[T_SDETN]));
+    const float2 b = __fadd2_rn(a, make_float2(ftop[T_PO4], ftop[T_NO3]));
+    inPN.add(__fmul2_rn(make_float2(w, w), make_float2(b.x, b.y + ftop[T_NH4])));
 #pragma unroll
     for (int s = 0; s < LPL; s++) n2[s] = fmaf(w * 0.8f, dn[s], n2[s]);
   }
@@ -375,9 +396,9 @@ struct Budget<float, LPL, BC4> {
     if (lane == 0) {  // lane 0 holds the surface inflow sums
       const double v1P = dw_value(inv1P), v1N = dw_value(inv1N);
       bud[0] = v1P;
-      bud[1] = v1P - dw_value(inv0P) - inP.value();
+      bud[1] = v1P - dw_value(inv0P) - inPN.value_x();
       bud[2] = v1N;
-      bud[3] = v1N - dw_value(inv0N) - inN.value() + dw_value(loss);
+      bud[3] = v1N - dw_value(inv0N) - inPN.value_y() + dw_value(loss);
     }
   }
 };
@@ -656,7 +677,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       Lane<real, LPL, BC4> lc;
       real C[LPL][NTR];
       load_lane<real, LPL, BC4, BIO3>(lc, C, s_conc, s_coef, s_cap, s_force, j, KT,
-                                      tcp, lane, K, p.mol_mode);
+                                      tcp, lane, K, p.mol_mode, p.bcup_d);
       real ftop[NTR];
 #pragma unroll
       for (int n = 0; n < NTR; n++) ftop[n] = real(0);
@@ -815,7 +836,7 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
     // per tracer / coefficient, columns of stride nslot; then the surface
     // values the substeps read come from the warp's shared copy
     load_lane<real, LPL, BC4, BIO3>(lc, C, a.conc, a.coef, a.cap, a.force, slot, a.kmax,
-                                    (int)ns, lane, K, p.mol_mode);
+                                    (int)ns, lane, K, p.mol_mode, p.bcup_d);
     lc.bnd_s = sb + 2;
     lc.bnd_stride = 1;
     Params<real> pc = p;
