@@ -119,7 +119,7 @@ struct sed_handle {
   DevBuf d_bgc_base, d_rfac;  // its unscaled form; [ncol] rate factors
   DevBuf d_slot_col, d_kact, d_tile_k, d_conc, d_coef, d_cap, d_force, d_sflux,
       d_budget, d_nsub, d_queue, d_stats, d_flag, d_stage, d_bdys, d_fluxes,
-      d_rhs, d_rhs_stage, d_grid, d_force64, d_skip, d_xfeat, d_yhat, d_backup,
+      d_rhs, d_rhs_stage, d_grid, d_force64, d_xfeat, d_yhat, d_backup,
       d_col_slot, d_top, d_bcin, d_mindt;
   // surrogate step: heavy-column slot list, its counter, hidden activations
   DevBuf d_list, d_gate, d_act;
@@ -1381,8 +1381,7 @@ static cudaError_t launch_warp_columns(sed_handle* h, const ColumnArgs<float>& a
                                        const Params<float>& p, const Bin& bin, int kind) {
   const bool bc4 = h->prm.bcup_particulate == 4;
   const int threads = bin.threads;
-  const int occ = column_warp_blocks_per_sm<float>(
-      bin.lpl, bc4, kind == KIND_FIXED ? KIND_FIXED : KIND_ADAPT, threads, p.bio3 != 0);
+  const int occ = column_warp_blocks_per_sm<float>(bin.lpl, bc4, kind, threads, p.bio3 != 0);
   const int warps = threads / 32;
   const int blocks =
       std::max(1, std::min(std::max(occ, 1) * h->sms, (a.ntiles + warps - 1) / warps));
@@ -1416,7 +1415,6 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
   const Bin& bin = h->bins[b];
   const size_t ns = h->nslot;
   const int maxrows = pad128(bin.nslots);
-  CK(h->d_skip.alloc(ns * sizeof(int)), "skip flags");
   CK(h->d_list.alloc((size_t)bin.nslots * sizeof(int)), "heavy list");
   CK(h->d_gate.alloc(128), "heavy counter");
   CK(h->d_xfeat.alloc((size_t)maxrows * s->pin[0] * sizeof(bf16)), "features");
@@ -1428,12 +1426,21 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
   Params<float> p = make_params<float>(h->prm);
   set_clock(p, dt, h->prm.dt_min);
   // the gate's tile kernel: the class's tile width (or, for a warp-direct
-  // class, the width its other kinds use); the occupancy query also raises
-  // the kernel's shared-memory limit, before any launch
+  // class, the width its other kinds use), with 256 threads where that fits
+  // (one attempt per column is latency-bound: the more resident warps, the
+  // better; 8.0 ms against 11.9 ms at 128 threads on the 2048^2 grid at day
+  // 10); the occupancy query also raises the kernel's shared-memory limit,
+  // before any launch
   const bool bc4 = h->prm.bcup_particulate == 4;
   const int gate_tc = bin.tc ? bin.tc : bin.tc_fb;
-  const int gate_occ =
-      column_blocks_per_sm<float>(gate_tc, bin.lpl, bc4, KIND_PROBE, bin.threads, p.bio3 != 0);
+  int gate_threads = 256;
+  int gate_occ =
+      column_blocks_per_sm<float>(gate_tc, bin.lpl, bc4, KIND_PROBE, gate_threads, p.bio3 != 0);
+  if (gate_occ <= 0) {
+    gate_threads = bin.threads;
+    gate_occ = column_blocks_per_sm<float>(gate_tc, bin.lpl, bc4, KIND_PROBE, gate_threads,
+                                           p.bio3 != 0);
+  }
   if (gate_occ <= 0) return h->fail(SED_E_CUDA, "the gate's tile kernel does not fit");
   unsigned* nheavy = h->d_gate.as<unsigned>();
   int* list = h->d_list.as<int>();
@@ -1457,7 +1464,7 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
     }
     a.ntiles = bin.nslots / gate_tc;
     CK(launch_column<float>(a, p, bin.lpl, bc4, KIND_PROBE,
-                            std::max(1, std::min(a.ntiles, gate_occ * h->sms)), bin.threads,
+                            std::max(1, std::min(a.ntiles, gate_occ * h->sms)), gate_threads,
                             h->stream),
        "gate launch");
     h->launches++;
@@ -1480,8 +1487,9 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
     // one fused kernel, or one GEMM per layer
     h->launches -= sur_uses_tc(s) ? s->L - 1 : 0;
     h->launches += 1 + s->L;
-    // 3. each column's proposal from its prediction row and its residual
-    //    test; passing ones replace the state
+    // 3. each listed column's proposal from its prediction row and its
+    //    residual test; a column whose proposal passes takes it, the others
+    //    take the plain adaptive step from their state, in the same kernel
     ColumnArgs<float> r = column_args<float>(h, bin, b, dt, SED_ADAPTIVE_EULER);
     r.list = list;
     r.ntiles = nh;
@@ -1490,19 +1498,11 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
     r.norm = s->norm;
     r.nin = s->nin;
     r.nout = s->nout;
-    r.skip = h->d_skip.as<int>();
     r.res_tol = tol;
     r.res_atol = res_atol;
     CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
-    CK(launch_warp_columns(h, r, p, bin, KIND_RESID), "residual launch");
-    // 4. the plain solver on the listed columns that failed it
-    ColumnArgs<float> f = column_args<float>(h, bin, b, dt, SED_ADAPTIVE_EULER);
-    f.list = list;
-    f.ntiles = nh;
-    f.skip = h->d_skip.as<int>();
-    CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
-    CK(launch_warp_columns(h, f, p, bin, KIND_ADAPT), "fallback launch");
-    h->launches += 2;
+    CK(launch_warp_columns(h, r, p, bin, KIND_SUR), "residual and fallback launch");
+    h->launches++;
   }
   CK(cudaEventRecord(h->ev1, h->stream), "event");
   rc = stats_fetch(h, stats, l0, true);

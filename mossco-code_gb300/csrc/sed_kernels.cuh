@@ -51,8 +51,22 @@ size_t tile_smem_bytes(int tc, int lpl, bool bc4, int kind, bool bio3) {
   return TileLayout<real>(tc, 32 * lpl, bc4, coef_rows<real>(bio3)).total;
 }
 
+// 16-byte global -> shared copy in flight (cp.async, L2 only): a thread
+// issues all its pieces of a tile before waiting once, instead of one
+// load-to-use latency per piece.  Both addresses are 16-byte aligned: tiles
+// start at multiples of 8 slots, rows are padded to 16 bytes.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 // Copy `rows` rows of tc reals between global (row stride gstride, first
 // element at gbase + row_index*gstride) and shared memory (row stride tcp).
+// To shared memory the copies are asynchronous: cp_async_wait_all before
+// the block barrier that publishes them.
 template <typename real, bool TO_SHARED>
 __device__ __forceinline__ void copy_rows(real* sm, real* gbase, size_t gstride,
                                           int rows, int tc, int tcp,
@@ -67,7 +81,7 @@ __device__ __forceinline__ void copy_rows(real* sm, real* gbase, size_t gstride,
     real* g = gbase + (size_t)row * row_step_global * gstride + v * EPV;
     real* s = sm + (size_t)row * tcp + v * EPV;
     if (TO_SHARED)
-      *reinterpret_cast<uint4*>(s) = *reinterpret_cast<const uint4*>(g);
+      cp_async16(s, g);
     else
       *reinterpret_cast<uint4*>(g) = *reinterpret_cast<const uint4*>(s);
   }
@@ -91,7 +105,7 @@ __device__ __forceinline__ void copy_grouped(real* sm, real* g0, int ngroups,
     real* gp = g0 + ((size_t)g * kmax + k) * nslot + v * EPV;
     real* sp = sm + ((size_t)g * KT + k) * tcp + v * EPV;
     if (TO_SHARED)
-      *reinterpret_cast<uint4*>(sp) = *reinterpret_cast<const uint4*>(gp);
+      cp_async16(sp, gp);
     else
       *reinterpret_cast<uint4*>(gp) = *reinterpret_cast<const uint4*>(sp);
   }
@@ -655,6 +669,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
                                KT, a.kmax, ns, tc, tcp, tid, nthr);
     copy_rows<real, true>(s_force, const_cast<real*>(a.force) + slot0, ns,
                           NFORCE, tc, tcp, 1, tid, nthr);
+    cp_async_wait_all();
     __syncthreads();
 
     for (;;) {
@@ -813,16 +828,12 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
     // columns), or of the slot range
     const int slot = a.list ? a.list[j] : a.slot0 + j;
     const int K = a.kact[slot];
-    // (KIND_RESID writes the skip flags; the stepping kinds read them)
-    const bool skipped = KIND != KIND_RESID && a.skip && K > 0 && a.skip[slot];
-    if (K <= 0 || skipped) {
-      // land or padding: zero outputs; accepted surrogate step: the state
-      // and surface flux are already in place
+    if (K <= 0) {
+      // land or padding: zero outputs
       if (lane == 0) {
         a.nsub[slot] = 0;
         if (a.mindt) a.mindt[slot] = 0.0;
-        if (!skipped)
-          for (int d = 0; d < NDISS; d++) a.sflux[d * ns + slot] = real(0);
+        for (int d = 0; d < NDISS; d++) a.sflux[d * ns + slot] = real(0);
         if (a.budget)
           for (int b = 0; b < 4; b++) a.budget[b * ns + slot] = 0.0;
       }
@@ -842,10 +853,12 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
     Params<real> pc = p;
     if (ENS) load_bgc(pc, a.bgc, ns, slot);
     real ftop[NTR];
-    if constexpr (KIND == KIND_RESID) {
+    if constexpr (KIND == KIND_SUR) {
       // The network's proposal P from the state C and prediction row j:
       // P = max(exp(log(max(C, 0) + c0) + mu_d + sd_d y) - c0, 0), cell
       // (n, k) at feature n K + k (every column has K = kmax layers here).
+      // C stays the start state for the fallback.
+      real P[LPL][NTR];
       {
         const float* yr = a.yhat + (size_t)j * a.ldy;
         const float* c0 = a.norm;
@@ -854,13 +867,15 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
 #pragma unroll
         for (int s = 0; s < LPL; s++) {
           const int L = s * 32 + lane;
-          if (L < K)
 #pragma unroll
-            for (int n = 0; n < NTR; n++) {
+          for (int n = 0; n < NTR; n++) {
+            P[s][n] = C[s][n];  // lanes past the column: zero
+            if (L < K) {
               const int f = n * K + L;
               const float u = logf(fmaxf((float)C[s][n], 0.0f) + c0[n]) + mud[f] + sdd[f] * yr[f];
-              C[s][n] = (real)fmaxf(expf(u) - c0[n], 0.0f);
+              P[s][n] = (real)fmaxf(expf(u) - c0[n], 0.0f);
             }
+          }
         }
       }
       // Quasi-steady test of P: the plain right-hand side at P may change no
@@ -869,35 +884,35 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
       // end of a column's heavy steps the plain solver's own states change
       // by about 1 % per step this way; a proposal off the slow manifold of
       // the stiff cells fails by orders of magnitude.  NaN fails.
-      epilogue<real, LPL>(pc, lane, K, C);
-      real R[LPL][NTR];
-      real dn[LPL];
+      epilogue<real, LPL>(pc, lane, K, P);
+      bool pass;
+      {
+        real R[LPL][NTR];
+        real dn[LPL];
 #pragma unroll
-      for (int n = 0; n < NTR; n++) ftop[n] = real(0);
-      rhs_any<real, LPL, BC4, BIO3>(pc, lc, lane, K, C, R, ftop, dn);
-      const real dtr = (real)a.dt, at = (real)a.res_atol, tol = (real)a.res_tol;
-      bool ok = true;
+        for (int n = 0; n < NTR; n++) ftop[n] = real(0);
+        rhs_any<real, LPL, BC4, BIO3>(pc, lc, lane, K, P, R, ftop, dn);
+        const real dtr = (real)a.dt, at = (real)a.res_atol, tol = (real)a.res_tol;
+        bool ok = true;
 #pragma unroll
-      for (int s = 0; s < LPL; s++) {
-        const int L = s * 32 + lane;
-        if (L < K)
+        for (int s = 0; s < LPL; s++) {
+          const int L = s * 32 + lane;
+          if (L < K)
 #pragma unroll
-          for (int n = 0; n < NTR; n++)
-            ok = ok && (dtr * fabs(R[s][n]) <= tol * (fabs(C[s][n]) + at));
+            for (int n = 0; n < NTR; n++)
+              ok = ok && (dtr * fabs(R[s][n]) <= tol * (fabs(P[s][n]) + at));
+        }
+        pass = __all_sync(FULL, ok);
       }
-      const bool pass = __all_sync(FULL, ok);
       if (pass) {
 #pragma unroll
         for (int s = 0; s < LPL; s++) {
           const int L = s * 32 + lane;
           if (L < K)
 #pragma unroll
-            for (int n = 0; n < NTR; n++) a.conc[((size_t)n * a.kmax + L) * ns + slot] = C[s][n];
+            for (int n = 0; n < NTR; n++) a.conc[((size_t)n * a.kmax + L) * ns + slot] = P[s][n];
         }
-      }
-      if (lane == 0) {
-        a.skip[slot] = pass ? 1 : 0;
-        if (pass) {
+        if (lane == 0) {
 #pragma unroll
           for (int d = 0; d < NDISS; d++) a.sflux[d * ns + slot] = ftop[NPART + d];
           a.nsub[slot] = 0;
@@ -907,9 +922,10 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
           atomicAdd(&b_sur, 1ull);
           atomicAdd(&b_cols, 1ull);
         }
+        __syncwarp();
+        continue;
       }
-      __syncwarp();
-      continue;
+      // failed: the plain adaptive step from C, below
     }
     double bud[4];
     ColResult r;
@@ -920,7 +936,7 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
 #pragma unroll
       for (int n = 0; n < NTR; n++) ftop[n] = real(0);
       for (int b = 0; b < 4; b++) bud[b] = 0.0;
-      if (KIND == KIND_ADAPT)
+      if (KIND == KIND_ADAPT || KIND == KIND_SUR)
         r = pc.ticks
                 ? solve_adaptive<real, LPL, BC4, BIO3, true>(pc, lc, lane, K, C, ftop, a.dt, bud)
                 : solve_adaptive<real, LPL, BC4, BIO3, false>(pc, lc, lane, K, C, ftop, a.dt, bud);
@@ -1443,12 +1459,12 @@ static cudaError_t launch_warp_t(const ColumnArgs<real>& a, const Params<real>& 
 template <typename real, int LPL, bool BC4, bool BIO3, bool ENS>
 cudaError_t launch_warp_e(const ColumnArgs<real>& a, const Params<real>& p, int kind,
                           int blocks, int threads, cudaStream_t st) {
-  if (kind == KIND_RESID) {
-    // the surrogate step's residual test: FP32 state, one parameter set
+  if (kind == KIND_SUR) {
+    // the surrogate step's residual test and fallback: FP32 state, one
+    // parameter set
     if constexpr (std::is_same<real, float>::value && !ENS) {
       if (a.nrepeat > 1) return cudaErrorInvalidValue;
-      return launch_warp_t<real, LPL, BC4, BIO3, KIND_RESID, false, ENS>(a, p, blocks, threads,
-                                                                        st);
+      return launch_warp_t<real, LPL, BC4, BIO3, KIND_SUR, false, ENS>(a, p, blocks, threads, st);
     }
     return cudaErrorInvalidValue;
   }
@@ -1485,6 +1501,11 @@ static int warp_occupancy_t(int threads) {
 template <typename real, int LPL, bool BC4, bool BIO3>
 int warp_occupancy_k(int kind, int threads) {
   if (kind == KIND_FIXED) return warp_occupancy_t<real, LPL, BC4, BIO3, KIND_FIXED, false>(threads);
+  if (kind == KIND_SUR) {
+    if constexpr (std::is_same<real, float>::value)
+      return warp_occupancy_t<real, LPL, BC4, BIO3, KIND_SUR, false>(threads);
+    return 0;
+  }
   return std::min(warp_occupancy_t<real, LPL, BC4, BIO3, KIND_ADAPT, false>(threads),
                   warp_occupancy_t<real, LPL, BC4, BIO3, KIND_ADAPT, true>(threads));
 }

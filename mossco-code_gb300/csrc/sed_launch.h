@@ -8,9 +8,9 @@
 
 namespace sed {
 
-// KIND_PROBE and KIND_RESID are the surrogate step's gate (tile kernel) and
-// residual test (warp-direct kernel), FP32 state only
-enum : int { KIND_ADAPT = 0, KIND_FIXED = 1, KIND_RHS = 2, KIND_RESID = 3, KIND_PROBE = 4 };
+// KIND_PROBE and KIND_SUR are the surrogate step's gate (tile kernel) and
+// its residual test with the plain fallback (warp-direct kernel), FP32 state
+enum : int { KIND_ADAPT = 0, KIND_FIXED = 1, KIND_RHS = 2, KIND_SUR = 3, KIND_PROBE = 4 };
 
 // Arguments of the tile kernel.  Device layouts (slot = compacted column):
 //   conc  [NTR][kmax][nslot]     coef  [coef_rows][kmax][nslot]
@@ -37,11 +37,9 @@ struct ColumnArgs {
   int nslot, kmax, tc, slot0, tile0, ntiles;
   double dt;
   int method;
-  // surrogate coupling step: per-slot flags (1 = the surrogate's state was
-  // accepted, the step kernels skip the column) and the tolerances of the
-  // residual test (KIND_RESID: the proposal, formed from yhat, is written
-  // into conc when it passes)
-  int* skip;
+  // surrogate coupling step (KIND_SUR): the tolerances of the residual test;
+  // a proposal that passes is written into conc, a column whose proposal
+  // fails takes the plain adaptive step
   double res_tol, res_atol;
   // warp-direct kernel: the launch's columns are list[0 .. ntiles) (slots)
   // instead of the slot range.  KIND_PROBE (tile kernel) appends the slot of
@@ -50,7 +48,7 @@ struct ColumnArgs {
   const int* list;
   int* heavy;
   unsigned* nheavy;
-  // KIND_RESID: the network's prediction rows (row j for the list's j-th
+  // KIND_SUR: the network's prediction rows (row j for the list's j-th
   // column, pitch ldy) and its normalisation c0[11] | mu_x[nin] | sd_x[nin] |
   // mu_d[nout] | sd_d[nout]
   const float* yhat;
