@@ -109,6 +109,16 @@ int pel_set_forcing(pel_handle *h, const double *I_0, const double *albedo,
                     const double *bottom_flux, const double *surface_flux,
                     const double *soil_flux);
 
+/* Vertically homogeneous open-boundary values of the Run
+ * (fabm_pelagic_component.F90:2115-2155, `<name>_boundary_value_hz`
+ * fields): after every internal step's bottom fluxes, every water cell of a
+ * column with open_boundary[col] != 0 takes boundary_value[n][col] for each
+ * tracer n with has_value[n] != 0 (a field present in the import state).
+ * open_boundary [ncol] (NULL: no open boundary from now on),
+ * boundary_value [ntr][ncol], has_value [ntr]. */
+int pel_set_open_boundary(pel_handle *h, const int *open_boundary,
+                          const double *boundary_value, const int *has_value);
+
 int pel_set_state(pel_handle *h, const double *conc);
 int pel_get_state(pel_handle *h, double *conc);
 

@@ -62,6 +62,11 @@ struct Args {
   const real* bfl;            // [NTR][ncol] or null
   const real* sfl;
   const real* soil;
+  // open boundaries (fabm_pelagic_component.F90:2115-2155): columns with
+  // ob[col] set take bv[n][col] in every layer for each tracer n of bvmask
+  const unsigned char* ob;    // [ncol] or null
+  const real* bv;             // [NTR][ncol]
+  unsigned bvmask;
   real* par;                  // [K][ncol]
   const int* wcols;           // [nwater] columns with a water cell, ascending
   int nwater;
@@ -292,9 +297,10 @@ __device__ __forceinline__ void step_cell(const Args<real>& a, real (&c)[NTR], r
 
 // The Run's per-step epilogue on one cell (fabm_pelagic_component.F90):
 // NaN count after ode_solver (:2084), the soil-surface upward fluxes where
-// the bottom layer has a height (:2100-2105), the external surface fluxes
-// into the top layer (:2193-2194), the soil-surface flux fields unless the
-// bottom cell would go negative (:2196-2203), then clip_below_minimum
+// the bottom layer has a height (:2100-2105), the vertically homogeneous
+// open-boundary values (:2115-2155), the external surface fluxes into the
+// top layer (:2193-2194), the soil-surface flux fields unless the bottom
+// cell would go negative (:2196-2203), then clip_below_minimum
 // (fabm_pelagic_driver.F90:910-927).
 template <typename real>
 __device__ __forceinline__ void epilogue_cell(const Args<real>& a, real (&c)[NTR], int k, int col,
@@ -305,6 +311,11 @@ __device__ __forceinline__ void epilogue_cell(const Args<real>& a, real (&c)[NTR
   if (k == 0 && a.bfl && hk > real(0)) {
 #pragma unroll
     for (int n = 0; n < NTR; n++) c[n] = c[n] + a.bfl[(size_t)n * a.ncol + col] * dt / hk;
+  }
+  if (a.ob && a.ob[col]) {
+#pragma unroll
+    for (int n = 0; n < NTR; n++)
+      if ((a.bvmask >> n) & 1u) c[n] = a.bv[(size_t)n * a.ncol + col];
   }
   if (k == a.K - 1 && a.sfl) {
 #pragma unroll
@@ -566,8 +577,9 @@ struct pel_handle {
   std::string err;
   bool have_grid = false, have_forcing = false, have_state = false, have_par = false;
   bool has_mask = false, has_alb = false, has_bfl = false, has_sfl = false, has_soil = false;
+  unsigned bvmask = 0;  // tracers with open-boundary values (0: none)
   DevBuf d_h, d_mask, d_I0, d_alb, d_bfl, d_sfl, d_soil, d_par, d_state, d_stage, d_rhs,
-      d_work, d_stats, d_wcols;
+      d_work, d_stats, d_wcols, d_ob, d_bv;
   DevStats* h_stats = nullptr;  // pinned
   long long launches = 0;
   std::vector<int> wcols;       // host copy of d_wcols
@@ -696,6 +708,9 @@ Args<real> make_args(pel_handle* h, double t_couple, double dt) {
   a.bfl = h->has_bfl ? h->d_bfl.as<real>() : nullptr;
   a.sfl = h->has_sfl ? h->d_sfl.as<real>() : nullptr;
   a.soil = h->has_soil ? h->d_soil.as<real>() : nullptr;
+  a.ob = h->bvmask ? h->d_ob.as<unsigned char>() : nullptr;
+  a.bv = h->bvmask ? h->d_bv.as<real>() : nullptr;
+  a.bvmask = h->bvmask;
   a.par = h->d_par.as<real>();
   a.wcols = h->d_wcols.as<int>();
   a.nwater = h->water_cols;
@@ -1186,6 +1201,39 @@ int pel_set_forcing(pel_handle* h, const double* I_0, const double* albedo,
   h->has_soil = soil_flux != nullptr;
   h->have_forcing = true;
   h->have_par = false;
+  return SED_OK;
+}
+
+int pel_set_open_boundary(pel_handle* h, const int* open_boundary,
+                          const double* boundary_value, const int* has_value) {
+  if (!h) return SED_E_ARG;
+  if (!h->have_grid) return h->fail(SED_E_STATE, "pel_set_grid has not been called");
+  cudaSetDevice(h->device);
+  if (!open_boundary) {
+    h->bvmask = 0;
+    return SED_OK;
+  }
+  if (!boundary_value || !has_value)
+    return h->fail(SED_E_ARG, "boundary_value and has_value are required");
+  const size_t nc = h->ncol;
+  unsigned mask = 0;
+  for (int n = 0; n < NTR; n++)
+    if (has_value[n]) mask |= 1u << n;
+  std::vector<unsigned char> ob(nc);
+  for (size_t c = 0; c < nc; c++) ob[c] = open_boundary[c] != 0;
+  for (int n = 0; n < NTR; n++) {
+    if (!(mask >> n & 1u)) continue;
+    for (size_t c = 0; c < nc; c++)
+      if (ob[c] && !std::isfinite(boundary_value[(size_t)n * nc + c]))
+        return h->fail(SED_E_ARG, "boundary value %d of open column %zu is not finite", n, c);
+  }
+  PK(h->d_ob.alloc(nc), "open boundary");
+  PK(cudaMemcpyAsync(h->d_ob.p, ob.data(), nc, cudaMemcpyHostToDevice, h->stream),
+     "open boundary");
+  PK(cudaStreamSynchronize(h->stream), "open boundary");  // ob goes out of scope
+  int rc = upload(h, h->d_bv, boundary_value, NTR * nc, "boundary values");
+  if (rc) return rc;
+  h->bvmask = mask;
   return SED_OK;
 }
 

@@ -67,6 +67,11 @@ module pel_gpu
       import :: c_int, c_ptr
       type(c_ptr), value :: h, I_0, albedo, bottom_flux, surface_flux, soil_flux
     end function
+    integer(c_int) function pel_set_open_boundary(h, open_boundary, boundary_value, &
+                                                  has_value) bind(C, name='pel_set_open_boundary')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, open_boundary, boundary_value, has_value
+    end function
     integer(c_int) function pel_set_state(h, conc) bind(C, name='pel_set_state')
       import :: c_int, c_ptr
       type(c_ptr), value :: h, conc
@@ -107,7 +112,7 @@ module pel_gpu
   end interface
 
   public :: pel_default_params, pel_create, pel_destroy, pel_set_grid, pel_set_forcing, &
-            pel_set_state, pel_get_state, pel_light, pel_get_rhs, pel_ode_solver, &
+            pel_set_open_boundary, pel_set_state, pel_get_state, pel_light, pel_get_rhs, pel_ode_solver, &
             pel_run, pel_step, pel_last_error
   public :: pel_gpu_init, pel_gpu_forcing, pel_gpu_run, pel_gpu_ode_solver, pel_gpu_finalize
 

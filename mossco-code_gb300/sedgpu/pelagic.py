@@ -83,6 +83,7 @@ PEL_SIGNATURES = {
     "pel_last_error": (ctypes.c_char_p, [_H]),
     "pel_set_grid": (_i, [_H, _dp, _ip]),
     "pel_set_forcing": (_i, [_H, _dp, _dp, _dp, _dp, _dp]),
+    "pel_set_open_boundary": (_i, [_H, _ip, _dp, _ip]),
     "pel_set_state": (_i, [_H, _dp]),
     "pel_get_state": (_i, [_H, _dp]),
     "pel_light": (_i, [_H, _dp, _dp]),
@@ -258,6 +259,24 @@ class PelagicSolver:
         arrs = [None if a is None else _f64(a) for a in arrs]
         self._check(self.lib.pel_set_forcing(self.h, *[_p(a) for a in arrs]),
                     "pel_set_forcing")
+
+    def set_open_boundary(self, open_boundary=None, boundary_value=None, has_value=None):
+        """Open-boundary values (fabm_pelagic_component.F90:2115-2155):
+        open_boundary [ncol] (nonzero: open; None: none), boundary_value
+        [ntr][ncol]; has_value [ntr] defaults to the tracers whose values
+        are finite in every open column."""
+        if open_boundary is None:
+            self._check(self.lib.pel_set_open_boundary(self.h, None, None, None),
+                        "pel_set_open_boundary")
+            return
+        ob = np.ascontiguousarray(np.asarray(open_boundary) != 0, dtype=np.int32)
+        bv = _f64(boundary_value)
+        if has_value is None:
+            has_value = [bool(np.isfinite(bv[n, ob != 0]).all()) for n in range(PEL_NTR)]
+        hv = np.ascontiguousarray(np.asarray(has_value) != 0, dtype=np.int32)
+        bv = np.where(np.isfinite(bv), bv, 0.0)   # rows without a value are not read
+        self._check(self.lib.pel_set_open_boundary(self.h, _p(ob, _ip), _p(_f64(bv)),
+                                                   _p(hv, _ip)), "pel_set_open_boundary")
 
     def set_state(self, conc):
         self._check(self.lib.pel_set_state(self.h, _p(_f64(conc))), "pel_set_state")

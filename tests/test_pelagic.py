@@ -192,7 +192,7 @@ def test_library_exports_pelagic_abi():
     path = build.build()
     text = open(f"{build.INCLUDE}/mossco_pel.h").read()
     declared = sorted(set(re.findall(r"\b(pel_[a-z_]+)\s*\(", text)))
-    assert len(declared) == 13
+    assert len(declared) == 14
     out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True,
                          text=True, check=True).stdout
     exported = {l.split()[-1] for l in out.splitlines() if " T " in l}
@@ -444,3 +444,51 @@ def test_soil_flux_guard_and_clip_fp64_bit_exact(po):
         w = pcs.water()
         np.testing.assert_array_equal(out[:, w], ref[:, w])
         assert np.all(out[1][w] >= 0.3)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cut", [pelagic.PEL_CUT_PER_CELL, pelagic.PEL_CUT_GLOBAL])
+def test_open_boundary_values_fp64_bit_exact(po, cut):
+    """The Run's vertically homogeneous open-boundary values
+    (fabm_pelagic_component.F90:2115-2155) on the device: after every
+    internal step's bottom fluxes an open column takes the value of every
+    tracer that has one.  FP64 equals the oracle bit for bit for both cut
+    scopes and every method; FP32 is close; clearing the boundaries gives
+    the run without them."""
+    pcs = small(96, seed=9)
+    water = np.flatnonzero(pcs.water().all(axis=0))
+    ob = np.zeros(pcs.ncol, dtype=np.int32)
+    ob[water[[0, 5, 11, 40]]] = 1
+    bv = np.full((4, pcs.ncol), np.nan)
+    bv[0], bv[3] = 7.5, 0.25
+    bv[1, ob != 0] = np.linspace(0.1, 0.4, int(ob.sum()))
+
+    def device(precision, method, open_=True):
+        s = pelagic.PelagicSolver(pcs, precision=precision, cut_scope=cut)
+        if open_:
+            s.set_open_boundary(ob, bv)
+        s.set_state(pcs.conc)
+        st = s.step(2, method=method)
+        out = s.get_state()
+        if open_:   # cleared: the next Run has no boundary values
+            s.set_open_boundary(None)
+        s.close()
+        return out, st
+
+    w = pcs.water()
+    for method in (EULER, RUNGE_KUTTA_4, ADAPTIVE_EULER):
+        out, st = device(capi.SED_FP64, method)
+        ref = pcs.conc.copy()
+        rc, sref, _ = po.PelOracle(pcs, cut_scope=cut, open_boundary=ob,
+                                   boundary_value=bv).run(ref, method=method, nruns=2)
+        assert rc == 0
+        np.testing.assert_array_equal(out[:, w], ref[:, w])
+        assert st["attempts"] == sref["attempts"]
+        plain, _ = device(capi.SED_FP64, method, open_=False)
+        assert not np.array_equal(plain[:, w], out[:, w])
+    out32, _ = device(capi.SED_FP32, RUNGE_KUTTA_4)
+    ref = pcs.conc.copy()
+    po.PelOracle(pcs, cut_scope=cut, open_boundary=ob, boundary_value=bv).run(
+        ref, method=RUNGE_KUTTA_4, nruns=2)
+    scale = np.abs(ref[:, w]).max(axis=1, keepdims=True)
+    assert np.max(np.abs(out32[:, w] - ref[:, w]) / scale) < 1e-4
