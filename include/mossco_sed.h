@@ -109,6 +109,11 @@ typedef struct sed_params {
    * kernels, as per-column parameter sets do; the surrogate, training rows,
    * sed_get_rhs and sed_ode_solver_noalloc refuse it. */
   double temp_activation;
+  /* type_rhs_driver's adaptive_solver_diagnostics (solver_library.F90:43,
+   * :129-136): with SED_CUT_GLOBAL, every accepted adaptive substep smaller
+   * than the smallest so far records its size and the grid cell of the
+   * smallest relative change (c1 - c) / c; see sed_get_min_dt_grid_cell. */
+  int adaptive_solver_diagnostics;
 } sed_params;
 
 typedef struct sed_stats {
@@ -242,6 +247,16 @@ int sed_get_min_dt(sed_handle *h, double *min_dt);
  * A column whose set equals the handle's gives the same bits as without. */
 #define SED_NBGC 17
 int sed_set_column_bgc(sed_handle *h, const double *params);
+
+/* type_rhs_driver's last_min_dt and last_min_dt_grid_cell
+ * (solver_library.F90:44-45, :129-136), kept across calls since sed_create:
+ * 1e20 (as a default real) and -99 until a recording substep.  cell[4] =
+ * (i, j, k, n), 1-based, of the smallest relative change in the substep
+ * that set last_min_dt; NaN quotients are skipped (gfortran's MINLOC), and
+ * cells the solver does not step count with relative change 0.  Recorded by
+ * the grid-wide cut (SED_CUT_GLOBAL) with adaptive_solver_diagnostics set;
+ * SED_E_STATE otherwise. */
+int sed_get_min_dt_grid_cell(sed_handle *h, double *last_min_dt, int *cell);
 
 /* FP64 budgets of the last step, [4][ncol]: P inventory, P residual,
  * N inventory, N residual (mmol/m2).  Requires params.budgets. */

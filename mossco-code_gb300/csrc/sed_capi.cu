@@ -106,6 +106,15 @@ struct sed_handle {
   // slots: depth class, then column segment, then active layers
   int nslot = 0, nactive = 0;
   std::vector<int> slot_col, slot_k;
+  // adaptive_solver_diagnostics (grid-wide cut): last_min_dt and its cell
+  // (1-based i, j, k, n), kept across calls; still_zero: the first Fortran
+  // element of a cell the solver does not step that has a valid quotient
+  // (c - c) / c = 0 (a nonzero finite value), from the last host state
+  // (-1: none)
+  double last_min_dt = (double)1e20f;
+  int last_cell[4] = {-99, -99, -99, -99};
+  long long still_zero = -1;
+  DevBuf d_minloc;
   Bin bins[2];
   int nseg = 1;                 // column ranges of the layout
   std::vector<int> seg_col;     // [nseg + 1] column bounds
@@ -338,6 +347,45 @@ int step_percol(sed_handle* h, double dt, int method) {
 
 // One coupling step with the reference's grid-wide cut: any() over every
 // active cell of the grid decides the substep (solver_library.F90:121).
+// adaptive_solver_diagnostics (solver_library.F90:129-136) at an accepted
+// substep dt_red smaller than last_min_dt: the substep and the cell of the
+// smallest relative change, as gfortran's MINLOC takes it over the whole
+// grid -- first in element order, NaN skipped; cells the solver does not
+// step have quotient 0 where their value is nonzero and finite; with no
+// valid quotient at all, the first element.
+template <typename real>
+int record_min_dt(sed_handle* h, double dt_red) {
+  CK(h->d_minloc.alloc(2 * sizeof(unsigned long long)), "diagnostics");
+  CK(launch_minloc<real>(h->d_conc.as<real>(), h->d_rhs.as<real>(), h->d_kact.as<int>(),
+                         h->d_slot_col.as<int>(), h->nslot, h->kmax, h->ncol, (real)dt_red,
+                         h->d_minloc.as<unsigned long long>(), h->sms, h->stream),
+     "diagnostics launch");
+  h->launches += 2;
+  unsigned long long r[2];
+  CK(cudaMemcpyAsync(r, h->d_minloc.p, sizeof r, cudaMemcpyDeviceToHost, h->stream),
+     "diagnostics copy");
+  CK(cudaStreamSynchronize(h->stream), "diagnostics");
+  const bool active = r[0] != ~0ull;
+  double vmin = 0.0;
+  if (active) {  // the key's double
+    const unsigned long long b = (r[0] >> 63) ? (r[0] & 0x7FFFFFFFFFFFFFFFull) : ~r[0];
+    memcpy(&vmin, &b, sizeof vmin);
+  }
+  const long long still = h->still_zero;
+  long long pos;
+  if (!active) pos = still >= 0 ? still : 0;
+  else if (vmin < 0.0 || still < 0) pos = (long long)r[1];
+  else if (vmin == 0.0) pos = std::min((long long)r[1], still);
+  else pos = still;
+  const long long nc = h->ncol, col = pos % nc, kn = pos / nc;
+  h->last_min_dt = dt_red;
+  h->last_cell[0] = (int)(col % h->inum) + 1;
+  h->last_cell[1] = (int)(col / h->inum) + 1;
+  h->last_cell[2] = (int)(kn % h->kmax) + 1;
+  h->last_cell[3] = (int)(kn / h->kmax) + 1;
+  return SED_OK;
+}
+
 template <typename real>
 int step_global(sed_handle* h, double dt) {
   const Params<real> p = make_params<real>(h->prm);
@@ -370,6 +418,10 @@ int step_global(sed_handle* h, double dt) {
     if (*h->h_flag && dt_red > h->prm.dt_min) {
       dt_red = dt_red * 0.25;
     } else {
+      if (h->prm.adaptive_solver_diagnostics && dt_red < h->last_min_dt) {
+        int rc = record_min_dt<real>(h, dt_red);
+        if (rc) return rc;
+      }
       CK(launch_accept<real>(h->d_conc.as<real>(), h->d_rhs.as<real>(), h->d_kact.as<int>(),
                              h->nslot, h->kmax, (real)dt_red, h->sms, h->stream),
          "accept launch");
@@ -536,7 +588,29 @@ int upload_forcing(sed_handle* h, const double* bdys, const double* fluxes) {
   return SED_OK;
 }
 
+// The first Fortran element (n, k, col order) of a cell the solver does not
+// step -- a land column or a masked tail -- with a nonzero finite value.
+long long first_still_cell(const sed_handle* h, const double* conc) {
+  const int nc = h->ncol, km = h->kmax;
+  std::vector<int> kcol(nc, 0);
+  for (int s = 0; s < h->nslot; s++)
+    if (h->slot_col[s] >= 0) kcol[h->slot_col[s]] = h->slot_k[s];
+  std::vector<int> still;
+  for (int c = 0; c < nc; c++)
+    if (kcol[c] < km) still.push_back(c);
+  if (still.empty()) return -1;
+  for (int n = 0; n < NTR; n++)
+    for (int k = 0; k < km; k++)
+      for (int c : still) {
+        if (k < kcol[c]) continue;
+        const double v = conc[((size_t)n * km + k) * nc + c];
+        if (v != 0.0 && std::isfinite(v)) return (long long)c + (long long)nc * (k + (long long)km * n);
+      }
+  return -1;
+}
+
 int upload_state(sed_handle* h, const double* conc) {
+  if (h->prm.adaptive_solver_diagnostics) h->still_zero = first_still_cell(h, conc);
   const size_t bytes = (size_t)NTR * h->kmax * h->ncol * sizeof(double);
   CK(cudaMemcpyAsync(h->d_stage.p, conc, bytes, cudaMemcpyHostToDevice, h->stream), "conc copy");
   int rc = h->fp64() ? gather_state<double>(h) : gather_state<float>(h);
@@ -997,6 +1071,7 @@ int sed_default_params(sed_params* p) {
   p->bioturb_b = 1.334;
   p->bioturb_dry_density = 1000.0;
   p->temp_activation = 0.0;
+  p->adaptive_solver_diagnostics = 0;
   return SED_OK;
 }
 
@@ -1625,6 +1700,16 @@ int sed_get_attempts(sed_handle* h, int* attempts) {
   for (int c = 0; c < h->ncol; c++) attempts[c] = 0;
   for (int s = 0; s < h->nslot; s++)
     if (h->slot_col[s] >= 0) attempts[h->slot_col[s]] = tmp[s];
+  return SED_OK;
+}
+
+int sed_get_min_dt_grid_cell(sed_handle* h, double* last_min_dt, int* cell) {
+  if (!h || !last_min_dt || !cell) return SED_E_ARG;
+  if (!h->prm.adaptive_solver_diagnostics || h->prm.cut_scope != SED_CUT_GLOBAL)
+    return h->fail(SED_E_STATE, "recorded by the grid-wide cut with "
+                                "adaptive_solver_diagnostics set");
+  *last_min_dt = h->last_min_dt;
+  for (int i = 0; i < 4; i++) cell[i] = h->last_cell[i];
   return SED_OK;
 }
 

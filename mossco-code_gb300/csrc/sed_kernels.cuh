@@ -1034,6 +1034,80 @@ __global__ void k_accept(real* __restrict__ conc, const real* __restrict__ rhs,
   }
 }
 
+// adaptive_solver_diagnostics (solver_library.F90:133-134): the smallest
+// relative change (c1 - c) / c of the substep about to be accepted, over the
+// active cells, in FP64 (NaN quotients skipped).  Pass 1: the minimum as an
+// order-preserving key of its bits; pass 2: the smallest Fortran element
+// index, col + ncol (k + kmax n), among the cells equal to it.
+__device__ __forceinline__ unsigned long long order_key(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double key_value(unsigned long long k) {
+  return __longlong_as_double((long long)((k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k));
+}
+
+template <typename real>
+__device__ __forceinline__ double rel_change(real c, real dtr, real r) {
+  const real c1 = upd(c, dtr, r);
+  return ((double)c1 - (double)c) / (double)c;
+}
+
+template <typename real>
+__global__ void k_minloc_value(const real* __restrict__ conc, const real* __restrict__ rhs,
+                               const int* __restrict__ kact, int nslot, int kmax, real dtr,
+                               unsigned long long* key) {
+  const size_t total = (size_t)NTR * kmax * nslot;
+  unsigned long long best = ~0ull;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int slot = (int)(i % nslot);
+    const int k = (int)((i / nslot) % kmax);
+    if (k >= kact[slot]) continue;
+    const double v = rel_change(conc[i], dtr, rhs[i]);
+    if (v != v) continue;
+    const unsigned long long kv = order_key(v);
+    best = kv < best ? kv : best;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(FULL, best, o);
+    best = t < best ? t : best;
+  }
+  if ((threadIdx.x & 31) == 0 && best != ~0ull) atomicMin(key, best);
+}
+
+template <typename real>
+__global__ void k_minloc_index(const real* __restrict__ conc, const real* __restrict__ rhs,
+                               const int* __restrict__ kact, const int* __restrict__ slot_col,
+                               int nslot, int kmax, int ncol, real dtr,
+                               const unsigned long long* key, unsigned long long* index) {
+  const unsigned long long kmin = *key;
+  if (kmin == ~0ull) return;  // no valid quotient
+  const double vmin = key_value(kmin);
+  const size_t total = (size_t)NTR * kmax * nslot;
+  unsigned long long best = ~0ull;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int slot = (int)(i % nslot);
+    const size_t nk = i / nslot;
+    const int k = (int)(nk % kmax);
+    if (k >= kact[slot]) continue;
+    const double v = rel_change(conc[i], dtr, rhs[i]);
+    if (!(v == vmin)) continue;
+    const int n = (int)(nk / kmax);
+    const unsigned long long f =
+        (unsigned long long)slot_col[slot] + (unsigned long long)ncol * (k + (size_t)kmax * n);
+    best = f < best ? f : best;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(FULL, best, o);
+    best = t < best ? t : best;
+  }
+  if ((threadIdx.x & 31) == 0 && best != ~0ull) atomicMin(index, best);
+}
+
 template <typename real>
 __global__ void k_epilogue(real* __restrict__ conc, const int* __restrict__ kact,
                            int nslot, int kmax, Params<real> p, DevStats* st) {
@@ -1556,6 +1630,20 @@ cudaError_t launch_broadcast(real* conc, const int* kact, int src, int nslot, in
 }
 
 template <typename real>
+cudaError_t launch_minloc(const real* conc, const real* rhs, const int* kact, const int* slot_col,
+                          int nslot, int kmax, int ncol, real dtr, unsigned long long* out,
+                          int sms, cudaStream_t st) {
+  const size_t total = (size_t)NTR * kmax * nslot;
+  cudaError_t e = cudaMemsetAsync(out, 0xFF, 2 * sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  k_minloc_value<real><<<grid_for(total, 256, sms), 256, 0, st>>>(conc, rhs, kact, nslot, kmax,
+                                                                  dtr, out);
+  k_minloc_index<real><<<grid_for(total, 256, sms), 256, 0, st>>>(
+      conc, rhs, kact, slot_col, nslot, kmax, ncol, dtr, out, out + 1);
+  return cudaGetLastError();
+}
+
+template <typename real>
 cudaError_t launch_trial(const real* conc, const real* rhs, const int* kact,
                          int nslot, int kmax, real dtr, real keep, real natol,
                          int* flag, int sms, cudaStream_t st) {
@@ -1715,6 +1803,9 @@ cudaError_t launch_rate_temperature(const real* base, real* tab, const int* slot
                                            const Params<real>&, int, bool, int, \
                                            int, int, cudaStream_t);             \
   template int column_blocks_per_sm<real>(int, int, bool, int, int, bool);      \
+  template cudaError_t launch_minloc<real>(const real*, const real*, const int*, \
+                                           const int*, int, int, int, real,     \
+                                           unsigned long long*, int, cudaStream_t); \
   template cudaError_t launch_trial<real>(const real*, const real*, const int*, \
                                           int, int, real, real, real, int*,     \
                                           int, cudaStream_t);                   \

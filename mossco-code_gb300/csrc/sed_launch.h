@@ -83,6 +83,14 @@ cudaError_t launch_column_warp(const ColumnArgs<real>& a, const Params<real>& p,
 template <typename real>
 int column_warp_blocks_per_sm(int lpl, bool bc4, int kind, int threads, bool bio3);
 
+// adaptive_solver_diagnostics: out[0] = order key of the smallest relative
+// change (c1 - c) / c over the active cells of the substep dtr, out[1] =
+// the smallest Fortran element index holding it (all ones: none)
+template <typename real>
+cudaError_t launch_minloc(const real* conc, const real* rhs, const int* kact, const int* slot_col,
+                          int nslot, int kmax, int ncol, real dtr, unsigned long long* out,
+                          int sms, cudaStream_t st);
+
 template <typename real>
 cudaError_t launch_trial(const real* conc, const real* rhs, const int* kact,
                          int nslot, int kmax, real dtr, real keep, real natol,

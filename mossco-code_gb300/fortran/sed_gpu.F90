@@ -46,6 +46,8 @@ module sed_gpu
                        bioturb_b, bioturb_dry_density
     !> > 0: microbial rates times exp(-temp_activation (1/(T+273) - 1/288))
     real(c_double)  :: temp_activation
+    !> type_rhs_driver's adaptive_solver_diagnostics (grid-wide cut)
+    integer(c_int)  :: adaptive_solver_diagnostics
   end type
 
   type, bind(C), public :: sed_stats_t
@@ -145,6 +147,11 @@ module sed_gpu
       import :: c_int, c_ptr
       type(c_ptr), value :: h, min_dt
     end function
+    integer(c_int) function sed_get_min_dt_grid_cell(h, last_min_dt, cell) &
+        bind(C, name='sed_get_min_dt_grid_cell')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, last_min_dt, cell
+    end function
     integer(c_int) function sed_get_boundary(h, bdys, fluxes) bind(C, name='sed_get_boundary')
       import :: c_int, c_ptr
       type(c_ptr), value :: h, bdys, fluxes
@@ -237,7 +244,7 @@ module sed_gpu
   public :: sed_default_params, sed_gpu_init, sed_gpu_ode_solver, &
             sed_gpu_get_rhs, sed_gpu_finalize, sed_get_tuning, sed_set_tuning, &
             sed_autotune, sed_set_boundary, sed_get_boundary, sed_spinup, &
-            sed_get_min_dt, sed_set_column_bgc, sed_set_state, sed_get_state, &
+            sed_get_min_dt, sed_get_min_dt_grid_cell, sed_set_column_bgc, sed_set_state, sed_get_state, &
             sed_step, sed_get_fluxes, sed_get_attempts, sed_get_budgets, sed_set_stream, &
             sed_host_register, sed_host_unregister, sed_ode_solver_noalloc, &
             sed_error_string, sed_last_error, sed_tracer_name, sed_tracer_is_particulate, &

@@ -56,7 +56,8 @@ class SedParams(ctypes.Structure):
                    ("bioturb_beta", ctypes.c_double),
                    ("bioturb_b", ctypes.c_double),
                    ("bioturb_dry_density", ctypes.c_double),
-                   ("temp_activation", ctypes.c_double)])
+                   ("temp_activation", ctypes.c_double),
+                   ("adaptive_solver_diagnostics", ctypes.c_int)])
 
 
 class SedStats(ctypes.Structure):
@@ -130,6 +131,7 @@ SIGNATURES = {
     "sed_get_attempts": (ctypes.c_int, [_H, _ip]),
     "sed_get_budgets": (ctypes.c_int, [_H, _dp]),
     "sed_get_min_dt": (ctypes.c_int, [_H, _dp]),
+    "sed_get_min_dt_grid_cell": (ctypes.c_int, [_H, _dp, ctypes.POINTER(ctypes.c_int)]),
     "sed_set_stream": (ctypes.c_int, [_H, _vp]),
     "sed_host_register": (ctypes.c_int, [_vp, ctypes.c_size_t]),
     "sed_host_unregister": (ctypes.c_int, [_vp]),
@@ -244,6 +246,7 @@ def params_from(cs: ColumnSet, precision: int = SED_FP32, budgets: bool = False,
               "bioturb_dry_density"):
         setattr(p, n, float(getattr(d, n)))
     p.temp_activation = float(getattr(d, "temp_activation", 0.0))
+    p.adaptive_solver_diagnostics = int(bool(getattr(d, "adaptive_solver_diagnostics", False)))
     return p
 
 
@@ -441,6 +444,15 @@ class Solver:
         out = np.zeros(self.cs.ncol)
         self._check(self.lib.sed_get_min_dt(self.h, _p(out)), "sed_get_min_dt")
         return out
+
+    def min_dt_grid_cell(self):
+        """type_rhs_driver's last_min_dt and last_min_dt_grid_cell (i, j, k, n),
+        1-based, of the grid-wide cut with adaptive_solver_diagnostics."""
+        v = ctypes.c_double(0.0)
+        cell = (ctypes.c_int * 4)()
+        self._check(self.lib.sed_get_min_dt_grid_cell(self.h, ctypes.byref(v), cell),
+                    "sed_get_min_dt_grid_cell")
+        return v.value, tuple(cell)
 
     def budgets(self) -> np.ndarray:
         out = np.zeros((4, self.cs.ncol))

@@ -91,6 +91,9 @@ class DriverParams:
     # times exp(-temp_activation (1/(T+273) - 1/288)) in each column, the
     # Arrhenius form of the driver's bioturbation factor f_T (:648); 0: none
     temp_activation: float = 0.0
+    # type_rhs_driver's adaptive_solver_diagnostics (solver_library.F90:43):
+    # last_min_dt and last_min_dt_grid_cell of the grid-wide cut
+    adaptive_solver_diagnostics: bool = False
 
     def minimum_array(self) -> np.ndarray:
         if self.minimum is None:
