@@ -461,32 +461,38 @@ def run_headline(args) -> None:
                       "max_rel_err_vs_fp64": a["max_rel_err"],
                       "budget_drift_vs_fp64": a["budget_drift_vs_fp64"]})
 
-    # 4. end to end through the public calls with host buffers: per step the
-    #    state in (sed_set_state, FP64), the surrogate step, the state out
-    #    (sed_get_state)
+    # 4. end to end through the drop-in call with host buffers: per step the
+    #    FP64 state, bottom-water values and fluxes in, the gated surrogate
+    #    step, the state and fluxes out (sed_ode_solver_surrogate, copies
+    #    pipelined over the column segments)
     e2e = None
     if not args.no_e2e:
         host = np.array(S0, dtype=np.float64, copy=True)
-        capi.host_register(host)
+        bd = np.ascontiguousarray(cs.bdys, dtype=np.float64)
+        fl = np.array(cs.fluxes, dtype=np.float64, copy=True)
+        for a in (host, bd, fl):
+            capi.host_register(a)
         n_e2e = args.e2e_steps or steps
         for _ in range(args.warmup):
-            s.set_state(host)
-            S.step_surrogate(s, sur, 1, tol=args.sur_tol, res_atol=args.sur_res_atol)
-            s.get_state(out=host)
+            S.ode_solver_surrogate(s, sur, host, bd, fl, tol=args.sur_tol,
+                                   res_atol=args.sur_res_atol)
         host[:] = S0
+        fl[:] = cs.fluxes
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         for _ in range(n_e2e):
-            s.set_state(host)
-            S.step_surrogate(s, sur, 1, tol=args.sur_tol, res_atol=args.sur_res_atol)
-            s.get_state(out=host)
+            S.ode_solver_surrogate(s, sur, host, bd, fl, tol=args.sur_tol,
+                                   res_atol=args.sur_res_atol)
         e2e_s = time.perf_counter() - t1
-        capi.host_unregister(host)
+        for a in (host, bd, fl):
+            capi.host_unregister(a)
         e2e = {"value": world * cs.n_active * n_e2e / e2e_s, "unit": UNIT,
-               "h2d_bytes_per_step": int(host.nbytes), "d2h_bytes_per_step": int(host.nbytes),
+               "h2d_bytes_per_step": int(host.nbytes + bd.nbytes + fl.nbytes),
+               "d2h_bytes_per_step": int(host.nbytes + fl.nbytes),
                "steps": n_e2e,
-               "calls": "sed_set_state + sed_step_surrogate + sed_get_state (FP64 host state)"}
-        del host
+               "call": "sed_ode_solver_surrogate (FP64 host state in and out, copies "
+                       "pipelined over the column segments)"}
+        del host, bd, fl
     t_now = s.tuning().as_dict()
     s.close()
     if rank != 0:

@@ -413,6 +413,17 @@ int sed_sur_set_norm(sed_surrogate *s, const float *norm, int n);
  * network; their attempts count 0 and their budgets are zero. */
 int sed_step_surrogate(sed_handle *h, sed_surrogate *s, double dt, int nsteps,
                        double tol, double res_atol, sed_stats *stats);
+/* The drop-in call with the surrogate: sed_ode_solver's arguments (host
+ * arrays conc [ntr][kmax][ncol] in and out, bdys, fluxes in and out) and one
+ * gated surrogate coupling step as sed_step_surrogate takes it, with the
+ * state's host<->device copies pipelined over the column segments: each
+ * segment is gated as it arrives, and copied back as soon as its columns are
+ * done.  Results equal sed_set_state + sed_step_surrogate + sed_get_state,
+ * bit for bit. */
+int sed_ode_solver_surrogate(sed_handle *h, sed_surrogate *s, double *conc,
+                             const double *bdys, double *fluxes, double dt,
+                             double tol, double res_atol, sed_stats *stats);
+
 /* Training rows from the plain solver: one plain adaptive coupling step of
  * the handle's device state (FP32, per-column cuts, every active column at
  * kmax layers), then a row for every column whose step took more than one

@@ -122,7 +122,7 @@ struct sed_handle {
   // pipelined sed_ode_solver: copy-in, two step, copy-out streams
   cudaStream_t s_in = nullptr, s_out = nullptr, s_cmp[kMaxSeg] = {};
   cudaEvent_t pe_start = nullptr, pe_done = nullptr;
-  cudaEvent_t pe_in[kMaxSeg] = {}, pe_cmp[kMaxSeg] = {};
+  cudaEvent_t pe_in[kMaxSeg] = {}, pe_cmp[kMaxSeg] = {}, pe_cnt[kMaxSeg] = {};
   // device buffers
   DevBuf d_bgc;  // [NBGC_DEV][nslot] derived per-slot rate parameters
   DevBuf d_bgc_base, d_rfac;  // its unscaled form; [ncol] rate factors
@@ -136,7 +136,7 @@ struct sed_handle {
   std::vector<double> rfac64;   // host rate factors (FP64 state)
   DevStats* h_stats = nullptr;  // pinned
   int* h_flag = nullptr;        // pinned
-  unsigned long long* h_count = nullptr;  // pinned
+  unsigned long long* h_count = nullptr;  // pinned, kMaxSeg counters
   // graph of one coupling step
   cudaGraphExec_t graph = nullptr;
   double graph_dt = -1.0;
@@ -736,6 +736,7 @@ int ensure_pipeline(sed_handle* h) {
   for (int c = 0; c < kMaxSeg; c++) {
     CK(cudaEventCreateWithFlags(&h->pe_in[c], cudaEventDisableTiming), "event");
     CK(cudaEventCreateWithFlags(&h->pe_cmp[c], cudaEventDisableTiming), "event");
+    CK(cudaEventCreateWithFlags(&h->pe_cnt[c], cudaEventDisableTiming), "event");
   }
   return SED_OK;
 }
@@ -1017,6 +1018,7 @@ sed_handle::~sed_handle() {
   for (int c = 0; c < kMaxSeg; c++) {
     if (pe_in[c]) cudaEventDestroy(pe_in[c]);
     if (pe_cmp[c]) cudaEventDestroy(pe_cmp[c]);
+    if (pe_cnt[c]) cudaEventDestroy(pe_cnt[c]);
   }
   if (h_stats) cudaFreeHost(h_stats);
   if (h_flag) cudaFreeHost(h_flag);
@@ -1108,7 +1110,8 @@ int sed_create(const sed_params* p, int inum, int jnum, int kmax, int ntr,
     CK(cudaEventCreate(&h->ev1), "event");
     CK(cudaHostAlloc((void**)&h->h_stats, sizeof(DevStats), cudaHostAllocDefault), "pinned stats");
     CK(cudaHostAlloc((void**)&h->h_flag, sizeof(int), cudaHostAllocDefault), "pinned flag");
-    CK(cudaHostAlloc((void**)&h->h_count, sizeof(unsigned long long), cudaHostAllocDefault),
+    CK(cudaHostAlloc((void**)&h->h_count, kMaxSeg * sizeof(unsigned long long),
+                     cudaHostAllocDefault),
        "pinned counter");
     CK(h->d_queue.alloc(kQueues * sizeof(unsigned)), "queue");
     CK(h->d_stats.alloc(sizeof(DevStats)), "stats");
@@ -1453,26 +1456,43 @@ static int surrogate_bin(sed_handle* h) {
 // Warp-direct launch of one class's kernel over a's columns (a.ntiles of
 // them: the class's slot range, or a slot list).
 static cudaError_t launch_warp_columns(sed_handle* h, const ColumnArgs<float>& a,
-                                       const Params<float>& p, const Bin& bin, int kind) {
+                                       const Params<float>& p, const Bin& bin, int kind,
+                                       cudaStream_t st) {
   const bool bc4 = h->prm.bcup_particulate == 4;
   const int threads = bin.threads;
   const int occ = column_warp_blocks_per_sm<float>(bin.lpl, bc4, kind, threads, p.bio3 != 0);
   const int warps = threads / 32;
   const int blocks =
       std::max(1, std::min(std::max(occ, 1) * h->sms, (a.ntiles + warps - 1) / warps));
-  return launch_column_warp<float>(a, p, bin.lpl, bc4, kind, blocks, threads, h->stream);
+  return launch_column_warp<float>(a, p, bin.lpl, bc4, kind, blocks, threads, st);
 }
 
-int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, double tol,
-                       double res_atol, sed_stats* stats) {
-  int rc = ready(h);
-  if (rc) return rc;
+// The gated surrogate step over slot ranges of the surrogate's class: the
+// checks, buffers and launch choices shared by sed_step_surrogate (one
+// range, the whole class) and sed_ode_solver_surrogate (one range per
+// pipeline chunk).  Chunk c lists its heavy columns in its own part of the
+// list (from its first slot), counts them in d_gate[c] and takes feature
+// and prediction rows from row0(c); d_gate[8 + c] and d_gate[16 + c] are
+// its gate's tile counter and its fused kernel's column counter.
+struct SurPlan {
+  sed_handle* h = nullptr;
+  sed_surrogate* s = nullptr;
+  int b = 0;
+  Params<float> p{};
+  bool bc4 = false;
+  int gate_tc = 0, gate_threads = 0, gate_occ = 0;
+  double dt = 0.0, tol = 0.0, res_atol = 0.0;
+  const Bin& bin() const { return h->bins[b]; }
+  int row0(int sl0, int c) const { return (sl0 - bin().slot0) + 128 * c; }
+};
+
+static int sur_plan(sed_handle* h, sed_surrogate* s, double dt, double tol, double res_atol,
+                    int chunks, SurPlan* P) {
   if (!s) return h->fail(SED_E_ARG, "no surrogate");
   if (h->table())
     return h->fail(SED_E_STATE,
                    "the surrogate has no per-column parameter sets or temperature-dependent "
                    "rates");
-  if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");
   if (h->fp64()) return h->fail(SED_E_ARG, "the surrogate step runs on FP32 state");
   if (h->prm.cut_scope != SED_CUT_PER_COLUMN)
     return h->fail(SED_E_ARG, "the surrogate step cuts substeps per column");
@@ -1484,102 +1504,240 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
   if (!s->norm) return h->fail(SED_E_STATE, "sed_sur_set_norm has not been called");
   const int b = surrogate_bin(h);
   if (b < 0) return h->fail(SED_E_ARG, "the surrogate needs every active column at %d layers", K);
-  if (!(dt > 0.0) || nsteps < 0 || !(tol >= 0.0) || !(res_atol >= 0.0))
-    return h->fail(SED_E_ARG, "bad dt, nsteps, tol or res_atol");
+  if (!(dt > 0.0) || !(tol >= 0.0) || !(res_atol >= 0.0))
+    return h->fail(SED_E_ARG, "bad dt, tol or res_atol");
   CK(cudaSetDevice(h->device), "set device");
+  P->h = h;
+  P->s = s;
+  P->b = b;
+  P->dt = dt;
+  P->tol = tol;
+  P->res_atol = res_atol;
   const Bin& bin = h->bins[b];
-  const size_t ns = h->nslot;
-  const int maxrows = pad128(bin.nslots);
+  const int maxrows = pad128(bin.nslots) + 128 * chunks;
   CK(h->d_list.alloc((size_t)bin.nslots * sizeof(int)), "heavy list");
-  CK(h->d_gate.alloc(128), "heavy counter");
+  CK(h->d_gate.alloc(32 * sizeof(unsigned)), "heavy counters");
   CK(h->d_xfeat.alloc((size_t)maxrows * s->pin[0] * sizeof(bf16)), "features");
   CK(h->d_yhat.alloc((size_t)maxrows * s->pout[s->L - 1] * sizeof(float)), "predictions");
   if (!sur_uses_tc(s))
     CK(h->d_act.alloc((size_t)2 * maxrows * s->pout[0] * sizeof(bf16)), "activations");
-  const long long l0 = h->launches;
-  if ((rc = stats_reset(h))) return rc;
-  Params<float> p = make_params<float>(h->prm);
-  set_clock(p, dt, h->prm.dt_min);
+  P->p = make_params<float>(h->prm);
+  set_clock(P->p, dt, h->prm.dt_min);
   // the gate's tile kernel: the class's tile width (or, for a warp-direct
   // class, the width its other kinds use), with 256 threads where that fits
   // (one attempt per column is latency-bound: the more resident warps, the
   // better; 8.0 ms against 11.9 ms at 128 threads on the 2048^2 grid at day
   // 10); the occupancy query also raises the kernel's shared-memory limit,
   // before any launch
-  const bool bc4 = h->prm.bcup_particulate == 4;
-  const int gate_tc = bin.tc ? bin.tc : bin.tc_fb;
-  int gate_threads = 256;
-  int gate_occ =
-      column_blocks_per_sm<float>(gate_tc, bin.lpl, bc4, KIND_PROBE, gate_threads, p.bio3 != 0);
-  if (gate_occ <= 0) {
-    gate_threads = bin.threads;
-    gate_occ = column_blocks_per_sm<float>(gate_tc, bin.lpl, bc4, KIND_PROBE, gate_threads,
-                                           p.bio3 != 0);
+  P->bc4 = h->prm.bcup_particulate == 4;
+  P->gate_tc = bin.tc ? bin.tc : bin.tc_fb;
+  P->gate_threads = 256;
+  P->gate_occ = column_blocks_per_sm<float>(P->gate_tc, bin.lpl, P->bc4, KIND_PROBE,
+                                            P->gate_threads, P->p.bio3 != 0);
+  if (P->gate_occ <= 0) {
+    P->gate_threads = bin.threads;
+    P->gate_occ = column_blocks_per_sm<float>(P->gate_tc, bin.lpl, P->bc4, KIND_PROBE,
+                                              P->gate_threads, P->p.bio3 != 0);
   }
-  if (gate_occ <= 0) return h->fail(SED_E_CUDA, "the gate's tile kernel does not fit");
-  unsigned* nheavy = h->d_gate.as<unsigned>();
-  int* list = h->d_list.as<int>();
+  if (P->gate_occ <= 0) return h->fail(SED_E_CUDA, "the gate's tile kernel does not fit");
+  return SED_OK;
+}
+
+// 1. gate over slots [sl0, sl1) (whole tiles): every column's first
+//    (whole-step) attempt; columns that pass are done, exactly as the plain
+//    step; the others are listed from list[0], counted in *count.  Then the
+//    count is copied to the pinned h_count[c] and pe_cnt[c] recorded.
+static int sur_gate(SurPlan& P, int c, int sl0, int sl1, cudaStream_t st) {
+  sed_handle* h = P.h;
+  const Bin& bin = P.bin();
+  unsigned* cnt = h->d_gate.as<unsigned>();
+  CK(cudaMemsetAsync(cnt + c, 0, sizeof(unsigned), st), "counter reset");
+  CK(cudaMemsetAsync(cnt + 8 + c, 0, sizeof(unsigned), st), "queue reset");
+  ColumnArgs<float> a = column_args<float>(h, bin, P.b, P.dt, SED_ADAPTIVE_EULER);
+  a.heavy = h->d_list.as<int>() + (sl0 - bin.slot0);
+  a.nheavy = cnt + c;
+  a.queue = cnt + 8 + c;
+  a.tc = P.gate_tc;
+  a.tile_k = nullptr;  // every listed column has kmax layers: stage them all
+  a.tile0 = 0;
+  a.slot0 = sl0;
+  a.ntiles = (sl1 - sl0) / P.gate_tc;
+  if (a.ntiles <= 0) return SED_OK;
+  CK(launch_column<float>(a, P.p, bin.lpl, P.bc4, KIND_PROBE,
+                          std::max(1, std::min(a.ntiles, P.gate_occ * h->sms)), P.gate_threads,
+                          st),
+     "gate launch");
+  h->launches++;
+  CK(cudaMemcpyAsync(h->h_count + c, cnt + c, sizeof(unsigned), cudaMemcpyDeviceToHost, st),
+     "counter copy");
+  CK(cudaEventRecord(h->pe_cnt[c], st), "event");
+  return SED_OK;
+}
+
+// chunk c's heavy count, once its gate is done (-1: CUDA error, recorded)
+static int sur_count(SurPlan& P, int c) {
+  const cudaError_t e = cudaEventSynchronize(P.h->pe_cnt[c]);
+  if (e != cudaSuccess) {
+    P.h->cuda_fail(e, "gate");
+    return -1;
+  }
+  unsigned n = 0;
+  memcpy(&n, P.h->h_count + c, sizeof n);
+  return (int)n;
+}
+
+// 2. the network's proposal rows for the nh listed columns of chunk c
+static int sur_propose(SurPlan& P, int c, int sl0, int nh, cudaStream_t st) {
+  sed_handle* h = P.h;
+  sed_surrogate* s = P.s;
+  const int rows = pad128(nh), r0 = P.row0(sl0, c);
+  const int* list = h->d_list.as<int>() + (sl0 - P.bin().slot0);
+  bf16* x = h->d_xfeat.as<bf16>() + (size_t)r0 * s->pin[0];
+  float* y = h->d_yhat.as<float>() + (size_t)r0 * s->pout[s->L - 1];
+  CK(sur::features(h->d_conc.as<float>(), h->d_force.as<float>(), s->norm, list, nh, h->kmax,
+                   h->kmax, h->nslot, rows, s->nin, s->pin[0], x, st),
+     "features");
   bf16* act0 = h->d_act.as<bf16>();
-  bf16* act1 = act0 + (size_t)maxrows * s->pout[0];
+  bf16* act1 = act0 ? act0 + (size_t)h->d_act.bytes / sizeof(bf16) / 2 : nullptr;
+  int rc = sur_infer_rows(s, x, y, rows, act0, act1, st);
+  if (rc) return h->fail(rc, "surrogate forward: %s", s->err.c_str());
+  // one fused kernel, or one GEMM per layer
+  h->launches += 1 + (sur_uses_tc(s) ? 1 : s->L);
+  return SED_OK;
+}
+
+// 3. each listed column's proposal from its prediction row and its residual
+//    test; a column whose proposal passes takes it, the others take the
+//    plain adaptive step from their state, in the same kernel
+static int sur_finish(SurPlan& P, int c, int sl0, int nh, cudaStream_t st) {
+  sed_handle* h = P.h;
+  sed_surrogate* s = P.s;
+  const Bin& bin = P.bin();
+  unsigned* cnt = h->d_gate.as<unsigned>();
+  ColumnArgs<float> r = column_args<float>(h, bin, P.b, P.dt, SED_ADAPTIVE_EULER);
+  r.list = h->d_list.as<int>() + (sl0 - bin.slot0);
+  r.ntiles = nh;
+  r.yhat = h->d_yhat.as<float>() + (size_t)P.row0(sl0, c) * s->pout[s->L - 1];
+  r.ldy = s->pout[s->L - 1];
+  r.norm = s->norm;
+  r.nin = s->nin;
+  r.nout = s->nout;
+  r.res_tol = P.tol;
+  r.res_atol = P.res_atol;
+  r.queue = cnt + 16 + c;
+  CK(cudaMemsetAsync(r.queue, 0, sizeof(unsigned), st), "queue reset");
+  CK(launch_warp_columns(h, r, P.p, bin, KIND_SUR, st), "residual and fallback launch");
+  h->launches++;
+  return SED_OK;
+}
+
+int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, double tol,
+                       double res_atol, sed_stats* stats) {
+  int rc = ready(h);
+  if (rc) return rc;
+  if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");
+  if (nsteps < 0) return h->fail(SED_E_ARG, "nsteps < 0");
+  SurPlan P;
+  if ((rc = sur_plan(h, s, dt, tol, res_atol, 1, &P))) return rc;
+  const long long l0 = h->launches;
+  if ((rc = stats_reset(h))) return rc;
+  const int sl0 = P.bin().slot0, sl1 = sl0 + P.bin().nslots;
   CK(cudaEventRecord(h->ev0, h->stream), "event");
+  if (nsteps > 0 && (rc = ensure_pipeline(h))) return rc;
   for (int step = 0; step < nsteps; step++) {
-    // 1. gate: every column's first (whole-step) attempt; columns that pass
-    //    are done, exactly as the plain step; the others are listed
-    CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
-    CK(cudaMemsetAsync(nheavy, 0, sizeof(unsigned), h->stream), "counter reset");
-    // (the tile kernel: one attempt per column is uniform work, staged with
-    // coalesced loads, one list reservation per tile)
-    ColumnArgs<float> a = column_args<float>(h, bin, b, dt, SED_ADAPTIVE_EULER);
-    a.heavy = list;
-    a.nheavy = nheavy;
-    a.tc = gate_tc;
-    if (!bin.tc) {  // whole tiles of the class, all layers staged
-      a.tile_k = nullptr;
-      a.tile0 = 0;
-    }
-    a.ntiles = bin.nslots / gate_tc;
-    CK(launch_column<float>(a, p, bin.lpl, bc4, KIND_PROBE,
-                            std::max(1, std::min(a.ntiles, gate_occ * h->sms)), gate_threads,
-                            h->stream),
-       "gate launch");
-    h->launches++;
-    CK(cudaMemcpyAsync(h->h_count, nheavy, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream),
-       "counter copy");
-    CK(cudaStreamSynchronize(h->stream), "gate");
-    unsigned nh_u = 0;
-    memcpy(&nh_u, h->h_count, sizeof nh_u);
-    const int nh = (int)nh_u;
-    if (nh <= 0) continue;
-    // 2. the network's proposal for the listed columns
-    const int rows = pad128(nh);
-    CK(sur::features(h->d_conc.as<float>(), h->d_force.as<float>(), s->norm, list, nh, K,
-                     h->kmax, h->nslot, rows, s->nin, s->pin[0], h->d_xfeat.as<bf16>(),
-                     h->stream),
-       "features");
-    rc = sur_infer_rows(s, h->d_xfeat.as<bf16>(), h->d_yhat.as<float>(), rows, act0, act1,
-                        h->stream);
-    if (rc) return h->fail(rc, "surrogate forward: %s", s->err.c_str());
-    // one fused kernel, or one GEMM per layer
-    h->launches -= sur_uses_tc(s) ? s->L - 1 : 0;
-    h->launches += 1 + s->L;
-    // 3. each listed column's proposal from its prediction row and its
-    //    residual test; a column whose proposal passes takes it, the others
-    //    take the plain adaptive step from their state, in the same kernel
-    ColumnArgs<float> r = column_args<float>(h, bin, b, dt, SED_ADAPTIVE_EULER);
-    r.list = list;
-    r.ntiles = nh;
-    r.yhat = h->d_yhat.as<float>();
-    r.ldy = s->pout[s->L - 1];
-    r.norm = s->norm;
-    r.nin = s->nin;
-    r.nout = s->nout;
-    r.res_tol = tol;
-    r.res_atol = res_atol;
-    CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
-    CK(launch_warp_columns(h, r, p, bin, KIND_SUR), "residual and fallback launch");
-    h->launches++;
+    if ((rc = sur_gate(P, 0, sl0, sl1, h->stream))) return rc;
+    const int nh = sur_count(P, 0);
+    if (nh < 0) return SED_E_CUDA;
+    if (nh == 0) continue;
+    if ((rc = sur_propose(P, 0, sl0, nh, h->stream))) return rc;
+    if ((rc = sur_finish(P, 0, sl0, nh, h->stream))) return rc;
   }
   CK(cudaEventRecord(h->ev1, h->stream), "event");
+  rc = stats_fetch(h, stats, l0, true);
+  if (rc) return rc;
+  if (sur_uses_tc(s) && (rc = sur_check_tc(s))) return h->fail(rc, "%s", s->err.c_str());
+  return SED_OK;
+}
+
+// The drop-in step with the surrogate, its copies in flight: the column
+// segments are the chunks.  Every chunk's host->device copy is queued at
+// once on the copy-in stream; on the handle's stream each chunk is
+// gathered and gated as it arrives, the next chunk's gate is queued before
+// this chunk's network and fused kernel (so the host, which reads each
+// chunk's heavy count, stays ahead), and each chunk is scattered and its
+// device->host copy queued on the copy-out stream as soon as it is done.
+int sed_ode_solver_surrogate(sed_handle* h, sed_surrogate* s, double* conc, const double* bdys,
+                             double* fluxes, double dt, double tol, double res_atol,
+                             sed_stats* stats) {
+  int rc = ready(h);
+  if (rc) return rc;
+  if (!conc || !bdys || !fluxes) return h->fail(SED_E_ARG, "conc, bdys and fluxes are required");
+  const int nch = h->nseg;
+  SurPlan P;
+  if ((rc = sur_plan(h, s, dt, tol, res_atol, nch, &P))) return rc;
+  if ((rc = ensure_pipeline(h))) return rc;
+  if ((rc = upload_forcing(h, bdys, fluxes))) return rc;
+  const long long l0 = h->launches;
+  if ((rc = stats_reset(h))) return rc;
+  const Bin& bin = P.bin();
+  const size_t pitch = (size_t)h->ncol * sizeof(double);
+  const size_t rows = (size_t)NTR * h->kmax;
+  double* stage = h->d_stage.as<double>();
+  CK(cudaEventRecord(h->ev0, h->stream), "event");
+  CK(cudaEventRecord(h->pe_start, h->stream), "event");
+  CK(cudaStreamWaitEvent(h->s_in, h->pe_start, 0), "wait");
+  CK(cudaStreamWaitEvent(h->s_out, h->pe_start, 0), "wait");
+  for (int c = 0; c < nch; c++) {
+    const int col0 = h->seg_col[c], col1 = h->seg_col[c + 1];
+    const size_t width = (size_t)(col1 - col0) * sizeof(double);
+    if (width)
+      CK(cudaMemcpy2DAsync(stage + col0, pitch, conc + col0, pitch, width, rows,
+                           cudaMemcpyHostToDevice, h->s_in), "conc chunk copy");
+    CK(cudaEventRecord(h->pe_in[c], h->s_in), "event");
+  }
+  auto front = [&](int c) -> int {
+    const int sl0 = bin.segb[c], sl1 = bin.segb[c + 1];
+    CK(cudaStreamWaitEvent(h->stream, h->pe_in[c], 0), "wait");
+    if (sl1 == sl0) return SED_OK;
+    CK(launch_gather_range<float>(stage, h->d_conc.as<float>(), h->d_slot_col.as<int>(), NTR,
+                                  h->kmax, h->ncol, h->nslot, sl0, sl1 - sl0, h->sms, h->stream),
+       "gather launch");
+    h->launches++;
+    return sur_gate(P, c, sl0, sl1, h->stream);
+  };
+  if ((rc = front(0))) return rc;
+  for (int c = 0; c < nch; c++) {
+    const int sl0 = bin.segb[c], sl1 = bin.segb[c + 1];
+    const int nh = sl1 > sl0 ? sur_count(P, c) : 0;
+    if (nh < 0) return SED_E_CUDA;
+    if (nh > 0 && (rc = sur_propose(P, c, sl0, nh, h->stream))) return rc;
+    if (c + 1 < nch && (rc = front(c + 1))) return rc;
+    if (nh > 0 && (rc = sur_finish(P, c, sl0, nh, h->stream))) return rc;
+    if (sl1 > sl0) {
+      CK(launch_scatter_range<float>(h->d_conc.as<float>(), stage, h->d_slot_col.as<int>(),
+                                     h->d_kact.as<int>(), NTR, h->kmax, h->ncol, h->nslot, sl0,
+                                     sl1 - sl0, h->sms, h->stream), "scatter launch");
+      h->launches++;
+    }
+    CK(cudaEventRecord(h->pe_cmp[c], h->stream), "event");
+    CK(cudaStreamWaitEvent(h->s_out, h->pe_cmp[c], 0), "wait");
+    const int col0 = h->seg_col[c], col1 = h->seg_col[c + 1];
+    const size_t width = (size_t)(col1 - col0) * sizeof(double);
+    if (width)
+      CK(cudaMemcpy2DAsync(conc + col0, pitch, stage + col0, pitch, width, rows,
+                           cudaMemcpyDeviceToHost, h->s_out), "conc chunk copy back");
+  }
+  // s_out has waited for every chunk: the surface fluxes are final
+  CK(launch_scatter_flux<float>(h->d_sflux.as<float>(), h->d_fluxes.as<double>(),
+                                h->d_slot_col.as<int>(), h->d_kact.as<int>(), h->ncol, h->nslot,
+                                h->sms, h->s_out), "flux scatter launch");
+  h->launches++;
+  CK(cudaMemcpyAsync(fluxes, h->d_fluxes.p, (size_t)NTR * h->ncol * sizeof(double),
+                     cudaMemcpyDeviceToHost, h->s_out), "fluxes copy back");
+  CK(cudaEventRecord(h->pe_done, h->s_out), "event");
+  CK(cudaStreamWaitEvent(h->stream, h->pe_done, 0), "wait");
+  CK(cudaEventRecord(h->ev1, h->stream), "event");
+  h->have_state = true;
   rc = stats_fetch(h, stats, l0, true);
   if (rc) return rc;
   if (sur_uses_tc(s) && (rc = sur_check_tc(s))) return h->fail(rc, "%s", s->err.c_str());

@@ -166,6 +166,9 @@ SIGNATURES = {
     "sed_step_surrogate": (ctypes.c_int, [_H, _H, ctypes.c_double, ctypes.c_int,
                                           ctypes.c_double, ctypes.c_double,
                                           ctypes.POINTER(SedStats)]),
+    "sed_ode_solver_surrogate": (ctypes.c_int, [_H, _H, _dp, _dp, _dp, ctypes.c_double,
+                                                ctypes.c_double, ctypes.c_double,
+                                                ctypes.POINTER(SedStats)]),
     "sed_sur_collect": (ctypes.c_int, [_H, _fp, ctypes.c_double, _vp, _vp, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_longlong,
                                        ctypes.POINTER(ctypes.c_longlong),

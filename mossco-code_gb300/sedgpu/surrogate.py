@@ -431,3 +431,22 @@ def step_surrogate(solver: capi.Solver, sur: Surrogate, nsteps: int = 1,
                                        float(res_atol), ctypes.byref(st))
     solver._check(rc, "sed_step_surrogate")
     return st.as_dict()
+
+
+def ode_solver_surrogate(solver: capi.Solver, sur: Surrogate, conc: np.ndarray,
+                         bdys: np.ndarray, fluxes: np.ndarray, tol: float = 1e-3,
+                         res_atol: float = 1e-2, dt: Optional[float] = None) -> dict:
+    """The drop-in call with the surrogate (sed_ode_solver_surrogate): conc
+    [ntr][kmax][ncol] FP64 in place, bdys in, fluxes in and out; copies
+    pipelined over the column segments."""
+    for a in (conc, fluxes):
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+    bdys = np.ascontiguousarray(bdys, dtype=np.float64)
+    st = capi.SedStats()
+    dt = solver.cs.dt if dt is None else dt
+    p = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    rc = solver.lib.sed_ode_solver_surrogate(solver.h, sur.h, p(conc), p(bdys), p(fluxes),
+                                             float(dt), float(tol), float(res_atol),
+                                             ctypes.byref(st))
+    solver._check(rc, "sed_ode_solver_surrogate")
+    return st.as_dict()

@@ -111,3 +111,45 @@ def test_trained_network_beats_untrained(trained):
           f"{base['row_max_rel_err_quantiles'][50]:.3e}")
     assert ho["mse_standardised"] < 0.5 * base["mse_standardised"]
     assert ho["row_max_rel_err_quantiles"][50] < base["row_max_rel_err_quantiles"][50]
+
+
+@pytest.fixture(scope="module")
+def segmented(trained):
+    """A grid of several column segments (the drop-in call's chunks) ten
+    coupling steps in."""
+    grid = synth.make_workload("surrogate_200k", cols=np.arange(100000, 140000))
+    s = capi.Solver(grid)
+    s.set_forcing()
+    s.set_state(grid.conc)
+    s.step(10)
+    state = s.get_state()
+    s.close()
+    return grid, state
+
+
+@pytest.mark.parametrize("tol", [0.0, 1e-3, 1e30])
+def test_drop_in_call_equals_device_resident_step(trained, segmented, tol):
+    """sed_ode_solver_surrogate (host arrays, copies pipelined over the
+    column segments) equals sed_set_state + sed_step_surrogate +
+    sed_get_state bit for bit: state, surface fluxes and statistics."""
+    sur = trained[0]
+    grid, state = segmented
+    a = capi.Solver(grid)
+    a.set_forcing()
+    a.set_state(state)
+    sa = S.step_surrogate(a, sur, 1, tol=tol)
+    out_a = a.get_state()
+    fl_a = a.fluxes()
+    a.close()
+    b = capi.Solver(grid)
+    assert b.tuning().segments > 1
+    conc = np.array(state, dtype=np.float64, copy=True)
+    fluxes = np.array(grid.fluxes, dtype=np.float64, copy=True)
+    sb = S.ode_solver_surrogate(b, sur, conc, grid.bdys, fluxes, tol=tol)
+    b.close()
+    np.testing.assert_array_equal(conc, out_a)
+    np.testing.assert_array_equal(fluxes, fl_a)
+    for k in ("surrogate_columns", "column_steps", "attempts", "accepted"):
+        assert sa[k] == sb[k], k
+    if tol == 1e30:
+        assert sb["surrogate_columns"] > 0
