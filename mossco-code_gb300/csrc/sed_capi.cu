@@ -1669,8 +1669,10 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
 int sed_ode_solver_surrogate(sed_handle* h, sed_surrogate* s, double* conc, const double* bdys,
                              double* fluxes, double dt, double tol, double res_atol,
                              sed_stats* stats) {
-  int rc = ready(h);
-  if (rc) return rc;
+  // the call brings its own forcing (bdys, fluxes), as sed_ode_solver does
+  int rc;
+  if (!h) return SED_E_ARG;
+  if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
   if (!conc || !bdys || !fluxes) return h->fail(SED_E_ARG, "conc, bdys and fluxes are required");
   const int nch = h->nseg;
   SurPlan P;
