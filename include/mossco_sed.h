@@ -379,13 +379,15 @@ int sed_sur_train_step(sed_surrogate *s, const void *x_dev, const void *y_dev,
 /* MSE loss and its parameter gradients for host rows (no update) */
 int sed_sur_grads(sed_surrogate *s, const float *x, const float *y, int m,
                   float *grads, float *loss);
-/* Inference engine (no counterpart in the reference): on (the default)
- * runs the network's inference -- sed_sur_forward_device and the surrogate
- * step -- as one fused kernel on the tcgen05 tensor cores (accumulators in
- * tensor memory, operands staged by TMA), when the shape fits (input width
- * up to 384, hidden width 256, output width up to 512); off runs it as one
- * mma.sync GEMM per layer.  Training always uses the GEMMs.  Returns 1 when
- * the fused kernel is in use, 0 when not, < 0 on error. */
+/* Tensor-core engine (no counterpart in the reference).  On (the default):
+ * the network's inference -- sed_sur_forward_device and the surrogate step
+ * -- runs as one fused kernel on the tcgen05 tensor cores (accumulators in
+ * tensor memory, operands staged by TMA) when the shape fits (input width
+ * up to 384, hidden width 256, output width up to 512), and the training
+ * products (sed_sur_train_step, sed_sur_grads, sed_sur_forward: forward
+ * with kept pre-activations, input and weight gradients) run as tcgen05
+ * GEMMs.  Off: every product runs as an mma.sync GEMM.  Returns 1 when the
+ * fused inference kernel is in use, 0 when not, < 0 on error. */
 int sed_sur_set_tensor_cores(sed_surrogate *s, int on);
 /* Run the surrogate's work on a caller's CUDA stream (a cudaStream_t as
  * void*; NULL restores its own stream). */

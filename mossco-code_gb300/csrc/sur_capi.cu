@@ -28,14 +28,27 @@
       return s->fail(SED_E_CUDA, "%s: %s", what, cudaGetErrorString(e_));      \
   } while (0)
 
+// whether the training products run as tcgen05 GEMMs
+static bool train_tc(const sed_surrogate* s) { return s->use_tc && sur::gemm_tc_supported(); }
+
+// One training product C = A B^T (sur_kernels.h): the tcgen05 GEMM of
+// sur_tc.cu when the engine is on, else the mma.sync GEMM.
+static cudaError_t train_gemm(sed_surrogate* s, int epi, const bf16* A, const bf16* B, int M,
+                              int N, int K, const float* bias, float* out_f32, bf16* out_bf16,
+                              const float* zprev, int ld_out) {
+  if (train_tc(s))
+    return sur::gemm_tc(epi, A, B, M, N, K, bias, out_f32, out_bf16, zprev, ld_out, s->gsplit,
+                        s->gsplit_n, s->d_err, s->stream);
+  return sur::gemm_nt(epi, A, B, M, N, K, bias, out_f32, out_bf16, zprev, ld_out, s->stream);
+}
+
 // forward pass over m rows already in s->x; output pre-activation in z[L-1]
 int sur_forward_rows(sed_surrogate* s, int m) {
   const bf16* in = s->x;
   for (int l = 0; l < s->L; l++) {
     const bool last = l == s->L - 1;
-    SCK(sur::gemm_nt(last ? sur::EPI_BIAS : sur::EPI_BIAS_GELU, in, s->wb[l], m, s->pout[l],
-                     s->pin[l], s->b[l], s->z[l], last ? nullptr : s->a[l], nullptr,
-                     s->pout[l], s->stream),
+    SCK(train_gemm(s, last ? sur::EPI_BIAS : sur::EPI_BIAS_GELU, in, s->wb[l], m, s->pout[l],
+                   s->pin[l], s->b[l], s->z[l], last ? nullptr : s->a[l], nullptr, s->pout[l]),
         "forward gemm");
     in = s->a[l];
   }
@@ -91,14 +104,14 @@ int backward(sed_surrogate* s, int m, int m_valid) {
     // gW = dZ^T A_in : A = dZ^T [po x m], B = A_in^T [pi x m]
     SCK(sur::transpose_bf16(dcur, s->dzt, m, po, s->stream), "transpose dZ");
     SCK(sur::transpose_bf16(ain, s->at, m, pi, s->stream), "transpose A");
-    SCK(sur::gemm_nt(sur::EPI_F32, s->dzt, s->at, po, pi, m, nullptr, s->gw[l], nullptr,
-                     nullptr, pi, s->stream),
+    SCK(train_gemm(s, sur::EPI_F32, s->dzt, s->at, po, pi, m, nullptr, s->gw[l], nullptr,
+                   nullptr, pi),
         "weight gradient gemm");
     SCK(sur::bias_grad(dcur, m, po, s->gpart, s->gb[l], s->stream), "bias gradient");
     if (l > 0) {
       // dZ_{l-1} = (dZ_l W_l) * GELU'(Z_{l-1}) : A = dZ [m x po], B = W^T [pi x po]
-      SCK(sur::gemm_nt(sur::EPI_GELU_BWD, dcur, s->wbt[l], m, pi, po, nullptr, nullptr, dnext,
-                       s->z[l - 1], pi, s->stream),
+      SCK(train_gemm(s, sur::EPI_GELU_BWD, dcur, s->wbt[l], m, pi, po, nullptr, nullptr, dnext,
+                     s->z[l - 1], pi),
           "input gradient gemm");
       bf16* t = dcur;
       dcur = dnext;
@@ -182,6 +195,9 @@ int sed_sur_create(int nin, int nout, int hidden, int nhidden, int max_batch,
        s->alloc(&s->mask, (size_t)s->pout[s->L - 1]) == cudaSuccess &&
        s->alloc(&s->loss, 4) == cudaSuccess && s->alloc(&s->d_err, 1) == cudaSuccess &&
        s->alloc(&s->gpart, (size_t)sur::bias_grad_parts() * maxd) == cudaSuccess;
+  // up to 32 K-splits of the largest weight gradient
+  s->gsplit_n = (size_t)32 * maxd * maxd;
+  ok = ok && s->alloc(&s->gsplit, s->gsplit_n) == cudaSuccess;
   if (!ok) return bail(SED_E_NOMEM);
   // output mask; initial weights U(-1/sqrt(in), 1/sqrt(in)), zero biases
   std::vector<float> mask(s->pout[s->L - 1], 0.0f);
@@ -317,6 +333,7 @@ int sed_sur_forward(sed_surrogate* s, const float* x, float* y, int m) {
     SCK(cudaMemcpyAsync(out.data(), s->z[s->L - 1], out.size() * sizeof(float),
                         cudaMemcpyDeviceToHost, s->stream), "y copy");
     SCK(cudaStreamSynchronize(s->stream), "forward");
+    if (train_tc(s) && (rc = sur_check_tc(s))) return rc;
     for (int r = 0; r < mm; r++)
       for (int c = 0; c < s->nout; c++) y[(size_t)(r0 + r) * s->nout + c] = out[(size_t)r * nlast + c];
   }
@@ -350,7 +367,7 @@ int sed_sur_forward_device(sed_surrogate* s, const void* x_dev, void* y_dev, int
                         s->stream), "y copy");
   }
   SCK(cudaStreamSynchronize(s->stream), "forward");
-  return SED_OK;
+  return train_tc(s) ? sur_check_tc(s) : SED_OK;
 }
 
 // One Adam step on a device batch: x BF16 [m][pad128(nin)], y BF16
@@ -378,6 +395,7 @@ int sed_sur_train_step(sed_surrogate* s, const void* x_dev, const void* y_dev, i
   if (loss) {
     SCK(cudaMemcpyAsync(loss, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->stream), "loss");
     SCK(cudaStreamSynchronize(s->stream), "train step");
+    if (train_tc(s)) return sur_check_tc(s);
   }
   return SED_OK;
 }
@@ -395,7 +413,8 @@ int sed_sur_grads(sed_surrogate* s, const float* x, const float* y, int m, float
   if ((rc = sur_forward_rows(s, mp))) return rc;
   if ((rc = backward(s, mp, m))) return rc;
   if (loss) SCK(cudaMemcpyAsync(loss, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->stream), "loss");
-  return fetch_params(s, s->gw, s->gb, grads);
+  if ((rc = fetch_params(s, s->gw, s->gb, grads))) return rc;
+  return train_tc(s) ? sur_check_tc(s) : SED_OK;
 }
 
 int sed_sur_set_stream(sed_surrogate* s, void* stream) {

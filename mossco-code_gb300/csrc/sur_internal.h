@@ -35,10 +35,14 @@ struct sed_surrogate {
   // c0[11] | mu_x[nin] | sd_x[nin] | mu_d[nout] | sd_d[nout]
   float* norm = nullptr;
   int norm_len = 0;
-  // inference on the tcgen05 fused kernel (when the shape fits) or on the
-  // mma.sync GEMMs; d_err: the fused kernel's barrier-timeout code
+  // the tcgen05 engine (the fused inference kernel when the shape fits, and
+  // the training products as tcgen05 GEMMs) or the mma.sync GEMMs for both;
+  // d_err: the tcgen05 kernels' barrier-timeout code
   bool use_tc = true;
   int* d_err = nullptr;
+  // partial tiles of the K-split weight-gradient products (gsplit_n floats)
+  float* gsplit = nullptr;
+  size_t gsplit_n = 0;
   std::vector<void*> allocs;
   std::string err;
 

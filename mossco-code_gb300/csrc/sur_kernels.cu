@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "sur_gelu.cuh"
 #include "sur_kernels.h"
 
 namespace sur {
@@ -52,19 +53,6 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4],
       "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
       : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-// tanh form of GELU and its derivative
-__device__ __forceinline__ float gelu(float z) {
-  const float k0 = 0.7978845608028654f, k1 = 0.044715f;
-  const float u = k0 * (z + k1 * z * z * z);
-  return 0.5f * z * (1.0f + tanhf(u));
-}
-__device__ __forceinline__ float gelu_grad(float z) {
-  const float k0 = 0.7978845608028654f, k1 = 0.044715f;
-  const float u = k0 * (z + k1 * z * z * z);
-  const float t = tanhf(u);
-  return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * k0 * (1.0f + 3.0f * k1 * z * z);
 }
 
 // Epilogues.  EPI_BIAS_GELU: Z = acc + bias -> store Z (fp32) and GELU(Z)

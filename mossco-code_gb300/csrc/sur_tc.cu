@@ -22,7 +22,9 @@
 
 #include <algorithm>
 
+#include "sur_gelu.cuh"
 #include "sur_internal.h"
+#include "sur_kernels.h"
 #include "sur_tc.h"
 
 namespace sur {
@@ -432,6 +434,205 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
 }
 
 // ---------------------------------------------------------------------------
+// Training products on the tcgen05 tensor cores: C[M x N] = A[M x K] .
+// B[N x K]^T with A and B BF16 and the reduction dimension contiguous (the
+// forward Z = X W^T, the input gradient dX = dZ W and the weight gradient
+// dW = dZ^T X, as sur_kernels.cu writes them), FP32 accumulation in TMEM.
+//
+// One CTA per 128 x 128 output tile and K range (blockIdx.z; the weight
+// gradient, whose K is the batch, splits K so the few output tiles fill the
+// SMs).  Warp 4 streams the A and B K-chunks ([128][64] boxes each, 128-byte
+// swizzle) through a ring of GST stages by TMA, warp 5 issues four
+// M128 N128 K16 MMAs per chunk, and warps 0-3 (one TMEM lane = one output
+// row per thread) apply the epilogue.  A split writes its partial tile to
+// its own slice of a workspace; k_split_sum adds the slices in a fixed
+// order, so results do not depend on scheduling.  Every barrier wait is
+// bounded as in k_mlp_tc.
+constexpr int GN = 128;                 // output columns per tile (MMA N)
+constexpr int GST = 4;                  // ring stages
+constexpr int GSTAGE = 2 * CHUNK;       // A [128][64] + B [128][64]: 32 KB
+constexpr int GTHREADS = 192;           // warps 0-3 epilogue, 4 TMA, 5 MMA
+constexpr int GBAR_OFF = GST * GSTAGE;  // then full[GST], empty[GST], acc
+constexpr int GSMEM = 1024 + GBAR_OFF + 8 * (2 * GST + 1);
+constexpr int GTMEM_COLS = 128;
+
+template <int EPI>
+__global__ void __launch_bounds__(GTHREADS, 1)
+k_gemm_tc(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
+          int nkc, int kc_per_split, const float* __restrict__ bias,
+          float* __restrict__ out_f32, __nv_bfloat16* __restrict__ out_bf16,
+          const float* __restrict__ zprev, int ld_out, size_t split_stride, int* err) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + GBAR_OFF);
+  __shared__ uint32_t s_tmem;
+  __shared__ volatile int s_abort;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t b_full = saddr(bars), b_empty = saddr(bars + GST), b_acc = saddr(bars + 2 * GST);
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * GN;
+  const int kc0 = blockIdx.z * kc_per_split;
+  const int nk = min(nkc, kc0 + kc_per_split) - kc0;  // >= 1 (host)
+
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    for (int i = 0; i < GST; i++) {
+      mbar_init(b_full + 8 * i, 1);
+      mbar_init(b_empty + 8 * i, 1);
+    }
+    mbar_init(b_acc, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     saddr(&s_tmem)),
+                 "r"(GTMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (warp == 4 && lane == 0) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&ta)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tb)) : "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = s_tmem;
+
+  if (warp == 4) {
+    // ---- TMA producer (one lane)
+    if (lane == 0) {
+      bool ok = true;
+      int g = 0;
+      for (; g < nk; g++) {
+        const int s = g % GST;
+        if (g >= GST) {
+          ok = mbar_wait(b_empty + 8 * s, ((g / GST) - 1) & 1, &s_abort, err, 11);
+          if (!ok) break;
+        }
+        mbar_expect_tx(b_full + 8 * s, GSTAGE);
+        tma_load_2d(saddr(smem + s * GSTAGE), &ta, (kc0 + g) * BK, m0, b_full + 8 * s);
+        tma_load_2d(saddr(smem + s * GSTAGE + CHUNK), &tb, (kc0 + g) * BK, n0, b_full + 8 * s);
+      }
+      if (!ok) {
+        // the copies already issued land before the CTA's memory goes
+        for (int k = 0; k < GST && k < g; k++) {
+          const int gg = g - 1 - k, s = gg % GST;
+          const long long t0 = clock64();
+          while (!mbar_test(b_full + 8 * s, (gg / GST) & 1) && clock64() - t0 < WAIT_CYCLES) {
+          }
+        }
+      }
+    }
+  } else if (warp == 5) {
+    // ---- MMA issuer (one lane)
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16(GN);
+      bool ok = true;
+      int g = 0;
+      for (; g < nk; g++) {
+        const int s = g % GST;
+        ok = mbar_wait(b_full + 8 * s, (g / GST) & 1, &s_abort, err, 12);
+        if (!ok) break;
+        fence_after();
+        const uint32_t a0 = saddr(smem + s * GSTAGE), b0 = a0 + CHUNK;
+#pragma unroll
+        for (int k = 0; k < BK / 16; k++)
+          mma_bf16(tmem, desc_sw128(a0 + 32 * k), desc_sw128(b0 + 32 * k), idesc,
+                   (g > 0 || k > 0) ? 1u : 0u);
+        mma_commit(b_empty + 8 * s);  // the stage is free once these complete
+      }
+      if (ok) {
+        mma_commit(b_acc);  // the accumulator is complete
+      } else if (g > 0) {
+        // the MMAs in flight complete before the TMEM is released
+        const int gg = g - 1, s = gg % GST;
+        const long long t0 = clock64();
+        while (!mbar_test(b_empty + 8 * s, (gg / GST) & 1) && clock64() - t0 < WAIT_CYCLES) {
+        }
+      }
+    }
+  } else {
+    // ---- epilogue (warps 0-3): TMEM lane = tile row
+    bool ok = mbar_wait(b_acc, 0, &s_abort, err, 13);
+    ok = __all_sync(0xffffffffu, ok);
+    if (ok) {
+      fence_after();
+      const int row = warp * 32 + lane;
+      const size_t orow = (size_t)(m0 + row) * ld_out;
+      const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+      float* part = out_f32 + (EPI == EPI_F32 ? blockIdx.z * split_stride : 0);
+#pragma unroll 1
+      for (int c = 0; c < GN / 32; c++) {
+        uint32_t r[32];
+        tmem_ld32_async(tl + 32 * c, r);
+        tmem_wait(r);
+        const int col = n0 + 32 * c;
+        float v[32];
+#pragma unroll
+        for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+        if (EPI == EPI_BIAS_GELU || EPI == EPI_BIAS || EPI == EPI_GELU) {
+#pragma unroll
+          for (int i = 0; i < 32; i++) v[i] += bias[col + i];
+        }
+        if (EPI == EPI_BIAS_GELU || EPI == EPI_BIAS || EPI == EPI_F32) {
+          float* dst = part + orow + col;
+#pragma unroll
+          for (int i = 0; i < 32; i += 4)
+            *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+        }
+        if (EPI == EPI_BIAS_GELU || EPI == EPI_GELU || EPI == EPI_GELU_BWD) {
+          float g[32];
+          if (EPI == EPI_GELU_BWD) {
+            const float* z = zprev + orow + col;
+#pragma unroll
+            for (int i = 0; i < 32; i += 4) {
+              const float4 q = *reinterpret_cast<const float4*>(z + i);
+              g[i] = v[i] * gelu_grad(q.x);
+              g[i + 1] = v[i + 1] * gelu_grad(q.y);
+              g[i + 2] = v[i + 2] * gelu_grad(q.z);
+              g[i + 3] = v[i + 3] * gelu_grad(q.w);
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < 32; i++) g[i] = gelu(v[i]);
+          }
+          __nv_bfloat16* dst = out_bf16 + orow + col;
+#pragma unroll
+          for (int i = 0; i < 32; i += 8) {
+            uint4 w;
+            w.x = pack_bf16(g[i], g[i + 1]);
+            w.y = pack_bf16(g[i + 2], g[i + 3]);
+            w.z = pack_bf16(g[i + 4], g[i + 5]);
+            w.w = pack_bf16(g[i + 6], g[i + 7]);
+            *reinterpret_cast<uint4*>(dst + i) = w;
+          }
+        }
+      }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(GTMEM_COLS)
+                 : "memory");
+  }
+}
+
+// out[i] = sum over the splits of part[z][i], z in order
+__global__ void k_split_sum(const float* __restrict__ part, int nsplit, size_t n,
+                            float* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    float t = part[i];
+    for (int z = 1; z < nsplit; z++) t += part[z * n + i];
+    out[i] = t;
+  }
+}
+
+// ---------------------------------------------------------------------------
 PFN_cuTensorMapEncodeTiled_v12000 encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   if (!fn) {
@@ -503,6 +704,67 @@ cudaError_t infer_tc(sed_surrogate* s, const __nv_bfloat16* x, float* y, int m, 
   const int ntiles = m / tc::BM;
   const int grid = std::max(1, std::min(ntiles, sms));
   tc::k_mlp_tc<<<grid, tc::NTHREADS, smem, st>>>(tx, P, y, s->pout[s->L - 1], ntiles, err);
+  return cudaGetLastError();
+}
+
+bool gemm_tc_supported() { return tc::encoder() != nullptr; }
+
+cudaError_t gemm_tc(int epi, const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K,
+                    const float* bias, float* out_f32, __nv_bfloat16* out_bf16,
+                    const float* zprev, int ld_out, float* work, size_t work_floats, int* err,
+                    cudaStream_t st) {
+  if (M <= 0 || N <= 0 || K <= 0 || M % tc::BM || N % tc::GN || K % tc::BK || ld_out < N ||
+      ld_out % 8)
+    return cudaErrorInvalidValue;
+  CUtensorMap ta, tb;
+  if (!tc::encode_bf16(&ta, A, M, K) || !tc::encode_bf16(&tb, B, N, K))
+    return cudaErrorInvalidValue;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int nkc = K / tc::BK;
+  const int tiles = (M / tc::BM) * (N / tc::GN);
+  // the weight gradient (few output tiles, K = the batch) splits K over the
+  // SMs, at least two K-chunks per split
+  int splits = 1;
+  if (epi == EPI_F32 && work && ld_out == N) {
+    splits = std::max(1, std::min(nkc / 2, sms / tiles));
+    while (splits > 1 && (size_t)splits * M * N > work_floats) splits--;
+  }
+  const int kps = (nkc + splits - 1) / splits;
+  splits = (nkc + kps - 1) / kps;
+  // the dynamic shared-memory limit, raised once per device and epilogue
+  static unsigned char raised[64][5];
+  if (epi < 0 || epi > 4) return cudaErrorInvalidValue;
+  const dim3 grid(N / tc::GN, M / tc::BM, splits);
+  float* dst = splits > 1 ? work : out_f32;
+  const size_t stride = (size_t)M * N;
+#define SUR_GEMM_TC_CASE(E)                                                                    \
+  case E: {                                                                                   \
+    if (dev < 64 && !raised[dev][E]) {                                                        \
+      cudaError_t e = cudaFuncSetAttribute(tc::k_gemm_tc<E>,                                  \
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                                           tc::GSMEM);                                        \
+      if (e != cudaSuccess) return e;                                                         \
+      raised[dev][E] = 1;                                                                     \
+    }                                                                                         \
+    tc::k_gemm_tc<E><<<grid, tc::GTHREADS, tc::GSMEM, st>>>(ta, tb, nkc, kps, bias, dst,      \
+                                                           out_bf16, zprev, ld_out, stride,   \
+                                                           err);                              \
+    break;                                                                                    \
+  }
+  switch (epi) {
+    SUR_GEMM_TC_CASE(EPI_BIAS_GELU)
+    SUR_GEMM_TC_CASE(EPI_BIAS)
+    SUR_GEMM_TC_CASE(EPI_F32)
+    SUR_GEMM_TC_CASE(EPI_GELU_BWD)
+    SUR_GEMM_TC_CASE(EPI_GELU)
+  }
+#undef SUR_GEMM_TC_CASE
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || splits == 1) return e;
+  const int blocks = (int)std::min<size_t>((stride + 255) / 256, (size_t)4 * sms);
+  tc::k_split_sum<<<blocks, 256, 0, st>>>(work, splits, stride, out_f32);
   return cudaGetLastError();
 }
 

@@ -43,7 +43,7 @@ EXTRA_FLAGS = {"sed_kernels_f64.cu": ["-fmad=false"],
                "cpl_capi.cu": ["-fmad=false"]}
 HEADERS = ["sed_device.cuh", "sed_kernels.cuh", "sed_launch.h", "sed_params.h",
            "sur_kernels.h", "sur_internal.h", "sur_loop.h", "cpl_internal.h",
-           "cpl_map.cuh", "sur_tc.h"]
+           "cpl_map.cuh", "sur_tc.h", "sur_gelu.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no multiply-add contraction either (aarch64 g++ contracts by
 # default), so host-side FP64 forcing rows match the CPU restatement's

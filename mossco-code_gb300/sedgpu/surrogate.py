@@ -284,20 +284,35 @@ class Surrogate:
         lp = loss.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
         log = []
         m = self.batch
+        # The batches are gathered and the library's steps run on one torch
+        # stream of their own, so each step's copy of its batch is ordered
+        # after the gather that writes it and before the caching allocator
+        # hands the batch's memory to a later gather.  (With the steps on
+        # another stream, a step could copy a batch that a later gather was
+        # already overwriting.)  The stream is a created one: the library
+        # reads a null stream as "its own stream".
+        stream = torch.cuda.Stream()
+        stream.wait_stream(torch.cuda.current_stream())
+        self._check(self.lib.sed_sur_set_stream(self.h, ctypes.c_void_p(stream.cuda_stream)),
+                    "sed_sur_set_stream")
         t0 = time.perf_counter()
-        for it in range(steps):
-            idx = torch.randint(0, n, (m,), device="cuda", generator=gen)
-            xb = X.index_select(0, idx)
-            yb = Y.index_select(0, idx)
-            torch.cuda.current_stream().synchronize()
-            frac = it / max(steps - 1, 1)
-            lr_t = lr_final + 0.5 * (lr - lr_final) * (1.0 + math.cos(math.pi * frac))
-            want = (it % log_every == 0) or it == steps - 1
-            self._check(self.lib.sed_sur_train_step(
-                self.h, ctypes.c_void_p(xb.data_ptr()), ctypes.c_void_p(yb.data_ptr()), m,
-                float(lr_t), lp if want else None), "train step")
-            if want:
-                log.append((it, float(loss[0]), time.perf_counter() - t0))
+        try:
+            with torch.cuda.stream(stream):
+                for it in range(steps):
+                    idx = torch.randint(0, n, (m,), device="cuda", generator=gen)
+                    xb = X.index_select(0, idx)
+                    yb = Y.index_select(0, idx)
+                    frac = it / max(steps - 1, 1)
+                    lr_t = lr_final + 0.5 * (lr - lr_final) * (1.0 + math.cos(math.pi * frac))
+                    want = (it % log_every == 0) or it == steps - 1
+                    self._check(self.lib.sed_sur_train_step(
+                        self.h, ctypes.c_void_p(xb.data_ptr()), ctypes.c_void_p(yb.data_ptr()),
+                        m, float(lr_t), lp if want else None), "train step")
+                    if want:
+                        log.append((it, float(loss[0]), time.perf_counter() - t0))
+        finally:
+            self._check(self.lib.sed_sur_set_stream(self.h, None), "sed_sur_set_stream")
+            torch.cuda.current_stream().wait_stream(stream)
         return log
 
     def predict_device(self, X):

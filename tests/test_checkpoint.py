@@ -76,6 +76,8 @@ def test_training_resumes_bit_for_bit():
             rc = sur.lib.sed_sur_train_step(sur.h, ctypes.c_void_p(xb.data_ptr()),
                                             ctypes.c_void_p(yb.data_ptr()), m, 1e-3, None)
             assert rc == 0, sur.lib.sed_sur_last_error(sur.h)
+            # the step runs on the library's stream: keep the batch until it is read
+            torch.cuda.synchronize()
 
     a = S.Surrogate(K, batch=m, seed=3)
     train(a, batches)

@@ -53,9 +53,14 @@ def _fp(a):
 
 
 @pytest.mark.gpu
-def test_gpu_forward_and_gradients_match_fp64_reference():
+@pytest.mark.parametrize("tc", [True, False], ids=["tcgen05", "mma_sync"])
+def test_gpu_forward_and_gradients_match_fp64_reference(tc):
+    """Forward pass and gradients of both engines: the tcgen05 GEMMs (TMA
+    operands, TMEM accumulators, the weight gradient split over K) and the
+    mma.sync GEMMs."""
     lib, h = _sur(**SHAPE, batch=256)
     try:
+        lib.sed_sur_set_tensor_cores(h, 1 if tc else 0)
         shapes = M.layer_shapes(**SHAPE)
         n = lib.sed_sur_num_params(h)
         assert n == sum(r * c + r for r, c in shapes)
@@ -100,10 +105,12 @@ def test_gpu_forward_and_gradients_match_fp64_reference():
 
 
 @pytest.mark.gpu
-def test_gpu_training_reduces_loss():
+@pytest.mark.parametrize("tc", [True, False], ids=["tcgen05", "mma_sync"])
+def test_gpu_training_reduces_loss(tc):
     import torch
     lib, h = _sur(**SHAPE, batch=1024)
     try:
+        lib.sed_sur_set_tensor_cores(h, 1 if tc else 0)
         rng = np.random.default_rng(2)
         m = 1024
         A = rng.normal(0, 1 / np.sqrt(SHAPE["nin"]), (SHAPE["nin"], SHAPE["nout"]))
@@ -185,5 +192,40 @@ def test_tensor_core_inference_matches_fp64_reference():
         # row by row: no tile is missing or misplaced
         rrow = np.linalg.norm(a - b, axis=1) / np.linalg.norm(b, axis=1)
         assert rrow.max() < 5e-2, rrow.max()
+    finally:
+        lib.sed_sur_destroy(h)
+
+
+@pytest.mark.gpu
+def test_tcgen05_training_products_match_mma_sync_at_full_batch():
+    """At the training batch (8192 rows) the weight gradients' K is split
+    over the SMs and added in a fixed order: the gradients of the two
+    engines agree, and the tcgen05 ones repeat bit for bit."""
+    lib, h = _sur(**SHAPE, batch=8192, seed=7)
+    try:
+        shapes = M.layer_shapes(**SHAPE)
+        n = lib.sed_sur_num_params(h)
+        rng = np.random.default_rng(4)
+        m = 8192
+        x = rng.normal(0, 1, (m, SHAPE["nin"])).astype(np.float32)
+        y = (0.3 * rng.normal(0, 1, (m, SHAPE["nout"]))).astype(np.float32)
+        out = {}
+        for tc in (True, False, True):
+            lib.sed_sur_set_tensor_cores(h, 1 if tc else 0)
+            g = np.zeros(n, dtype=np.float32)
+            loss = np.zeros(1, dtype=np.float32)
+            assert lib.sed_sur_grads(h, _fp(x), _fp(y), m, _fp(g), _fp(loss)) == 0, \
+                lib.sed_sur_last_error(h)
+            if tc and tc in out:
+                np.testing.assert_array_equal(g, out[tc])
+            out[tc] = g
+        o = 0
+        for r, c in shapes:
+            for blk in (slice(o, o + r * c), slice(o + r * c, o + r * c + r)):
+                a, b = out[True][blk].astype(np.float64), out[False][blk].astype(np.float64)
+                relg = np.linalg.norm(a - b) / np.linalg.norm(b)
+                cos = a @ b / (np.linalg.norm(a) * np.linalg.norm(b))
+                assert relg < 2e-2 and cos > 0.9995, (relg, cos)
+            o += r * c + r
     finally:
         lib.sed_sur_destroy(h)
