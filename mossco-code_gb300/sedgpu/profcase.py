@@ -8,6 +8,10 @@ bracketed by cudaProfilerStart / cudaProfilerStop so that
     python -m sedgpu.profcase surrogate --day 10
         the whole 2048 x 2048 workload at day DAY: one plain step, then one
         gated surrogate step (tolerance 1e-3) with a briefly trained network
+    python -m sedgpu.profcase train --engine tcgen05
+        one training step of the surrogate network at batch 8192 on rows
+        of the 200 000-column workload (ENGINE: tcgen05 or mma_sync), after
+        TIMED steps measured with CUDA events on the library's stream
 
 The tuning is the workload's autotuned one at DAY.  Run from the repository
 root with ``mossco-code_gb300`` on the path (``python -m`` from that folder,
@@ -82,14 +86,74 @@ def surrogate(day: float, train_steps: int = 300) -> dict:
             "launches": {"plain": p["gpu_launches"], "surrogate": q["gpu_launches"]}}
 
 
+def train(engine: str, timed: int = 200) -> dict:
+    import ctypes
+
+    import torch
+    from . import surrogate as S
+    cs = synth.make_workload("surrogate_200k", cols=np.arange(16384))
+    rows = S.collect_rows(cs, 48, 3, warm=12)
+    nz = S.fit_normalizer(rows)
+    X, Y = S.standardised(rows, nz)
+    m = 8192
+    sur = S.Surrogate(cs.kmax, batch=m)
+    sur.set_norm(nz)
+    lib = sur.lib
+    lib.sed_sur_set_tensor_cores(sur.h, 1 if engine == "tcgen05" else 0)
+    st = torch.cuda.Stream()
+    st.wait_stream(torch.cuda.current_stream())
+    sur._check(lib.sed_sur_set_stream(sur.h, ctypes.c_void_p(st.cuda_stream)), "stream")
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(1)
+    with torch.cuda.stream(st):
+        idx = torch.randint(0, X.shape[0], (m,), device="cuda", generator=gen)
+        xb = X.index_select(0, idx)
+        yb = Y.index_select(0, idx)
+
+        def step():
+            sur._check(lib.sed_sur_train_step(sur.h, ctypes.c_void_p(xb.data_ptr()),
+                                              ctypes.c_void_p(yb.data_ptr()), m, 1e-4, None),
+                       "train step")
+
+        for _ in range(5):
+            step()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(timed):
+            step()
+        e1.record(st)
+        st.synchronize()
+        ms = e0.elapsed_time(e1) / timed
+        torch.cuda.profiler.start()
+        step()
+        st.synchronize()
+        torch.cuda.profiler.stop()
+    sur._check(lib.sed_sur_set_stream(sur.h, None), "stream")
+    # products per step: forward, input gradients (not of the first layer)
+    # and weight gradients, 2 m n k FLOPs each at the padded widths
+    dims = [(384, 256), (256, 256), (256, 256), (256, 256), (256, 384)]
+    flops = sum(2 * m * a * b * (3 if l > 0 else 2) for l, (a, b) in enumerate(dims))
+    sur.close()
+    return {"case": "train", "engine": engine, "batch": m, "ms_per_step": round(ms, 4),
+            "gemm_tflops_per_step": flops / 1e12,
+            "tflop_s": round(flops / (ms * 1e-3) / 1e12, 1)}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("case", choices=("plain", "surrogate"))
+    ap.add_argument("case", choices=("plain", "surrogate", "train"))
     ap.add_argument("--columns", type=int, default=262144)
     ap.add_argument("--day", type=float, default=10.0)
+    ap.add_argument("--engine", default="tcgen05", choices=("tcgen05", "mma_sync"))
+    ap.add_argument("--timed", type=int, default=200)
     a = ap.parse_args(argv)
     t = time.perf_counter()
-    out = plain(a.columns, a.day) if a.case == "plain" else surrogate(a.day)
+    if a.case == "plain":
+        out = plain(a.columns, a.day)
+    elif a.case == "surrogate":
+        out = surrogate(a.day)
+    else:
+        out = train(a.engine, a.timed)
     out["wall_s"] = round(time.perf_counter() - t, 1)
     print(json.dumps(out), flush=True)
 
