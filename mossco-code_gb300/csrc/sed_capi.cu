@@ -1557,6 +1557,12 @@ static int sur_gate(SurPlan& P, int c, int sl0, int sl1, cudaStream_t st) {
   a.heavy = h->d_list.as<int>() + (sl0 - bin.slot0);
   a.nheavy = cnt + c;
   a.queue = cnt + 8 + c;
+  // the gate also writes the network's input rows of the columns it lists
+  a.xfeat = reinterpret_cast<unsigned short*>(h->d_xfeat.as<bf16>() +
+                                              (size_t)P.row0(sl0, c) * P.s->pin[0]);
+  a.pin = P.s->pin[0];
+  a.norm = P.s->norm;
+  a.nin = P.s->nin;
   a.tc = P.gate_tc;
   a.tile_k = nullptr;  // every listed column has kmax layers: stage them all
   a.tile0 = 0;
@@ -1586,23 +1592,25 @@ static int sur_count(SurPlan& P, int c) {
   return (int)n;
 }
 
-// 2. the network's proposal rows for the nh listed columns of chunk c
+// 2. the network's proposal rows for the nh listed columns of chunk c (the
+//    gate wrote their input rows; the rows up to the next multiple of 128
+//    are cleared)
 static int sur_propose(SurPlan& P, int c, int sl0, int nh, cudaStream_t st) {
   sed_handle* h = P.h;
   sed_surrogate* s = P.s;
   const int rows = pad128(nh), r0 = P.row0(sl0, c);
-  const int* list = h->d_list.as<int>() + (sl0 - P.bin().slot0);
   bf16* x = h->d_xfeat.as<bf16>() + (size_t)r0 * s->pin[0];
   float* y = h->d_yhat.as<float>() + (size_t)r0 * s->pout[s->L - 1];
-  CK(sur::features(h->d_conc.as<float>(), h->d_force.as<float>(), s->norm, list, nh, h->kmax,
-                   h->kmax, h->nslot, rows, s->nin, s->pin[0], x, st),
-     "features");
+  if (rows > nh)
+    CK(cudaMemsetAsync(x + (size_t)nh * s->pin[0], 0,
+                       (size_t)(rows - nh) * s->pin[0] * sizeof(bf16), st),
+       "padding rows");
   bf16* act0 = h->d_act.as<bf16>();
   bf16* act1 = act0 ? act0 + (size_t)h->d_act.bytes / sizeof(bf16) / 2 : nullptr;
   int rc = sur_infer_rows(s, x, y, rows, act0, act1, st);
   if (rc) return h->fail(rc, "surrogate forward: %s", s->err.c_str());
   // one fused kernel, or one GEMM per layer
-  h->launches += 1 + (sur_uses_tc(s) ? 1 : s->L);
+  h->launches += sur_uses_tc(s) ? 1 : s->L;
   return SED_OK;
 }
 

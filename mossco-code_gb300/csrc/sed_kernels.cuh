@@ -18,6 +18,7 @@
 #include "sed_device.cuh"
 #include "sed_launch.h"
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -63,6 +64,27 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
+// Row walk of a staging copy: the 16-byte pieces of rows [0, rows) of tc
+// reals, nthreads threads.  When the pieces per row (vpr) are a power of two
+// dividing nthreads (every tile width and block size the launches use), a
+// thread keeps its piece index v and steps its row by nthreads / vpr, so the
+// per-piece index arithmetic is a few adds; otherwise each piece index is
+// divided out.  f(row, v) copies one piece.
+template <typename F>
+__device__ __forceinline__ void walk_pieces(int rows, int vpr, int tid, int nthreads, F f) {
+  if ((vpr & (vpr - 1)) == 0 && nthreads % vpr == 0) {
+    const int sh = __ffs(vpr) - 1;
+    const int v = tid & (vpr - 1);
+    const int rstep = nthreads >> sh;
+    for (int row = tid >> sh; row < rows; row += rstep) f(row, v);
+  } else {
+    for (int i = tid; i < rows * vpr; i += nthreads) {
+      const int row = i / vpr;
+      f(row, i - row * vpr);
+    }
+  }
+}
+
 // Copy `rows` rows of tc reals between global (row stride gstride, first
 // element at gbase + row_index*gstride) and shared memory (row stride tcp).
 // To shared memory the copies are asynchronous: cp_async_wait_all before
@@ -73,42 +95,41 @@ __device__ __forceinline__ void copy_rows(real* sm, real* gbase, size_t gstride,
                                           int row_step_global, int tid,
                                           int nthreads) {
   constexpr int EPV = 16 / sizeof(real);  // elements per 16-byte vector
-  const int vpr = tc / EPV;
-  const int total = rows * vpr;
-  for (int i = tid; i < total; i += nthreads) {
-    const int row = i / vpr;
-    const int v = i - row * vpr;
+  walk_pieces(rows, tc / EPV, tid, nthreads, [&](int row, int v) {
     real* g = gbase + (size_t)row * row_step_global * gstride + v * EPV;
     real* s = sm + (size_t)row * tcp + v * EPV;
     if (TO_SHARED)
       cp_async16(s, g);
     else
       *reinterpret_cast<uint4*>(g) = *reinterpret_cast<const uint4*>(s);
-  }
+  });
 }
 
 // rows of a [nrow_groups][kmax][nslot] array restricted to k < kt:
-// copies group g, layer k for all g < ngroups, k < kt.
+// copies group g, layer k for all g < ngroups, k < kt.  The (g, k) of a
+// row follows the row walk incrementally.
 template <typename real, bool TO_SHARED>
 __device__ __forceinline__ void copy_grouped(real* sm, real* g0, int ngroups,
                                              int kt, int KT, int kmax,
                                              size_t nslot, int tc, int tcp,
                                              int tid, int nthreads) {
   constexpr int EPV = 16 / sizeof(real);
-  const int vpr = tc / EPV;
-  const int total = ngroups * kt * vpr;
-  for (int i = tid; i < total; i += nthreads) {
-    const int row = i / vpr;
-    const int v = i - row * vpr;
-    const int g = row / kt;
-    const int k = row - g * kt;
+  int g = 0, k = 0, at = 0;  // the row (g, k) = g kt + k last visited
+  walk_pieces(ngroups * kt, tc / EPV, tid, nthreads, [&](int row, int v) {
+    k += row - at;
+    at = row;
+    if (k >= kt) {
+      const int q = k < 2 * kt ? 1 : k / kt;
+      g += q;
+      k -= q * kt;
+    }
     real* gp = g0 + ((size_t)g * kmax + k) * nslot + v * EPV;
     real* sp = sm + ((size_t)g * KT + k) * tcp + v * EPV;
     if (TO_SHARED)
       cp_async16(sp, gp);
     else
       *reinterpret_cast<uint4*>(gp) = *reinterpret_cast<const uint4*>(sp);
-  }
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -460,7 +481,8 @@ __device__ __forceinline__ ColResult solve_adaptive(
   real dn[LPL];
   ColResult res{0, 0, 0, 0, 1e300};
   Budget<real, LPL, BC4> B;
-  B.start(p, lc, C);
+  // the gate takes the column's inventories only once it keeps the column
+  if (!PROBE) B.start(p, lc, C);
   unsigned long long t = 0, T = 0, inc = 0;
   double dt_int = 0.0, dt_red = dt;
   if (TICKS) { T = 1ull << (2 * p.mstop); inc = T; }
@@ -502,6 +524,7 @@ __device__ __forceinline__ ColResult solve_adaptive(
       res.attempts = -1;
       return res;
     }
+    if (PROBE && res.attempts == 1) B.start(p, lc, C);
     if (reject && can_cut) {
       m++;
       dtr = dtr * real(0.25);
@@ -642,6 +665,8 @@ k_column(ColumnArgs<real> a, Params<real> p) {
   int* s_nsub = reinterpret_cast<int*>(smem + L.nsub);
   __shared__ int s_tile, s_next;
   __shared__ int s_heavy[64];  // KIND_PROBE: the tile's columns the gate rejects
+  __shared__ int s_hcol[64], s_hn;  // KIND_PROBE: their tile columns, in order
+  __shared__ unsigned s_hat;        // and their first list entry
   __shared__ unsigned long long b_att, b_acc, b_cols, b_mindt;
   __shared__ int b_maxatt, b_cap, b_nan;
 
@@ -760,14 +785,58 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       }
     }
     __syncthreads();
-    if (KIND == KIND_PROBE && tid == 0) {
-      // the tile's rejected columns into the list: one reservation per tile
-      int n = 0;
-      for (int q = 0; q < tc; q++) n += s_heavy[q];
-      if (n > 0) {
-        unsigned at = atomicAdd(a.nheavy, (unsigned)n);
+    if (KIND == KIND_PROBE) {
+      if (tid == 0) {
+        // the tile's rejected columns into the list: one reservation per tile
+        int n = 0;
         for (int q = 0; q < tc; q++)
-          if (s_heavy[q]) a.heavy[at++] = slot0 + q;
+          if (s_heavy[q]) s_hcol[n++] = q;
+        unsigned at = 0;
+        if (n > 0) {
+          at = atomicAdd(a.nheavy, (unsigned)n);
+          for (int q = 0; q < n; q++) a.heavy[at + q] = slot0 + s_hcol[q];
+        }
+        s_hn = n;
+        s_hat = at;
+      }
+      if (a.xfeat) {
+        // their network input rows, from the staged (unchanged) state and
+        // forcing: a thread owns features f, tid + nthr, ... and writes them
+        // for every listed column of the tile (consecutive threads,
+        // consecutive features of a row); the logarithm is the hardware
+        // approximation, far below the BF16 rounding of the row
+        __syncthreads();
+        const int n = s_hn, pin = a.pin, nin = a.nin, K = a.kmax;
+        const int nstate = NTR * K;
+        const float* c0 = a.norm;
+        const float* mu = c0 + NTR;
+        const float* sd = mu + nin;
+        unsigned short* x = a.xfeat + (size_t)s_hat * pin;
+        for (int f = tid; f < pin; f += nthr) {
+          const real* src = nullptr;
+          float add = 0.0f, m = 0.0f, isd = 0.0f;
+          bool state = false;
+          if (f < nstate) {
+            const int tr = f / K, k = f - tr * K;
+            src = s_conc + (tr * KT + k) * tcp;
+            add = c0[tr];
+            state = true;
+          } else if (f < nin) {
+            src = s_force + (f - nstate) * tcp;
+          }
+          if (src) {
+            m = mu[f];
+            isd = 1.0f / sd[f];
+          }
+          for (int r = 0; r < n; r++) {
+            float v = 0.0f;
+            if (src) {
+              const float c = (float)src[s_hcol[r]];
+              v = ((state ? __logf(fmaxf(c, 0.0f) + add) : c) - m) * isd;
+            }
+            x[(size_t)r * pin + f] = __bfloat16_as_ushort(__float2bfloat16(v));
+          }
+        }
       }
     }
     // stage out

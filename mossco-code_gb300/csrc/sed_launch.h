@@ -54,6 +54,12 @@ struct ColumnArgs {
   const float* yhat;
   const float* norm;
   int ldy, nin, nout;
+  // KIND_PROBE: the network's input rows of the rejected columns, BF16 bits
+  // [row][pin], row i for heavy[i]: the standardised log(max(C, 0) + c0)
+  // of the 11 K state values (tracer-major) and the 13 forcing rows, zero
+  // up to pin (normalisation in norm, nin = 11 K + 13); null: none
+  unsigned short* xfeat;
+  int pin;
   // warp-direct kernel: coupling steps per launch with constant forcing
   // (0 or 1: one); each warp keeps its column in registers between them
   int nrepeat;

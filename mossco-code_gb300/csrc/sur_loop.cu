@@ -1,16 +1,16 @@
 // sur_loop.cu -- kernels between the solver's slot layout and the
 // surrogate's row layout.
 //
-// Features of a column (row r of the MLP batch, the column in slot list[r]),
-// tracer-major:
+// Features of a column (a row of the MLP batch), tracer-major:
 //   x[n*K + k]   = (log(max(C[n][k], 0) + c0[n]) - mu_x) / sd_x     n < 11, k < K
 //   x[11*K + f]  = (force[f] - mu_x) / sd_x                          f < 13
 // (the 13 per-column forcing rows of the solver: bioturbation x f_T, the
-// molecular multiplier and the 11 surface values), zero in padded rows and
-// columns.  The network predicts the standardised change of log(C + c0)
-// over one coupling step; the surrogate step's residual kernel forms the
-// proposed state from it.  The features kernel is a 32 x 32 tiled transpose
-// (row tiles on blockIdx.x, feature tiles on blockIdx.y).
+// molecular multiplier and the 11 surface values), zero in padded columns.
+// The network predicts the standardised change of log(C + c0) over one
+// coupling step; the surrogate step's residual kernel forms the proposed
+// state from it.  In the surrogate step the gate (the tile kernel's
+// KIND_PROBE) writes these rows for the columns it lists, from the tile it
+// has staged.
 //
 // Training rows (k_collect): for every column whose plain step took more
 // than one attempt (its first, whole-step attempt was rejected: the columns
@@ -27,41 +27,6 @@ namespace sur {
 
 using sed::NFORCE;
 using sed::NTR;
-
-__global__ void k_features(const float* __restrict__ conc, const float* __restrict__ force,
-                           const float* __restrict__ norm, const int* __restrict__ list,
-                           int nrows, int K, int kmax, int nslot, int rows, int nin, int pin,
-                           __nv_bfloat16* __restrict__ x) {
-  __shared__ float tile[32][33];
-  const int f0 = blockIdx.y * 32, r0 = blockIdx.x * 32;
-  const float* c0 = norm;
-  const float* mu = norm + NTR;
-  const float* sd = mu + nin;
-  const int nstate = NTR * K;
-  // read: feature rows f, the tile's columns along threadIdx.x
-  const int r = r0 + threadIdx.x;
-  const int slot = r < nrows ? list[r] : -1;
-  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
-    const int f = f0 + y;
-    float v = 0.0f;
-    if (slot >= 0 && f < nin) {
-      if (f < nstate) {
-        const int n = f / K, k = f - n * K;
-        v = (logf(fmaxf(conc[((size_t)n * kmax + k) * nslot + slot], 0.0f) + c0[n]) - mu[f]) /
-            sd[f];
-      } else {
-        v = (force[(size_t)(f - nstate) * nslot + slot] - mu[f]) / sd[f];
-      }
-    }
-    tile[y][threadIdx.x] = v;
-  }
-  __syncthreads();
-  // write: rows, features contiguous
-  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
-    const int rr = r0 + y, f = f0 + threadIdx.x;
-    if (rr < rows && f < pin) x[(size_t)rr * pin + f] = __float2bfloat16(tile[threadIdx.x][y]);
-  }
-}
 
 // One warp per slot of the class range [slot0, slot0 + nslots).
 __global__ void k_collect(const float* __restrict__ conc0, const float* __restrict__ conc1,
@@ -91,16 +56,6 @@ __global__ void k_collect(const float* __restrict__ conc0, const float* __restri
     }
     if (lane < NFORCE) xr[NTR * K + lane] = force[(size_t)lane * nslot + slot];
   }
-}
-
-cudaError_t features(const float* conc, const float* force, const float* norm, const int* list,
-                     int nrows, int K, int kmax, int nslot, int rows, int nin, int pin,
-                     __nv_bfloat16* x, cudaStream_t st) {
-  // rows on x (up to 2^31 - 1 blocks), features on y (a few dozen)
-  dim3 grid((rows + 31) / 32, (pin + 31) / 32);
-  k_features<<<grid, dim3(32, 8), 0, st>>>(conc, force, norm, list, nrows, K, kmax, nslot, rows,
-                                           nin, pin, x);
-  return cudaGetLastError();
 }
 
 cudaError_t collect(const float* conc0, const float* conc1, const float* force, const int* kact,

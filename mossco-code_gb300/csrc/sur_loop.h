@@ -7,12 +7,6 @@
 
 namespace sur {
 
-// norm: c0[11] | mu_x[nin] | sd_x[nin] | mu_d[nout] | sd_d[nout]
-// Row r < nrows of x is the column in slot list[r]; rows nrows .. rows-1
-// are zero.
-cudaError_t features(const float* conc, const float* force, const float* norm, const int* list,
-                     int nrows, int K, int kmax, int nslot, int rows, int nin, int pin,
-                     __nv_bfloat16* x, cudaStream_t st);
 // training rows of the columns of slots [slot0, slot0 + nslots) whose step
 // took more than one attempt (conc0: state before the step, conc1: after)
 cudaError_t collect(const float* conc0, const float* conc1, const float* force, const int* kact,

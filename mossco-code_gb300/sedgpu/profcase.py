@@ -5,9 +5,11 @@ bracketed by cudaProfilerStart / cudaProfilerStop so that
     python -m sedgpu.profcase plain --columns 262144 --day 10
         one plain FP32 step (budgets on) of the first COLUMNS columns of the
         2048 x 2048 workload, from the state DAY simulated days in
-    python -m sedgpu.profcase surrogate --day 10
-        the whole 2048 x 2048 workload at day DAY: one plain step, then one
-        gated surrogate step (tolerance 1e-3) with a briefly trained network
+    python -m sedgpu.profcase surrogate --day 10 [--sur-columns N]
+        the whole 2048 x 2048 workload (or its first N columns) at day DAY:
+        one plain step, then one gated surrogate step (tolerance 1e-3) with
+        a briefly trained network; budgets off as in the bench's headline
+        (--budgets: on)
     python -m sedgpu.profcase train --engine tcgen05
         one training step of the surrogate network at batch 8192 on rows
         of the 200 000-column workload (ENGINE: tcgen05 or mma_sync), after
@@ -25,8 +27,8 @@ import numpy as np
 from . import capi, synth
 
 
-def _develop(cs, day: float):
-    s = capi.Solver(cs, budgets=True)
+def _develop(cs, day: float, budgets: bool = True):
+    s = capi.Solver(cs, budgets=budgets)
     s.set_forcing()
     s.set_state(cs.conc)
     n = int(round(day * 86400.0 / cs.dt))
@@ -57,14 +59,16 @@ def plain(columns: int, day: float) -> dict:
             "column_steps": st["column_steps"], "device_ms": st["device_ms"]}
 
 
-def surrogate(day: float, train_steps: int = 300) -> dict:
+def surrogate(day: float, train_steps: int = 300, columns: int = 0,
+              budgets: bool = False) -> dict:
     import torch
     from . import surrogate as S
     train = synth.make_workload("surrogate_200k", cols=np.arange(8192))
     sur, _ = S.train_surrogate(train, None, nsteps=48, every=3, warm=12,
                                train_steps=train_steps, batch=2048, log_every=100)
-    cs = synth.make_workload("surrogate_2048x2048")
-    s = _develop(cs, day)
+    cs = synth.make_workload("surrogate_2048x2048",
+                             cols=np.arange(columns) if columns > 0 else None)
+    s = _develop(cs, day, budgets=budgets)
     s0 = s.get_state()
     # one untimed pass of each, then the profiled pair from the same state
     s.step(1)
@@ -80,7 +84,7 @@ def surrogate(day: float, train_steps: int = 300) -> dict:
     torch.cuda.profiler.stop()
     s.close()
     sur.close()
-    return {"case": "surrogate", "columns": int(cs.n_active), "day": day,
+    return {"case": "surrogate", "columns": int(cs.n_active), "day": day, "budgets": budgets,
             "plain_ms": p["device_ms"], "surrogate_ms": q["device_ms"],
             "surrogate_columns": q["surrogate_columns"],
             "launches": {"plain": p["gpu_launches"], "surrogate": q["gpu_launches"]}}
@@ -144,6 +148,10 @@ def main(argv=None):
     ap.add_argument("case", choices=("plain", "surrogate", "train"))
     ap.add_argument("--columns", type=int, default=262144)
     ap.add_argument("--day", type=float, default=10.0)
+    ap.add_argument("--sur-columns", type=int, default=0,
+                    help="surrogate case: the first SUR_COLUMNS columns (0: the whole grid)")
+    ap.add_argument("--budgets", action="store_true",
+                    help="surrogate case: budgets on (the plain case always has them)")
     ap.add_argument("--engine", default="tcgen05", choices=("tcgen05", "mma_sync"))
     ap.add_argument("--timed", type=int, default=200)
     a = ap.parse_args(argv)
@@ -151,7 +159,7 @@ def main(argv=None):
     if a.case == "plain":
         out = plain(a.columns, a.day)
     elif a.case == "surrogate":
-        out = surrogate(a.day)
+        out = surrogate(a.day, columns=a.sur_columns, budgets=a.budgets)
     else:
         out = train(a.engine, a.timed)
     out["wall_s"] = round(time.perf_counter() - t, 1)
