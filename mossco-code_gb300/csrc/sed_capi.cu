@@ -1523,18 +1523,26 @@ static int sur_plan(sed_handle* h, sed_surrogate* s, double dt, double tol, doub
     CK(h->d_act.alloc((size_t)2 * maxrows * s->pout[0] * sizeof(bf16)), "activations");
   P->p = make_params<float>(h->prm);
   set_clock(P->p, dt, h->prm.dt_min);
-  // the gate's tile kernel: the class's tile width (or, for a warp-direct
-  // class, the width its other kinds use), with 256 threads where that fits
-  // (one attempt per column is latency-bound: the more resident warps, the
-  // better; 8.0 ms against 11.9 ms at 128 threads on the 2048^2 grid at day
-  // 10); the occupancy query also raises the kernel's shared-memory limit,
-  // before any launch
+  // the gate's tile kernel: 256 threads and the widest tile of 32, 16 or 8
+  // columns with the most resident blocks (one attempt per column is
+  // latency-bound: the more resident warps, the better; at 256 threads the
+  // kernel's registers allow four blocks per SM, which 16-column tiles fit
+  // in shared memory and 32-column ones do not); the occupancy query also
+  // raises the kernel's shared-memory limit, before any launch
   P->bc4 = h->prm.bcup_particulate == 4;
-  P->gate_tc = bin.tc ? bin.tc : bin.tc_fb;
   P->gate_threads = 256;
-  P->gate_occ = column_blocks_per_sm<float>(P->gate_tc, bin.lpl, P->bc4, KIND_PROBE,
-                                            P->gate_threads, P->p.bio3 != 0);
+  P->gate_tc = 0;
+  P->gate_occ = 0;
+  for (int tc = 32; tc >= 8; tc /= 2) {
+    const int occ = column_blocks_per_sm<float>(tc, bin.lpl, P->bc4, KIND_PROBE,
+                                                P->gate_threads, P->p.bio3 != 0);
+    if (occ > P->gate_occ) {
+      P->gate_occ = occ;
+      P->gate_tc = tc;
+    }
+  }
   if (P->gate_occ <= 0) {
+    P->gate_tc = bin.tc ? bin.tc : bin.tc_fb;
     P->gate_threads = bin.threads;
     P->gate_occ = column_blocks_per_sm<float>(P->gate_tc, bin.lpl, P->bc4, KIND_PROBE,
                                               P->gate_threads, P->p.bio3 != 0);

@@ -459,6 +459,63 @@ __device__ __forceinline__ int epilogue(const Params<real>& p, int lane, int K,
   return nan;
 }
 
+// One attempt of the adaptive Euler step at substep dtr: whether any of
+// the lane's cells fails the positivity test c1 - (1+rcm) c < -atol with
+// c1 = c + dtr r (:117-121).  Lanes past the column hold zeros: c1 = 0
+// never falls below -atol.
+template <typename real, int LPL>
+__device__ __forceinline__ bool attempt_fails(const Params<real>& p, const real (&C)[LPL][NTR],
+                                              const real (&R)[LPL][NTR], real dtr) {
+  bool bad = false;
+#pragma unroll
+  for (int s = 0; s < LPL; s++) {
+    if constexpr (std::is_same<real, float>::value) {
+      // tracer pairs in packed FP32x2 FMAs (per component the scalar's
+      // rounding), tracer 10 alone
+#pragma unroll
+      for (int n = 0; n + 1 < NTR; n += 2) {
+        const float2 c = make_float2(C[s][n], C[s][n + 1]);
+        const float2 c1 = __ffma2_rn(make_float2(dtr, dtr),
+                                     make_float2(R[s][n], R[s][n + 1]), c);
+        const float2 t = __ffma2_rn(make_float2(-p.keep, -p.keep), c, c1);
+        bad |= (t.x < p.natol) | (t.y < p.natol);
+      }
+      bad |= below_keep(upd(C[s][NTR - 1], dtr, R[s][NTR - 1]), p.keep, C[s][NTR - 1],
+                        p.natol);
+    } else {
+#pragma unroll
+      for (int n = 0; n < NTR; n++) {
+        const real c1 = upd(C[s][n], dtr, R[s][n]);
+        // sign of c1 - (1+rcm) c; in FP32 exact for the operands (one FMA)
+        bad |= below_keep(c1, p.keep, C[s][n], p.natol);
+      }
+    }
+  }
+  return bad;
+}
+
+// The accepted attempt: C = C + dtr R (:137), the same roundings as the test.
+template <typename real, int LPL>
+__device__ __forceinline__ void attempt_apply(real (&C)[LPL][NTR], const real (&R)[LPL][NTR],
+                                              real dtr) {
+#pragma unroll
+  for (int s = 0; s < LPL; s++) {
+    if constexpr (std::is_same<real, float>::value) {
+#pragma unroll
+      for (int n = 0; n + 1 < NTR; n += 2) {
+        const float2 c1 = __ffma2_rn(make_float2(dtr, dtr), make_float2(R[s][n], R[s][n + 1]),
+                                     make_float2(C[s][n], C[s][n + 1]));
+        C[s][n] = c1.x;
+        C[s][n + 1] = c1.y;
+      }
+      C[s][NTR - 1] = upd(C[s][NTR - 1], dtr, R[s][NTR - 1]);
+    } else {
+#pragma unroll
+      for (int n = 0; n < NTR; n++) C[s][n] = upd(C[s][n], dtr, R[s][n]);
+    }
+  }
+}
+
 // ADAPTIVE_EULER (solver_library.F90:104-140) on one column, cut decided by
 // the column's own cells.  A rejected attempt re-evaluates get_rhs at the
 // same state in the reference, which yields the same rhs, so it is reused.
@@ -468,12 +525,7 @@ __device__ __forceinline__ int epilogue(const Params<real>& p, int lane, int K,
 // exact in FP64 (p.ticks), the same decisions are taken with integer ticks
 // of dt/4^mstop (mstop = first level with dt/4^m <= dt_min), which keeps the
 // loop off the FP64 pipe; otherwise the FP64 sums are kept.
-//
-// PROBE: the gate of the surrogate step.  A column whose first attempt (the
-// whole coupling step at once) is accepted finishes exactly as without
-// PROBE; a column whose first attempt is rejected returns at once with
-// attempts = -1, its state C untouched, and no budget or epilogue work.
-template <typename real, int LPL, bool BC4, bool BIO3, bool TICKS, bool PROBE = false>
+template <typename real, int LPL, bool BC4, bool BIO3, bool TICKS>
 __device__ __forceinline__ ColResult solve_adaptive(
     const Params<real>& p, const Lane<real, LPL, BC4>& lc, int lane, int K,
     real (&C)[LPL][NTR], real (&ftop)[NTR], double dt, double (&bud)[4]) {
@@ -481,8 +533,7 @@ __device__ __forceinline__ ColResult solve_adaptive(
   real dn[LPL];
   ColResult res{0, 0, 0, 0, 1e300};
   Budget<real, LPL, BC4> B;
-  // the gate takes the column's inventories only once it keeps the column
-  if (!PROBE) B.start(p, lc, C);
+  B.start(p, lc, C);
   unsigned long long t = 0, T = 0, inc = 0;
   double dt_int = 0.0, dt_red = dt;
   if (TICKS) { T = 1ull << (2 * p.mstop); inc = T; }
@@ -492,39 +543,8 @@ __device__ __forceinline__ ColResult solve_adaptive(
   while (TICKS ? (t < T) : (dt_int < dt)) {
     if (res.attempts >= p.max_attempts) { res.capped = 1; break; }
     res.attempts++;
-    bool bad = false;
-#pragma unroll
-    for (int s = 0; s < LPL; s++) {
-      // lanes past the column hold zeros: c1 = 0 never falls below -atol
-      if constexpr (std::is_same<real, float>::value) {
-        // tracer pairs in packed FP32x2 FMAs (per component the scalar's
-        // rounding), tracer 10 alone
-#pragma unroll
-        for (int n = 0; n + 1 < NTR; n += 2) {
-          const float2 c = make_float2(C[s][n], C[s][n + 1]);
-          const float2 c1 = __ffma2_rn(make_float2(dtr, dtr),
-                                       make_float2(R[s][n], R[s][n + 1]), c);
-          const float2 t = __ffma2_rn(make_float2(-p.keep, -p.keep), c, c1);
-          bad |= (t.x < p.natol) | (t.y < p.natol);
-        }
-        bad |= below_keep(upd(C[s][NTR - 1], dtr, R[s][NTR - 1]), p.keep, C[s][NTR - 1],
-                          p.natol);
-      } else {
-#pragma unroll
-        for (int n = 0; n < NTR; n++) {
-          const real c1 = upd(C[s][n], dtr, R[s][n]);
-          // sign of c1 - (1+rcm) c; in FP32 exact for the operands (one FMA)
-          bad |= below_keep(c1, p.keep, C[s][n], p.natol);
-        }
-      }
-    }
-    const bool reject = __any_sync(FULL, bad);
+    const bool reject = __any_sync(FULL, attempt_fails<real, LPL>(p, C, R, dtr));
     const bool can_cut = TICKS ? (m < p.mstop) : (dt_red > p.dt_min);
-    if (PROBE && reject && can_cut) {
-      res.attempts = -1;
-      return res;
-    }
-    if (PROBE && res.attempts == 1) B.start(p, lc, C);
     if (reject && can_cut) {
       m++;
       dtr = dtr * real(0.25);
@@ -532,22 +552,7 @@ __device__ __forceinline__ ColResult solve_adaptive(
       else dt_red = dt_red * 0.25;
     } else {
       B.account(p, dtr, ftop, dn);
-#pragma unroll
-      for (int s = 0; s < LPL; s++) {
-        if constexpr (std::is_same<real, float>::value) {
-#pragma unroll
-          for (int n = 0; n + 1 < NTR; n += 2) {
-            const float2 c1 = __ffma2_rn(make_float2(dtr, dtr), make_float2(R[s][n], R[s][n + 1]),
-                                         make_float2(C[s][n], C[s][n + 1]));
-            C[s][n] = c1.x;
-            C[s][n + 1] = c1.y;
-          }
-          C[s][NTR - 1] = upd(C[s][NTR - 1], dtr, R[s][NTR - 1]);
-        } else {
-#pragma unroll
-          for (int n = 0; n < NTR; n++) C[s][n] = upd(C[s][n], dtr, R[s][n]);
-        }
-      }
+      attempt_apply<real, LPL>(C, R, dtr);
       if (TICKS) t += inc;
       else dt_int = dt_int + dt_red;
       res.accepted++;
@@ -557,6 +562,36 @@ __device__ __forceinline__ ColResult solve_adaptive(
     }
   }
   if (mmax >= 0) res.min_dt = ldexp(dt, -2 * mmax);
+  B.finish(p, lc, C, bud, lane);
+  res.nan = epilogue<real, LPL>(p, lane, K, C);
+  return res;
+}
+
+// The gate of the surrogate step: the adaptive Euler step's first attempt,
+// the whole coupling step dt at once.  If it is accepted (or no cut is
+// allowed) the column is finished exactly as solve_adaptive finishes it
+// after that one attempt; otherwise the result has attempts = -1, the state
+// C untouched and no budget or epilogue work.
+template <typename real, int LPL, bool BC4, bool BIO3>
+__device__ __forceinline__ ColResult probe_column(
+    const Params<real>& p, const Lane<real, LPL, BC4>& lc, int lane, int K,
+    real (&C)[LPL][NTR], real (&ftop)[NTR], double dt, double (&bud)[4]) {
+  real R[LPL][NTR];
+  real dn[LPL];
+  ColResult res{-1, 0, 0, 0, 1e300};
+  const real dtr = (real)dt;
+  rhs_any<real, LPL, BC4, BIO3>(p, lc, lane, K, C, R, ftop, dn);
+  const bool reject = __any_sync(FULL, attempt_fails<real, LPL>(p, C, R, dtr));
+  // a cut is allowed at the first attempt (m = 0 < mstop, or dt > dt_min)
+  const bool can_cut = p.ticks ? (0 < p.mstop) : (dt > p.dt_min);
+  if (reject && can_cut) return res;
+  Budget<real, LPL, BC4> B;
+  B.start(p, lc, C);
+  B.account(p, dtr, ftop, dn);
+  attempt_apply<real, LPL>(C, R, dtr);
+  res.attempts = 1;
+  res.accepted = 1;
+  res.min_dt = dt;
   B.finish(p, lc, C, bud, lane);
   res.nan = epilogue<real, LPL>(p, lane, K, C);
   return res;
@@ -742,11 +777,13 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       double bud[4] = {0.0, 0.0, 0.0, 0.0};
       ColResult r;
       constexpr bool PROBE = KIND == KIND_PROBE;
-      if (KIND == KIND_ADAPT || PROBE)
-        r = p.ticks ? solve_adaptive<real, LPL, BC4, BIO3, true, PROBE>(p, lc, lane, K, C, ftop,
-                                                                       a.dt, bud)
-                    : solve_adaptive<real, LPL, BC4, BIO3, false, PROBE>(p, lc, lane, K, C, ftop,
-                                                                        a.dt, bud);
+      if (PROBE)
+        r = probe_column<real, LPL, BC4, BIO3>(p, lc, lane, K, C, ftop, a.dt, bud);
+      else if (KIND == KIND_ADAPT)
+        r = p.ticks ? solve_adaptive<real, LPL, BC4, BIO3, true>(p, lc, lane, K, C, ftop, a.dt,
+                                                                bud)
+                    : solve_adaptive<real, LPL, BC4, BIO3, false>(p, lc, lane, K, C, ftop, a.dt,
+                                                                 bud);
       else
         r = solve_fixed<real, LPL, BC4, BIO3>(p, lc, lane, K, C, ftop, a.dt, a.method,
                                               bud);
@@ -786,18 +823,31 @@ k_column(ColumnArgs<real> a, Params<real> p) {
     }
     __syncthreads();
     if (KIND == KIND_PROBE) {
-      if (tid == 0) {
-        // the tile's rejected columns into the list: one reservation per tile
-        int n = 0;
-        for (int q = 0; q < tc; q++)
-          if (s_heavy[q]) s_hcol[n++] = q;
+      if (tid < 32) {
+        // the tile's rejected columns into the list in tile order, one
+        // reservation per tile: warp 0 ranks them by ballot (tiles of up to
+        // 64 columns, two halves)
+        const unsigned lo = __ballot_sync(FULL, lane < tc && s_heavy[lane]);
+        const unsigned hi = __ballot_sync(FULL, lane + 32 < tc && s_heavy[lane + 32]);
+        const int nlo = __popc(lo), n = nlo + __popc(hi);
         unsigned at = 0;
-        if (n > 0) {
-          at = atomicAdd(a.nheavy, (unsigned)n);
-          for (int q = 0; q < n; q++) a.heavy[at + q] = slot0 + s_hcol[q];
+        if (lane == 0 && n > 0) at = atomicAdd(a.nheavy, (unsigned)n);
+        at = __shfl_sync(FULL, at, 0);
+        const unsigned below = (1u << lane) - 1u;
+        if ((lo >> lane) & 1u) {
+          const int r = __popc(lo & below);
+          s_hcol[r] = lane;
+          a.heavy[at + r] = slot0 + lane;
         }
-        s_hn = n;
-        s_hat = at;
+        if ((hi >> lane) & 1u) {
+          const int r = nlo + __popc(hi & below);
+          s_hcol[r] = lane + 32;
+          a.heavy[at + r] = slot0 + lane + 32;
+        }
+        if (lane == 0) {
+          s_hn = n;
+          s_hat = at;
+        }
       }
       if (a.xfeat) {
         // their network input rows, from the staged (unchanged) state and
