@@ -30,8 +30,9 @@ extern "C" {
 #endif
 
 #define SED_NTR 11        /* OMEXDIA+P tracers, order in sed_tracer_name() */
-#define SED_KMAX_LIMIT 63 /* layers per column the kernels hold on chip (one
-                             or two per lane of a warp, the last lane free) */
+#define SED_KMAX_LIMIT 127 /* layers per column the kernels hold on chip
+                              (one, two or four per lane of a warp, the last
+                              lane free) */
 
 /* return codes */
 #define SED_OK 0
@@ -136,9 +137,10 @@ typedef struct sed_handle sed_handle;
  * hzg_omexdia_p parameters of fabm_sed.nml:51-77, clamp at 0, FP32. */
 int sed_default_params(sed_params *p);
 
-/* Create a solver for an inum x jnum grid of kmax layers (kmax <= 64) and
- * ntr tracers (must be SED_NTR).  Replaces the allocations of
- * fabm_sediment_component.F90:521-541 and type_sed%initialize. */
+/* Create a solver for an inum x jnum grid of kmax layers (kmax <=
+ * SED_KMAX_LIMIT) and ntr tracers (must be SED_NTR).  Replaces the
+ * allocations of fabm_sediment_component.F90:521-541 and
+ * type_sed%initialize. */
 int sed_create(const sed_params *p, int inum, int jnum, int kmax, int ntr,
                sed_handle **out);
 
@@ -275,7 +277,8 @@ int sed_host_unregister(void *ptr);
  * Launch tuning (no counterpart in the reference, whose solver has no
  * launch parameters).  Index [0] of the per-class fields is the class of
  * columns with up to 31 active layers (one layer per lane), [1] the class
- * with 32..63 (two layers per lane).  sed_set_grid lays the active columns
+ * with 32..63 (two layers per lane); the class with 64..127 (four layers
+ * per lane) keeps the defaults.  sed_set_grid lays the active columns
  * out once (depth class, then `segments` contiguous column ranges balanced
  * by active layers, each padded to 64 slots), so every tuning below is a
  * pure launch choice: results are bit-identical under any of them.  The
@@ -398,7 +401,8 @@ const char *sed_sur_last_error(const sed_surrogate *s);
  * 11 K + 13 and nout = 11 K for a grid of K layers. */
 int sed_sur_set_norm(sed_surrogate *s, const float *norm, int n);
 /* nsteps coupling steps of the handle's device state with the surrogate
- * (FP32 state, per-column cuts, every active column at kmax layers).  Each
+ * (FP32 state, per-column cuts, every active column at kmax <= 63 layers).
+ * Each
  * step runs:
  *   1. the gate: every column's first adaptive attempt, the whole step at
  *      once.  A column whose attempt is accepted is done, with exactly the

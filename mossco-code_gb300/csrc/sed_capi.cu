@@ -41,7 +41,12 @@ const char* kTracerNames[SED_NTR] = {
 // Column ranges of the layout, and work counters: 2 for whole-class
 // launches, 2 per pipeline chunk and class.
 constexpr int kMaxSeg = 8;
-constexpr int kQueues = 2 + 2 * kMaxSeg;
+// depth classes: up to 31 active layers (one per lane of a warp), 32..63
+// (two), 64..127 (four); the first two are the tunable ones of sed_tuning
+constexpr int kBins = 3;
+constexpr int kTunedBins = 2;
+constexpr int kQueues = kBins + kBins * kMaxSeg;
+inline int depth_class(int k) { return k <= 31 ? 0 : (k <= 63 ? 1 : 2); }
 constexpr int kSlotPad = 64;  // every segment is a multiple of every tile width
 
 // One depth class: its slots, split into the segments of the column ranges,
@@ -115,7 +120,7 @@ struct sed_handle {
   int last_cell[4] = {-99, -99, -99, -99};
   long long still_zero = -1;
   DevBuf d_minloc;
-  Bin bins[2];
+  Bin bins[kBins];
   int nseg = 1;                 // column ranges of the layout
   std::vector<int> seg_col;     // [nseg + 1] column bounds
   int pipe = 1;                 // sed_ode_solver pipeline chunks
@@ -268,8 +273,8 @@ template <typename real>
 int enqueue_columns(sed_handle* h, double dt, int method, int kind) {
   Params<real> p = make_params<real>(h->prm);
   set_clock(p, dt, h->prm.dt_min);
-  CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
-  for (int b = 0; b < 2; b++) {
+  CK(cudaMemsetAsync(h->d_queue.p, 0, kBins * sizeof(unsigned), h->stream), "queue reset");
+  for (int b = 0; b < kBins; b++) {
     const Bin& bin = h->bins[b];
     if (bin.nslots == 0) continue;
     ColumnArgs<real> a = column_args<real>(h, bin, b, dt, method);
@@ -681,7 +686,7 @@ int upload_bgc(sed_handle* h) {
 
 int apply_tuning(sed_handle* h) {
   std::vector<int> tile_k;
-  for (int b = 0; b < 2; b++) {
+  for (int b = 0; b < kBins; b++) {
     Bin& bin = h->bins[b];
     bin.tk0 = (int)tile_k.size();
     bin.occ = 0;
@@ -775,7 +780,7 @@ int ode_solver_pipelined(sed_handle* h, double* conc, double dt, int method) {
     CK(cudaEventRecord(h->pe_in[c], h->s_in), "event");
     cudaStream_t cs = h->s_cmp[c];
     CK(cudaStreamWaitEvent(cs, h->pe_in[c], 0), "wait");
-    for (int b = 0; b < 2; b++) {
+    for (int b = 0; b < kBins; b++) {
       const Bin& bin = h->bins[b];
       const int sl0 = bin.segb[g0], sl1 = bin.segb[g1];
       if (sl1 == sl0) continue;
@@ -783,7 +788,7 @@ int ode_solver_pipelined(sed_handle* h, double* conc, double dt, int method) {
                                    h->kmax, h->ncol, h->nslot, sl0, sl1 - sl0, h->sms, cs),
          "gather launch");
       ColumnArgs<real> a = column_args<real>(h, bin, b, dt, method);
-      restrict_args(a, bin, sl0, sl1, q + 2 + 2 * c + b);
+      restrict_args(a, bin, sl0, sl1, q + kBins + kBins * c + b);
       CK(launch_bin<real>(h, a, p, bin, kind, cs), "column kernel launch");
       CK(launch_scatter_range<real>(h->d_conc.as<real>(), stage, h->d_slot_col.as<int>(),
                                     h->d_kact.as<int>(), NTR, h->kmax, h->ncol, h->nslot,
@@ -880,7 +885,7 @@ int time_step(sed_handle* h, int b, double dt, int method, int reps, float* best
     CK(cudaEventRecord(h->ev0, h->stream), "event");
     if (b >= 0) {
       const Bin& bin = h->bins[b];
-      CK(cudaMemsetAsync(h->d_queue.p, 0, 2 * sizeof(unsigned), h->stream), "queue reset");
+      CK(cudaMemsetAsync(h->d_queue.p, 0, kBins * sizeof(unsigned), h->stream), "queue reset");
       ColumnArgs<real> a = column_args<real>(h, bin, b, dt, method);
       CK(launch_bin<real>(h, a, p, bin, kind, h->stream), "autotune launch");
     } else {
@@ -903,7 +908,7 @@ int autotune_t(sed_handle* h, double dt, int method, int flags, sed_tuning* out)
   int trials = 0;
   const int tcs[] = {0, 8, 16, 32, 64};
   const int thr[] = {64, 128, 256};
-  for (int b = 0; b < 2; b++) {
+  for (int b = 0; b < kTunedBins; b++) {
     Bin& bin = h->bins[b];
     if (bin.nslots == 0) continue;
     int best_tc = bin.tc, best_thr = bin.threads;
@@ -1186,20 +1191,21 @@ int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
       if (acc * h->nseg >= work * s && (c + 1) % 32 == 0) h->seg_col[s++] = c + 1;
     }
   }
-  // slots: depth class (<= 31 layers, 32..63: the warp's last lane stays
-  // free, so the no-flux bottom needs no select), then segment, then active
-  // layers (stable); every (class, segment) run is padded to kSlotPad slots
+  // slots: depth class (<= 31 layers, 32..63, 64..127: the warp's last
+  // lane stays free, so the no-flux bottom needs no select), then segment,
+  // then active layers (stable); every (class, segment) run is padded to
+  // kSlotPad slots
   h->slot_col.clear();
   h->slot_k.clear();
-  for (int b = 0; b < 2; b++) {
+  for (int b = 0; b < kBins; b++) {
     Bin& bin = h->bins[b];
-    bin.lpl = b + 1;
+    bin.lpl = b == 2 ? 4 : b + 1;
     bin.slot0 = (int)h->slot_col.size();
     for (int sg = 0; sg < h->nseg; sg++) {
       bin.segb[sg] = (int)h->slot_col.size();
       std::vector<int> cols;
       for (int c = h->seg_col[sg]; c < h->seg_col[sg + 1]; c++)
-        if (ka[c] > 0 && (ka[c] > 31) == (b == 1)) cols.push_back(c);
+        if (ka[c] > 0 && depth_class(ka[c]) == b) cols.push_back(c);
       std::stable_sort(cols.begin(), cols.end(), [&](int x, int y) { return ka[x] < ka[y]; });
       for (int c : cols) { h->slot_col.push_back(c); h->slot_k.push_back(ka[c]); }
       while (h->slot_col.size() % kSlotPad) { h->slot_col.push_back(-1); h->slot_k.push_back(0); }
@@ -1209,7 +1215,7 @@ int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
     bin.nslots = (int)h->slot_col.size() - bin.slot0;
     // FP32: the warp-direct kernel (the faster one over every regime of the
     // reference workloads); FP64: tiles
-    bin.tc = !h->fp64() ? 0 : (b == 0 ? 32 : 16);
+    bin.tc = !h->fp64() ? 0 : (b == 0 ? 32 : (b == 1 ? 16 : 8));
     bin.threads = !h->fp64() ? 128 : 256;
     bin.bps = 0;
   }
@@ -1262,7 +1268,10 @@ int sed_set_grid(sed_handle* h, const double* dz, const double* dzc,
   }
   CK(h->d_tile_k.alloc((size_t)(h->nslot / 8 + 1) * sizeof(int)), "tile_k");
   if (h->table()) {  // the per-slot table follows the new layout
-    h->bins[0].tc = h->bins[1].tc = 0;
+    if (h->bins[2].nslots > 0)
+      return h->fail(SED_E_ARG, "per-column parameter sets and temperature-dependent rates "
+                                "need columns of at most 63 active layers");
+    for (Bin& bin : h->bins) bin.tc = 0;
     int rc = h->fp64() ? upload_bgc<double>(h) : upload_bgc<float>(h);
     if (rc) return rc;
   }
@@ -1449,7 +1458,8 @@ int sed_sur_set_norm(sed_surrogate* s, const float* norm, int n) {
 static int surrogate_bin(sed_handle* h) {
   for (int i = 0; i < h->nslot; i++)
     if (h->slot_col[i] >= 0 && h->slot_k[i] != h->kmax) return -1;
-  const int b = h->kmax > 31 ? 1 : 0;
+  if (h->kmax > 63) return -1;
+  const int b = depth_class(h->kmax);
   return h->bins[b].nslots > 0 ? b : -1;
 }
 
@@ -1503,7 +1513,9 @@ static int sur_plan(sed_handle* h, sed_surrogate* s, double dt, double tol, doub
                    s->nin, s->nout, NTR * K + NFORCE, NTR * K);
   if (!s->norm) return h->fail(SED_E_STATE, "sed_sur_set_norm has not been called");
   const int b = surrogate_bin(h);
-  if (b < 0) return h->fail(SED_E_ARG, "the surrogate needs every active column at %d layers", K);
+  if (b < 0)
+    return h->fail(SED_E_ARG, "the surrogate needs every active column at %d layers (at most 63)",
+                   K);
   if (!(dt > 0.0) || !(tol >= 0.0) || !(res_atol >= 0.0))
     return h->fail(SED_E_ARG, "bad dt, tol or res_atol");
   CK(cudaSetDevice(h->device), "set device");
@@ -1781,7 +1793,9 @@ int sed_sur_collect(sed_handle* h, const float* c0, double dt, float* x_dev, flo
     return h->fail(SED_E_ARG, "row pitches %d / %d below %d / %d", pitch_x, pitch_y,
                    NTR * K + NFORCE, NTR * K);
   const int b = surrogate_bin(h);
-  if (b < 0) return h->fail(SED_E_ARG, "training rows need every active column at %d layers", K);
+  if (b < 0)
+    return h->fail(SED_E_ARG, "training rows need every active column at %d layers (at most 63)",
+                   K);
   if (!(dt > 0.0)) return h->fail(SED_E_ARG, "bad dt");
   CK(cudaSetDevice(h->device), "set device");
   const size_t state = (size_t)NTR * K * h->nslot * sizeof(float);
@@ -1929,16 +1943,19 @@ int sed_set_column_bgc(sed_handle* h, const double* params) {
     return h->fail(SED_E_ARG, "per-column parameter sets need per-column cuts");
   h->bgc_cols.assign(params, params + SED_NBGC * nc);
   h->has_bgc = true;
+  if (h->bins[2].nslots > 0)
+    return h->fail(SED_E_ARG, "per-column parameter sets need columns of at most 63 active "
+                              "layers");
   // ensembles step with the warp-direct kernels
-  Bin keep[2] = {h->bins[0], h->bins[1]};
-  h->bins[0].tc = h->bins[1].tc = 0;
+  Bin keep[kBins];
+  std::copy(h->bins, h->bins + kBins, keep);
+  for (Bin& bin : h->bins) bin.tc = 0;
   int rc = h->fp64() ? upload_bgc<double>(h) : upload_bgc<float>(h);
   if (!rc) rc = apply_tuning(h);
   if (rc) {
     const std::string why = h->err;
     h->has_bgc = false;
-    h->bins[0] = keep[0];
-    h->bins[1] = keep[1];
+    std::copy(keep, keep + kBins, h->bins);
     apply_tuning(h);
     h->err = why;
     return rc;
@@ -2024,7 +2041,7 @@ int spinup_t(sed_handle* h, int mode, int column, const double* bdys1, const dou
   const bool bc4 = h->prm.bcup_particulate == 4, bio3 = h->prm.bioturbation_profile == 3;
   const int kind = method == SED_ADAPTIVE_EULER ? KIND_ADAPT : KIND_FIXED;
   if (mode == SED_SPINUP_ALL) {
-    for (int b = 0; b < 2; b++) {
+    for (int b = 0; b < kBins; b++) {
       const Bin& bin = h->bins[b];
       if (bin.nslots == 0) continue;
       const int occ = column_warp_blocks_per_sm<real>(bin.lpl, bc4, kind, 128, bio3);
@@ -2051,7 +2068,9 @@ int spinup_t(sed_handle* h, int mode, int column, const double* bdys1, const dou
       if (h->slot_col[s] == column) slot = s;
   }
   if (slot < 0) return h->fail(SED_E_ARG, "spin-up column %d is not an active column", column);
-  const int b = slot >= h->bins[1].slot0 && h->bins[1].nslots > 0 ? 1 : 0;
+  int b = 0;
+  for (int q = 0; q < kBins; q++)
+    if (slot >= h->bins[q].slot0 && slot < h->bins[q].slot0 + h->bins[q].nslots) b = q;
   // its forcing rows replaced by the spin-up forcing, and put back after
   const size_t rs = h->rsize(), pitch = (size_t)h->nslot * rs;
   std::vector<real> saved(NFORCE), spin(NFORCE);
@@ -2246,7 +2265,7 @@ int sed_get_boundary(sed_handle* h, double* bdys, double* fluxes) {
 int sed_get_tuning(const sed_handle* h, sed_tuning* t) {
   if (!h || !t) return SED_E_ARG;
   memset(t, 0, sizeof *t);
-  for (int b = 0; b < 2; b++) {
+  for (int b = 0; b < kTunedBins; b++) {
     t->tile_columns[b] = h->bins[b].tc;
     t->threads[b] = h->bins[b].threads;
     t->blocks_per_sm[b] = h->bins[b].bps;
@@ -2260,7 +2279,7 @@ int sed_get_tuning(const sed_handle* h, sed_tuning* t) {
 int sed_set_tuning(sed_handle* h, const sed_tuning* t) {
   if (!h || !t) return SED_E_ARG;
   if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
-  for (int b = 0; b < 2; b++) {
+  for (int b = 0; b < kTunedBins; b++) {
     const int tc = t->tile_columns[b], th = t->threads[b];
     if (tc != 0 && tc != 8 && tc != 16 && tc != 32 && tc != 64)
       return h->fail(SED_E_ARG, "tile_columns[%d]=%d: 0 (warp-direct), 8, 16, 32 or 64", b, tc);
@@ -2277,8 +2296,9 @@ int sed_set_tuning(sed_handle* h, const sed_tuning* t) {
                    h->nseg);
   if (t->max_attempts <= 0) return h->fail(SED_E_ARG, "max_attempts must be > 0");
   CK(cudaSetDevice(h->device), "set device");
-  Bin keep[2] = {h->bins[0], h->bins[1]};
-  for (int b = 0; b < 2; b++) {
+  Bin keep[kBins];
+  std::copy(h->bins, h->bins + kBins, keep);
+  for (int b = 0; b < kTunedBins; b++) {
     h->bins[b].tc = t->tile_columns[b];
     h->bins[b].threads = t->threads[b];
     h->bins[b].bps = t->blocks_per_sm[b];
@@ -2286,8 +2306,7 @@ int sed_set_tuning(sed_handle* h, const sed_tuning* t) {
   int rc = apply_tuning(h);
   if (rc) {
     const std::string why = h->err;
-    h->bins[0] = keep[0];
-    h->bins[1] = keep[1];
+    std::copy(keep, keep + kBins, h->bins);
     apply_tuning(h);
     h->err = why;
     return rc;

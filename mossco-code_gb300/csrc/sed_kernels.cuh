@@ -678,7 +678,7 @@ __device__ __forceinline__ ColResult solve_fixed(
 // for two layers per lane, one for the FP64 path.
 template <typename real, int LPL>
 struct MinBlocks {
-  static constexpr int value = sizeof(real) == 4 ? (LPL == 1 ? 3 : 2) : 1;
+  static constexpr int value = sizeof(real) == 4 ? (LPL == 1 ? 3 : LPL == 2 ? 2 : 1) : 1;
 };
 
 template <typename real, int LPL, bool BC4, bool BIO3, int KIND>
@@ -1563,7 +1563,8 @@ cudaError_t launch_column_k(const ColumnArgs<real>& a, const Params<real>& p,
   if (kind == KIND_FIXED)
     return launch_column_t<real, LPL, BC4, BIO3, KIND_FIXED>(a, p, blocks, threads, st);
   if (kind == KIND_PROBE) {
-    if constexpr (std::is_same<real, float>::value)
+    // the surrogate's gate: FP32 state of at most 63 layers
+    if constexpr (std::is_same<real, float>::value && LPL <= 2)
       return launch_column_t<real, LPL, BC4, BIO3, KIND_PROBE>(a, p, blocks, threads, st);
     return cudaErrorInvalidValue;
   }
@@ -1584,6 +1585,9 @@ cudaError_t launch_column(const ColumnArgs<real>& a, const Params<real>& p,
   if (lpl == 1)
     return bc4 ? launch_column_b<real, 1, true>(a, p, kind, blocks, threads, st)
                : launch_column_b<real, 1, false>(a, p, kind, blocks, threads, st);
+  if (lpl == 4)
+    return bc4 ? launch_column_b<real, 4, true>(a, p, kind, blocks, threads, st)
+               : launch_column_b<real, 4, false>(a, p, kind, blocks, threads, st);
   return bc4 ? launch_column_b<real, 2, true>(a, p, kind, blocks, threads, st)
              : launch_column_b<real, 2, false>(a, p, kind, blocks, threads, st);
 }
@@ -1618,7 +1622,7 @@ int occupancy_k(int tc, int kind, int threads) {
   if (kind == KIND_ADAPT) return occupancy_t<real, LPL, BC4, BIO3, KIND_ADAPT>(tc, threads);
   if (kind == KIND_FIXED) return occupancy_t<real, LPL, BC4, BIO3, KIND_FIXED>(tc, threads);
   if (kind == KIND_PROBE) {
-    if constexpr (std::is_same<real, float>::value)
+    if constexpr (std::is_same<real, float>::value && LPL <= 2)
       return occupancy_t<real, LPL, BC4, BIO3, KIND_PROBE>(tc, threads);
     return 0;
   }
@@ -1636,6 +1640,9 @@ int column_blocks_per_sm(int tc, int lpl, bool bc4, int kind, int threads, bool 
   if (lpl == 1)
     return bc4 ? occupancy_b<real, 1, true>(tc, kind, threads, bio3)
                : occupancy_b<real, 1, false>(tc, kind, threads, bio3);
+  if (lpl == 4)
+    return bc4 ? occupancy_b<real, 4, true>(tc, kind, threads, bio3)
+               : occupancy_b<real, 4, false>(tc, kind, threads, bio3);
   return bc4 ? occupancy_b<real, 2, true>(tc, kind, threads, bio3)
              : occupancy_b<real, 2, false>(tc, kind, threads, bio3);
 }
@@ -1655,7 +1662,7 @@ cudaError_t launch_warp_e(const ColumnArgs<real>& a, const Params<real>& p, int 
   if (kind == KIND_SUR) {
     // the surrogate step's residual test and fallback: FP32 state, one
     // parameter set
-    if constexpr (std::is_same<real, float>::value && !ENS) {
+    if constexpr (std::is_same<real, float>::value && !ENS && LPL <= 2) {
       if (a.nrepeat > 1) return cudaErrorInvalidValue;
       return launch_warp_t<real, LPL, BC4, BIO3, KIND_SUR, false, ENS>(a, p, blocks, threads, st);
     }
@@ -1695,7 +1702,7 @@ template <typename real, int LPL, bool BC4, bool BIO3>
 int warp_occupancy_k(int kind, int threads) {
   if (kind == KIND_FIXED) return warp_occupancy_t<real, LPL, BC4, BIO3, KIND_FIXED, false>(threads);
   if (kind == KIND_SUR) {
-    if constexpr (std::is_same<real, float>::value)
+    if constexpr (std::is_same<real, float>::value && LPL <= 2)
       return warp_occupancy_t<real, LPL, BC4, BIO3, KIND_SUR, false>(threads);
     return 0;
   }
@@ -1706,8 +1713,14 @@ int warp_occupancy_k(int kind, int threads) {
 template <typename real, int LPL, bool BC4, bool BIO3>
 static cudaError_t launch_warp_any(const ColumnArgs<real>& a, const Params<real>& p, int kind,
                                    int blocks, int threads, cudaStream_t st) {
-  return a.bgc ? launch_warp_ens<real, LPL, BC4, BIO3>(a, p, kind, blocks, threads, st)
-               : launch_warp_k<real, LPL, BC4, BIO3>(a, p, kind, blocks, threads, st);
+  // per-column parameter sets: columns of at most 63 layers
+  if constexpr (LPL > 2) {
+    if (a.bgc) return cudaErrorInvalidValue;
+    return launch_warp_k<real, LPL, BC4, BIO3>(a, p, kind, blocks, threads, st);
+  } else {
+    return a.bgc ? launch_warp_ens<real, LPL, BC4, BIO3>(a, p, kind, blocks, threads, st)
+                 : launch_warp_k<real, LPL, BC4, BIO3>(a, p, kind, blocks, threads, st);
+  }
 }
 
 template <typename real>
@@ -1719,6 +1732,12 @@ cudaError_t launch_column_warp(const ColumnArgs<real>& a, const Params<real>& p,
                        : launch_warp_any<real, 1, true, false>(a, p, kind, blocks, threads, st);
     return b3 ? launch_warp_any<real, 1, false, true>(a, p, kind, blocks, threads, st)
               : launch_warp_any<real, 1, false, false>(a, p, kind, blocks, threads, st);
+  }
+  if (lpl == 4) {
+    if (bc4) return b3 ? launch_warp_any<real, 4, true, true>(a, p, kind, blocks, threads, st)
+                       : launch_warp_any<real, 4, true, false>(a, p, kind, blocks, threads, st);
+    return b3 ? launch_warp_any<real, 4, false, true>(a, p, kind, blocks, threads, st)
+              : launch_warp_any<real, 4, false, false>(a, p, kind, blocks, threads, st);
   }
   if (bc4) return b3 ? launch_warp_any<real, 2, true, true>(a, p, kind, blocks, threads, st)
                      : launch_warp_any<real, 2, true, false>(a, p, kind, blocks, threads, st);
@@ -1733,6 +1752,12 @@ int column_warp_blocks_per_sm(int lpl, bool bc4, int kind, int threads, bool bio
                          : warp_occupancy_k<real, 1, true, false>(kind, threads);
     return bio3 ? warp_occupancy_k<real, 1, false, true>(kind, threads)
                 : warp_occupancy_k<real, 1, false, false>(kind, threads);
+  }
+  if (lpl == 4) {
+    if (bc4) return bio3 ? warp_occupancy_k<real, 4, true, true>(kind, threads)
+                         : warp_occupancy_k<real, 4, true, false>(kind, threads);
+    return bio3 ? warp_occupancy_k<real, 4, false, true>(kind, threads)
+                : warp_occupancy_k<real, 4, false, false>(kind, threads);
   }
   if (bc4) return bio3 ? warp_occupancy_k<real, 2, true, true>(kind, threads)
                        : warp_occupancy_k<real, 2, true, false>(kind, threads);
@@ -1904,6 +1929,27 @@ cudaError_t launch_rate_temperature(const real* base, real* tab, const int* slot
   prefix template int warp_occupancy_k<real, 1, true, BIO3>(int, int);          \
   prefix template int warp_occupancy_k<real, 2, false, BIO3>(int, int);         \
   prefix template int warp_occupancy_k<real, 2, true, BIO3>(int, int);
+
+// The kernels of the deepest class (64..127 layers, four per lane), one
+// parameter set, compiled in their own translation units: the tile kernels
+// and the warp-direct ones.
+#define SED_DEEP_TILE_VARIANT(prefix, real, BIO3)                               \
+  prefix template cudaError_t launch_column_k<real, 4, false, BIO3>(            \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t); \
+  prefix template cudaError_t launch_column_k<real, 4, true, BIO3>(             \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t); \
+  prefix template int occupancy_k<real, 4, false, BIO3>(int, int, int);         \
+  prefix template int occupancy_k<real, 4, true, BIO3>(int, int, int);
+#define SED_DEEP_WARP_VARIANT(prefix, real, BIO3)                               \
+  prefix template cudaError_t launch_warp_k<real, 4, false, BIO3>(              \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t); \
+  prefix template cudaError_t launch_warp_k<real, 4, true, BIO3>(               \
+      const ColumnArgs<real>&, const Params<real>&, int, int, int, cudaStream_t); \
+  prefix template int warp_occupancy_k<real, 4, false, BIO3>(int, int);         \
+  prefix template int warp_occupancy_k<real, 4, true, BIO3>(int, int);
+#define SED_DEEP_VARIANT(prefix, real, BIO3)                                    \
+  SED_DEEP_TILE_VARIANT(prefix, real, BIO3)                                     \
+  SED_DEEP_WARP_VARIANT(prefix, real, BIO3)
 
 // The warp-direct kernels with a parameter set per column.
 #define SED_WARP_ENS_VARIANT(prefix, real, BIO3)                                \

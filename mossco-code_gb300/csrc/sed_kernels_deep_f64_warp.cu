@@ -1,0 +1,8 @@
+// sed_kernels_deep_f64_warp.cu -- the warp-direct kernels of the deepest depth
+// class (64..127 active layers, four layers per lane of a warp), double state,
+// compiled apart so the build runs in parallel.
+#include "sed_kernels.cuh"
+
+namespace sed {
+SED_DEEP_WARP_VARIANT(, double, false)
+}  // namespace sed

@@ -9,5 +9,7 @@ SED_WARP_VARIANT(extern, float, false)
 SED_WARP_VARIANT(extern, float, true)
 SED_WARP_ENS_VARIANT(extern, float, false)
 SED_WARP_ENS_VARIANT(extern, float, true)
+SED_DEEP_VARIANT(extern, float, false)
+SED_DEEP_VARIANT(extern, float, true)
 SED_INSTANTIATE(float)
 }  // namespace sed

@@ -9,5 +9,7 @@ SED_WARP_VARIANT(extern, double, false)
 SED_WARP_VARIANT(extern, double, true)
 SED_WARP_ENS_VARIANT(extern, double, false)
 SED_WARP_ENS_VARIANT(extern, double, true)
+SED_DEEP_VARIANT(extern, double, false)
+SED_DEEP_VARIANT(extern, double, true)
 SED_INSTANTIATE(double)
 }  // namespace sed

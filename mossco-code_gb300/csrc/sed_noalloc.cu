@@ -131,8 +131,8 @@ extern "C" int sed_ode_solver_noalloc(const sed_params* p, int inum, int jnum,
     }
   }
   const bool bc4 = p->bcup_particulate == 4;
-  const int lpl = kmax > 31 ? 2 : 1;
-  const int tc = kmax > 31 ? 16 : 32;
+  const int lpl = kmax > 63 ? 4 : (kmax > 31 ? 2 : 1);
+  const int tc = kmax > 63 ? 8 : (kmax > 31 ? 16 : 32);
   const int ntiles = (ncol + tc - 1) / tc;
   const int nslot = ntiles * tc;
   const Layout L = make_layout(ncol, kmax, nslot, ntiles, bc4);

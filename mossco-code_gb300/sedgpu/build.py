@@ -25,7 +25,10 @@ SOURCES = ["sed_kernels_f32.cu", "sed_kernels_f64.cu", "sed_kernels_f32_bio3.cu"
            "sed_kernels_f64_bio3.cu", "sed_kernels_warp.cu", "sed_kernels_warp_bio3.cu",
            "sed_capi.cu", "sed_noalloc.cu", "sur_kernels.cu", "sur_capi.cu", "sur_loop.cu",
            "sed_kernels_warp_ens.cu", "sed_kernels_warp_ens_bio3.cu", "pel_capi.cu",
-           "cpl_capi.cu", "sur_tc.cu"]
+           "cpl_capi.cu", "sur_tc.cu", "sed_kernels_deep_f32.cu",
+           "sed_kernels_deep_f32_bio3.cu", "sed_kernels_deep_f64_tile.cu",
+           "sed_kernels_deep_f64_warp.cu", "sed_kernels_deep_f64_bio3_tile.cu",
+           "sed_kernels_deep_f64_bio3_warp.cu"]
 # The FP64 kernels evaluate the reference's arithmetic operation by
 # operation: no multiply-add contraction.
 # The FP32 kernels write every fused multiply-add explicitly (fmaf): without
@@ -40,7 +43,13 @@ EXTRA_FLAGS = {"sed_kernels_f64.cu": ["-fmad=false"],
                "sed_kernels_warp_ens.cu": ["-fmad=false"],
                "sed_kernels_warp_ens_bio3.cu": ["-fmad=false"],
                "pel_capi.cu": ["-fmad=false"],
-               "cpl_capi.cu": ["-fmad=false"]}
+               "cpl_capi.cu": ["-fmad=false"],
+               "sed_kernels_deep_f32.cu": ["-fmad=false"],
+               "sed_kernels_deep_f32_bio3.cu": ["-fmad=false"],
+               "sed_kernels_deep_f64_tile.cu": ["-fmad=false"],
+               "sed_kernels_deep_f64_warp.cu": ["-fmad=false"],
+               "sed_kernels_deep_f64_bio3_tile.cu": ["-fmad=false"],
+               "sed_kernels_deep_f64_bio3_warp.cu": ["-fmad=false"]}
 HEADERS = ["sed_device.cuh", "sed_kernels.cuh", "sed_launch.h", "sed_params.h",
            "sur_kernels.h", "sur_internal.h", "sur_loop.h", "cpl_internal.h",
            "cpl_map.cuh", "sur_tc.h", "sur_gelu.cuh"]

@@ -22,7 +22,7 @@ SED_E_CUDA, SED_E_STATE, SED_E_NOMEM, SED_E_NODEVICE = -4, -5, -6, -7
 SED_E_TOO_LARGE = -9
 SED_FP32, SED_FP64 = 0, 1
 SED_CUT_PER_COLUMN, SED_CUT_GLOBAL = 0, 1
-SED_KMAX_LIMIT = 63
+SED_KMAX_LIMIT = 127
 
 
 class SedError(RuntimeError):

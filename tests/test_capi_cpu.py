@@ -56,7 +56,8 @@ def test_bad_sizes_rejected_before_device(lib):
     p = capi.default_params()
     h = capi._H()
     assert lib.sed_create(ctypes.byref(p), 0, 4, 10, NTR, ctypes.byref(h)) == capi.SED_E_ARG
-    assert lib.sed_create(ctypes.byref(p), 4, 4, 65, NTR, ctypes.byref(h)) == capi.SED_E_ARG
+    assert lib.sed_create(ctypes.byref(p), 4, 4, capi.SED_KMAX_LIMIT + 1, NTR,
+                          ctypes.byref(h)) == capi.SED_E_ARG
     assert lib.sed_create(ctypes.byref(p), 4, 4, 10, 12, ctypes.byref(h)) == capi.SED_E_ARG
     assert lib.sed_create(None, 4, 4, 10, NTR, ctypes.byref(h)) == capi.SED_E_ARG
 

@@ -1,6 +1,7 @@
 """Edge cases of the sediment path on the GPU, FP64 state against the oracle
-bit for bit: the depth-class boundaries (1, 31, 32, 33 and the maximum 63
-active layers, where a warp's lanes hold one or two layers), a single
+bit for bit: the depth-class boundaries (1, 31, 32, 33, 63, 64, 65 and the
+maximum 127 active layers, where a warp's lanes hold one, two or four
+layers), a single
 column, a grid without any active column, and the column counts that leave
 partial warps, tiles and segments."""
 import numpy as np
@@ -32,11 +33,11 @@ def active(cs):
     return np.arange(cs.kmax)[:, None] < cs.kact[None, :]
 
 
-@pytest.mark.parametrize("K", [1, 2, 31, 32, 33, 63])
+@pytest.mark.parametrize("K", [1, 2, 31, 32, 33, 63, 64, 65, 127])
 def test_depth_class_edges(oracle_mod, K):
     cs = small(ncol=37, K=K, kmin=1, land=0.2, seed=11)
     kact = cs.kact.copy()
-    for i, k in enumerate((K, 0, min(K, 31), min(K, 32), 1)):
+    for i, k in enumerate((K, 0, min(K, 31), min(K, 32), 1, min(K, 63), min(K, 64))):
         kact[i] = k
     cs.kact = kact
     out, fl, st, ref, fref, sref = run_both(oracle_mod, cs)
@@ -86,3 +87,39 @@ def test_partial_warps_tiles_and_segments(oracle_mod, ncol):
     a = active(cs)
     np.testing.assert_array_equal(out[:, a], ref[:, a])
     np.testing.assert_array_equal(fl[:, cs.kact > 0], fref[:, cs.kact > 0])
+
+
+def test_deep_columns_rhs_and_fixed_methods(oracle_mod):
+    """Columns of 64..127 layers (four per lane): the right-hand side, RK4
+    and the drop-in call equal the oracle in FP64 bit for bit, beside
+    shallower columns on the same grid."""
+    cs = small(ncol=40, K=100, kmin=40, land=0.1, seed=5)
+    assert (cs.kact > 63).any() and ((cs.kact > 31) & (cs.kact <= 63)).any()
+    a = active(cs)
+    s = capi.Solver(cs, precision=capi.SED_FP64)
+    s.set_forcing()
+    rhs, fl = s.get_rhs(cs.conc)
+    s.close()
+    ref, fref, _ = oracle_mod.OracleModel(cs).get_rhs(cs.conc)
+    np.testing.assert_array_equal(rhs[:, a], ref[:, a])
+    np.testing.assert_array_equal(fl[:, cs.kact > 0], fref[:, cs.kact > 0])
+    out, _, _, sref_state, _, _ = run_both(oracle_mod, cs, nsteps=2, method=RUNGE_KUTTA_4)
+    np.testing.assert_array_equal(out[:, a], sref_state[:, a])
+    # the drop-in call (host arrays in and out)
+    s = capi.Solver(cs, precision=capi.SED_FP64)
+    c = cs.conc.copy()
+    f = cs.fluxes.copy()
+    s.ode_solver(c, cs.bdys, f, cs.dt, ADAPTIVE_EULER)
+    s.close()
+    r1 = cs.conc.copy()
+    oracle_mod.OracleModel(cs).run(r1, nsteps=1, percol=True, nthreads=1)
+    np.testing.assert_array_equal(c[:, a], r1[:, a])
+
+
+def test_deep_columns_refuse_per_column_sets():
+    """Per-column parameter sets step only columns of at most 63 layers."""
+    cs = small(ncol=8, K=80, seed=2)
+    s = capi.Solver(cs)
+    with pytest.raises(capi.SedError):
+        s.set_column_bgc(cs.bgc_columns().copy())
+    s.close()

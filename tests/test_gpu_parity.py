@@ -255,7 +255,8 @@ def test_status_codes():
     p = capi.params_from(cs)
     h = capi._H()
     import ctypes
-    assert lib.sed_create(ctypes.byref(p), 4, 4, 65, 11, ctypes.byref(h)) == capi.SED_E_ARG
+    assert lib.sed_create(ctypes.byref(p), 4, 4, capi.SED_KMAX_LIMIT + 1, 11,
+                          ctypes.byref(h)) == capi.SED_E_ARG
     assert lib.sed_create(ctypes.byref(p), 4, 4, 10, 12, ctypes.byref(h)) == capi.SED_E_ARG
     p.bcup_dissolved = 7
     assert lib.sed_create(ctypes.byref(p), 4, 4, 10, 11, ctypes.byref(h)) == capi.SED_E_ARG

@@ -229,3 +229,51 @@ def test_tcgen05_training_products_match_mma_sync_at_full_batch():
             o += r * c + r
     finally:
         lib.sed_sur_destroy(h)
+
+
+@pytest.mark.gpu
+def test_adam_step_matches_the_update_formula():
+    """One sed_sur_train_step from known weights equals Adam's first update
+    (m = (1-b1) g, v = (1-b2) g^2, bias-corrected: w - lr g / (|g| + eps))
+    applied in numpy to the gradients sed_sur_grads gives on the same batch,
+    for the FP32 master weights and biases."""
+    import torch
+    shapes = M.layer_shapes(**SHAPE)
+    m, lr, eps = 256, 1e-3, 1e-8
+    rng = np.random.default_rng(6)
+    x = rng.normal(0, 1, (m, SHAPE["nin"])).astype(np.float32)
+    y = (0.3 * rng.normal(0, 1, (m, SHAPE["nout"]))).astype(np.float32)
+    lib, h = _sur(**SHAPE, batch=m, seed=9)
+    try:
+        n = lib.sed_sur_num_params(h)
+        w0 = np.zeros(n, dtype=np.float32)
+        assert lib.sed_sur_get_weights(h, _fp(w0)) == 0
+        g = np.zeros(n, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        assert lib.sed_sur_grads(h, _fp(x), _fp(y), m, _fp(g), _fp(loss)) == 0
+        xp = np.zeros((m, 384), dtype=np.float32)
+        yp = np.zeros((m, 384), dtype=np.float32)
+        xp[:, :SHAPE["nin"]] = x
+        yp[:, :SHAPE["nout"]] = y
+        xd = torch.tensor(xp, device="cuda").to(torch.bfloat16).contiguous()
+        yd = torch.tensor(yp, device="cuda").to(torch.bfloat16).contiguous()
+        torch.cuda.synchronize()
+        rc = lib.sed_sur_train_step(h, ctypes.c_void_p(xd.data_ptr()),
+                                    ctypes.c_void_p(yd.data_ptr()), m, lr, _fp(loss))
+        assert rc == 0, lib.sed_sur_last_error(h)
+        w1 = np.zeros(n, dtype=np.float32)
+        assert lib.sed_sur_get_weights(h, _fp(w1)) == 0
+    finally:
+        lib.sed_sur_destroy(h)
+    g64 = g.astype(np.float64)
+    mhat = (1 - 0.9) * g64 / (1 - 0.9)
+    vhat = (1 - 0.999) * g64 * g64 / (1 - 0.999)
+    expect = w0.astype(np.float64) - lr * mhat / (np.sqrt(vhat) + eps)
+    step = w1.astype(np.float64) - w0
+    # the same gradients (deterministic products) give the same step; the
+    # FP32 arithmetic of the update rounds to within a few ulp of w
+    assert np.abs(w1 - expect).max() <= 4 * np.spacing(np.abs(w0).max() + lr), \
+        np.abs(w1 - expect).max()
+    # Adam's first step moves every parameter with a nonzero gradient by lr
+    nz = np.abs(g64) > 1e-6
+    assert np.allclose(np.abs(step[nz]), lr, rtol=1e-2), np.abs(step[nz]).min()
