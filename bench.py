@@ -467,11 +467,13 @@ def run_headline(args) -> None:
     #    pipelined over the column segments)
     e2e = None
     if not args.no_e2e:
-        host = np.array(S0, dtype=np.float64, copy=True)
-        bd = np.ascontiguousarray(cs.bdys, dtype=np.float64)
-        fl = np.array(cs.fluxes, dtype=np.float64, copy=True)
-        for a in (host, bd, fl):
-            capi.host_register(a)
+        # the caller's arrays in pinned host memory (sed_host_alloc)
+        host = capi.host_empty(S0.shape)
+        host[:] = S0
+        bd = capi.host_empty(cs.bdys.shape)
+        bd[:] = cs.bdys
+        fl = capi.host_empty(cs.fluxes.shape)
+        fl[:] = cs.fluxes
         n_e2e = args.e2e_steps or steps
         for _ in range(args.warmup):
             S.ode_solver_surrogate(s, sur, host, bd, fl, tol=args.sur_tol,
@@ -484,14 +486,13 @@ def run_headline(args) -> None:
             S.ode_solver_surrogate(s, sur, host, bd, fl, tol=args.sur_tol,
                                    res_atol=args.sur_res_atol)
         e2e_s = time.perf_counter() - t1
-        for a in (host, bd, fl):
-            capi.host_unregister(a)
         e2e = {"value": world * cs.n_active * n_e2e / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(host.nbytes + bd.nbytes + fl.nbytes),
                "d2h_bytes_per_step": int(host.nbytes + fl.nbytes),
                "steps": n_e2e,
                "call": "sed_ode_solver_surrogate (FP64 host state in and out, copies "
-                       "pipelined over the column segments)"}
+                       "pipelined over the column segments)",
+               "host_arrays": "pinned (sed_host_alloc)"}
         del host, bd, fl
     t_now = s.tuning().as_dict()
     s.close()
@@ -984,11 +985,13 @@ def run_gpu(args) -> None:
     coupled = None
     if not args.no_e2e:
         n_e2e = args.e2e_steps or steps
-        conc = np.array(cs.conc, dtype=np.float64, copy=True)
-        fluxes = np.array(cs.fluxes, dtype=np.float64, copy=True)
-        bdys = np.array(cs.bdys, dtype=np.float64, copy=True)
-        for a in (conc, fluxes, bdys):
-            capi.host_register(a)
+        # the caller's arrays in pinned host memory (sed_host_alloc)
+        conc = capi.host_empty(cs.conc.shape)
+        conc[:] = cs.conc
+        fluxes = capi.host_empty(cs.fluxes.shape)
+        fluxes[:] = cs.fluxes
+        bdys = capi.host_empty(cs.bdys.shape)
+        bdys[:] = cs.bdys
         for _ in range(args.warmup):
             s.ode_solver(conc, bdys, fluxes, cs.dt)
         torch.cuda.synchronize()
@@ -996,13 +999,11 @@ def run_gpu(args) -> None:
         for _ in range(n_e2e):
             s.ode_solver(conc, bdys, fluxes, cs.dt)
         e2e_s = time.perf_counter() - t1
-        for a in (conc, fluxes, bdys):
-            capi.host_unregister(a)
         h2d = conc.nbytes + bdys.nbytes + fluxes.nbytes
         d2h = conc.nbytes + fluxes.nbytes
         e2e = {"value": world * cs.n_active * n_e2e / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-               "steps": n_e2e, "call": "sed_ode_solver",
+               "steps": n_e2e, "call": "sed_ode_solver", "host_arrays": "pinned (sed_host_alloc)",
                "simulated_days_timed": days(args.warmup, args.warmup + n_e2e, cs.dt)}
         coupled = coupled_e2e(s, cs, args.warmup, n_e2e, world)
 
@@ -1187,8 +1188,9 @@ def run_pelagic(args) -> None:
 
     e2e = None
     if not args.no_e2e:
-        conc = np.array(pcs.conc, dtype=np.float64, copy=True)
-        capi.host_register(conc)
+        # the caller's array in pinned host memory (sed_host_alloc)
+        conc = capi.host_empty(pcs.conc.shape)
+        conc[:] = pcs.conc
         for _ in range(args.warmup):
             s.run(conc)
         torch.cuda.synchronize()
@@ -1196,10 +1198,9 @@ def run_pelagic(args) -> None:
         for _ in range(runs):
             s.run(conc)
         e2e_s = time.perf_counter() - t1
-        capi.host_unregister(conc)
         e2e = {"value": world * wcols * runs / e2e_s, "unit": "column-runs/s",
                "h2d_bytes_per_step": int(conc.nbytes), "d2h_bytes_per_step": int(conc.nbytes),
-               "steps": runs, "call": "pel_run"}
+               "steps": runs, "call": "pel_run", "host_arrays": "pinned (sed_host_alloc)"}
     s.close()
     if rank != 0:
         if dist:

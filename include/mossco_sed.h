@@ -272,6 +272,14 @@ int sed_set_stream(sed_handle *h, void *stream);
 /* Pin (or unpin) a caller's host array so copies run at full speed. */
 int sed_host_register(void *ptr, size_t bytes);
 int sed_host_unregister(void *ptr);
+/* Pinned host memory from the CUDA allocator (no counterpart in the
+ * reference): a caller that allocates its state, bdys and fluxes arrays
+ * here gets the drop-in calls' column-chunk copies at the link's rate.  On
+ * the Grace hosts measured, the same copies from malloc'd memory pinned
+ * with sed_host_register ran 8-10x slower for multi-GB arrays.  *ptr is
+ * NULL on failure; free with sed_host_free. */
+int sed_host_alloc(size_t bytes, void **ptr);
+int sed_host_free(void *ptr);
 
 /* ------------------------------------------------------------------------
  * Launch tuning (no counterpart in the reference, whose solver has no

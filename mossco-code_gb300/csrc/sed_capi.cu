@@ -2341,6 +2341,31 @@ int sed_host_unregister(void* ptr) {
   return SED_OK;
 }
 
+int sed_host_alloc(size_t bytes, void** ptr) {
+  if (!ptr) return SED_E_ARG;
+  *ptr = nullptr;
+  if (!bytes) return SED_E_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return SED_E_NODEVICE;
+  }
+  cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocPortable);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *ptr = nullptr;
+    return SED_E_NOMEM;
+  }
+  return SED_OK;
+}
+
+int sed_host_free(void* ptr) {
+  if (!ptr) return SED_E_ARG;
+  cudaError_t e = cudaFreeHost(ptr);
+  if (e != cudaSuccess) { cudaGetLastError(); return SED_E_CUDA; }
+  return SED_OK;
+}
+
 const char* sed_error_string(int code) {
   switch (code) {
     case SED_OK: return "ok";

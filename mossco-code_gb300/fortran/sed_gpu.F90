@@ -205,6 +205,17 @@ module sed_gpu
       import :: c_int, c_ptr
       type(c_ptr), value :: ptr
     end function
+    !> pinned host memory for the state, bdys and fluxes arrays (c_f_pointer
+    !! gives the Fortran array); freed by sed_host_free
+    integer(c_int) function sed_host_alloc(bytes, ptr) bind(C, name='sed_host_alloc')
+      import :: c_int, c_ptr, c_size_t
+      integer(c_size_t), value :: bytes
+      type(c_ptr), intent(out) :: ptr
+    end function
+    integer(c_int) function sed_host_free(ptr) bind(C, name='sed_host_free')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ptr
+    end function
     !> one drop-in coupling step without a handle and without allocation
     integer(c_int) function sed_ode_solver_noalloc(p, inum, jnum, kmax, dz, dzc, phi, phi_i, &
         biofac, flux_cap, kact, conc, bdys, fluxes, dt, method, st) &
@@ -246,7 +257,8 @@ module sed_gpu
             sed_autotune, sed_set_boundary, sed_get_boundary, sed_spinup, &
             sed_get_min_dt, sed_get_min_dt_grid_cell, sed_set_column_bgc, sed_set_state, sed_get_state, &
             sed_step, sed_get_fluxes, sed_get_attempts, sed_get_budgets, sed_set_stream, &
-            sed_host_register, sed_host_unregister, sed_ode_solver_noalloc, &
+            sed_host_register, sed_host_unregister, sed_host_alloc, sed_host_free, &
+            sed_ode_solver_noalloc, &
             sed_error_string, sed_last_error, sed_tracer_name, sed_tracer_is_particulate, &
             sed_c_string
 

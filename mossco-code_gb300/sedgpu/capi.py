@@ -135,6 +135,8 @@ SIGNATURES = {
     "sed_set_stream": (ctypes.c_int, [_H, _vp]),
     "sed_host_register": (ctypes.c_int, [_vp, ctypes.c_size_t]),
     "sed_host_unregister": (ctypes.c_int, [_vp]),
+    "sed_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_vp)]),
+    "sed_host_free": (ctypes.c_int, [_vp]),
     "sed_get_tuning": (ctypes.c_int, [_H, ctypes.POINTER(SedTuning)]),
     "sed_set_tuning": (ctypes.c_int, [_H, ctypes.POINTER(SedTuning)]),
     "sed_autotune": (ctypes.c_int, [_H, ctypes.c_double, ctypes.c_int, ctypes.c_int,
@@ -472,3 +474,20 @@ def host_register(a: np.ndarray) -> None:
 
 def host_unregister(a: np.ndarray) -> None:
     load().sed_host_unregister(a.ctypes.data)
+
+
+def host_empty(shape, dtype=np.float64) -> np.ndarray:
+    """An uninitialised numpy array in pinned host memory (sed_host_alloc),
+    freed with sed_host_free when the array and its views are gone."""
+    import weakref
+    dt = np.dtype(dtype)
+    n = int(np.prod(shape)) * dt.itemsize
+    lib = load()
+    p = _vp()
+    rc = lib.sed_host_alloc(max(n, 1), ctypes.byref(p))
+    if rc != SED_OK:
+        raise SedError(rc, "sed_host_alloc")
+    buf = (ctypes.c_char * max(n, 1)).from_address(p.value)
+    a = np.frombuffer(buf, dtype=dt, count=int(np.prod(shape))).reshape(shape)
+    weakref.finalize(buf, lib.sed_host_free, ctypes.c_void_p(p.value))
+    return a

@@ -420,3 +420,26 @@ def test_min_dt_per_column(oracle_mod, cut):
         rc, sref, _ = oracle_mod.OracleModel(sub).run(c, nsteps=1, percol=True)
         assert rc == 0
         assert md[col] == sref["min_dt"], col
+
+
+def test_pinned_host_arrays_give_the_same_drop_in_result():
+    """The drop-in call on arrays from sed_host_alloc (pinned host memory)
+    equals the call on ordinary arrays, bit for bit."""
+    cs = synth.make_workload("plain_cpu_10x10")
+    out = []
+    for pinned in (False, True):
+        if pinned:
+            conc = capi.host_empty(cs.conc.shape)
+            conc[:] = cs.conc
+            fl = capi.host_empty(cs.fluxes.shape)
+            fl[:] = cs.fluxes
+        else:
+            conc = cs.conc.copy()
+            fl = cs.fluxes.copy()
+        s = capi.Solver(cs)
+        for _ in range(3):
+            s.ode_solver(conc, cs.bdys, fl, cs.dt)
+        s.close()
+        out.append((np.array(conc), np.array(fl)))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
