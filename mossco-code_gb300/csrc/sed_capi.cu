@@ -1725,31 +1725,37 @@ int sed_ode_solver_surrogate(sed_handle* h, sed_surrogate* s, double* conc, cons
                            cudaMemcpyHostToDevice, h->s_in), "conc chunk copy");
     CK(cudaEventRecord(h->pe_in[c], h->s_in), "event");
   }
+  // each chunk's work runs on a stream of its own, so the slow tail of one
+  // chunk's fallback columns shares the GPU with the next chunks' gates and
+  // fallbacks (the mma.sync network shares its activation buffers across
+  // chunks: then one stream for all)
+  auto cst = [&](int c) { return sur_uses_tc(s) ? h->s_cmp[c] : h->stream; };
+  for (int c = 0; c < nch; c++) CK(cudaStreamWaitEvent(cst(c), h->pe_start, 0), "wait");
   auto front = [&](int c) -> int {
     const int sl0 = bin.segb[c], sl1 = bin.segb[c + 1];
-    CK(cudaStreamWaitEvent(h->stream, h->pe_in[c], 0), "wait");
+    CK(cudaStreamWaitEvent(cst(c), h->pe_in[c], 0), "wait");
     if (sl1 == sl0) return SED_OK;
     CK(launch_gather_range<float>(stage, h->d_conc.as<float>(), h->d_slot_col.as<int>(), NTR,
-                                  h->kmax, h->ncol, h->nslot, sl0, sl1 - sl0, h->sms, h->stream),
+                                  h->kmax, h->ncol, h->nslot, sl0, sl1 - sl0, h->sms, cst(c)),
        "gather launch");
     h->launches++;
-    return sur_gate(P, c, sl0, sl1, h->stream);
+    return sur_gate(P, c, sl0, sl1, cst(c));
   };
   if ((rc = front(0))) return rc;
   for (int c = 0; c < nch; c++) {
     const int sl0 = bin.segb[c], sl1 = bin.segb[c + 1];
     const int nh = sl1 > sl0 ? sur_count(P, c) : 0;
     if (nh < 0) return SED_E_CUDA;
-    if (nh > 0 && (rc = sur_propose(P, c, sl0, nh, h->stream))) return rc;
+    if (nh > 0 && (rc = sur_propose(P, c, sl0, nh, cst(c)))) return rc;
     if (c + 1 < nch && (rc = front(c + 1))) return rc;
-    if (nh > 0 && (rc = sur_finish(P, c, sl0, nh, h->stream))) return rc;
+    if (nh > 0 && (rc = sur_finish(P, c, sl0, nh, cst(c)))) return rc;
     if (sl1 > sl0) {
       CK(launch_scatter_range<float>(h->d_conc.as<float>(), stage, h->d_slot_col.as<int>(),
                                      h->d_kact.as<int>(), NTR, h->kmax, h->ncol, h->nslot, sl0,
-                                     sl1 - sl0, h->sms, h->stream), "scatter launch");
+                                     sl1 - sl0, h->sms, cst(c)), "scatter launch");
       h->launches++;
     }
-    CK(cudaEventRecord(h->pe_cmp[c], h->stream), "event");
+    CK(cudaEventRecord(h->pe_cmp[c], cst(c)), "event");
     CK(cudaStreamWaitEvent(h->s_out, h->pe_cmp[c], 0), "wait");
     const int col0 = h->seg_col[c], col1 = h->seg_col[c + 1];
     const size_t width = (size_t)(col1 - col0) * sizeof(double);
