@@ -853,8 +853,9 @@ k_column(ColumnArgs<real> a, Params<real> p) {
         // their network input rows, from the staged (unchanged) state and
         // forcing: a thread owns features f, tid + nthr, ... and writes them
         // for every listed column of the tile (consecutive threads,
-        // consecutive features of a row); the logarithm is the hardware
-        // approximation, far below the BF16 rounding of the row
+        // consecutive features of a row); the full-accuracy FP32 logarithm
+        // and the IEEE quotient, so a row rounds to BF16 as the host's FP64
+        // features of the same state almost always do
         __syncthreads();
         const int n = s_hn, pin = a.pin, nin = a.nin, K = a.kmax;
         const int nstate = NTR * K;
@@ -864,7 +865,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
         unsigned short* x = a.xfeat + (size_t)s_hat * pin;
         for (int f = tid; f < pin; f += nthr) {
           const real* src = nullptr;
-          float add = 0.0f, m = 0.0f, isd = 0.0f;
+          float add = 0.0f, m = 0.0f, sdf = 1.0f;
           bool state = false;
           if (f < nstate) {
             const int tr = f / K, k = f - tr * K;
@@ -876,13 +877,13 @@ k_column(ColumnArgs<real> a, Params<real> p) {
           }
           if (src) {
             m = mu[f];
-            isd = 1.0f / sd[f];
+            sdf = sd[f];
           }
           for (int r = 0; r < n; r++) {
             float v = 0.0f;
             if (src) {
               const float c = (float)src[s_hcol[r]];
-              v = ((state ? __logf(fmaxf(c, 0.0f) + add) : c) - m) * isd;
+              v = __fdiv_rn((state ? logf(fmaxf(c, 0.0f) + add) : c) - m, sdf);
             }
             x[(size_t)r * pin + f] = __bfloat16_as_ushort(__float2bfloat16(v));
           }

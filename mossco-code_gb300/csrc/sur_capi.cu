@@ -165,6 +165,8 @@ int sed_sur_create(int nin, int nout, int hidden, int nhidden, int max_batch,
   s->max_batch = pad128(max_batch);
   auto bail = [&](int rc) { delete s; return rc; };
   if (cudaSetDevice(device) != cudaSuccess) return bail(SED_E_CUDA);
+  if (cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+    return bail(SED_E_CUDA);
   if (cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking) != cudaSuccess)
     return bail(SED_E_CUDA);
   s->stream = s->own_stream;
@@ -385,13 +387,20 @@ int sed_sur_train_step(sed_surrogate* s, const void* x_dev, const void* y_dev, i
   if (rc) return rc;
   if ((rc = backward(s, m, m))) return rc;
   s->step++;
+  // one Adam launch over every layer's weights and biases
+  sur::AdamSet set{};
+  long long at = 0;
   for (int l = 0; l < s->L; l++) {
-    const int nw = s->pout[l] * s->pin[l];
-    SCK(sur::adam(s->w[l], s->mw[l], s->vw[l], s->gw[l], nw, lr, 0.9f, 0.999f, 1e-8f, s->step,
-                  s->wb[l], s->wbt[l], s->pout[l], s->pin[l], s->stream), "adam w");
-    SCK(sur::adam(s->b[l], s->mb[l], s->vb[l], s->gb[l], s->pout[l], lr, 0.9f, 0.999f, 1e-8f,
-                  s->step, nullptr, nullptr, 1, s->pout[l], s->stream), "adam b");
+    set.seg[set.n] = {s->w[l], s->mw[l], s->vw[l], s->gw[l], s->wb[l], s->wbt[l], s->pout[l],
+                      s->pin[l]};
+    set.start[set.n++] = at;
+    at += (long long)s->pout[l] * s->pin[l];
+    set.seg[set.n] = {s->b[l], s->mb[l], s->vb[l], s->gb[l], nullptr, nullptr, 1, s->pout[l]};
+    set.start[set.n++] = at;
+    at += s->pout[l];
   }
+  set.start[set.n] = at;
+  SCK(sur::adam_all(set, lr, 0.9f, 0.999f, 1e-8f, s->step, s->sms, s->stream), "adam");
   if (loss) {
     SCK(cudaMemcpyAsync(loss, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->stream), "loss");
     SCK(cudaStreamSynchronize(s->stream), "train step");

@@ -18,6 +18,7 @@ inline int pad128(int x) { return (x + 127) / 128 * 128; }
 
 struct sed_surrogate {
   int device = 0;
+  int sms = 0;                        // the device's SM count
   cudaStream_t stream = nullptr;      // stream in use
   cudaStream_t own_stream = nullptr;  // stream created by the handle
   int nin = 0, nout = 0, hidden = 0, nhidden = 0, L = 0, max_batch = 0;

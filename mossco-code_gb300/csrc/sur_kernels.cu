@@ -186,25 +186,36 @@ __global__ void k_transpose_bf16(const __nv_bfloat16* __restrict__ in,
 }
 
 // MSE over the valid outputs: loss = sum mask (yhat - y)^2 / count,
-// dY = 2 (yhat - y) / count as bf16 (zero where masked)
+// dY = 2 (yhat - y) / count as bf16 (zero where masked).  Blocks walk rows,
+// threads the row's columns; the squares are reduced in the block and added
+// to the loss with one atomic per block.
 __global__ void k_mse(const float* __restrict__ yhat, const __nv_bfloat16* __restrict__ y,
                       const float* __restrict__ mask, int M, int N, int m_valid,
                       float inv_count, __nv_bfloat16* __restrict__ dy,
                       float* __restrict__ loss) {
+  __shared__ float red[32];
   float s = 0.0f;
-  const size_t total = (size_t)M * N;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const int col = (int)(i % N);
-    const int row = (int)(i / N);
-    const float w = row < m_valid ? mask[col] : 0.0f;
-    const float d = (yhat[i] - __bfloat162float(y[i])) * w;
-    s += d * d;
-    dy[i] = __float2bfloat16(2.0f * d * inv_count);
+  for (int row = blockIdx.x; row < M; row += gridDim.x) {
+    const size_t o = (size_t)row * N;
+    const bool valid = row < m_valid;
+    for (int col = threadIdx.x; col < N; col += blockDim.x) {
+      const float w = valid ? mask[col] : 0.0f;
+      const float d = (yhat[o + col] - __bfloat162float(y[o + col])) * w;
+      s += d * d;
+      dy[o + col] = __float2bfloat16(2.0f * d * inv_count);
+    }
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(loss, s * inv_count);
+  for (int k = 16; k > 0; k >>= 1) s += __shfl_xor_sync(0xffffffffu, s, k);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) red[warp] = s;
+  __syncthreads();
+  if (warp == 0) {
+    s = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0f;
+#pragma unroll
+    for (int k = 16; k > 0; k >>= 1) s += __shfl_xor_sync(0xffffffffu, s, k);
+    if (lane == 0) atomicAdd(loss, s * inv_count);
+  }
 }
 
 // db[n] = sum_m dZ[m][n]; dZ bf16 [M][N], in a fixed order so that training
@@ -239,25 +250,32 @@ __global__ void k_bias_sum(const float* __restrict__ part, int N, int nparts,
   db[n] = t;
 }
 
-// Adam on FP32 master weights; refreshes the BF16 copy W and its transpose.
-__global__ void k_adam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
-                       const float* __restrict__ g, int n, float lr, float b1, float b2,
-                       float eps, float c1, float c2, __nv_bfloat16* __restrict__ wb,
-                       __nv_bfloat16* __restrict__ wbt, int rows, int cols) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float gi = g[i];
-    const float mi = b1 * m[i] + (1.0f - b1) * gi;
-    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
-    m[i] = mi;
-    v[i] = vi;
-    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
-    w[i] = wi;
-    if (wb) {
+// Adam over several parameter arrays in one launch (every layer's weights
+// and biases) on FP32 master weights, refreshing the BF16 copies W and W^T:
+// element i of the concatenation belongs to the segment whose start is the
+// last one <= i.
+__global__ void k_adam_all(AdamSet set, float lr, float b1, float b2, float eps, float c1,
+                           float c2) {
+  const long long total = set.start[set.n];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    int q = 0;
+    while (q + 1 < set.n && i >= set.start[q + 1]) q++;
+    const AdamSeg& a = set.seg[q];
+    const int j = (int)(i - set.start[q]);
+    const float gi = a.g[j];
+    const float mi = b1 * a.m[j] + (1.0f - b1) * gi;
+    const float vi = b2 * a.v[j] + (1.0f - b2) * gi * gi;
+    a.m[j] = mi;
+    a.v[j] = vi;
+    const float wi = a.w[j] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    a.w[j] = wi;
+    if (a.wb) {
       const __nv_bfloat16 b = __float2bfloat16(wi);
-      wb[i] = b;
-      if (wbt) {
-        const int r = i / cols, c = i - r * cols;
-        wbt[(size_t)c * rows + r] = b;
+      a.wb[j] = b;
+      if (a.wbt) {
+        const int r = j / a.cols, c = j - r * a.cols;
+        a.wbt[(size_t)c * a.rows + r] = b;
       }
     }
   }
@@ -312,10 +330,8 @@ cudaError_t transpose_bf16(const __nv_bfloat16* in, __nv_bfloat16* out, int rows
 cudaError_t mse(const float* yhat, const __nv_bfloat16* y, const float* mask, int M, int N,
                 int m_valid, float inv_count, __nv_bfloat16* dy, float* loss,
                 cudaStream_t st) {
-  const size_t total = (size_t)M * N;
-  int blocks = (int)((total + 255) / 256);
-  if (blocks > 4096) blocks = 4096;
-  k_mse<<<blocks, 256, 0, st>>>(yhat, y, mask, M, N, m_valid, inv_count, dy, loss);
+  const int blocks = M < 1024 ? M : 1024;
+  k_mse<<<blocks, 128, 0, st>>>(yhat, y, mask, M, N, m_valid, inv_count, dy, loss);
   return cudaGetLastError();
 }
 
@@ -328,13 +344,14 @@ cudaError_t bias_grad(const __nv_bfloat16* dz, int M, int N, float* part, float*
 
 int bias_grad_parts() { return kBiasRowBlocks; }
 
-cudaError_t adam(float* w, float* m, float* v, const float* g, int n, float lr, float b1,
-                 float b2, float eps, int step, __nv_bfloat16* wb, __nv_bfloat16* wbt,
-                 int rows, int cols, cudaStream_t st) {
+cudaError_t adam_all(const AdamSet& set, float lr, float b1, float b2, float eps, int step,
+                     int sms, cudaStream_t st) {
+  if (set.n <= 0 || set.n > kAdamMaxSeg) return cudaErrorInvalidValue;
   const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
-  int blocks = (n + 255) / 256;
-  if (blocks > 1024) blocks = 1024;
-  k_adam<<<blocks, 256, 0, st>>>(w, m, v, g, n, lr, b1, b2, eps, c1, c2, wb, wbt, rows, cols);
+  const long long total = set.start[set.n];
+  long long blocks = (total + 255) / 256;
+  if (blocks > 4LL * sms) blocks = 4LL * sms;
+  k_adam_all<<<(int)(blocks > 0 ? blocks : 1), 256, 0, st>>>(set, lr, b1, b2, eps, c1, c2);
   return cudaGetLastError();
 }
 

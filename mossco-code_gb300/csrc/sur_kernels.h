@@ -22,9 +22,23 @@ cudaError_t mse(const float* yhat, const __nv_bfloat16* y, const float* mask, in
 cudaError_t bias_grad(const __nv_bfloat16* dz, int M, int N, float* part, float* db,
                       cudaStream_t st);
 int bias_grad_parts();
-cudaError_t adam(float* w, float* m, float* v, const float* g, int n, float lr, float b1,
-                 float b2, float eps, int step, __nv_bfloat16* wb, __nv_bfloat16* wbt,
-                 int rows, int cols, cudaStream_t st);
+// Adam over several parameter arrays in one launch: segment q is n = start[q+1]
+// - start[q] elements of w, m, v, g, with the BF16 copy wb (and its
+// transpose wbt, rows x cols) refreshed when wb is set
+constexpr int kAdamMaxSeg = 16;
+struct AdamSeg {
+  float *w, *m, *v;
+  const float* g;
+  __nv_bfloat16 *wb, *wbt;
+  int rows, cols;
+};
+struct AdamSet {
+  AdamSeg seg[kAdamMaxSeg];
+  long long start[kAdamMaxSeg + 1];
+  int n;
+};
+cudaError_t adam_all(const AdamSet& set, float lr, float b1, float b2, float eps, int step,
+                     int sms, cudaStream_t st);
 cudaError_t to_bf16(const float* w, int rows, int cols, __nv_bfloat16* wb,
                     __nv_bfloat16* wbt, cudaStream_t st);
 
