@@ -43,12 +43,20 @@ def active(cs, c):
     return c[:, K]
 
 
+def deep_grid():
+    """Columns of 20..100 active layers: every depth class, four layers per
+    lane in the deepest."""
+    return synth.make_columns(inum=40, jnum=1, kmin=20, kmax=100, total=0.3, land=0.1,
+                              poc="uniform", days=1, seed=3, name="deep40x100")
+
+
 @pytest.mark.parametrize("workload,cols", [
     ("plain_cpu_10x10", None),
     ("uneven_1024x1024", np.arange(0, 1024 * 1024, 3499)[:300]),
+    ("deep", None),
 ])
 def test_noalloc_matches_handle_two_calls(workload, cols):
-    cs = synth.make_workload(workload, cols=cols)
+    cs = deep_grid() if workload == "deep" else synth.make_workload(workload, cols=cols)
     params = capi.params_from(cs, capi.SED_FP32)
     ref_conc = cs.conc.copy()
     ref_fl = cs.fluxes.copy()
