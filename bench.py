@@ -1,9 +1,12 @@
 #!/usr/bin/env python3
 """Benchmark of the sediment-column hot path on GB300.
 
-Default workload: 256 x 256 columns, 30 layers, 11 OMEXDIA+P tracers,
-3600 s coupling steps, per-column adaptive Euler, FP32 state with FP64
-budgets (the GPU plain-solver configuration).  One bench "step" is one
+Default line (the headline): the surrogate step with its plain fallback
+against the plain solver on the 2048 x 2048 workload (30 % land, 30 layers,
+11 OMEXDIA+P tracers, 3600 s coupling steps, per-column adaptive Euler, FP32
+state), timed from simulated day 10 after the network is trained at its
+configured size.  ``--solver plain --workload NAME`` times the plain solver
+on another workload (e.g. plain_gpu_256x256).  One bench "step" is one
 coupling step of every column; the unit is column-steps/s (one active column
 advanced by one 3600 s coupling step, all its substeps included).
 
@@ -12,11 +15,12 @@ advanced by one 3600 s coupling step, all its substeps included).
 Prints one JSON line.  ``value`` is device throughput with the state
 resident in HBM (CUDA events around each step on the library's stream, L2
 flushed between steps); ``e2e`` is the same metric through the drop-in call
-sed_ode_solver on pinned FP64 host arrays, copies included; ``roofline`` is
-the column kernel against the measured HBM copy bandwidth;
-``cpu_baseline`` is the FP64 oracle on the host cores on a column sample.
-``--impl reference`` times the reference algorithm on the host CPU (the
-FP64 restatement; the Fortran reference cannot be built here).
+(sed_ode_solver_surrogate, or sed_ode_solver for the plain solver) on
+pinned FP64 host arrays, copies included; ``roofline`` is the plain column
+kernel against the measured HBM copy bandwidth; ``cpu_baseline`` is the
+FP64 oracle on the host cores on a column sample.  ``--impl reference``
+times the reference algorithm on the host CPU (the FP64 restatement; the
+Fortran reference cannot be built here).
 """
 from __future__ import annotations
 
