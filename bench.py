@@ -401,6 +401,8 @@ def run_headline(args) -> None:
         tot["ms_per_step"] = tot["device_ms"] / steps
         tot["surrogate_fraction"] = tot["surrogate_columns"] / max(tot["column_steps"], 1)
         tot["attempts_per_column_step"] = tot["attempts"] / max(tot["column_steps"], 1)
+        # substeps per column of the window's last step (power-of-two bins)
+        tot["attempt_histogram"] = [int(v) for v in s.attempt_histogram()]
         return tot
 
     plain = window(None)
@@ -538,6 +540,7 @@ def run_headline(args) -> None:
                    "tuning": {k: t_now[k] for k in ("tile_columns", "threads")}},
         "plain": {"value": plain["value"], "ms_per_step": plain["ms_per_step"],
                   "attempts_per_column_step": plain["attempts_per_column_step"],
+                  "attempt_histogram_last_step": plain["attempt_histogram"],
                   "gpu_launches": plain["gpu_launches"]},
         "speedup_vs_plain": head["value"] / plain["value"],
         "surrogate_fraction": head["surrogate_fraction"],

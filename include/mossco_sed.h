@@ -231,6 +231,14 @@ int sed_get_fluxes(sed_handle *h, double *fluxes);
 /* Per column of the last step: attempts [ncol] (0 on land). */
 int sed_get_attempts(sed_handle *h, int *attempts);
 
+/* Substep histogram of the last step (no counterpart in the reference,
+ * whose solver logs each cut): counts[SED_HIST_BINS] over the active
+ * columns, bin 0 the columns without an attempt (taken by the surrogate),
+ * bin b >= 1 those with 2^(b-1) <= attempts < 2^b, the last bin every
+ * count above.  Formed on the device from the per-column attempt counters. */
+#define SED_HIST_BINS 16
+int sed_get_attempt_histogram(sed_handle *h, long long *counts);
+
 /* Smallest accepted substep of every column in the last step, [ncol] (s;
  * 0 for land columns and columns without one): the per-column form of
  * type_rhs_driver's last_min_dt (solver_library.F90:130-136); the grid's

@@ -9,6 +9,7 @@
 // coupling step is a captured CUDA graph (queue reset + one persistent
 // kernel per depth class), replayed for every step.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -25,6 +26,16 @@
 #include "sed_params.h"
 #include "sur_internal.h"
 #include "sur_loop.h"
+
+// A named NVTX range over the rest of the enclosing scope: profilers (nsys,
+// ncu --nvtx) show every entry point's span on the timeline.  Without a
+// profiler attached the push and pop are a check of a function pointer.
+struct NvtxScope {
+  explicit NvtxScope(const char* name) { nvtxRangePushA(name); }
+  ~NvtxScope() { nvtxRangePop(); }
+  NvtxScope(const NvtxScope&) = delete;
+  NvtxScope& operator=(const NvtxScope&) = delete;
+};
 
 using namespace sed;
 
@@ -137,6 +148,7 @@ struct sed_handle {
       d_col_slot, d_top, d_bcin, d_mindt;
   // surrogate step: heavy-column slot list, its counter, hidden activations
   DevBuf d_list, d_gate, d_act;
+  DevBuf d_hist;  // [SED_HIST_BINS] attempts histogram
   std::vector<double> force64;  // host forcing rows (FP64 state)
   std::vector<double> rfac64;   // host rate factors (FP64 state)
   DevStats* h_stats = nullptr;  // pinned
@@ -1383,6 +1395,7 @@ int sed_set_forcing(sed_handle* h, const double* bdys, const double* fluxes) {
 }
 
 int sed_set_state(sed_handle* h, const double* conc) {
+  NvtxScope range("sed_set_state");
   if (!h) return SED_E_ARG;
   if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
   if (!conc) return h->fail(SED_E_ARG, "conc is required");
@@ -1394,6 +1407,7 @@ int sed_set_state(sed_handle* h, const double* conc) {
 }
 
 int sed_get_state(sed_handle* h, double* conc) {
+  NvtxScope range("sed_get_state");
   if (!h) return SED_E_ARG;
   if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");
   if (!conc) return h->fail(SED_E_ARG, "conc is required");
@@ -1405,6 +1419,7 @@ int sed_get_state(sed_handle* h, double* conc) {
 }
 
 int sed_step(sed_handle* h, double dt, int method, int nsteps, sed_stats* stats) {
+  NvtxScope range("sed_step");
   int rc = ready(h);
   if (rc) return rc;
   if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");
@@ -1425,6 +1440,7 @@ int sed_step(sed_handle* h, double dt, int method, int nsteps, sed_stats* stats)
 
 int sed_ode_solver(sed_handle* h, double* conc, const double* bdys, double* fluxes,
                    double dt, int method, sed_stats* stats) {
+  NvtxScope range("sed_ode_solver");
   int rc;
   if (!h) return SED_E_ARG;
   if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
@@ -1661,6 +1677,7 @@ static int sur_finish(SurPlan& P, int c, int sl0, int nh, cudaStream_t st) {
 
 int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, double tol,
                        double res_atol, sed_stats* stats) {
+  NvtxScope range("sed_step_surrogate");
   int rc = ready(h);
   if (rc) return rc;
   if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");
@@ -1697,6 +1714,7 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
 int sed_ode_solver_surrogate(sed_handle* h, sed_surrogate* s, double* conc, const double* bdys,
                              double* fluxes, double dt, double tol, double res_atol,
                              sed_stats* stats) {
+  NvtxScope range("sed_ode_solver_surrogate");
   // the call brings its own forcing (bdys, fluxes), as sed_ode_solver does
   int rc;
   if (!h) return SED_E_ARG;
@@ -1896,6 +1914,46 @@ int sed_get_attempts(sed_handle* h, int* attempts) {
   for (int c = 0; c < h->ncol; c++) attempts[c] = 0;
   for (int s = 0; s < h->nslot; s++)
     if (h->slot_col[s] >= 0) attempts[h->slot_col[s]] = tmp[s];
+  return SED_OK;
+}
+
+// Histogram of the last step's attempts over the active slots: bin 0 counts
+// the columns without an attempt (the surrogate's), bin b >= 1 those with
+// 2^(b-1) <= attempts < 2^b, the last bin every count above.  Block counts
+// in shared memory, one global atomic per bin and block.
+__global__ void k_attempt_hist(const int* __restrict__ nsub, const int* __restrict__ kact,
+                               int nslot, unsigned long long* __restrict__ hist) {
+  __shared__ unsigned int sh[SED_HIST_BINS];
+  for (int i = threadIdx.x; i < SED_HIST_BINS; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nslot; s += gridDim.x * blockDim.x) {
+    if (kact[s] <= 0) continue;
+    const int a = nsub[s];
+    const int b = a <= 0 ? 0 : min(32 - __clz(a), SED_HIST_BINS - 1);
+    atomicAdd(&sh[b], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < SED_HIST_BINS; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], (unsigned long long)sh[i]);
+}
+
+int sed_get_attempt_histogram(sed_handle* h, long long* counts) {
+  if (!h || !counts) return SED_E_ARG;
+  if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
+  CK(cudaSetDevice(h->device), "set device");
+  CK(h->d_hist.alloc(SED_HIST_BINS * sizeof(unsigned long long)), "histogram");
+  CK(cudaMemsetAsync(h->d_hist.p, 0, SED_HIST_BINS * sizeof(unsigned long long), h->stream),
+     "histogram reset");
+  const int blocks = std::max(1, std::min((h->nslot + 255) / 256, 4 * h->sms));
+  k_attempt_hist<<<blocks, 256, 0, h->stream>>>(h->d_nsub.as<int>(), h->d_kact.as<int>(),
+                                                h->nslot, h->d_hist.as<unsigned long long>());
+  CK(cudaGetLastError(), "histogram launch");
+  h->launches++;
+  unsigned long long tmp[SED_HIST_BINS];
+  CK(cudaMemcpyAsync(tmp, h->d_hist.p, sizeof tmp, cudaMemcpyDeviceToHost, h->stream),
+     "histogram copy");
+  CK(cudaStreamSynchronize(h->stream), "histogram");
+  for (int i = 0; i < SED_HIST_BINS; i++) counts[i] = (long long)tmp[i];
   return SED_OK;
 }
 
@@ -2123,6 +2181,7 @@ extern "C" {
 
 int sed_spinup(sed_handle* h, int mode, int column, const double* bdys1, const double* fluxes1,
                double dt, int method, long long nsteps, sed_stats* stats) {
+  NvtxScope range("sed_spinup");
   int rc;
   if (!h) return SED_E_ARG;
   if (!h->have_grid) return h->fail(SED_E_STATE, "sed_set_grid has not been called");
@@ -2323,6 +2382,7 @@ int sed_set_tuning(sed_handle* h, const sed_tuning* t) {
 }
 
 int sed_autotune(sed_handle* h, double dt, int method, int flags, sed_tuning* out) {
+  NvtxScope range("sed_autotune");
   int rc = ready(h);
   if (rc) return rc;
   if (!h->have_state) return h->fail(SED_E_STATE, "no state: call sed_set_state first");

@@ -17,6 +17,7 @@ module sed_gpu
 
   integer, parameter, public :: SED_NTR = 11
   integer, parameter, public :: SED_NBGC = 17
+  integer, parameter, public :: SED_HIST_BINS = 16, SED_KMAX_LIMIT = 127
   integer, parameter, public :: SED_OK = 0, SED_E_ARG = -1, SED_E_NAN = -2
   integer, parameter, public :: SED_E_SUBSTEP_CAP = -3, SED_E_CUDA = -4
   integer, parameter, public :: SED_E_STATE = -5, SED_E_NOMEM = -6
@@ -192,6 +193,14 @@ module sed_gpu
       import :: c_int, c_ptr
       type(c_ptr), value :: h, attempts
     end function
+    !> substep histogram of the last step: counts(SED_HIST_BINS), bin 0 no
+    !! attempt, bin b attempts in [2**(b-1), 2**b), the last bin all above
+    integer(c_int) function sed_get_attempt_histogram(h, counts) &
+        bind(C, name='sed_get_attempt_histogram')
+      import :: c_int, c_ptr, c_long_long
+      type(c_ptr), value :: h
+      integer(c_long_long), intent(out) :: counts(*)
+    end function
     integer(c_int) function sed_get_budgets(h, budgets) bind(C, name='sed_get_budgets')
       import :: c_int, c_ptr
       type(c_ptr), value :: h, budgets
@@ -258,6 +267,7 @@ module sed_gpu
             sed_get_min_dt, sed_get_min_dt_grid_cell, sed_set_column_bgc, sed_set_state, sed_get_state, &
             sed_step, sed_get_fluxes, sed_get_attempts, sed_get_budgets, sed_set_stream, &
             sed_host_register, sed_host_unregister, sed_host_alloc, sed_host_free, &
+            sed_get_attempt_histogram, &
             sed_ode_solver_noalloc, &
             sed_error_string, sed_last_error, sed_tracer_name, sed_tracer_is_particulate, &
             sed_c_string

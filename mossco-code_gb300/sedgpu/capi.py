@@ -23,6 +23,7 @@ SED_E_TOO_LARGE = -9
 SED_FP32, SED_FP64 = 0, 1
 SED_CUT_PER_COLUMN, SED_CUT_GLOBAL = 0, 1
 SED_KMAX_LIMIT = 127
+SED_HIST_BINS = 16
 
 
 class SedError(RuntimeError):
@@ -136,6 +137,7 @@ SIGNATURES = {
     "sed_host_register": (ctypes.c_int, [_vp, ctypes.c_size_t]),
     "sed_host_unregister": (ctypes.c_int, [_vp]),
     "sed_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_vp)]),
+    "sed_get_attempt_histogram": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_longlong)]),
     "sed_host_free": (ctypes.c_int, [_vp]),
     "sed_get_tuning": (ctypes.c_int, [_H, ctypes.POINTER(SedTuning)]),
     "sed_set_tuning": (ctypes.c_int, [_H, ctypes.POINTER(SedTuning)]),
@@ -442,6 +444,16 @@ class Solver:
         out = np.zeros(self.cs.ncol, dtype=np.int32)
         self._check(self.lib.sed_get_attempts(self.h, _p(out, _ip)),
                     "sed_get_attempts")
+        return out
+
+    def attempt_histogram(self) -> np.ndarray:
+        """Substep histogram of the last step (sed_get_attempt_histogram):
+        [SED_HIST_BINS] column counts, bin 0 without an attempt, bin b the
+        columns with 2^(b-1) <= attempts < 2^b, the last bin all above."""
+        out = np.zeros(SED_HIST_BINS, dtype=np.int64)
+        self._check(self.lib.sed_get_attempt_histogram(
+            self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))),
+            "sed_get_attempt_histogram")
         return out
 
     def min_dt(self) -> np.ndarray:

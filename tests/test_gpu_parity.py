@@ -443,3 +443,22 @@ def test_pinned_host_arrays_give_the_same_drop_in_result():
         out.append((np.array(conc), np.array(fl)))
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
+def test_attempt_histogram_counts_the_attempt_array():
+    """sed_get_attempt_histogram bins the last step's per-column attempts
+    (power-of-two bins, land and empty slots excluded) exactly as the
+    attempt array itself gives them, for uneven columns and land."""
+    cs = synth.make_workload("uneven_1024x1024", cols=np.arange(0, 1024 * 1024, 997)[:800])
+    s = capi.Solver(cs)
+    s.set_forcing()
+    s.set_state(cs.conc)
+    for _ in range(3):
+        s.step(4)
+        att = s.attempts()[cs.kact > 0]
+        bins = np.zeros(capi.SED_HIST_BINS, dtype=np.int64)
+        for a in att:
+            b = 0 if a <= 0 else min(int(a).bit_length(), capi.SED_HIST_BINS - 1)
+            bins[b] += 1
+        np.testing.assert_array_equal(s.attempt_histogram(), bins)
+    s.close()
