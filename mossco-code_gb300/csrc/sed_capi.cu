@@ -1628,22 +1628,30 @@ static int sur_count(SurPlan& P, int c) {
   return (int)n;
 }
 
-// 2. the network's proposal rows for the nh listed columns of chunk c (the
-//    gate wrote their input rows; the rows up to the next multiple of 128
-//    are cleared)
-static int sur_propose(SurPlan& P, int c, int sl0, int nh, cudaStream_t st) {
+// Whether the step runs without host round trips: the fused tcgen05 network
+// and the fallback kernel read the gate's count on the device.  The
+// mma.sync network needs the count on the host for its GEMM grids.
+static bool sur_device_count(const SurPlan& P) { return sur_uses_tc(P.s); }
+
+// 2. the network's proposal rows for the listed columns of chunk c (slots
+//    [sl0, sl1)): nh of them (host count; the rows up to the next multiple
+//    of 128 are cleared), or, with nh < 0, as many as the gate counted on
+//    the device (the fused kernel runs only the tiles holding them)
+static int sur_propose(SurPlan& P, int c, int sl0, int sl1, int nh, cudaStream_t st) {
   sed_handle* h = P.h;
   sed_surrogate* s = P.s;
-  const int rows = pad128(nh), r0 = P.row0(sl0, c);
+  const bool dev = nh < 0;
+  const int rows = pad128(dev ? sl1 - sl0 : nh), r0 = P.row0(sl0, c);
   bf16* x = h->d_xfeat.as<bf16>() + (size_t)r0 * s->pin[0];
   float* y = h->d_yhat.as<float>() + (size_t)r0 * s->pout[s->L - 1];
-  if (rows > nh)
+  if (!dev && rows > nh)
     CK(cudaMemsetAsync(x + (size_t)nh * s->pin[0], 0,
                        (size_t)(rows - nh) * s->pin[0] * sizeof(bf16), st),
        "padding rows");
   bf16* act0 = h->d_act.as<bf16>();
   bf16* act1 = act0 ? act0 + (size_t)h->d_act.bytes / sizeof(bf16) / 2 : nullptr;
-  int rc = sur_infer_rows(s, x, y, rows, act0, act1, st);
+  int rc = sur_infer_rows(s, x, y, rows, act0, act1, st,
+                          dev ? h->d_gate.as<unsigned>() + c : nullptr);
   if (rc) return h->fail(rc, "surrogate forward: %s", s->err.c_str());
   // one fused kernel, or one GEMM per layer
   h->launches += sur_uses_tc(s) ? 1 : s->L;
@@ -1652,15 +1660,17 @@ static int sur_propose(SurPlan& P, int c, int sl0, int nh, cudaStream_t st) {
 
 // 3. each listed column's proposal from its prediction row and its residual
 //    test; a column whose proposal passes takes it, the others take the
-//    plain adaptive step from their state, in the same kernel
-static int sur_finish(SurPlan& P, int c, int sl0, int nh, cudaStream_t st) {
+//    plain adaptive step from their state, in the same kernel (nh as for
+//    sur_propose)
+static int sur_finish(SurPlan& P, int c, int sl0, int sl1, int nh, cudaStream_t st) {
   sed_handle* h = P.h;
   sed_surrogate* s = P.s;
   const Bin& bin = P.bin();
   unsigned* cnt = h->d_gate.as<unsigned>();
   ColumnArgs<float> r = column_args<float>(h, bin, P.b, P.dt, SED_ADAPTIVE_EULER);
   r.list = h->d_list.as<int>() + (sl0 - bin.slot0);
-  r.ntiles = nh;
+  r.ntiles = nh < 0 ? sl1 - sl0 : nh;
+  r.nlist = nh < 0 ? cnt + c : nullptr;
   r.yhat = h->d_yhat.as<float>() + (size_t)P.row0(sl0, c) * s->pout[s->L - 1];
   r.ldy = s->pout[s->L - 1];
   r.norm = s->norm;
@@ -1691,11 +1701,14 @@ int sed_step_surrogate(sed_handle* h, sed_surrogate* s, double dt, int nsteps, d
   if (nsteps > 0 && (rc = ensure_pipeline(h))) return rc;
   for (int step = 0; step < nsteps; step++) {
     if ((rc = sur_gate(P, 0, sl0, sl1, h->stream))) return rc;
-    const int nh = sur_count(P, 0);
-    if (nh < 0) return SED_E_CUDA;
-    if (nh == 0) continue;
-    if ((rc = sur_propose(P, 0, sl0, nh, h->stream))) return rc;
-    if ((rc = sur_finish(P, 0, sl0, nh, h->stream))) return rc;
+    int nh = -1;  // counted on the device: no host round trip
+    if (!sur_device_count(P)) {
+      nh = sur_count(P, 0);
+      if (nh < 0) return SED_E_CUDA;
+      if (nh == 0) continue;
+    }
+    if ((rc = sur_propose(P, 0, sl0, sl1, nh, h->stream))) return rc;
+    if ((rc = sur_finish(P, 0, sl0, sl1, nh, h->stream))) return rc;
   }
   CK(cudaEventRecord(h->ev1, h->stream), "event");
   rc = stats_fetch(h, stats, l0, true);
@@ -1762,11 +1775,16 @@ int sed_ode_solver_surrogate(sed_handle* h, sed_surrogate* s, double* conc, cons
   if ((rc = front(0))) return rc;
   for (int c = 0; c < nch; c++) {
     const int sl0 = bin.segb[c], sl1 = bin.segb[c + 1];
-    const int nh = sl1 > sl0 ? sur_count(P, c) : 0;
-    if (nh < 0) return SED_E_CUDA;
-    if (nh > 0 && (rc = sur_propose(P, c, sl0, nh, cst(c)))) return rc;
+    // with the device count nothing waits on the host: every chunk's work
+    // is queued at once
+    int nh = 0;
+    if (sl1 > sl0) {
+      if (sur_device_count(P)) nh = -1;
+      else if ((nh = sur_count(P, c)) < 0) return SED_E_CUDA;
+    }
+    if (nh != 0 && (rc = sur_propose(P, c, sl0, sl1, nh, cst(c)))) return rc;
     if (c + 1 < nch && (rc = front(c + 1))) return rc;
-    if (nh > 0 && (rc = sur_finish(P, c, sl0, nh, cst(c)))) return rc;
+    if (nh != 0 && (rc = sur_finish(P, c, sl0, sl1, nh, cst(c)))) return rc;
     if (sl1 > sl0) {
       CK(launch_scatter_range<float>(h->d_conc.as<float>(), stage, h->d_slot_col.as<int>(),
                                      h->d_kact.as<int>(), NTR, h->kmax, h->ncol, h->nslot, sl0,

@@ -939,11 +939,16 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
   __syncthreads();
   const size_t ns = (size_t)a.nslot;
   real* sb = s_bnd[warp];
+  int ncols = a.ntiles;
+  if (a.list && a.nlist) {
+    const int n = (int)*a.nlist;
+    ncols = n < ncols ? n : ncols;
+  }
   for (;;) {
     int j = 0;
     if (lane == 0) j = (int)atomicAdd(a.queue, 1u);
     j = __shfl_sync(FULL, j, 0);
-    if (j >= a.ntiles) break;
+    if (j >= ncols) break;
     // the launch's j-th column: of a slot list (the surrogate step's heavy
     // columns), or of the slot range
     const int slot = a.list ? a.list[j] : a.slot0 + j;

@@ -48,6 +48,9 @@ struct ColumnArgs {
   const int* list;
   int* heavy;
   unsigned* nheavy;
+  // warp-direct kernel with a list: when set, the list's length on the
+  // device (the gate's count); the launch covers min(ntiles, *nlist) columns
+  const unsigned* nlist;
   // KIND_SUR: the network's prediction rows (row j for the list's j-th
   // column, pitch ldy) and its normalisation c0[11] | mu_x[nin] | sd_x[nin] |
   // mu_d[nout] | sd_d[nout]

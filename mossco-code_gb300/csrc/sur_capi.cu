@@ -68,11 +68,12 @@ int sur_check_tc(sed_surrogate* s) {
 }
 
 int sur_infer_rows(sed_surrogate* s, const bf16* x, float* y, int m, bf16* act0, bf16* act1,
-                   cudaStream_t st) {
+                   cudaStream_t st, const unsigned* nrows) {
   if (sur_uses_tc(s)) {
-    SCK(sur::infer_tc(s, x, y, m, s->d_err, st), "tensor-core inference");
+    SCK(sur::infer_tc(s, x, y, m, s->d_err, st, nrows), "tensor-core inference");
     return SED_OK;
   }
+  if (nrows) return s->fail(SED_E_ARG, "a device row count needs the fused tcgen05 kernel");
   const bf16* in = x;
   for (int l = 0; l < s->L; l++) {
     const bool last = l == s->L - 1;

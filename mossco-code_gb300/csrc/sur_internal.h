@@ -81,9 +81,11 @@ int sur_forward_rows(sed_surrogate* s, int m);
 // inference over m rows (a multiple of 128): x BF16 [m][pin[0]] -> y FP32
 // [m][pout[L-1]]: the fused tcgen05 kernel when s->use_tc and the shape
 // fits, else the mma.sync GEMMs with the hidden activations in act0 / act1
-// (BF16 [m][hidden padded]; unused by the fused kernel, may be null then)
+// (BF16 [m][hidden padded]; unused by the fused kernel, may be null then).
+// nrows (device, fused kernel only): run just the tiles of the first
+// min(m, *nrows) rows
 int sur_infer_rows(sed_surrogate* s, const bf16* x, float* y, int m, bf16* act0, bf16* act1,
-                   cudaStream_t st);
+                   cudaStream_t st, const unsigned* nrows = nullptr);
 // whether sur_infer_rows takes the fused tcgen05 kernel
 bool sur_uses_tc(const sed_surrogate* s);
 // the fused kernel's error flag: reset before, checked after a synchronised

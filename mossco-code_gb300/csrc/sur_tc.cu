@@ -197,7 +197,12 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
 // epilogue to have read region 0 (barrier lastepi).
 __global__ void __launch_bounds__(NTHREADS, 1)
 k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers P,
-         float* __restrict__ y, int ldy, int ntiles, int* err) {
+         float* __restrict__ y, int ldy, int maxtiles, const unsigned* __restrict__ nrows,
+         int* err) {
+  // the rows to run: all maxtiles tiles, or the tiles holding the first
+  // *nrows rows when the count lives on the device
+  const int ntiles =
+      nrows ? min(maxtiles, (int)((*nrows + (unsigned)BM - 1) / (unsigned)BM)) : maxtiles;
   extern __shared__ unsigned char smem_raw[];
   // 1024-byte alignment for the swizzle atoms
   unsigned char* smem = reinterpret_cast<unsigned char*>(
@@ -682,7 +687,7 @@ bool tc_supported(const sed_surrogate* s) {
 }
 
 cudaError_t infer_tc(sed_surrogate* s, const __nv_bfloat16* x, float* y, int m, int* err,
-                     cudaStream_t st) {
+                     cudaStream_t st, const unsigned* nrows) {
   if (m <= 0 || m % tc::BM || !tc_supported(s)) return cudaErrorInvalidValue;
   tc::Layers P{};
   P.L = s->L;
@@ -703,7 +708,8 @@ cudaError_t infer_tc(sed_surrogate* s, const __nv_bfloat16* x, float* y, int m, 
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int ntiles = m / tc::BM;
   const int grid = std::max(1, std::min(ntiles, sms));
-  tc::k_mlp_tc<<<grid, tc::NTHREADS, smem, st>>>(tx, P, y, s->pout[s->L - 1], ntiles, err);
+  tc::k_mlp_tc<<<grid, tc::NTHREADS, smem, st>>>(tx, P, y, s->pout[s->L - 1], ntiles, nrows,
+                                                  err);
   return cudaGetLastError();
 }
 

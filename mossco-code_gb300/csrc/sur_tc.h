@@ -14,10 +14,11 @@ namespace sur {
 // and the driver's tensor-map encoder is available.
 bool tc_supported(const sed_surrogate* s);
 // y[m][pout_last] (FP32) = the network on x[m][pin_0] (BF16), m a multiple
-// of 128.  *err (device) receives a nonzero code if the kernel gave up
-// waiting on one of its barriers (it then leaves y incomplete).
+// of 128; with nrows (device), only the 128-row tiles holding the first
+// min(m, *nrows) rows.  *err (device) receives a nonzero code if the kernel
+// gave up waiting on one of its barriers (it then leaves y incomplete).
 cudaError_t infer_tc(sed_surrogate* s, const __nv_bfloat16* x, float* y, int m, int* err,
-                     cudaStream_t st);
+                     cudaStream_t st, const unsigned* nrows = nullptr);
 
 // The training products on the tcgen05 tensor cores: C[M x N] = A[M x K] .
 // B[N x K]^T with the epilogues of sur_kernels.h (EPI_*), M and N multiples

@@ -65,6 +65,22 @@ def test_nothing_accepted_is_the_plain_step(trained):
     np.testing.assert_array_equal(out, plain)
 
 
+def test_gemm_engine_step_takes_the_host_count_path(trained):
+    """With the mma.sync network the step reads the gate's count on the host
+    (its GEMM grids need it): tol 0 is still the plain step bit for bit, and
+    a tolerance everything meets takes exactly the gated-out columns."""
+    sur, rep, grid, state = trained
+    plain, _, att = _one_step(grid, state)
+    sur.lib.sed_sur_set_tensor_cores(sur.h, 0)
+    try:
+        out, st, _ = _one_step(grid, state, sur, tol=0.0)
+        np.testing.assert_array_equal(out, plain)
+        _, st, _ = _one_step(grid, state, sur, tol=1e30)
+        assert st["surrogate_columns"] == int(np.sum((att > 1) & (grid.kact > 0)))
+    finally:
+        sur.lib.sed_sur_set_tensor_cores(sur.h, 1)
+
+
 def test_everything_accepted(trained):
     sur, rep, grid, state = trained
     plain, _, att = _one_step(grid, state)
