@@ -62,6 +62,22 @@ def test_bad_sizes_rejected_before_device(lib):
     assert lib.sed_create(None, 4, 4, 10, NTR, ctypes.byref(h)) == capi.SED_E_ARG
 
 
+def test_host_allocator_checks_its_arguments(lib):
+    """sed_host_alloc refuses a null result pointer or zero bytes, and
+    without a device it answers SED_E_NODEVICE with a null pointer."""
+    p = ctypes.c_void_p(123)
+    assert lib.sed_host_alloc(0, ctypes.byref(p)) == capi.SED_E_ARG
+    assert p.value is None
+    assert lib.sed_host_alloc(16, None) == capi.SED_E_ARG
+    assert lib.sed_host_free(None) == capi.SED_E_ARG
+    rc = lib.sed_host_alloc(16, ctypes.byref(p))
+    if rc == capi.SED_OK:       # a GPU is present: the memory is usable
+        assert p.value is not None
+        assert lib.sed_host_free(p) == capi.SED_OK
+    else:
+        assert rc == capi.SED_E_NODEVICE and p.value is None
+
+
 def test_synth_subset_is_counter_based():
     full = synth.make_workload("uneven_1024x1024", cols=np.arange(0, 5000))
     sub = synth.make_workload("uneven_1024x1024", cols=np.array([17, 4242, 999]))
