@@ -38,7 +38,10 @@ def unpack(params, shapes):
     return out
 
 
-def forward(params, shapes, x):
+def forward(params, shapes, x, bf16=False):
+    """Outputs, pre-activations and layer inputs.  bf16: each hidden
+    activation is rounded to BF16 where the GPU stores it (the products
+    themselves stay FP64)."""
     layers = unpack(np.asarray(params, dtype=np.float64), shapes)
     a = np.asarray(x, dtype=np.float64)
     zs, acts = [], [a]
@@ -47,18 +50,25 @@ def forward(params, shapes, x):
         zs.append(z)
         if i < len(layers) - 1:
             a = gelu(z)
+            if bf16:
+                a = bf16_round(a)
             acts.append(a)
         else:
             a = z
     return a, zs, acts
 
 
-def loss_and_grads(params, shapes, x, y):
-    yhat, zs, acts = forward(params, shapes, x)
+def loss_and_grads(params, shapes, x, y, bf16=False):
+    """MSE loss and the flat gradient.  bf16: the output gradient and each
+    back-propagated gradient are rounded to BF16 where the GPU stores them,
+    and the activations as in forward(bf16=True)."""
+    yhat, zs, acts = forward(params, shapes, x, bf16=bf16)
     m, nout = yhat.shape
     d = yhat - y
     loss = float(np.sum(d * d) / (m * nout))
     dz = 2.0 * d / (m * nout)
+    if bf16:
+        dz = bf16_round(dz)
     layers = unpack(np.asarray(params, dtype=np.float64), shapes)
     grads = [None] * len(layers)
     for i in range(len(layers) - 1, -1, -1):
@@ -68,6 +78,8 @@ def loss_and_grads(params, shapes, x, y):
         grads[i] = (gW, gb)
         if i > 0:
             dz = (dz @ W) * gelu_grad(zs[i - 1])
+            if bf16:
+                dz = bf16_round(dz)
     flat = np.concatenate([np.concatenate([g[0].ravel(), g[1]]) for g in grads])
     return loss, flat
 

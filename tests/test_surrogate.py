@@ -57,7 +57,10 @@ def _fp(a):
 def test_gpu_forward_and_gradients_match_fp64_reference(tc):
     """Forward pass and gradients of both engines: the tcgen05 GEMMs (TMA
     operands, TMEM accumulators, the weight gradient split over K) and the
-    mma.sync GEMMs."""
+    mma.sync GEMMs.  Against the FP64 MLP on the BF16-rounded operands the
+    bar is the BF16 storage of activations and gradients (5e-2); against the
+    FP64 MLP that also rounds those stores to BF16 it is the FP32
+    accumulation (1e-3 forward, 3e-3 per gradient block)."""
     lib, h = _sur(**SHAPE, batch=256)
     try:
         lib.sed_sur_set_tensor_cores(h, 1 if tc else 0)
@@ -83,23 +86,38 @@ def test_gpu_forward_and_gradients_match_fp64_reference(tc):
         xb = M.bf16_round(x)
         yb = M.bf16_round(y)
         yref, _, _ = M.forward(pb, shapes, xb)
+        yemu, _, _ = M.forward(pb, shapes, xb, bf16=True)
         yg = np.zeros((m, SHAPE["nout"]), dtype=np.float32)
         assert lib.sed_sur_forward(h, _fp(x), _fp(yg), m) == 0
         rel = np.linalg.norm(yg - yref) / np.linalg.norm(yref)
         assert rel < 1e-2, rel
+        # with the activations rounded to BF16 where the GPU stores them the
+        # reference leaves only the FP32 accumulation: far closer
+        rel_e = np.linalg.norm(yg - yemu) / np.linalg.norm(yemu)
+        assert rel_e < 1e-3, rel_e   # measured 1.8e-4 on GB300
         lref, gref = M.loss_and_grads(pb, shapes, xb, yb)
+        _, gemu = M.loss_and_grads(pb, shapes, xb, yb, bf16=True)
         g = np.zeros(n, dtype=np.float32)
         loss = np.zeros(1, dtype=np.float32)
         assert lib.sed_sur_grads(h, _fp(x), _fp(y), m, _fp(g), _fp(loss)) == 0
         assert abs(loss[0] - lref) < 2e-2 * lref
         o = 0
+        worst = 0.0
         for r, c in shapes:
             for blk in (slice(o, o + r * c), slice(o + r * c, o + r * c + r)):
                 a, b = g[blk].astype(np.float64), gref[blk]
                 relg = np.linalg.norm(a - b) / np.linalg.norm(b)
                 cos = a @ b / (np.linalg.norm(a) * np.linalg.norm(b))
                 assert relg < 5e-2 and cos > 0.998, (relg, cos)
+                # against the BF16-storage emulation
+                e = gemu[blk]
+                rel_g = np.linalg.norm(a - e) / np.linalg.norm(e)
+                worst = max(worst, rel_g)
+                # measured: at most 8.9e-4 over the blocks, both engines
+                assert rel_g < 3e-3 and a @ e / (np.linalg.norm(a) * np.linalg.norm(e)) > 0.99999, \
+                    rel_g
             o += r * c + r
+        print(f"forward vs emulation {rel_e:.2e}, worst gradient block {worst:.2e}")
     finally:
         lib.sed_sur_destroy(h)
 
