@@ -548,6 +548,10 @@ def run_headline(args) -> None:
         "accuracy": dict(acc, columns=int(len(cols)),
                          reference="FP64 device path (bit-identical to the FP64 CPU "
                                    "restatement), one coupling step from the same state",
+                         parity="stepper, transport, epilogue and boundary assembly pinned "
+                                "to the reference's source and solver test; the OMEXDIA+P "
+                                "rates are a restatement of the published model (FABM is not "
+                                "in the reference tree): parity of the rates unpinned",
                          floor="1e-4 x tracer max", sample="64 x 64 regular subsample"),
         "sweep": sweep,
         "training": training,
@@ -978,6 +982,8 @@ def run_gpu(args) -> None:
                     "columns": int(len(acc_cols)),
                     "reference": "FP64 device path (bit-identical to the FP64 CPU "
                                  "restatement), one coupling step from the same state",
+                    "parity": "OMEXDIA+P rates unpinned (a restatement of the published "
+                              "model; FABM is not in the reference tree)",
                     "floor": "1e-4 x tracer max"}
 
     # budgets of the last timed step
