@@ -747,7 +747,16 @@ int ensure_pipeline(sed_handle* h) {
   if (h->s_in) return SED_OK;
   CK(cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking), "stream");
   CK(cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking), "stream");
-  for (auto& st : h->s_cmp) CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
+  // chunk c's step stream has a higher priority than chunk c+1's (as far
+  // as the device's priority range goes): the block scheduler then finishes
+  // the chunks in order, so each chunk's copy back overlaps the steps of
+  // the later ones, which fill only the SMs the earlier chunks leave free
+  int least = 0, greatest = 0;
+  CK(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
+  for (int c = 0; c < kMaxSeg; c++)
+    CK(cudaStreamCreateWithPriority(&h->s_cmp[c], cudaStreamNonBlocking,
+                                    std::min(least, greatest + c)),
+       "stream");
   CK(cudaEventCreateWithFlags(&h->pe_start, cudaEventDisableTiming), "event");
   CK(cudaEventCreateWithFlags(&h->pe_done, cudaEventDisableTiming), "event");
   for (int c = 0; c < kMaxSeg; c++) {
