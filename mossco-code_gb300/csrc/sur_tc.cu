@@ -39,9 +39,11 @@ constexpr int STAGE = 2 * CHUNK;         // [256][64] weights: 32 KB
 constexpr int NST = 3;                   // weight ring stages
 constexpr int HID = 256;                 // hidden width (TMEM columns used)
 constexpr int TMEM_COLS = 512;
-constexpr int EPI_THREADS = 256;         // warps 0-7
-constexpr int PRODUCER = 8, MMA = 9;     // warps
-constexpr int NTHREADS = 320;
+constexpr int EPI_WARPS = 16;            // warps 0-15 run the epilogue
+constexpr int EPI_THREADS = 32 * EPI_WARPS;
+constexpr int ECOLS = BK / (EPI_WARPS / 4);  // columns of a 64-column chunk per warp
+constexpr int PRODUCER = EPI_WARPS, MMA = EPI_WARPS + 1;  // warps
+constexpr int NTHREADS = 32 * (EPI_WARPS + 2);
 constexpr long long WAIT_CYCLES = 2000000000ll;  // ~1 s at 2 GHz
 // shared memory after the weight ring: 2 NST + 9 barriers, then the biases
 constexpr int BAR_OFF = XBUF + NST * STAGE;
@@ -153,6 +155,26 @@ __device__ __forceinline__ void tmem_ld32_async(uint32_t taddr, uint32_t (&r)[32
         "=r"(r[31])
       : "r"(taddr));
 }
+// 16 consecutive FP32 columns of this thread's TMEM lane, issued without
+// waiting (the epilogue's half-width form of tmem_ld32_async)
+__device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait16(uint32_t (&r)[16]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                 "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                 "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+               :
+               : "memory");
+}
+
 // Wait for the thread's TMEM loads; the registers are operands, so no use
 // of them moves above the wait.
 __device__ __forceinline__ void tmem_wait(uint32_t (&r)[32]) {
@@ -168,13 +190,19 @@ __device__ __forceinline__ void tmem_wait(uint32_t (&r)[32]) {
 }
 
 // tanh form of GELU, 0.5 z (1 + tanh(k0 (z + k1 z^3))), with the hardware
-// tanh approximation: z2 = z z; u = z (k0 + k0 k1 z2); h = z / 2; h + h t
-__device__ __forceinline__ float gelu_fast(float z) {
-  const float w = fmaf(0.035677408136300125f, z * z, 0.7978845608028654f);
-  float t;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(z * w));
-  const float hz = 0.5f * z;
-  return fmaf(hz, t, hz);
+// tanh approximation: z2 = z z; u = z (k0 + k0 k1 z2); h = z / 2; h + h t.
+// A pair at a time in packed FP32x2 arithmetic (each component rounds as
+// the scalar operation would; the tanh stays scalar).
+__device__ __forceinline__ float2 gelu_fast2(float2 z) {
+  const float2 w = __ffma2_rn(make_float2(0.035677408136300125f, 0.035677408136300125f),
+                              __fmul2_rn(z, z),
+                              make_float2(0.7978845608028654f, 0.7978845608028654f));
+  const float2 u = __fmul2_rn(z, w);
+  float tx, ty;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(tx) : "f"(u.x));
+  asm("tanh.approx.f32 %0, %1;" : "=f"(ty) : "f"(u.y));
+  const float2 hz = __fmul2_rn(make_float2(0.5f, 0.5f), z);
+  return __ffma2_rn(hz, make_float2(tx, ty), hz);
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
@@ -182,10 +210,12 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   return *reinterpret_cast<uint32_t*>(&h);
 }
 
-// Roles of the 320 threads: warps 0-7 run the epilogue (warp w reads the
+// Roles of the 576 threads: warps 0-15 run the epilogue (warp w reads the
 // TMEM lanes 32 (w % 4) .. +31, one row per thread, and the columns
-// 32 (w / 4) .. +31 of every 64-column chunk), warp 8 issues the TMA loads,
-// warp 9 the MMAs.
+// 16 (w / 4) .. +15 of every 64-column chunk: four warps per lane quarter,
+// so each thread's chain of TMEM load, bias, GELU and store is short and
+// sixteen warps hide one another's latency), warp 16 issues the TMA loads,
+// warp 17 the MMAs.
 //
 // Overlap.  Hidden layer l accumulates in TMEM region l % 2 (columns
 // 256 (l % 2) .. +255), so layer l+1's MMAs run while the epilogue still
@@ -358,7 +388,7 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
       }
     }
   } else {
-    // ---- epilogue (warps 0-7)
+    // ---- epilogue (warps 0 .. EPI_WARPS-1)
     const int q = warp & 3, h = warp >> 2;
     const int row = q * 32 + lane;
     const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16);
@@ -377,47 +407,58 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
           // TMEM column of chunk kc: the output column for the last layer,
           // region l % 2 for a hidden one
           auto tcol = [&](int kc) {
-            const int c0 = n0 + kc * BK + 32 * h;
+            const int c0 = n0 + kc * BK + ECOLS * h;
             return is_last ? (uint32_t)c0 : (uint32_t)(HID * (l & 1) + c0);
           };
-          uint32_t ra[32], rb[32];
-          tmem_ld32_async(tl + tcol(0), ra);
-          tmem_wait(ra);
+          uint32_t ra[ECOLS], rb[ECOLS];
+          tmem_ld16_async(tl + tcol(0), ra);
+          tmem_wait16(ra);
 #pragma unroll
           for (int kc = 0; kc < HID / BK; kc++) {
             if (kc >= nchunk) break;
-            uint32_t(&cur)[32] = (kc & 1) ? rb : ra;
-            uint32_t(&nxt)[32] = (kc & 1) ? ra : rb;
+            uint32_t(&cur)[ECOLS] = (kc & 1) ? rb : ra;
+            uint32_t(&nxt)[ECOLS] = (kc & 1) ? ra : rb;
             // the next chunk's load runs while this one is processed
-            if (kc + 1 < nchunk) tmem_ld32_async(tl + tcol(kc + 1), nxt);
-            const int c0 = n0 + kc * BK + 32 * h;  // output column
-            float v[32];
+            if (kc + 1 < nchunk) tmem_ld16_async(tl + tcol(kc + 1), nxt);
+            const int c0 = n0 + kc * BK + ECOLS * h;  // output column
+            float v[ECOLS];
 #pragma unroll
-            for (int i = 0; i < 32; i++) v[i] = __uint_as_float(cur[i]) + bias[c0 + i];
+            for (int i = 0; i < ECOLS; i += 2) {
+              const float2 acc = make_float2(__uint_as_float(cur[i]), __uint_as_float(cur[i + 1]));
+              const float2 bb = *reinterpret_cast<const float2*>(bias + c0 + i);
+              const float2 sum = __fadd2_rn(acc, bb);
+              v[i] = sum.x;
+              v[i + 1] = sum.y;
+            }
             if (is_last) {
               float* dst = y + (size_t)(tile * BM + row) * ldy + c0;
 #pragma unroll
-              for (int i = 0; i < 32; i += 4)
+              for (int i = 0; i < ECOLS; i += 4)
                 *reinterpret_cast<float4*>(dst + i) =
                     make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
             } else {
               // BF16 GELU into chunk kc of the next layer's A operand: row
-              // `row`, 16-byte pieces 4h .. 4h+3 at (piece ^ row % 8)
+              // `row`, the warp's 16-byte pieces (ECOLS / 8) h + p at
+              // (piece ^ row % 8)
               unsigned char* rbase = xbuf + kc * CHUNK + row * 128;
 #pragma unroll
-              for (int p = 0; p < 4; p++) {
+              for (int p = 0; p < ECOLS / 8; p++) {
                 uint4 w;
-                w.x = pack_bf16(gelu_fast(v[8 * p + 0]), gelu_fast(v[8 * p + 1]));
-                w.y = pack_bf16(gelu_fast(v[8 * p + 2]), gelu_fast(v[8 * p + 3]));
-                w.z = pack_bf16(gelu_fast(v[8 * p + 4]), gelu_fast(v[8 * p + 5]));
-                w.w = pack_bf16(gelu_fast(v[8 * p + 6]), gelu_fast(v[8 * p + 7]));
-                *reinterpret_cast<uint4*>(rbase + (((4 * h + p) ^ (row & 7)) << 4)) = w;
+                const float2 g0 = gelu_fast2(make_float2(v[8 * p + 0], v[8 * p + 1]));
+                const float2 g1 = gelu_fast2(make_float2(v[8 * p + 2], v[8 * p + 3]));
+                const float2 g2 = gelu_fast2(make_float2(v[8 * p + 4], v[8 * p + 5]));
+                const float2 g3 = gelu_fast2(make_float2(v[8 * p + 6], v[8 * p + 7]));
+                w.x = pack_bf16(g0.x, g0.y);
+                w.y = pack_bf16(g1.x, g1.y);
+                w.z = pack_bf16(g2.x, g2.y);
+                w.w = pack_bf16(g3.x, g3.y);
+                *reinterpret_cast<uint4*>(rbase + ((((ECOLS / 8) * h + p) ^ (row & 7)) << 4)) = w;
               }
               fence_before();
               asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
               mbar_arrive(b_actc + 8 * kc);
             }
-            if (kc + 1 < nchunk) tmem_wait(nxt);
+            if (kc + 1 < nchunk) tmem_wait16(nxt);
           }
           if (is_last && n0 == 0) {
             // region 0 read: the next tile's first layer may start
