@@ -5,7 +5,8 @@
 // framework owns the GPU's memory pool and forbids other allocators, or a
 // call site that cannot keep a solver handle (and the buffers it allocates)
 // alive between calls.  This entry point runs the tile form of the column
-// kernel (k_column: 32- or 16-column tiles, 256 threads), with every device
+// kernel (k_column: 32-, 16- or 8-column tiles for columns of up to 31, 63
+// or 127 layers, 256 threads), with every device
 // buffer it needs -- the staging of the caller's FP64 arrays, the FP32 state,
 // coefficients and forcing, the tile work counter and the step statistics --
 // in one file-scope __device__ array of SED_NOALLOC_SCRATCH_BYTES.  Every GPU
