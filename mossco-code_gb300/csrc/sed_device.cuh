@@ -25,6 +25,7 @@ constexpr int NDISS = 5;   // tracers 6..10 are dissolved
 constexpr int NCOEF = 4;   // FP32 per-layer coefficient rows: phi, vol, gb, gm
 constexpr int NCOEF64 = 6; // FP64 rows: phi, phi_i, biofac, dz, len, mol
 constexpr int NFORCE = 13; // per-column forcing rows: bioT, dmul, bnd[11]
+constexpr int SURF_ROW = 12; // premultiplied surface row: NTR reals, padded to 8 bytes
 constexpr unsigned FULL = 0xffffffffu;
 
 enum : int { ST_NAN = 1, ST_CAP = 2, ST_ARG = 4 };
@@ -187,12 +188,15 @@ __device__ __forceinline__ void omexdia_p(const Params<real>& p,
   const real Rads = sdiv(p.pads * fm(p.PAdsODU, PO4, -(ODU * adsP)), d67.y);
   const real NprodF = NprodFS.x, NprodS = NprodFS.y;
   const real Pprod = p.rF * fdetP;
-  const float2 rC = __fmul2_rn(make_float2(lim, lim), CprodFS);
-  const float2 rN = __fmul2_rn(make_float2(lim, lim), NprodFS);
-  r[T_FDETC] = -rC.x;
-  r[T_SDETC] = -rC.y;
-  r[T_FDETN] = -rN.x;
-  r[T_SDETN] = -rN.y;
+  // detritus decay -(lim prod) as (-lim) prod: the same values, one sign
+  // flip instead of one per packed component
+  const real nlim = -lim;
+  const float2 rC = __fmul2_rn(make_float2(nlim, nlim), CprodFS);
+  const float2 rN = __fmul2_rn(make_float2(nlim, nlim), NprodFS);
+  r[T_FDETC] = rC.x;
+  r[T_SDETC] = rC.y;
+  r[T_FDETN] = rN.x;
+  r[T_SDETN] = rN.y;
   r[T_FDETP] = -(lim * Pprod);
   r[T_ADSP] = Rads;
   r[T_O2] = fm(real(-2), Nitri, -OxicMin) - OduOx;
@@ -254,6 +258,21 @@ struct Lane {
   // alpha_d = beta = ad0 (concentration condition, ad0 the dissolved
   // surface conductance), alpha_d = 1, beta = 0 (flux), or both 0 (none)
   real alpha_p, alpha_d, beta;
+  // FP32 form: alpha b of every tracer, multiplied once per column and
+  // read by the right-hand sides from shared memory (a 32-bit shared
+  // address): lane 0 reads its warp's row (SURF_ROW floats, 8-byte aligned,
+  // so a tracer pair is one 64-bit load), every other lane a row of zeros
+  unsigned ab_sa;
+  __device__ __forceinline__ float ab(int n) const {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(ab_sa + 4u * n));
+    return v;
+  }
+  __device__ __forceinline__ float2 ab2(int n) const {
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(ab_sa + 4u * n));
+    return v;
+  }
   // FP64 reference-order path (diff3d's own operands)
   real dz[LPL], len[LPL], Dp[LPL], Dd[LPL];
   real ext_a[BC4 ? LPL : 1][BC4 ? NPART : 1];  // cascade additions in the loop
@@ -311,7 +330,7 @@ __device__ __forceinline__ void bio3_conductances(const Params<real>& p,
 // on lane 0 (a = 0 there), then dC = (F - F_below) / (phi dz).  Branch- and
 // select-free: lanes past the column hold zero state and conductances; the
 // no-flux bottom drops F_below at K-1 by the zero conductance below it.
-template <int LPL, bool BC4, bool PART>
+template <int LPL, bool BC4, bool PART, bool PRE>
 __device__ __forceinline__ void transport_one(const Lane<float, LPL, BC4>& lc, int n,
                                               const float (&a)[LPL], float alpha, float beta,
                                               int lane, const float (&C)[LPL][NTR],
@@ -320,7 +339,7 @@ __device__ __forceinline__ void transport_one(const Lane<float, LPL, BC4>& lc, i
 #pragma unroll
   for (int s = 0; s < LPL; s++) v[s] = PART ? lc.phi[s] * C[s][n] : C[s][n];
   from_above<float, LPL>(v, vm, lane);
-  const float ab = alpha * lc.bnd(n);
+  const float ab = PRE ? lc.ab(n) : alpha * lc.bnd(n);
   const float top = PART ? ab : fm(-beta, v[0], ab);
 #pragma unroll
   for (int s = 0; s < LPL; s++) F[s] = s == 0 ? fm(a[s], vm[s] - v[s], top) : a[s] * (vm[s] - v[s]);
@@ -336,13 +355,18 @@ __device__ __forceinline__ void transport_one(const Lane<float, LPL, BC4>& lc, i
   }
 }
 
-__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 __device__ __forceinline__ float2 splat(float a) { return make_float2(a, a); }
+// a - b per component as one packed FMA, b (-1) + a: the product is exact,
+// so each component rounds once, exactly as the subtraction does (signed
+// zeros included), and no separate sign flip of b is issued.
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+}
 
 // transport_one for tracers n and n+1 of one class at once: the same
 // operations in packed FP32x2 arithmetic (each component rounds as the
 // scalar operation does), halving the arithmetic instructions.
-template <int LPL, bool BC4, bool PART>
+template <int LPL, bool BC4, bool PART, bool PRE>
 __device__ __forceinline__ void transport_pair(const Lane<float, LPL, BC4>& lc, int n,
                                                const float (&a)[LPL], float alpha, float beta,
                                                int lane, const float (&C)[LPL][NTR],
@@ -358,11 +382,14 @@ __device__ __forceinline__ void transport_pair(const Lane<float, LPL, BC4>& lc, 
   }
   from_above<float, LPL>(vx, mx, lane);
   from_above<float, LPL>(vy, my, lane);
-  const float2 ab = __fmul2_rn(splat(alpha), make_float2(lc.bnd(n), lc.bnd(n + 1)));
+  // alpha b: the column's premultiplied pair (n even: one 64-bit load), or
+  // formed here when alpha changes between right-hand sides
+  const float2 ab = PRE ? lc.ab2(n)
+                        : __fmul2_rn(splat(alpha), make_float2(lc.bnd(n), lc.bnd(n + 1)));
   const float2 top = PART ? ab : __ffma2_rn(splat(-beta), v[0], ab);
 #pragma unroll
   for (int s = 0; s < LPL; s++) {
-    const float2 d = __fadd2_rn(make_float2(mx[s], my[s]), neg2(v[s]));
+    const float2 d = sub2(make_float2(mx[s], my[s]), v[s]);
     F[s] = s == 0 ? __ffma2_rn(splat(a[s]), d, top) : __fmul2_rn(splat(a[s]), d);
   }
   ftop[n] = F[0].x;
@@ -374,7 +401,7 @@ __device__ __forceinline__ void transport_pair(const Lane<float, LPL, BC4>& lc, 
   from_below<float, LPL>(fy, by, lane);
 #pragma unroll
   for (int s = 0; s < LPL; s++) {
-    const float2 div = __fadd2_rn(F[s], neg2(make_float2(bx[s], by[s])));
+    const float2 div = sub2(F[s], make_float2(bx[s], by[s]));
     float2 r = make_float2(R[s][n], R[s][n + 1]);
     if (BC4 && PART)
       r = __fadd2_rn(r, __ffma2_rn(div, splat(lc.ivol[s]),
@@ -418,13 +445,16 @@ __device__ __forceinline__ void column_rhs(const Params<real>& p,
 #pragma unroll
   for (int s = 0; s < LPL; s++) omexdia_p<real>(p, C[s], R[s], dn[s]);
   // tracer pairs of one class in packed FP32x2 arithmetic, tracer 10 alone
+  // alpha b from the column's premultiplied row, except for dissolved
+  // tracers under profile 3, whose alpha may follow this rhs's conductance
   const real alpha_p = lc.alpha_p;
-  transport_pair<LPL, BC4, true>(lc, 0, apv, alpha_p, 0.0f, lane, C, R, ftop);
-  transport_pair<LPL, BC4, true>(lc, 2, apv, alpha_p, 0.0f, lane, C, R, ftop);
-  transport_pair<LPL, BC4, true>(lc, 4, apv, alpha_p, 0.0f, lane, C, R, ftop);
-  transport_pair<LPL, BC4, false>(lc, 6, adv, alpha_d, beta, lane, C, R, ftop);
-  transport_pair<LPL, BC4, false>(lc, 8, adv, alpha_d, beta, lane, C, R, ftop);
-  transport_one<LPL, BC4, false>(lc, NTR - 1, adv, alpha_d, beta, lane, C, R, ftop);
+  constexpr bool PRE_D = !BIO3;
+  transport_pair<LPL, BC4, true, true>(lc, 0, apv, alpha_p, 0.0f, lane, C, R, ftop);
+  transport_pair<LPL, BC4, true, true>(lc, 2, apv, alpha_p, 0.0f, lane, C, R, ftop);
+  transport_pair<LPL, BC4, true, true>(lc, 4, apv, alpha_p, 0.0f, lane, C, R, ftop);
+  transport_pair<LPL, BC4, false, PRE_D>(lc, 6, adv, alpha_d, beta, lane, C, R, ftop);
+  transport_pair<LPL, BC4, false, PRE_D>(lc, 8, adv, alpha_d, beta, lane, C, R, ftop);
+  transport_one<LPL, BC4, false, PRE_D>(lc, NTR - 1, adv, alpha_d, beta, lane, C, R, ftop);
 }
 
 // ---------------------------------------------------------------------------

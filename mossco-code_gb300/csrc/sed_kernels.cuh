@@ -218,6 +218,30 @@ __device__ __forceinline__ void load_lane(Lane<real, LPL, BC4>& lc,
   }
 }
 
+// A block's surface rows (FP32 form): warp w's alpha b row at w SURF_ROW,
+// the zero row at SURF_ZERO.  The zero row starts in bank 2 of 32, so a
+// load of one tracer pair by lane 0 (its warp's row) and by the other lanes
+// (the zero row) touches disjoint banks for every warp of a 256-thread block.
+constexpr int SURF_ZERO = 8 * SURF_ROW + 2;
+constexpr int SURF_FLOATS = SURF_ZERO + SURF_ROW;
+
+// The column's alpha b row, formed once per column by lane 0 with the same
+// rounding as the product it replaces, and read by every right-hand side.
+template <typename real, int LPL, bool BC4>
+__device__ __forceinline__ void set_surface_row(Lane<real, LPL, BC4>& lc, float* s_surf,
+                                                int warp, int lane) {
+  if constexpr (std::is_same<real, float>::value) {
+    float* row = s_surf + warp * SURF_ROW;
+    __syncwarp();  // the previous column's right-hand sides are done with the row
+    if (lane == 0) {
+#pragma unroll
+      for (int n = 0; n < NTR; n++) row[n] = (n < NPART ? lc.alpha_p : lc.alpha_d) * lc.bnd(n);
+    }
+    __syncwarp();
+    lc.ab_sa = (unsigned)__cvta_generic_to_shared(lane == 0 ? row : s_surf + SURF_ZERO);
+  }
+}
+
 // The right-hand side used by the steppers: folded FP32 form, or the
 // reference-order FP64 form.
 template <typename real, int LPL, bool BC4, bool BIO3>
@@ -324,10 +348,9 @@ struct CompSum2 {
   __device__ __forceinline__ void zero() { s = make_float2(0.0f, 0.0f); c = s; }
   __device__ __forceinline__ void add(float2 x) {
     const float2 t = __fadd2_rn(s, x);
-    const float2 bp = __fadd2_rn(t, make_float2(-s.x, -s.y));
-    const float2 tb = __fadd2_rn(t, make_float2(-bp.x, -bp.y));
-    const float2 e = __fadd2_rn(__fadd2_rn(s, make_float2(-tb.x, -tb.y)),
-                                __fadd2_rn(x, make_float2(-bp.x, -bp.y)));
+    const float2 bp = sub2(t, s);
+    const float2 tb = sub2(t, bp);
+    const float2 e = __fadd2_rn(sub2(s, tb), sub2(x, bp));
     c = __fadd2_rn(c, e);
     s = t;
   }
@@ -704,6 +727,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
   __shared__ unsigned s_hat;        // and their first list entry
   __shared__ unsigned long long b_att, b_acc, b_cols, b_mindt;
   __shared__ int b_maxatt, b_cap, b_nan;
+  __shared__ __align__(16) float s_surf[SURF_FLOATS];
 
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lane = tid & 31;
@@ -711,6 +735,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
     b_att = 0; b_acc = 0; b_cols = 0; b_mindt = 0x7FF0000000000000ull;
     b_maxatt = 0; b_cap = 0; b_nan = 0;
   }
+  if (tid < SURF_ROW) s_surf[SURF_ZERO + tid] = 0.0f;
   const size_t ns = (size_t)a.nslot;
 
   for (;;) {
@@ -753,6 +778,7 @@ k_column(ColumnArgs<real> a, Params<real> p) {
       real C[LPL][NTR];
       load_lane<real, LPL, BC4, BIO3>(lc, C, s_conc, s_coef, s_cap, s_force, j, KT,
                                       tcp, lane, K, p.mol_mode, p.bcup_d);
+      set_surface_row(lc, s_surf, tid >> 5, lane);
       real ftop[NTR];
 #pragma unroll
       for (int n = 0; n < NTR; n++) ftop[n] = real(0);
@@ -929,6 +955,7 @@ template <typename real, int LPL, bool BC4, bool BIO3, int KIND, bool MULTI, boo
 __global__ void __launch_bounds__(256, (MinBlocks<real, LPL>::value))
 k_column_warp(ColumnArgs<real> a, Params<real> p) {
   __shared__ real s_bnd[8][NFORCE];
+  __shared__ __align__(16) float s_surf[SURF_FLOATS];
   __shared__ unsigned long long b_att, b_acc, b_cols, b_mindt, b_sur;
   __shared__ int b_maxatt, b_cap, b_nan;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -936,6 +963,7 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
     b_att = 0; b_acc = 0; b_cols = 0; b_sur = 0; b_mindt = 0x7FF0000000000000ull;
     b_maxatt = 0; b_cap = 0; b_nan = 0;
   }
+  if (tid < SURF_ROW) s_surf[SURF_ZERO + tid] = 0.0f;
   __syncthreads();
   const size_t ns = (size_t)a.nslot;
   real* sb = s_bnd[warp];
@@ -975,6 +1003,7 @@ k_column_warp(ColumnArgs<real> a, Params<real> p) {
                                     (int)ns, lane, K, p.mol_mode, p.bcup_d);
     lc.bnd_s = sb + 2;
     lc.bnd_stride = 1;
+    set_surface_row(lc, s_surf, warp, lane);
     Params<real> pc = p;
     if (ENS) load_bgc(pc, a.bgc, ns, slot);
     real ftop[NTR];
