@@ -48,16 +48,16 @@ NTR, NCOEF, NFORCE, NDISS = 11, 4, 13, 5
 L2_BYTES = 129 * 1024 * 1024
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the hot
 # kernel, from an ncu --set full capture of the launch at day 10 of the run
-# (surrogate_2048x2048: the capture of 183,315 active columns, 3,251 B per
+# (surrogate_2048x2048: the capture of 183,315 active columns, 3,271 B per
 # column-step, scaled to the grid's 2,936,778)
 MEASURED_TRAFFIC = {"plain_gpu_256x256": 168.4e6,
-                    "surrogate_2048x2048": 3251.0 * 2936778}
+                    "surrogate_2048x2048": 3271.0 * 2936778}
 # ncu counters of the hot kernel in the headline's window (day 10), from
 # the committed profile summary profiles/k_column_warp_surrogate_2048x2048_day10.md
 NCU_KERNEL = {"surrogate_2048x2048": {
-    "issue_active": 0.830, "fp32_pipe": 0.555, "alu_pipe": 0.438, "lsu_pipe": 0.337,
-    "warps_active": 0.369, "warp_instructions_per_attempt": 231,
-    "traffic_per_column_step": 3251, "bound": "instruction issue",
+    "issue_active": 0.809, "fp32_pipe": 0.560, "alu_pipe": 0.365, "lsu_pipe": 0.420,
+    "warps_active": 0.372, "warp_instructions_per_attempt": 227,
+    "traffic_per_column_step": 3271, "bound": "instruction issue",
     "capture": "ncu --set full, 183,315 active columns at day 10, budgets on"}}
 # the same for one Run of the pelagic kernel (the first timed Run)
 PEL_TRAFFIC = {"pelagic_1024x1024": 1384.8e6}
