@@ -53,7 +53,8 @@ L2_BYTES = 129 * 1024 * 1024
 MEASURED_TRAFFIC = {"plain_gpu_256x256": 168.4e6,
                     "surrogate_2048x2048": 3271.0 * 2936778}
 # ncu counters of the hot kernel in the headline's window (day 10), from
-# the committed profile summary profiles/k_column_warp_surrogate_2048x2048_day10.md
+# an ncu --set full capture of one launch on the grid's first 262,144
+# columns (python -m sedgpu.profcase plain --columns 262144 --day 10)
 NCU_KERNEL = {"surrogate_2048x2048": {
     "issue_active": 0.809, "fp32_pipe": 0.560, "alu_pipe": 0.365, "lsu_pipe": 0.420,
     "warps_active": 0.372, "warp_instructions_per_attempt": 227,
