@@ -388,7 +388,7 @@ int sed_sur_set_state(sed_surrogate *s, const float *state, long long step);
 /* host rows x[m][nin] -> y[m][nout] */
 int sed_sur_forward(sed_surrogate *s, const float *x, float *y, int m);
 /* device rows: x BF16 [m][pad128(nin)] -> y FP32 [m][pad128(nout)],
- * m a multiple of 128 */
+ * m a multiple of 128, both arrays 16-byte aligned (else SED_E_ARG) */
 int sed_sur_forward_device(sed_surrogate *s, const void *x_dev, void *y_dev,
                            int m);
 /* one Adam step on a device batch (x BF16 [m][pad128(nin)], y BF16

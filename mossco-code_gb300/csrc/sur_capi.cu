@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -348,6 +349,9 @@ int sed_sur_forward(sed_surrogate* s, const float* x, float* y, int m) {
 // group; larger m is processed in chunks).
 int sed_sur_forward_device(sed_surrogate* s, const void* x_dev, void* y_dev, int m) {
   if (!s || !x_dev || !y_dev || m <= 0 || m % 128) return SED_E_ARG;
+  // the rows are read by TMA and written in 16-byte pieces
+  if (reinterpret_cast<uintptr_t>(x_dev) % 16 || reinterpret_cast<uintptr_t>(y_dev) % 16)
+    return SED_E_ARG;
   SCK(cudaSetDevice(s->device), "set device");
   if (sur_uses_tc(s)) {
     // the fused kernel reads and writes the caller's rows directly

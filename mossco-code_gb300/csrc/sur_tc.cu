@@ -205,6 +205,14 @@ __device__ __forceinline__ float2 gelu_fast2(float2 z) {
   return __ffma2_rn(hz, make_float2(tx, ty), hz);
 }
 
+// Eight FP32 values to a 32-byte aligned global address in one 256-bit
+// store.
+__device__ __forceinline__ void st_global_v8(float* p, const float* v) {
+  asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(v[0]),
+               "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
+               : "memory");
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<uint32_t*>(&h);
@@ -227,8 +235,8 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
 // epilogue to have read region 0 (barrier lastepi).
 __global__ void __launch_bounds__(NTHREADS, 1)
 k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers P,
-         float* __restrict__ y, int ldy, int maxtiles, const unsigned* __restrict__ nrows,
-         int* err) {
+         float* __restrict__ y, int ldy, bool y32, int maxtiles,
+         const unsigned* __restrict__ nrows, int* err) {
   // the rows to run: all maxtiles tiles, or the tiles holding the first
   // *nrows rows when the count lives on the device
   const int ntiles =
@@ -432,10 +440,17 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
             }
             if (is_last) {
               float* dst = y + (size_t)(tile * BM + row) * ldy + c0;
+              if (y32) {
+                // 32-byte row pieces: half the store instructions, each
+                // a whole sector of its row
 #pragma unroll
-              for (int i = 0; i < ECOLS; i += 4)
-                *reinterpret_cast<float4*>(dst + i) =
-                    make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                for (int i = 0; i < ECOLS; i += 8) st_global_v8(dst + i, v + i);
+              } else {
+#pragma unroll
+                for (int i = 0; i < ECOLS; i += 4)
+                  *reinterpret_cast<float4*>(dst + i) =
+                      make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+              }
             } else {
               // BF16 GELU into chunk kc of the next layer's A operand: row
               // `row`, the warp's 16-byte pieces (ECOLS / 8) h + p at
@@ -729,7 +744,11 @@ bool tc_supported(const sed_surrogate* s) {
 
 cudaError_t infer_tc(sed_surrogate* s, const __nv_bfloat16* x, float* y, int m, int* err,
                      cudaStream_t st, const unsigned* nrows) {
-  if (m <= 0 || m % tc::BM || !tc_supported(s)) return cudaErrorInvalidValue;
+  // the output rows are written in 16-byte pieces, or in 32-byte pieces when
+  // the rows start on 32-byte boundaries (the width is a multiple of 128)
+  if (m <= 0 || m % tc::BM || !tc_supported(s) || reinterpret_cast<uintptr_t>(y) % 16)
+    return cudaErrorInvalidValue;
+  const bool y32 = reinterpret_cast<uintptr_t>(y) % 32 == 0;
   tc::Layers P{};
   P.L = s->L;
   P.k0 = s->pin[0];
@@ -749,8 +768,8 @@ cudaError_t infer_tc(sed_surrogate* s, const __nv_bfloat16* x, float* y, int m, 
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int ntiles = m / tc::BM;
   const int grid = std::max(1, std::min(ntiles, sms));
-  tc::k_mlp_tc<<<grid, tc::NTHREADS, smem, st>>>(tx, P, y, s->pout[s->L - 1], ntiles, nrows,
-                                                  err);
+  tc::k_mlp_tc<<<grid, tc::NTHREADS, smem, st>>>(tx, P, y, s->pout[s->L - 1], y32, ntiles,
+                                                  nrows, err);
   return cudaGetLastError();
 }
 

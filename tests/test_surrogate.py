@@ -215,6 +215,48 @@ def test_tensor_core_inference_matches_fp64_reference():
 
 
 @pytest.mark.gpu
+def test_tensor_core_inference_output_alignment():
+    """The fused kernel writes 32-byte row pieces when the output rows start
+    on 32-byte boundaries and 16-byte pieces when they start on 16-byte ones:
+    the same values either way.  An output or input that is not 16-byte
+    aligned is refused before any launch."""
+    import torch
+    lib, h = _sur(**SHAPE, batch=256, seed=5)
+    try:
+        m = 256
+        rng = np.random.default_rng(11)
+        n = lib.sed_sur_num_params(h)
+        params = (rng.normal(0, 1, n) * 0.05).astype(np.float32)
+        assert lib.sed_sur_set_weights(h, _fp(params)) == 0
+        assert lib.sed_sur_set_tensor_cores(h, 1) == 1
+        xp = np.zeros((m, 384), dtype=np.float32)
+        xp[:, :SHAPE["nin"]] = rng.normal(0, 1, (m, SHAPE["nin"]))
+        xd = torch.tensor(xp, device="cuda").to(torch.bfloat16).contiguous()
+        # one buffer, the rows placed at byte offsets 0 (32-byte pieces),
+        # 16 (16-byte pieces) and 4 (refused)
+        buf = torch.zeros(m * 384 + 8, dtype=torch.float32, device="cuda")
+        base = buf.data_ptr()
+        assert base % 32 == 0
+        out = {}
+        for off in (0, 4):
+            buf.zero_()
+            torch.cuda.synchronize()
+            rc = lib.sed_sur_forward_device(h, ctypes.c_void_p(xd.data_ptr()),
+                                            ctypes.c_void_p(base + 4 * off), m)
+            assert rc == 0, lib.sed_sur_last_error(h)
+            torch.cuda.synchronize()
+            out[off] = buf[off:off + m * 384].reshape(m, 384).cpu().numpy().copy()
+        assert np.array_equal(out[0], out[4])
+        assert np.abs(out[0][:, :SHAPE["nout"]]).max() > 0
+        assert lib.sed_sur_forward_device(h, ctypes.c_void_p(xd.data_ptr()),
+                                          ctypes.c_void_p(base + 4), m) == -1
+        assert lib.sed_sur_forward_device(h, ctypes.c_void_p(xd.data_ptr() + 2),
+                                          ctypes.c_void_p(base), m) == -1
+    finally:
+        lib.sed_sur_destroy(h)
+
+
+@pytest.mark.gpu
 def test_tcgen05_training_products_match_mma_sync_at_full_batch():
     """At the training batch (8192 rows) the weight gradients' K is split
     over the SMs and added in a fixed order: the gradients of the two
