@@ -40,7 +40,6 @@ constexpr int NST = 3;                   // weight ring stages
 constexpr int HID = 256;                 // hidden width (TMEM columns used)
 constexpr int TMEM_COLS = 512;
 constexpr int EPI_WARPS = 16;            // warps 0-15 run the epilogue
-constexpr int EPI_THREADS = 32 * EPI_WARPS;
 constexpr int ECOLS = BK / (EPI_WARPS / 4);  // columns of a 64-column chunk per warp
 constexpr int PRODUCER = EPI_WARPS, MMA = EPI_WARPS + 1;  // warps
 constexpr int NTHREADS = 32 * (EPI_WARPS + 2);
@@ -271,8 +270,9 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
     mbar_init(b_xempty, 1);
     mbar_init(b_acc, 1);
     mbar_init(b_acc + 8, 1);
-    mbar_init(b_last, EPI_THREADS);
-    for (int i = 0; i < HID / BK; i++) mbar_init(b_actc + 8 * i, EPI_THREADS);
+    // the epilogue arrives once per warp
+    mbar_init(b_last, EPI_WARPS);
+    for (int i = 0; i < HID / BK; i++) mbar_init(b_actc + 8 * i, EPI_WARPS);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -408,6 +408,9 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
         const bool is_last = l == last;
         for (int n0 = 0; n0 < P.nout[l] && ok; n0 += HID) {
           ok = mbar_wait(b_acc + 8 * (a & 1), (a >> 1) & 1, &s_abort, err, 6);
+          // one outcome per warp, so the warp stays converged for its
+          // per-warp arrivals below
+          ok = __all_sync(0xffffffffu, ok);
           a++;
           if (!ok) break;
           fence_after();
@@ -469,16 +472,20 @@ k_mlp_tc(const __grid_constant__ CUtensorMap tx, const __grid_constant__ Layers 
                 w.w = pack_bf16(g3.x, g3.y);
                 *reinterpret_cast<uint4*>(rbase + ((((ECOLS / 8) * h + p) ^ (row & 7)) << 4)) = w;
               }
+              // every lane's stores made visible to the tensor cores'
+              // (async) reads, then one arrival for the warp
               fence_before();
               asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-              mbar_arrive(b_actc + 8 * kc);
+              __syncwarp();
+              if (lane == 0) mbar_arrive(b_actc + 8 * kc);
             }
             if (kc + 1 < nchunk) tmem_wait16(nxt);
           }
           if (is_last && n0 == 0) {
             // region 0 read: the next tile's first layer may start
             fence_before();
-            mbar_arrive(b_last);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(b_last);
           }
         }
       }
