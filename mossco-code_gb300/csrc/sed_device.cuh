@@ -330,6 +330,8 @@ __device__ __forceinline__ void bio3_conductances(const Params<real>& p,
 // on lane 0 (a = 0 there), then dC = (F - F_below) / (phi dz).  Branch- and
 // select-free: lanes past the column hold zero state and conductances; the
 // no-flux bottom drops F_below at K-1 by the zero conductance below it.
+// PRE: alpha b is read from the column's premultiplied surface row; else it
+// is formed from alpha and the boundary value (alpha varies per rhs).
 template <int LPL, bool BC4, bool PART, bool PRE>
 __device__ __forceinline__ void transport_one(const Lane<float, LPL, BC4>& lc, int n,
                                               const float (&a)[LPL], float alpha, float beta,
