@@ -1547,7 +1547,8 @@ def main():
     ap.add_argument("--path", default="sediment",
                     choices=["sediment", "pelagic", "coupling", "mlp"],
                     help="pelagic: the fabm_pelagic driver path instead; coupling: the "
-                         "pelagic -> soil connector")
+                         "pelagic -> soil connector; mlp: the surrogate network's "
+                         "inference on the tensor cores")
     ap.add_argument("--cpl-cpu-seconds", type=float, default=8.0,
                     help="coupling CPU baseline: about this many seconds of oracle calls")
     ap.add_argument("--pel-cpu-columns", type=int, default=0,
