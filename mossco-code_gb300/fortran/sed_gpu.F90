@@ -237,6 +237,129 @@ module sed_gpu
       integer(c_int), value :: method
       type(sed_stats_t), intent(out) :: st
     end function
+    !> Column-increment surrogate (no counterpart in the reference): an MLP
+    !! whose trained state a Fortran component loads from arrays (state of
+    !! sed_sur_state_size floats, norm of 11 + 2 nin + 2 nout floats, both as
+    !! the Python side's Surrogate.checkpoint() gives them) and then steps
+    !! with sed_step_surrogate or sed_ode_solver_surrogate.  Arrays are
+    !! c_loc of real(c_float) / real(c_double) arrays; s is the surrogate's
+    !! handle (type(c_ptr)).
+    integer(c_int) function sed_sur_create(nin, nout, hidden, nhidden, max_batch, seed, &
+        device, s) bind(C, name='sed_sur_create')
+      import :: c_int, c_ptr, c_long_long
+      integer(c_int), value :: nin, nout, hidden, nhidden, max_batch
+      integer(c_long_long), value :: seed
+      integer(c_int), value :: device
+      type(c_ptr), intent(out) :: s
+    end function
+    integer(c_int) function sed_sur_num_params(s) bind(C, name='sed_sur_num_params')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: s
+    end function
+    integer(c_int) function sed_sur_set_weights(s, params) bind(C, name='sed_sur_set_weights')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: s, params
+    end function
+    integer(c_int) function sed_sur_get_weights(s, params) bind(C, name='sed_sur_get_weights')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: s, params
+    end function
+    integer(c_int) function sed_sur_state_size(s) bind(C, name='sed_sur_state_size')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: s
+    end function
+    integer(c_int) function sed_sur_get_state(s, state, step) bind(C, name='sed_sur_get_state')
+      import :: c_int, c_ptr, c_long_long
+      type(c_ptr), value :: s, state
+      integer(c_long_long), intent(out) :: step
+    end function
+    integer(c_int) function sed_sur_set_state(s, state, step) bind(C, name='sed_sur_set_state')
+      import :: c_int, c_ptr, c_long_long
+      type(c_ptr), value :: s, state
+      integer(c_long_long), value :: step
+    end function
+    integer(c_int) function sed_sur_set_norm(s, norm, n) bind(C, name='sed_sur_set_norm')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: s, norm
+      integer(c_int), value :: n
+    end function
+    !> host rows x(nin, m) -> y(nout, m) (the C rows [m][nin], [m][nout])
+    integer(c_int) function sed_sur_forward(s, x, y, m) bind(C, name='sed_sur_forward')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: s, x, y
+      integer(c_int), value :: m
+    end function
+    !> device rows (device addresses as c_ptr), m a multiple of 128
+    integer(c_int) function sed_sur_forward_device(s, x_dev, y_dev, m) &
+        bind(C, name='sed_sur_forward_device')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: s, x_dev, y_dev
+      integer(c_int), value :: m
+    end function
+    !> one Adam step on a device batch; loss: c_loc of a real(c_float), or
+    !! c_null_ptr
+    integer(c_int) function sed_sur_train_step(s, x_dev, y_dev, m, lr, loss) &
+        bind(C, name='sed_sur_train_step')
+      import :: c_int, c_ptr, c_float
+      type(c_ptr), value :: s, x_dev, y_dev
+      integer(c_int), value :: m
+      real(c_float), value :: lr
+      type(c_ptr), value :: loss
+    end function
+    integer(c_int) function sed_sur_grads(s, x, y, m, grads, loss) bind(C, name='sed_sur_grads')
+      import :: c_int, c_ptr, c_float
+      type(c_ptr), value :: s, x, y
+      integer(c_int), value :: m
+      type(c_ptr), value :: grads
+      real(c_float), intent(out) :: loss
+    end function
+    integer(c_int) function sed_sur_set_tensor_cores(s, on) bind(C, name='sed_sur_set_tensor_cores')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: s
+      integer(c_int), value :: on
+    end function
+    integer(c_int) function sed_sur_set_stream(s, stream) bind(C, name='sed_sur_set_stream')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: s, stream
+    end function
+    type(c_ptr) function sed_sur_last_error(s) bind(C, name='sed_sur_last_error')
+      import :: c_ptr
+      type(c_ptr), value :: s
+    end function
+    !> nsteps gated surrogate coupling steps of the handle's device state
+    integer(c_int) function sed_step_surrogate(h, s, dt, nsteps, tol, res_atol, st) &
+        bind(C, name='sed_step_surrogate')
+      import :: c_int, c_ptr, c_double, sed_stats_t
+      type(c_ptr), value :: h, s
+      real(c_double), value :: dt
+      integer(c_int), value :: nsteps
+      real(c_double), value :: tol, res_atol
+      type(sed_stats_t), intent(out) :: st
+    end function
+    !> the drop-in call with the surrogate: sed_ode_solver's host arrays
+    integer(c_int) function sed_ode_solver_surrogate(h, s, conc, bdys, fluxes, dt, tol, &
+        res_atol, st) bind(C, name='sed_ode_solver_surrogate')
+      import :: c_int, c_ptr, c_double, sed_stats_t
+      type(c_ptr), value :: h, s, conc, bdys, fluxes
+      real(c_double), value :: dt, tol, res_atol
+      type(sed_stats_t), intent(out) :: st
+    end function
+    !> training rows of one plain step into device arrays (c_ptr)
+    integer(c_int) function sed_sur_collect(h, c0, dt, x_dev, y_dev, pitch_x, pitch_y, &
+        capacity, count, st) bind(C, name='sed_sur_collect')
+      import :: c_int, c_ptr, c_double, c_long_long, sed_stats_t
+      type(c_ptr), value :: h, c0
+      real(c_double), value :: dt
+      type(c_ptr), value :: x_dev, y_dev
+      integer(c_int), value :: pitch_x, pitch_y
+      integer(c_long_long), value :: capacity
+      integer(c_long_long), intent(inout) :: count
+      type(sed_stats_t), intent(out) :: st
+    end function
+    subroutine sed_sur_destroy(s) bind(C, name='sed_sur_destroy')
+      import :: c_ptr
+      type(c_ptr), value :: s
+    end subroutine
     !> C strings (const char*), read with sed_c_string
     type(c_ptr) function sed_error_string(code) bind(C, name='sed_error_string')
       import :: c_ptr, c_int
@@ -269,6 +392,11 @@ module sed_gpu
             sed_host_register, sed_host_unregister, sed_host_alloc, sed_host_free, &
             sed_get_attempt_histogram, &
             sed_ode_solver_noalloc, &
+            sed_sur_create, sed_sur_num_params, sed_sur_set_weights, sed_sur_get_weights, &
+            sed_sur_state_size, sed_sur_get_state, sed_sur_set_state, sed_sur_set_norm, &
+            sed_sur_forward, sed_sur_forward_device, sed_sur_train_step, sed_sur_grads, &
+            sed_sur_set_tensor_cores, sed_sur_set_stream, sed_sur_last_error, &
+            sed_step_surrogate, sed_ode_solver_surrogate, sed_sur_collect, sed_sur_destroy, &
             sed_error_string, sed_last_error, sed_tracer_name, sed_tracer_is_particulate, &
             sed_c_string
 

@@ -74,6 +74,50 @@ class Normalizer:
                             for i in range(5)))
 
 
+# Flat checkpoint for hosts without numpy (a Fortran component reads it with
+# stream access): nine little-endian int64 -- RAW_MAGIC, K, nin, nout,
+# hidden, nhidden, the state's length (sed_sur_state_size), the
+# normalisation's length (11 + 2 nin + 2 nout) and Adam's step count --
+# then the FP32 state (sed_sur_get_state's layout) and the FP32
+# normalisation (sed_sur_set_norm's layout).
+RAW_MAGIC = 0x5345445355524731  # "SEDSURG1"
+RAW_HEADER = 9
+
+
+def write_raw(path: str, ck: dict) -> None:
+    """Write a checkpoint (Surrogate.checkpoint()) in the flat format."""
+    K = int(ck["K"])
+    nin, nout = NTR * K + NFORCE, NTR * K
+    state = np.ascontiguousarray(ck["state"], dtype="<f4")
+    norm = np.ascontiguousarray(ck["norm"], dtype="<f4")
+    if norm.size != NTR + 2 * nin + 2 * nout:
+        raise ValueError(f"normalisation of {norm.size} floats for K = {K}")
+    hdr = np.array([RAW_MAGIC, K, nin, nout, HIDDEN, NHIDDEN, state.size, norm.size,
+                    int(ck["step"])], dtype="<i8")
+    with open(path, "wb") as f:
+        f.write(hdr.tobytes())
+        f.write(state.tobytes())
+        f.write(norm.tobytes())
+
+
+def read_raw(path: str) -> dict:
+    """Read a flat checkpoint back into Surrogate.restore()'s form."""
+    with open(path, "rb") as f:
+        hdr = np.frombuffer(f.read(8 * RAW_HEADER), dtype="<i8")
+        if hdr.size != RAW_HEADER or hdr[0] != RAW_MAGIC:
+            raise ValueError(f"{path}: not a flat surrogate checkpoint")
+        K, nin, nout, hidden, nhidden, nstate, nnorm, step = (int(v) for v in hdr[1:])
+        if (nin, nout) != (NTR * K + NFORCE, NTR * K) or (hidden, nhidden) != (HIDDEN, NHIDDEN) \
+                or nnorm != NTR + 2 * nin + 2 * nout:
+            raise ValueError(f"{path}: header {hdr.tolist()} does not describe this network")
+        state = np.frombuffer(f.read(4 * nstate), dtype="<f4")
+        norm = np.frombuffer(f.read(4 * nnorm), dtype="<f4")
+        if state.size != nstate or norm.size != nnorm or f.read(1):
+            raise ValueError(f"{path}: length does not match its header")
+    return {"state": state.astype(np.float32), "step": step,
+            "norm": norm.astype(np.float32), "K": K}
+
+
 def log_state(conc: np.ndarray, c0: np.ndarray) -> np.ndarray:
     """[ntr][K][cols] -> [cols][ntr*K] of log(max(C, 0) + c0)."""
     ntr, K, n = conc.shape
@@ -269,6 +313,18 @@ class Surrogate:
         s = Surrogate(int(d["K"]), batch=batch)
         s.restore({"state": d["state"], "step": int(d["step"]), "norm": d["norm"],
                    "K": int(d["K"])})
+        return s
+
+    def save_raw(self, path: str):
+        """The checkpoint in the flat format of write_raw (for a Fortran
+        host: sed_sur_create, sed_sur_set_state, sed_sur_set_norm)."""
+        write_raw(path, self.checkpoint())
+
+    @staticmethod
+    def load_raw(path: str, batch: int = 8192) -> "Surrogate":
+        ck = read_raw(path)
+        s = Surrogate(ck["K"], batch=batch)
+        s.restore(ck)
         return s
 
     def train(self, X, Y, steps: int, lr: float = 1e-3, lr_final: float = 2e-5,

@@ -165,18 +165,16 @@ def fortran_interfaces():
     return out
 
 
-# the column-increment surrogate is a GB300 extension without a Fortran
-# caller in the reference; its C and Python bindings serve it
-NO_FORTRAN = "sed_sur_"
 LIBC = ("strlen",)
 
 
 def test_fortran_interfaces_match_the_prototypes():
+    """Every function of the three headers, the surrogate's included, has a
+    bind(C) interface with the prototype's argument count."""
     c = c_prototypes()
     f = {k: v for k, v in fortran_interfaces().items() if k not in LIBC}
     for name, n in f.items():
         assert name in c, name
         assert n == c[name], (name, n, c[name])
-    missing = sorted(k for k in c if k not in f and not k.startswith(NO_FORTRAN)
-                     and k not in ("sed_step_surrogate", "sed_ode_solver_surrogate"))
+    missing = sorted(k for k in c if k not in f)
     assert missing == [], missing

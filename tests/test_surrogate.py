@@ -39,6 +39,41 @@ def test_bf16_rounding_matches_definition():
     assert r[4] == 3.140625
 
 
+def test_flat_checkpoint_round_trip(tmp_path):
+    """The flat checkpoint a Fortran host reads with stream access: nine
+    little-endian int64 (magic, K, nin, nout, hidden, nhidden, state and
+    normalisation lengths, Adam step), the FP32 state, the FP32
+    normalisation; read back unchanged, and refused when cut short or
+    described for another network."""
+    from sedgpu import surrogate as S
+    K = 30
+    nin, nout = 11 * K + 13, 11 * K
+    rng = np.random.default_rng(4)
+    ck = {"state": rng.normal(0, 1, 1000).astype(np.float32), "step": 50000,
+          "norm": rng.normal(0, 1, 11 + 2 * nin + 2 * nout).astype(np.float32), "K": K}
+    path = str(tmp_path / "sur.raw")
+    S.write_raw(path, ck)
+    raw = open(path, "rb").read()
+    hdr = np.frombuffer(raw[:72], dtype="<i8")
+    assert hdr.tolist() == [S.RAW_MAGIC, K, nin, nout, 256, 4, 1000, ck["norm"].size, 50000]
+    assert len(raw) == 72 + 4 * (1000 + ck["norm"].size)
+    assert np.array_equal(np.frombuffer(raw[72:72 + 4000], dtype="<f4"), ck["state"])
+    back = S.read_raw(path)
+    assert back["K"] == K and back["step"] == 50000
+    assert np.array_equal(back["state"], ck["state"])
+    assert np.array_equal(back["norm"], ck["norm"])
+    open(path, "wb").write(raw[:-4])
+    with pytest.raises(ValueError):
+        S.read_raw(path)
+    bad = bytearray(raw)
+    bad[8:16] = np.array([K + 1], dtype="<i8").tobytes()
+    open(path, "wb").write(bytes(bad))
+    with pytest.raises(ValueError):
+        S.read_raw(path)
+    with pytest.raises(ValueError):
+        S.write_raw(path, dict(ck, K=K + 1))
+
+
 def _sur(nin, nout, hidden, nhidden, batch, seed=3):
     from sedgpu import capi
     lib = capi.load()
